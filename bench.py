@@ -1,0 +1,365 @@
+"""Benchmark of the GB300 expression path (one JSON line on rank 0).
+
+Default workload: fused_project — the 200M-row, 12-op fused projection with 5
+nullable inputs and 3 outputs (f1, f2 float64; i1 int64), evaluated by
+ral_perform_operation_async on HBM-resident columns.  Other workloads:
+  --workload plain_vm          1M-row filter + project (fused)
+  --workload filter_gather     500M-row filter + compaction + gather, --selectivity 0.01/0.5/0.99
+
+value     rows/s over the timed steps (inputs resident in HBM; every input > L2, so no flush)
+e2e       same metric through the C ABI with host buffers: pinned H2D of the inputs and D2H of
+          the outputs inside the timed region
+roofline  algorithmic bytes / kernel time of the dominant kernel vs MEASURED_PEAKS.json hbm_gbs
+cpu_baseline  the CPU oracle (a row-by-row port of the reference interpreter) on all host cores,
+          timed on a bounded sample of the same workload
+
+--impl reference times the reference's CPU implementation of the path: the reference's
+interpreter only exists as GPU code built against cudf, which is not available, so the oracle
+port stands in (kind "port").  Multi-GPU: replicas (each rank runs its own copy of the workload).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "blazingdb-ral_gb300"))
+sys.path.insert(0, ROOT)
+
+METRIC = "filter+project rows/s & HBM GB/s vs 8 TB/s; batched/served rows/s, p99 vs plain"
+
+
+def load_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return float(d.get("hbm_gbs", 6800.0)), "measured"
+    return 6800.0, "fallback"
+
+
+def load_traffic(key):
+    p = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return d.get(key)
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons during the timed region."""
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 8:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                smax.append(float(parts[1]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[4:8]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dist_setup(args):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        backend = "nccl" if args.impl != "reference" else "gloo"
+        dist.init_process_group(backend=backend)
+    return world, rank, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(world, v):
+    if world == 1:
+        return v
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([v], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+# ---- CPU oracle timing --------------------------------------------------------------------------
+
+def cpu_fused_project(rows: int, threads: int):
+    import numpy as np
+    import oracle as O
+    from oracle import frontend as fe
+    from ralgpu import workloads as W
+    spec = W.fused_project_program()
+    inputs = W.fused_project_host(rows, seed=99)
+    ins = [O.make_column(v, t, m) for t, v, m in inputs]
+    outs = [O.alloc_column(t, rows) for t in spec.output_dtypes]
+    ls = [fe.Scalar(*s) for s in spec.lscalars]
+    rs = [fe.Scalar(*s) for s in spec.rscalars]
+    t0 = time.perf_counter()
+    O.perform_operation(outs, ins, spec.left, spec.right, spec.outputs, spec.final, spec.ops, spec.uops, ls, rs,
+                        nthreads=threads)
+    return time.perf_counter() - t0
+
+
+def cpu_plain_vm(rows: int, threads: int):
+    import oracle as O
+    from ralgpu import workloads as W
+    spec = W.plain_vm_host(rows, seed=99)
+    frame = [O.make_column(v, t, m) for t, v, m in spec]
+    t0 = time.perf_counter()
+    f = O.process_filter(frame, W.PLAIN_VM_FILTER, nthreads=threads)
+    O.execute_project_plan(f, W.PLAIN_VM_PROJECT, nthreads=threads)
+    return time.perf_counter() - t0
+
+
+def cpu_filter_gather(rows: int, threads: int, selectivity: float):
+    import oracle as O
+    from ralgpu import workloads as W
+    spec = W.filter_gather_host(rows, seed=99)
+    frame = [O.make_column(v, t, m) for t, v, m in spec]
+    t0 = time.perf_counter()
+    O.process_filter(frame, W.filter_gather_query(selectivity), nthreads=threads)
+    return time.perf_counter() - t0
+
+
+def cpu_time(workload, rows, threads, selectivity):
+    if workload == "fused_project":
+        return cpu_fused_project(rows, threads)
+    if workload == "plain_vm":
+        return cpu_plain_vm(rows, threads)
+    return cpu_filter_gather(rows, threads, selectivity)
+
+
+def cpu_baseline(workload, full_rows, selectivity, budget_s=12.0):
+    """rows/s of the oracle on all cores over a bounded sample sized for about budget_s of work."""
+    threads = os.cpu_count() or 1
+    probe = min(full_rows, 2_000_000)
+    dt = cpu_time(workload, probe, threads, selectivity)
+    rate = probe / max(dt, 1e-9)
+    rows = int(min(full_rows, max(probe, rate * budget_s / 3)))
+    times = [cpu_time(workload, rows, threads, selectivity) for _ in range(3)]
+    t = statistics.median(times)
+    return {"value": rows / t, "unit": "rows/s", "cores": threads, "kind": "port",
+            "sample": f"{rows} of {full_rows} rows, median of 3 runs, {threads} threads"}
+
+
+# ---- GPU workloads --------------------------------------------------------------------------------
+
+def fused_project_setup(n, device):
+    import torch
+    import ralgpu as R
+    from ralgpu import workloads as W
+    spec = W.fused_project_program()
+    cols = []
+    for t, data, valid, nulls in W.fused_project_device(n, device=device):
+        cols.append(R.Column(data, valid, t, size=n, null_count=nulls))
+    outs = [R.Column.empty(t, n, device=device) for t in spec.output_dtypes]
+    bytes_per_row_in = sum(R.dtypes.WIDTH[t] for t in spec.input_dtypes) + len(spec.input_dtypes) / 8
+    bytes_per_row_out = sum(R.dtypes.WIDTH[t] for t in spec.output_dtypes) + len(spec.output_dtypes) / 8
+    alg_bytes = n * (bytes_per_row_in + bytes_per_row_out)
+
+    def step(stream):
+        R.perform_operation_async(outs, cols, spec.left, spec.right, spec.outputs, spec.final, spec.ops, spec.uops,
+                                  spec.lscalars, spec.rscalars, stream=stream)
+
+    return dict(step=step, alg_bytes=alg_bytes, cols=cols, outs=outs, spec=spec,
+                config={"workload": "fused_project", "rows": n, "inputs": "a,b int64; x,y float64; k int32; 5% nulls",
+                        "program_ops": len(spec.ops), "outputs": "f1,f2 float64; i1 int64",
+                        "l2": "inputs (12.2 GB at 200M rows) exceed L2; no flush"})
+
+
+def fused_project_e2e(ctx, steps, device):
+    """C ABI with host buffers: pinned H2D of every input (data + mask), kernel, D2H of every output."""
+    import torch
+    import ralgpu as R
+    spec = ctx["spec"]
+    n = ctx["cols"][0].size
+    host_in = [(c.data.cpu().pin_memory(), c.valid.cpu().pin_memory()) for c in ctx["cols"]]
+    host_out = [(torch.empty_like(o.data, device="cpu").pin_memory(),
+                 torch.empty_like(o.valid, device="cpu").pin_memory()) for o in ctx["outs"]]
+    h2d = sum(a.numel() * a.element_size() + b.numel() for a, b in host_in)
+    d2h = sum(a.numel() * a.element_size() + b.numel() for a, b in host_out)
+    stream = torch.cuda.current_stream()
+
+    def one():
+        for (hd, hv), c in zip(host_in, ctx["cols"]):
+            c.data.copy_(hd, non_blocking=True)
+            c.valid.copy_(hv, non_blocking=True)
+        R.perform_operation_async(ctx["outs"], ctx["cols"], spec.left, spec.right, spec.outputs, spec.final,
+                                  spec.ops, spec.uops, spec.lscalars, spec.rscalars, stream=stream)
+        for (hd, hv), o in zip(host_out, ctx["outs"]):
+            hd.copy_(o.data, non_blocking=True)
+            hv.copy_(o.valid, non_blocking=True)
+
+    one()
+    torch.cuda.synchronize()
+    start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    start.record()
+    for _ in range(steps):
+        one()
+    end.record()
+    torch.cuda.synchronize()
+    ms = start.elapsed_time(end) / steps
+    return {"value": n / (ms / 1e3), "unit": "rows/s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
+            "ms_per_step": ms}
+
+
+def run_ours(args):
+    import torch
+    import ralgpu as R
+    world, rank, local = dist_setup(args)
+    torch.cuda.set_device(local)
+    device = f"cuda:{local}"
+    n = args.rows or {"fused_project": 200_000_000, "plain_vm": 1_000_000, "filter_gather": 500_000_000}[args.workload]
+    if args.workload != "fused_project":
+        raise SystemExit("workload not built into bench.py yet: " + args.workload)
+    ctx = fused_project_setup(n, device)
+    stream = torch.cuda.current_stream()
+    for _ in range(args.warmup):
+        ctx["step"](stream)
+    torch.cuda.synchronize()
+    barrier(world)
+    sampler = ClockSampler(local)
+    sampler.start()
+    launches0 = R.kernel_launches()
+    events = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    torch.cuda.synchronize()
+    t_start = torch.cuda.Event(enable_timing=True)
+    t_end = torch.cuda.Event(enable_timing=True)
+    t_start.record()
+    for s, e in events:
+        s.record()
+        ctx["step"](stream)
+        e.record()
+    t_end.record()
+    torch.cuda.synchronize()
+    launches = R.kernel_launches() - launches0
+    clocks = sampler.stop()
+    barrier(world)
+    total_ms = t_start.elapsed_time(t_end)
+    total_ms = max_over_ranks(world, total_ms)
+    kernel_ms = statistics.mean(s.elapsed_time(e) for s, e in events)
+    ms_per_step = total_ms / args.steps
+    value = world * n / (ms_per_step / 1e3)
+    peak, peak_kind = load_peaks()
+    achieved = ctx["alg_bytes"] / (kernel_ms / 1e3) / 1e9
+    traffic = load_traffic(args.workload)
+    out = {
+        "metric": METRIC, "value": value, "unit": "rows/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded, generated on the GPU)",
+        "config": dict(ctx["config"], parallelism=f"replicas x{world}"),
+        "hbm_gbs": achieved,
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "peak_kind": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else peak_kind,
+                     "frac_of_8tbs": achieved / 8000.0, "traffic": traffic,
+                     "algorithmic_bytes_per_launch": ctx["alg_bytes"], "kernel_ms": kernel_ms},
+        "gpu_launches": int(launches),
+        "clocks": clocks,
+    }
+    if rank == 0:
+        if not args.skip_e2e:
+            out["e2e"] = fused_project_e2e(ctx, max(2, min(args.steps, 3)), device)
+        if not args.skip_cpu:
+            out["cpu_baseline"] = cpu_baseline(args.workload, n, args.selectivity)
+        print(json.dumps(out), flush=True)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+def run_reference(args):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    n = args.rows or {"fused_project": 200_000_000, "plain_vm": 1_000_000, "filter_gather": 500_000_000}[args.workload]
+    threads = os.cpu_count() or 1
+    # bounded sample per step, sized from a probe so the whole run stays within a few minutes
+    probe = min(n, 1_000_000)
+    dt = cpu_time(args.workload, probe, threads, args.selectivity)
+    rows = int(min(n, max(probe, (probe / max(dt, 1e-9)) * 4.0)))
+    for _ in range(args.warmup):
+        cpu_time(args.workload, min(rows, probe), threads, args.selectivity)
+    times = [cpu_time(args.workload, rows, threads, args.selectivity) for _ in range(args.steps)]
+    t = sum(times) / len(times)
+    v = rows / t
+    out = {"metric": METRIC, "value": v, "unit": "rows/s", "n_gpus": world, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": t * 1e3, "higher_is_better": True, "scaling": "weak",
+           "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)", "impl": "reference",
+           "config": {"workload": args.workload, "rows": n},
+           "cpu_baseline": {"value": v, "unit": "rows/s", "cores": threads, "kind": "port",
+                            "sample": f"{rows} of {n} rows per step"},
+           "e2e": {"value": v, "unit": "rows/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(out), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="fused_project", choices=["fused_project", "plain_vm", "filter_gather"])
+    ap.add_argument("--selectivity", type=float, default=0.5)
+    ap.add_argument("--rows", type=int, default=0)
+    ap.add_argument("--skip-e2e", action="store_true")
+    ap.add_argument("--skip-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3 and args.impl == "ours":
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,345 @@
+// capi.cpp — the extern "C" entry points declared in include/ral/ral_c.h.
+#include <cuda_runtime.h>
+
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "codegen.h"
+#include "engine.h"
+#include "filter.h"
+#include "frontend.h"
+#include "jit.h"
+#include "kernels.h"
+#include "ral/ral_c.h"
+
+using namespace ral;
+
+namespace {
+
+template <typename F>
+int guarded(F&& f) {
+    try {
+        return f();
+    } catch (const ParseError& e) {
+        return set_error(kParseError, e.what());
+    } catch (const std::exception& e) {
+        return set_error(kInvalidArgument, e.what());
+    }
+}
+
+void copy_out(const std::string& s, char* buf, int64_t cap) {
+    if (!buf || cap <= 0) return;
+    size_t n = std::min<size_t>(s.size(), (size_t)cap - 1);
+    std::memcpy(buf, s.data(), n);
+    buf[n] = '\0';
+}
+
+int count_nulls(gdf_column* col, cudaStream_t st) {
+    if (col->size == 0 || col->valid == nullptr) {
+        col->null_count = 0;
+        return kSuccess;
+    }
+    unsigned long long* d = nullptr;
+    if (int e = check_cuda(cudaMallocAsync((void**)&d, sizeof(unsigned long long), st), "cudaMallocAsync")) return e;
+    cudaMemsetAsync(d, 0, sizeof(unsigned long long), st);
+    if (int e = check_cuda(launch_count_valid((const uint32_t*)col->valid, col->size, d, st), "count_valid")) return e;
+    unsigned long long h = 0;
+    cudaMemcpyAsync(&h, d, sizeof h, cudaMemcpyDeviceToHost, st);
+    cudaFreeAsync(d, st);
+    if (int e = check_cuda(cudaStreamSynchronize(st), "cudaStreamSynchronize")) return e;
+    col->null_count = (gdf_size_type)(col->size - (int64_t)h);
+    return kSuccess;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* ral_last_error(void) { return last_error(); }
+const char* ral_version(void) { return "ralgpu 0.1 (sm_103a)"; }
+
+int ral_perform_operation(gdf_column* const* output_columns, int32_t num_outputs, gdf_column* const* input_columns,
+                          int32_t num_inputs, const column_index_type* left_inputs,
+                          const column_index_type* right_inputs, const column_index_type* outputs,
+                          int32_t num_operations, const column_index_type* final_output_positions,
+                          const int32_t* operators, const int32_t* unary_operators, const gdf_scalar* left_scalars,
+                          const gdf_scalar* right_scalars, const column_index_type* new_input_indices,
+                          int32_t num_new_input_indices) {
+    (void)new_input_indices;
+    (void)num_new_input_indices;
+    return guarded([&] {
+        ProgramArrays pa{left_inputs, right_inputs, outputs, num_operations, final_output_positions,
+                         operators, unary_operators, left_scalars, right_scalars};
+        EvalOptions opt;
+        opt.stream = cudaStreamPerThread;
+        opt.sync = true;
+        return perform_operation(output_columns, num_outputs, input_columns, num_inputs, pa, opt);
+    });
+}
+
+int ral_perform_operation_async(gdf_column* const* output_columns, int32_t num_outputs,
+                                gdf_column* const* input_columns, int32_t num_inputs,
+                                const column_index_type* left_inputs, const column_index_type* right_inputs,
+                                const column_index_type* outputs, int32_t num_operations,
+                                const column_index_type* final_output_positions, const int32_t* operators,
+                                const int32_t* unary_operators, const gdf_scalar* left_scalars,
+                                const gdf_scalar* right_scalars, void* stream, int64_t* null_counts) {
+    return guarded([&] {
+        ProgramArrays pa{left_inputs, right_inputs, outputs, num_operations, final_output_positions,
+                         operators, unary_operators, left_scalars, right_scalars};
+        EvalOptions opt;
+        opt.stream = (cudaStream_t)stream;
+        opt.sync = false;
+        opt.null_counts = null_counts;
+        return perform_operation(output_columns, num_outputs, input_columns, num_inputs, pa, opt);
+    });
+}
+
+int ral_evaluate_expression(gdf_column* const* frame, int32_t num_columns, const char* expression,
+                            gdf_column* output) {
+    return guarded([&] {
+        if (!frame || num_columns <= 0 || !expression || !output)
+            return set_error(kInvalidArgument, "evaluate_expression: null argument");
+        ExpressionPlan ep = plan_expression(expression, num_columns);
+        cudaStream_t st = cudaStreamPerThread;
+        if (ep.clone) {
+            const gdf_column* src = frame[ep.clone_column];
+            if (src->dtype != output->dtype)
+                return set_error(kInvalidArgument, "evaluate_expression: \"$k\" output must have column k's dtype");
+            if (output->size < src->size) return set_error(kInvalidArgument, "evaluate_expression: output too small");
+            const size_t bytes = (size_t)src->size * gdf_dtype_size(src->dtype);
+            if (bytes) cudaMemcpyAsync(output->data, src->data, bytes, cudaMemcpyDeviceToDevice, st);
+            if (src->valid && output->valid) {
+                cudaMemcpyAsync(output->valid, src->valid, (src->size + 7) / 8, cudaMemcpyDeviceToDevice, st);
+            } else if (output->valid) {
+                cudaMemsetAsync(output->valid, 0xFF, (src->size + 7) / 8, st);
+            }
+            output->null_count = src->null_count;
+            return check_cuda(cudaStreamSynchronize(st), "evaluate_expression clone");
+        }
+        std::vector<gdf_column*> ins;
+        for (int c : ep.input_columns) ins.push_back(frame[c]);
+        gdf_column* outs[1] = {output};
+        ProgramArrays pa{ep.pv.left.data(), ep.pv.right.data(), ep.pv.outs.data(), (int32_t)ep.pv.left.size(),
+                         ep.pv.final_pos.data(), ep.pv.bops.data(), ep.pv.uops.data(), ep.pv.lscalars.data(),
+                         ep.pv.rscalars.data()};
+        EvalOptions opt;
+        opt.stream = st;
+        return perform_operation(outs, 1, ins.data(), (int)ins.size(), pa, opt);
+    });
+}
+
+int ral_add_expression_to_plan(const char* expression, column_index_type expression_position,
+                               column_index_type num_outputs, column_index_type num_inputs,
+                               const column_index_type* new_input_indices, int32_t num_frame_columns,
+                               column_index_type* left_inputs, column_index_type* right_inputs,
+                               column_index_type* outputs, int32_t* operators, int32_t* unary_operators,
+                               gdf_scalar* left_scalars, gdf_scalar* right_scalars, int32_t* num_operations,
+                               int32_t capacity) {
+    return guarded([&] {
+        if (!expression || !num_operations) return set_error(kInvalidArgument, "null argument");
+        auto e = parse_expression(expression);
+        std::vector<int> remap(new_input_indices, new_input_indices + num_frame_columns);
+        ProgramVectors pv;
+        emit_expression(*e, expression_position, num_outputs, num_inputs, remap, pv);
+        const int base = *num_operations;
+        if (base + (int)pv.left.size() > capacity) return set_error(kInvalidArgument, "capacity too small");
+        for (size_t k = 0; k < pv.left.size(); k++) {
+            left_inputs[base + k] = pv.left[k];
+            right_inputs[base + k] = pv.right[k];
+            outputs[base + k] = pv.outs[k];
+            operators[base + k] = pv.bops[k];
+            unary_operators[base + k] = pv.uops[k];
+            left_scalars[base + k] = pv.lscalars[k];
+            right_scalars[base + k] = pv.rscalars[k];
+        }
+        *num_operations = base + (int)pv.left.size();
+        return (int)kSuccess;
+    });
+}
+
+int ral_get_output_type_expression(const gdf_dtype* frame_dtypes, int32_t num_columns, const char* expression,
+                                   gdf_dtype* dtype_out) {
+    return guarded([&] {
+        auto e = parse_expression(expression);
+        std::vector<gdf_dtype> f(frame_dtypes, frame_dtypes + num_columns);
+        *dtype_out = expression_output_type(*e, f);
+        return (int)kSuccess;
+    });
+}
+
+int ral_project_output_types(const gdf_dtype* frame_dtypes, int32_t num_columns, const char* query_part,
+                             int32_t* num_projected, gdf_dtype* dtypes_out, int32_t* is_evaluated_out,
+                             int32_t capacity) {
+    return guarded([&] {
+        std::vector<gdf_dtype> f(frame_dtypes, frame_dtypes + num_columns);
+        ProjectPlan pp = plan_project(query_part, f);
+        *num_projected = (int32_t)pp.columns.size();
+        if ((int)pp.columns.size() > capacity) return set_error(kInvalidArgument, "capacity too small");
+        for (size_t i = 0; i < pp.columns.size(); i++) {
+            is_evaluated_out[i] = pp.columns[i].first ? 1 : 0;
+            dtypes_out[i] = pp.columns[i].first ? pp.eval_dtypes[pp.columns[i].second] : f[pp.columns[i].second];
+        }
+        return (int)kSuccess;
+    });
+}
+
+int ral_execute_project_plan(gdf_column* const* frame, int32_t num_columns, const char* query_part,
+                             gdf_column* const* out_columns, int32_t num_out_columns) {
+    return guarded([&] {
+        std::vector<gdf_dtype> f(num_columns);
+        for (int c = 0; c < num_columns; c++) f[c] = frame[c]->dtype;
+        ProjectPlan pp = plan_project(query_part, f);
+        if ((int)pp.columns.size() != num_out_columns)
+            return set_error(kInvalidArgument, "out_columns count differs from the projection's");
+        cudaStream_t st = cudaStreamPerThread;
+        const int64_t n = frame[0]->size;
+        std::vector<gdf_column*> evald;
+        for (size_t i = 0; i < pp.columns.size(); i++) {
+            if (!pp.columns[i].first) continue;
+            gdf_column* o = out_columns[i];
+            if (o->dtype != pp.eval_dtypes[pp.columns[i].second])
+                return set_error(kInvalidArgument, "out column " + std::to_string(i) + " has the wrong dtype");
+            evald.push_back(o);
+        }
+        std::vector<int64_t> nulls(evald.size(), 0);
+        if (!evald.empty()) {
+            std::vector<gdf_column*> ins;
+            for (int c : pp.input_columns) ins.push_back(frame[c]);
+            ProgramArrays pa{pp.pv.left.data(), pp.pv.right.data(), pp.pv.outs.data(), (int32_t)pp.pv.left.size(),
+                             pp.pv.final_pos.data(), pp.pv.bops.data(), pp.pv.uops.data(), pp.pv.lscalars.data(),
+                             pp.pv.rscalars.data()};
+            EvalOptions opt;
+            opt.stream = st;
+            opt.null_counts = nulls.data();
+            if (int e = perform_operation(evald.data(), (int)evald.size(), ins.data(), (int)ins.size(), pa, opt)) return e;
+        }
+        for (size_t i = 0, k = 0; i < pp.columns.size(); i++) {
+            gdf_column* o = out_columns[i];
+            if (pp.columns[i].first) {
+                o->size = (gdf_size_type)n;
+                o->null_count = (gdf_size_type)nulls[k++];
+            } else {
+                *o = *frame[pp.columns[i].second];
+                if (int e = count_nulls(o, st)) return e;
+                frame[pp.columns[i].second]->null_count = o->null_count;
+            }
+        }
+        return (int)kSuccess;
+    });
+}
+
+int ral_materialize_column(const gdf_column* input, gdf_column* output, const gdf_column* row_indices) {
+    return guarded([&] {
+        if (!input || !output || !row_indices) return set_error(kInvalidArgument, "null argument");
+        const int w = gdf_dtype_size(input->dtype);
+        const int iw = gdf_dtype_size(row_indices->dtype);
+        if (w == 0 || iw == 0 || dtype_is_float(row_indices->dtype))
+            return set_error(kInvalidArgument, "materialize_column: unsupported dtype");
+        if (gdf_dtype_size(output->dtype) != w) return set_error(kInvalidArgument, "materialize_column: width mismatch");
+        const int64_t n = row_indices->size;
+        cudaStream_t st = cudaStreamPerThread;
+        unsigned long long* d = nullptr;
+        if (output->valid) {
+            if (int e = check_cuda(cudaMallocAsync((void**)&d, sizeof(unsigned long long), st), "cudaMallocAsync")) return e;
+            cudaMemsetAsync(d, 0, sizeof(unsigned long long), st);
+        }
+        if (int e = check_cuda(launch_gather(w, input->data, (const uint32_t*)input->valid, row_indices->data, iw, n,
+                                             output->data, (uint32_t*)output->valid, d, st),
+                               "gather"))
+            return e;
+        unsigned long long h = 0;
+        if (d) {
+            cudaMemcpyAsync(&h, d, sizeof h, cudaMemcpyDeviceToHost, st);
+            cudaFreeAsync(d, st);
+        }
+        if (int e = check_cuda(cudaStreamSynchronize(st), "materialize_column")) return e;
+        output->size = (gdf_size_type)n;
+        output->null_count = output->valid ? (gdf_size_type)(n - (int64_t)h) : 0;
+        return (int)kSuccess;
+    });
+}
+
+int ral_process_filter(gdf_column* const* frame, int32_t num_columns, const char* query_part,
+                       gdf_column* const* out_columns, gdf_size_type* num_rows_out) {
+    return guarded([&] {
+        FilterOptions opt;
+        opt.stream = cudaStreamPerThread;
+        opt.sync = true;
+        return process_filter(frame, num_columns, query_part, out_columns, num_rows_out, opt);
+    });
+}
+
+int ral_process_filter_async(gdf_column* const* frame, int32_t num_columns, const char* query_part,
+                             gdf_column* const* out_columns, gdf_size_type* num_rows_out, void* stream) {
+    return guarded([&] {
+        FilterOptions opt;
+        opt.stream = (cudaStream_t)stream;
+        opt.sync = true;
+        return process_filter(frame, num_columns, query_part, out_columns, num_rows_out, opt);
+    });
+}
+
+int ral_filter_project(gdf_column* const* frame, int32_t num_columns, const char* filter_query_part,
+                       const char* project_query_part, gdf_column* const* out_columns, int32_t num_out_columns,
+                       gdf_size_type* num_rows_out) {
+    return guarded([&] {
+        FilterOptions opt;
+        opt.stream = cudaStreamPerThread;
+        opt.sync = true;
+        return filter_project(frame, num_columns, filter_query_part, project_query_part, out_columns,
+                              num_out_columns, num_rows_out, opt);
+    });
+}
+
+int ral_debug_program_source(const gdf_dtype* input_dtypes, const int32_t* input_nullable, int32_t num_inputs,
+                             const gdf_dtype* output_dtypes, const int32_t* output_nullable, int32_t num_outputs,
+                             const column_index_type* left_inputs, const column_index_type* right_inputs,
+                             const column_index_type* outputs, int32_t num_operations,
+                             const column_index_type* final_output_positions, const int32_t* operators,
+                             const int32_t* unary_operators, const gdf_scalar* left_scalars,
+                             const gdf_scalar* right_scalars, int32_t compile, char* source_out,
+                             int64_t source_capacity, char* log_out, int64_t log_capacity) {
+    return guarded([&] {
+        std::vector<ColumnDesc> ins(num_inputs);
+        for (int c = 0; c < num_inputs; c++) {
+            ins[c].dtype = input_dtypes[c];
+            ins[c].has_valid = input_nullable[c] != 0;
+            ins[c].nulls_possible = input_nullable[c] != 0;
+        }
+        std::vector<gdf_dtype> ot(output_dtypes, output_dtypes + num_outputs);
+        std::vector<bool> ov(num_outputs);
+        for (int o = 0; o < num_outputs; o++) ov[o] = output_nullable[o] != 0;
+        Program p;
+        std::string err;
+        if (!p.build(ins, ot, ov, left_inputs, right_inputs, outputs, num_operations, final_output_positions,
+                     operators, unary_operators, left_scalars, right_scalars, err))
+            return set_error(kUnsupported, err);
+        GeneratedKernel gk = generate_eval_kernel(p, default_shape(p));
+        copy_out(std::string(jit_prelude()) + "\n" + gk.source, source_out, source_capacity);
+        if (compile) {
+            size_t bytes = 0;
+            std::string log;
+            if (!jit_compile_only(gk, &bytes, &log, err)) {
+                copy_out(err, log_out, log_capacity);
+                return set_error(kJitError, err);
+            }
+            copy_out(log, log_out, log_capacity);
+        }
+        return (int)kSuccess;
+    });
+}
+
+int64_t ral_kernel_launches(void) { return (int64_t)launch_count(); }
+
+int ral_jit_stats(int64_t* compiles, int64_t* disk_hits, int64_t* memory_hits, double* compile_ms) {
+    JitStats s = jit_stats();
+    if (compiles) *compiles = s.compiles;
+    if (disk_hits) *disk_hits = s.disk_hits;
+    if (memory_hits) *memory_hits = s.memory_hits;
+    if (compile_ms) *compile_ms = s.compile_ms_total;
+    return 0;
+}
+
+}  // extern "C"

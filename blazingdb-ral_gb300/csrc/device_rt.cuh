@@ -1,0 +1,135 @@
+// device_rt.cuh — device-side building blocks of the generated expression kernels.
+//
+// This file is compiled twice: by NVRTC as the prelude of every generated
+// kernel (embedded into the library as a string at build time), and by nvcc
+// as part of the ahead-of-time kernels.  It includes no headers so that NVRTC
+// needs no include path.
+//
+// Arithmetic follows the reference interpreter's C++ semantics on {int64,
+// double} registers (src/Interpreter/interpreter_ops.cuh:574-838): explicit
+// _rn intrinsics keep every double operation separately rounded (never
+// contracted into an FMA), integer add/sub/mul wrap, double->int64 truncates
+// and saturates with NaN -> 0 (cvt.rzi.s64.f64).
+#ifndef RAL_DEVICE_RT_CUH_
+#define RAL_DEVICE_RT_CUH_
+
+typedef long long ral_i64;
+typedef unsigned long long ral_u64;
+typedef unsigned int ral_u32;
+
+#define RAL_FI __device__ __forceinline__
+
+// ---- conversions ---------------------------------------------------------------------------
+RAL_FI ral_i64 ral_d2i(double d) { return __double2ll_rz(d); }
+RAL_FI double ral_i2d(ral_i64 x) { return __ll2double_rn(x); }
+RAL_FI double ral_bits_d(ral_i64 b) { return __longlong_as_double(b); }
+RAL_FI ral_i64 ral_d_bits(double d) { return __double_as_longlong(d); }
+
+// ---- integer ops (two's complement wrap, as the GPU executes them) -------------------------
+RAL_FI ral_i64 ral_addi(ral_i64 a, ral_i64 b) { return (ral_i64)((ral_u64)a + (ral_u64)b); }
+RAL_FI ral_i64 ral_subi(ral_i64 a, ral_i64 b) { return (ral_i64)((ral_u64)a - (ral_u64)b); }
+RAL_FI ral_i64 ral_muli(ral_i64 a, ral_i64 b) { return (ral_i64)((ral_u64)a * (ral_u64)b); }
+RAL_FI ral_i64 ral_divi(ral_i64 a, ral_i64 b) { return a / b; }
+RAL_FI ral_i64 ral_modi(ral_i64 a, ral_i64 b) { return a % b; }
+// Integer POWER: the reference multiplies `base` into 1, `e` times (e <= 0 -> 1);
+// square-and-multiply gives the same value modulo 2^64.
+RAL_FI ral_i64 ral_powi(ral_i64 base, ral_i64 e) {
+    ral_u64 acc = 1, b = (ral_u64)base;
+    if (e <= 0) return 1;
+    ral_u64 ue = (ral_u64)e;
+    while (ue) {
+        if (ue & 1ull) acc *= b;
+        b *= b;
+        ue >>= 1;
+    }
+    return (ral_i64)acc;
+}
+
+// ---- calendar extraction (interpreter_ops.cuh:61-153) --------------------------------------
+// Days-from-civil inverse on 32-bit int / unsigned arithmetic as written there.
+// Every signed add/sub/mul that can overflow for out-of-range inputs is done in
+// unsigned arithmetic, i.e. it wraps the way the GPU's integer instructions do.
+struct RalCivil { ral_i64 y, m, d; };
+RAL_FI int ral_wadd(int a, int b) { return (int)((unsigned)a + (unsigned)b); }
+RAL_FI int ral_wmul(int a, int b) { return (int)((unsigned)a * (unsigned)b); }
+RAL_FI RalCivil ral_civil(int z) {
+    const int era = (z >= 0 ? z : ral_wadd(z, -146096)) / 146097;
+    const unsigned doe = (unsigned)ral_wadd(z, -ral_wmul(era, 146097));
+    const unsigned yoe = (doe - doe / 1460 + doe / 36524 - doe / 146096) / 365;
+    const int y = ral_wadd((int)yoe, ral_wmul(era, 400));
+    const unsigned doy = doe - (365 * yoe + yoe / 4 - yoe / 100);
+    const unsigned mp = (5 * doy + 2) / 153;
+    const unsigned m = mp + (mp < 10 ? 3u : (unsigned)-9);
+    RalCivil c;
+    c.y = (m <= 2) ? (ral_i64)y + 1 : (ral_i64)y;
+    c.m = (ral_i64)m;
+    c.d = (ral_i64)(doy - (153 * mp + 2) / 5 + 1);
+    return c;
+}
+#define RAL_MS_DAY 86400000ll
+#define RAL_MS_HOUR 3600000ll
+#define RAL_MS_MINUTE 60000ll
+#define RAL_MS_SECOND 1000ll
+RAL_FI int ral_z_days(ral_i64 d) { return (int)(unsigned)((ral_u64)d + 719468ull); }
+RAL_FI int ral_z_ms(ral_i64 t) {
+    const ral_i64 a = t >= 0 ? t : (ral_i64)((ral_u64)t - (ral_u64)(RAL_MS_DAY - 1));
+    return (int)(unsigned)((ral_u64)(a / RAL_MS_DAY) + 719468ull);
+}
+RAL_FI ral_i64 ral_year32(ral_i64 d) { return ral_civil(ral_z_days(d)).y; }
+RAL_FI ral_i64 ral_month32(ral_i64 d) { return ral_civil(ral_z_days(d)).m; }
+RAL_FI ral_i64 ral_day32(ral_i64 d) { return ral_civil(ral_z_days(d)).d; }
+RAL_FI ral_i64 ral_year64(ral_i64 t) { return ral_civil(ral_z_ms(t)).y; }
+RAL_FI ral_i64 ral_month64(ral_i64 t) { return ral_civil(ral_z_ms(t)).m; }
+RAL_FI ral_i64 ral_day64(ral_i64 t) { return ral_civil(ral_z_ms(t)).d; }
+RAL_FI ral_i64 ral_hour64(ral_i64 t) {
+    return t >= 0 ? ((t % RAL_MS_DAY) / RAL_MS_HOUR) : ((RAL_MS_DAY + (t % RAL_MS_DAY)) / RAL_MS_HOUR);
+}
+RAL_FI ral_i64 ral_minute64(ral_i64 t) {
+    return t >= 0 ? ((t % RAL_MS_HOUR) / RAL_MS_MINUTE) : ((RAL_MS_HOUR + (t % RAL_MS_HOUR)) / RAL_MS_MINUTE);
+}
+RAL_FI ral_i64 ral_second64(ral_i64 t) {
+    return t >= 0 ? ((t % RAL_MS_MINUTE) / RAL_MS_SECOND) : ((RAL_MS_MINUTE + (t % RAL_MS_MINUTE)) / RAL_MS_SECOND);
+}
+
+// ---- vector loads / stores of G consecutive elements ---------------------------------------
+template <int BYTES> struct RalVecT;
+template <> struct RalVecT<16> { typedef uint4 T; };
+template <> struct RalVecT<8> { typedef uint2 T; };
+template <> struct RalVecT<4> { typedef unsigned int T; };
+template <> struct RalVecT<2> { typedef unsigned short T; };
+template <> struct RalVecT<1> { typedef unsigned char T; };
+
+// Streaming load of G elements starting at p[row]; p + row must be aligned to G*sizeof(E).
+template <typename E, int G>
+RAL_FI void ral_ldg(const E* __restrict__ p, ral_i64 row, E (&v)[G]) {
+    typedef typename RalVecT<sizeof(E) * G>::T V;
+    union { V vec; E e[G]; } u;
+    u.vec = __ldcs(reinterpret_cast<const V*>(p + row));
+#pragma unroll
+    for (int g = 0; g < G; ++g) v[g] = u.e[g];
+}
+template <typename E, int G>
+RAL_FI void ral_stg(E* __restrict__ p, ral_i64 row, const E (&v)[G]) {
+    typedef typename RalVecT<sizeof(E) * G>::T V;
+    union { V vec; E e[G]; } u;
+#pragma unroll
+    for (int g = 0; g < G; ++g) u.e[g] = v[g];
+    __stcs(reinterpret_cast<V*>(p + row), u.vec);
+}
+
+// ---- ordered flag access for the single-pass scan -------------------------------------------
+RAL_FI ral_u64 ral_ld_acquire(const ral_u64* p) {
+    ral_u64 v;
+    asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+    return v;
+}
+RAL_FI void ral_st_release(ral_u64* p, ral_u64 v) {
+    asm volatile("st.release.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+RAL_FI ral_u32 ral_lanemask_lt() {
+    ral_u32 m;
+    asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+    return m;
+}
+
+#endif  // RAL_DEVICE_RT_CUH_

@@ -1,0 +1,244 @@
+// engine.cpp — perform_operation: validate, specialise, launch.
+//
+// Replaces src/Interpreter/interpreter_cpp.cu:219-286.  The reference creates
+// a stream, sizes the grid with an occupancy if-chain, allocates temp space,
+// copies the program with 18 host-to-device copies and synchronises, per call.
+// Here the program is baked into a cached kernel, the column pointers and
+// literals travel as one kernel parameter block, and nothing is allocated.
+#include "engine.h"
+
+#include <algorithm>
+#include <atomic>
+#include <cstdlib>
+#include <cstring>
+#include <mutex>
+#include <unordered_map>
+
+namespace ral {
+
+namespace {
+std::atomic<long long> g_launches{0};
+thread_local std::string t_error;
+thread_local int t_error_code = 0;
+}  // namespace
+
+int set_error(int code, const std::string& msg) {
+    t_error = msg;
+    t_error_code = code;
+    return code;
+}
+const char* last_error() { return t_error.c_str(); }
+
+int check_cuda(cudaError_t e, const char* what) {
+    if (e == cudaSuccess) return kSuccess;
+    return set_error(kCudaError, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+void note_launch(int count) { g_launches += count; }
+long long launch_count() { return g_launches.load(); }
+
+Config& config() {
+    static Config c = [] {
+        Config x;
+        const char* v = std::getenv("RAL_FLOAT_LITERAL_COMPAT");
+        x.float_literal_compat = v && v[0] == '1';
+        return x;
+    }();
+    return c;
+}
+
+int build_program(Program& p, gdf_column* const* outputs, int n_out, gdf_column* const* inputs, int n_in,
+                  const ProgramArrays& pa, bool ignore_null_count) {
+    if (n_in <= 0 || inputs == nullptr) return set_error(kInvalidArgument, "no input columns");
+    if (n_out <= 0 || outputs == nullptr) return set_error(kInvalidArgument, "no output columns");
+    if (pa.n_ops < 0) return set_error(kInvalidArgument, "negative operation count");
+    if (pa.n_ops > 0 && (!pa.left || !pa.right || !pa.outs || !pa.bops || !pa.uops || !pa.lscalars || !pa.rscalars))
+        return set_error(kInvalidArgument, "program arrays must not be null");
+    if (!pa.final_positions) return set_error(kInvalidArgument, "final_output_positions must not be null");
+    std::vector<ColumnDesc> ins(n_in);
+    for (int c = 0; c < n_in; c++) {
+        const gdf_column* col = inputs[c];
+        if (!col) return set_error(kInvalidArgument, "null input column");
+        ins[c].dtype = col->dtype;
+        ins[c].has_valid = col->valid != nullptr;
+        ins[c].nulls_possible = col->valid != nullptr && (ignore_null_count || col->null_count != 0);
+    }
+    std::vector<gdf_dtype> out_types(n_out);
+    std::vector<bool> out_valid(n_out);
+    for (int o = 0; o < n_out; o++) {
+        if (!outputs[o]) return set_error(kInvalidArgument, "null output column");
+        out_types[o] = outputs[o]->dtype;
+        out_valid[o] = outputs[o]->valid != nullptr;
+    }
+    p.float_literal_compat = config().float_literal_compat;
+    std::string err;
+    if (!p.build(ins, out_types, out_valid, pa.left, pa.right, pa.outs, pa.n_ops, pa.final_positions, pa.bops,
+                 pa.uops, pa.lscalars, pa.rscalars, err))
+        return set_error(kUnsupported, err);
+    return kSuccess;
+}
+
+void fill_scalars(const Program& p, const ParamLayout& L, std::vector<uint64_t>& slots) {
+    for (size_t k = 0; k < p.ops.size(); k++) {
+        if (L.lscalar_slot[k] >= 0) slots[L.lscalar_slot[k]] = p.ops[k].lscalar;
+        if (L.rscalar_slot[k] >= 0) slots[L.rscalar_slot[k]] = p.ops[k].rscalar;
+    }
+}
+
+namespace {
+
+struct DeviceInfo {
+    int sms = 0;
+};
+std::mutex g_dev_mu;
+std::unordered_map<int, DeviceInfo> g_devs;
+std::unordered_map<std::string, int> g_occupancy;  // kernel name + device -> blocks/SM
+
+int device_sms() {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    std::lock_guard<std::mutex> lock(g_dev_mu);
+    auto it = g_devs.find(dev);
+    if (it != g_devs.end()) return it->second.sms;
+    DeviceInfo d;
+    cudaDeviceGetAttribute(&d.sms, cudaDevAttrMultiProcessorCount, dev);
+    if (d.sms <= 0) d.sms = 1;
+    g_devs[dev] = d;
+    return d.sms;
+}
+
+int blocks_per_sm(const CompiledKernel& k, int threads) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    const std::string key = k.name + "@" + std::to_string(dev) + "/" + std::to_string(threads);
+    {
+        std::lock_guard<std::mutex> lock(g_dev_mu);
+        auto it = g_occupancy.find(key);
+        if (it != g_occupancy.end()) return it->second;
+    }
+    int b = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, (const void*)k.kernel, threads, 0) != cudaSuccess) {
+        cudaGetLastError();
+        b = 1;
+    }
+    if (b < 1) b = 1;
+    std::lock_guard<std::mutex> lock(g_dev_mu);
+    g_occupancy[key] = b;
+    return b;
+}
+
+bool aligned(const void* p, size_t a) { return ((uintptr_t)p % a) == 0; }
+
+// Key of the generated-kernel cache: program structure + launch shape.
+std::mutex g_gen_mu;
+std::unordered_map<std::string, GeneratedKernel> g_generated;
+
+const GeneratedKernel& generated_eval(const Program& p, const Shape& s) {
+    const std::string key = p.structure_key() + "#" + std::to_string(s.G) + "/" + std::to_string(s.J) + "/" +
+                            std::to_string(s.threads) + "/" + std::to_string(s.min_blocks);
+    std::lock_guard<std::mutex> lock(g_gen_mu);
+    auto it = g_generated.find(key);
+    if (it != g_generated.end()) return it->second;
+    auto res = g_generated.emplace(key, generate_eval_kernel(p, s));
+    return res.first->second;
+}
+
+}  // namespace
+
+int launch_blocks(const CompiledKernel& k, int threads, int64_t rows_per_block, int64_t rows) {
+    const int sms = device_sms();
+    const int per_sm = blocks_per_sm(k, threads);
+    int64_t want = rows_per_block > 0 ? (rows + rows_per_block - 1) / rows_per_block : 1;
+    int64_t cap = (int64_t)sms * per_sm;
+    int64_t b = std::min<int64_t>(std::max<int64_t>(want, 1), cap);
+    return (int)std::max<int64_t>(b, 1);
+}
+
+int perform_operation(gdf_column* const* outputs, int n_out, gdf_column* const* inputs, int n_in,
+                      const ProgramArrays& pa, const EvalOptions& opt) {
+    Program p;
+    int rc = build_program(p, outputs, n_out, inputs, n_in, pa, opt.ignore_null_count);
+    if (rc) return rc;
+    const int64_t n = inputs[0]->size;
+    if (n < 0) return set_error(kInvalidArgument, "negative row count");
+    for (int c = 0; c < n_in; c++)
+        if (inputs[c]->size < n) return set_error(kInvalidArgument, "input column shorter than input 0");
+    for (int o = 0; o < n_out; o++)
+        if (outputs[o]->size < n) return set_error(kInvalidArgument, "output column shorter than the input");
+
+    Shape s = opt.shape.G > 0 ? opt.shape : default_shape(p);
+    // vector loads need every touched buffer aligned to G elements
+    const auto ref = p.inputs_referenced();
+    bool ok_align = true;
+    for (int c = 0; c < n_in; c++) {
+        if (ref[c] && n > 0 && !aligned(inputs[c]->data, (size_t)s.G * gdf_dtype_size(inputs[c]->dtype))) ok_align = false;
+        if (inputs[c]->valid && !aligned(inputs[c]->valid, 4))
+            return set_error(kInvalidArgument, "validity masks must be 4-byte aligned");
+    }
+    for (int o = 0; o < n_out; o++) {
+        if (n > 0 && !aligned(outputs[o]->data, (size_t)s.G * gdf_dtype_size(outputs[o]->dtype))) ok_align = false;
+        if (outputs[o]->valid && !aligned(outputs[o]->valid, 4))
+            return set_error(kInvalidArgument, "validity masks must be 4-byte aligned");
+    }
+    if (!ok_align) { s.G = 1; s.J = 4; }
+    if (n > 0) {
+        for (int c = 0; c < n_in; c++)
+            if (ref[c] && !inputs[c]->data) return set_error(kInvalidArgument, "input column without data");
+        for (int o = 0; o < n_out; o++)
+            if (!outputs[o]->data) return set_error(kInvalidArgument, "output column without data");
+    }
+
+    const GeneratedKernel& gk = generated_eval(p, s);
+    std::string err;
+    const CompiledKernel* k = jit_get(gk, err);
+    if (!k) return set_error(kJitError, err);
+    const ParamLayout& L = k->layout;
+
+    bool want_counts = opt.null_counts != nullptr;
+    uint64_t* d_counts = nullptr;
+    cudaStream_t st = opt.stream;
+    if (want_counts) {
+        if (int e = check_cuda(cudaMallocAsync((void**)&d_counts, sizeof(uint64_t) * n_out, st), "cudaMallocAsync"))
+            return e;
+        if (int e = check_cuda(cudaMemsetAsync(d_counts, 0, sizeof(uint64_t) * n_out, st), "cudaMemsetAsync"))
+            return e;
+    }
+    std::vector<uint64_t> slots(L.total, 0);
+    slots[L.n_rows] = (uint64_t)n;
+    for (int c = 0; c < n_in; c++) {
+        slots[L.in_data + c] = (uint64_t)(uintptr_t)inputs[c]->data;
+        slots[L.in_valid + c] = (uint64_t)(uintptr_t)inputs[c]->valid;
+    }
+    for (int o = 0; o < n_out; o++) {
+        slots[L.out_data + o] = (uint64_t)(uintptr_t)outputs[o]->data;
+        slots[L.out_valid + o] = (uint64_t)(uintptr_t)outputs[o]->valid;
+    }
+    slots[L.counts] = (uint64_t)(uintptr_t)d_counts;
+    fill_scalars(p, L, slots);
+
+    if (n > 0) {
+        const int64_t rows_per_block = (int64_t)32 * s.G * s.J * (s.threads / 32);
+        const int grid = launch_blocks(*k, s.threads, rows_per_block, n);
+        void* args[] = {slots.data()};
+        if (int e = check_cuda(cudaLaunchKernel((const void*)k->kernel, dim3(grid), dim3(s.threads), args, 0, st),
+                               "launch of the expression kernel"))
+            return e;
+        note_launch();
+    }
+    if (want_counts) {
+        std::vector<uint64_t> h(n_out, 0);
+        if (int e = check_cuda(cudaMemcpyAsync(h.data(), d_counts, sizeof(uint64_t) * n_out, cudaMemcpyDeviceToHost, st),
+                               "cudaMemcpyAsync"))
+            return e;
+        cudaFreeAsync(d_counts, st);
+        if (int e = check_cuda(cudaStreamSynchronize(st), "cudaStreamSynchronize")) return e;
+        for (int o = 0; o < n_out; o++)
+            opt.null_counts[o] = outputs[o]->valid ? (int64_t)n - (int64_t)h[o] : 0;
+    } else if (opt.sync) {
+        if (int e = check_cuda(cudaStreamSynchronize(st), "cudaStreamSynchronize")) return e;
+    }
+    if (int e = check_cuda(cudaGetLastError(), "expression kernel")) return e;
+    return kSuccess;
+}
+
+}  // namespace ral

@@ -1,0 +1,85 @@
+// engine.h — host side of the expression path: program -> kernel -> launch.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "codegen.h"
+#include "jit.h"
+#include "program.h"
+#include "ral/gdf_compat.h"
+
+namespace ral {
+
+// Status codes of the C ABI (include/ral/ral_c.h).
+enum Status : int {
+    kSuccess = 0,
+    kInvalidArgument = 1,
+    kUnsupported = 2,
+    kCudaError = 3,
+    kJitError = 4,
+    kAllocError = 5,
+    kTimeout = 6,
+    kParseError = 7,
+};
+
+// Thread-local error text of the last failing call.
+int set_error(int code, const std::string& msg);
+const char* last_error();
+
+// Maps a CUDA error to kCudaError with context; returns kSuccess on cudaSuccess.
+int check_cuda(cudaError_t e, const char* what);
+
+struct ProgramArrays {
+    const int16_t* left;
+    const int16_t* right;
+    const int16_t* outs;
+    int32_t n_ops;
+    const int16_t* final_positions;
+    const int32_t* bops;
+    const int32_t* uops;
+    const gdf_scalar* lscalars;
+    const gdf_scalar* rscalars;
+};
+
+struct EvalOptions {
+    cudaStream_t stream = nullptr;
+    bool sync = true;
+    // when non-null, receives per output the number of null rows in [0, n)
+    // (outputs without a valid mask report 0)
+    int64_t* null_counts = nullptr;
+    // override the default launch shape (autotuner); G == 0 keeps the default
+    Shape shape{0, 0, 0, 0};
+    // treat every input's validity mask as possibly holding nulls, ignoring
+    // null_count (fused filter+project semantics)
+    bool ignore_null_count = false;
+};
+
+// perform_operation over gdf_columns.  Outputs are written in place.
+int perform_operation(gdf_column* const* outputs, int n_out, gdf_column* const* inputs, int n_in,
+                      const ProgramArrays& prog, const EvalOptions& opt);
+
+// Build a Program from gdf_columns (shared by the eval, filter and batch paths).
+int build_program(Program& p, gdf_column* const* outputs, int n_out, gdf_column* const* inputs, int n_in,
+                  const ProgramArrays& prog, bool ignore_null_count);
+
+// Number of SMs and resident blocks per SM for a compiled kernel on the current device.
+int launch_blocks(const CompiledKernel& k, int threads, int64_t work_items_per_block_unit, int64_t units);
+
+// Parameter block filled in ParamLayout order.
+void fill_scalars(const Program& p, const ParamLayout& L, std::vector<uint64_t>& slots);
+
+// Count of kernels this library has launched (all entry points).
+void note_launch(int count = 1);
+long long launch_count();
+
+// Process-wide options.
+struct Config {
+    bool float_literal_compat = false;  // RAL_FLOAT_LITERAL_COMPAT=1
+};
+Config& config();
+
+}  // namespace ral

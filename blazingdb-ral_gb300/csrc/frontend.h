@@ -1,0 +1,87 @@
+// frontend.h — Calcite RexNode text -> register program.
+//
+// Accepts the expression language of src/CalciteExpressionParsing.cpp and
+// emits exactly the program src/LogicalFilter.cpp:44-268 emits for it (same op
+// order, same temp registers), because the program layout is observable: the
+// validity pass's column flags depend on op positions
+// (src/Interpreter/interpreter_ops.cuh:1314).
+#pragma once
+
+#include <cstdint>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "ral/gdf_compat.h"
+
+namespace ral {
+
+struct ProgramVectors {
+    std::vector<int16_t> left, right, outs, final_pos;
+    std::vector<int32_t> bops, uops;
+    std::vector<gdf_scalar> lscalars, rscalars;
+};
+
+struct ParseError : std::exception {
+    std::string msg;
+    explicit ParseError(std::string m) : msg(std::move(m)) {}
+    const char* what() const noexcept override { return msg.c_str(); }
+};
+
+struct Expr {
+    enum Kind { Column, Literal, Call } kind = Literal;
+    int column = -1;                 // frame column index for Column
+    std::string text;                // literal text, or operator name for Call
+    std::vector<std::unique_ptr<Expr>> args;
+};
+
+// Applies the reference's textual rewrites (CASE(IS NOT NULL(x), x, y) ->
+// COALESCE(x, y), IS [NOT] NULL -> IS_[NOT_]NULL, CAST removal, EXTRACT ->
+// BL_*, FLOOR -> BL_FLOUR), then parses.  N-ary AND/OR become left-nested
+// binary calls.  Throws ParseError.
+std::unique_ptr<Expr> parse_expression(const std::string& text);
+
+// Frame column indices referenced by the expression.
+void collect_columns(const Expr& e, std::vector<bool>& used);
+
+// add_expression_to_plan: appends the ops of `e` to `pv`.  new_input_indices
+// maps frame column -> input register.  Throws ParseError.
+void emit_expression(const Expr& e, int expression_position, int num_outputs, int num_inputs,
+                     const std::vector<int>& new_input_indices, ProgramVectors& pv);
+
+// get_output_type_expression (literals count as "invalid" and take the other
+// operand's type).  Throws ParseError.
+gdf_dtype expression_output_type(const Expr& e, const std::vector<gdf_dtype>& frame_dtypes);
+
+// True when the expression text contains an evaluation (contains_evaluation).
+bool contains_evaluation(const std::string& expr_text);
+// get_index of a bare "$k" reference.
+int column_reference_index(const std::string& expr_text);
+
+// get_named_expression(query_part, name)
+std::string named_expression(const std::string& query_part, const std::string& name);
+
+// Splits "LogicalProject(a=[e1], b=[e2])" into (name, expression text) pairs
+// (get_expressions_from_expression_list + the substr logic of parse_project_plan).
+std::vector<std::pair<std::string, std::string>> project_expressions(const std::string& query_part);
+
+// Plan for evaluate_expression: the "$k" clone shortcut or a one-output program.
+struct ExpressionPlan {
+    bool clone = false;
+    int clone_column = -1;
+    std::vector<int> input_columns;  // frame columns in register order
+    ProgramVectors pv;
+};
+ExpressionPlan plan_expression(const std::string& expression, int num_frame_columns);
+
+// Plan for a LogicalProject.
+struct ProjectPlan {
+    std::vector<int> input_columns;
+    ProgramVectors pv;
+    std::vector<gdf_dtype> eval_dtypes;        // per evaluated expression
+    std::vector<std::pair<bool, int>> columns; // per projected column: (evaluated, k or frame column)
+    std::vector<std::string> names;
+};
+ProjectPlan plan_project(const std::string& query_part, const std::vector<gdf_dtype>& frame_dtypes);
+
+}  // namespace ral

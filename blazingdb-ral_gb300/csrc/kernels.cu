@@ -1,0 +1,239 @@
+// kernels.cu — ahead-of-time kernels of the expression path (nvcc, sm_103a).
+//
+//   ral_count_valid      null_count recount (GDFColumn.cu:519-529 uses cudf's
+//                        gdf_count_nonzero_mask)
+//   ral_gather_*         materialize_column (ColumnManipulation.cu:26-150): data
+//                        gather plus validity gather with ballot-built words
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdint>
+
+#include "device_rt.cuh"
+#include "kernels.h"
+#include "engine.h"
+
+namespace ral {
+
+namespace {
+
+__global__ void count_valid_kernel(const ral_u32* __restrict__ valid, ral_i64 n, unsigned long long* out) {
+    const ral_i64 words = (n + 31) >> 5;
+    ral_u64 acc = 0;
+    for (ral_i64 w = (ral_i64)blockIdx.x * blockDim.x + threadIdx.x; w < words; w += (ral_i64)gridDim.x * blockDim.x) {
+        ral_u32 v = __ldg(valid + w);
+        const ral_i64 rem = n - (w << 5);
+        if (rem < 32) v &= (1u << rem) - 1u;
+        acc += __popc(v);
+    }
+    for (int off = 16; off > 0; off >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, off);
+    __shared__ ral_u64 red[32];
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        ral_u64 t = 0;
+        for (int k = 0; k < (int)(blockDim.x >> 5); k++) t += red[k];
+        if (t) atomicAdd(out, (unsigned long long)t);
+    }
+}
+
+// One thread per output row; a warp builds each 32-row output validity word
+// with a ballot, so there is no read-modify-write of shared words.
+template <typename E, typename I>
+__global__ void gather_kernel(const E* __restrict__ in, const ral_u32* __restrict__ in_valid,
+                              const I* __restrict__ idx, ral_i64 n_out, E* __restrict__ out,
+                              ral_u32* __restrict__ out_valid, unsigned long long* valid_count) {
+    ral_u64 cnt = 0;
+    const ral_i64 stride = (ral_i64)gridDim.x * blockDim.x;
+    const ral_i64 n_round = (n_out + 31) & ~(ral_i64)31;
+    for (ral_i64 i = (ral_i64)blockIdx.x * blockDim.x + threadIdx.x; i < n_round; i += stride) {
+        bool bit = false;
+        if (i < n_out) {
+            const ral_i64 j = (ral_i64)idx[i];
+            if (j >= 0) {
+                out[i] = in[j];
+                bit = in_valid ? ((__ldg(in_valid + (j >> 5)) >> (j & 31)) & 1u) : true;
+            }
+        }
+        if (out_valid) {
+            const ral_u32 word = __ballot_sync(0xffffffffu, bit);
+            if ((threadIdx.x & 31) == 0) {
+                out_valid[i >> 5] = word;
+                cnt += __popc(word);
+            }
+        }
+    }
+    if (valid_count) {
+        for (int off = 16; off > 0; off >>= 1) cnt += __shfl_down_sync(0xffffffffu, cnt, off);
+        if ((threadIdx.x & 31) == 0 && cnt) atomicAdd(valid_count, (unsigned long long)cnt);
+    }
+}
+
+template <typename E>
+cudaError_t gather_by_index(const void* in, const uint32_t* in_valid, const void* idx, int idx_width, int64_t n_out,
+                            void* out, uint32_t* out_valid, unsigned long long* valid_count, cudaStream_t st) {
+    const int threads = 256;
+    int64_t blocks = (n_out + threads - 1) / threads;
+    if (blocks > 152 * 16) blocks = 152 * 16;
+    if (blocks < 1) blocks = 1;
+    const E* i_ = (const E*)in;
+    E* o_ = (E*)out;
+    switch (idx_width) {
+    case 1: gather_kernel<E, int8_t><<<(int)blocks, threads, 0, st>>>(i_, in_valid, (const int8_t*)idx, n_out, o_, out_valid, valid_count); break;
+    case 2: gather_kernel<E, int16_t><<<(int)blocks, threads, 0, st>>>(i_, in_valid, (const int16_t*)idx, n_out, o_, out_valid, valid_count); break;
+    case 4: gather_kernel<E, int32_t><<<(int)blocks, threads, 0, st>>>(i_, in_valid, (const int32_t*)idx, n_out, o_, out_valid, valid_count); break;
+    case 8: gather_kernel<E, int64_t><<<(int)blocks, threads, 0, st>>>(i_, in_valid, (const int64_t*)idx, n_out, o_, out_valid, valid_count); break;
+    default: return cudaErrorInvalidValue;
+    }
+    return cudaGetLastError();
+}
+
+
+// ---- single-pass stream compaction (decoupled look-back) ---------------------------------
+// Tile = 256 threads x 16 rows.  Tiles are taken in order from a ticket counter,
+// so every predecessor of a tile is already running and the look-back always
+// ends; the wait is still bounded (error flag, see kCompactSpinLimit).
+constexpr ral_u64 kFlagAggregate = 1ull << 62;
+constexpr ral_u64 kFlagInclusive = 2ull << 62;
+constexpr ral_u64 kValueMask = (1ull << 62) - 1;
+constexpr long kCompactSpinLimit = 1l << 22;
+
+// Returns the exclusive prefix of `tile` (called by all 32 lanes of warp 0).
+__device__ ral_u64 lookback(ral_u64* status, ral_i64 tile, ral_u64 aggregate, ral_u64* error_flag) {
+    const int lane = threadIdx.x & 31;
+    if (tile == 0) {
+        if (lane == 0) ral_st_release(status, kFlagInclusive | aggregate);
+        return 0;
+    }
+    if (lane == 0) ral_st_release(status + tile, kFlagAggregate | aggregate);
+    ral_u64 excl = 0;
+    ral_i64 j = tile - 1 - lane;
+    long spins = 0;
+    for (;;) {
+        const ral_u64 s = j >= 0 ? ral_ld_acquire(status + j) : kFlagInclusive;
+        const ral_u64 flag = s & ~kValueMask;
+        const unsigned incl = __ballot_sync(0xffffffffu, flag == kFlagInclusive);
+        const unsigned empty = __ballot_sync(0xffffffffu, flag == 0);
+        const int f = incl ? __ffs(incl) - 1 : 32;
+        const unsigned upto = f == 32 ? 0xffffffffu : (f == 31 ? 0xffffffffu : ((2u << f) - 1u));
+        if (empty & upto) {
+            if (++spins > kCompactSpinLimit) {
+                if (lane == 0) atomicExch((unsigned long long*)error_flag, 1ull);
+                break;
+            }
+            __nanosleep(64);
+            continue;
+        }
+        ral_u64 v = (lane <= f) ? (s & kValueMask) : 0;
+        for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
+        excl += __shfl_sync(0xffffffffu, v, 0);
+        if (f < 32) break;
+        j -= 32;
+    }
+    if (lane == 0) ral_st_release(status + tile, kFlagInclusive | ((excl + aggregate) & kValueMask));
+    return excl;
+}
+
+__global__ void __launch_bounds__(256) compact_stencil_kernel(const int8_t* __restrict__ stencil,
+                                                              const ral_u32* __restrict__ valid, ral_i64 n,
+                                                              int32_t* __restrict__ out, ral_u64* scratch) {
+    __shared__ ral_u32 s_tile;
+    __shared__ ral_u32 s_warp[8];
+    __shared__ ral_u64 s_prefix;
+    ral_u64* status = scratch + 3;
+    const ral_i64 ntiles = (n + kCompactTileRows - 1) / kCompactTileRows;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const bool vec_ok = (((uintptr_t)stencil) & 15) == 0;
+    for (;;) {
+        if (threadIdx.x == 0) s_tile = atomicAdd((unsigned int*)scratch, 1u);
+        __syncthreads();
+        const ral_i64 tile = s_tile;
+        if (tile >= ntiles) break;
+        const ral_i64 r0 = tile * kCompactTileRows + (ral_i64)threadIdx.x * 16;
+        ral_u32 keep = 0;
+        if (r0 + 16 <= n && vec_ok) {
+            const uint4 v = __ldcs(reinterpret_cast<const uint4*>(stencil + r0));
+            const ral_u32 w[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+            for (int k = 0; k < 16; k++) keep |= (((w[k >> 2] >> (8 * (k & 3))) & 0xffu) != 0u ? 1u : 0u) << k;
+        } else {
+            for (int k = 0; k < 16; k++)
+                if (r0 + k < n && stencil[r0 + k] != 0) keep |= 1u << k;
+        }
+        if (valid && r0 < n) keep &= (__ldg(valid + (r0 >> 5)) >> (r0 & 31)) & 0xffffu;
+        const ral_u32 cnt = __popc(keep);
+        ral_u32 incl = cnt;
+        for (int off = 1; off < 32; off <<= 1) {
+            const ral_u32 t = __shfl_up_sync(0xffffffffu, incl, off);
+            if (lane >= off) incl += t;
+        }
+        if (lane == 31) s_warp[warp] = incl;
+        __syncthreads();
+        if (warp == 0) {
+            ral_u32 wv = lane < 8 ? s_warp[lane] : 0;
+            ral_u32 wi = wv;
+            for (int off = 1; off < 8; off <<= 1) {
+                const ral_u32 t = __shfl_up_sync(0xffffffffu, wi, off);
+                if (lane >= off) wi += t;
+            }
+            const ral_u32 total = __shfl_sync(0xffffffffu, wi, 7);
+            const ral_u64 excl = lookback(status, tile, total, scratch + 1);
+            if (lane < 8) s_warp[lane] = wi - wv;
+            if (lane == 0) {
+                s_prefix = excl;
+                if (tile == ntiles - 1) scratch[2] = excl + total;
+            }
+        }
+        __syncthreads();
+        ral_u64 pos = s_prefix + s_warp[warp] + (incl - cnt);
+        while (keep) {
+            const int k = __ffs(keep) - 1;
+            keep &= keep - 1;
+            out[pos++] = (int32_t)(r0 + k);
+        }
+        __syncthreads();
+    }
+}
+
+}  // namespace
+
+cudaError_t launch_count_valid(const uint32_t* valid, int64_t n, unsigned long long* out, cudaStream_t st) {
+    if (n <= 0) return cudaSuccess;
+    const int threads = 256;
+    int64_t words = (n + 31) / 32;
+    int64_t blocks = (words + threads - 1) / threads;
+    if (blocks > 152 * 8) blocks = 152 * 8;
+    count_valid_kernel<<<(int)blocks, threads, 0, st>>>(valid, n, out);
+    note_launch();
+    return cudaGetLastError();
+}
+
+cudaError_t launch_compact_stencil(const int8_t* stencil, const uint32_t* stencil_valid, int64_t n, int32_t* out_idx,
+                                   unsigned long long* scratch, cudaStream_t st) {
+    if (n <= 0) return cudaSuccess;
+    int dev = 0, sms = 1, per_sm = 1;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, compact_stencil_kernel, 256, 0);
+    if (per_sm < 1) per_sm = 1;
+    const int64_t tiles = (n + kCompactTileRows - 1) / kCompactTileRows;
+    int64_t grid = std::min<int64_t>(tiles, (int64_t)sms * per_sm);
+    compact_stencil_kernel<<<(int)grid, 256, 0, st>>>(stencil, stencil_valid, n, out_idx, (ral_u64*)scratch);
+    note_launch();
+    return cudaGetLastError();
+}
+
+cudaError_t launch_gather(int width, const void* in, const uint32_t* in_valid, const void* idx, int idx_width,
+                          int64_t n_out, void* out, uint32_t* out_valid, unsigned long long* valid_count,
+                          cudaStream_t st) {
+    if (n_out <= 0) return cudaSuccess;
+    switch (width) {
+    case 1: return gather_by_index<int8_t>(in, in_valid, idx, idx_width, n_out, out, out_valid, valid_count, st);
+    case 2: return gather_by_index<int16_t>(in, in_valid, idx, idx_width, n_out, out, out_valid, valid_count, st);
+    case 4: return gather_by_index<int32_t>(in, in_valid, idx, idx_width, n_out, out, out_valid, valid_count, st);
+    case 8: return gather_by_index<int64_t>(in, in_valid, idx, idx_width, n_out, out, out_valid, valid_count, st);
+    default: return cudaErrorInvalidValue;
+    }
+}
+
+}  // namespace ral

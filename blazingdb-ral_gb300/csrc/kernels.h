@@ -1,0 +1,38 @@
+// kernels.h — launchers of the ahead-of-time kernels in kernels.cu.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+namespace ral {
+
+// Adds the number of set bits among the first n bits of `valid` to *out.
+cudaError_t launch_count_valid(const uint32_t* valid, int64_t n, unsigned long long* out, cudaStream_t st);
+
+// out[i] = in[idx[i]] for idx[i] >= 0 (elements of `width` bytes, indices of
+// `idx_width` bytes); out_valid (optional) gets bit i = in bit idx[i] (0 for
+// a negative index, 1 when in_valid is null); valid_count (optional) gets the
+// number of set output bits added.
+cudaError_t launch_gather(int width, const void* in, const uint32_t* in_valid, const void* idx, int idx_width,
+                          int64_t n_out, void* out, uint32_t* out_valid, unsigned long long* valid_count,
+                          cudaStream_t st);
+
+}  // namespace ral
+
+namespace ral {
+
+// Scratch layout of the single-pass compaction (one zeroed block per call):
+//   word 0: tile ticket counter, word 1: error flag (1 = a look-back wait gave up),
+//   word 2: kept-row total, words 3.. : one status word per tile.
+constexpr int64_t kCompactTileRows = 4096;  // 256 threads x 16 rows
+inline int64_t compact_scratch_words(int64_t n) { return 3 + (n + kCompactTileRows - 1) / kCompactTileRows; }
+
+// cudf::apply_boolean_mask over the row-index column (CalciteInterpreter.cpp:531-543):
+// writes the indices of rows whose stencil byte is nonzero and whose stencil
+// valid bit is set (stencil_valid may be null) to out_idx, in row order, and the
+// count to scratch[2].  `scratch` must hold compact_scratch_words(n) zeroed words.
+cudaError_t launch_compact_stencil(const int8_t* stencil, const uint32_t* stencil_valid, int64_t n, int32_t* out_idx,
+                                   unsigned long long* scratch, cudaStream_t st);
+
+}  // namespace ral

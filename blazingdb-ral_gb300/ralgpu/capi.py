@@ -1,0 +1,323 @@
+"""ctypes bindings of include/ral/ral_c.h and Python-shaped entry points."""
+from __future__ import annotations
+
+import ctypes
+import os
+from typing import List, Optional, Sequence, Tuple
+
+import numpy as np
+
+from . import dtypes as D
+from .column import Column, GdfColumn, GdfScalar, Scalar
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_LIB_PATH = os.path.join(os.path.dirname(_HERE), "_build", "libralgpu.so")
+_lib = None
+
+C = ctypes
+P = C.c_void_p
+I16P = C.POINTER(C.c_int16)
+I32P = C.POINTER(C.c_int32)
+COLPP = C.POINTER(C.POINTER(GdfColumn))
+SCP = C.POINTER(GdfScalar)
+
+_SIGS = {
+    "ral_last_error": (C.c_char_p, []),
+    "ral_version": (C.c_char_p, []),
+    "ral_perform_operation": (C.c_int, [COLPP, C.c_int32, COLPP, C.c_int32, I16P, I16P, I16P, C.c_int32, I16P,
+                                        I32P, I32P, SCP, SCP, I16P, C.c_int32]),
+    "ral_perform_operation_async": (C.c_int, [COLPP, C.c_int32, COLPP, C.c_int32, I16P, I16P, I16P, C.c_int32,
+                                              I16P, I32P, I32P, SCP, SCP, P, C.POINTER(C.c_int64)]),
+    "ral_evaluate_expression": (C.c_int, [COLPP, C.c_int32, C.c_char_p, C.POINTER(GdfColumn)]),
+    "ral_process_filter": (C.c_int, [COLPP, C.c_int32, C.c_char_p, COLPP, C.POINTER(C.c_int32)]),
+    "ral_process_filter_async": (C.c_int, [COLPP, C.c_int32, C.c_char_p, COLPP, C.POINTER(C.c_int32), P]),
+    "ral_project_output_types": (C.c_int, [I32P, C.c_int32, C.c_char_p, I32P, I32P, I32P, C.c_int32]),
+    "ral_execute_project_plan": (C.c_int, [COLPP, C.c_int32, C.c_char_p, COLPP, C.c_int32]),
+    "ral_filter_project": (C.c_int, [COLPP, C.c_int32, C.c_char_p, C.c_char_p, COLPP, C.c_int32,
+                                     C.POINTER(C.c_int32)]),
+    "ral_materialize_column": (C.c_int, [C.POINTER(GdfColumn), C.POINTER(GdfColumn), C.POINTER(GdfColumn)]),
+    "ral_add_expression_to_plan": (C.c_int, [C.c_char_p, C.c_int16, C.c_int16, C.c_int16, I16P, C.c_int32,
+                                             I16P, I16P, I16P, I32P, I32P, SCP, SCP, I32P, C.c_int32]),
+    "ral_get_output_type_expression": (C.c_int, [I32P, C.c_int32, C.c_char_p, I32P]),
+    "ral_debug_program_source": (C.c_int, [I32P, I32P, C.c_int32, I32P, I32P, C.c_int32, I16P, I16P, I16P,
+                                           C.c_int32, I16P, I32P, I32P, SCP, SCP, C.c_int32, C.c_char_p,
+                                           C.c_int64, C.c_char_p, C.c_int64]),
+    "ral_kernel_launches": (C.c_int64, []),
+    "ral_jit_stats": (C.c_int, [C.POINTER(C.c_int64), C.POINTER(C.c_int64), C.POINTER(C.c_int64),
+                                C.POINTER(C.c_double)]),
+}
+
+
+class RalError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"[{code}] {msg}")
+        self.code = code
+
+
+def lib():
+    """Loads libralgpu.so (built by blazingdb-ral_gb300/build.py); raises if it is absent."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(_LIB_PATH):
+            raise RalError(-1, f"libralgpu.so not built ({_LIB_PATH}); run __graft_entry__.build()")
+        L = C.CDLL(_LIB_PATH)
+        for name, (res, args) in _SIGS.items():
+            f = getattr(L, name)
+            f.restype = res
+            f.argtypes = args
+        _lib = L
+    return _lib
+
+
+def _check(rc: int) -> None:
+    if rc != 0:
+        raise RalError(rc, lib().ral_last_error().decode(errors="replace"))
+
+
+def version() -> str:
+    return lib().ral_version().decode()
+
+
+def _i16(a) -> np.ndarray:
+    return np.ascontiguousarray(np.asarray(a, dtype=np.int16))
+
+
+def _i32(a) -> np.ndarray:
+    return np.ascontiguousarray(np.asarray(a, dtype=np.int32))
+
+
+def _p16(a: np.ndarray):
+    return a.ctypes.data_as(I16P)
+
+
+def _p32(a: np.ndarray):
+    return a.ctypes.data_as(I32P)
+
+
+def _colarray(cols: Sequence[Column]):
+    structs = [c.to_c() for c in cols]
+    arr = (C.POINTER(GdfColumn) * max(1, len(structs)))()
+    for i, s in enumerate(structs):
+        arr[i] = C.pointer(s)
+    return arr, structs
+
+
+def _scalars(ss: Sequence[Scalar]):
+    arr = (GdfScalar * max(1, len(ss)))()
+    for i, s in enumerate(ss):
+        arr[i] = s.to_c()
+    return arr
+
+
+def _as_scalar(s) -> Scalar:
+    if isinstance(s, Scalar):
+        return s
+    if isinstance(s, tuple):
+        return Scalar(*s)
+    raise TypeError("scalars are ralgpu.Scalar or (dtype, value[, is_valid]) tuples")
+
+
+def perform_operation(output_columns: List[Column], input_columns: List[Column], left_inputs, right_inputs,
+                      outputs, final_output_positions, operators, unary_operators, left_scalars, right_scalars,
+                      new_input_indices=None) -> None:
+    """perform_operation (src/Interpreter/interpreter_cpp.h:25-37), synchronous."""
+    oa, _os = _colarray(output_columns)
+    ia, _is = _colarray(input_columns)
+    l, r, o, f = _i16(left_inputs), _i16(right_inputs), _i16(outputs), _i16(final_output_positions)
+    b, u = _i32(operators), _i32(unary_operators)
+    ls = _scalars([_as_scalar(s) for s in left_scalars])
+    rs = _scalars([_as_scalar(s) for s in right_scalars])
+    nii = _i16(new_input_indices if new_input_indices is not None else list(range(len(input_columns))))
+    _check(lib().ral_perform_operation(oa, len(output_columns), ia, len(input_columns), _p16(l), _p16(r), _p16(o),
+                                       len(l), _p16(f), _p32(b), _p32(u), ls, rs, _p16(nii), len(nii)))
+
+
+def perform_operation_async(output_columns: List[Column], input_columns: List[Column], left_inputs, right_inputs,
+                            outputs, final_output_positions, operators, unary_operators, left_scalars,
+                            right_scalars, stream=None, want_null_counts: bool = False):
+    """Enqueues on `stream` (torch.cuda.Stream, raw handle, or None = torch's current stream)."""
+    import torch
+    if stream is None:
+        handle = torch.cuda.current_stream().cuda_stream
+    elif isinstance(stream, int):
+        handle = stream
+    else:
+        handle = stream.cuda_stream
+    oa, _os = _colarray(output_columns)
+    ia, _is = _colarray(input_columns)
+    l, r, o, f = _i16(left_inputs), _i16(right_inputs), _i16(outputs), _i16(final_output_positions)
+    b, u = _i32(operators), _i32(unary_operators)
+    ls = _scalars([_as_scalar(s) for s in left_scalars])
+    rs = _scalars([_as_scalar(s) for s in right_scalars])
+    nc = np.zeros(len(output_columns), dtype=np.int64)
+    ncp = nc.ctypes.data_as(C.POINTER(C.c_int64)) if want_null_counts else None
+    _check(lib().ral_perform_operation_async(oa, len(output_columns), ia, len(input_columns), _p16(l), _p16(r),
+                                             _p16(o), len(l), _p16(f), _p32(b), _p32(u), ls, rs, C.c_void_p(handle),
+                                             ncp))
+    if want_null_counts:
+        for col, v in zip(output_columns, nc):
+            col.null_count = int(v)
+        return nc
+    return None
+
+
+def evaluate_expression(frame: List[Column], expression: str, output: Column) -> Column:
+    """evaluate_expression (src/LogicalFilter.h:20-23)."""
+    fa, _fs = _colarray(frame)
+    oc = output.to_c()
+    _check(lib().ral_evaluate_expression(fa, len(frame), expression.encode(), C.byref(oc)))
+    output.sync_from_c(oc)
+    return output
+
+
+def process_filter(frame: List[Column], query_part: str) -> List[Column]:
+    """LogicalFilter (src/CalciteInterpreter.cpp:509-573): returns the filtered frame (new columns)."""
+    n = frame[0].size
+    outs = [Column.empty(c.dtype, n, with_valid=c.valid is not None) for c in frame]
+    fa, _fs = _colarray(frame)
+    oa, ostructs = _colarray(outs)
+    n_out = C.c_int32(0)
+    _check(lib().ral_process_filter(fa, len(frame), query_part.encode(), oa, C.byref(n_out)))
+    for col, s in zip(outs, ostructs):
+        col.sync_from_c(s)
+    return outs
+
+
+def project_output_types(frame_dtypes: Sequence[int], query_part: str) -> Tuple[List[int], List[bool]]:
+    fd = _i32(frame_dtypes)
+    cap = 4096
+    n = C.c_int32(0)
+    dt = np.zeros(cap, dtype=np.int32)
+    ev = np.zeros(cap, dtype=np.int32)
+    _check(lib().ral_project_output_types(_p32(fd), len(fd), query_part.encode(), C.byref(n), _p32(dt), _p32(ev), cap))
+    return [int(x) for x in dt[:n.value]], [bool(x) for x in ev[:n.value]]
+
+
+def execute_project_plan(frame: List[Column], query_part: str) -> List[Column]:
+    """LogicalProject (src/CalciteInterpreter.cpp:311-336): returns the projected frame."""
+    types, evald = project_output_types([c.dtype for c in frame], query_part)
+    n = frame[0].size
+    outs = [Column.empty(t, n, with_valid=True) if e else Column(None, None, t, 0) for t, e in zip(types, evald)]
+    fa, _fs = _colarray(frame)
+    structs = []
+    arr = (C.POINTER(GdfColumn) * max(1, len(outs)))()
+    for i, c in enumerate(outs):
+        s = c.to_c() if c.data is not None else GdfColumn()
+        structs.append(s)
+        arr[i] = C.pointer(s)
+    _check(lib().ral_execute_project_plan(fa, len(frame), query_part.encode(), arr, len(outs)))
+    result = []
+    for i, (c, s, e) in enumerate(zip(outs, structs, evald)):
+        if e:
+            c.sync_from_c(s)
+            result.append(c)
+        else:
+            src = next(f for f in frame if f.data is not None and f.data.data_ptr() == s.data) \
+                if s.data else frame[0]
+            src.null_count = int(s.null_count)
+            result.append(src)
+    return result
+
+
+def filter_project(frame: List[Column], filter_query_part: str, project_query_part: str) -> List[Column]:
+    """LogicalProject over LogicalFilter, fused: returns the projected, filtered frame."""
+    types, evald = project_output_types([c.dtype for c in frame], project_query_part)
+    n = frame[0].size
+    srcs = _passthrough_sources(frame, project_query_part)
+    outs = []
+    for i, (t, e) in enumerate(zip(types, evald)):
+        with_valid = True if e else (srcs[i].valid is not None)
+        outs.append(Column.empty(t, n, with_valid=with_valid))
+    fa, _fs = _colarray(frame)
+    oa, ostructs = _colarray(outs)
+    n_out = C.c_int32(0)
+    _check(lib().ral_filter_project(fa, len(frame), filter_query_part.encode(), project_query_part.encode(), oa,
+                                    len(outs), C.byref(n_out)))
+    for col, s in zip(outs, ostructs):
+        col.sync_from_c(s)
+    return outs
+
+
+def _passthrough_sources(frame: List[Column], project_query_part: str) -> dict:
+    """Frame column behind each pass-through projection ("$k")."""
+    out = {}
+    inner = project_query_part[project_query_part.find("(") + 1:project_query_part.rfind(")")]
+    depth, start, parts = 0, 0, []
+    for i, ch in enumerate(inner):
+        if ch in "([":
+            depth += 1
+        elif ch in ")]":
+            depth -= 1
+        elif ch == "," and depth == 0:
+            parts.append(inner[start:i])
+            start = i + 1
+    parts.append(inner[start:])
+    for i, p in enumerate(parts):
+        body = p.strip()
+        body = body[body.find("=[") + 2:-1]
+        if "(" not in body.replace("CAST(", "").replace("):BIGINT", ""):
+            out[i] = frame[int(body.strip()[1:])]
+    return out
+
+
+def materialize_column(input_column: Column, row_indices: Column, with_valid: Optional[bool] = None) -> Column:
+    """materialize_column (src/ColumnManipulation.cuh:16-18): gather by row index."""
+    n = row_indices.size
+    wv = (input_column.valid is not None) if with_valid is None else with_valid
+    out = Column.empty(input_column.dtype, n, with_valid=wv)
+    ic, oc, rc = input_column.to_c(), out.to_c(), row_indices.to_c()
+    _check(lib().ral_materialize_column(C.byref(ic), C.byref(oc), C.byref(rc)))
+    out.sync_from_c(oc)
+    return out
+
+
+def add_expression_to_plan(expression: str, expression_position: int, num_outputs: int, num_inputs: int,
+                           new_input_indices: Sequence[int]):
+    """The register-program emitter (src/LogicalFilter.h:26-42); returns the op arrays."""
+    cap = 1024
+    l, r, o = (np.zeros(cap, dtype=np.int16) for _ in range(3))
+    b, u = np.zeros(cap, dtype=np.int32), np.zeros(cap, dtype=np.int32)
+    ls, rs = (GdfScalar * cap)(), (GdfScalar * cap)()
+    nii = _i16(new_input_indices)
+    n = C.c_int32(0)
+    _check(lib().ral_add_expression_to_plan(expression.encode(), expression_position, num_outputs, num_inputs,
+                                            _p16(nii), len(nii), _p16(l), _p16(r), _p16(o), _p32(b), _p32(u), ls, rs,
+                                            C.byref(n), cap))
+    k = n.value
+    return dict(left=l[:k].tolist(), right=r[:k].tolist(), outputs=o[:k].tolist(), operators=b[:k].tolist(),
+                unary_operators=u[:k].tolist(), left_scalars=[Scalar.from_c(ls[i]) for i in range(k)],
+                right_scalars=[Scalar.from_c(rs[i]) for i in range(k)])
+
+
+def get_output_type_expression(frame_dtypes: Sequence[int], expression: str) -> int:
+    fd = _i32(frame_dtypes)
+    out = C.c_int32(0)
+    _check(lib().ral_get_output_type_expression(_p32(fd), len(fd), expression.encode(), C.byref(out)))
+    return out.value
+
+
+def debug_program_source(input_dtypes, input_nullable, output_dtypes, output_nullable, left, right, outputs,
+                         final_positions, operators, unary_operators, left_scalars, right_scalars,
+                         compile: bool = False) -> Tuple[str, str]:
+    """Generated CUDA source (and NVRTC log when compile=True) of a program; needs no GPU."""
+    idt, inl, odt, onl = _i32(input_dtypes), _i32(input_nullable), _i32(output_dtypes), _i32(output_nullable)
+    l, r, o, f = _i16(left), _i16(right), _i16(outputs), _i16(final_positions)
+    b, u = _i32(operators), _i32(unary_operators)
+    ls = _scalars([_as_scalar(s) for s in left_scalars])
+    rs = _scalars([_as_scalar(s) for s in right_scalars])
+    src = C.create_string_buffer(1 << 20)
+    log = C.create_string_buffer(1 << 16)
+    _check(lib().ral_debug_program_source(_p32(idt), _p32(inl), len(idt), _p32(odt), _p32(onl), len(odt), _p16(l),
+                                          _p16(r), _p16(o), len(l), _p16(f), _p32(b), _p32(u), ls, rs,
+                                          1 if compile else 0, src, len(src), log, len(log)))
+    return src.value.decode(), log.value.decode()
+
+
+def kernel_launches() -> int:
+    return int(lib().ral_kernel_launches())
+
+
+def jit_stats() -> dict:
+    a, b, c, d = C.c_int64(), C.c_int64(), C.c_int64(), C.c_double()
+    lib().ral_jit_stats(C.byref(a), C.byref(b), C.byref(c), C.byref(d))
+    return dict(compiles=a.value, disk_hits=b.value, memory_hits=c.value, compile_ms=d.value)

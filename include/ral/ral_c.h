@@ -1,0 +1,175 @@
+/*
+ * ral_c.h — C ABI of the GB300 expression-evaluation library (libralgpu.so).
+ *
+ * These entry points replace the BlazingSQL RAL's expression path.  Each one
+ * names the reference interface it stands in for (paths relative to the
+ * reference project root).  Conventions:
+ *   - Every function returns RAL_SUCCESS (0) or an error code; the message of
+ *     the last failure on the calling thread is ral_last_error().  (The
+ *     reference throws std::runtime_error; include/ral/ral.hpp rethrows.)
+ *   - Columns are gdf_column (include/ral/gdf_compat.h).  Data and validity
+ *     buffers are device memory.  Validity buffers must be 4-byte aligned and
+ *     hold gdf_valid_allocation_size(size) bytes, as the reference allocates
+ *     them: kernels read and write whole 32-bit words.
+ *   - Synchronous entry points return after the GPU work is complete, like the
+ *     reference.  *_async variants take a cudaStream_t (as void*) and return
+ *     after enqueueing.
+ *   - Entry points are thread-safe.
+ */
+#ifndef RAL_C_H_
+#define RAL_C_H_
+
+#include "ral/gdf_compat.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define RAL_SUCCESS 0
+#define RAL_ERROR_INVALID_ARGUMENT 1
+#define RAL_ERROR_UNSUPPORTED 2 /* a program or expression the interpreter cannot run */
+#define RAL_ERROR_CUDA 3
+#define RAL_ERROR_JIT 4
+#define RAL_ERROR_ALLOC 5
+#define RAL_ERROR_TIMEOUT 6     /* a bounded device-side wait gave up */
+#define RAL_ERROR_PARSE 7
+
+const char *ral_last_error(void);
+const char *ral_version(void);
+
+/*
+ * perform_operation — src/Interpreter/interpreter_cpp.h:25-37
+ * (implementation src/Interpreter/interpreter_cpp.cu:219-286).
+ * Runs one register program over n = input_columns[0]->size rows into the
+ * caller-allocated output columns.  Arrays left_inputs .. right_scalars have
+ * num_operations entries; final_output_positions has num_outputs entries.
+ * new_input_indices is accepted and ignored, as in the reference.  Output
+ * null_count is not updated (the reference leaves it too).
+ */
+int ral_perform_operation(gdf_column *const *output_columns, int32_t num_outputs,
+                          gdf_column *const *input_columns, int32_t num_inputs,
+                          const column_index_type *left_inputs, const column_index_type *right_inputs,
+                          const column_index_type *outputs, int32_t num_operations,
+                          const column_index_type *final_output_positions,
+                          const int32_t *operators /* gdf_binary_operator */,
+                          const int32_t *unary_operators /* gdf_unary_operator */,
+                          const gdf_scalar *left_scalars, const gdf_scalar *right_scalars,
+                          const column_index_type *new_input_indices, int32_t num_new_input_indices);
+
+/* Same, enqueued on `stream` (cudaStream_t); when null_counts is non-null the
+ * call synchronises and stores each output's null count there (the fused
+ * form of execute_project_plan's update_null_count, CalciteInterpreter.cpp:332-335). */
+int ral_perform_operation_async(gdf_column *const *output_columns, int32_t num_outputs,
+                                gdf_column *const *input_columns, int32_t num_inputs,
+                                const column_index_type *left_inputs, const column_index_type *right_inputs,
+                                const column_index_type *outputs, int32_t num_operations,
+                                const column_index_type *final_output_positions, const int32_t *operators,
+                                const int32_t *unary_operators, const gdf_scalar *left_scalars,
+                                const gdf_scalar *right_scalars, void *stream, int64_t *null_counts);
+
+/*
+ * evaluate_expression — src/LogicalFilter.h:20-23 (src/LogicalFilter.cpp:271-371).
+ * Compiles one Calcite RexNode expression over the frame's columns and
+ * evaluates it into `output` (caller-allocated, n rows).  For an expression
+ * that is a bare column reference "$k" the reference replaces the output with
+ * a clone of column k; here column k's data, mask and null count are copied
+ * into `output`, whose dtype must then equal column k's.
+ */
+int ral_evaluate_expression(gdf_column *const *frame_columns, int32_t num_columns, const char *expression,
+                            gdf_column *output);
+
+/*
+ * process_filter — src/CalciteInterpreter.cpp:509-573.
+ * Evaluates the LogicalFilter condition, keeps the rows whose stencil is valid
+ * and nonzero and gathers EVERY frame column, in row order, into out_columns.
+ * out_columns[i] must have the dtype of frame column i, data capacity for
+ * frame_columns[0]->size rows and, exactly when frame column i has one, a
+ * validity buffer of that capacity.  On return each out column's size and
+ * null_count are set and *num_rows_out holds the kept row count.
+ * One fused kernel: predicate, single-pass ballot/look-back compaction and the
+ * gather of all columns.
+ */
+int ral_process_filter(gdf_column *const *frame_columns, int32_t num_columns, const char *query_part,
+                       gdf_column *const *out_columns, gdf_size_type *num_rows_out);
+int ral_process_filter_async(gdf_column *const *frame_columns, int32_t num_columns, const char *query_part,
+                             gdf_column *const *out_columns, gdf_size_type *num_rows_out, void *stream);
+
+/*
+ * execute_project_plan — src/CalciteInterpreter.cpp:311-336 with
+ * parse_project_plan :123-309.  All evaluated expressions of the
+ * LogicalProject run as one program.  out_columns has one entry per projected
+ * expression: for a pass-through "$k" the entry is filled with frame column k's
+ * buffers (shared, not copied, like the reference); for an evaluated
+ * expression the caller provides data (and validity, always expected, as the
+ * reference allocates it) of the dtype ral_project_output_types reports.
+ * null_count of every output is set.
+ */
+int ral_project_output_types(const gdf_dtype *frame_dtypes, int32_t num_columns, const char *query_part,
+                             int32_t *num_projected, gdf_dtype *dtypes_out, int32_t *is_evaluated_out,
+                             int32_t capacity);
+int ral_execute_project_plan(gdf_column *const *frame_columns, int32_t num_columns, const char *query_part,
+                             gdf_column *const *out_columns, int32_t num_out_columns);
+
+/*
+ * LogicalFilter followed by LogicalProject, fused (the plan shape
+ * "LogicalProject(...)\n  LogicalFilter(condition=[...])", evaluated by
+ * CalciteInterpreter.cpp:719-723 as process_filter then execute_project_plan).
+ * The projection is evaluated only on kept rows and written compacted; no
+ * filtered copy of the frame is materialised.  out_columns as for
+ * ral_execute_project_plan but with capacity for frame_columns[0]->size rows;
+ * pass-through columns are gathered (not shared).
+ */
+int ral_filter_project(gdf_column *const *frame_columns, int32_t num_columns, const char *filter_query_part,
+                       const char *project_query_part, gdf_column *const *out_columns, int32_t num_out_columns,
+                       gdf_size_type *num_rows_out);
+
+/*
+ * materialize_column — src/ColumnManipulation.cuh:16-18 (ColumnManipulation.cu:137-150).
+ * output[i] = input[row_indices[i]] for row_indices[i] >= 0; valid bit i =
+ * valid bit row_indices[i] (0 for a negative index); output->null_count is
+ * recounted.  row_indices is an INT8/16/32/64 column.
+ */
+int ral_materialize_column(const gdf_column *input, gdf_column *output, const gdf_column *row_indices);
+
+/*
+ * add_expression_to_plan — src/LogicalFilter.h:26-42 (src/LogicalFilter.cpp:44-268).
+ * The register-program emitter: appends the ops of `expression` to the arrays.
+ * *num_operations is in/out (ops already present / after); arrays have room
+ * for `capacity` ops.  new_input_indices maps frame column -> dense input
+ * register (size num_frame_columns).
+ */
+int ral_add_expression_to_plan(const char *expression, column_index_type expression_position,
+                               column_index_type num_outputs, column_index_type num_inputs,
+                               const column_index_type *new_input_indices, int32_t num_frame_columns,
+                               column_index_type *left_inputs, column_index_type *right_inputs,
+                               column_index_type *outputs, int32_t *operators, int32_t *unary_operators,
+                               gdf_scalar *left_scalars, gdf_scalar *right_scalars, int32_t *num_operations,
+                               int32_t capacity);
+
+/* get_output_type_expression — src/CalciteExpressionParsing.cpp:420-481. */
+int ral_get_output_type_expression(const gdf_dtype *frame_dtypes, int32_t num_columns, const char *expression,
+                                   gdf_dtype *dtype_out);
+
+/* Library introspection (no reference counterpart): generated CUDA source of
+ * the kernel a program maps to, and an NVRTC-only compile check that needs
+ * no GPU.  Buffers receive a NUL-terminated string truncated to capacity. */
+int ral_debug_program_source(const gdf_dtype *input_dtypes, const int32_t *input_nullable, int32_t num_inputs,
+                             const gdf_dtype *output_dtypes, const int32_t *output_nullable, int32_t num_outputs,
+                             const column_index_type *left_inputs, const column_index_type *right_inputs,
+                             const column_index_type *outputs, int32_t num_operations,
+                             const column_index_type *final_output_positions, const int32_t *operators,
+                             const int32_t *unary_operators, const gdf_scalar *left_scalars,
+                             const gdf_scalar *right_scalars, int32_t compile, char *source_out,
+                             int64_t source_capacity, char *log_out, int64_t log_capacity);
+
+/* Kernels launched by this library since load (all entry points). */
+int64_t ral_kernel_launches(void);
+
+/* JIT counters: kernels compiled, disk-cache hits, memory-cache hits, total compile ms. */
+int ral_jit_stats(int64_t *compiles, int64_t *disk_hits, int64_t *memory_hits, double *compile_ms);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* RAL_C_H_ */

@@ -1,0 +1,81 @@
+"""Generated kernels compile with NVRTC for sm_103a (no GPU needed) and do not spill."""
+import re
+
+import pytest
+
+import ralgpu
+from ralgpu import dtypes as D
+from ralgpu import workloads as W
+
+
+def compile_spec(spec: W.ProgramSpec, nullable=True):
+    src, log = ralgpu.debug_program_source(
+        spec.input_dtypes, [1 if nullable else 0] * len(spec.input_dtypes), spec.output_dtypes,
+        [1 if nullable else 0] * len(spec.output_dtypes), spec.left, spec.right, spec.outputs, spec.final,
+        spec.ops, spec.uops, spec.lscalars, spec.rscalars, compile=True)
+    return src, log
+
+
+def spills(log: str) -> int:
+    total = 0
+    for m in re.finditer(r"(\d+) bytes spill stores", log):
+        total += int(m.group(1))
+    return total
+
+
+def test_fused_project_kernel_compiles():
+    src, log = compile_spec(W.fused_project_program())
+    assert "__ddiv_rn" in src and "ral_modi" in src and "floor(" in src
+    assert "ral_eval_" in src
+    assert spills(log) == 0, log
+    assert "registers" in log
+
+
+def test_fused_project_kernel_without_masks_compiles():
+    src, log = compile_spec(W.fused_project_program(), nullable=False)
+    assert "ral_vword" not in src
+    assert spills(log) == 0, log
+
+
+def _all_ops_program():
+    """Every binary and unary operator over int32 / int64 / float32 / float64 / date32 / date64 inputs."""
+    ins = [D.GDF_INT32, D.GDF_INT64, D.GDF_FLOAT32, D.GDF_FLOAT64, D.GDF_DATE32, D.GDF_DATE64]
+    n_in = len(ins)
+    L, R, O, B, U = [], [], [], [], []
+    outs = []
+    binops = [D.GDF_ADD, D.GDF_SUB, D.GDF_MUL, D.GDF_DIV, D.GDF_FLOOR_DIV, D.GDF_MOD, D.GDF_POW, D.GDF_EQUAL,
+              D.GDF_NOT_EQUAL, D.GDF_LESS, D.GDF_GREATER, D.GDF_LESS_EQUAL, D.GDF_GREATER_EQUAL, D.GDF_COALESCE]
+    unops = [D.BLZ_FLOOR, D.BLZ_CEIL, D.BLZ_SIN, D.BLZ_COS, D.BLZ_ASIN, D.BLZ_ACOS, D.BLZ_TAN, D.BLZ_COTAN,
+             D.BLZ_ATAN, D.BLZ_ABS, D.BLZ_NOT, D.BLZ_LN, D.BLZ_LOG, D.BLZ_YEAR, D.BLZ_MONTH, D.BLZ_DAY,
+             D.BLZ_HOUR, D.BLZ_MINUTE, D.BLZ_SECOND, D.BLZ_IS_NULL, D.BLZ_IS_NOT_NULL, D.BLZ_INVALID_UNARY]
+    n_out = len(binops) + len(unops)
+    k = 0
+    for i, op in enumerate(binops):
+        L.append(i % n_in if op != D.GDF_COALESCE else 1)
+        R.append((i + 3) % n_in)
+        O.append(n_in + k); B.append(op); U.append(D.BLZ_INVALID_UNARY); k += 1
+    for i, op in enumerate(unops):
+        L.append(i % n_in); R.append(-1); O.append(n_in + k); B.append(D.GDF_INVALID_BINARY); U.append(op); k += 1
+    out_types = [D.GDF_FLOAT64 if j % 2 else D.GDF_INT64 for j in range(n_out)]
+    J = (D.GDF_INT32, 0)
+    return W.ProgramSpec(ins, out_types, L, R, O, [n_in + j for j in range(n_out)], B, U, [J] * len(L),
+                         [J] * len(L))
+
+
+def test_every_operator_compiles():
+    src, log = compile_spec(_all_ops_program())
+    for fn in ("ral_powi", "pow(", "sin(", "log10(", "ral_year32", "ral_hour64", "ral_month64"):
+        assert fn in src, fn
+
+
+@pytest.mark.parametrize("nullable", [True, False])
+def test_plain_vm_filter_program_compiles(nullable):
+    from oracle import frontend as fe
+    res = fe.plan_evaluate_expression(4, fe.get_condition_expression(W.PLAIN_VM_FILTER))
+    plan, cols = res[1], res[2]
+    src, log = ralgpu.debug_program_source(
+        [W.PLAIN_VM_DTYPES[c] for c in cols], [1 if nullable else 0] * len(cols), [D.GDF_INT8], [1],
+        plan.left, plan.right, plan.outputs, plan.final_output_positions, plan.operators, plan.unary_operators,
+        [ralgpu.Scalar(s.dtype, s.value, s.is_valid) for s in plan.left_scalars],
+        [ralgpu.Scalar(s.dtype, s.value, s.is_valid) for s in plan.right_scalars], compile=True)
+    assert spills(log) == 0, log
