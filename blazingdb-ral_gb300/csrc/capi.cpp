@@ -245,7 +245,7 @@ int ral_materialize_column(const gdf_column* input, gdf_column* output, const gd
             if (int e = check_cuda(cudaMallocAsync((void**)&d, sizeof(unsigned long long), st), "cudaMallocAsync")) return e;
             cudaMemsetAsync(d, 0, sizeof(unsigned long long), st);
         }
-        if (int e = check_cuda(launch_gather(w, input->data, (const uint32_t*)input->valid, row_indices->data, iw, n,
+        if (int e = check_cuda(launch_gather(w, input->data, (const uint32_t*)input->valid, input->size, row_indices->data, iw, n,
                                              output->data, (uint32_t*)output->valid, d, st),
                                "gather"))
             return e;

@@ -120,7 +120,8 @@ int gather_all(gdf_column* const* frame, int ncols, const int32_t* idx, int64_t 
     unsigned long long* dc = (unsigned long long*)counts.p;
     for (int c = 0; c < ncols; c++) {
         if (int e = check_cuda(launch_gather(gdf_dtype_size(frame[c]->dtype), frame[c]->data,
-                                             (const uint32_t*)frame[c]->valid, idx, 4, n_out, outs[c]->data,
+                                             (const uint32_t*)frame[c]->valid, frame[c]->size, idx, 4, n_out,
+                                             outs[c]->data,
                                              (uint32_t*)outs[c]->valid, outs[c]->valid ? dc + c : nullptr, st),
                                "gather"))
             return e;

@@ -40,7 +40,7 @@ __global__ void count_valid_kernel(const ral_u32* __restrict__ valid, ral_i64 n,
 // One thread per output row; a warp builds each 32-row output validity word
 // with a ballot, so there is no read-modify-write of shared words.
 template <typename E, typename I>
-__global__ void gather_kernel(const E* __restrict__ in, const ral_u32* __restrict__ in_valid,
+__global__ void gather_kernel(const E* __restrict__ in, const ral_u32* __restrict__ in_valid, ral_i64 n_in,
                               const I* __restrict__ idx, ral_i64 n_out, E* __restrict__ out,
                               ral_u32* __restrict__ out_valid, unsigned long long* valid_count) {
     ral_u64 cnt = 0;
@@ -50,7 +50,7 @@ __global__ void gather_kernel(const E* __restrict__ in, const ral_u32* __restric
         bool bit = false;
         if (i < n_out) {
             const ral_i64 j = (ral_i64)idx[i];
-            if (j >= 0) {
+            if (j >= 0 && j < n_in) {
                 out[i] = in[j];
                 bit = in_valid ? ((__ldg(in_valid + (j >> 5)) >> (j & 31)) & 1u) : true;
             }
@@ -70,7 +70,8 @@ __global__ void gather_kernel(const E* __restrict__ in, const ral_u32* __restric
 }
 
 template <typename E>
-cudaError_t gather_by_index(const void* in, const uint32_t* in_valid, const void* idx, int idx_width, int64_t n_out,
+cudaError_t gather_by_index(const void* in, const uint32_t* in_valid, int64_t n_in, const void* idx, int idx_width,
+                            int64_t n_out,
                             void* out, uint32_t* out_valid, unsigned long long* valid_count, cudaStream_t st) {
     const int threads = 256;
     int64_t blocks = (n_out + threads - 1) / threads;
@@ -79,10 +80,10 @@ cudaError_t gather_by_index(const void* in, const uint32_t* in_valid, const void
     const E* i_ = (const E*)in;
     E* o_ = (E*)out;
     switch (idx_width) {
-    case 1: gather_kernel<E, int8_t><<<(int)blocks, threads, 0, st>>>(i_, in_valid, (const int8_t*)idx, n_out, o_, out_valid, valid_count); break;
-    case 2: gather_kernel<E, int16_t><<<(int)blocks, threads, 0, st>>>(i_, in_valid, (const int16_t*)idx, n_out, o_, out_valid, valid_count); break;
-    case 4: gather_kernel<E, int32_t><<<(int)blocks, threads, 0, st>>>(i_, in_valid, (const int32_t*)idx, n_out, o_, out_valid, valid_count); break;
-    case 8: gather_kernel<E, int64_t><<<(int)blocks, threads, 0, st>>>(i_, in_valid, (const int64_t*)idx, n_out, o_, out_valid, valid_count); break;
+    case 1: gather_kernel<E, int8_t><<<(int)blocks, threads, 0, st>>>(i_, in_valid, n_in, (const int8_t*)idx, n_out, o_, out_valid, valid_count); break;
+    case 2: gather_kernel<E, int16_t><<<(int)blocks, threads, 0, st>>>(i_, in_valid, n_in, (const int16_t*)idx, n_out, o_, out_valid, valid_count); break;
+    case 4: gather_kernel<E, int32_t><<<(int)blocks, threads, 0, st>>>(i_, in_valid, n_in, (const int32_t*)idx, n_out, o_, out_valid, valid_count); break;
+    case 8: gather_kernel<E, int64_t><<<(int)blocks, threads, 0, st>>>(i_, in_valid, n_in, (const int64_t*)idx, n_out, o_, out_valid, valid_count); break;
     default: return cudaErrorInvalidValue;
     }
     return cudaGetLastError();
@@ -223,15 +224,15 @@ cudaError_t launch_compact_stencil(const int8_t* stencil, const uint32_t* stenci
     return cudaGetLastError();
 }
 
-cudaError_t launch_gather(int width, const void* in, const uint32_t* in_valid, const void* idx, int idx_width,
-                          int64_t n_out, void* out, uint32_t* out_valid, unsigned long long* valid_count,
+cudaError_t launch_gather(int width, const void* in, const uint32_t* in_valid, int64_t n_in, const void* idx,
+                          int idx_width, int64_t n_out, void* out, uint32_t* out_valid, unsigned long long* valid_count,
                           cudaStream_t st) {
     if (n_out <= 0) return cudaSuccess;
     switch (width) {
-    case 1: return gather_by_index<int8_t>(in, in_valid, idx, idx_width, n_out, out, out_valid, valid_count, st);
-    case 2: return gather_by_index<int16_t>(in, in_valid, idx, idx_width, n_out, out, out_valid, valid_count, st);
-    case 4: return gather_by_index<int32_t>(in, in_valid, idx, idx_width, n_out, out, out_valid, valid_count, st);
-    case 8: return gather_by_index<int64_t>(in, in_valid, idx, idx_width, n_out, out, out_valid, valid_count, st);
+    case 1: return gather_by_index<int8_t>(in, in_valid, n_in, idx, idx_width, n_out, out, out_valid, valid_count, st);
+    case 2: return gather_by_index<int16_t>(in, in_valid, n_in, idx, idx_width, n_out, out, out_valid, valid_count, st);
+    case 4: return gather_by_index<int32_t>(in, in_valid, n_in, idx, idx_width, n_out, out, out_valid, valid_count, st);
+    case 8: return gather_by_index<int64_t>(in, in_valid, n_in, idx, idx_width, n_out, out, out_valid, valid_count, st);
     default: return cudaErrorInvalidValue;
     }
 }

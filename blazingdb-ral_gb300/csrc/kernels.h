@@ -10,12 +10,13 @@ namespace ral {
 // Adds the number of set bits among the first n bits of `valid` to *out.
 cudaError_t launch_count_valid(const uint32_t* valid, int64_t n, unsigned long long* out, cudaStream_t st);
 
-// out[i] = in[idx[i]] for idx[i] >= 0 (elements of `width` bytes, indices of
-// `idx_width` bytes); out_valid (optional) gets bit i = in bit idx[i] (0 for
-// a negative index, 1 when in_valid is null); valid_count (optional) gets the
-// number of set output bits added.
-cudaError_t launch_gather(int width, const void* in, const uint32_t* in_valid, const void* idx, int idx_width,
-                          int64_t n_out, void* out, uint32_t* out_valid, unsigned long long* valid_count,
+// out[i] = in[idx[i]] for 0 <= idx[i] < n_in (elements of `width` bytes,
+// indices of `idx_width` bytes; other indices leave out[i] untouched);
+// out_valid (optional) gets bit i = in bit idx[i] (0 for an index outside
+// [0, n_in), 1 when in_valid is null); valid_count (optional) gets the number
+// of set output bits added.
+cudaError_t launch_gather(int width, const void* in, const uint32_t* in_valid, int64_t n_in, const void* idx,
+                          int idx_width, int64_t n_out, void* out, uint32_t* out_valid, unsigned long long* valid_count,
                           cudaStream_t st);
 
 }  // namespace ral
