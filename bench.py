@@ -52,54 +52,73 @@ def load_traffic(key):
 
 
 class ClockSampler:
-    """nvidia-smi clocks and throttle reasons during the timed region."""
+    """nvidia-smi clocks and throttle reasons, sampled every 20 ms; only samples that arrive
+    inside the timed window [mark_start, mark_end] are kept."""
     FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
               "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
               "clocks_event_reasons.sw_power_cap")
+    NAMES = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
 
     def __init__(self, index: int):
         self.index = index
         self.proc = None
         self.lines = []
+        self.t0 = self.t1 = None
 
     def start(self):
         try:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}",
-                                          "--format=csv,noheader,nounits", "-lms", "100"],
-                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+                                          "--format=csv,noheader,nounits", "-lms", "20"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True, bufsize=1)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
+            time.sleep(1.0)   # let nvidia-smi start emitting before the timed region
         except Exception:
             self.proc = None
 
     def _read(self):
         for line in self.proc.stdout:
-            self.lines.append(line.strip())
+            self.lines.append((time.monotonic(), line.strip()))
+
+    def mark_start(self):
+        self.t0 = time.monotonic()
+
+    def mark_end(self):
+        self.t1 = time.monotonic()
 
     def stop(self):
         if self.proc is None:
-            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"], "samples": 0}
+        time.sleep(0.1)
         self.proc.terminate()
         try:
             self.proc.wait(timeout=5)
         except Exception:
             self.proc.kill()
-        sm, smax, reasons = [], [], set()
-        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for ln in self.lines:
+        inside = [ln for t, ln in self.lines if self.t0 is not None and self.t0 <= t <= self.t1 + 0.05]
+        window = "timed region"
+        if not inside:
+            # a very short timed region: take the samples nearest to it
+            near = sorted(self.lines, key=lambda x: abs(x[0] - (self.t0 or 0)))[:3]
+            inside = [ln for _, ln in near]
+            window = "nearest samples (timed region shorter than the sampling period)"
+        sm, smax, power, reasons = [], [], [], set()
+        for ln in inside:
             parts = [p.strip() for p in ln.split(",")]
             if len(parts) < 8:
                 continue
             try:
                 sm.append(float(parts[0]))
                 smax.append(float(parts[1]))
+                power.append(float(parts[2]))
             except ValueError:
                 continue
-            for nm, v in zip(names, parts[4:8]):
+            for nm, v in zip(self.NAMES, parts[4:8]):
                 if v.lower().startswith("active"):
                     reasons.add(nm)
         return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
-                "reasons": sorted(reasons), "samples": len(sm)}
+                "reasons": sorted(reasons), "samples": len(sm), "window": window,
+                "power_w_max": max(power) if power else None}
 
 
 def dist_setup(args):
@@ -262,17 +281,18 @@ def run_ours(args):
         raise SystemExit("workload not built into bench.py yet: " + args.workload)
     ctx = fused_project_setup(n, device)
     stream = torch.cuda.current_stream()
+    sampler = ClockSampler(local)
+    sampler.start()
     for _ in range(args.warmup):
         ctx["step"](stream)
     torch.cuda.synchronize()
     barrier(world)
-    sampler = ClockSampler(local)
-    sampler.start()
     launches0 = R.kernel_launches()
     events = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
     torch.cuda.synchronize()
     t_start = torch.cuda.Event(enable_timing=True)
     t_end = torch.cuda.Event(enable_timing=True)
+    sampler.mark_start()
     t_start.record()
     for s, e in events:
         s.record()
@@ -280,6 +300,7 @@ def run_ours(args):
         e.record()
     t_end.record()
     torch.cuda.synchronize()
+    sampler.mark_end()
     launches = R.kernel_launches() - launches0
     clocks = sampler.stop()
     barrier(world)
@@ -344,7 +365,7 @@ def run_reference(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=100)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="fused_project", choices=["fused_project", "plain_vm", "filter_gather"])
