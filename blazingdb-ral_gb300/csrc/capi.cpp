@@ -261,6 +261,39 @@ int ral_materialize_column(const gdf_column* input, gdf_column* output, const gd
     });
 }
 
+int ral_apply_boolean_mask(const gdf_column* stencil, gdf_column* out_indices, gdf_size_type* num_rows_out) {
+    return guarded([&] {
+        if (!stencil || !out_indices || !num_rows_out) return set_error(kInvalidArgument, "null argument");
+        if (gdf_dtype_size(stencil->dtype) != 1) return set_error(kInvalidArgument, "stencil must be INT8 or BOOL8");
+        if (out_indices->dtype != GDF_INT32) return set_error(kInvalidArgument, "out_indices must be INT32");
+        if (stencil->valid && ((uintptr_t)stencil->valid & 3)) return set_error(kInvalidArgument, "mask must be 4-byte aligned");
+        const int64_t n = stencil->size;
+        if (n == 0) {
+            out_indices->size = 0;
+            *num_rows_out = 0;
+            return (int)kSuccess;
+        }
+        if (!stencil->data || !out_indices->data) return set_error(kInvalidArgument, "column without data");
+        cudaStream_t st = cudaStreamPerThread;
+        const int64_t words = compact_scratch_words(n);
+        unsigned long long* scratch = nullptr;
+        if (int e = check_cuda(cudaMallocAsync((void**)&scratch, (size_t)words * 8, st), "cudaMallocAsync")) return e;
+        cudaMemsetAsync(scratch, 0, (size_t)words * 8, st);
+        int rc = check_cuda(launch_compact_stencil((const int8_t*)stencil->data, (const uint32_t*)stencil->valid, n,
+                                                   (int32_t*)out_indices->data, scratch, st),
+                            "compaction");
+        unsigned long long h[3] = {0, 0, 0};
+        if (rc == kSuccess) cudaMemcpyAsync(h, scratch, sizeof h, cudaMemcpyDeviceToHost, st);
+        cudaFreeAsync(scratch, st);
+        if (int e = check_cuda(cudaStreamSynchronize(st), "apply_boolean_mask")) return e;
+        if (rc) return rc;
+        if (h[1]) return set_error(kTimeout, "compaction look-back wait gave up");
+        out_indices->size = (gdf_size_type)h[2];
+        *num_rows_out = (gdf_size_type)h[2];
+        return (int)kSuccess;
+    });
+}
+
 int ral_process_filter(gdf_column* const* frame, int32_t num_columns, const char* query_part,
                        gdf_column* const* out_columns, gdf_size_type* num_rows_out) {
     return guarded([&] {

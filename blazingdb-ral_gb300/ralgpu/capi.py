@@ -35,6 +35,7 @@ _SIGS = {
     "ral_execute_project_plan": (C.c_int, [COLPP, C.c_int32, C.c_char_p, COLPP, C.c_int32]),
     "ral_filter_project": (C.c_int, [COLPP, C.c_int32, C.c_char_p, C.c_char_p, COLPP, C.c_int32,
                                      C.POINTER(C.c_int32)]),
+    "ral_apply_boolean_mask": (C.c_int, [C.POINTER(GdfColumn), C.POINTER(GdfColumn), C.POINTER(C.c_int32)]),
     "ral_materialize_column": (C.c_int, [C.POINTER(GdfColumn), C.POINTER(GdfColumn), C.POINTER(GdfColumn)]),
     "ral_add_expression_to_plan": (C.c_int, [C.c_char_p, C.c_int16, C.c_int16, C.c_int16, I16P, C.c_int32,
                                              I16P, I16P, I16P, I32P, I32P, SCP, SCP, I32P, C.c_int32]),
@@ -267,6 +268,16 @@ def materialize_column(input_column: Column, row_indices: Column, with_valid: Op
     out = Column.empty(input_column.dtype, n, with_valid=wv)
     ic, oc, rc = input_column.to_c(), out.to_c(), row_indices.to_c()
     _check(lib().ral_materialize_column(C.byref(ic), C.byref(oc), C.byref(rc)))
+    out.sync_from_c(oc)
+    return out
+
+
+def apply_boolean_mask(stencil: Column) -> Column:
+    """Indices (INT32 column) of the rows whose stencil is valid and nonzero, in row order."""
+    out = Column.empty(D.GDF_INT32, stencil.size, with_valid=False)
+    sc, oc = stencil.to_c(), out.to_c()
+    n = C.c_int32(0)
+    _check(lib().ral_apply_boolean_mask(C.byref(sc), C.byref(oc), C.byref(n)))
     out.sync_from_c(oc)
     return out
 

@@ -132,6 +132,18 @@ int ral_filter_project(gdf_column *const *frame_columns, int32_t num_columns, co
 int ral_materialize_column(const gdf_column *input, gdf_column *output, const gdf_column *row_indices);
 
 /*
+ * apply_boolean_mask over the row-index column — src/CalciteInterpreter.cpp:531-543
+ * (gdf_sequence iota + cudf::apply_boolean_mask).  Writes, in row order, the
+ * indices of the rows whose stencil byte is nonzero and whose stencil validity
+ * bit is set (stencil->valid may be NULL) into out_indices (INT32, capacity
+ * stencil->size rows) and sets out_indices->size and *num_rows_out.  stencil is
+ * an INT8 or BOOL8 column.  Single-pass compaction (ballot/popc, block scan,
+ * decoupled look-back); the look-back state lives in scratch memory this call
+ * allocates and frees on the stream.
+ */
+int ral_apply_boolean_mask(const gdf_column *stencil, gdf_column *out_indices, gdf_size_type *num_rows_out);
+
+/*
  * add_expression_to_plan — src/LogicalFilter.h:26-42 (src/LogicalFilter.cpp:44-268).
  * The register-program emitter: appends the ops of `expression` to the arrays.
  * *num_operations is in/out (ops already present / after); arrays have room

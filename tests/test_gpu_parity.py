@@ -415,3 +415,16 @@ def test_rejected_programs_raise():
     assert ei.value.code == 2
     with pytest.raises(R.RalError):
         R.evaluate_expression([c], "LIKE($0, 'x')", out)
+
+
+@pytest.mark.parametrize("n", [1, 31, 4095, 4096, 4097, 1_000_003])
+def test_apply_boolean_mask(n):
+    rng = np.random.default_rng(n)
+    st = rng.integers(-3, 4, n).astype(np.int8)
+    v = rng.random(n) < 0.9
+    for valid in (v, None):
+        col = R.Column.from_numpy(st, D.GDF_INT8, valid)
+        got = R.apply_boolean_mask(col)
+        exp = O.apply_boolean_mask(O.make_column(st, D.GDF_INT8, valid))
+        assert got.size == len(exp)
+        np.testing.assert_array_equal(got.to_numpy(), exp)
