@@ -21,7 +21,7 @@ CUDA = os.environ.get("CUDA_HOME", "/usr/local/cuda")
 NVCC = os.path.join(CUDA, "bin", "nvcc")
 
 CPP = ["program.cpp", "frontend.cpp", "codegen.cpp", "jit.cpp", "engine.cpp", "filter.cpp", "capi.cpp"]
-CU = ["kernels.cu"]
+CU = ["kernels.cu", "noalloc.cu"]
 HEADERS = ["program.h", "frontend.h", "codegen.h", "jit.h", "engine.h", "filter.h", "kernels.h", "device_rt.cuh"]
 INCLUDES = [f"-I{os.path.join(ROOT, 'include')}", f"-I{CSRC}", f"-I{os.path.join(CUDA, 'include')}"]
 GENCODE = ["-gencode", "arch=compute_103a,code=sm_103a"]

@@ -144,6 +144,22 @@ int ral_materialize_column(const gdf_column *input, gdf_column *output, const gd
 int ral_apply_boolean_mask(const gdf_column *stencil, gdf_column *out_indices, gdf_size_type *num_rows_out);
 
 /*
+ * ral_apply_boolean_mask_noalloc — no counterpart in the reference.
+ * The same result as ral_apply_boolean_mask, for callers that cannot allocate
+ * device memory (an engine whose pool already owns the whole GPU, or a
+ * latency-critical path that must not enter the driver's allocator): the
+ * scratch block comes from a fixed 256 KiB array compiled into the library,
+ * which every GPU that loads the library holds until the process exits.
+ * Limit: stencil->size <= RAL_NOALLOC_MAX_ROWS; larger stencils are rejected
+ * with RAL_ERROR_INVALID_ARGUMENT.  The first call on a device looks up the
+ * array's device address (cudaGetSymbolAddress); make that first call before
+ * any stream capture.  All calls share the array: calls whose GPU work
+ * overlaps (from several threads or streams at once) race on it.
+ */
+#define RAL_NOALLOC_MAX_ROWS ((int64_t)(256 * 1024 / 8 - 3) * 4096)
+int ral_apply_boolean_mask_noalloc(const gdf_column *stencil, gdf_column *out_indices, gdf_size_type *num_rows_out);
+
+/*
  * add_expression_to_plan — src/LogicalFilter.h:26-42 (src/LogicalFilter.cpp:44-268).
  * The register-program emitter: appends the ops of `expression` to the arrays.
  * *num_operations is in/out (ops already present / after); arrays have room
