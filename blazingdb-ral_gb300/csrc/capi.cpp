@@ -364,6 +364,27 @@ int ral_debug_program_source(const gdf_dtype* input_dtypes, const int32_t* input
     });
 }
 
+int ral_debug_filter_source(const gdf_dtype* frame_dtypes, const int32_t* frame_nullable, int32_t num_columns,
+                            const char* filter_query_part, const char* project_query_part, int32_t compile,
+                            char* source_out, int64_t source_capacity, char* log_out, int64_t log_capacity) {
+    return guarded([&] {
+        std::vector<gdf_column> cols(num_columns);
+        std::vector<gdf_column*> ptrs(num_columns);
+        for (int c = 0; c < num_columns; c++) {
+            cols[c] = gdf_column{};
+            cols[c].dtype = frame_dtypes[c];
+            cols[c].valid = frame_nullable[c] ? (gdf_valid_type*)(uintptr_t)64 : nullptr;
+            cols[c].null_count = frame_nullable[c] ? 1 : 0;
+            ptrs[c] = &cols[c];
+        }
+        std::string src, log;
+        int rc = debug_filter_source(ptrs.data(), num_columns, filter_query_part, project_query_part, compile != 0, src, log);
+        copy_out(src, source_out, source_capacity);
+        copy_out(log, log_out, log_capacity);
+        return rc;
+    });
+}
+
 int64_t ral_kernel_launches(void) { return (int64_t)launch_count(); }
 
 int ral_jit_stats(int64_t* compiles, int64_t* disk_hits, int64_t* memory_hits, double* compile_ms) {

@@ -447,9 +447,390 @@ GeneratedKernel generate_eval_kernel(const Program& p, const Shape& s) {
     return gk;
 }
 
+int filter_max_width(const FilterSpec& f) {
+    int w = 1;
+    if (f.clone_stencil) w = std::max(w, gdf_dtype_size(f.frame_dtypes[f.clone_column]));
+    if (f.predicate) {
+        auto ref = f.predicate->inputs_referenced();
+        for (size_t c = 0; c < f.predicate_cols.size(); c++)
+            if (ref[c]) w = std::max(w, gdf_dtype_size(f.frame_dtypes[f.predicate_cols[c]]));
+    }
+    if (f.project) {
+        auto ref = f.project->inputs_referenced();
+        for (size_t c = 0; c < f.project_cols.size(); c++)
+            if (ref[c]) w = std::max(w, gdf_dtype_size(f.frame_dtypes[f.project_cols[c]]));
+    }
+    for (const FilterOutput& o : f.outputs) w = std::max(w, gdf_dtype_size(o.dtype));
+    return w;
+}
+
 GeneratedKernel generate_filter_kernel(const FilterSpec& f, const Shape& s) {
-    (void)f; (void)s;
-    throw std::runtime_error("filter kernel generation not built yet");
+    if (s.G * s.J > 30) throw std::runtime_error("filter kernel shape: G*J must be at most 30");
+    GeneratedKernel gk;
+    gk.shape = s;
+    ParamLayout& L = gk.layout;
+    const int NF = f.n_frame;
+    const int NO = (int)f.outputs.size();
+    int slot = 0;
+    L.n_rows = slot++;
+    L.in_data = slot; slot += NF;
+    L.in_valid = slot; slot += NF;
+    L.out_data = slot; slot += NO;
+    L.out_valid = slot; slot += NO;
+    L.scratch = slot++;
+    ParamLayout PL, QL;  // scalar slots of the predicate and projection programs
+    if (f.predicate) {
+        PL.lscalar_slot.assign(f.predicate->ops.size(), -1);
+        PL.rscalar_slot.assign(f.predicate->ops.size(), -1);
+        for (size_t k = 0; k < f.predicate->ops.size(); k++) {
+            if (f.predicate->ops[k].left == SCALAR_INDEX) PL.lscalar_slot[k] = slot++;
+            if (!f.predicate->ops[k].unary && f.predicate->ops[k].right == SCALAR_INDEX) PL.rscalar_slot[k] = slot++;
+        }
+    }
+    if (f.project) {
+        QL.lscalar_slot.assign(f.project->ops.size(), -1);
+        QL.rscalar_slot.assign(f.project->ops.size(), -1);
+        for (size_t k = 0; k < f.project->ops.size(); k++) {
+            if (f.project->ops[k].left == SCALAR_INDEX) QL.lscalar_slot[k] = slot++;
+            if (!f.project->ops[k].unary && f.project->ops[k].right == SCALAR_INDEX) QL.rscalar_slot[k] = slot++;
+        }
+    }
+    L.lscalar_slot = PL.lscalar_slot;
+    L.rscalar_slot = PL.rscalar_slot;
+    gk.layout_project_lscalar = QL.lscalar_slot;
+    gk.layout_project_rscalar = QL.rscalar_slot;
+    L.total = slot;
+
+    std::vector<int> vouts;  // outputs with a mask
+    for (int k = 0; k < NO; k++)
+        if (f.outputs[k].has_valid) vouts.push_back(k);
+    const int NVO = (int)vouts.size();
+    bool any_proj_valid = false;
+    for (int k : vouts) any_proj_valid |= f.outputs[k].from_project;
+
+    // which frame columns the kernel dereferences
+    std::vector<bool> f_data(NF, false), f_valid(NF, false);
+    auto pred_ref = f.predicate ? f.predicate->inputs_referenced() : std::vector<bool>();
+    auto pred_raw = f.predicate ? f.predicate->inputs_raw_valid() : std::vector<bool>();
+    auto proj_ref = f.project ? f.project->inputs_referenced() : std::vector<bool>();
+    auto proj_raw = f.project ? f.project->inputs_raw_valid() : std::vector<bool>();
+    if (f.clone_stencil) {
+        f_data[f.clone_column] = true;
+        f_valid[f.clone_column] = f.frame_has_valid[f.clone_column];
+    }
+    // masks the kernel body reads directly (the validity-word functions read theirs through P)
+    for (size_t c = 0; c < f.predicate_cols.size(); c++) {
+        if (pred_ref[c]) f_data[f.predicate_cols[c]] = true;
+        if (pred_raw[c] && f.frame_has_valid[f.predicate_cols[c]]) f_valid[f.predicate_cols[c]] = true;
+    }
+    for (size_t c = 0; c < f.project_cols.size(); c++) {
+        if (proj_ref[c]) f_data[f.project_cols[c]] = true;
+        if (proj_raw[c] && f.frame_has_valid[f.project_cols[c]]) f_valid[f.project_cols[c]] = true;
+    }
+    for (const FilterOutput& o : f.outputs) {
+        if (o.from_project) continue;
+        f_data[o.index] = true;
+        if (o.has_valid) f_valid[o.index] = true;
+    }
+
+    std::ostringstream key;
+    key << "filter|n" << NF << "|";
+    for (int c = 0; c < NF; c++) key << (int)f.frame_dtypes[c] << (f.frame_has_valid[c] ? "v" : "") << ",";
+    key << "|clone" << (f.clone_stencil ? f.clone_column : -1) << "|";
+    if (f.predicate) {
+        key << "P" << f.predicate->structure_key() << "@";
+        for (int c : f.predicate_cols) key << c << ",";
+    }
+    if (f.project) {
+        key << "|Q" << f.project->structure_key() << "@";
+        for (int c : f.project_cols) key << c << ",";
+    }
+    key << "|O";
+    for (const FilterOutput& o : f.outputs) key << (o.from_project ? "p" : "g") << o.index << ":" << (int)o.dtype << (o.has_valid ? "v" : "") << ",";
+    key << "|G" << s.G << "J" << s.J << "T" << s.threads;
+    char hex[32];
+    snprintf(hex, sizeof hex, "%016llx", (unsigned long long)fnv1a(key.str()));
+    gk.name = std::string("ral_filter_") + hex;
+
+    std::ostringstream os;
+    os << "// generated: " << key.str() << "\n";
+    os << "#define RAL_G " << s.G << "\n#define RAL_J " << s.J << "\n#define RAL_THREADS " << s.threads << "\n";
+    os << "#define RAL_WARPS (RAL_THREADS / 32)\n";
+    os << "struct RalParams { ral_u64 s[" << L.total << "]; };\n\n";
+    auto fdata = [&](int c) { return "f" + std::to_string(c); };
+    auto fvalid = [&](int c) { return "fv" + std::to_string(c); };
+
+    std::vector<Kind> pred_kind, proj_kind;
+    if (f.predicate) {
+        emit_row_function(os, *f.predicate, PL, "ral_pred_row");
+        pred_kind = final_kinds(*f.predicate, PL);
+        os << "RAL_FI ral_u32 ral_pred_vword(const RalParams& P, const ral_i64 w) {\n";
+        ValidEmitter ve(*f.predicate);
+        ve.emit(os, "    ", [&](int c) {
+            return "__ldg(((const ral_u32*)P.s[" + std::to_string(L.in_valid + f.predicate_cols[c]) + "]) + w)";
+        });
+        os << "    return " << ve.name[f.predicate->final_pos[0]] << ";\n}\n";
+    }
+    std::vector<int> proj_vouts;  // projection outputs with a mask, in output order
+    if (f.project) {
+        emit_row_function(os, *f.project, QL, "ral_proj_row");
+        proj_kind = final_kinds(*f.project, QL);
+        for (int k : vouts)
+            if (f.outputs[k].from_project) proj_vouts.push_back(f.outputs[k].index);
+        if (!proj_vouts.empty()) {
+            os << "RAL_FI void ral_proj_vword(const RalParams& P, const ral_i64 w, ral_u32* vo) {\n";
+            ValidEmitter ve(*f.project);
+            ve.emit(os, "    ", [&](int c) {
+                return "__ldg(((const ral_u32*)P.s[" + std::to_string(L.in_valid + f.project_cols[c]) + "]) + w)";
+            });
+            for (size_t i = 0; i < proj_vouts.size(); i++)
+                os << "    vo[" << i << "] = " << ve.name[f.project->final_pos[proj_vouts[i]]] << ";\n";
+            os << "}\n";
+        }
+    }
+
+    os << "\nextern \"C\" __global__ void __launch_bounds__(RAL_THREADS) " << gk.name
+       << "(const __grid_constant__ RalParams P) {\n";
+    os << "    __shared__ ral_u32 s_tile;\n    __shared__ ral_u32 s_wcnt[RAL_WARPS];\n    __shared__ ral_u64 s_prefix;\n";
+    if (NVO) os << "    __shared__ ral_u32 s_vb[" << NVO << "][RAL_WARPS][RAL_G * RAL_J + 2];\n";
+    os << "    const ral_i64 n = (ral_i64)P.s[" << L.n_rows << "];\n";
+    os << "    ral_u64* const scratch = (ral_u64*)P.s[" << L.scratch << "];\n";
+    os << "    ral_u64* const status = scratch + " << filter_scratch_header(NO) << ";\n";
+    for (int c = 0; c < NF; c++) {
+        if (f_data[c])
+            os << "    const " << element_ctype(f.frame_dtypes[c]) << "* __restrict__ " << fdata(c) << " = (const "
+               << element_ctype(f.frame_dtypes[c]) << "*)P.s[" << L.in_data + c << "];\n";
+        if (f_valid[c])
+            os << "    const ral_u32* __restrict__ " << fvalid(c) << " = (const ral_u32*)P.s[" << L.in_valid + c << "];\n";
+    }
+    for (int k = 0; k < NO; k++) {
+        os << "    " << element_ctype(f.outputs[k].dtype) << "* __restrict__ o" << k << " = ("
+           << element_ctype(f.outputs[k].dtype) << "*)P.s[" << L.out_data + k << "];\n";
+        if (f.outputs[k].has_valid)
+            os << "    ral_u32* __restrict__ ov" << k << " = (ral_u32*)P.s[" << L.out_valid + k << "];\n";
+    }
+    os << "    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;\n";
+    os << "    const ral_i64 WT = 32 * RAL_G * RAL_J;\n    const ral_i64 BT = WT * RAL_WARPS;\n";
+    os << "    const ral_i64 ntiles = (n + BT - 1) / BT;\n";
+    if (NVO) os << "    ral_u64 vcnt[" << NVO << "];\n    for (int i = 0; i < " << NVO << "; ++i) vcnt[i] = 0;\n";
+    os << "    for (;;) {\n";
+    os << "        if (threadIdx.x == 0) s_tile = atomicAdd((unsigned int*)scratch, 1u);\n";
+    os << "        __syncthreads();\n";
+    os << "        const ral_i64 tile = s_tile;\n";
+    os << "        if (tile >= ntiles) break;\n";
+    os << "        const ral_i64 wbase = tile * BT + (ral_i64)warp * WT;\n";
+    os << "        const bool full = wbase + WT <= n;\n";
+
+    // loads of a frame column for the G rows at r (vector in full warp tiles, guarded otherwise)
+    auto load = [&](std::ostream& o, const std::string& ind, int c, const std::string& arr) {
+        const char* et = element_ctype(f.frame_dtypes[c]);
+        o << ind << et << " " << arr << "[RAL_G];\n";
+        o << ind << "if (full) ral_ldg<" << et << ", RAL_G>(" << fdata(c) << ", r, " << arr << ");\n";
+        o << ind << "else {\n" << ind << "#pragma unroll\n" << ind << "    for (int g = 0; g < RAL_G; ++g) " << arr
+          << "[g] = (r + g < n) ? " << fdata(c) << "[r + g] : (" << et << ")0;\n" << ind << "}\n";
+    };
+    auto raw_word = [&](int c) {
+        if (!f.frame_has_valid[c]) return std::string("0xffffffffu");
+        return "((r < n) ? __ldg(" + fvalid(c) + " + (r >> 5)) : 0xffffffffu)";
+    };
+
+    // ---- predicate: keep bits per slice
+    os << "        ral_u32 sw = 0;\n";
+    os << "        if (lane < RAL_G * RAL_J) {\n";
+    os << "            const ral_i64 w = (wbase >> 5) + lane;\n";
+    if (f.clone_stencil) {
+        if (f.frame_has_valid[f.clone_column]) os << "            if ((w << 5) < n) sw = __ldg(" << fvalid(f.clone_column) << " + w);\n";
+        else os << "            if ((w << 5) < n) sw = 0xffffffffu;\n";
+    } else {
+        os << "            if ((w << 5) < n) sw = ral_pred_vword(P, w);\n";
+    }
+    os << "        }\n";
+    os << "        ral_u32 kb[RAL_J];\n";
+    os << "#pragma unroll\n        for (int j = 0; j < RAL_J; ++j) {\n";
+    os << "            const ral_i64 r = wbase + (ral_i64)j * 32 * RAL_G + lane * RAL_G;\n";
+    if (f.clone_stencil) {
+        load(os, "            ", f.clone_column, "sa");
+    } else {
+        for (size_t c = 0; c < f.predicate_cols.size(); c++)
+            if (pred_ref[c]) load(os, "            ", f.predicate_cols[c], "pa" + std::to_string(c));
+        for (size_t c = 0; c < f.predicate_cols.size(); c++)
+            if (pred_raw[c]) os << "            const ral_u32 rw" << c << " = " << raw_word(f.predicate_cols[c]) << ";\n";
+    }
+    os << "            ral_u32 bits = 0;\n";
+    os << "#pragma unroll\n            for (int g = 0; g < RAL_G; ++g) {\n";
+    if (f.clone_stencil) {
+        os << "                const signed char sv = (signed char)sa[g];\n";
+    } else {
+        os << "                " << kind_ctype(pred_kind[0]) << " y0;\n";
+        os << "                ral_pred_row(P";
+        for (size_t c = 0; c < f.predicate_cols.size(); c++)
+            if (pred_ref[c]) os << ", " << widen("pa" + std::to_string(c) + "[g]", f.frame_dtypes[f.predicate_cols[c]]);
+        for (size_t c = 0; c < f.predicate_cols.size(); c++)
+            if (pred_raw[c]) os << ", (rw" << c << " >> ((int)(r & 31) + g)) & 1u";
+        os << ", y0);\n";
+        os << "                const signed char sv = " << narrow("y0", pred_kind[0], GDF_INT8) << ";\n";
+    }
+    os << "                bits |= (sv != 0 ? 1u : 0u) << g;\n";
+    os << "            }\n";
+    os << "            const ral_u32 word = __shfl_sync(0xffffffffu, sw, (j * 32 * RAL_G + lane * RAL_G) >> 5);\n";
+    os << "            bits &= (word >> (int)(r & 31)) & ((1u << RAL_G) - 1u);\n";
+    os << "            if (!full) {\n#pragma unroll\n                for (int g = 0; g < RAL_G; ++g) if (r + g >= n) bits &= ~(1u << g);\n            }\n";
+    os << "            kb[j] = bits;\n";
+    os << "        }\n";
+
+    // ---- ranks within the warp tile, block scan, look-back
+    os << "        ral_u32 lex[RAL_J], sex[RAL_J];\n        ral_u32 wtot = 0;\n";
+    os << "#pragma unroll\n        for (int j = 0; j < RAL_J; ++j) {\n";
+    os << "            const ral_u32 c = __popc(kb[j]);\n            ral_u32 inc = c;\n";
+    os << "            for (int off = 1; off < 32; off <<= 1) {\n";
+    os << "                const ral_u32 t = __shfl_up_sync(0xffffffffu, inc, off);\n";
+    os << "                if (lane >= off) inc += t;\n            }\n";
+    os << "            lex[j] = inc - c;\n            sex[j] = wtot;\n";
+    os << "            wtot += __shfl_sync(0xffffffffu, inc, 31);\n        }\n";
+    os << "        if (lane == 0) s_wcnt[warp] = wtot;\n";
+    os << "        __syncthreads();\n";
+    os << "        if (warp == 0) {\n";
+    os << "            const ral_u32 v = lane < RAL_WARPS ? s_wcnt[lane] : 0u;\n            ral_u32 inc = v;\n";
+    os << "            for (int off = 1; off < RAL_WARPS; off <<= 1) {\n";
+    os << "                const ral_u32 t = __shfl_up_sync(0xffffffffu, inc, off);\n";
+    os << "                if (lane >= off) inc += t;\n            }\n";
+    os << "            const ral_u32 total = __shfl_sync(0xffffffffu, inc, RAL_WARPS - 1);\n";
+    os << "            const ral_u64 excl = ral_lookback(status, tile, total, scratch + 1);\n";
+    os << "            if (lane < RAL_WARPS) s_wcnt[lane] = inc - v;\n";
+    os << "            if (lane == 0) {\n                s_prefix = excl;\n";
+    os << "                if (tile == ntiles - 1) scratch[2] = excl + total;\n            }\n";
+    os << "        }\n";
+    os << "        __syncthreads();\n";
+    os << "        const ral_u64 wpos = s_prefix + s_wcnt[warp];\n";
+
+    // ---- data of every output
+    bool any_gather = false, any_proj = false;
+    for (const FilterOutput& o : f.outputs) (o.from_project ? any_proj : any_gather) = true;
+    if (any_gather) {
+        os << "#pragma unroll\n        for (int j = 0; j < RAL_J; ++j) {\n";
+        os << "            if (kb[j] == 0u) continue;\n";
+        os << "            const ral_i64 r = wbase + (ral_i64)j * 32 * RAL_G + lane * RAL_G;\n";
+        for (int k = 0; k < NO; k++) {
+            if (f.outputs[k].from_project) continue;
+            const int c = f.outputs[k].index;
+            os << "            {\n";
+            load(os, "                ", c, "ga");
+            os << "                ral_u64 pos = wpos + sex[j] + lex[j];\n";
+            os << "#pragma unroll\n                for (int g = 0; g < RAL_G; ++g)\n";
+            os << "                    if ((kb[j] >> g) & 1u) o" << k << "[pos++] = ga[g];\n";
+            os << "            }\n";
+        }
+        os << "        }\n";
+    }
+    if (any_proj) {
+        os << "#pragma unroll\n        for (int j = 0; j < RAL_J; ++j) {\n";
+        os << "            if (kb[j] == 0u) continue;\n";
+        os << "            const ral_i64 r = wbase + (ral_i64)j * 32 * RAL_G + lane * RAL_G;\n";
+        for (size_t c = 0; c < f.project_cols.size(); c++)
+            if (proj_ref[c]) load(os, "            ", f.project_cols[c], "qa" + std::to_string(c));
+        for (size_t c = 0; c < f.project_cols.size(); c++)
+            if (proj_raw[c]) os << "            const ral_u32 qw" << c << " = " << raw_word(f.project_cols[c]) << ";\n";
+        os << "            ral_u64 pos = wpos + sex[j] + lex[j];\n";
+        os << "#pragma unroll\n            for (int g = 0; g < RAL_G; ++g) {\n";
+        os << "                if (((kb[j] >> g) & 1u) == 0u) continue;\n";
+        for (int o = 0; o < f.project->n_out; o++) os << "                " << kind_ctype(proj_kind[o]) << " y" << o << ";\n";
+        os << "                ral_proj_row(P";
+        for (size_t c = 0; c < f.project_cols.size(); c++)
+            if (proj_ref[c]) os << ", " << widen("qa" + std::to_string(c) + "[g]", f.frame_dtypes[f.project_cols[c]]);
+        for (size_t c = 0; c < f.project_cols.size(); c++)
+            if (proj_raw[c]) os << ", (qw" << c << " >> ((int)(r & 31) + g)) & 1u";
+        for (int o = 0; o < f.project->n_out; o++) os << ", y" << o;
+        os << ");\n";
+        for (int k = 0; k < NO; k++) {
+            if (!f.outputs[k].from_project) continue;
+            const int o = f.outputs[k].index;
+            os << "                o" << k << "[pos] = " << narrow("y" + std::to_string(o), proj_kind[o], f.outputs[k].dtype) << ";\n";
+        }
+        os << "                ++pos;\n            }\n";
+        os << "        }\n";
+    }
+
+    // ---- validity of every masked output, staged per warp in shared memory
+    if (NVO) {
+        if (any_proj_valid) {
+            os << "        ral_u32 pw[" << proj_vouts.size() << "];\n";
+            os << "        for (int i = 0; i < " << proj_vouts.size() << "; ++i) pw[i] = 0;\n";
+            os << "        if (lane < RAL_G * RAL_J) {\n";
+            os << "            const ral_i64 w = (wbase >> 5) + lane;\n";
+            os << "            if ((w << 5) < n) ral_proj_vword(P, w, pw);\n";
+            os << "        }\n";
+        }
+        os << "        if (wtot) {\n";
+        os << "            const ral_u64 a0 = wpos & ~31ull;\n";
+        os << "            const ral_u32 nw = (ral_u32)(((wpos - a0) + wtot + 31) >> 5);\n";
+        for (int i = 0; i < NVO; i++) {
+            const int k = vouts[i];
+            const FilterOutput& o = f.outputs[k];
+            os << "            {\n";
+            os << "                ral_u32* buf = s_vb[" << i << "][warp];\n";
+            os << "                if (lane < RAL_G * RAL_J + 2) buf[lane] = 0u;\n";
+            os << "                __syncwarp();\n";
+            os << "#pragma unroll\n                for (int j = 0; j < RAL_J; ++j) {\n";
+            os << "                    const ral_i64 r = wbase + (ral_i64)j * 32 * RAL_G + lane * RAL_G;\n";
+            if (o.from_project) {
+                int pi = 0;
+                for (size_t q = 0; q < proj_vouts.size(); q++)
+                    if (proj_vouts[q] == o.index) pi = (int)q;
+                os << "                    const ral_u32 vw = __shfl_sync(0xffffffffu, pw[" << pi
+                   << "], (j * 32 * RAL_G + lane * RAL_G) >> 5);\n";
+            } else {
+                os << "                    const ral_u32 vw = (kb[j] != 0u) ? __ldg(" << fvalid(o.index) << " + (r >> 5)) : 0u;\n";
+            }
+            os << "                    ral_u32 lb = 0, t = 0;\n";
+            os << "#pragma unroll\n                    for (int g = 0; g < RAL_G; ++g)\n";
+            os << "                        if ((kb[j] >> g) & 1u) { lb |= ((vw >> ((int)(r & 31) + g)) & 1u) << t; ++t; }\n";
+            os << "                    vcnt[" << i << "] += __popc(lb);\n";
+            os << "                    const ral_u32 q = (ral_u32)(wpos - a0) + sex[j] + lex[j];\n";
+            os << "                    const ral_u64 X = (ral_u64)lb << (q & 31);\n";
+            os << "                    const ral_u32 qw = q >> 5;\n";
+            os << "                    const ral_u32 first = ((ral_u32)(wpos - a0) + sex[j]) >> 5;\n";
+            os << "#pragma unroll\n                    for (int k = 0; k <= RAL_G; ++k) {\n";
+            os << "                        const ral_u32 W = first + k;\n";
+            os << "                        const ral_u32 part = (t == 0u) ? 0u : (qw == W ? (ral_u32)X : (qw + 1u == W ? (ral_u32)(X >> 32) : 0u));\n";
+            os << "                        const ral_u32 v = __reduce_or_sync(0xffffffffu, part);\n";
+            os << "                        if (lane == 0 && v) buf[W] |= v;\n";
+            os << "                    }\n";
+            os << "                    __syncwarp();\n";
+            os << "                }\n";
+            os << "                if (lane < nw) {\n";
+            os << "                    const ral_u32 v = buf[lane];\n";
+            os << "                    ral_u32* dst = ov" << k << " + (a0 >> 5) + lane;\n";
+            os << "                    if (lane == 0 || lane == nw - 1) { if (v) atomicOr(dst, v); }\n";
+            os << "                    else *dst = v;\n";
+            os << "                }\n";
+            os << "                __syncwarp();\n";
+            os << "            }\n";
+        }
+        os << "        }\n";
+    }
+    os << "    }\n";  // tile loop
+
+    // ---- valid-bit counts: one atomic per block and masked output
+    if (NVO) {
+        os << "    __shared__ ral_u64 red[RAL_WARPS][" << NVO << "];\n";
+        os << "    for (int i = 0; i < " << NVO << "; ++i) {\n";
+        os << "        ral_u64 v = vcnt[i];\n";
+        os << "        for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);\n";
+        os << "        if (lane == 0) red[warp][i] = v;\n";
+        os << "    }\n";
+        os << "    __syncthreads();\n";
+        os << "    const int vmap[" << NVO << "] = {";
+        for (int i = 0; i < NVO; i++) os << (i ? ", " : "") << vouts[i];
+        os << "};\n";
+        os << "    if (threadIdx.x < " << NVO << ") {\n";
+        os << "        ral_u64 v = 0;\n";
+        os << "        for (int k = 0; k < RAL_WARPS; ++k) v += red[k][threadIdx.x];\n";
+        os << "        if (v) atomicAdd((unsigned long long*)(scratch + 3 + vmap[threadIdx.x]), (unsigned long long)v);\n";
+        os << "    }\n";
+    }
+    os << "}\n";
+    gk.source = os.str();
+    return gk;
 }
 
 }  // namespace ral

@@ -27,13 +27,11 @@ struct Shape {
 // Slot order of the kernel's parameter block (all 8-byte slots).
 struct ParamLayout {
     int n_rows = 0;
-    int in_data = 0, in_valid = 0;      // first slot of n_in pointers each
-    int out_data = 0, out_valid = 0;    // first slot of n_out pointers each
-    int counts = 0;                     // device array: per output, count of valid bits
+    int in_data = 0, in_valid = 0;      // first slot of the input (eval) or frame (filter) pointers
+    int out_data = 0, out_valid = 0;    // first slot of the output pointers
+    int counts = -1;                    // eval kernels: per output, count of valid bits
     int scratch = -1;                   // filter kernels: scratch block
-    int capacity = -1;                  // filter kernels: output capacity in rows
-    int gather_data = -1, gather_valid = -1, gather_out = -1, gather_out_valid = -1;  // filter kernels
-    std::vector<int> lscalar_slot, rscalar_slot;  // per op, -1 if none
+    std::vector<int> lscalar_slot, rscalar_slot;  // per op of the (predicate) program, -1 if none
     int total = 0;
 };
 
@@ -47,26 +45,47 @@ struct GeneratedKernel {
     std::string source;   // full translation unit (prelude prepended by the JIT)
     ParamLayout layout;
     Shape shape;
+    // filter kernels: scalar slots of the projection program
+    std::vector<int> layout_project_lscalar, layout_project_rscalar;
 };
 
 // perform_operation: evaluate the program over n rows into the outputs.
 GeneratedKernel generate_eval_kernel(const Program& p, const Shape& s);
 
-// Filter description for the fused stencil/compaction/gather kernel.
+// One output column of the fused filter kernel: either a gathered frame column
+// or an output of the projection program, written compacted.
+struct FilterOutput {
+    bool from_project = false;
+    int index = -1;          // frame column (gathered) or projection output number
+    gdf_dtype dtype = GDF_invalid;
+    bool has_valid = false;
+};
+
+// The fused LogicalFilter kernel: predicate (a one-output INT8 program, or the
+// "$k" clone of a one-byte frame column), single-pass compaction, and the
+// compacted write of every output.
 struct FilterSpec {
-    // predicate: either a program with one INT8 output (the stencil), or a
-    // clone of a one-byte frame column (evaluate_expression's "$n" shortcut)
+    int n_frame = 0;
+    std::vector<gdf_dtype> frame_dtypes;
+    std::vector<bool> frame_has_valid;
     bool clone_stencil = false;
-    int clone_column = -1;            // frame column index when clone_stencil
-    bool clone_has_valid = false;
+    int clone_column = -1;
     const Program* predicate = nullptr;   // inputs are frame columns predicate_cols[i]
     std::vector<int> predicate_cols;
-    // gathered columns (every frame column, in order)
-    std::vector<gdf_dtype> gather_dtypes;
-    std::vector<bool> gather_has_valid;
-    std::vector<int> gather_frame_col;    // frame column index of each gathered column
-    int n_frame = 0;
+    const Program* project = nullptr;     // optional; inputs are frame columns project_cols[i]
+    std::vector<int> project_cols;
+    std::vector<FilterOutput> outputs;
 };
+
+// Scratch words of a fused filter launch: ticket, error flag, kept-row total,
+// one valid-bit count per output, then one look-back status word per tile.
+inline int64_t filter_scratch_header(int n_outputs) { return 3 + n_outputs; }
+
+// Rows per block tile of a filter kernel with shape s.
+inline int64_t filter_tile_rows(const Shape& s) { return (int64_t)32 * s.G * s.J * (s.threads / 32); }
+
+// Widest column the fused filter touches.
+int filter_max_width(const FilterSpec& f);
 
 GeneratedKernel generate_filter_kernel(const FilterSpec& f, const Shape& s);
 

@@ -132,4 +132,49 @@ RAL_FI ral_u32 ral_lanemask_lt() {
     return m;
 }
 
+// ---- decoupled look-back (single-pass prefix over tiles) -----------------------------------
+// Status word of a tile: top two bits = state (1 aggregate known, 2 inclusive prefix known),
+// low 62 bits = the value.  Called by all 32 lanes of one warp of the tile's block; returns
+// the tile's exclusive prefix.  Tiles must be numbered in the order blocks took them (a ticket
+// counter), so every predecessor is already running and the wait ends; it is still bounded:
+// after RAL_LOOKBACK_SPIN_LIMIT polls the error word is set and the tile publishes what it has.
+#define RAL_FLAG_AGGREGATE (1ull << 62)
+#define RAL_FLAG_INCLUSIVE (2ull << 62)
+#define RAL_VALUE_MASK ((1ull << 62) - 1)
+#define RAL_LOOKBACK_SPIN_LIMIT (1l << 22)
+__device__ __forceinline__ ral_u64 ral_lookback(ral_u64* status, ral_i64 tile, ral_u64 aggregate, ral_u64* error_word) {
+    const int lane = threadIdx.x & 31;
+    if (tile == 0) {
+        if (lane == 0) ral_st_release(status, RAL_FLAG_INCLUSIVE | aggregate);
+        return 0;
+    }
+    if (lane == 0) ral_st_release(status + tile, RAL_FLAG_AGGREGATE | aggregate);
+    ral_u64 excl = 0;
+    ral_i64 j = tile - 1 - lane;
+    long spins = 0;
+    for (;;) {
+        const ral_u64 s = j >= 0 ? ral_ld_acquire(status + j) : RAL_FLAG_INCLUSIVE;
+        const ral_u64 flag = s & ~RAL_VALUE_MASK;
+        const ral_u32 incl = __ballot_sync(0xffffffffu, flag == RAL_FLAG_INCLUSIVE);
+        const ral_u32 empty = __ballot_sync(0xffffffffu, flag == 0);
+        const int f = incl ? __ffs(incl) - 1 : 32;
+        const ral_u32 upto = f >= 31 ? 0xffffffffu : ((2u << f) - 1u);
+        if (empty & upto) {
+            if (++spins > RAL_LOOKBACK_SPIN_LIMIT) {
+                if (lane == 0) atomicExch((unsigned long long*)error_word, 1ull);
+                break;
+            }
+            __nanosleep(64);
+            continue;
+        }
+        ral_u64 v = (lane <= f) ? (s & RAL_VALUE_MASK) : 0;
+        for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
+        excl += __shfl_sync(0xffffffffu, v, 0);
+        if (f < 32) break;
+        j -= 32;
+    }
+    if (lane == 0) ral_st_release(status + tile, RAL_FLAG_INCLUSIVE | ((excl + aggregate) & RAL_VALUE_MASK));
+    return excl;
+}
+
 #endif  // RAL_DEVICE_RT_CUH_

@@ -6,12 +6,18 @@
 // the byte is nonzero), then materialize_column every frame column.
 #include "filter.h"
 
+#include <algorithm>
 #include <cstdlib>
+#include <mutex>
+#include <sstream>
 #include <string>
+#include <unordered_map>
 #include <vector>
 
+#include "codegen.h"
 #include "engine.h"
 #include "frontend.h"
+#include "jit.h"
 #include "kernels.h"
 
 namespace ral {
@@ -149,10 +155,283 @@ int process_filter_unfused(gdf_column* const* frame, int ncols, const std::strin
     return kSuccess;
 }
 
-}  // namespace
+// The reference's two steps for LogicalProject over LogicalFilter: the filtered frame is
+// materialised in temporaries, then the projection runs over it.  Kept as a cross-check.
+int filter_project_unfused(gdf_column* const* frame, int ncols, const std::string& cond, const char* project_q,
+                           gdf_column* const* outs, int n_outs, gdf_size_type* n_out, cudaStream_t st) {
+    const int64_t n = frame[0]->size;
+    std::vector<gdf_column> tmp(ncols);
+    std::vector<DeviceBuffer> bufs(2 * ncols);
+    std::vector<gdf_column*> tp(ncols);
+    for (int c = 0; c < ncols; c++) {
+        tmp[c] = *frame[c];
+        if (int e = bufs[2 * c].alloc((size_t)n * gdf_dtype_size(frame[c]->dtype), st)) return e;
+        tmp[c].data = bufs[2 * c].p;
+        if (frame[c]->valid) {
+            if (int e = bufs[2 * c + 1].alloc(gdf_valid_allocation_size(n), st)) return e;
+            tmp[c].valid = (gdf_valid_type*)bufs[2 * c + 1].p;
+        }
+        tp[c] = &tmp[c];
+    }
+    if (int e = process_filter_unfused(frame, ncols, cond, tp.data(), n_out, st)) return e;
+    std::vector<gdf_dtype> f(ncols);
+    for (int c = 0; c < ncols; c++) f[c] = frame[c]->dtype;
+    ProjectPlan pp = plan_project(project_q, f);
+    std::vector<gdf_column*> evald;
+    for (size_t i = 0; i < pp.columns.size(); i++)
+        if (pp.columns[i].first) { outs[i]->size = *n_out; evald.push_back(outs[i]); }
+    std::vector<int64_t> nulls(evald.size(), 0);
+    if (!evald.empty() && *n_out > 0) {
+        std::vector<gdf_column*> ins;
+        for (int c : pp.input_columns) ins.push_back(tp[c]);
+        ProgramArrays pa{pp.pv.left.data(), pp.pv.right.data(), pp.pv.outs.data(), (int32_t)pp.pv.left.size(),
+                         pp.pv.final_pos.data(), pp.pv.bops.data(), pp.pv.uops.data(), pp.pv.lscalars.data(),
+                         pp.pv.rscalars.data()};
+        EvalOptions eo;
+        eo.stream = st;
+        eo.null_counts = nulls.data();
+        if (int e = perform_operation(evald.data(), (int)evald.size(), ins.data(), (int)ins.size(), pa, eo)) return e;
+    }
+    for (int i = 0, k = 0; i < n_outs; i++) {
+        gdf_column* o = outs[i];
+        if (pp.columns[i].first) {
+            o->size = *n_out;
+            o->null_count = (gdf_size_type)nulls[k++];
+        } else {
+            const gdf_column* src = tp[pp.columns[i].second];
+            const size_t bytes = (size_t)(*n_out) * gdf_dtype_size(src->dtype);
+            if (bytes) cudaMemcpyAsync(o->data, src->data, bytes, cudaMemcpyDeviceToDevice, st);
+            if (src->valid && o->valid)
+                cudaMemcpyAsync(o->valid, src->valid, gdf_valid_allocation_size(*n_out), cudaMemcpyDeviceToDevice, st);
+            o->size = *n_out;
+            o->null_count = src->null_count;
+        }
+    }
+    return check_cuda(cudaStreamSynchronize(st), "filter_project");
+}
+
+std::mutex g_filter_mu;
+std::unordered_map<std::string, GeneratedKernel> g_filter_kernels;
+
+bool aligned_to(const void* p, size_t a) { return ((uintptr_t)p % a) == 0; }
+
+// Launches the fused filter kernel described by `spec` over the frame.
+int run_fused(gdf_column* const* frame, FilterSpec& spec, const Program* pred, const Program* proj,
+              gdf_column* const* outs, gdf_size_type* n_out_p, cudaStream_t st) {
+    const int64_t n = frame[0]->size;
+    const int NO = (int)spec.outputs.size();
+    Shape sh;
+    sh.G = 16 / filter_max_width(spec);
+    sh.J = std::max(1, 8 / sh.G);
+    sh.threads = 256;
+    // vector loads need every frame column the kernel reads aligned to G elements
+    bool ok = true;
+    for (int c = 0; c < spec.n_frame; c++) {
+        const size_t a = (size_t)sh.G * gdf_dtype_size(spec.frame_dtypes[c]);
+        if (frame[c]->data && !aligned_to(frame[c]->data, a)) ok = false;
+        if (frame[c]->valid && !aligned_to(frame[c]->valid, 4))
+            return set_error(kInvalidArgument, "validity masks must be 4-byte aligned");
+    }
+    for (int k = 0; k < NO; k++)
+        if (outs[k]->valid && !aligned_to(outs[k]->valid, 4))
+            return set_error(kInvalidArgument, "validity masks must be 4-byte aligned");
+    if (!ok) { sh.G = 1; sh.J = 8; }
+
+    std::string key;
+    {
+        std::ostringstream k;
+        k << "G" << sh.G << "J" << sh.J << "|";
+        for (int c = 0; c < spec.n_frame; c++) k << (int)spec.frame_dtypes[c] << (spec.frame_has_valid[c] ? "v" : "") << ",";
+        k << "|c" << (spec.clone_stencil ? spec.clone_column : -1);
+        if (pred) { k << "|P" << pred->structure_key() << "@"; for (int c : spec.predicate_cols) k << c << ","; }
+        if (proj) { k << "|Q" << proj->structure_key() << "@"; for (int c : spec.project_cols) k << c << ","; }
+        k << "|O";
+        for (const FilterOutput& o : spec.outputs)
+            k << (o.from_project ? "p" : "g") << o.index << ":" << (int)o.dtype << (o.has_valid ? "v" : "") << ",";
+        key = k.str();
+    }
+    const GeneratedKernel* gk = nullptr;
+    {
+        std::lock_guard<std::mutex> lock(g_filter_mu);
+        auto it = g_filter_kernels.find(key);
+        if (it == g_filter_kernels.end()) it = g_filter_kernels.emplace(key, generate_filter_kernel(spec, sh)).first;
+        gk = &it->second;
+    }
+    std::string err;
+    const CompiledKernel* k = jit_get(*gk, err);
+    if (!k) return set_error(kJitError, err);
+    const ParamLayout& L = gk->layout;
+
+    const int64_t tile_rows = filter_tile_rows(sh);
+    const int64_t ntiles = (n + tile_rows - 1) / tile_rows;
+    const int64_t header = filter_scratch_header(NO);
+    DeviceBuffer scratch;
+    if (int e = scratch.alloc((size_t)(header + ntiles) * 8, st)) return e;
+    cudaMemsetAsync(scratch.p, 0, (size_t)(header + ntiles) * 8, st);
+    // output masks are assembled with OR at the edges of each warp's range: start from zero
+    for (int q = 0; q < NO; q++)
+        if (spec.outputs[q].has_valid) cudaMemsetAsync(outs[q]->valid, 0, (size_t)((n + 31) / 32) * 4, st);
+
+    std::vector<uint64_t> slots(L.total, 0);
+    slots[L.n_rows] = (uint64_t)n;
+    for (int c = 0; c < spec.n_frame; c++) {
+        slots[L.in_data + c] = (uint64_t)(uintptr_t)frame[c]->data;
+        slots[L.in_valid + c] = (uint64_t)(uintptr_t)frame[c]->valid;
+    }
+    for (int q = 0; q < NO; q++) {
+        slots[L.out_data + q] = (uint64_t)(uintptr_t)outs[q]->data;
+        slots[L.out_valid + q] = (uint64_t)(uintptr_t)outs[q]->valid;
+    }
+    slots[L.scratch] = (uint64_t)(uintptr_t)scratch.p;
+    if (pred) fill_scalars(*pred, L, slots);
+    if (proj) {
+        ParamLayout QL;
+        QL.lscalar_slot = gk->layout_project_lscalar;
+        QL.rscalar_slot = gk->layout_project_rscalar;
+        fill_scalars(*proj, QL, slots);
+    }
+    const int grid = launch_blocks(*k, sh.threads, tile_rows, n);
+    void* args[] = {slots.data()};
+    if (int e = check_cuda(cudaLaunchKernel((const void*)k->kernel, dim3(grid), dim3(sh.threads), args, 0, st),
+                           "launch of the filter kernel"))
+        return e;
+    note_launch();
+    std::vector<unsigned long long> h(header, 0);
+    cudaMemcpyAsync(h.data(), scratch.p, (size_t)header * 8, cudaMemcpyDeviceToHost, st);
+    if (int e = check_cuda(cudaStreamSynchronize(st), "filter kernel")) return e;
+    if (h[1]) return set_error(kTimeout, "filter look-back wait gave up");
+    const int64_t n_out = (int64_t)h[2];
+    for (int q = 0; q < NO; q++) {
+        outs[q]->size = (gdf_size_type)n_out;
+        outs[q]->null_count = spec.outputs[q].has_valid ? (gdf_size_type)(n_out - (int64_t)h[3 + q]) : 0;
+    }
+    *n_out_p = (gdf_size_type)n_out;
+    return kSuccess;
+}
+
+// Predicate part of a FilterSpec from the condition text.
+int predicate_spec(gdf_column* const* frame, int ncols, const std::string& cond, FilterSpec& spec, Program& pred,
+                   bool& have_pred) {
+    ExpressionPlan ep = plan_expression(cond, ncols);
+    have_pred = false;
+    if (ep.clone) {
+        if (gdf_dtype_size(frame[ep.clone_column]->dtype) != 1)
+            return set_error(kUnsupported, "a bare \"$k\" condition needs a one-byte column (the stencil is read as BOOL8)");
+        spec.clone_stencil = true;
+        spec.clone_column = ep.clone_column;
+        return kSuccess;
+    }
+    // the stencil the reference evaluates into: INT8 with a validity mask
+    gdf_column stencil{};
+    stencil.dtype = GDF_INT8;
+    stencil.valid = (gdf_valid_type*)(uintptr_t)64;  // never dereferenced: only its presence matters here
+    stencil.size = frame[0]->size;
+    gdf_column* souts[1] = {&stencil};
+    std::vector<gdf_column*> ins;
+    for (int c : ep.input_columns) ins.push_back(frame[c]);
+    ProgramArrays pa{ep.pv.left.data(), ep.pv.right.data(), ep.pv.outs.data(), (int32_t)ep.pv.left.size(),
+                     ep.pv.final_pos.data(), ep.pv.bops.data(), ep.pv.uops.data(), ep.pv.lscalars.data(),
+                     ep.pv.rscalars.data()};
+    if (int e = build_program(pred, souts, 1, ins.data(), (int)ins.size(), pa, false)) return e;
+    spec.predicate_cols = ep.input_columns;
+    have_pred = true;
+    return kSuccess;
+}
+
+void frame_spec(gdf_column* const* frame, int ncols, FilterSpec& spec) {
+    spec.n_frame = ncols;
+    for (int c = 0; c < ncols; c++) {
+        spec.frame_dtypes.push_back(frame[c]->dtype);
+        spec.frame_has_valid.push_back(frame[c]->valid != nullptr);
+    }
+}
 
 int process_filter_fused(gdf_column* const* frame, int ncols, const std::string& cond, gdf_column* const* outs,
-                         gdf_size_type* n_out, cudaStream_t st);
+                         gdf_size_type* n_out, cudaStream_t st) {
+    FilterSpec spec;
+    frame_spec(frame, ncols, spec);
+    Program pred;
+    bool have_pred = false;
+    if (int e = predicate_spec(frame, ncols, cond, spec, pred, have_pred)) return e;
+    if (have_pred) spec.predicate = &pred;
+    for (int c = 0; c < ncols; c++) {
+        FilterOutput o;
+        o.from_project = false;
+        o.index = c;
+        o.dtype = frame[c]->dtype;
+        o.has_valid = frame[c]->valid != nullptr;
+        spec.outputs.push_back(o);
+    }
+    return run_fused(frame, spec, have_pred ? &pred : nullptr, nullptr, outs, n_out, st);
+}
+
+}  // namespace
+
+int debug_filter_source(gdf_column* const* frame, int ncols, const char* filter_q, const char* project_q,
+                        bool compile, std::string& source, std::string& log) {
+    const std::string cond = named_expression(filter_q, "condition");
+    if (cond.empty()) return set_error(kParseError, "no condition=[...] in the LogicalFilter");
+    FilterSpec spec;
+    frame_spec(frame, ncols, spec);
+    Program pred, proj;
+    bool have_pred = false;
+    if (int e = predicate_spec(frame, ncols, cond, spec, pred, have_pred)) return e;
+    if (have_pred) spec.predicate = &pred;
+    std::vector<gdf_column> outcols;
+    if (project_q && *project_q) {
+        std::vector<gdf_dtype> fd(ncols);
+        for (int c = 0; c < ncols; c++) fd[c] = frame[c]->dtype;
+        ProjectPlan pp = plan_project(project_q, fd);
+        outcols.resize(pp.columns.size());
+        std::vector<gdf_column*> evald;
+        for (size_t i = 0; i < pp.columns.size(); i++) {
+            outcols[i] = gdf_column{};
+            const bool ev = pp.columns[i].first;
+            outcols[i].dtype = ev ? pp.eval_dtypes[pp.columns[i].second] : fd[pp.columns[i].second];
+            outcols[i].valid = (ev || frame[pp.columns[i].second]->valid) ? (gdf_valid_type*)(uintptr_t)64 : nullptr;
+            if (ev) evald.push_back(&outcols[i]);
+            FilterOutput o;
+            o.from_project = ev;
+            o.index = pp.columns[i].second;
+            o.dtype = outcols[i].dtype;
+            o.has_valid = outcols[i].valid != nullptr;
+            spec.outputs.push_back(o);
+        }
+        if (!evald.empty()) {
+            std::vector<gdf_column*> ins;
+            for (int c : pp.input_columns) ins.push_back(frame[c]);
+            ProgramArrays pa{pp.pv.left.data(), pp.pv.right.data(), pp.pv.outs.data(), (int32_t)pp.pv.left.size(),
+                             pp.pv.final_pos.data(), pp.pv.bops.data(), pp.pv.uops.data(), pp.pv.lscalars.data(),
+                             pp.pv.rscalars.data()};
+            if (int e = build_program(proj, evald.data(), (int)evald.size(), ins.data(), (int)ins.size(), pa, true)) return e;
+            spec.project = &proj;
+            spec.project_cols = pp.input_columns;
+        }
+    } else {
+        for (int c = 0; c < ncols; c++) {
+            FilterOutput o;
+            o.index = c;
+            o.dtype = frame[c]->dtype;
+            o.has_valid = frame[c]->valid != nullptr;
+            spec.outputs.push_back(o);
+        }
+    }
+    Shape sh;
+    sh.G = 16 / filter_max_width(spec);
+    sh.J = std::max(1, 8 / sh.G);
+    sh.threads = 256;
+    GeneratedKernel gk = generate_filter_kernel(spec, sh);
+    source = std::string(jit_prelude()) + "\n" + gk.source;
+    if (compile) {
+        std::string err;
+        size_t bytes = 0;
+        if (!jit_compile_only(gk, &bytes, &log, err)) {
+            log = err;
+            return set_error(kJitError, err);
+        }
+    }
+    return kSuccess;
+}
 
 int process_filter(gdf_column* const* frame, int ncols, const char* query_part, gdf_column* const* outs,
                    gdf_size_type* n_out, const FilterOptions& opt) {
@@ -170,74 +449,67 @@ int process_filter(gdf_column* const* frame, int ncols, const char* query_part, 
     return process_filter_fused(frame, ncols, cond, outs, n_out, opt.stream);
 }
 
-int process_filter_fused(gdf_column* const* frame, int ncols, const std::string& cond, gdf_column* const* outs,
-                         gdf_size_type* n_out, cudaStream_t st) {
-    // fused kernel not built yet: the three-step path
-    return process_filter_unfused(frame, ncols, cond, outs, n_out, st);
-}
-
 int filter_project(gdf_column* const* frame, int ncols, const char* filter_q, const char* project_q,
                    gdf_column* const* outs, int n_outs, gdf_size_type* n_out, const FilterOptions& opt) {
     if (!frame || ncols <= 0 || !filter_q || !project_q || !outs || !n_out)
         return set_error(kInvalidArgument, "null argument");
-    cudaStream_t st = opt.stream;
-    const int64_t n = frame[0]->size;
-    // filtered copy of the frame in temporaries, then the projection over it
-    std::vector<gdf_column> tmp(ncols);
-    std::vector<DeviceBuffer> bufs(2 * ncols);
-    std::vector<gdf_column*> tp(ncols);
     for (int c = 0; c < ncols; c++) {
-        tmp[c] = *frame[c];
-        if (int e = bufs[2 * c].alloc((size_t)n * gdf_dtype_size(frame[c]->dtype), st)) return e;
-        tmp[c].data = bufs[2 * c].p;
-        if (frame[c]->valid) {
-            if (int e = bufs[2 * c + 1].alloc(gdf_valid_allocation_size(n), st)) return e;
-            tmp[c].valid = (gdf_valid_type*)bufs[2 * c + 1].p;
-        }
-        tp[c] = &tmp[c];
+        if (!frame[c]) return set_error(kInvalidArgument, "null frame column");
+        if (frame[c]->size != frame[0]->size) return set_error(kInvalidArgument, "frame columns differ in size");
+        if (gdf_dtype_size(frame[c]->dtype) == 0) return set_error(kUnsupported, "column dtype has no fixed width");
     }
-    if (int e = process_filter(frame, ncols, filter_q, tp.data(), n_out, opt)) return e;
-    std::vector<gdf_dtype> f(ncols);
-    for (int c = 0; c < ncols; c++) f[c] = frame[c]->dtype;
-    ProjectPlan pp = plan_project(project_q, f);
+    const std::string cond = named_expression(filter_q, "condition");
+    if (cond.empty()) return set_error(kParseError, "no condition=[...] in the LogicalFilter");
+    std::vector<gdf_dtype> fd(ncols);
+    for (int c = 0; c < ncols; c++) fd[c] = frame[c]->dtype;
+    ProjectPlan pp = plan_project(project_q, fd);
     if ((int)pp.columns.size() != n_outs) return set_error(kInvalidArgument, "out_columns count differs from the projection's");
-    std::vector<gdf_column*> evald;
-    for (size_t i = 0; i < pp.columns.size(); i++) {
-        if (!pp.columns[i].first) continue;
-        if (outs[i]->dtype != pp.eval_dtypes[pp.columns[i].second])
-            return set_error(kInvalidArgument, "out column has the wrong dtype");
-        outs[i]->size = *n_out;
-        evald.push_back(outs[i]);
+    for (int i = 0; i < n_outs; i++) {
+        if (!outs[i]) return set_error(kInvalidArgument, "null out column");
+        const bool ev = pp.columns[i].first;
+        const gdf_dtype want = ev ? pp.eval_dtypes[pp.columns[i].second] : fd[pp.columns[i].second];
+        if (outs[i]->dtype != want) return set_error(kInvalidArgument, "out column " + std::to_string(i) + " has the wrong dtype");
+        if (!ev && (outs[i]->valid != nullptr) != (frame[pp.columns[i].second]->valid != nullptr))
+            return set_error(kInvalidArgument, "a pass-through out column carries a mask exactly when its frame column does");
+        if (frame[0]->size > 0 && !outs[i]->data) return set_error(kInvalidArgument, "out column without data");
     }
-    std::vector<int64_t> nulls(evald.size(), 0);
-    if (!evald.empty() && *n_out > 0) {
+    if (frame[0]->size == 0) {
+        for (int i = 0; i < n_outs; i++) { outs[i]->size = 0; outs[i]->null_count = 0; }
+        *n_out = 0;
+        return kSuccess;
+    }
+    if (filter_mode(opt) == 1) return filter_project_unfused(frame, ncols, cond, project_q, outs, n_outs, n_out, opt.stream);
+    FilterSpec spec;
+    frame_spec(frame, ncols, spec);
+    Program pred, proj;
+    bool have_pred = false;
+    if (int e = predicate_spec(frame, ncols, cond, spec, pred, have_pred)) return e;
+    if (have_pred) spec.predicate = &pred;
+    const bool have_proj = !pp.eval_dtypes.empty();
+    if (have_proj) {
+        std::vector<gdf_column*> evald;
+        for (int i = 0; i < n_outs; i++)
+            if (pp.columns[i].first) evald.push_back(outs[i]);
         std::vector<gdf_column*> ins;
-        for (int c : pp.input_columns) ins.push_back(tp[c]);
+        for (int c : pp.input_columns) ins.push_back(frame[c]);
         ProgramArrays pa{pp.pv.left.data(), pp.pv.right.data(), pp.pv.outs.data(), (int32_t)pp.pv.left.size(),
                          pp.pv.final_pos.data(), pp.pv.bops.data(), pp.pv.uops.data(), pp.pv.lscalars.data(),
                          pp.pv.rscalars.data()};
-        EvalOptions eo;
-        eo.stream = st;
-        eo.null_counts = nulls.data();
-        if (int e = perform_operation(evald.data(), (int)evald.size(), ins.data(), (int)ins.size(), pa, eo)) return e;
+        // the reference projects the filtered frame, whose null counts are recounted from the
+        // gathered masks: a mask is read whenever present
+        if (int e = build_program(proj, evald.data(), (int)evald.size(), ins.data(), (int)ins.size(), pa, true)) return e;
+        spec.project = &proj;
+        spec.project_cols = pp.input_columns;
     }
-    for (size_t i = 0, k = 0; i < pp.columns.size(); i++) {
-        gdf_column* o = outs[i];
-        if (pp.columns[i].first) {
-            o->size = *n_out;
-            o->null_count = (gdf_size_type)nulls[k++];
-        } else {
-            const gdf_column* src = tp[pp.columns[i].second];
-            if (o->dtype != src->dtype) return set_error(kInvalidArgument, "out column has the wrong dtype");
-            const size_t bytes = (size_t)(*n_out) * gdf_dtype_size(src->dtype);
-            if (bytes) cudaMemcpyAsync(o->data, src->data, bytes, cudaMemcpyDeviceToDevice, st);
-            if (src->valid && o->valid)
-                cudaMemcpyAsync(o->valid, src->valid, gdf_valid_allocation_size(*n_out), cudaMemcpyDeviceToDevice, st);
-            o->size = *n_out;
-            o->null_count = src->null_count;
-        }
+    for (int i = 0; i < n_outs; i++) {
+        FilterOutput o;
+        o.from_project = pp.columns[i].first;
+        o.index = pp.columns[i].second;
+        o.dtype = outs[i]->dtype;
+        o.has_valid = outs[i]->valid != nullptr;
+        spec.outputs.push_back(o);
     }
-    return check_cuda(cudaStreamSynchronize(st), "filter_project");
+    return run_fused(frame, spec, have_pred ? &pred : nullptr, have_proj ? &proj : nullptr, outs, n_out, opt.stream);
 }
 
 }  // namespace ral

@@ -3,6 +3,8 @@
 
 #include <cuda_runtime.h>
 
+#include <string>
+
 #include "ral/gdf_compat.h"
 
 namespace ral {
@@ -17,6 +19,11 @@ struct FilterOptions {
 
 int process_filter(gdf_column* const* frame, int num_columns, const char* query_part, gdf_column* const* out_columns,
                    gdf_size_type* num_rows_out, const FilterOptions& opt);
+
+// Generated source (and optionally an NVRTC-only compile) of the fused filter kernel
+// for a frame described by dtype and mask presence; needs no GPU.
+int debug_filter_source(gdf_column* const* frame, int num_columns, const char* filter_query_part,
+                        const char* project_query_part, bool compile, std::string& source, std::string& log);
 
 int filter_project(gdf_column* const* frame, int num_columns, const char* filter_query_part,
                    const char* project_query_part, gdf_column* const* out_columns, int num_out_columns,

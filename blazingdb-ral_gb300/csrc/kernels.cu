@@ -91,49 +91,7 @@ cudaError_t gather_by_index(const void* in, const uint32_t* in_valid, int64_t n_
 
 
 // ---- single-pass stream compaction (decoupled look-back) ---------------------------------
-// Tile = 256 threads x 16 rows.  Tiles are taken in order from a ticket counter,
-// so every predecessor of a tile is already running and the look-back always
-// ends; the wait is still bounded (error flag, see kCompactSpinLimit).
-constexpr ral_u64 kFlagAggregate = 1ull << 62;
-constexpr ral_u64 kFlagInclusive = 2ull << 62;
-constexpr ral_u64 kValueMask = (1ull << 62) - 1;
-constexpr long kCompactSpinLimit = 1l << 22;
-
-// Returns the exclusive prefix of `tile` (called by all 32 lanes of warp 0).
-__device__ ral_u64 lookback(ral_u64* status, ral_i64 tile, ral_u64 aggregate, ral_u64* error_flag) {
-    const int lane = threadIdx.x & 31;
-    if (tile == 0) {
-        if (lane == 0) ral_st_release(status, kFlagInclusive | aggregate);
-        return 0;
-    }
-    if (lane == 0) ral_st_release(status + tile, kFlagAggregate | aggregate);
-    ral_u64 excl = 0;
-    ral_i64 j = tile - 1 - lane;
-    long spins = 0;
-    for (;;) {
-        const ral_u64 s = j >= 0 ? ral_ld_acquire(status + j) : kFlagInclusive;
-        const ral_u64 flag = s & ~kValueMask;
-        const unsigned incl = __ballot_sync(0xffffffffu, flag == kFlagInclusive);
-        const unsigned empty = __ballot_sync(0xffffffffu, flag == 0);
-        const int f = incl ? __ffs(incl) - 1 : 32;
-        const unsigned upto = f == 32 ? 0xffffffffu : (f == 31 ? 0xffffffffu : ((2u << f) - 1u));
-        if (empty & upto) {
-            if (++spins > kCompactSpinLimit) {
-                if (lane == 0) atomicExch((unsigned long long*)error_flag, 1ull);
-                break;
-            }
-            __nanosleep(64);
-            continue;
-        }
-        ral_u64 v = (lane <= f) ? (s & kValueMask) : 0;
-        for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
-        excl += __shfl_sync(0xffffffffu, v, 0);
-        if (f < 32) break;
-        j -= 32;
-    }
-    if (lane == 0) ral_st_release(status + tile, kFlagInclusive | ((excl + aggregate) & kValueMask));
-    return excl;
-}
+// Tile = 256 threads x 16 rows; the look-back is ral_lookback (device_rt.cuh).
 
 __global__ void __launch_bounds__(256) compact_stencil_kernel(const int8_t* __restrict__ stencil,
                                                               const ral_u32* __restrict__ valid, ral_i64 n,
@@ -178,7 +136,7 @@ __global__ void __launch_bounds__(256) compact_stencil_kernel(const int8_t* __re
                 if (lane >= off) wi += t;
             }
             const ral_u32 total = __shfl_sync(0xffffffffu, wi, 7);
-            const ral_u64 excl = lookback(status, tile, total, scratch + 1);
+            const ral_u64 excl = ral_lookback(status, tile, total, scratch + 1);
             if (lane < 8) s_warp[lane] = wi - wv;
             if (lane == 0) {
                 s_prefix = excl;

@@ -44,6 +44,8 @@ _SIGS = {
                                            C.c_int32, I16P, I32P, I32P, SCP, SCP, C.c_int32, C.c_char_p,
                                            C.c_int64, C.c_char_p, C.c_int64]),
     "ral_kernel_launches": (C.c_int64, []),
+    "ral_debug_filter_source": (C.c_int, [I32P, I32P, C.c_int32, C.c_char_p, C.c_char_p, C.c_int32, C.c_char_p,
+                                          C.c_int64, C.c_char_p, C.c_int64]),
     "ral_jit_stats": (C.c_int, [C.POINTER(C.c_int64), C.POINTER(C.c_int64), C.POINTER(C.c_int64),
                                 C.POINTER(C.c_double)]),
 }
@@ -321,6 +323,18 @@ def debug_program_source(input_dtypes, input_nullable, output_dtypes, output_nul
     _check(lib().ral_debug_program_source(_p32(idt), _p32(inl), len(idt), _p32(odt), _p32(onl), len(odt), _p16(l),
                                           _p16(r), _p16(o), len(l), _p16(f), _p32(b), _p32(u), ls, rs,
                                           1 if compile else 0, src, len(src), log, len(log)))
+    return src.value.decode(), log.value.decode()
+
+
+def debug_filter_source(frame_dtypes, frame_nullable, filter_query_part: str, project_query_part=None,
+                        compile: bool = False):
+    """Generated CUDA source (and NVRTC log when compile=True) of the fused filter kernel; needs no GPU."""
+    fd, fn = _i32(frame_dtypes), _i32(frame_nullable)
+    src = C.create_string_buffer(1 << 20)
+    log = C.create_string_buffer(1 << 16)
+    _check(lib().ral_debug_filter_source(_p32(fd), _p32(fn), len(fd), filter_query_part.encode(),
+                                         project_query_part.encode() if project_query_part else None,
+                                         1 if compile else 0, src, len(src), log, len(log)))
     return src.value.decode(), log.value.decode()
 
 

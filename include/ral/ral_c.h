@@ -190,6 +190,13 @@ int ral_debug_program_source(const gdf_dtype *input_dtypes, const int32_t *input
                              const gdf_scalar *right_scalars, int32_t compile, char *source_out,
                              int64_t source_capacity, char *log_out, int64_t log_capacity);
 
+/* Generated source of the fused LogicalFilter kernel (optionally NVRTC-compiled, no GPU
+ * needed) for a frame described by dtypes and mask presence; project_query_part may be
+ * NULL (process_filter) or a LogicalProject (ral_filter_project). */
+int ral_debug_filter_source(const gdf_dtype *frame_dtypes, const int32_t *frame_nullable, int32_t num_columns,
+                            const char *filter_query_part, const char *project_query_part, int32_t compile,
+                            char *source_out, int64_t source_capacity, char *log_out, int64_t log_capacity);
+
 /* Kernels launched by this library since load (all entry points). */
 int64_t ral_kernel_launches(void);
 

@@ -19,6 +19,17 @@ import helpers as H
 pytestmark = pytest.mark.gpu
 
 
+@pytest.fixture(params=["fused", "unfused"])
+def filter_mode(request, monkeypatch):
+    """process_filter / filter_project run as one fused kernel (default) or as the reference's
+    three steps (stencil, compaction, gather); both must match the oracle."""
+    if request.param == "unfused":
+        monkeypatch.setenv("RAL_FILTER_MODE", "unfused")
+    else:
+        monkeypatch.delenv("RAL_FILTER_MODE", raising=False)
+    return request.param
+
+
 def program_dict(spec: W.ProgramSpec):
     return dict(left=spec.left, right=spec.right, outputs=spec.outputs, final=spec.final, ops=spec.ops,
                 uops=spec.uops, lscalars=spec.lscalars, rscalars=spec.rscalars)
@@ -63,7 +74,7 @@ def test_fused_project_without_masks():
 # ---- plain_vm shape: filter then project -----------------------------------------------------
 
 @pytest.mark.parametrize("n", [1, 64, 1000, 1_000_000])
-def test_plain_vm_filter_then_project(n):
+def test_plain_vm_filter_then_project(n, filter_mode):
     spec = W.plain_vm_host(n, seed=21)
     dev = H.to_device(spec)
     ora = H.to_oracle(spec)
@@ -77,7 +88,7 @@ def test_plain_vm_filter_then_project(n):
 
 
 @pytest.mark.parametrize("n", [1, 1000, 1_000_000])
-def test_plain_vm_fused_filter_project(n):
+def test_plain_vm_fused_filter_project(n, filter_mode):
     spec = W.plain_vm_host(n, seed=22)
     dev = H.to_device(spec)
     ora = H.to_oracle(spec)
@@ -92,7 +103,7 @@ def test_plain_vm_fused_filter_project(n):
 @pytest.mark.parametrize("sel", [0.01, 0.50, 0.99])
 @pytest.mark.parametrize("null_rate", [None, 0.05])
 @pytest.mark.parametrize("n", [777, 1_000_003])
-def test_filter_gather(sel, null_rate, n):
+def test_filter_gather(sel, null_rate, n, filter_mode):
     spec = W.filter_gather_host(n, seed=31, null_rate=null_rate)
     dev = H.to_device(spec)
     ora = H.to_oracle(spec)
@@ -103,7 +114,7 @@ def test_filter_gather(sel, null_rate, n):
         H.assert_columns_equal(g, e, what=f"column {k}")
 
 
-def test_filter_keeps_row_order_and_count():
+def test_filter_keeps_row_order_and_count(filter_mode):
     n = 300_001
     rng = np.random.default_rng(4)
     keep = rng.random(n) < 0.3
@@ -113,7 +124,7 @@ def test_filter_keeps_row_order_and_count():
     np.testing.assert_array_equal(res[1].to_numpy(), np.nonzero(keep)[0])
 
 
-def test_filter_stencil_or_sum_two_and_null_stencil():
+def test_filter_stencil_or_sum_two_and_null_stencil(filter_mode):
     """OR is integer addition: rows matching both sides give 2 (nonzero -> kept); a null stencil drops the row."""
     vals = np.array([1, 2, 3, 4, 5, 6], dtype=np.int32)
     valid = np.array([1, 1, 0, 1, 1, 1], dtype=bool)
@@ -126,7 +137,7 @@ def test_filter_stencil_or_sum_two_and_null_stencil():
     assert got[0].size == 5
 
 
-def test_filter_bare_column_condition():
+def test_filter_bare_column_condition(filter_mode):
     stencil = np.array([0, 1, 2, 0, -1, 0, 1], dtype=np.int8)
     sv = np.array([1, 1, 1, 1, 1, 0, 1], dtype=bool)
     spec = [(D.GDF_INT8, stencil, sv), (D.GDF_FLOAT64, np.arange(7) * 1.5, None)]
@@ -170,7 +181,7 @@ def test_null_count_zero_means_all_valid_but_is_null_reads_bits():
             H.assert_columns_equal(g, e, check_null_count=False)
 
 
-def test_is_null_in_compound_filter_follows_reference_column_flag():
+def test_is_null_in_compound_filter_follows_reference_column_flag(filter_mode):
     """AND(IS NULL($0), >($1, 5)): op 1 is IS_NULL, so the validity pass forces column 1 (not 0) all-valid."""
     n = 64
     rng = np.random.default_rng(2)
@@ -428,3 +439,49 @@ def test_apply_boolean_mask(n):
         exp = O.apply_boolean_mask(O.make_column(st, D.GDF_INT8, valid))
         assert got.size == len(exp)
         np.testing.assert_array_equal(got.to_numpy(), exp)
+
+
+@pytest.mark.parametrize("n", [1, 100, 2047, 2048, 2049, 300_001])
+def test_filter_project_mixed_outputs(n, filter_mode):
+    """Evaluated and pass-through projections over a filter; masks, literals, IS NULL, COALESCE."""
+    rng = np.random.default_rng(n + 7)
+    spec = [(D.GDF_INT32, rng.integers(0, 100, n), rng.random(n) < 0.9),
+            (D.GDF_FLOAT64, rng.standard_normal(n), rng.random(n) < 0.8),
+            (D.GDF_INT64, rng.integers(-1000, 1000, n), None),
+            (D.GDF_INT8, rng.integers(-5, 5, n), rng.random(n) < 0.7),
+            (D.GDF_FLOAT32, rng.standard_normal(n).astype(np.float32), None)]
+    filt = "LogicalFilter(condition=[OR(<($0, 30), >($2, 500))])"
+    proj = ("LogicalProject(a=[$2], b=[*($1, 2.5)], c=[+($0, $3)], d=[$3], e=[IS NULL($1)], "
+            "f=[CASE(IS NOT NULL($0), $0, -1)], g=[$4], h=[-($4, $1)])")
+    got = R.filter_project(H.to_device(spec), filt, proj)
+    ef = O.process_filter(H.to_oracle(spec), filt)
+    ep = O.execute_project_plan(ef, proj)
+    assert len(got) == len(ep)
+    for k, (g, e) in enumerate(zip(got, ep)):
+        H.assert_columns_equal(g, e, what=f"projection {k}")
+
+
+def test_filter_on_double_and_date_predicates(filter_mode):
+    n = 70_001
+    rng = np.random.default_rng(70)
+    spec = [(D.GDF_FLOAT64, rng.standard_normal(n), rng.random(n) < 0.95),
+            (D.GDF_DATE32, rng.integers(0, 2400, n), None),
+            (D.GDF_DATE64, rng.integers(0, 200 * 86400000, n).astype(np.int64), rng.random(n) < 0.9)]
+    q = "LogicalFilter(condition=[AND(>($0, -0.5), =(EXTRACT(FLAG(MONTH), $1), 3), <(EXTRACT(FLAG(DAY), $2), 15))])"
+    got = R.process_filter(H.to_device(spec), q)
+    exp = O.process_filter(H.to_oracle(spec), q)
+    for k, (g, e) in enumerate(zip(got, exp)):
+        H.assert_columns_equal(g, e, what=f"column {k}")
+
+
+def test_filter_unaligned_frame(filter_mode):
+    n = 9_999
+    rng = np.random.default_rng(5)
+    base = [(D.GDF_INT32, rng.integers(0, 100, n + 1), None), (D.GDF_FLOAT64, rng.standard_normal(n + 1), None)]
+    dev = H.to_device(base)
+    shifted = [R.Column(c.data[1:], None, c.dtype, size=n) for c in dev]
+    q = "LogicalFilter(condition=[<($0, 40)])"
+    got = R.process_filter(shifted, q)
+    exp = O.process_filter([O.make_column(v[1:], t) for t, v, _ in base], q)
+    for g, e in zip(got, exp):
+        H.assert_columns_equal(g, e)
