@@ -270,6 +270,104 @@ def fused_project_e2e(ctx, steps, device):
             "ms_per_step": ms}
 
 
+def _colarray(cols):
+    import ctypes
+    from ralgpu.column import GdfColumn
+    structs = [c.to_c() for c in cols]
+    arr = (ctypes.POINTER(GdfColumn) * len(structs))()
+    for i, st in enumerate(structs):
+        arr[i] = ctypes.pointer(st)
+    return arr, structs
+
+
+def filter_setup(workload, n, selectivity, device):
+    """plain_vm (fused filter + project) or filter_gather (fused filter over 6 columns)."""
+    import ctypes
+    import torch
+    import ralgpu as R
+    from ralgpu import workloads as W
+    L = R.lib()
+    if workload == "plain_vm":
+        spec = W.plain_vm_host(n)
+        frame = [R.Column.from_numpy(v, t, m) for t, v, m in spec]
+        fq, pq = W.PLAIN_VM_FILTER, W.PLAIN_VM_PROJECT
+        types, evald = R.project_output_types([c.dtype for c in frame], pq)
+        outs = [R.Column.empty(t, n) for t in types]
+        in_b = [8 + 0, 8 + 1 / 8, 4, 4]          # c0, c1 (+mask), c2, c3 read by the predicate / projection
+        out_b = 8 + 1 / 8
+        cfg = {"workload": "plain_vm", "rows": n, "filter": "((c2>=24 AND c1<0.05) OR c0%7=3) AND c3<1200",
+               "project": "c1*(1-c1)+c2", "fused": "filter+project in one kernel"}
+    else:
+        frame = []
+        for t, data, valid, nulls in W.filter_gather_device(n, device=device):
+            frame.append(R.Column(data, valid, t, size=n, null_count=nulls))
+        fq, pq = W.filter_gather_query(selectivity), None
+        outs = [R.Column.empty(c.dtype, n, with_valid=c.valid is not None) for c in frame]
+        in_b = [R.dtypes.WIDTH[c.dtype] for c in frame]
+        out_b = sum(in_b)
+        cfg = {"workload": "filter_gather", "rows": n, "selectivity": selectivity,
+               "predicate": f"<($0, {W.FILTER_THRESHOLDS[selectivity]})", "gathered_columns": 6,
+               "l2": "inputs exceed L2; no flush"}
+    fa, fs = _colarray(frame)
+    oa, os_ = _colarray(outs)
+    nout = ctypes.c_int32(0)
+
+    def step(stream):
+        if pq is None:
+            rc = L.ral_process_filter(fa, len(frame), fq.encode(), oa, ctypes.byref(nout))
+        else:
+            rc = L.ral_filter_project(fa, len(frame), fq.encode(), pq.encode(), oa, len(outs), ctypes.byref(nout))
+        if rc:
+            raise RuntimeError(L.ral_last_error().decode())
+
+    def alg_bytes():
+        k = nout.value
+        return n * sum(in_b) + k * out_b + 8
+
+    return dict(step=step, alg_bytes_fn=alg_bytes, nout=nout, cols=frame, outs=outs, config=cfg)
+
+
+def filter_e2e(ctx, steps):
+    """Host buffers: pinned H2D of the frame, the fused filter, D2H of the kept rows of every output."""
+    import torch
+    host_in = [(c.data.cpu().pin_memory(), None if c.valid is None else c.valid.cpu().pin_memory())
+               for c in ctx["cols"]]
+    host_out = [(torch.empty_like(o.data, device="cpu").pin_memory(),
+                 None if o.valid is None else torch.empty_like(o.valid, device="cpu").pin_memory()) for o in ctx["outs"]]
+
+    def one():
+        for (hd, hv), c in zip(host_in, ctx["cols"]):
+            c.data.copy_(hd, non_blocking=True)
+            if hv is not None:
+                c.valid.copy_(hv, non_blocking=True)
+        ctx["step"](None)
+        k = ctx["nout"].value
+        b = 0
+        for (hd, hv), o in zip(host_out, ctx["outs"]):
+            hd[:k].copy_(o.data[:k], non_blocking=True)
+            b += k * o.data.element_size()
+            if hv is not None:
+                nb = (k + 7) // 8
+                hv[:nb].copy_(o.valid[:nb], non_blocking=True)
+                b += nb
+        return b
+
+    one()
+    torch.cuda.synchronize()
+    start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    start.record()
+    d2h = 0
+    for _ in range(steps):
+        d2h = one()
+    end.record()
+    torch.cuda.synchronize()
+    ms = start.elapsed_time(end) / steps
+    n = ctx["cols"][0].size
+    h2d = sum(a.numel() * a.element_size() + (0 if b is None else b.numel()) for a, b in host_in)
+    return {"value": n / (ms / 1e3), "unit": "rows/s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
+            "ms_per_step": ms}
+
+
 def run_ours(args):
     import torch
     import ralgpu as R
@@ -277,9 +375,10 @@ def run_ours(args):
     torch.cuda.set_device(local)
     device = f"cuda:{local}"
     n = args.rows or {"fused_project": 200_000_000, "plain_vm": 1_000_000, "filter_gather": 500_000_000}[args.workload]
-    if args.workload != "fused_project":
-        raise SystemExit("workload not built into bench.py yet: " + args.workload)
-    ctx = fused_project_setup(n, device)
+    if args.workload == "fused_project":
+        ctx = fused_project_setup(n, device)
+    else:
+        ctx = filter_setup(args.workload, n, args.selectivity, device)
     stream = torch.cuda.current_stream()
     sampler = ClockSampler(local)
     sampler.start()
@@ -310,8 +409,10 @@ def run_ours(args):
     ms_per_step = total_ms / args.steps
     value = world * n / (ms_per_step / 1e3)
     peak, peak_kind = load_peaks()
-    achieved = ctx["alg_bytes"] / (kernel_ms / 1e3) / 1e9
-    traffic = load_traffic(args.workload)
+    alg = ctx["alg_bytes"] if "alg_bytes" in ctx else ctx["alg_bytes_fn"]()
+    achieved = alg / (kernel_ms / 1e3) / 1e9
+    traffic_key = args.workload if args.workload != "filter_gather" else f"filter_gather_{args.selectivity}"
+    traffic = load_traffic(traffic_key)
     out = {
         "metric": METRIC, "value": value, "unit": "rows/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
@@ -321,13 +422,18 @@ def run_ours(args):
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "peak_kind": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else peak_kind,
                      "frac_of_8tbs": achieved / 8000.0, "traffic": traffic,
-                     "algorithmic_bytes_per_launch": ctx["alg_bytes"], "kernel_ms": kernel_ms},
+                     "algorithmic_bytes_per_launch": alg, "kernel_ms": kernel_ms},
         "gpu_launches": int(launches),
         "clocks": clocks,
     }
+    if "nout" in ctx:
+        out["config"]["rows_out"] = ctx["nout"].value
+        out["dtype"] = "int32/int64/f32/f64/date32/bool8 gather" if args.workload == "filter_gather" else "f64+int"
     if rank == 0:
-        if not args.skip_e2e:
+        if not args.skip_e2e and args.workload == "fused_project":
             out["e2e"] = fused_project_e2e(ctx, max(2, min(args.steps, 3)), device)
+        elif not args.skip_e2e:
+            out["e2e"] = filter_e2e(ctx, max(2, min(args.steps, 3)))
         if not args.skip_cpu:
             out["cpu_baseline"] = cpu_baseline(args.workload, n, args.selectivity)
         print(json.dumps(out), flush=True)

@@ -547,7 +547,7 @@ GeneratedKernel generate_filter_kernel(const FilterSpec& f, const Shape& s) {
     }
     key << "|O";
     for (const FilterOutput& o : f.outputs) key << (o.from_project ? "p" : "g") << o.index << ":" << (int)o.dtype << (o.has_valid ? "v" : "") << ",";
-    key << "|G" << s.G << "J" << s.J << "T" << s.threads;
+    key << "|G" << s.G << "J" << s.J << "T" << s.threads << "B" << s.min_blocks;
     char hex[32];
     snprintf(hex, sizeof hex, "%016llx", (unsigned long long)fnv1a(key.str()));
     gk.name = std::string("ral_filter_") + hex;
@@ -589,7 +589,7 @@ GeneratedKernel generate_filter_kernel(const FilterSpec& f, const Shape& s) {
         }
     }
 
-    os << "\nextern \"C\" __global__ void __launch_bounds__(RAL_THREADS) " << gk.name
+    os << "\nextern \"C\" __global__ void __launch_bounds__(RAL_THREADS, " << std::max(1, s.min_blocks) << ") " << gk.name
        << "(const __grid_constant__ RalParams P) {\n";
     os << "    __shared__ ral_u32 s_tile;\n    __shared__ ral_u32 s_wcnt[RAL_WARPS];\n    __shared__ ral_u64 s_prefix;\n";
     if (NVO) os << "    __shared__ ral_u32 s_vb[" << NVO << "][RAL_WARPS][RAL_G * RAL_J + 2];\n";
@@ -612,20 +612,30 @@ GeneratedKernel generate_filter_kernel(const FilterSpec& f, const Shape& s) {
     os << "    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;\n";
     os << "    const ral_i64 WT = 32 * RAL_G * RAL_J;\n    const ral_i64 BT = WT * RAL_WARPS;\n";
     os << "    const ral_i64 ntiles = (n + BT - 1) / BT;\n";
-    if (NVO) os << "    ral_u64 vcnt[" << NVO << "];\n    for (int i = 0; i < " << NVO << "; ++i) vcnt[i] = 0;\n";
+    if (NVO) os << "    ral_u32 vcnt[" << NVO << "];\n    for (int i = 0; i < " << NVO << "; ++i) vcnt[i] = 0;\n";
+    // tickets: the next one is fetched while the current tile is processed
+    os << "    if (threadIdx.x == 0) s_tile = atomicAdd((unsigned int*)scratch, 1u);\n";
+    os << "    __syncthreads();\n";
     os << "    for (;;) {\n";
-    os << "        if (threadIdx.x == 0) s_tile = atomicAdd((unsigned int*)scratch, 1u);\n";
-    os << "        __syncthreads();\n";
     os << "        const ral_i64 tile = s_tile;\n";
     os << "        if (tile >= ntiles) break;\n";
+    os << "        ral_u32 next_tile = 0;\n";
+    os << "        if (threadIdx.x == 0) next_tile = atomicAdd((unsigned int*)scratch, 1u);\n";
     os << "        const ral_i64 wbase = tile * BT + (ral_i64)warp * WT;\n";
     os << "        const bool full = wbase + WT <= n;\n";
 
+    // columns the predicate reads: loaded with normal eviction, so that a second read by the
+    // gather or the projection hits in cache instead of DRAM
+    std::vector<bool> pred_col(NF, false);
+    if (f.clone_stencil) pred_col[f.clone_column] = true;
+    for (size_t c = 0; c < f.predicate_cols.size(); c++)
+        if (pred_ref[c]) pred_col[f.predicate_cols[c]] = true;
     // loads of a frame column for the G rows at r (vector in full warp tiles, guarded otherwise)
     auto load = [&](std::ostream& o, const std::string& ind, int c, const std::string& arr) {
         const char* et = element_ctype(f.frame_dtypes[c]);
         o << ind << et << " " << arr << "[RAL_G];\n";
-        o << ind << "if (full) ral_ldg<" << et << ", RAL_G>(" << fdata(c) << ", r, " << arr << ");\n";
+        o << ind << "if (full) " << (pred_col[c] ? "ral_ldg_keep<" : "ral_ldg<") << et << ", RAL_G>(" << fdata(c)
+          << ", r, " << arr << ");\n";
         o << ind << "else {\n" << ind << "#pragma unroll\n" << ind << "    for (int g = 0; g < RAL_G; ++g) " << arr
           << "[g] = (r + g < n) ? " << fdata(c) << "[r + g] : (" << et << ")0;\n" << ind << "}\n";
     };
@@ -679,13 +689,13 @@ GeneratedKernel generate_filter_kernel(const FilterSpec& f, const Shape& s) {
     os << "        }\n";
 
     // ---- ranks within the warp tile, block scan, look-back
-    os << "        ral_u32 lex[RAL_J], sex[RAL_J];\n        ral_u32 wtot = 0;\n";
+    os << "        ral_u32 off[RAL_J];\n        ral_u32 wtot = 0;\n";
     os << "#pragma unroll\n        for (int j = 0; j < RAL_J; ++j) {\n";
     os << "            const ral_u32 c = __popc(kb[j]);\n            ral_u32 inc = c;\n";
     os << "            for (int off = 1; off < 32; off <<= 1) {\n";
     os << "                const ral_u32 t = __shfl_up_sync(0xffffffffu, inc, off);\n";
     os << "                if (lane >= off) inc += t;\n            }\n";
-    os << "            lex[j] = inc - c;\n            sex[j] = wtot;\n";
+    os << "            off[j] = wtot + inc - c;\n";
     os << "            wtot += __shfl_sync(0xffffffffu, inc, 31);\n        }\n";
     os << "        if (lane == 0) s_wcnt[warp] = wtot;\n";
     os << "        __syncthreads();\n";
@@ -697,7 +707,7 @@ GeneratedKernel generate_filter_kernel(const FilterSpec& f, const Shape& s) {
     os << "            const ral_u32 total = __shfl_sync(0xffffffffu, inc, RAL_WARPS - 1);\n";
     os << "            const ral_u64 excl = ral_lookback(status, tile, total, scratch + 1);\n";
     os << "            if (lane < RAL_WARPS) s_wcnt[lane] = inc - v;\n";
-    os << "            if (lane == 0) {\n                s_prefix = excl;\n";
+    os << "            if (lane == 0) {\n                s_prefix = excl;\n                s_tile = next_tile;\n";
     os << "                if (tile == ntiles - 1) scratch[2] = excl + total;\n            }\n";
     os << "        }\n";
     os << "        __syncthreads();\n";
@@ -715,7 +725,7 @@ GeneratedKernel generate_filter_kernel(const FilterSpec& f, const Shape& s) {
             const int c = f.outputs[k].index;
             os << "            {\n";
             load(os, "                ", c, "ga");
-            os << "                ral_u64 pos = wpos + sex[j] + lex[j];\n";
+            os << "                ral_u64 pos = wpos + off[j];\n";
             os << "#pragma unroll\n                for (int g = 0; g < RAL_G; ++g)\n";
             os << "                    if ((kb[j] >> g) & 1u) o" << k << "[pos++] = ga[g];\n";
             os << "            }\n";
@@ -730,7 +740,7 @@ GeneratedKernel generate_filter_kernel(const FilterSpec& f, const Shape& s) {
             if (proj_ref[c]) load(os, "            ", f.project_cols[c], "qa" + std::to_string(c));
         for (size_t c = 0; c < f.project_cols.size(); c++)
             if (proj_raw[c]) os << "            const ral_u32 qw" << c << " = " << raw_word(f.project_cols[c]) << ";\n";
-        os << "            ral_u64 pos = wpos + sex[j] + lex[j];\n";
+        os << "            ral_u64 pos = wpos + off[j];\n";
         os << "#pragma unroll\n            for (int g = 0; g < RAL_G; ++g) {\n";
         os << "                if (((kb[j] >> g) & 1u) == 0u) continue;\n";
         for (int o = 0; o < f.project->n_out; o++) os << "                " << kind_ctype(proj_kind[o]) << " y" << o << ";\n";
@@ -785,10 +795,10 @@ GeneratedKernel generate_filter_kernel(const FilterSpec& f, const Shape& s) {
             os << "#pragma unroll\n                    for (int g = 0; g < RAL_G; ++g)\n";
             os << "                        if ((kb[j] >> g) & 1u) { lb |= ((vw >> ((int)(r & 31) + g)) & 1u) << t; ++t; }\n";
             os << "                    vcnt[" << i << "] += __popc(lb);\n";
-            os << "                    const ral_u32 q = (ral_u32)(wpos - a0) + sex[j] + lex[j];\n";
+            os << "                    const ral_u32 q = (ral_u32)(wpos - a0) + off[j];\n";
             os << "                    const ral_u64 X = (ral_u64)lb << (q & 31);\n";
             os << "                    const ral_u32 qw = q >> 5;\n";
-            os << "                    const ral_u32 first = ((ral_u32)(wpos - a0) + sex[j]) >> 5;\n";
+            os << "                    const ral_u32 first = __shfl_sync(0xffffffffu, q, 0) >> 5;\n";
             os << "#pragma unroll\n                    for (int k = 0; k <= RAL_G; ++k) {\n";
             os << "                        const ral_u32 W = first + k;\n";
             os << "                        const ral_u32 part = (t == 0u) ? 0u : (qw == W ? (ral_u32)X : (qw + 1u == W ? (ral_u32)(X >> 32) : 0u));\n";
@@ -814,7 +824,7 @@ GeneratedKernel generate_filter_kernel(const FilterSpec& f, const Shape& s) {
     if (NVO) {
         os << "    __shared__ ral_u64 red[RAL_WARPS][" << NVO << "];\n";
         os << "    for (int i = 0; i < " << NVO << "; ++i) {\n";
-        os << "        ral_u64 v = vcnt[i];\n";
+        os << "        ral_u64 v = (ral_u64)vcnt[i];\n";
         os << "        for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);\n";
         os << "        if (lane == 0) red[warp][i] = v;\n";
         os << "    }\n";

@@ -108,6 +108,15 @@ RAL_FI void ral_ldg(const E* __restrict__ p, ral_i64 row, E (&v)[G]) {
 #pragma unroll
     for (int g = 0; g < G; ++g) v[g] = u.e[g];
 }
+// Same, through the read-only cache with normal eviction: for data read again soon.
+template <typename E, int G>
+RAL_FI void ral_ldg_keep(const E* __restrict__ p, ral_i64 row, E (&v)[G]) {
+    typedef typename RalVecT<sizeof(E) * G>::T V;
+    union { V vec; E e[G]; } u;
+    u.vec = __ldg(reinterpret_cast<const V*>(p + row));
+#pragma unroll
+    for (int g = 0; g < G; ++g) v[g] = u.e[g];
+}
 template <typename E, int G>
 RAL_FI void ral_stg(E* __restrict__ p, ral_i64 row, const E (&v)[G]) {
     typedef typename RalVecT<sizeof(E) * G>::T V;
@@ -117,14 +126,17 @@ RAL_FI void ral_stg(E* __restrict__ p, ral_i64 row, const E (&v)[G]) {
     __stcs(reinterpret_cast<V*>(p + row), u.vec);
 }
 
-// ---- ordered flag access for the single-pass scan -------------------------------------------
-RAL_FI ral_u64 ral_ld_acquire(const ral_u64* p) {
+// ---- status-word access for the single-pass scan --------------------------------------------
+// A tile's status word carries its own value, and nothing else is published through it, so
+// relaxed gpu-scope accesses suffice: a store needs no fence (which would wait for the
+// tile's outstanding data stores) and a load reads the coherent copy in L2.
+RAL_FI ral_u64 ral_ld_status(const ral_u64* p) {
     ral_u64 v;
-    asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+    asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
     return v;
 }
-RAL_FI void ral_st_release(ral_u64* p, ral_u64 v) {
-    asm volatile("st.release.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+RAL_FI void ral_st_status(ral_u64* p, ral_u64 v) {
+    asm volatile("st.relaxed.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
 }
 RAL_FI ral_u32 ral_lanemask_lt() {
     ral_u32 m;
@@ -145,15 +157,15 @@ RAL_FI ral_u32 ral_lanemask_lt() {
 __device__ __forceinline__ ral_u64 ral_lookback(ral_u64* status, ral_i64 tile, ral_u64 aggregate, ral_u64* error_word) {
     const int lane = threadIdx.x & 31;
     if (tile == 0) {
-        if (lane == 0) ral_st_release(status, RAL_FLAG_INCLUSIVE | aggregate);
+        if (lane == 0) ral_st_status(status, RAL_FLAG_INCLUSIVE | aggregate);
         return 0;
     }
-    if (lane == 0) ral_st_release(status + tile, RAL_FLAG_AGGREGATE | aggregate);
+    if (lane == 0) ral_st_status(status + tile, RAL_FLAG_AGGREGATE | aggregate);
     ral_u64 excl = 0;
     ral_i64 j = tile - 1 - lane;
     long spins = 0;
     for (;;) {
-        const ral_u64 s = j >= 0 ? ral_ld_acquire(status + j) : RAL_FLAG_INCLUSIVE;
+        const ral_u64 s = j >= 0 ? ral_ld_status(status + j) : RAL_FLAG_INCLUSIVE;
         const ral_u64 flag = s & ~RAL_VALUE_MASK;
         const ral_u32 incl = __ballot_sync(0xffffffffu, flag == RAL_FLAG_INCLUSIVE);
         const ral_u32 empty = __ballot_sync(0xffffffffu, flag == 0);
@@ -173,7 +185,7 @@ __device__ __forceinline__ ral_u64 ral_lookback(ral_u64* status, ral_i64 tile, r
         if (f < 32) break;
         j -= 32;
     }
-    if (lane == 0) ral_st_release(status + tile, RAL_FLAG_INCLUSIVE | ((excl + aggregate) & RAL_VALUE_MASK));
+    if (lane == 0) ral_st_status(status + tile, RAL_FLAG_INCLUSIVE | ((excl + aggregate) & RAL_VALUE_MASK));
     return excl;
 }
 

@@ -210,105 +210,6 @@ int filter_project_unfused(gdf_column* const* frame, int ncols, const std::strin
     return check_cuda(cudaStreamSynchronize(st), "filter_project");
 }
 
-std::mutex g_filter_mu;
-std::unordered_map<std::string, GeneratedKernel> g_filter_kernels;
-
-bool aligned_to(const void* p, size_t a) { return ((uintptr_t)p % a) == 0; }
-
-// Launches the fused filter kernel described by `spec` over the frame.
-int run_fused(gdf_column* const* frame, FilterSpec& spec, const Program* pred, const Program* proj,
-              gdf_column* const* outs, gdf_size_type* n_out_p, cudaStream_t st) {
-    const int64_t n = frame[0]->size;
-    const int NO = (int)spec.outputs.size();
-    Shape sh;
-    sh.G = 16 / filter_max_width(spec);
-    sh.J = std::max(1, 8 / sh.G);
-    sh.threads = 256;
-    // vector loads need every frame column the kernel reads aligned to G elements
-    bool ok = true;
-    for (int c = 0; c < spec.n_frame; c++) {
-        const size_t a = (size_t)sh.G * gdf_dtype_size(spec.frame_dtypes[c]);
-        if (frame[c]->data && !aligned_to(frame[c]->data, a)) ok = false;
-        if (frame[c]->valid && !aligned_to(frame[c]->valid, 4))
-            return set_error(kInvalidArgument, "validity masks must be 4-byte aligned");
-    }
-    for (int k = 0; k < NO; k++)
-        if (outs[k]->valid && !aligned_to(outs[k]->valid, 4))
-            return set_error(kInvalidArgument, "validity masks must be 4-byte aligned");
-    if (!ok) { sh.G = 1; sh.J = 8; }
-
-    std::string key;
-    {
-        std::ostringstream k;
-        k << "G" << sh.G << "J" << sh.J << "|";
-        for (int c = 0; c < spec.n_frame; c++) k << (int)spec.frame_dtypes[c] << (spec.frame_has_valid[c] ? "v" : "") << ",";
-        k << "|c" << (spec.clone_stencil ? spec.clone_column : -1);
-        if (pred) { k << "|P" << pred->structure_key() << "@"; for (int c : spec.predicate_cols) k << c << ","; }
-        if (proj) { k << "|Q" << proj->structure_key() << "@"; for (int c : spec.project_cols) k << c << ","; }
-        k << "|O";
-        for (const FilterOutput& o : spec.outputs)
-            k << (o.from_project ? "p" : "g") << o.index << ":" << (int)o.dtype << (o.has_valid ? "v" : "") << ",";
-        key = k.str();
-    }
-    const GeneratedKernel* gk = nullptr;
-    {
-        std::lock_guard<std::mutex> lock(g_filter_mu);
-        auto it = g_filter_kernels.find(key);
-        if (it == g_filter_kernels.end()) it = g_filter_kernels.emplace(key, generate_filter_kernel(spec, sh)).first;
-        gk = &it->second;
-    }
-    std::string err;
-    const CompiledKernel* k = jit_get(*gk, err);
-    if (!k) return set_error(kJitError, err);
-    const ParamLayout& L = gk->layout;
-
-    const int64_t tile_rows = filter_tile_rows(sh);
-    const int64_t ntiles = (n + tile_rows - 1) / tile_rows;
-    const int64_t header = filter_scratch_header(NO);
-    DeviceBuffer scratch;
-    if (int e = scratch.alloc((size_t)(header + ntiles) * 8, st)) return e;
-    cudaMemsetAsync(scratch.p, 0, (size_t)(header + ntiles) * 8, st);
-    // output masks are assembled with OR at the edges of each warp's range: start from zero
-    for (int q = 0; q < NO; q++)
-        if (spec.outputs[q].has_valid) cudaMemsetAsync(outs[q]->valid, 0, (size_t)((n + 31) / 32) * 4, st);
-
-    std::vector<uint64_t> slots(L.total, 0);
-    slots[L.n_rows] = (uint64_t)n;
-    for (int c = 0; c < spec.n_frame; c++) {
-        slots[L.in_data + c] = (uint64_t)(uintptr_t)frame[c]->data;
-        slots[L.in_valid + c] = (uint64_t)(uintptr_t)frame[c]->valid;
-    }
-    for (int q = 0; q < NO; q++) {
-        slots[L.out_data + q] = (uint64_t)(uintptr_t)outs[q]->data;
-        slots[L.out_valid + q] = (uint64_t)(uintptr_t)outs[q]->valid;
-    }
-    slots[L.scratch] = (uint64_t)(uintptr_t)scratch.p;
-    if (pred) fill_scalars(*pred, L, slots);
-    if (proj) {
-        ParamLayout QL;
-        QL.lscalar_slot = gk->layout_project_lscalar;
-        QL.rscalar_slot = gk->layout_project_rscalar;
-        fill_scalars(*proj, QL, slots);
-    }
-    const int grid = launch_blocks(*k, sh.threads, tile_rows, n);
-    void* args[] = {slots.data()};
-    if (int e = check_cuda(cudaLaunchKernel((const void*)k->kernel, dim3(grid), dim3(sh.threads), args, 0, st),
-                           "launch of the filter kernel"))
-        return e;
-    note_launch();
-    std::vector<unsigned long long> h(header, 0);
-    cudaMemcpyAsync(h.data(), scratch.p, (size_t)header * 8, cudaMemcpyDeviceToHost, st);
-    if (int e = check_cuda(cudaStreamSynchronize(st), "filter kernel")) return e;
-    if (h[1]) return set_error(kTimeout, "filter look-back wait gave up");
-    const int64_t n_out = (int64_t)h[2];
-    for (int q = 0; q < NO; q++) {
-        outs[q]->size = (gdf_size_type)n_out;
-        outs[q]->null_count = spec.outputs[q].has_valid ? (gdf_size_type)(n_out - (int64_t)h[3 + q]) : 0;
-    }
-    *n_out_p = (gdf_size_type)n_out;
-    return kSuccess;
-}
-
 // Predicate part of a FilterSpec from the condition text.
 int predicate_spec(gdf_column* const* frame, int ncols, const std::string& cond, FilterSpec& spec, Program& pred,
                    bool& have_pred) {
@@ -346,23 +247,195 @@ void frame_spec(gdf_column* const* frame, int ncols, FilterSpec& spec) {
     }
 }
 
+bool aligned_to(const void* p, size_t a) { return ((uintptr_t)p % a) == 0; }
+
+// Everything a fused filter call needs that depends only on the query text and the frame's
+// shape (dtypes, masks, null counts being zero or not, alignment) and the outputs' shape.
+struct PreparedFilter {
+    FilterSpec spec;
+    Program pred, proj;
+    bool have_pred = false, have_proj = false;
+    GeneratedKernel gk;
+    const CompiledKernel* k = nullptr;
+};
+
+std::mutex g_prep_mu;
+std::unordered_map<std::string, std::unique_ptr<PreparedFilter>> g_prepared;
+
+// Per-thread device scratch for the look-back states, grown on demand and reused: the
+// synchronous entry points finish with it before they return.
+struct ThreadScratch {
+    void* p = nullptr;
+    size_t bytes = 0;
+};
+thread_local std::unordered_map<int, ThreadScratch> t_scratch;
+
+int scratch_get(size_t bytes, cudaStream_t st, void** out) {
+    int dev = 0;
+    if (int e = check_cuda(cudaGetDevice(&dev), "cudaGetDevice")) return e;
+    ThreadScratch& ts = t_scratch[dev];
+    if (ts.bytes < bytes) {
+        if (ts.p) cudaFreeAsync(ts.p, st);
+        ts.p = nullptr;
+        ts.bytes = 0;
+        const size_t want = std::max<size_t>(bytes + bytes / 4, 1 << 16);
+        if (int e = check_cuda(cudaMallocAsync(&ts.p, want, st), "cudaMallocAsync")) return e;
+        ts.bytes = want;
+    }
+    *out = ts.p;
+    return kSuccess;
+}
+
+std::string frame_signature(gdf_column* const* frame, int ncols, gdf_column* const* outs, int n_outs) {
+    std::string k;
+    bool al = true;
+    for (int c = 0; c < ncols; c++) {
+        k += (char)('A' + (int)frame[c]->dtype);
+        k += frame[c]->valid ? (frame[c]->null_count ? 'n' : 'v') : '-';
+        if (frame[c]->data && !aligned_to(frame[c]->data, 16)) al = false;
+    }
+    k += al ? "|a|" : "|u|";
+    for (int q = 0; q < n_outs; q++) {
+        k += (char)('A' + (int)outs[q]->dtype);
+        k += outs[q]->valid ? 'v' : '-';
+    }
+    return k;
+}
+
+// Finishes a PreparedFilter whose spec (frame, predicate, projection, outputs) is filled in.
+int prepare_kernel(PreparedFilter& pf, bool aligned16) {
+    Shape sh;
+    sh.G = aligned16 ? 16 / filter_max_width(pf.spec) : 1;
+    sh.J = std::max(1, 16 / sh.G);
+    sh.threads = 256;
+    sh.min_blocks = 3;
+    pf.gk = generate_filter_kernel(pf.spec, sh);
+    std::string err;
+    pf.k = jit_get(pf.gk, err);
+    if (!pf.k) return set_error(kJitError, err);
+    return kSuccess;
+}
+
+// Launches a prepared fused filter over the frame.
+int run_prepared(const PreparedFilter& pf, gdf_column* const* frame, gdf_column* const* outs, gdf_size_type* n_out_p,
+                 cudaStream_t st) {
+    const int64_t n = frame[0]->size;
+    const FilterSpec& spec = pf.spec;
+    const int NO = (int)spec.outputs.size();
+    for (int c = 0; c < spec.n_frame; c++)
+        if (frame[c]->valid && !aligned_to(frame[c]->valid, 4))
+            return set_error(kInvalidArgument, "validity masks must be 4-byte aligned");
+    for (int q = 0; q < NO; q++)
+        if (outs[q]->valid && !aligned_to(outs[q]->valid, 4))
+            return set_error(kInvalidArgument, "validity masks must be 4-byte aligned");
+    const ParamLayout& L = pf.gk.layout;
+    const int64_t tile_rows = filter_tile_rows(pf.gk.shape);
+    const int64_t ntiles = (n + tile_rows - 1) / tile_rows;
+    const int64_t header = filter_scratch_header(NO);
+    void* scratch = nullptr;
+    if (int e = scratch_get((size_t)(header + ntiles) * 8, st, &scratch)) return e;
+    cudaMemsetAsync(scratch, 0, (size_t)(header + ntiles) * 8, st);
+    // output masks are assembled with OR at the edges of each warp's range: start from zero
+    for (int q = 0; q < NO; q++)
+        if (spec.outputs[q].has_valid) cudaMemsetAsync(outs[q]->valid, 0, (size_t)((n + 31) / 32) * 4, st);
+
+    std::vector<uint64_t> slots(L.total, 0);
+    slots[L.n_rows] = (uint64_t)n;
+    for (int c = 0; c < spec.n_frame; c++) {
+        slots[L.in_data + c] = (uint64_t)(uintptr_t)frame[c]->data;
+        slots[L.in_valid + c] = (uint64_t)(uintptr_t)frame[c]->valid;
+    }
+    for (int q = 0; q < NO; q++) {
+        slots[L.out_data + q] = (uint64_t)(uintptr_t)outs[q]->data;
+        slots[L.out_valid + q] = (uint64_t)(uintptr_t)outs[q]->valid;
+    }
+    slots[L.scratch] = (uint64_t)(uintptr_t)scratch;
+    if (pf.have_pred) fill_scalars(pf.pred, L, slots);
+    if (pf.have_proj) {
+        ParamLayout QL;
+        QL.lscalar_slot = pf.gk.layout_project_lscalar;
+        QL.rscalar_slot = pf.gk.layout_project_rscalar;
+        fill_scalars(pf.proj, QL, slots);
+    }
+    const int grid = launch_blocks(*pf.k, pf.gk.shape.threads, tile_rows, n);
+    void* args[] = {slots.data()};
+    if (int e = check_cuda(cudaLaunchKernel((const void*)pf.k->kernel, dim3(grid), dim3(pf.gk.shape.threads), args, 0, st),
+                           "launch of the filter kernel"))
+        return e;
+    note_launch();
+    unsigned long long h[64];
+    std::vector<unsigned long long> hv;
+    unsigned long long* hp = h;
+    if (header > 64) { hv.resize(header); hp = hv.data(); }
+    cudaMemcpyAsync(hp, scratch, (size_t)header * 8, cudaMemcpyDeviceToHost, st);
+    if (int e = check_cuda(cudaStreamSynchronize(st), "filter kernel")) return e;
+    if (hp[1]) return set_error(kTimeout, "filter look-back wait gave up");
+    const int64_t n_out = (int64_t)hp[2];
+    for (int q = 0; q < NO; q++) {
+        outs[q]->size = (gdf_size_type)n_out;
+        outs[q]->null_count = spec.outputs[q].has_valid ? (gdf_size_type)(n_out - (int64_t)hp[3 + q]) : 0;
+    }
+    *n_out_p = (gdf_size_type)n_out;
+    return kSuccess;
+}
+
+// Looks up or builds the prepared plan.  `build` fills spec/programs of a fresh plan.
+template <typename Build>
+int prepared(const std::string& key, bool aligned16, Build&& build, const PreparedFilter** out) {
+    {
+        std::lock_guard<std::mutex> lock(g_prep_mu);
+        auto it = g_prepared.find(key);
+        if (it != g_prepared.end()) { *out = it->second.get(); return kSuccess; }
+    }
+    auto pf = std::make_unique<PreparedFilter>();
+    if (int e = build(*pf)) return e;
+    if (int e = prepare_kernel(*pf, aligned16)) return e;
+    std::lock_guard<std::mutex> lock(g_prep_mu);
+    auto res = g_prepared.emplace(key, std::move(pf));
+    *out = res.first->second.get();
+    return kSuccess;
+}
+
+// LogicalProject plans by text and frame dtypes (parsing is the costly part of a small call).
+std::mutex g_pp_mu;
+std::unordered_map<std::string, std::unique_ptr<ProjectPlan>> g_project_plans;
+
+const ProjectPlan& cached_project_plan(const char* project_q, const std::vector<gdf_dtype>& fd) {
+    std::string key(project_q);
+    key += '|';
+    for (gdf_dtype t : fd) key += (char)('A' + (int)t);
+    {
+        std::lock_guard<std::mutex> lock(g_pp_mu);
+        auto it = g_project_plans.find(key);
+        if (it != g_project_plans.end()) return *it->second;
+    }
+    auto pp = std::make_unique<ProjectPlan>(plan_project(project_q, fd));
+    std::lock_guard<std::mutex> lock(g_pp_mu);
+    auto res = g_project_plans.emplace(key, std::move(pp));
+    return *res.first->second;
+}
+
 int process_filter_fused(gdf_column* const* frame, int ncols, const std::string& cond, gdf_column* const* outs,
                          gdf_size_type* n_out, cudaStream_t st) {
-    FilterSpec spec;
-    frame_spec(frame, ncols, spec);
-    Program pred;
-    bool have_pred = false;
-    if (int e = predicate_spec(frame, ncols, cond, spec, pred, have_pred)) return e;
-    if (have_pred) spec.predicate = &pred;
-    for (int c = 0; c < ncols; c++) {
-        FilterOutput o;
-        o.from_project = false;
-        o.index = c;
-        o.dtype = frame[c]->dtype;
-        o.has_valid = frame[c]->valid != nullptr;
-        spec.outputs.push_back(o);
-    }
-    return run_fused(frame, spec, have_pred ? &pred : nullptr, nullptr, outs, n_out, st);
+    const std::string sig = frame_signature(frame, ncols, outs, ncols);
+    const bool al = sig.find("|a|") != std::string::npos;
+    const PreparedFilter* pf = nullptr;
+    int rc = prepared("F|" + cond + "|" + sig, al, [&](PreparedFilter& p) {
+        frame_spec(frame, ncols, p.spec);
+        if (int e = predicate_spec(frame, ncols, cond, p.spec, p.pred, p.have_pred)) return e;
+        if (p.have_pred) p.spec.predicate = &p.pred;
+        for (int c = 0; c < ncols; c++) {
+            FilterOutput o;
+            o.from_project = false;
+            o.index = c;
+            o.dtype = frame[c]->dtype;
+            o.has_valid = frame[c]->valid != nullptr;
+            p.spec.outputs.push_back(o);
+        }
+        return (int)kSuccess;
+    }, &pf);
+    if (rc) return rc;
+    return run_prepared(*pf, frame, outs, n_out, st);
 }
 
 }  // namespace
@@ -418,8 +491,9 @@ int debug_filter_source(gdf_column* const* frame, int ncols, const char* filter_
     }
     Shape sh;
     sh.G = 16 / filter_max_width(spec);
-    sh.J = std::max(1, 8 / sh.G);
+    sh.J = std::max(1, 16 / sh.G);
     sh.threads = 256;
+    sh.min_blocks = 3;
     GeneratedKernel gk = generate_filter_kernel(spec, sh);
     source = std::string(jit_prelude()) + "\n" + gk.source;
     if (compile) {
@@ -462,7 +536,7 @@ int filter_project(gdf_column* const* frame, int ncols, const char* filter_q, co
     if (cond.empty()) return set_error(kParseError, "no condition=[...] in the LogicalFilter");
     std::vector<gdf_dtype> fd(ncols);
     for (int c = 0; c < ncols; c++) fd[c] = frame[c]->dtype;
-    ProjectPlan pp = plan_project(project_q, fd);
+    const ProjectPlan& pp = cached_project_plan(project_q, fd);
     if ((int)pp.columns.size() != n_outs) return set_error(kInvalidArgument, "out_columns count differs from the projection's");
     for (int i = 0; i < n_outs; i++) {
         if (!outs[i]) return set_error(kInvalidArgument, "null out column");
@@ -479,37 +553,42 @@ int filter_project(gdf_column* const* frame, int ncols, const char* filter_q, co
         return kSuccess;
     }
     if (filter_mode(opt) == 1) return filter_project_unfused(frame, ncols, cond, project_q, outs, n_outs, n_out, opt.stream);
-    FilterSpec spec;
-    frame_spec(frame, ncols, spec);
-    Program pred, proj;
-    bool have_pred = false;
-    if (int e = predicate_spec(frame, ncols, cond, spec, pred, have_pred)) return e;
-    if (have_pred) spec.predicate = &pred;
-    const bool have_proj = !pp.eval_dtypes.empty();
-    if (have_proj) {
-        std::vector<gdf_column*> evald;
-        for (int i = 0; i < n_outs; i++)
-            if (pp.columns[i].first) evald.push_back(outs[i]);
-        std::vector<gdf_column*> ins;
-        for (int c : pp.input_columns) ins.push_back(frame[c]);
-        ProgramArrays pa{pp.pv.left.data(), pp.pv.right.data(), pp.pv.outs.data(), (int32_t)pp.pv.left.size(),
-                         pp.pv.final_pos.data(), pp.pv.bops.data(), pp.pv.uops.data(), pp.pv.lscalars.data(),
-                         pp.pv.rscalars.data()};
-        // the reference projects the filtered frame, whose null counts are recounted from the
-        // gathered masks: a mask is read whenever present
-        if (int e = build_program(proj, evald.data(), (int)evald.size(), ins.data(), (int)ins.size(), pa, true)) return e;
-        spec.project = &proj;
-        spec.project_cols = pp.input_columns;
-    }
-    for (int i = 0; i < n_outs; i++) {
-        FilterOutput o;
-        o.from_project = pp.columns[i].first;
-        o.index = pp.columns[i].second;
-        o.dtype = outs[i]->dtype;
-        o.has_valid = outs[i]->valid != nullptr;
-        spec.outputs.push_back(o);
-    }
-    return run_fused(frame, spec, have_pred ? &pred : nullptr, have_proj ? &proj : nullptr, outs, n_out, opt.stream);
+    const std::string sig = frame_signature(frame, ncols, outs, n_outs);
+    const bool al = sig.find("|a|") != std::string::npos;
+    const PreparedFilter* pf = nullptr;
+    int rc = prepared("FP|" + cond + "|" + std::string(project_q) + "|" + sig, al, [&](PreparedFilter& p) {
+        frame_spec(frame, ncols, p.spec);
+        if (int e = predicate_spec(frame, ncols, cond, p.spec, p.pred, p.have_pred)) return e;
+        if (p.have_pred) p.spec.predicate = &p.pred;
+        p.have_proj = !pp.eval_dtypes.empty();
+        if (p.have_proj) {
+            std::vector<gdf_column*> evald;
+            for (int i = 0; i < n_outs; i++)
+                if (pp.columns[i].first) evald.push_back(outs[i]);
+            std::vector<gdf_column*> ins;
+            for (int c : pp.input_columns) ins.push_back(frame[c]);
+            ProgramArrays pa{pp.pv.left.data(), pp.pv.right.data(), pp.pv.outs.data(), (int32_t)pp.pv.left.size(),
+                             pp.pv.final_pos.data(), pp.pv.bops.data(), pp.pv.uops.data(), pp.pv.lscalars.data(),
+                             pp.pv.rscalars.data()};
+            // the reference projects the filtered frame, whose null counts are recounted from the
+            // gathered masks: a mask is read whenever present
+            if (int e = build_program(p.proj, evald.data(), (int)evald.size(), ins.data(), (int)ins.size(), pa, true))
+                return e;
+            p.spec.project = &p.proj;
+            p.spec.project_cols = pp.input_columns;
+        }
+        for (int i = 0; i < n_outs; i++) {
+            FilterOutput o;
+            o.from_project = pp.columns[i].first;
+            o.index = pp.columns[i].second;
+            o.dtype = outs[i]->dtype;
+            o.has_valid = outs[i]->valid != nullptr;
+            p.spec.outputs.push_back(o);
+        }
+        return (int)kSuccess;
+    }, &pf);
+    if (rc) return rc;
+    return run_prepared(*pf, frame, outs, n_out, opt.stream);
 }
 
 }  // namespace ral
