@@ -465,7 +465,7 @@ int filter_max_width(const FilterSpec& f) {
 }
 
 GeneratedKernel generate_filter_kernel(const FilterSpec& f, const Shape& s) {
-    if (s.G * s.J > 30) throw std::runtime_error("filter kernel shape: G*J must be at most 30");
+    if (s.G * s.J > 4096) throw std::runtime_error("filter kernel shape: G*J out of range");
     GeneratedKernel gk;
     gk.shape = s;
     ParamLayout& L = gk.layout;
@@ -589,9 +589,33 @@ GeneratedKernel generate_filter_kernel(const FilterSpec& f, const Shape& s) {
         }
     }
 
+    // ---- kernel: one warp-sized chunk of 32*G*J rows per ticket, no block-wide barriers.
+    // Pass 1 evaluates the predicate over the chunk into packed keep bits (G bits per lane and
+    // slice, in registers); the warp then publishes its kept count and looks back over the
+    // preceding chunks; pass 2 recomputes each slice's ranks from the bits and writes every
+    // output.  While one warp waits in its look-back the other warps of the SM keep loading.
+    // columns the predicate reads: loaded with normal eviction, so that a second read by the
+    // gather or the projection hits in cache instead of DRAM
+    std::vector<bool> pred_col(NF, false);
+    if (f.clone_stencil) pred_col[f.clone_column] = true;
+    for (size_t c = 0; c < f.predicate_cols.size(); c++)
+        if (pred_ref[c]) pred_col[f.predicate_cols[c]] = true;
+    // loads of a frame column for the G rows at r (vector in full chunks, guarded otherwise)
+    auto load = [&](std::ostream& o, const std::string& ind, int c, const std::string& arr) {
+        const char* et = element_ctype(f.frame_dtypes[c]);
+        o << ind << et << " " << arr << "[RAL_G];\n";
+        o << ind << "if (full) " << (pred_col[c] ? "ral_ldg_keep<" : "ral_ldg<") << et << ", RAL_G>(" << fdata(c)
+          << ", r, " << arr << ");\n";
+        o << ind << "else {\n" << ind << "#pragma unroll\n" << ind << "    for (int g = 0; g < RAL_G; ++g) " << arr
+          << "[g] = (r + g < n) ? " << fdata(c) << "[r + g] : (" << et << ")0;\n" << ind << "}\n";
+    };
+    auto raw_word = [&](int c) {
+        if (!f.frame_has_valid[c]) return std::string("0xffffffffu");
+        return "((r < n) ? __ldg(" + fvalid(c) + " + (r >> 5)) : 0xffffffffu)";
+    };
+    const int KBW = (s.G * s.J + 31) / 32;  // packed keep-bit words per lane
     os << "\nextern \"C\" __global__ void __launch_bounds__(RAL_THREADS, " << std::max(1, s.min_blocks) << ") " << gk.name
        << "(const __grid_constant__ RalParams P) {\n";
-    os << "    __shared__ ral_u32 s_tile;\n    __shared__ ral_u32 s_wcnt[RAL_WARPS];\n    __shared__ ral_u64 s_prefix;\n";
     if (NVO) os << "    __shared__ ral_u32 s_vb[" << NVO << "][RAL_WARPS][RAL_G * RAL_J + 2];\n";
     os << "    const ral_i64 n = (ral_i64)P.s[" << L.n_rows << "];\n";
     os << "    ral_u64* const scratch = (ral_u64*)P.s[" << L.scratch << "];\n";
@@ -610,54 +634,35 @@ GeneratedKernel generate_filter_kernel(const FilterSpec& f, const Shape& s) {
             os << "    ral_u32* __restrict__ ov" << k << " = (ral_u32*)P.s[" << L.out_valid + k << "];\n";
     }
     os << "    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;\n";
-    os << "    const ral_i64 WT = 32 * RAL_G * RAL_J;\n    const ral_i64 BT = WT * RAL_WARPS;\n";
-    os << "    const ral_i64 ntiles = (n + BT - 1) / BT;\n";
+    os << "    const ral_i64 WT = 32 * RAL_G * RAL_J;\n";
+    os << "    const ral_i64 nchunks = (n + WT - 1) / WT;\n";
+    os << "    const ral_u32 GMASK = (RAL_G == 32) ? 0xffffffffu : ((1u << RAL_G) - 1u);\n";
     if (NVO) os << "    ral_u32 vcnt[" << NVO << "];\n    for (int i = 0; i < " << NVO << "; ++i) vcnt[i] = 0;\n";
-    // tickets: the next one is fetched while the current tile is processed
-    os << "    if (threadIdx.x == 0) s_tile = atomicAdd((unsigned int*)scratch, 1u);\n";
-    os << "    __syncthreads();\n";
     os << "    for (;;) {\n";
-    os << "        const ral_i64 tile = s_tile;\n";
-    os << "        if (tile >= ntiles) break;\n";
-    os << "        ral_u32 next_tile = 0;\n";
-    os << "        if (threadIdx.x == 0) next_tile = atomicAdd((unsigned int*)scratch, 1u);\n";
-    os << "        const ral_i64 wbase = tile * BT + (ral_i64)warp * WT;\n";
-    os << "        const bool full = wbase + WT <= n;\n";
+    os << "        ral_u32 ticket = 0;\n";
+    os << "        if (lane == 0) ticket = atomicAdd((unsigned int*)scratch, 1u);\n";
+    os << "        const ral_i64 chunk = __shfl_sync(0xffffffffu, ticket, 0);\n";
+    os << "        if (chunk >= nchunks) break;\n";
+    os << "        const ral_i64 base = chunk * WT;\n";
+    os << "        const bool full = base + WT <= n;\n";
+    os << "        ral_u32 kbw[" << KBW << "];\n";
+    os << "        for (int q = 0; q < " << KBW << "; ++q) kbw[q] = 0u;\n";
+    os << "        ral_u32 total = 0;\n";
 
-    // columns the predicate reads: loaded with normal eviction, so that a second read by the
-    // gather or the projection hits in cache instead of DRAM
-    std::vector<bool> pred_col(NF, false);
-    if (f.clone_stencil) pred_col[f.clone_column] = true;
-    for (size_t c = 0; c < f.predicate_cols.size(); c++)
-        if (pred_ref[c]) pred_col[f.predicate_cols[c]] = true;
-    // loads of a frame column for the G rows at r (vector in full warp tiles, guarded otherwise)
-    auto load = [&](std::ostream& o, const std::string& ind, int c, const std::string& arr) {
-        const char* et = element_ctype(f.frame_dtypes[c]);
-        o << ind << et << " " << arr << "[RAL_G];\n";
-        o << ind << "if (full) " << (pred_col[c] ? "ral_ldg_keep<" : "ral_ldg<") << et << ", RAL_G>(" << fdata(c)
-          << ", r, " << arr << ");\n";
-        o << ind << "else {\n" << ind << "#pragma unroll\n" << ind << "    for (int g = 0; g < RAL_G; ++g) " << arr
-          << "[g] = (r + g < n) ? " << fdata(c) << "[r + g] : (" << et << ")0;\n" << ind << "}\n";
-    };
-    auto raw_word = [&](int c) {
-        if (!f.frame_has_valid[c]) return std::string("0xffffffffu");
-        return "((r < n) ? __ldg(" + fvalid(c) + " + (r >> 5)) : 0xffffffffu)";
-    };
-
-    // ---- predicate: keep bits per slice
-    os << "        ral_u32 sw = 0;\n";
-    os << "        if (lane < RAL_G * RAL_J) {\n";
-    os << "            const ral_i64 w = (wbase >> 5) + lane;\n";
+    // ---- pass 1: predicate
+    os << "#pragma unroll 4\n        for (int j = 0; j < RAL_J; ++j) {\n";
+    os << "            const ral_i64 r = base + (ral_i64)j * 32 * RAL_G + lane * RAL_G;\n";
+    // stencil validity word of this slice for the lane's rows
+    os << "            ral_u32 sw = 0;\n";
+    os << "            if (lane < RAL_G) {\n";
+    os << "                const ral_i64 w = (base >> 5) + (ral_i64)j * RAL_G + lane;\n";
     if (f.clone_stencil) {
-        if (f.frame_has_valid[f.clone_column]) os << "            if ((w << 5) < n) sw = __ldg(" << fvalid(f.clone_column) << " + w);\n";
-        else os << "            if ((w << 5) < n) sw = 0xffffffffu;\n";
+        if (f.frame_has_valid[f.clone_column]) os << "                if ((w << 5) < n) sw = __ldg(" << fvalid(f.clone_column) << " + w);\n";
+        else os << "                if ((w << 5) < n) sw = 0xffffffffu;\n";
     } else {
-        os << "            if ((w << 5) < n) sw = ral_pred_vword(P, w);\n";
+        os << "                if ((w << 5) < n) sw = ral_pred_vword(P, w);\n";
     }
-    os << "        }\n";
-    os << "        ral_u32 kb[RAL_J];\n";
-    os << "#pragma unroll\n        for (int j = 0; j < RAL_J; ++j) {\n";
-    os << "            const ral_i64 r = wbase + (ral_i64)j * 32 * RAL_G + lane * RAL_G;\n";
+    os << "            }\n";
     if (f.clone_stencil) {
         load(os, "            ", f.clone_column, "sa");
     } else {
@@ -682,69 +687,73 @@ GeneratedKernel generate_filter_kernel(const FilterSpec& f, const Shape& s) {
     }
     os << "                bits |= (sv != 0 ? 1u : 0u) << g;\n";
     os << "            }\n";
-    os << "            const ral_u32 word = __shfl_sync(0xffffffffu, sw, (j * 32 * RAL_G + lane * RAL_G) >> 5);\n";
-    os << "            bits &= (word >> (int)(r & 31)) & ((1u << RAL_G) - 1u);\n";
+    os << "            const ral_u32 word = __shfl_sync(0xffffffffu, sw, (lane * RAL_G) >> 5);\n";
+    os << "            bits &= (word >> (int)(r & 31)) & GMASK;\n";
     os << "            if (!full) {\n#pragma unroll\n                for (int g = 0; g < RAL_G; ++g) if (r + g >= n) bits &= ~(1u << g);\n            }\n";
-    os << "            kb[j] = bits;\n";
+    os << "            kbw[(j * RAL_G) >> 5] |= bits << ((j * RAL_G) & 31);\n";
+    os << "            total += __reduce_add_sync(0xffffffffu, __popc(bits));\n";
     os << "        }\n";
+    os << "        const ral_u64 excl = ral_lookback(status, chunk, total, scratch + 1);\n";
+    os << "        if (chunk == nchunks - 1 && lane == 0) scratch[2] = excl + total;\n";
+    os << "        if (total == 0u) continue;\n";
 
-    // ---- ranks within the warp tile, block scan, look-back
-    os << "        ral_u32 off[RAL_J];\n        ral_u32 wtot = 0;\n";
-    os << "#pragma unroll\n        for (int j = 0; j < RAL_J; ++j) {\n";
-    os << "            const ral_u32 c = __popc(kb[j]);\n            ral_u32 inc = c;\n";
+    // ---- pass 2: ranks and outputs
+    bool any_gather = false, any_proj = false;
+    for (const FilterOutput& o : f.outputs) (o.from_project ? any_proj : any_gather) = true;
+    if (NVO) {
+        for (int i = 0; i < NVO; i++) os << "        if (lane < RAL_G * RAL_J + 2) s_vb[" << i << "][warp][lane] = 0u;\n";
+        os << "        if (RAL_G * RAL_J + 2 > 32) {\n";
+        os << "            for (int q = 32 + lane; q < RAL_G * RAL_J + 2; q += 32) {\n";
+        for (int i = 0; i < NVO; i++) os << "                s_vb[" << i << "][warp][q] = 0u;\n";
+        os << "            }\n        }\n";
+        os << "        __syncwarp();\n";
+        os << "        const ral_u64 a0 = excl & ~31ull;\n";
+    }
+    if (any_proj && !proj_vouts.empty()) os << "        ral_u32 pw[" << proj_vouts.size() << "];\n";
+    os << "        ral_u64 sbase = excl;\n";
+    os << "#pragma unroll 2\n        for (int j = 0; j < RAL_J; ++j) {\n";
+    os << "            const ral_u32 kb = (kbw[(j * RAL_G) >> 5] >> ((j * RAL_G) & 31)) & GMASK;\n";
+    os << "            const ral_u32 c = __popc(kb);\n";
+    os << "            ral_u32 inc = c;\n";
     os << "            for (int off = 1; off < 32; off <<= 1) {\n";
     os << "                const ral_u32 t = __shfl_up_sync(0xffffffffu, inc, off);\n";
     os << "                if (lane >= off) inc += t;\n            }\n";
-    os << "            off[j] = wtot + inc - c;\n";
-    os << "            wtot += __shfl_sync(0xffffffffu, inc, 31);\n        }\n";
-    os << "        if (lane == 0) s_wcnt[warp] = wtot;\n";
-    os << "        __syncthreads();\n";
-    os << "        if (warp == 0) {\n";
-    os << "            const ral_u32 v = lane < RAL_WARPS ? s_wcnt[lane] : 0u;\n            ral_u32 inc = v;\n";
-    os << "            for (int off = 1; off < RAL_WARPS; off <<= 1) {\n";
-    os << "                const ral_u32 t = __shfl_up_sync(0xffffffffu, inc, off);\n";
-    os << "                if (lane >= off) inc += t;\n            }\n";
-    os << "            const ral_u32 total = __shfl_sync(0xffffffffu, inc, RAL_WARPS - 1);\n";
-    os << "            const ral_u64 excl = ral_lookback(status, tile, total, scratch + 1);\n";
-    os << "            if (lane < RAL_WARPS) s_wcnt[lane] = inc - v;\n";
-    os << "            if (lane == 0) {\n                s_prefix = excl;\n                s_tile = next_tile;\n";
-    os << "                if (tile == ntiles - 1) scratch[2] = excl + total;\n            }\n";
-    os << "        }\n";
-    os << "        __syncthreads();\n";
-    os << "        const ral_u64 wpos = s_prefix + s_wcnt[warp];\n";
-
-    // ---- data of every output
-    bool any_gather = false, any_proj = false;
-    for (const FilterOutput& o : f.outputs) (o.from_project ? any_proj : any_gather) = true;
+    os << "            const ral_u32 stot = __shfl_sync(0xffffffffu, inc, 31);\n";
+    os << "            if (stot == 0u) continue;\n";
+    os << "            const ral_u64 pos0 = sbase + inc - c;\n";
+    os << "            const ral_i64 r = base + (ral_i64)j * 32 * RAL_G + lane * RAL_G;\n";
     if (any_gather) {
-        os << "#pragma unroll\n        for (int j = 0; j < RAL_J; ++j) {\n";
-        os << "            if (kb[j] == 0u) continue;\n";
-        os << "            const ral_i64 r = wbase + (ral_i64)j * 32 * RAL_G + lane * RAL_G;\n";
+        os << "            if (kb) {\n";
         for (int k = 0; k < NO; k++) {
             if (f.outputs[k].from_project) continue;
             const int c = f.outputs[k].index;
-            os << "            {\n";
-            load(os, "                ", c, "ga");
-            os << "                ral_u64 pos = wpos + off[j];\n";
-            os << "#pragma unroll\n                for (int g = 0; g < RAL_G; ++g)\n";
-            os << "                    if ((kb[j] >> g) & 1u) o" << k << "[pos++] = ga[g];\n";
-            os << "            }\n";
+            os << "                {\n";
+            load(os, "                    ", c, "ga");
+            os << "                    ral_u64 pos = pos0;\n";
+            os << "#pragma unroll\n                    for (int g = 0; g < RAL_G; ++g)\n";
+            os << "                        if ((kb >> g) & 1u) o" << k << "[pos++] = ga[g];\n";
+            os << "                }\n";
         }
-        os << "        }\n";
+        os << "            }\n";
     }
     if (any_proj) {
-        os << "#pragma unroll\n        for (int j = 0; j < RAL_J; ++j) {\n";
-        os << "            if (kb[j] == 0u) continue;\n";
-        os << "            const ral_i64 r = wbase + (ral_i64)j * 32 * RAL_G + lane * RAL_G;\n";
+        if (!proj_vouts.empty()) {
+            os << "            for (int i = 0; i < " << proj_vouts.size() << "; ++i) pw[i] = 0u;\n";
+            os << "            if (lane < RAL_G) {\n";
+            os << "                const ral_i64 w = (base >> 5) + (ral_i64)j * RAL_G + lane;\n";
+            os << "                if ((w << 5) < n) ral_proj_vword(P, w, pw);\n";
+            os << "            }\n";
+        }
+        os << "            if (kb) {\n";
         for (size_t c = 0; c < f.project_cols.size(); c++)
-            if (proj_ref[c]) load(os, "            ", f.project_cols[c], "qa" + std::to_string(c));
+            if (proj_ref[c]) load(os, "                ", f.project_cols[c], "qa" + std::to_string(c));
         for (size_t c = 0; c < f.project_cols.size(); c++)
-            if (proj_raw[c]) os << "            const ral_u32 qw" << c << " = " << raw_word(f.project_cols[c]) << ";\n";
-        os << "            ral_u64 pos = wpos + off[j];\n";
-        os << "#pragma unroll\n            for (int g = 0; g < RAL_G; ++g) {\n";
-        os << "                if (((kb[j] >> g) & 1u) == 0u) continue;\n";
-        for (int o = 0; o < f.project->n_out; o++) os << "                " << kind_ctype(proj_kind[o]) << " y" << o << ";\n";
-        os << "                ral_proj_row(P";
+            if (proj_raw[c]) os << "                const ral_u32 qw" << c << " = " << raw_word(f.project_cols[c]) << ";\n";
+        os << "                ral_u64 pos = pos0;\n";
+        os << "#pragma unroll\n                for (int g = 0; g < RAL_G; ++g) {\n";
+        os << "                    if (((kb >> g) & 1u) == 0u) continue;\n";
+        for (int o = 0; o < f.project->n_out; o++) os << "                    " << kind_ctype(proj_kind[o]) << " y" << o << ";\n";
+        os << "                    ral_proj_row(P";
         for (size_t c = 0; c < f.project_cols.size(); c++)
             if (proj_ref[c]) os << ", " << widen("qa" + std::to_string(c) + "[g]", f.frame_dtypes[f.project_cols[c]]);
         for (size_t c = 0; c < f.project_cols.size(); c++)
@@ -754,88 +763,67 @@ GeneratedKernel generate_filter_kernel(const FilterSpec& f, const Shape& s) {
         for (int k = 0; k < NO; k++) {
             if (!f.outputs[k].from_project) continue;
             const int o = f.outputs[k].index;
-            os << "                o" << k << "[pos] = " << narrow("y" + std::to_string(o), proj_kind[o], f.outputs[k].dtype) << ";\n";
+            os << "                    o" << k << "[pos] = " << narrow("y" + std::to_string(o), proj_kind[o], f.outputs[k].dtype) << ";\n";
         }
-        os << "                ++pos;\n            }\n";
-        os << "        }\n";
+        os << "                    ++pos;\n                }\n";
+        os << "            }\n";
     }
-
-    // ---- validity of every masked output, staged per warp in shared memory
-    if (NVO) {
-        if (any_proj_valid) {
-            os << "        ral_u32 pw[" << proj_vouts.size() << "];\n";
-            os << "        for (int i = 0; i < " << proj_vouts.size() << "; ++i) pw[i] = 0;\n";
-            os << "        if (lane < RAL_G * RAL_J) {\n";
-            os << "            const ral_i64 w = (wbase >> 5) + lane;\n";
-            os << "            if ((w << 5) < n) ral_proj_vword(P, w, pw);\n";
-            os << "        }\n";
+    // validity of the masked outputs for this slice, staged in the warp's shared-memory buffer
+    for (int i = 0; i < NVO; i++) {
+        const int k = vouts[i];
+        const FilterOutput& o = f.outputs[k];
+        os << "            {\n";
+        if (o.from_project) {
+            int pi = 0;
+            for (size_t q = 0; q < proj_vouts.size(); q++)
+                if (proj_vouts[q] == o.index) pi = (int)q;
+            os << "                const ral_u32 vw = __shfl_sync(0xffffffffu, pw[" << pi << "], (lane * RAL_G) >> 5);\n";
+        } else {
+            os << "                const ral_u32 vw = kb ? __ldg(" << fvalid(o.index) << " + (r >> 5)) : 0u;\n";
         }
-        os << "        if (wtot) {\n";
-        os << "            const ral_u64 a0 = wpos & ~31ull;\n";
-        os << "            const ral_u32 nw = (ral_u32)(((wpos - a0) + wtot + 31) >> 5);\n";
+        os << "                ral_u32 lb = 0, t = 0;\n";
+        os << "#pragma unroll\n                for (int g = 0; g < RAL_G; ++g)\n";
+        os << "                    if ((kb >> g) & 1u) { lb |= ((vw >> ((int)(r & 31) + g)) & 1u) << t; ++t; }\n";
+        os << "                vcnt[" << i << "] += __popc(lb);\n";
+        os << "                const ral_u32 q = (ral_u32)(pos0 - a0);\n";
+        os << "                const ral_u64 X = (ral_u64)lb << (q & 31);\n";
+        os << "                const ral_u32 qw = q >> 5;\n";
+        os << "                const ral_u32 first = (ral_u32)(sbase - a0) >> 5;\n";
+        os << "#pragma unroll\n                for (int kk = 0; kk <= RAL_G; ++kk) {\n";
+        os << "                    const ral_u32 W = first + kk;\n";
+        os << "                    const ral_u32 part = (t == 0u) ? 0u : (qw == W ? (ral_u32)X : (qw + 1u == W ? (ral_u32)(X >> 32) : 0u));\n";
+        os << "                    const ral_u32 v = __reduce_or_sync(0xffffffffu, part);\n";
+        os << "                    if (lane == 0 && v) s_vb[" << i << "][warp][W] |= v;\n";
+        os << "                }\n";
+        os << "            }\n";
+    }
+    os << "            sbase += stot;\n";
+    os << "        }\n";
+    // flush the staged masks: edge words may be shared with neighbouring chunks
+    if (NVO) {
+        os << "        __syncwarp();\n";
+        os << "        const ral_u32 nw = (ral_u32)(((excl - a0) + total + 31) >> 5);\n";
         for (int i = 0; i < NVO; i++) {
             const int k = vouts[i];
-            const FilterOutput& o = f.outputs[k];
-            os << "            {\n";
-            os << "                ral_u32* buf = s_vb[" << i << "][warp];\n";
-            os << "                if (lane < RAL_G * RAL_J + 2) buf[lane] = 0u;\n";
-            os << "                __syncwarp();\n";
-            os << "#pragma unroll\n                for (int j = 0; j < RAL_J; ++j) {\n";
-            os << "                    const ral_i64 r = wbase + (ral_i64)j * 32 * RAL_G + lane * RAL_G;\n";
-            if (o.from_project) {
-                int pi = 0;
-                for (size_t q = 0; q < proj_vouts.size(); q++)
-                    if (proj_vouts[q] == o.index) pi = (int)q;
-                os << "                    const ral_u32 vw = __shfl_sync(0xffffffffu, pw[" << pi
-                   << "], (j * 32 * RAL_G + lane * RAL_G) >> 5);\n";
-            } else {
-                os << "                    const ral_u32 vw = (kb[j] != 0u) ? __ldg(" << fvalid(o.index) << " + (r >> 5)) : 0u;\n";
-            }
-            os << "                    ral_u32 lb = 0, t = 0;\n";
-            os << "#pragma unroll\n                    for (int g = 0; g < RAL_G; ++g)\n";
-            os << "                        if ((kb[j] >> g) & 1u) { lb |= ((vw >> ((int)(r & 31) + g)) & 1u) << t; ++t; }\n";
-            os << "                    vcnt[" << i << "] += __popc(lb);\n";
-            os << "                    const ral_u32 q = (ral_u32)(wpos - a0) + off[j];\n";
-            os << "                    const ral_u64 X = (ral_u64)lb << (q & 31);\n";
-            os << "                    const ral_u32 qw = q >> 5;\n";
-            os << "                    const ral_u32 first = __shfl_sync(0xffffffffu, q, 0) >> 5;\n";
-            os << "#pragma unroll\n                    for (int k = 0; k <= RAL_G; ++k) {\n";
-            os << "                        const ral_u32 W = first + k;\n";
-            os << "                        const ral_u32 part = (t == 0u) ? 0u : (qw == W ? (ral_u32)X : (qw + 1u == W ? (ral_u32)(X >> 32) : 0u));\n";
-            os << "                        const ral_u32 v = __reduce_or_sync(0xffffffffu, part);\n";
-            os << "                        if (lane == 0 && v) buf[W] |= v;\n";
-            os << "                    }\n";
-            os << "                    __syncwarp();\n";
-            os << "                }\n";
-            os << "                if (lane < nw) {\n";
-            os << "                    const ral_u32 v = buf[lane];\n";
-            os << "                    ral_u32* dst = ov" << k << " + (a0 >> 5) + lane;\n";
-            os << "                    if (lane == 0 || lane == nw - 1) { if (v) atomicOr(dst, v); }\n";
-            os << "                    else *dst = v;\n";
-            os << "                }\n";
-            os << "                __syncwarp();\n";
-            os << "            }\n";
+            os << "        for (ral_u32 q = lane; q < nw; q += 32) {\n";
+            os << "            const ral_u32 v = s_vb[" << i << "][warp][q];\n";
+            os << "            ral_u32* dst = ov" << k << " + (a0 >> 5) + q;\n";
+            os << "            if (q == 0 || q == nw - 1) { if (v) atomicOr(dst, v); }\n";
+            os << "            else *dst = v;\n";
+            os << "        }\n";
         }
-        os << "        }\n";
+        os << "        __syncwarp();\n";
     }
-    os << "    }\n";  // tile loop
+    os << "    }\n";  // chunk loop
 
-    // ---- valid-bit counts: one atomic per block and masked output
+    // ---- valid-bit counts: one atomic per warp and masked output
     if (NVO) {
-        os << "    __shared__ ral_u64 red[RAL_WARPS][" << NVO << "];\n";
-        os << "    for (int i = 0; i < " << NVO << "; ++i) {\n";
-        os << "        ral_u64 v = (ral_u64)vcnt[i];\n";
-        os << "        for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);\n";
-        os << "        if (lane == 0) red[warp][i] = v;\n";
-        os << "    }\n";
-        os << "    __syncthreads();\n";
         os << "    const int vmap[" << NVO << "] = {";
         for (int i = 0; i < NVO; i++) os << (i ? ", " : "") << vouts[i];
         os << "};\n";
-        os << "    if (threadIdx.x < " << NVO << ") {\n";
-        os << "        ral_u64 v = 0;\n";
-        os << "        for (int k = 0; k < RAL_WARPS; ++k) v += red[k][threadIdx.x];\n";
-        os << "        if (v) atomicAdd((unsigned long long*)(scratch + 3 + vmap[threadIdx.x]), (unsigned long long)v);\n";
+        os << "    for (int i = 0; i < " << NVO << "; ++i) {\n";
+        os << "        const ral_u32 v = __reduce_add_sync(0xffffffffu, vcnt[i]);\n";
+        os << "        if (lane == 0 && v) atomicAdd((unsigned long long*)(scratch + 3 + vmap[i]), (unsigned long long)v);\n";
         os << "    }\n";
     }
     os << "}\n";

@@ -81,8 +81,8 @@ struct FilterSpec {
 // one valid-bit count per output, then one look-back status word per tile.
 inline int64_t filter_scratch_header(int n_outputs) { return 3 + n_outputs; }
 
-// Rows per block tile of a filter kernel with shape s.
-inline int64_t filter_tile_rows(const Shape& s) { return (int64_t)32 * s.G * s.J * (s.threads / 32); }
+// Rows per look-back tile of a filter kernel with shape s: one warp's chunk of J slices.
+inline int64_t filter_tile_rows(const Shape& s) { return (int64_t)32 * s.G * s.J; }
 
 // Widest column the fused filter touches.
 int filter_max_width(const FilterSpec& f);

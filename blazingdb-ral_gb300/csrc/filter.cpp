@@ -306,9 +306,9 @@ std::string frame_signature(gdf_column* const* frame, int ncols, gdf_column* con
 int prepare_kernel(PreparedFilter& pf, bool aligned16) {
     Shape sh;
     sh.G = aligned16 ? 16 / filter_max_width(pf.spec) : 1;
-    sh.J = std::max(1, 16 / sh.G);
+    sh.J = 64 / sh.G;            // 2048-row chunks
     sh.threads = 256;
-    sh.min_blocks = 3;
+    sh.min_blocks = 2;
     pf.gk = generate_filter_kernel(pf.spec, sh);
     std::string err;
     pf.k = jit_get(pf.gk, err);
@@ -357,7 +357,7 @@ int run_prepared(const PreparedFilter& pf, gdf_column* const* frame, gdf_column*
         QL.rscalar_slot = pf.gk.layout_project_rscalar;
         fill_scalars(pf.proj, QL, slots);
     }
-    const int grid = launch_blocks(*pf.k, pf.gk.shape.threads, tile_rows, n);
+    const int grid = launch_blocks(*pf.k, pf.gk.shape.threads, tile_rows * (pf.gk.shape.threads / 32), n);
     void* args[] = {slots.data()};
     if (int e = check_cuda(cudaLaunchKernel((const void*)pf.k->kernel, dim3(grid), dim3(pf.gk.shape.threads), args, 0, st),
                            "launch of the filter kernel"))
@@ -491,9 +491,9 @@ int debug_filter_source(gdf_column* const* frame, int ncols, const char* filter_
     }
     Shape sh;
     sh.G = 16 / filter_max_width(spec);
-    sh.J = std::max(1, 16 / sh.G);
+    sh.J = 64 / sh.G;
     sh.threads = 256;
-    sh.min_blocks = 3;
+    sh.min_blocks = 2;
     GeneratedKernel gk = generate_filter_kernel(spec, sh);
     source = std::string(jit_prelude()) + "\n" + gk.source;
     if (compile) {
