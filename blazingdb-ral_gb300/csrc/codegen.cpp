@@ -617,6 +617,8 @@ GeneratedKernel generate_filter_kernel(const FilterSpec& f, const Shape& s) {
     os << "\nextern \"C\" __global__ void __launch_bounds__(RAL_THREADS, " << std::max(1, s.min_blocks) << ") " << gk.name
        << "(const __grid_constant__ RalParams P) {\n";
     if (NVO) os << "    __shared__ ral_u32 s_vb[" << NVO << "][RAL_WARPS][RAL_G * RAL_J + 2];\n";
+    // per-warp staging of one slice's compacted values, so that stores are contiguous
+    os << "    __shared__ ral_u64 s_stage[RAL_WARPS][32 * RAL_G];\n";
     os << "    const ral_i64 n = (ral_i64)P.s[" << L.n_rows << "];\n";
     os << "    ral_u64* const scratch = (ral_u64*)P.s[" << L.scratch << "];\n";
     os << "    ral_u64* const status = scratch + " << filter_scratch_header(NO) << ";\n";
@@ -650,7 +652,7 @@ GeneratedKernel generate_filter_kernel(const FilterSpec& f, const Shape& s) {
     os << "        ral_u32 total = 0;\n";
 
     // ---- pass 1: predicate
-    os << "#pragma unroll 4\n        for (int j = 0; j < RAL_J; ++j) {\n";
+    os << "#pragma unroll 8\n        for (int j = 0; j < RAL_J; ++j) {\n";
     os << "            const ral_i64 r = base + (ral_i64)j * 32 * RAL_G + lane * RAL_G;\n";
     // stencil validity word of this slice for the lane's rows
     os << "            ral_u32 sw = 0;\n";
@@ -723,18 +725,25 @@ GeneratedKernel generate_filter_kernel(const FilterSpec& f, const Shape& s) {
     os << "            const ral_u64 pos0 = sbase + inc - c;\n";
     os << "            const ral_i64 r = base + (ral_i64)j * 32 * RAL_G + lane * RAL_G;\n";
     if (any_gather) {
-        os << "            if (kb) {\n";
+        // each gathered column: kept values to the warp's stage in rank order, then one
+        // contiguous run of stores for the slice
         for (int k = 0; k < NO; k++) {
             if (f.outputs[k].from_project) continue;
             const int c = f.outputs[k].index;
-            os << "                {\n";
+            const char* et = element_ctype(f.frame_dtypes[c]);
+            os << "            {\n";
+            os << "                " << et << "* const st = reinterpret_cast<" << et << "*>(s_stage[warp]);\n";
+            os << "                if (kb) {\n";
             load(os, "                    ", c, "ga");
-            os << "                    ral_u64 pos = pos0;\n";
+            os << "                    ral_u32 q = inc - c;\n";
             os << "#pragma unroll\n                    for (int g = 0; g < RAL_G; ++g)\n";
-            os << "                        if ((kb >> g) & 1u) o" << k << "[pos++] = ga[g];\n";
+            os << "                        if ((kb >> g) & 1u) st[q++] = ga[g];\n";
             os << "                }\n";
+            os << "                __syncwarp();\n";
+            os << "                for (ral_u32 m = lane; m < stot; m += 32) o" << k << "[sbase + m] = st[m];\n";
+            os << "                __syncwarp();\n";
+            os << "            }\n";
         }
-        os << "            }\n";
     }
     if (any_proj) {
         if (!proj_vouts.empty()) {

@@ -302,11 +302,20 @@ std::string frame_signature(gdf_column* const* frame, int ncols, gdf_column* con
     return k;
 }
 
+// Slices per warp chunk for n rows: chunks of up to 2048 rows, smaller for small frames so
+// that every SM gets several chunks per resident warp.
+int chunk_slices(int64_t n, int G) {
+    const int64_t target = n / (152 * 64);
+    int J = 1;
+    while (J < 64 / G && (int64_t)32 * G * J * 2 <= target) J *= 2;
+    return J;
+}
+
 // Finishes a PreparedFilter whose spec (frame, predicate, projection, outputs) is filled in.
-int prepare_kernel(PreparedFilter& pf, bool aligned16) {
+int prepare_kernel(PreparedFilter& pf, bool aligned16, int64_t n) {
     Shape sh;
     sh.G = aligned16 ? 16 / filter_max_width(pf.spec) : 1;
-    sh.J = 64 / sh.G;            // 2048-row chunks
+    sh.J = std::max(1, std::min(64 / sh.G, chunk_slices(n, sh.G)));
     sh.threads = 256;
     sh.min_blocks = 2;
     pf.gk = generate_filter_kernel(pf.spec, sh);
@@ -381,7 +390,11 @@ int run_prepared(const PreparedFilter& pf, gdf_column* const* frame, gdf_column*
 
 // Looks up or builds the prepared plan.  `build` fills spec/programs of a fresh plan.
 template <typename Build>
-int prepared(const std::string& key, bool aligned16, Build&& build, const PreparedFilter** out) {
+int prepared(const std::string& key0, bool aligned16, int64_t n, Build&& build, const PreparedFilter** out) {
+    // the chunk size depends on the row count: one plan per size class
+    int64_t cls = 1;
+    while (cls < n && cls < ((int64_t)1 << 40)) cls <<= 1;
+    const std::string key = key0 + "#" + std::to_string(cls);
     {
         std::lock_guard<std::mutex> lock(g_prep_mu);
         auto it = g_prepared.find(key);
@@ -389,7 +402,7 @@ int prepared(const std::string& key, bool aligned16, Build&& build, const Prepar
     }
     auto pf = std::make_unique<PreparedFilter>();
     if (int e = build(*pf)) return e;
-    if (int e = prepare_kernel(*pf, aligned16)) return e;
+    if (int e = prepare_kernel(*pf, aligned16, cls / 2 + 1)) return e;
     std::lock_guard<std::mutex> lock(g_prep_mu);
     auto res = g_prepared.emplace(key, std::move(pf));
     *out = res.first->second.get();
@@ -420,7 +433,7 @@ int process_filter_fused(gdf_column* const* frame, int ncols, const std::string&
     const std::string sig = frame_signature(frame, ncols, outs, ncols);
     const bool al = sig.find("|a|") != std::string::npos;
     const PreparedFilter* pf = nullptr;
-    int rc = prepared("F|" + cond + "|" + sig, al, [&](PreparedFilter& p) {
+    int rc = prepared("F|" + cond + "|" + sig, al, frame[0]->size, [&](PreparedFilter& p) {
         frame_spec(frame, ncols, p.spec);
         if (int e = predicate_spec(frame, ncols, cond, p.spec, p.pred, p.have_pred)) return e;
         if (p.have_pred) p.spec.predicate = &p.pred;
@@ -556,7 +569,8 @@ int filter_project(gdf_column* const* frame, int ncols, const char* filter_q, co
     const std::string sig = frame_signature(frame, ncols, outs, n_outs);
     const bool al = sig.find("|a|") != std::string::npos;
     const PreparedFilter* pf = nullptr;
-    int rc = prepared("FP|" + cond + "|" + std::string(project_q) + "|" + sig, al, [&](PreparedFilter& p) {
+    int rc = prepared("FP|" + cond + "|" + std::string(project_q) + "|" + sig, al, frame[0]->size,
+                      [&](PreparedFilter& p) {
         frame_spec(frame, ncols, p.spec);
         if (int e = predicate_spec(frame, ncols, cond, p.spec, p.pred, p.have_pred)) return e;
         if (p.have_pred) p.spec.predicate = &p.pred;
