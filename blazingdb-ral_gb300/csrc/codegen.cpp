@@ -725,25 +725,44 @@ GeneratedKernel generate_filter_kernel(const FilterSpec& f, const Shape& s) {
     os << "            const ral_u64 pos0 = sbase + inc - c;\n";
     os << "            const ral_i64 r = base + (ral_i64)j * 32 * RAL_G + lane * RAL_G;\n";
     if (any_gather) {
-        // each gathered column: kept values to the warp's stage in rank order, then one
-        // contiguous run of stores for the slice
+        // every gathered column of the slice is loaded first (all loads in flight together);
+        // a slice that keeps many rows is then written through the warp's stage as one
+        // contiguous run per column, a sparse slice with direct stores
         for (int k = 0; k < NO; k++) {
             if (f.outputs[k].from_project) continue;
             const int c = f.outputs[k].index;
             const char* et = element_ctype(f.frame_dtypes[c]);
-            os << "            {\n";
-            os << "                " << et << "* const st = reinterpret_cast<" << et << "*>(s_stage[warp]);\n";
-            os << "                if (kb) {\n";
-            load(os, "                    ", c, "ga");
-            os << "                    ral_u32 q = inc - c;\n";
-            os << "#pragma unroll\n                    for (int g = 0; g < RAL_G; ++g)\n";
-            os << "                        if ((kb >> g) & 1u) st[q++] = ga[g];\n";
-            os << "                }\n";
-            os << "                __syncwarp();\n";
-            os << "                for (ral_u32 m = lane; m < stot; m += 32) o" << k << "[sbase + m] = st[m];\n";
-            os << "                __syncwarp();\n";
+            os << "            " << et << " ga" << k << "[RAL_G];\n";
+            os << "            if (kb) {\n";
+            os << "                if (full) " << (pred_col[c] ? "ral_ldg_keep<" : "ral_ldg<") << et << ", RAL_G>(" << fdata(c)
+               << ", r, ga" << k << ");\n";
+            os << "                else {\n#pragma unroll\n                    for (int g = 0; g < RAL_G; ++g) ga" << k
+               << "[g] = (r + g < n) ? " << fdata(c) << "[r + g] : (" << et << ")0;\n                }\n";
             os << "            }\n";
         }
+        os << "            if (stot >= 16u) {\n";
+        for (int k = 0; k < NO; k++) {
+            if (f.outputs[k].from_project) continue;
+            const char* et = element_ctype(f.frame_dtypes[f.outputs[k].index]);
+            os << "                {\n";
+            os << "                    " << et << "* const st = reinterpret_cast<" << et << "*>(s_stage[warp]);\n";
+            os << "                    ral_u32 q = inc - c;\n";
+            os << "#pragma unroll\n                    for (int g = 0; g < RAL_G; ++g)\n";
+            os << "                        if ((kb >> g) & 1u) st[q++] = ga" << k << "[g];\n";
+            os << "                    __syncwarp();\n";
+            os << "                    for (ral_u32 m = lane; m < stot; m += 32) o" << k << "[sbase + m] = st[m];\n";
+            os << "                    __syncwarp();\n";
+            os << "                }\n";
+        }
+        os << "            } else if (kb) {\n";
+        for (int k = 0; k < NO; k++) {
+            if (f.outputs[k].from_project) continue;
+            os << "                {\n                    ral_u64 pos = pos0;\n";
+            os << "#pragma unroll\n                    for (int g = 0; g < RAL_G; ++g)\n";
+            os << "                        if ((kb >> g) & 1u) o" << k << "[pos++] = ga" << k << "[g];\n";
+            os << "                }\n";
+        }
+        os << "            }\n";
     }
     if (any_proj) {
         if (!proj_vouts.empty()) {
