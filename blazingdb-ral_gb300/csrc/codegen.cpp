@@ -547,7 +547,7 @@ GeneratedKernel generate_filter_kernel(const FilterSpec& f, const Shape& s) {
     }
     key << "|O";
     for (const FilterOutput& o : f.outputs) key << (o.from_project ? "p" : "g") << o.index << ":" << (int)o.dtype << (o.has_valid ? "v" : "") << ",";
-    key << "|G" << s.G << "J" << s.J << "T" << s.threads << "B" << s.min_blocks;
+    key << "|G" << s.G << "J" << s.J << "T" << s.threads << "B" << s.min_blocks << "U" << s.unroll << "S" << s.stage;
     char hex[32];
     snprintf(hex, sizeof hex, "%016llx", (unsigned long long)fnv1a(key.str()));
     gk.name = std::string("ral_filter_") + hex;
@@ -618,7 +618,7 @@ GeneratedKernel generate_filter_kernel(const FilterSpec& f, const Shape& s) {
        << "(const __grid_constant__ RalParams P) {\n";
     if (NVO) os << "    __shared__ ral_u32 s_vb[" << NVO << "][RAL_WARPS][RAL_G * RAL_J + 2];\n";
     // per-warp staging of one slice's compacted values, so that stores are contiguous
-    os << "    __shared__ ral_u64 s_stage[RAL_WARPS][32 * RAL_G];\n";
+    if (s.stage) os << "    __shared__ ral_u64 s_stage[RAL_WARPS][32 * RAL_G];\n";
     os << "    const ral_i64 n = (ral_i64)P.s[" << L.n_rows << "];\n";
     os << "    ral_u64* const scratch = (ral_u64*)P.s[" << L.scratch << "];\n";
     os << "    ral_u64* const status = scratch + " << filter_scratch_header(NO) << ";\n";
@@ -652,7 +652,7 @@ GeneratedKernel generate_filter_kernel(const FilterSpec& f, const Shape& s) {
     os << "        ral_u32 total = 0;\n";
 
     // ---- pass 1: predicate
-    os << "#pragma unroll 8\n        for (int j = 0; j < RAL_J; ++j) {\n";
+    os << "#pragma unroll " << std::max(1, s.unroll) << "\n        for (int j = 0; j < RAL_J; ++j) {\n";
     os << "            const ral_i64 r = base + (ral_i64)j * 32 * RAL_G + lane * RAL_G;\n";
     // stencil validity word of this slice for the lane's rows
     os << "            ral_u32 sw = 0;\n";
@@ -740,21 +740,24 @@ GeneratedKernel generate_filter_kernel(const FilterSpec& f, const Shape& s) {
                << "[g] = (r + g < n) ? " << fdata(c) << "[r + g] : (" << et << ")0;\n                }\n";
             os << "            }\n";
         }
-        os << "            if (stot >= 16u) {\n";
-        for (int k = 0; k < NO; k++) {
-            if (f.outputs[k].from_project) continue;
-            const char* et = element_ctype(f.frame_dtypes[f.outputs[k].index]);
-            os << "                {\n";
-            os << "                    " << et << "* const st = reinterpret_cast<" << et << "*>(s_stage[warp]);\n";
-            os << "                    ral_u32 q = inc - c;\n";
-            os << "#pragma unroll\n                    for (int g = 0; g < RAL_G; ++g)\n";
-            os << "                        if ((kb >> g) & 1u) st[q++] = ga" << k << "[g];\n";
-            os << "                    __syncwarp();\n";
-            os << "                    for (ral_u32 m = lane; m < stot; m += 32) o" << k << "[sbase + m] = st[m];\n";
-            os << "                    __syncwarp();\n";
-            os << "                }\n";
+        if (s.stage) {
+            os << "            if (stot >= 16u) {\n";
+            for (int k = 0; k < NO; k++) {
+                if (f.outputs[k].from_project) continue;
+                const char* et = element_ctype(f.frame_dtypes[f.outputs[k].index]);
+                os << "                {\n";
+                os << "                    " << et << "* const st = reinterpret_cast<" << et << "*>(s_stage[warp]);\n";
+                os << "                    ral_u32 q = inc - c;\n";
+                os << "#pragma unroll\n                    for (int g = 0; g < RAL_G; ++g)\n";
+                os << "                        if ((kb >> g) & 1u) st[q++] = ga" << k << "[g];\n";
+                os << "                    __syncwarp();\n";
+                os << "                    for (ral_u32 m = lane; m < stot; m += 32) o" << k << "[sbase + m] = st[m];\n";
+                os << "                    __syncwarp();\n";
+                os << "                }\n";
+            }
+            os << "            } else\n";
         }
-        os << "            } else if (kb) {\n";
+        os << "            if (kb) {\n";
         for (int k = 0; k < NO; k++) {
             if (f.outputs[k].from_project) continue;
             os << "                {\n                    ral_u64 pos = pos0;\n";

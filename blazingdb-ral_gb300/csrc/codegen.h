@@ -22,6 +22,8 @@ struct Shape {
     int J = 2;         // slices per warp tile
     int threads = 256; // threads per block
     int min_blocks = 1;  // __launch_bounds__ minimum resident blocks per SM
+    int unroll = 4;    // filter kernels: unroll of the predicate pass over slices
+    bool stage = false;  // filter kernels: dense slices written through a shared-memory stage
 };
 
 // Slot order of the kernel's parameter block (all 8-byte slots).

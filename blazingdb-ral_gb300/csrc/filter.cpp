@@ -311,6 +311,34 @@ int chunk_slices(int64_t n, int G) {
     return J;
 }
 
+// Launch-shape overrides for tuning sweeps: RAL_FILTER_TUNE="J=16,U=4,T=256,B=2,S=0"
+// (J: slices per chunk, U: predicate-pass unroll, T: threads, B: min blocks per SM,
+// S: stage dense slices through shared memory).
+std::string filter_tune() {
+    const char* v = std::getenv("RAL_FILTER_TUNE");
+    return v ? std::string(v) : std::string();
+}
+
+void apply_tune(Shape& sh, const std::string& t) {
+    size_t i = 0;
+    while (i < t.size()) {
+        size_t e = t.find(',', i);
+        if (e == std::string::npos) e = t.size();
+        const std::string kv = t.substr(i, e - i);
+        const size_t eq = kv.find('=');
+        if (eq != std::string::npos) {
+            const std::string k = kv.substr(0, eq);
+            const int v = std::atoi(kv.c_str() + eq + 1);
+            if (k == "J" && v >= 1 && v * sh.G <= 2048) sh.J = v;
+            else if (k == "U" && v >= 1 && v <= 64) sh.unroll = v;
+            else if (k == "T" && (v == 128 || v == 256 || v == 512)) sh.threads = v;
+            else if (k == "B" && v >= 1 && v <= 16) sh.min_blocks = v;
+            else if (k == "S") sh.stage = v != 0;
+        }
+        i = e + 1;
+    }
+}
+
 // Finishes a PreparedFilter whose spec (frame, predicate, projection, outputs) is filled in.
 int prepare_kernel(PreparedFilter& pf, bool aligned16, int64_t n) {
     Shape sh;
@@ -318,6 +346,9 @@ int prepare_kernel(PreparedFilter& pf, bool aligned16, int64_t n) {
     sh.J = std::max(1, std::min(64 / sh.G, chunk_slices(n, sh.G)));
     sh.threads = 256;
     sh.min_blocks = 2;
+    sh.unroll = 4;
+    sh.stage = false;
+    apply_tune(sh, filter_tune());
     pf.gk = generate_filter_kernel(pf.spec, sh);
     std::string err;
     pf.k = jit_get(pf.gk, err);
@@ -394,7 +425,7 @@ int prepared(const std::string& key0, bool aligned16, int64_t n, Build&& build, 
     // the chunk size depends on the row count: one plan per size class
     int64_t cls = 1;
     while (cls < n && cls < ((int64_t)1 << 40)) cls <<= 1;
-    const std::string key = key0 + "#" + std::to_string(cls);
+    const std::string key = key0 + "#" + std::to_string(cls) + "#" + filter_tune();
     {
         std::lock_guard<std::mutex> lock(g_prep_mu);
         auto it = g_prepared.find(key);
@@ -507,6 +538,7 @@ int debug_filter_source(gdf_column* const* frame, int ncols, const char* filter_
     sh.J = 64 / sh.G;
     sh.threads = 256;
     sh.min_blocks = 2;
+    apply_tune(sh, filter_tune());
     GeneratedKernel gk = generate_filter_kernel(spec, sh);
     source = std::string(jit_prelude()) + "\n" + gk.source;
     if (compile) {

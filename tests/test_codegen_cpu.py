@@ -79,3 +79,25 @@ def test_plain_vm_filter_program_compiles(nullable):
         [ralgpu.Scalar(s.dtype, s.value, s.is_valid) for s in plan.left_scalars],
         [ralgpu.Scalar(s.dtype, s.value, s.is_valid) for s in plan.right_scalars], compile=True)
     assert spills(log) == 0, log
+
+
+FILTER_CASES = [
+    ("filter_gather nullable", W.FILTER_GATHER_DTYPES, [1] * 6, W.filter_gather_query(0.5), None),
+    ("filter_gather null-free", W.FILTER_GATHER_DTYPES, [0] * 6, W.filter_gather_query(0.01), None),
+    ("plain_vm filter+project", W.PLAIN_VM_DTYPES, [0, 1, 0, 0], W.PLAIN_VM_FILTER, W.PLAIN_VM_PROJECT),
+    ("bare column stencil", [D.GDF_INT8, D.GDF_BOOL8, D.GDF_FLOAT64], [1, 0, 1], "LogicalFilter(condition=[$1])",
+     None),
+    ("is null + coalesce projection", [D.GDF_INT32, D.GDF_FLOAT64, D.GDF_INT64], [1, 1, 0],
+     "LogicalFilter(condition=[AND(IS NULL($0), >($2, 5))])",
+     "LogicalProject(a=[$2], b=[CASE(IS NOT NULL($0), $0, -1)], c=[IS NOT NULL($1)], d=[*($1, 2.5)])"),
+]
+
+
+@pytest.mark.parametrize("tune", ["", "S=1", "J=8,U=2,T=128,B=4", "J=64,U=8,T=512,B=1,S=1"])
+@pytest.mark.parametrize("case", FILTER_CASES, ids=[c[0] for c in FILTER_CASES])
+def test_filter_kernels_compile(case, tune, monkeypatch):
+    _, dtypes, nullable, fq, pq = case
+    monkeypatch.setenv("RAL_FILTER_TUNE", tune)
+    src, log = ralgpu.debug_filter_source(dtypes, nullable, fq, pq, compile=True)
+    assert "ral_filter_" in src and "ral_lookback" in src
+    assert spills(log) <= 64, log
