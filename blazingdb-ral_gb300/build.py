@@ -20,9 +20,9 @@ LIB = os.path.join(OUT, "libralgpu.so")
 CUDA = os.environ.get("CUDA_HOME", "/usr/local/cuda")
 NVCC = os.path.join(CUDA, "bin", "nvcc")
 
-CPP = ["program.cpp", "frontend.cpp", "codegen.cpp", "jit.cpp", "engine.cpp", "filter.cpp", "capi.cpp"]
+CPP = ["program.cpp", "frontend.cpp", "codegen.cpp", "jit.cpp", "engine.cpp", "filter.cpp", "batch.cpp", "capi.cpp"]
 CU = ["kernels.cu", "noalloc.cu"]
-HEADERS = ["program.h", "frontend.h", "codegen.h", "jit.h", "engine.h", "filter.h", "kernels.h", "device_rt.cuh"]
+HEADERS = ["program.h", "frontend.h", "codegen.h", "jit.h", "engine.h", "filter.h", "batch.h", "kernels.h", "device_rt.cuh"]
 INCLUDES = [f"-I{os.path.join(ROOT, 'include')}", f"-I{CSRC}", f"-I{os.path.join(CUDA, 'include')}"]
 GENCODE = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
@@ -83,7 +83,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
                     print(out)
     if force or jobs or _mtime(LIB) < max(_mtime(o) for o in objs):
         tmp = LIB + ".tmp"
-        _run([NVCC, *GENCODE, "-shared", "-o", tmp, *objs, f"-L{os.path.join(CUDA, 'lib64')}", "-lnvrtc",
+        _run([NVCC, *GENCODE, "-shared", "-o", tmp, *objs, f"-L{os.path.join(CUDA, 'lib64')}", "-lnvrtc", "-lnvJitLink",
               "-Xlinker", f"-rpath,{os.path.join(CUDA, 'lib64')}"])
         os.replace(tmp, LIB)
     return LIB

@@ -5,6 +5,7 @@
 #include <string>
 #include <vector>
 
+#include "batch.h"
 #include "codegen.h"
 #include "engine.h"
 #include "filter.h"
@@ -184,6 +185,43 @@ int ral_project_output_types(const gdf_dtype* frame_dtypes, int32_t num_columns,
         return (int)kSuccess;
     });
 }
+
+int ral_parse_project_plan(const gdf_dtype* frame_dtypes, int32_t num_columns, const char* query_part,
+                           int32_t capacity_ops, int32_t capacity_cols, int32_t* num_input_columns,
+                           int32_t* input_columns, int32_t* num_evaluated, gdf_dtype* evaluated_dtypes,
+                           int32_t* num_operations, column_index_type* left_inputs, column_index_type* right_inputs,
+                           column_index_type* outputs, column_index_type* final_output_positions,
+                           int32_t* operators, int32_t* unary_operators, gdf_scalar* left_scalars,
+                           gdf_scalar* right_scalars) {
+    return guarded([&] {
+        std::vector<gdf_dtype> f(frame_dtypes, frame_dtypes + num_columns);
+        ProjectPlan pp = plan_project(query_part, f);
+        const int nops = (int)pp.pv.left.size();
+        if (nops > capacity_ops || (int)pp.input_columns.size() > capacity_cols || (int)pp.eval_dtypes.size() > capacity_cols)
+            return set_error(kInvalidArgument, "capacity too small");
+        *num_input_columns = (int32_t)pp.input_columns.size();
+        for (size_t i = 0; i < pp.input_columns.size(); i++) input_columns[i] = pp.input_columns[i];
+        *num_evaluated = (int32_t)pp.eval_dtypes.size();
+        for (size_t i = 0; i < pp.eval_dtypes.size(); i++) {
+            evaluated_dtypes[i] = pp.eval_dtypes[i];
+            final_output_positions[i] = pp.pv.final_pos[i];
+        }
+        *num_operations = nops;
+        for (int k = 0; k < nops; k++) {
+            left_inputs[k] = pp.pv.left[k];
+            right_inputs[k] = pp.pv.right[k];
+            outputs[k] = pp.pv.outs[k];
+            operators[k] = pp.pv.bops[k];
+            unary_operators[k] = pp.pv.uops[k];
+            left_scalars[k] = pp.pv.lscalars[k];
+            right_scalars[k] = pp.pv.rscalars[k];
+        }
+        return (int)kSuccess;
+    });
+}
+
+int ral_batch_debug_source(const ral_batch* batch, int32_t compile, char* source_out, int64_t source_capacity,
+                           char* log_out, int64_t log_capacity);
 
 int ral_execute_project_plan(gdf_column* const* frame, int32_t num_columns, const char* query_part,
                              gdf_column* const* out_columns, int32_t num_out_columns) {
@@ -382,6 +420,154 @@ int ral_debug_filter_source(const gdf_dtype* frame_dtypes, const int32_t* frame_
         copy_out(src, source_out, source_capacity);
         copy_out(log, log_out, log_capacity);
         return rc;
+    });
+}
+
+struct ral_batch_s {
+    ral::Batch b;
+};
+
+int ral_batch_create(ral_batch** batch) {
+    return guarded([&] {
+        if (!batch) return set_error(kInvalidArgument, "null argument");
+        *batch = new ral_batch_s();
+        return (int)kSuccess;
+    });
+}
+
+int ral_batch_add(ral_batch* batch, gdf_column* const* output_columns, int32_t num_outputs,
+                  gdf_column* const* input_columns, int32_t num_inputs, const column_index_type* left_inputs,
+                  const column_index_type* right_inputs, const column_index_type* outputs, int32_t num_operations,
+                  const column_index_type* final_output_positions, const int32_t* operators,
+                  const int32_t* unary_operators, const gdf_scalar* left_scalars, const gdf_scalar* right_scalars,
+                  int32_t* program_index) {
+    return guarded([&] {
+        if (!batch) return set_error(kInvalidArgument, "null batch");
+        ProgramArrays pa{left_inputs, right_inputs, outputs, num_operations, final_output_positions,
+                         operators, unary_operators, left_scalars, right_scalars};
+        const int idx = batch->b.add(output_columns, num_outputs, input_columns, num_inputs, pa);
+        if (idx < 0) return -idx;
+        if (program_index) *program_index = idx;
+        return (int)kSuccess;
+    });
+}
+
+int ral_batch_prepare(ral_batch* batch) {
+    return guarded([&] {
+        if (!batch) return set_error(kInvalidArgument, "null batch");
+        return batch->b.prepare(cudaStreamPerThread);
+    });
+}
+
+int ral_batch_run(ral_batch* batch, void* stream, int32_t use_graph) {
+    return guarded([&] {
+        if (!batch) return set_error(kInvalidArgument, "null batch");
+        cudaStream_t st = stream ? (cudaStream_t)stream : cudaStreamPerThread;
+        return batch->b.run(st, use_graph != 0);
+    });
+}
+
+int ral_batch_info(const ral_batch* batch, int32_t* num_programs, int64_t* total_rows, int64_t* work_items) {
+    if (!batch) return set_error(kInvalidArgument, "null batch");
+    if (num_programs) *num_programs = batch->b.programs();
+    if (total_rows) *total_rows = batch->b.total_rows();
+    if (work_items) *work_items = batch->b.total_items();
+    return kSuccess;
+}
+
+int ral_batch_kernel_info(const ral_batch* batch, int32_t* registers, int32_t* grid, int32_t* blocks_per_sm) {
+    if (!batch) return set_error(kInvalidArgument, "null batch");
+    if (registers) *registers = batch->b.registers();
+    if (grid) *grid = batch->b.grid();
+    if (blocks_per_sm) *blocks_per_sm = batch->b.blocks_per_sm();
+    return kSuccess;
+}
+
+int ral_batch_debug_source(const ral_batch* batch, int32_t compile, char* source_out, int64_t source_capacity,
+                           char* log_out, int64_t log_capacity) {
+    return guarded([&] {
+        if (!batch) return set_error(kInvalidArgument, "null batch");
+        std::string src, log;
+        int rc = batch->b.debug_source(compile != 0, src, log);
+        copy_out(std::string(jit_prelude()) + "\n" + src, source_out, source_capacity);
+        copy_out(log, log_out, log_capacity);
+        return rc;
+    });
+}
+
+int ral_batch_destroy(ral_batch* batch) {
+    delete batch;
+    return kSuccess;
+}
+
+int ral_batch_tune_key(gdf_column* const* output_columns, int32_t num_outputs, gdf_column* const* input_columns,
+                       int32_t num_inputs, const column_index_type* left_inputs, const column_index_type* right_inputs,
+                       const column_index_type* outputs, int32_t num_operations,
+                       const column_index_type* final_output_positions, const int32_t* operators,
+                       const int32_t* unary_operators, const gdf_scalar* left_scalars, const gdf_scalar* right_scalars,
+                       char* key_out, int64_t key_capacity) {
+    return guarded([&] {
+        ProgramArrays pa{left_inputs, right_inputs, outputs, num_operations, final_output_positions,
+                         operators, unary_operators, left_scalars, right_scalars};
+        Program p;
+        if (int e = build_program(p, output_columns, num_outputs, input_columns, num_inputs, pa, false)) return e;
+        copy_out(tune_key(p, 16 / max_width(p)), key_out, key_capacity);
+        return (int)kSuccess;
+    });
+}
+
+int ral_autotune_program(gdf_column* const* output_columns, int32_t num_outputs, gdf_column* const* input_columns,
+                         int32_t num_inputs, const column_index_type* left_inputs,
+                         const column_index_type* right_inputs, const column_index_type* outputs,
+                         int32_t num_operations, const column_index_type* final_output_positions,
+                         const int32_t* operators, const int32_t* unary_operators, const gdf_scalar* left_scalars,
+                         const gdf_scalar* right_scalars, int32_t* best_slices, int32_t* best_unroll,
+                         double* best_ms) {
+    return guarded([&] {
+        ProgramArrays pa{left_inputs, right_inputs, outputs, num_operations, final_output_positions,
+                         operators, unary_operators, left_scalars, right_scalars};
+        Program p;
+        if (int e = build_program(p, output_columns, num_outputs, input_columns, num_inputs, pa, false)) return e;
+        const int G = 16 / max_width(p);
+        // candidates: rows per item 32*G*J, slice loop unrolled U times; all compiled up front
+        std::vector<std::pair<int, int>> cand;
+        for (int J : {2, 4, 8, 16})
+            for (int U : {1, 2})
+                if (U <= J && (int64_t)32 * G * J <= 8192) cand.push_back({J, U});
+        std::vector<std::unique_ptr<ral_batch_s>> bs;
+        for (auto& c : cand) {
+            auto b = std::make_unique<ral_batch_s>();
+            const int idx = b->b.add(output_columns, num_outputs, input_columns, num_inputs, pa);
+            if (idx < 0) return -idx;
+            b->b.force_shape(c.first, c.second);
+            bs.push_back(std::move(b));
+        }
+        cudaStream_t st = cudaStreamPerThread;
+        for (auto& b : bs)
+            if (int e = b->b.prepare(st)) return e;
+        cudaEvent_t e0, e1;
+        cudaEventCreate(&e0);
+        cudaEventCreate(&e1);
+        int bi = 0;
+        double best = 1e30;
+        for (size_t i = 0; i < bs.size(); i++) {
+            int rc = bs[i]->b.run(st, true);
+            cudaEventRecord(e0, st);
+            for (int k = 0; k < 5 && !rc; k++) rc = bs[i]->b.run(st, true);
+            cudaEventRecord(e1, st);
+            cudaEventSynchronize(e1);
+            if (rc) { cudaEventDestroy(e0); cudaEventDestroy(e1); return rc; }
+            float ms = 0;
+            cudaEventElapsedTime(&ms, e0, e1);
+            if (ms / 5 < best) { best = ms / 5; bi = (int)i; }
+        }
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        record_tuned_shape(p, G, cand[bi].first, cand[bi].second, best);
+        if (best_slices) *best_slices = cand[bi].first;
+        if (best_unroll) *best_unroll = cand[bi].second;
+        if (best_ms) *best_ms = best;
+        return check_cuda(cudaGetLastError(), "autotune");
     });
 }
 

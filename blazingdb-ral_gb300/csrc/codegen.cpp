@@ -382,8 +382,8 @@ GeneratedKernel generate_eval_kernel(const Program& p, const Shape& s) {
         os << "            ral_stg<" << element_ctype(p.out_dtypes[o]) << ", RAL_G>(pout" << o << ", r, b" << o << ");\n";
     os << "        }\n";
     if (NOV > 0) {
-        os << "        if (lane < RAL_G * RAL_J) {\n";
-        os << "            const ral_i64 w = (base >> 5) + lane;\n";
+        os << "        for (int wl = lane; wl < RAL_G * RAL_J; wl += 32) {\n";
+        os << "            const ral_i64 w = (base >> 5) + wl;\n";
         os << "            ral_u32 vo[" << NOV << "]; ral_vword(P, w, vo);\n";
         for (int i = 0; i < NOV; i++) os << "            pvo" << i << "[w] = vo[" << i << "]; vcnt[" << i << "] += __popc(vo[" << i << "]);\n";
         os << "        }\n";
@@ -857,6 +857,178 @@ GeneratedKernel generate_filter_kernel(const FilterSpec& f, const Shape& s) {
         os << "        if (lane == 0 && v) atomicAdd((unsigned long long*)(scratch + 3 + vmap[i]), (unsigned long long)v);\n";
         os << "    }\n";
     }
+    os << "}\n";
+    gk.source = os.str();
+    return gk;
+}
+
+GeneratedKernel generate_batch_item(const Program& p, const Shape& sh) {
+    GeneratedKernel gk;
+    gk.shape = sh;
+    gk.layout = make_layout(p, 0);
+    const ParamLayout& L = gk.layout;
+    std::ostringstream key;
+    key << "item|" << p.structure_key() << "#" << sh.G << "/" << sh.J << "/" << sh.unroll;
+    char hex[32];
+    snprintf(hex, sizeof hex, "%016llx", (unsigned long long)fnv1a(key.str()));
+    gk.name = std::string("ral_item_") + hex;
+    const std::string sfx = hex;
+
+    std::ostringstream os;
+    os << "// generated: one warp tile of a batched program\n";
+    os << "struct RalParams { ral_u64 s[" << L.total << "]; };\n\n";
+    const auto ref = p.inputs_referenced();
+    const auto raw = p.inputs_raw_valid();
+    const auto fk = final_kinds(p, L);
+    std::vector<int> vouts;
+    for (int o = 0; o < p.n_out; o++)
+        if (p.out_has_valid[o]) vouts.push_back(o);
+    const int NOV = (int)vouts.size();
+    emit_row_function(os, p, L, ("ral_row_" + sfx).c_str());
+    if (NOV > 0) {
+        os << "RAL_FI void ral_vword_" << sfx << "(const RalParams& P, const ral_i64 w, ral_u32* vo) {\n";
+        ValidEmitter ve(p);
+        ve.emit(os, "    ", [&](int c) {
+            return "__ldg(((const ral_u32*)P.s[" + std::to_string(L.in_valid + c) + "]) + w)";
+        });
+        for (int i = 0; i < NOV; i++) os << "    vo[" << i << "] = " << ve.name[p.final_pos[vouts[i]]] << ";\n";
+        os << "}\n";
+    }
+    // one warp tile of this program
+    os << "extern \"C\" __device__ __noinline__ void " << gk.name
+       << "(const ral_u64* __restrict__ slots, const ral_i64 t) {\n";
+    os << "    const RalParams& P = *reinterpret_cast<const RalParams*>(slots);\n";
+    os << "    const int G = " << sh.G << ", J = " << sh.J << ";\n";
+    os << "    const int lane = threadIdx.x & 31;\n";
+    os << "    const ral_i64 n = (ral_i64)P.s[" << L.n_rows << "];\n";
+    for (int c = 0; c < p.n_in; c++) {
+        if (ref[c])
+            os << "    const " << element_ctype(p.inputs[c].dtype) << "* __restrict__ pin" << c << " = (const "
+               << element_ctype(p.inputs[c].dtype) << "*)P.s[" << L.in_data + c << "];\n";
+        if (raw[c] && p.inputs[c].has_valid)
+            os << "    const ral_u32* __restrict__ pvr" << c << " = (const ral_u32*)P.s[" << L.in_valid + c << "];\n";
+    }
+    for (int o = 0; o < p.n_out; o++)
+        os << "    " << element_ctype(p.out_dtypes[o]) << "* __restrict__ pout" << o << " = ("
+           << element_ctype(p.out_dtypes[o]) << "*)P.s[" << L.out_data + o << "];\n";
+    for (int i = 0; i < NOV; i++)
+        os << "    ral_u32* __restrict__ pvo" << i << " = (ral_u32*)P.s[" << L.out_valid + vouts[i] << "];\n";
+    os << "    const ral_i64 TILE = 32 * G * J;\n";
+    os << "    const ral_i64 base = t * TILE;\n";
+    os << "    if (base + TILE <= n) {\n";
+    os << "#pragma unroll " << std::max(1, std::min(sh.unroll, sh.J)) << "\n        for (int j = 0; j < J; ++j) {\n";
+    os << "            const ral_i64 r = base + (ral_i64)j * 32 * G + lane * G;\n";
+    for (int c = 0; c < p.n_in; c++) {
+        if (!ref[c]) continue;
+        const char* et = element_ctype(p.inputs[c].dtype);
+        os << "            " << et << " a" << c << "[" << sh.G << "]; ral_ldg<" << et << ", " << sh.G << ">(pin" << c
+           << ", r, a" << c << ");\n";
+    }
+    for (int c = 0; c < p.n_in; c++) {
+        if (!raw[c]) continue;
+        if (p.inputs[c].has_valid) os << "            const ral_u32 rw" << c << " = __ldg(pvr" << c << " + (r >> 5));\n";
+        else os << "            const ral_u32 rw" << c << " = 0xffffffffu;\n";
+    }
+    for (int o = 0; o < p.n_out; o++)
+        os << "            " << element_ctype(p.out_dtypes[o]) << " b" << o << "[" << sh.G << "];\n";
+    os << "#pragma unroll\n            for (int g = 0; g < G; ++g) {\n";
+    for (int o = 0; o < p.n_out; o++) os << "                " << kind_ctype(fk[o]) << " y" << o << ";\n";
+    os << "                ral_row_" << sfx << "(P";
+    for (int c = 0; c < p.n_in; c++)
+        if (ref[c]) os << ", " << widen("a" + std::to_string(c) + "[g]", p.inputs[c].dtype);
+    for (int c = 0; c < p.n_in; c++)
+        if (raw[c]) os << ", (rw" << c << " >> ((int)(r & 31) + g)) & 1u";
+    for (int o = 0; o < p.n_out; o++) os << ", y" << o;
+    os << ");\n";
+    for (int o = 0; o < p.n_out; o++)
+        os << "                b" << o << "[g] = " << narrow("y" + std::to_string(o), fk[o], p.out_dtypes[o]) << ";\n";
+    os << "            }\n";
+    for (int o = 0; o < p.n_out; o++)
+        os << "            ral_stg<" << element_ctype(p.out_dtypes[o]) << ", " << sh.G << ">(pout" << o << ", r, b" << o << ");\n";
+    os << "        }\n";
+    if (NOV > 0) {
+        os << "        for (int wl = lane; wl < G * J; wl += 32) {\n";
+        os << "            const ral_i64 w = (base >> 5) + wl;\n";
+        os << "            ral_u32 vo[" << NOV << "]; ral_vword_" << sfx << "(P, w, vo);\n";
+        for (int i = 0; i < NOV; i++) os << "            pvo" << i << "[w] = vo[" << i << "];\n";
+        os << "        }\n";
+    }
+    os << "    } else {\n";
+    os << "        for (ral_i64 r = base + lane; r < n; r += 32) {\n";
+    for (int c = 0; c < p.n_in; c++) {
+        if (!raw[c]) continue;
+        if (p.inputs[c].has_valid) os << "            const ral_u32 rw" << c << " = __ldg(pvr" << c << " + (r >> 5));\n";
+        else os << "            const ral_u32 rw" << c << " = 0xffffffffu;\n";
+    }
+    for (int o = 0; o < p.n_out; o++) os << "            " << kind_ctype(fk[o]) << " y" << o << ";\n";
+    os << "            ral_row_" << sfx << "(P";
+    for (int c = 0; c < p.n_in; c++)
+        if (ref[c]) os << ", " << widen("pin" + std::to_string(c) + "[r]", p.inputs[c].dtype);
+    for (int c = 0; c < p.n_in; c++)
+        if (raw[c]) os << ", (rw" << c << " >> (int)(r & 31)) & 1u";
+    for (int o = 0; o < p.n_out; o++) os << ", y" << o;
+    os << ");\n";
+    for (int o = 0; o < p.n_out; o++)
+        os << "            pout" << o << "[r] = " << narrow("y" + std::to_string(o), fk[o], p.out_dtypes[o]) << ";\n";
+    os << "        }\n";
+    if (NOV > 0) {
+        os << "        const ral_i64 wend = (n + 31) >> 5;\n";
+        os << "        for (ral_i64 w = (base >> 5) + lane; w < wend; w += 32) {\n";
+        os << "            ral_u32 vo[" << NOV << "]; ral_vword_" << sfx << "(P, w, vo);\n";
+        for (int i = 0; i < NOV; i++) os << "            pvo" << i << "[w] = vo[" << i << "];\n";
+        os << "        }\n";
+    }
+    os << "    }\n";
+    os << "}\n\n";
+    gk.source = os.str();
+    return gk;
+}
+
+GeneratedKernel generate_batch_dispatch(const std::vector<std::string>& item_names) {
+    GeneratedKernel gk;
+    std::ostringstream key;
+    key << "dispatch|";
+    for (const auto& n : item_names) key << n << ";";
+    char hex[32];
+    snprintf(hex, sizeof hex, "%016llx", (unsigned long long)fnv1a(key.str()));
+    gk.name = std::string("ral_batch_") + hex;
+    const int NF = (int)item_names.size();
+    std::ostringstream os;
+    os << "// generated: persistent dispatcher over " << NF << " item functions\n";
+    for (const auto& n : item_names)
+        os << "extern \"C\" __device__ void " << n << "(const ral_u64* __restrict__ slots, const ral_i64 t);\n";
+    os << "#define RAL_BATCH_GRAB 8\n";
+    // dynamic shared memory: item prefix (n_programs + 1 long longs), then one function index per program
+    os << "extern \"C\" __global__ void __launch_bounds__(256) " << gk.name
+       << "(const ral_u64* __restrict__ descs, const int stride, const long long* __restrict__ item_prefix, "
+          "const int* __restrict__ fn_index, const int np, unsigned int* counter, const long long total_items) {\n";
+    os << "    extern __shared__ long long s_prefix[];\n";
+    os << "    int* s_fn = reinterpret_cast<int*>(s_prefix + np + 1);\n";
+    os << "    for (int i = threadIdx.x; i <= np; i += blockDim.x) s_prefix[i] = item_prefix[i];\n";
+    os << "    for (int i = threadIdx.x; i < np; i += blockDim.x) s_fn[i] = fn_index[i];\n";
+    os << "    __syncthreads();\n";
+    os << "    const int lane = threadIdx.x & 31;\n";
+    os << "    for (;;) {\n";
+    os << "        unsigned int got = 0;\n";
+    os << "        if (lane == 0) got = atomicAdd(counter, (unsigned int)RAL_BATCH_GRAB);\n";
+    os << "        const long long first = (long long)__shfl_sync(0xffffffffu, got, 0);\n";
+    os << "        if (first >= total_items) break;\n";
+    os << "        const long long last = first + RAL_BATCH_GRAB < total_items ? first + RAL_BATCH_GRAB : total_items;\n";
+    os << "        int lo = 0;\n";
+    os << "        for (long long item = first; item < last; ++item) {\n";
+    // largest q with s_prefix[q] <= item; items of one grab are consecutive, so start from the last q
+    os << "            if (s_prefix[lo + 1] <= item) {\n";
+    os << "                int hi = np;\n";
+    os << "                while (hi - lo > 1) { const int mid = (lo + hi) >> 1; if (s_prefix[mid] <= item) lo = mid; else hi = mid; }\n";
+    os << "            }\n";
+    os << "            const ral_u64* slots = descs + (size_t)lo * stride;\n";
+    os << "            const ral_i64 t = item - s_prefix[lo];\n";
+    os << "            switch (s_fn[lo]) {\n";
+    for (int f = 0; f < NF; f++) os << "            case " << f << ": " << item_names[f] << "(slots, t); break;\n";
+    os << "            default: break;\n";
+    os << "            }\n";
+    os << "        }\n";
+    os << "    }\n";
     os << "}\n";
     gk.source = os.str();
     return gk;

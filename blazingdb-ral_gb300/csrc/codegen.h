@@ -51,6 +51,20 @@ struct GeneratedKernel {
     std::vector<int> layout_project_lscalar, layout_project_rscalar;
 };
 
+// Batched and served launches run many programs in one persistent kernel.  Each program's warp
+// tile is a relocatable device function of its own, compiled once per program structure and
+// shape and cached:
+//   extern "C" __device__ void <name>(const ral_u64* slots, long long tile)
+// with slots laid out as gk.layout.  A dispatcher kernel, linked with the item functions, takes
+// work items (program, tile) from a device counter in chunks, finds the program by binary search
+// over the item prefix (in shared memory) and calls its function:
+//   <name>(const ral_u64* descs, int stride, const long long* item_prefix, const int* fn_index,
+//          int n_programs, unsigned int* counter, long long total_items)
+// descs holds `stride` slots per program; fn_index[q] indexes item_names.  Dynamic shared memory:
+// (n_programs + 1) * 8 + n_programs * 4 bytes.
+GeneratedKernel generate_batch_item(const Program& p, const Shape& s);
+GeneratedKernel generate_batch_dispatch(const std::vector<std::string>& item_names);
+
 // perform_operation: evaluate the program over n rows into the outputs.
 GeneratedKernel generate_eval_kernel(const Program& p, const Shape& s);
 

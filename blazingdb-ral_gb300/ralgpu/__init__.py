@@ -10,7 +10,8 @@ library is missing the import of the first entry point raises.
 from .capi import (RalError, lib, perform_operation, perform_operation_async, evaluate_expression,
                    process_filter, execute_project_plan, filter_project, project_output_types,
                    materialize_column, apply_boolean_mask, add_expression_to_plan, get_output_type_expression,
-                   debug_program_source, debug_filter_source, jit_stats, kernel_launches, version)
+                   debug_program_source, debug_filter_source, jit_stats, kernel_launches, version,
+                   parse_project_plan, Batch, autotune_program, batch_tune_key)
 from .column import Column, Scalar, valid_alloc_size
 from . import dtypes
 
@@ -18,5 +19,6 @@ __all__ = [
     "RalError", "lib", "perform_operation", "perform_operation_async", "evaluate_expression",
     "process_filter", "execute_project_plan", "filter_project", "project_output_types",
     "materialize_column", "apply_boolean_mask", "add_expression_to_plan", "get_output_type_expression",
-    "debug_program_source", "debug_filter_source", "jit_stats", "kernel_launches", "version", "Column", "Scalar", "valid_alloc_size", "dtypes",
+    "debug_program_source", "debug_filter_source", "jit_stats", "kernel_launches", "version", "Column", "Scalar",
+    "valid_alloc_size", "dtypes", "parse_project_plan", "Batch", "autotune_program", "batch_tune_key",
 ]

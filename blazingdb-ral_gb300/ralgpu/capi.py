@@ -48,6 +48,21 @@ _SIGS = {
                                           C.c_int64, C.c_char_p, C.c_int64]),
     "ral_jit_stats": (C.c_int, [C.POINTER(C.c_int64), C.POINTER(C.c_int64), C.POINTER(C.c_int64),
                                 C.POINTER(C.c_double)]),
+    "ral_parse_project_plan": (C.c_int, [I32P, C.c_int32, C.c_char_p, C.c_int32, C.c_int32, I32P, I32P, I32P, I32P,
+                                         I32P, I16P, I16P, I16P, I16P, I32P, I32P, SCP, SCP]),
+    "ral_batch_create": (C.c_int, [C.POINTER(C.c_void_p)]),
+    "ral_batch_add": (C.c_int, [P, COLPP, C.c_int32, COLPP, C.c_int32, I16P, I16P, I16P, C.c_int32, I16P, I32P, I32P,
+                                SCP, SCP, I32P]),
+    "ral_batch_prepare": (C.c_int, [P]),
+    "ral_batch_run": (C.c_int, [P, P, C.c_int32]),
+    "ral_batch_info": (C.c_int, [P, I32P, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),
+    "ral_batch_debug_source": (C.c_int, [P, C.c_int32, C.c_char_p, C.c_int64, C.c_char_p, C.c_int64]),
+    "ral_batch_destroy": (C.c_int, [P]),
+    "ral_batch_kernel_info": (C.c_int, [P, I32P, I32P, I32P]),
+    "ral_batch_tune_key": (C.c_int, [COLPP, C.c_int32, COLPP, C.c_int32, I16P, I16P, I16P, C.c_int32, I16P, I32P, I32P,
+                                     SCP, SCP, C.c_char_p, C.c_int64]),
+    "ral_autotune_program": (C.c_int, [COLPP, C.c_int32, COLPP, C.c_int32, I16P, I16P, I16P, C.c_int32, I16P, I32P,
+                                       I32P, SCP, SCP, I32P, I32P, C.POINTER(C.c_double)]),
 }
 
 
@@ -346,3 +361,128 @@ def jit_stats() -> dict:
     a, b, c, d = C.c_int64(), C.c_int64(), C.c_int64(), C.c_double()
     lib().ral_jit_stats(C.byref(a), C.byref(b), C.byref(c), C.byref(d))
     return dict(compiles=a.value, disk_hits=b.value, memory_hits=c.value, compile_ms=d.value)
+
+
+def _stream_handle(stream) -> int:
+    import torch
+    if stream is None:
+        return torch.cuda.current_stream().cuda_stream
+    if isinstance(stream, int):
+        return stream
+    return stream.cuda_stream
+
+
+def parse_project_plan(frame_dtypes: Sequence[int], query_part: str) -> dict:
+    """parse_project_plan (src/CalciteInterpreter.cpp:123-309): the register program of a LogicalProject.
+
+    Returns the frame columns the program reads (dense input order), the dtype of each evaluated
+    expression and the op arrays (final positions are output registers n_in + k)."""
+    fd = _i32(frame_dtypes)
+    cap_ops, cap_cols = 4096, 1024
+    nin, nev, nops = C.c_int32(0), C.c_int32(0), C.c_int32(0)
+    inc = np.zeros(cap_cols, dtype=np.int32)
+    edt = np.zeros(cap_cols, dtype=np.int32)
+    l, r, o, f = (np.zeros(cap_ops, dtype=np.int16) for _ in range(4))
+    b, u = np.zeros(cap_ops, dtype=np.int32), np.zeros(cap_ops, dtype=np.int32)
+    ls, rs = (GdfScalar * cap_ops)(), (GdfScalar * cap_ops)()
+    _check(lib().ral_parse_project_plan(_p32(fd), len(fd), query_part.encode(), cap_ops, cap_cols, C.byref(nin),
+                                        _p32(inc), C.byref(nev), _p32(edt), C.byref(nops), _p16(l), _p16(r),
+                                        _p16(o), _p16(f), _p32(b), _p32(u), ls, rs))
+    k = nops.value
+    return dict(input_columns=inc[:nin.value].tolist(), evaluated_dtypes=edt[:nev.value].tolist(),
+                left=l[:k].tolist(), right=r[:k].tolist(), outputs=o[:k].tolist(),
+                final_output_positions=f[:nev.value].tolist(), operators=b[:k].tolist(),
+                unary_operators=u[:k].tolist(), left_scalars=[Scalar.from_c(ls[i]) for i in range(k)],
+                right_scalars=[Scalar.from_c(rs[i]) for i in range(k)])
+
+
+class Batch:
+    """Many register programs run by one persistent kernel, replayed as a CUDA graph.
+
+    add() takes perform_operation's arguments; the column descriptors are copied, so the
+    buffers must stay allocated (and in place) for the life of the batch.  run() evaluates
+    every program once, asynchronously on the given stream."""
+
+    def __init__(self):
+        h = C.c_void_p()
+        _check(lib().ral_batch_create(C.byref(h)))
+        self._h = h
+        self._keep = []
+
+    def add(self, output_columns: List[Column], input_columns: List[Column], left_inputs, right_inputs, outputs,
+            final_output_positions, operators, unary_operators, left_scalars, right_scalars) -> int:
+        oa, os_ = _colarray(output_columns)
+        ia, is_ = _colarray(input_columns)
+        l, r, o, f = _i16(left_inputs), _i16(right_inputs), _i16(outputs), _i16(final_output_positions)
+        b, u = _i32(operators), _i32(unary_operators)
+        ls = _scalars([_as_scalar(s) for s in left_scalars])
+        rs = _scalars([_as_scalar(s) for s in right_scalars])
+        idx = C.c_int32(-1)
+        _check(lib().ral_batch_add(self._h, oa, len(output_columns), ia, len(input_columns), _p16(l), _p16(r),
+                                   _p16(o), len(l), _p16(f), _p32(b), _p32(u), ls, rs, C.byref(idx)))
+        self._keep.append((list(output_columns), list(input_columns)))
+        return idx.value
+
+    def prepare(self) -> None:
+        _check(lib().ral_batch_prepare(self._h))
+
+    def run(self, stream=None, use_graph: bool = True) -> None:
+        _check(lib().ral_batch_run(self._h, C.c_void_p(_stream_handle(stream)), 1 if use_graph else 0))
+
+    def info(self) -> dict:
+        n, rows, items = C.c_int32(0), C.c_int64(0), C.c_int64(0)
+        _check(lib().ral_batch_info(self._h, C.byref(n), C.byref(rows), C.byref(items)))
+        regs, grid, per_sm = C.c_int32(0), C.c_int32(0), C.c_int32(0)
+        _check(lib().ral_batch_kernel_info(self._h, C.byref(regs), C.byref(grid), C.byref(per_sm)))
+        return dict(programs=n.value, rows=rows.value, work_items=items.value, registers=regs.value,
+                    grid=grid.value, blocks_per_sm=per_sm.value)
+
+    def debug_source(self, compile: bool = False) -> Tuple[str, str]:
+        src = C.create_string_buffer(1 << 24)
+        log = C.create_string_buffer(1 << 16)
+        _check(lib().ral_batch_debug_source(self._h, 1 if compile else 0, src, len(src), log, len(log)))
+        return src.value.decode(), log.value.decode()
+
+    def close(self) -> None:
+        if self._h:
+            lib().ral_batch_destroy(self._h)
+            self._h = None
+            self._keep = []
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def batch_tune_key(output_columns: List[Column], input_columns: List[Column], left_inputs, right_inputs, outputs,
+                   final_output_positions, operators, unary_operators, left_scalars, right_scalars) -> str:
+    """The autotuner's table key of a program (dtype mix and program length)."""
+    oa, _os = _colarray(output_columns)
+    ia, _is = _colarray(input_columns)
+    l, r, o, f = _i16(left_inputs), _i16(right_inputs), _i16(outputs), _i16(final_output_positions)
+    b, u = _i32(operators), _i32(unary_operators)
+    ls = _scalars([_as_scalar(s) for s in left_scalars])
+    rs = _scalars([_as_scalar(s) for s in right_scalars])
+    key = C.create_string_buffer(256)
+    _check(lib().ral_batch_tune_key(oa, len(output_columns), ia, len(input_columns), _p16(l), _p16(r), _p16(o),
+                                    len(l), _p16(f), _p32(b), _p32(u), ls, rs, key, len(key)))
+    return key.value.decode()
+
+
+def autotune_program(output_columns: List[Column], input_columns: List[Column], left_inputs, right_inputs, outputs,
+                     final_output_positions, operators, unary_operators, left_scalars,
+                     right_scalars) -> Tuple[int, int, float]:
+    """Times the program as a one-program batch at each candidate tile shape and records the
+    best in the autotuner's table (used by batches); returns (slices, unroll, ms per launch)."""
+    oa, _os = _colarray(output_columns)
+    ia, _is = _colarray(input_columns)
+    l, r, o, f = _i16(left_inputs), _i16(right_inputs), _i16(outputs), _i16(final_output_positions)
+    b, u = _i32(operators), _i32(unary_operators)
+    ls = _scalars([_as_scalar(s) for s in left_scalars])
+    rs = _scalars([_as_scalar(s) for s in right_scalars])
+    J, U, ms = C.c_int32(0), C.c_int32(0), C.c_double(0)
+    _check(lib().ral_autotune_program(oa, len(output_columns), ia, len(input_columns), _p16(l), _p16(r), _p16(o),
+                                      len(l), _p16(f), _p32(b), _p32(u), ls, rs, C.byref(J), C.byref(U), C.byref(ms)))
+    return J.value, U.value, ms.value

@@ -13,9 +13,14 @@ dataset for this path, so every input is seeded synthetic data.
   filter_gather 500M rows: int32 U[0,10000), int64, float32, float64, date32,
                bool8; predicate <($0, T) with T = 100 / 5000 / 9900 for
                selectivity 1% / 50% / 99%; every column gathered
+  batched      256 programs of 4-48 operators (uniform over arithmetic /
+               compare / logical / unary), each over its own table of
+               log-uniform [1e3, 5e7] rows and 2-8 int32/int64/float32/float64
+               columns with 0-20% nulls
 """
 from __future__ import annotations
 
+import math
 from dataclasses import dataclass, field
 from typing import List, Optional
 
@@ -183,3 +188,114 @@ def filter_gather_device(n: int, seed: int = SEED, device="cuda", null_rate: Opt
             valid, nulls = random_valid_mask(n, null_rate, g, device)
             out.append((t, v, valid, nulls))
     return out
+
+
+# ---- batched: many independent programs over uneven tables ---------------------------------
+
+BATCH_DTYPES = [D.GDF_INT32, D.GDF_INT64, D.GDF_FLOAT32, D.GDF_FLOAT64]
+BATCH_ARITH = ["+", "-", "*", "/", "MOD"]
+BATCH_COMPARE = ["=", "<>", "<", ">", "<=", ">="]
+BATCH_LOGICAL = ["AND", "OR", "NOT"]
+BATCH_UNARY = ["FLOOR", "CEIL", "ABS", "SIN", "COS", "IS NULL", "IS NOT NULL"]
+
+
+@dataclass
+class BatchTable:
+    """One program of the batched mix: its table shape and its LogicalProject text."""
+    rows: int
+    dtypes: List[int]
+    null_rates: List[float]
+    project: str
+    n_ops: int
+    seed: int
+
+
+def random_rex(rng, k: int, n_cols: int, literal_ok: bool = True) -> str:
+    """A RexNode call tree with exactly k operators; the category of each operator is uniform
+    over arithmetic / compare / logical / unary.  Every operator has a column below it: the
+    emitter takes no unary operator on a literal and no binary operator on two literals."""
+    if k == 0:
+        if literal_ok and rng.random() < 0.2:
+            return str(int(rng.integers(1, 100))) if rng.random() < 0.5 else f"{rng.integers(1, 400) / 4.0:.2f}"
+        return f"${int(rng.integers(0, n_cols))}"
+    cat = int(rng.integers(0, 4))
+    if cat == 3 or (cat == 2 and rng.random() < 1 / 3):
+        op = "NOT" if cat == 2 else BATCH_UNARY[int(rng.integers(0, len(BATCH_UNARY)))]
+        if op.startswith("IS ") and k > 1:
+            # the VM tests the mask of an input column, not of an intermediate register
+            op = BATCH_UNARY[int(rng.integers(0, len(BATCH_UNARY) - 2))]
+        return f"{op}({random_rex(rng, k - 1, n_cols, False)})"
+    ops = BATCH_ARITH if cat == 0 else BATCH_COMPARE if cat == 1 else ["AND", "OR"]
+    op = ops[int(rng.integers(0, len(ops)))]
+    kl = int(rng.integers(0, k))
+    left = random_rex(rng, kl, n_cols)
+    right = random_rex(rng, k - 1 - kl, n_cols, not (kl == 0 and not left.startswith("$")))
+    return f"{op}({left}, {right})"
+
+
+def batched_mix(n_programs: int = 256, seed: int = SEED, min_rows: float = 1e3, max_rows: float = 5e7,
+                min_ops: int = 4, max_ops: int = 48) -> List[BatchTable]:
+    """The batched workload: each program runs over its own table with a log-uniform row count,
+    2-8 columns drawn from int32/int64/float32/float64 with 0-20% nulls, and 4-48 operators
+    split over 1-3 projected expressions."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for q in range(n_programs):
+        rows = int(round(math.exp(rng.uniform(math.log(min_rows), math.log(max_rows)))))
+        nc = int(rng.integers(2, 9))
+        dts = [BATCH_DTYPES[int(i)] for i in rng.integers(0, len(BATCH_DTYPES), nc)]
+        nr = [float(rng.uniform(0.0, 0.2)) for _ in range(nc)]
+        n_ops = int(rng.integers(min_ops, max_ops + 1))
+        n_expr = int(rng.integers(1, min(3, n_ops) + 1))
+        cuts = sorted(rng.choice(np.arange(1, n_ops), n_expr - 1, replace=False).tolist()) if n_expr > 1 else []
+        parts = np.diff([0] + cuts + [n_ops]).tolist()
+        exprs = [random_rex(rng, int(k), nc) for k in parts]
+        project = "LogicalProject(" + ", ".join(f"e{i}=[{e}]" for i, e in enumerate(exprs)) + ")"
+        out.append(BatchTable(rows, dts, nr, project, n_ops, int(rng.integers(0, 2**31))))
+    return out
+
+
+def _batch_values_np(rng, dtype: int, n: int) -> np.ndarray:
+    if dtype == D.GDF_INT32:
+        return rng.integers(-1000, 1000, n, dtype=np.int32)
+    if dtype == D.GDF_INT64:
+        return rng.integers(-(1 << 20), 1 << 20, n, dtype=np.int64)
+    if dtype == D.GDF_FLOAT32:
+        return rng.uniform(-100, 100, n).astype(np.float32)
+    return rng.normal(0.0, 100.0, n)
+
+
+def batched_table_host(t: BatchTable, rows: Optional[int] = None):
+    """Host columns of one table: list of (dtype, values, valid bools or None)."""
+    rng = np.random.default_rng(t.seed)
+    n = t.rows if rows is None else rows
+    cols = []
+    for dt, nr in zip(t.dtypes, t.null_rates):
+        v = _batch_values_np(rng, dt, n)
+        valid = rng.random(n) >= nr if nr > 0 else None
+        cols.append((dt, v, valid))
+    return cols
+
+
+def batched_table_device(t: BatchTable, device="cuda"):
+    """Device columns of one table: list of (dtype, tensor, packed mask or None, null count)."""
+    import torch
+    g = torch.Generator(device=device)
+    g.manual_seed(t.seed)
+    n = t.rows
+    cols = []
+    for dt, nr in zip(t.dtypes, t.null_rates):
+        if dt == D.GDF_INT32:
+            v = torch.randint(-1000, 1000, (n,), generator=g, device=device, dtype=torch.int32)
+        elif dt == D.GDF_INT64:
+            v = torch.randint(-(1 << 20), 1 << 20, (n,), generator=g, device=device, dtype=torch.int64)
+        elif dt == D.GDF_FLOAT32:
+            v = torch.rand(n, generator=g, device=device, dtype=torch.float32) * 200 - 100
+        else:
+            v = torch.randn(n, generator=g, device=device, dtype=torch.float64) * 100
+        if nr > 0:
+            valid, nulls = random_valid_mask(n, nr, g, device)
+        else:
+            valid, nulls = None, 0
+        cols.append((dt, v, valid, nulls))
+    return cols

@@ -111,6 +111,21 @@ int ral_execute_project_plan(gdf_column *const *frame_columns, int32_t num_colum
                              gdf_column *const *out_columns, int32_t num_out_columns);
 
 /*
+ * parse_project_plan — src/CalciteInterpreter.cpp:123-309 (project_plan_params,
+ * src/CalciteInterpreter.h:17-32): the program of a LogicalProject over a frame of the given
+ * dtypes.  Receives the frame columns the program reads (dense order), the dtype of each
+ * evaluated expression and the op arrays; arrays have room for capacity_ops ops and
+ * capacity_cols columns / expressions.
+ */
+int ral_parse_project_plan(const gdf_dtype *frame_dtypes, int32_t num_columns, const char *query_part,
+                           int32_t capacity_ops, int32_t capacity_cols, int32_t *num_input_columns,
+                           int32_t *input_columns, int32_t *num_evaluated, gdf_dtype *evaluated_dtypes,
+                           int32_t *num_operations, column_index_type *left_inputs, column_index_type *right_inputs,
+                           column_index_type *outputs, column_index_type *final_output_positions,
+                           int32_t *operators, int32_t *unary_operators, gdf_scalar *left_scalars,
+                           gdf_scalar *right_scalars);
+
+/*
  * LogicalFilter followed by LogicalProject, fused (the plan shape
  * "LogicalProject(...)\n  LogicalFilter(condition=[...])", evaluated by
  * CalciteInterpreter.cpp:719-723 as process_filter then execute_project_plan).
@@ -189,6 +204,63 @@ int ral_debug_program_source(const gdf_dtype *input_dtypes, const int32_t *input
                              const int32_t *unary_operators, const gdf_scalar *left_scalars,
                              const gdf_scalar *right_scalars, int32_t compile, char *source_out,
                              int64_t source_capacity, char *log_out, int64_t log_capacity);
+
+/*
+ * Batched execution — no single reference counterpart: the reference runs each program as its
+ * own perform_operation call.  A batch holds many perform_operation calls (each over its own
+ * columns) and runs them all in ONE persistent kernel whose warps pull (program, row-tile)
+ * work items from a device counter; the launch is captured once in a CUDA graph and replayed.
+ * Column descriptors are copied at add time; their buffers must stay allocated and in place.
+ * Results are identical to calling ral_perform_operation on each program.
+ */
+typedef struct ral_batch_s ral_batch;
+int ral_batch_create(ral_batch **batch);
+/* Adds one program with perform_operation's arguments; *program_index receives its index. */
+int ral_batch_add(ral_batch *batch, gdf_column *const *output_columns, int32_t num_outputs,
+                  gdf_column *const *input_columns, int32_t num_inputs, const column_index_type *left_inputs,
+                  const column_index_type *right_inputs, const column_index_type *outputs, int32_t num_operations,
+                  const column_index_type *final_output_positions, const int32_t *operators,
+                  const int32_t *unary_operators, const gdf_scalar *left_scalars, const gdf_scalar *right_scalars,
+                  int32_t *program_index);
+/* Picks launch shapes (autotuner table), compiles the batch kernel, uploads work
+ * descriptors and captures the CUDA graph.  Optional: ral_batch_run prepares on first use. */
+int ral_batch_prepare(ral_batch *batch);
+/* Runs every program once on `stream` (NULL: per-thread default stream); use_graph = 0
+ * launches the kernel directly instead of replaying the graph.  Asynchronous. */
+int ral_batch_run(ral_batch *batch, void *stream, int32_t use_graph);
+int ral_batch_info(const ral_batch *batch, int32_t *num_programs, int64_t *total_rows, int64_t *work_items);
+int ral_batch_destroy(ral_batch *batch);
+/* Registers per thread, grid and resident blocks per SM of the prepared batch kernel (0 before
+ * ral_batch_prepare). */
+int ral_batch_kernel_info(const ral_batch *batch, int32_t *registers, int32_t *grid, int32_t *blocks_per_sm);
+/* Generated source of the batch kernel for the programs added so far (and an NVRTC-only
+ * compile when compile != 0); needs no GPU. */
+int ral_batch_debug_source(const ral_batch *batch, int32_t compile, char *source_out, int64_t source_capacity,
+                           char *log_out, int64_t log_capacity);
+
+/* The autotuner's table key of a perform_operation program (dtype mix and program length). */
+int ral_batch_tune_key(gdf_column *const *output_columns, int32_t num_outputs, gdf_column *const *input_columns,
+                       int32_t num_inputs, const column_index_type *left_inputs, const column_index_type *right_inputs,
+                       const column_index_type *outputs, int32_t num_operations,
+                       const column_index_type *final_output_positions, const int32_t *operators,
+                       const int32_t *unary_operators, const gdf_scalar *left_scalars, const gdf_scalar *right_scalars,
+                       char *key_out, int64_t key_capacity);
+
+/*
+ * Autotuner: runs the perform_operation program as a one-program batch at each candidate tile
+ * shape (rows per warp tile 32*G*J for J in 2, 4, 8, 16; slice loop unrolled 1 or 2 times),
+ * times it and records the fastest in the tuning table (keyed by dtype mix and program length;
+ * persisted as JSON in the JIT cache directory), which batches consult.  Writes the program's
+ * outputs as a side effect.  *best_slices / *best_unroll receive the chosen shape and *best_ms
+ * its kernel time.
+ */
+int ral_autotune_program(gdf_column *const *output_columns, int32_t num_outputs, gdf_column *const *input_columns,
+                         int32_t num_inputs, const column_index_type *left_inputs,
+                         const column_index_type *right_inputs, const column_index_type *outputs,
+                         int32_t num_operations, const column_index_type *final_output_positions,
+                         const int32_t *operators, const int32_t *unary_operators, const gdf_scalar *left_scalars,
+                         const gdf_scalar *right_scalars, int32_t *best_slices, int32_t *best_unroll,
+                         double *best_ms);
 
 /* Generated source of the fused LogicalFilter kernel (optionally NVRTC-compiled, no GPU
  * needed) for a frame described by dtypes and mask presence; project_query_part may be
