@@ -8,6 +8,10 @@ ral_perform_operation_async on HBM-resident columns.  Other workloads:
   --workload batched           256 programs of 4-48 ops over tables of log-uniform [1e3, 5e7] rows,
                                all in one persistent launch replayed as a CUDA graph, against the
                                same 256 programs as plain synchronous perform_operation calls
+  --workload served            Poisson request loop over 24 resident tables (log-uniform [1e4, 1e8]
+                               rows) and 96 prepared filter + project queries of 4-32 ops, at 5
+                               rates, ~50k requests: p50 / p99 latency and rows/s of the served
+                               (continuously batched) loop against serial plain execution
 
 value     rows/s over the timed steps (inputs resident in HBM; every input > L2, so no flush)
 e2e       same metric through the C ABI with host buffers: pinned H2D of the inputs and D2H of
@@ -236,6 +240,27 @@ def cpu_batched(threads: int, n_programs: int, rows_cap: int, seed: int = 202612
                             [fe.Scalar(x.dtype, x.value, x.is_valid) for x in pp["left_scalars"]],
                             [fe.Scalar(x.dtype, x.value, x.is_valid) for x in pp["right_scalars"]], nthreads=threads)
         rows += n
+    return rows, time.perf_counter() - t0
+
+
+def cpu_served(threads: int, n_queries: int, rows_cap: int, seed: int = 20261203):
+    """Oracle filter + project over the first n_queries of the served workload, tables capped at
+    rows_cap rows; returns (rows scanned, seconds)."""
+    import oracle as O
+    from ralgpu import workloads as W
+    tabs = W.served_tables(24, seed=seed)
+    qs = W.served_queries(tabs, 96, seed=seed)[:n_queries]
+    frames = {}
+    for q in qs:
+        if q.table not in frames:
+            host = W.served_table_host(tabs[q.table], rows=min(tabs[q.table].rows, rows_cap))
+            frames[q.table] = [O.make_column(v, t, m) for t, v, m in host]
+    t0 = time.perf_counter()
+    rows = 0
+    for q in qs:
+        f = O.process_filter(frames[q.table], q.filter, nthreads=threads)
+        O.execute_project_plan(f, q.project, nthreads=threads)
+        rows += frames[q.table][0].size
     return rows, time.perf_counter() - t0
 
 
@@ -472,8 +497,9 @@ def run_ours(args):
         dist.destroy_process_group()
 
 
-def batched_setup(n_programs, seed, device):
-    """Device tables, outputs and plans of the batched mix."""
+def batched_setup(n_programs, seed, device, max_rows=0):
+    """Device tables, outputs and plans of the batched mix (tables capped at max_rows when set,
+    for small profiling captures)."""
     import torch
     import ralgpu as R
     from ralgpu import dtypes as D
@@ -482,6 +508,8 @@ def batched_setup(n_programs, seed, device):
     progs = []
     alg = 0
     for t in mix:
+        if max_rows:
+            t.rows = min(t.rows, max_rows)
         pp = R.parse_project_plan(t.dtypes, t.project)
         cols = W.batched_table_device(t, device)
         ins = [R.Column(cols[c][1], cols[c][2], cols[c][0], t.rows, cols[c][3]) for c in pp["input_columns"]]
@@ -505,7 +533,7 @@ def run_batched(args):
     torch.cuda.set_device(local)
     device = f"cuda:{local}"
     t0 = time.perf_counter()
-    progs, alg = batched_setup(args.programs, args.seed, device)
+    progs, alg = batched_setup(args.programs, args.seed, device, args.max_rows)
     rows = sum(p["rows"] for p in progs)
     gen_s = time.perf_counter() - t0
     # autotune: one program per tuning key (dtype mix x program length), timed as a batch item
@@ -552,23 +580,28 @@ def run_batched(args):
     value = world * rows / (ms_per_step / 1e3)
 
     # the same programs as plain per-call launches: one synchronous ral_perform_operation each
-    t0 = time.perf_counter()
-    with cf.ThreadPoolExecutor(max_workers=min(16, os.cpu_count() or 4)) as ex:   # compile the 256 kernels
-        list(ex.map(lambda p: R.perform_operation(p["outs"], p["ins"], *p["args"]), progs))
-    torch.cuda.synchronize()
-    plain_compile_s = time.perf_counter() - t0
-    for p in progs:
-        R.perform_operation(p["outs"], p["ins"], *p["args"])
-    torch.cuda.synchronize()
-    plain_times = []
-    for _ in range(args.plain_steps):
+    plain = None
+    if args.plain_steps > 0:
         t0 = time.perf_counter()
+        with cf.ThreadPoolExecutor(max_workers=min(16, os.cpu_count() or 4)) as ex:   # compile the kernels
+            list(ex.map(lambda p: R.perform_operation(p["outs"], p["ins"], *p["args"]), progs))
+        torch.cuda.synchronize()
+        plain_compile_s = time.perf_counter() - t0
         for p in progs:
             R.perform_operation(p["outs"], p["ins"], *p["args"])
         torch.cuda.synchronize()
-        plain_times.append(time.perf_counter() - t0)
-    plain_s = statistics.median(plain_times)
-    plain_value = world * rows / plain_s
+        plain_times = []
+        for _ in range(args.plain_steps):
+            t0 = time.perf_counter()
+            for p in progs:
+                R.perform_operation(p["outs"], p["ins"], *p["args"])
+            torch.cuda.synchronize()
+            plain_times.append(time.perf_counter() - t0)
+        plain_s = statistics.median(plain_times)
+        plain = {"value": world * rows / plain_s, "unit": "rows/s", "ms_per_step": plain_s * 1e3,
+                 "calls_per_step": len(progs), "steps": args.plain_steps,
+                 "timing": "host clock around synchronous ral_perform_operation calls, one per program",
+                 "first_compile_s": round(plain_compile_s, 2)}
 
     peak, peak_kind = load_peaks()
     achieved = alg / (ms_per_step / 1e3) / 1e9
@@ -579,17 +612,14 @@ def run_batched(args):
         "data": "synthetic (seeded, generated on the GPU)",
         "config": {"workload": "batched", "programs": len(progs), "rows_total": rows, "ops": "4-48 per program",
                    "rows_per_table": "log-uniform [1e3, 5e7]", "columns": "2-8 of int32/int64/f32/f64, 0-20% nulls",
-                   "seed": args.seed, "parallelism": f"replicas x{world}",
+                   "seed": args.seed, "parallelism": f"replicas x{world}", "max_rows": args.max_rows or None,
                    "l2": "inputs of the whole batch (tens of GB) exceed L2; no flush"},
         "batched": {"launch": "one persistent kernel per step, replayed as a CUDA graph",
                     "kernel": info, "ms_per_step": ms_per_step,
                     "prepare_s": round(prep_s, 2), "autotune_s": round(tune_s, 2), "tuned_keys": len(tuned),
                     "generate_s": round(gen_s, 2)},
-        "plain_per_call": {"value": plain_value, "unit": "rows/s", "ms_per_step": plain_s * 1e3,
-                           "calls_per_step": len(progs), "steps": args.plain_steps,
-                           "timing": "host clock around 256 synchronous ral_perform_operation calls",
-                           "first_compile_s": round(plain_compile_s, 2)},
-        "speedup_vs_plain": value / plain_value,
+        "plain_per_call": plain,
+        "speedup_vs_plain": value / plain["value"] if plain else None,
         "hbm_gbs": achieved,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "peak_kind": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else peak_kind,
@@ -615,24 +645,156 @@ def run_batched(args):
         dist.destroy_process_group()
 
 
+def _plain_filter_project_call(R, frame, q):
+    """A synchronous ral_filter_project over a resident table with preallocated outputs; returns
+    a zero-argument callable (the serial plain execution of one request)."""
+    import ctypes as C
+    from ralgpu.capi import _colarray, lib, _check
+    types, evald = R.project_output_types([c.dtype for c in frame], q.project)
+    srcs = R.capi._passthrough_sources(frame, q.project)
+    n = frame[0].size
+    outs = [R.Column.empty(t, n, with_valid=True if e else (srcs[i].valid is not None))
+            for i, (t, e) in enumerate(zip(types, evald))]
+    fa, fs = _colarray(frame)
+    oa, os_ = _colarray(outs)
+    fq, pq = q.filter.encode(), q.project.encode()
+    n_out = C.c_int32(0)
+    keep = (outs, fa, fs, oa, os_)
+
+    def call():
+        _check(lib().ral_filter_project(keep[1], len(frame), fq, pq, keep[3], len(keep[0]), C.byref(n_out)))
+        return n_out.value
+    return call
+
+
+def run_served(args):
+    import numpy as np
+    import torch
+    import ralgpu as R
+    from ralgpu import workloads as W
+    world, rank, local = dist_setup(args)
+    torch.cuda.set_device(local)
+    device = f"cuda:{local}"
+    t0 = time.perf_counter()
+    tabs = W.served_tables(args.tables, seed=args.seed, max_rows=args.max_rows or 1e8)
+    qs = W.served_queries(tabs, args.queries, seed=args.seed)
+    frames = []
+    for t in tabs:
+        cols = W.served_table_device(t, device)
+        frames.append([R.Column(v, m, dt, t.rows, nn) for dt, v, m, nn in cols])
+    torch.cuda.synchronize()
+    gen_s = time.perf_counter() - t0
+    budget = int(args.budget_gb * (1 << 30))
+    srv = R.Server(budget_bytes=budget, max_waves=args.waves, max_wave_requests=1024)
+    tids = [srv.add_table(f) for f in frames]
+    qids = [srv.add_query(tids[q.table], q.filter, q.project) for q in qs]
+    t0 = time.perf_counter()
+    srv.start()
+    start_s = time.perf_counter() - t0
+    q_rows = np.array([tabs[q.table].rows for q in qs], dtype=np.float64)
+
+    # serial plain execution: each query's service time as one synchronous ral_filter_project
+    calls = [_plain_filter_project_call(R, frames[q.table], q) for q in qs]
+    for c in calls:
+        c()
+    torch.cuda.synchronize()
+    service = np.zeros(len(qs))
+    for i, c in enumerate(calls):
+        ts = []
+        for _ in range(3):
+            a = time.perf_counter()
+            c()
+            ts.append(time.perf_counter() - a)
+        service[i] = statistics.median(ts)
+    del calls
+    torch.cuda.empty_cache()
+
+    # warm the served loop, then its capacity: every request of a trace arriving at once
+    n_rate = max(50, args.requests // 5)
+    wq, wa = W.served_trace(min(500, n_rate), 1e9, len(qs), seed=args.seed + 99)
+    srv.run_trace(wq, np.zeros(len(wq)))
+    cq, _ = W.served_trace(min(4000, 2 * n_rate), 1.0, len(qs), seed=args.seed + 7)
+    lat, rows, mk = srv.run_trace(cq, np.zeros(len(cq)))
+    capacity = len(cq) / mk
+    sampler = ClockSampler(local)
+    sampler.start()
+    launches0 = R.kernel_launches()
+    sampler.mark_start()
+    per_rate = []
+    for frac in (0.2, 0.4, 0.6, 0.8, 0.95):
+        rate = frac * capacity
+        tq, ta = W.served_trace(n_rate, rate, len(qs), seed=args.seed + int(frac * 100))
+        lat, rows, mk = srv.run_trace(tq, ta)
+        scanned = float(q_rows[tq].sum())
+        # serial plain execution of the same arrivals: one request at a time, in arrival order
+        done = 0.0
+        slat = np.zeros(len(tq))
+        for k, (qq, a) in enumerate(zip(tq, ta)):
+            done = max(done, a) + service[qq]
+            slat[k] = done - a
+        s_mk = done - ta[0]
+        per_rate.append({
+            "rate_rps": rate, "fraction_of_served_capacity": frac, "requests": int(len(tq)),
+            "served": {"p50_ms": float(np.percentile(lat, 50) * 1e3), "p99_ms": float(np.percentile(lat, 99) * 1e3),
+                       "rows_per_s": scanned / mk, "requests_per_s": len(tq) / mk},
+            "serial_plain": {"p50_ms": float(np.percentile(slat, 50) * 1e3),
+                             "p99_ms": float(np.percentile(slat, 99) * 1e3),
+                             "rows_per_s": scanned / s_mk, "requests_per_s": len(tq) / s_mk},
+        })
+    sampler.mark_end()
+    clocks = sampler.stop()
+    launches = R.kernel_launches() - launches0
+    st = srv.stats()
+    serial_capacity = 1.0 / float(service.mean())
+    top = per_rate[-1]
+    out = {
+        "metric": METRIC, "value": top["served"]["rows_per_s"], "unit": "rows/s", "n_gpus": world,
+        "steps": len(per_rate), "warmup": 1, "ms_per_step": None, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "int32/int64/f32/f64/date32 (VM registers int64/f64)",
+        "data": "synthetic (seeded, generated on the GPU)",
+        "config": {"workload": "served", "tables": len(tabs), "rows_resident": int(sum(t.rows for t in tabs)),
+                   "queries": len(qs), "ops": "4-32 per request (filter + project)", "nulls": "5% per column",
+                   "requests": int(n_rate * len(per_rate)), "arrivals": "Poisson, 5 rates",
+                   "budget_gb": args.budget_gb, "max_waves": args.waves, "parallelism": f"replicas x{world}",
+                   "l2": "tables of up to 1e8 rows exceed L2; no flush"},
+        "served_capacity_rps": capacity, "serial_plain_capacity_rps": serial_capacity,
+        "served_rows_per_s_at_capacity": float(q_rows[cq].sum() / mk),
+        "serial_plain_rows_per_s": float(q_rows.mean() / service.mean()),
+        "per_rate": per_rate,
+        "server": dict(st, start_s=round(start_s, 2), generate_s=round(gen_s, 2)),
+        "gpu_launches": int(launches), "clocks": clocks, "e2e": None,
+        "e2e_note": "served tables are resident in HBM by design; requests carry no host data",
+    }
+    if rank == 0:
+        print(json.dumps(out), flush=True)
+    srv.close()
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
 def run_reference(args):
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
-    if args.workload == "batched":
+    if args.workload in ("batched", "served"):
         threads = os.cpu_count() or 1
-        cpu_batched(threads, 8, 20_000, args.seed)
-        times = [cpu_batched(threads, 64, 200_000, args.seed) for _ in range(max(1, args.steps))]
+        fn = cpu_batched if args.workload == "batched" else cpu_served
+        what = "programs of the mix" if args.workload == "batched" else "queries of the served workload"
+        fn(threads, 8, 20_000, args.seed)
+        times = [fn(threads, 64 if args.workload == "batched" else 32, 200_000, args.seed)
+                 for _ in range(max(1, min(args.steps, 5)))]
         rows = times[0][0]
         t = statistics.mean(x[1] for x in times)
         v = rows / t
         out = {"metric": METRIC, "value": v, "unit": "rows/s", "n_gpus": world, "steps": args.steps,
                "warmup": args.warmup, "ms_per_step": t * 1e3, "higher_is_better": True, "scaling": "weak",
                "vs_baseline": None, "dtype": "int32/int64/f32/f64", "data": "synthetic (seeded)",
-               "impl": "reference", "config": {"workload": "batched", "programs": args.programs, "seed": args.seed},
+               "impl": "reference", "config": {"workload": args.workload, "seed": args.seed},
                "cpu_baseline": {"value": v, "unit": "rows/s", "cores": threads, "kind": "port",
-                                "sample": f"first 64 programs of the mix, tables capped at 200000 rows ({rows} rows)"},
+                                "sample": f"first {64 if args.workload == 'batched' else 32} {what}, "
+                                          f"tables capped at 200000 rows ({rows} rows)"},
                "e2e": {"value": v, "unit": "rows/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
         print(json.dumps(out), flush=True)
         return
@@ -664,11 +826,17 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="fused_project",
-                    choices=["fused_project", "plain_vm", "filter_gather", "batched"])
+                    choices=["fused_project", "plain_vm", "filter_gather", "batched", "served"])
+    ap.add_argument("--tables", type=int, default=24)
+    ap.add_argument("--queries", type=int, default=96)
+    ap.add_argument("--requests", type=int, default=50_000)
+    ap.add_argument("--budget-gb", type=float, default=120.0)
+    ap.add_argument("--waves", type=int, default=2)
     ap.add_argument("--programs", type=int, default=256)
     ap.add_argument("--seed", type=int, default=20261203)
     ap.add_argument("--plain-steps", type=int, default=3)
     ap.add_argument("--no-autotune", action="store_true")
+    ap.add_argument("--max-rows", type=int, default=0, help="batched: cap every table (profiling captures)")
     ap.add_argument("--selectivity", type=float, default=0.5)
     ap.add_argument("--rows", type=int, default=0)
     ap.add_argument("--skip-e2e", action="store_true")
@@ -680,6 +848,8 @@ def main():
         run_reference(args)
     elif args.workload == "batched":
         run_batched(args)
+    elif args.workload == "served":
+        run_served(args)
     else:
         run_ours(args)
 

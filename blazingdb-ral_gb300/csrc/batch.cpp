@@ -232,9 +232,9 @@ int Batch::prepare(cudaStream_t st) {
         }
         fn[q] = f->second;
     }
-    std::vector<std::string> names;
-    for (const auto& it : items) names.push_back(it.name);
-    GeneratedKernel disp = generate_batch_dispatch(names);
+    std::vector<DispatchEntry> names;
+    for (const auto& it : items) names.push_back({it.name, false});
+    GeneratedKernel disp = generate_batch_dispatch(names, 0);
     items.push_back(disp);
     std::vector<const std::vector<char>*> objects;
     if (int e = compile_items(items, objects, nullptr)) return e;
@@ -277,7 +277,7 @@ int Batch::prepare(cudaStream_t st) {
     cudaMemcpyAsync(d_prefix_, prefix.data(), prefix.size() * 8, cudaMemcpyHostToDevice, st);
     cudaMemcpyAsync(d_fn_, fn.data(), fn.size() * sizeof(int), cudaMemcpyHostToDevice, st);
     if (int e = check_cuda(cudaStreamSynchronize(st), "batch upload")) return e;
-    smem_ = (size_t)(NP + 1) * 8 + (size_t)NP * 4;
+    smem_ = batch_dispatch_smem(NP, 0);
     if (smem_ > 48 * 1024 &&
         check_cuda(cudaFuncSetAttribute((const void*)kernel_->kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_),
                    "cudaFuncSetAttribute"))
@@ -324,9 +324,9 @@ int Batch::debug_source(bool compile, std::string& source, std::string& log) con
         GeneratedKernel it = generate_batch_item(e->program, sh);
         if (seen.emplace(it.name, 1).second) items.push_back(std::move(it));
     }
-    std::vector<std::string> names;
-    for (const auto& it : items) names.push_back(it.name);
-    items.push_back(generate_batch_dispatch(names));
+    std::vector<DispatchEntry> names;
+    for (const auto& it : items) names.push_back({it.name, false});
+    items.push_back(generate_batch_dispatch(names, 0));
     source.clear();
     for (const auto& it : items) source += "// ---- " + it.name + "\n" + it.source + "\n";
     if (compile) {

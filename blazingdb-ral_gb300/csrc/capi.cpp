@@ -12,6 +12,7 @@
 #include "frontend.h"
 #include "jit.h"
 #include "kernels.h"
+#include "server.h"
 #include "ral/ral_c.h"
 
 using namespace ral;
@@ -423,6 +424,11 @@ int ral_debug_filter_source(const gdf_dtype* frame_dtypes, const int32_t* frame_
     });
 }
 
+struct ral_server_s {
+    ral::Server s;
+    ral_server_s(size_t b, int w, int m) : s(b, w, m) {}
+};
+
 struct ral_batch_s {
     ral::Batch b;
 };
@@ -542,6 +548,18 @@ int ral_autotune_program(gdf_column* const* output_columns, int32_t num_outputs,
             b->b.force_shape(c.first, c.second);
             bs.push_back(std::move(b));
         }
+        {   // compile every candidate's item and dispatcher at once, on the host thread pool
+            std::vector<GeneratedKernel> tus;
+            for (auto& c : cand) {
+                Shape sh = tuned_shape(p, G);
+                sh.J = c.first;
+                sh.unroll = c.second;
+                tus.push_back(generate_batch_item(p, sh));
+                tus.push_back(generate_batch_dispatch({{tus.back().name, false}}, 0));
+            }
+            std::vector<const std::vector<char>*> objs;
+            if (int e = compile_items(tus, objs, nullptr)) return e;
+        }
         cudaStream_t st = cudaStreamPerThread;
         for (auto& b : bs)
             if (int e = b->b.prepare(st)) return e;
@@ -580,6 +598,147 @@ int ral_jit_stats(int64_t* compiles, int64_t* disk_hits, int64_t* memory_hits, d
     if (memory_hits) *memory_hits = s.memory_hits;
     if (compile_ms) *compile_ms = s.compile_ms_total;
     return 0;
+}
+
+int ral_server_create(int64_t budget_bytes, int32_t max_waves, int32_t max_wave_requests, ral_server** server) {
+    return guarded([&] {
+        if (!server || budget_bytes <= 0) return set_error(kInvalidArgument, "bad argument");
+        *server = new ral_server_s((size_t)budget_bytes, max_waves, max_wave_requests);
+        return (int)kSuccess;
+    });
+}
+
+int ral_server_add_table(ral_server* server, gdf_column* const* columns, int32_t num_columns, int32_t* table_id) {
+    return guarded([&] {
+        if (!server) return set_error(kInvalidArgument, "null server");
+        int id = -1;
+        int rc = server->s.add_table(columns, num_columns, &id);
+        if (!rc && table_id) *table_id = id;
+        return rc;
+    });
+}
+
+int ral_server_add_query(ral_server* server, int32_t table_id, const char* filter_query_part,
+                         const char* project_query_part, int32_t* query_id) {
+    return guarded([&] {
+        if (!server) return set_error(kInvalidArgument, "null server");
+        int id = -1;
+        int rc = server->s.add_query(table_id, filter_query_part, project_query_part, &id);
+        if (!rc && query_id) *query_id = id;
+        return rc;
+    });
+}
+
+int ral_server_query_outputs(ral_server* server, int32_t query_id, gdf_dtype* dtypes, int32_t* has_valid,
+                             int32_t capacity, int32_t* num_outputs) {
+    return guarded([&] {
+        if (!server) return set_error(kInvalidArgument, "null server");
+        std::vector<gdf_dtype> d;
+        std::vector<bool> v;
+        if (int e = server->s.query_outputs(query_id, d, v)) return e;
+        if ((int)d.size() > capacity) return set_error(kInvalidArgument, "capacity too small");
+        for (size_t i = 0; i < d.size(); i++) {
+            dtypes[i] = d[i];
+            has_valid[i] = v[i] ? 1 : 0;
+        }
+        if (num_outputs) *num_outputs = (int32_t)d.size();
+        return (int)kSuccess;
+    });
+}
+
+int ral_server_debug_compile(ral_server* server, char* log_out, int64_t log_capacity) {
+    return guarded([&] {
+        if (!server) return set_error(kInvalidArgument, "null server");
+        std::string log;
+        int rc = server->s.debug_compile(log);
+        copy_out(log, log_out, log_capacity);
+        return rc;
+    });
+}
+
+int ral_server_start(ral_server* server) {
+    return guarded([&] {
+        if (!server) return set_error(kInvalidArgument, "null server");
+        return server->s.start();
+    });
+}
+
+int ral_server_submit(ral_server* server, int32_t query_id, int32_t keep, int64_t* request_id) {
+    return guarded([&] {
+        if (!server) return set_error(kInvalidArgument, "null server");
+        return server->s.submit(query_id, keep != 0, request_id);
+    });
+}
+
+int ral_server_wait(ral_server* server, int64_t request_id, double timeout_s, int64_t* rows_out, double* latency_s) {
+    return guarded([&] {
+        if (!server) return set_error(kInvalidArgument, "null server");
+        return server->s.wait(request_id, timeout_s, rows_out, latency_s);
+    });
+}
+
+int ral_server_result(ral_server* server, int64_t request_id, gdf_column* out_columns, int32_t num_outputs) {
+    return guarded([&] {
+        if (!server || !out_columns) return set_error(kInvalidArgument, "null argument");
+        return server->s.result(request_id, out_columns, num_outputs);
+    });
+}
+
+int ral_server_copy_result(ral_server* server, int64_t request_id, gdf_column* const* out_columns,
+                           int32_t num_outputs) {
+    return guarded([&] {
+        if (!server || !out_columns || num_outputs <= 0) return set_error(kInvalidArgument, "bad argument");
+        std::vector<gdf_column> src(num_outputs);
+        if (int e = server->s.result(request_id, src.data(), num_outputs)) return e;
+        cudaStream_t st = cudaStreamPerThread;
+        for (int o = 0; o < num_outputs; o++) {
+            gdf_column* d = out_columns[o];
+            if (!d) return set_error(kInvalidArgument, "null out column");
+            if (d->dtype != src[o].dtype) return set_error(kInvalidArgument, "out column has the wrong dtype");
+            if ((d->valid != nullptr) != (src[o].valid != nullptr))
+                return set_error(kInvalidArgument, "out column mask presence differs from the query's");
+            const size_t nb = (size_t)src[o].size * gdf_dtype_size(src[o].dtype);
+            if (nb) cudaMemcpyAsync(d->data, src[o].data, nb, cudaMemcpyDeviceToDevice, st);
+            if (src[o].valid && src[o].size)
+                cudaMemcpyAsync(d->valid, src[o].valid, ((size_t)src[o].size + 7) / 8, cudaMemcpyDeviceToDevice, st);
+            d->size = src[o].size;
+            d->null_count = src[o].null_count;
+        }
+        return check_cuda(cudaStreamSynchronize(st), "copy of a served result");
+    });
+}
+
+int ral_server_release(ral_server* server, int64_t request_id) {
+    return guarded([&] {
+        if (!server) return set_error(kInvalidArgument, "null server");
+        return server->s.release(request_id);
+    });
+}
+
+int ral_server_run_trace(ral_server* server, int32_t num_requests, const int32_t* queries, const double* arrival_s,
+                         double* latency_s, int64_t* rows_out, double* makespan_s) {
+    return guarded([&] {
+        if (!server || num_requests < 0 || (num_requests > 0 && (!queries || !arrival_s)))
+            return set_error(kInvalidArgument, "bad argument");
+        return server->s.run_trace(num_requests, queries, arrival_s, latency_s, rows_out, makespan_s);
+    });
+}
+
+int ral_server_stats(ral_server* server, int64_t* stats6) {
+    if (!server || !stats6) return set_error(kInvalidArgument, "null argument");
+    ServerStats st = server->s.stats();
+    stats6[0] = st.submitted;
+    stats6[1] = st.completed;
+    stats6[2] = st.waves;
+    stats6[3] = st.max_wave_requests;
+    stats6[4] = (int64_t)st.peak_reserved;
+    stats6[5] = (int64_t)(st.busy_s * 1e6);
+    return kSuccess;
+}
+
+int ral_server_destroy(ral_server* server) {
+    delete server;
+    return kSuccess;
 }
 
 }  // extern "C"

@@ -464,8 +464,9 @@ int filter_max_width(const FilterSpec& f) {
     return w;
 }
 
-GeneratedKernel generate_filter_kernel(const FilterSpec& f, const Shape& s) {
+GeneratedKernel generate_filter_kernel(const FilterSpec& f, const Shape& s, bool item) {
     if (s.G * s.J > 4096) throw std::runtime_error("filter kernel shape: G*J out of range");
+    if (item && s.stage) throw std::runtime_error("filter item functions take no shared-memory stage");
     GeneratedKernel gk;
     gk.shape = s;
     ParamLayout& L = gk.layout;
@@ -548,9 +549,10 @@ GeneratedKernel generate_filter_kernel(const FilterSpec& f, const Shape& s) {
     key << "|O";
     for (const FilterOutput& o : f.outputs) key << (o.from_project ? "p" : "g") << o.index << ":" << (int)o.dtype << (o.has_valid ? "v" : "") << ",";
     key << "|G" << s.G << "J" << s.J << "T" << s.threads << "B" << s.min_blocks << "U" << s.unroll << "S" << s.stage;
+    if (item) key << "|item";
     char hex[32];
     snprintf(hex, sizeof hex, "%016llx", (unsigned long long)fnv1a(key.str()));
-    gk.name = std::string("ral_filter_") + hex;
+    gk.name = std::string(item ? "ral_fitem_" : "ral_filter_") + hex;
 
     std::ostringstream os;
     os << "// generated: " << key.str() << "\n";
@@ -614,9 +616,19 @@ GeneratedKernel generate_filter_kernel(const FilterSpec& f, const Shape& s) {
         return "((r < n) ? __ldg(" + fvalid(c) + " + (r >> 5)) : 0xffffffffu)";
     };
     const int KBW = (s.G * s.J + 31) / 32;  // packed keep-bit words per lane
-    os << "\nextern \"C\" __global__ void __launch_bounds__(RAL_THREADS, " << std::max(1, s.min_blocks) << ") " << gk.name
-       << "(const __grid_constant__ RalParams P) {\n";
-    if (NVO) os << "    __shared__ ral_u32 s_vb[" << NVO << "][RAL_WARPS][RAL_G * RAL_J + 2];\n";
+    if (item) {
+        // one chunk of a batched request: the dispatcher hands over the chunk index and this
+        // warp's shared-memory area (masks staged per output)
+        os << "\nextern \"C\" __device__ __noinline__ void " << gk.name
+           << "(const ral_u64* __restrict__ slots, const ral_i64 chunk_index, ral_u32* __restrict__ wsm) {\n";
+        os << "    const RalParams& P = *reinterpret_cast<const RalParams*>(slots);\n";
+        if (NVO) os << "    ral_u32 (*const s_vbw)[RAL_G * RAL_J + 2] = reinterpret_cast<ral_u32 (*)[RAL_G * RAL_J + 2]>(wsm);\n";
+        gk.item_smem_words = NVO * (s.G * s.J + 2);
+    } else {
+        os << "\nextern \"C\" __global__ void __launch_bounds__(RAL_THREADS, " << std::max(1, s.min_blocks) << ") " << gk.name
+           << "(const __grid_constant__ RalParams P) {\n";
+        if (NVO) os << "    __shared__ ral_u32 s_vb[RAL_WARPS][" << NVO << "][RAL_G * RAL_J + 2];\n";
+    }
     // per-warp staging of one slice's compacted values, so that stores are contiguous
     if (s.stage) os << "    __shared__ ral_u64 s_stage[RAL_WARPS][32 * RAL_G];\n";
     os << "    const ral_i64 n = (ral_i64)P.s[" << L.n_rows << "];\n";
@@ -635,16 +647,26 @@ GeneratedKernel generate_filter_kernel(const FilterSpec& f, const Shape& s) {
         if (f.outputs[k].has_valid)
             os << "    ral_u32* __restrict__ ov" << k << " = (ral_u32*)P.s[" << L.out_valid + k << "];\n";
     }
-    os << "    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;\n";
+    os << "    const int lane = threadIdx.x & 31;\n";
+    if (!item) {
+        os << "    const int warp = threadIdx.x >> 5;\n";
+        if (NVO) os << "    ral_u32 (*const s_vbw)[RAL_G * RAL_J + 2] = s_vb[warp];\n";
+        if (s.stage) os << "    ral_u64* const s_stw = s_stage[warp];\n";
+    }
     os << "    const ral_i64 WT = 32 * RAL_G * RAL_J;\n";
     os << "    const ral_i64 nchunks = (n + WT - 1) / WT;\n";
     os << "    const ral_u32 GMASK = (RAL_G == 32) ? 0xffffffffu : ((1u << RAL_G) - 1u);\n";
     if (NVO) os << "    ral_u32 vcnt[" << NVO << "];\n    for (int i = 0; i < " << NVO << "; ++i) vcnt[i] = 0;\n";
-    os << "    for (;;) {\n";
-    os << "        ral_u32 ticket = 0;\n";
-    os << "        if (lane == 0) ticket = atomicAdd((unsigned int*)scratch, 1u);\n";
-    os << "        const ral_i64 chunk = __shfl_sync(0xffffffffu, ticket, 0);\n";
-    os << "        if (chunk >= nchunks) break;\n";
+    if (item) {
+        os << "    do {\n";
+        os << "        const ral_i64 chunk = chunk_index;\n";
+    } else {
+        os << "    for (;;) {\n";
+        os << "        ral_u32 ticket = 0;\n";
+        os << "        if (lane == 0) ticket = atomicAdd((unsigned int*)scratch, 1u);\n";
+        os << "        const ral_i64 chunk = __shfl_sync(0xffffffffu, ticket, 0);\n";
+        os << "        if (chunk >= nchunks) break;\n";
+    }
     os << "        const ral_i64 base = chunk * WT;\n";
     os << "        const bool full = base + WT <= n;\n";
     os << "        ral_u32 kbw[" << KBW << "];\n";
@@ -703,10 +725,10 @@ GeneratedKernel generate_filter_kernel(const FilterSpec& f, const Shape& s) {
     bool any_gather = false, any_proj = false;
     for (const FilterOutput& o : f.outputs) (o.from_project ? any_proj : any_gather) = true;
     if (NVO) {
-        for (int i = 0; i < NVO; i++) os << "        if (lane < RAL_G * RAL_J + 2) s_vb[" << i << "][warp][lane] = 0u;\n";
+        for (int i = 0; i < NVO; i++) os << "        if (lane < RAL_G * RAL_J + 2) s_vbw[" << i << "][lane] = 0u;\n";
         os << "        if (RAL_G * RAL_J + 2 > 32) {\n";
         os << "            for (int q = 32 + lane; q < RAL_G * RAL_J + 2; q += 32) {\n";
-        for (int i = 0; i < NVO; i++) os << "                s_vb[" << i << "][warp][q] = 0u;\n";
+        for (int i = 0; i < NVO; i++) os << "                s_vbw[" << i << "][q] = 0u;\n";
         os << "            }\n        }\n";
         os << "        __syncwarp();\n";
         os << "        const ral_u64 a0 = excl & ~31ull;\n";
@@ -746,7 +768,7 @@ GeneratedKernel generate_filter_kernel(const FilterSpec& f, const Shape& s) {
                 if (f.outputs[k].from_project) continue;
                 const char* et = element_ctype(f.frame_dtypes[f.outputs[k].index]);
                 os << "                {\n";
-                os << "                    " << et << "* const st = reinterpret_cast<" << et << "*>(s_stage[warp]);\n";
+                os << "                    " << et << "* const st = reinterpret_cast<" << et << "*>(s_stw);\n";
                 os << "                    ral_u32 q = inc - c;\n";
                 os << "#pragma unroll\n                    for (int g = 0; g < RAL_G; ++g)\n";
                 os << "                        if ((kb >> g) & 1u) st[q++] = ga" << k << "[g];\n";
@@ -824,7 +846,7 @@ GeneratedKernel generate_filter_kernel(const FilterSpec& f, const Shape& s) {
         os << "                    const ral_u32 W = first + kk;\n";
         os << "                    const ral_u32 part = (t == 0u) ? 0u : (qw == W ? (ral_u32)X : (qw + 1u == W ? (ral_u32)(X >> 32) : 0u));\n";
         os << "                    const ral_u32 v = __reduce_or_sync(0xffffffffu, part);\n";
-        os << "                    if (lane == 0 && v) s_vb[" << i << "][warp][W] |= v;\n";
+        os << "                    if (lane == 0 && v) s_vbw[" << i << "][W] |= v;\n";
         os << "                }\n";
         os << "            }\n";
     }
@@ -837,7 +859,7 @@ GeneratedKernel generate_filter_kernel(const FilterSpec& f, const Shape& s) {
         for (int i = 0; i < NVO; i++) {
             const int k = vouts[i];
             os << "        for (ral_u32 q = lane; q < nw; q += 32) {\n";
-            os << "            const ral_u32 v = s_vb[" << i << "][warp][q];\n";
+            os << "            const ral_u32 v = s_vbw[" << i << "][q];\n";
             os << "            ral_u32* dst = ov" << k << " + (a0 >> 5) + q;\n";
             os << "            if (q == 0 || q == nw - 1) { if (v) atomicOr(dst, v); }\n";
             os << "            else *dst = v;\n";
@@ -845,7 +867,7 @@ GeneratedKernel generate_filter_kernel(const FilterSpec& f, const Shape& s) {
         }
         os << "        __syncwarp();\n";
     }
-    os << "    }\n";  // chunk loop
+    os << (item ? "    } while (0);\n" : "    }\n");  // chunk loop
 
     // ---- valid-bit counts: one atomic per warp and masked output
     if (NVO) {
@@ -984,21 +1006,27 @@ GeneratedKernel generate_batch_item(const Program& p, const Shape& sh) {
     return gk;
 }
 
-GeneratedKernel generate_batch_dispatch(const std::vector<std::string>& item_names) {
+GeneratedKernel generate_batch_dispatch(const std::vector<DispatchEntry>& items, int smem_words_per_warp) {
     GeneratedKernel gk;
     std::ostringstream key;
-    key << "dispatch|";
-    for (const auto& n : item_names) key << n << ";";
+    key << "dispatch|" << smem_words_per_warp << "|";
+    for (const auto& it : items) key << it.name << (it.filter ? "f" : "") << ";";
     char hex[32];
     snprintf(hex, sizeof hex, "%016llx", (unsigned long long)fnv1a(key.str()));
     gk.name = std::string("ral_batch_") + hex;
-    const int NF = (int)item_names.size();
+    const int NF = (int)items.size();
     std::ostringstream os;
     os << "// generated: persistent dispatcher over " << NF << " item functions\n";
-    for (const auto& n : item_names)
-        os << "extern \"C\" __device__ void " << n << "(const ral_u64* __restrict__ slots, const ral_i64 t);\n";
+    for (const auto& it : items) {
+        if (it.filter)
+            os << "extern \"C\" __device__ void " << it.name
+               << "(const ral_u64* __restrict__ slots, const ral_i64 t, ral_u32* __restrict__ wsm);\n";
+        else
+            os << "extern \"C\" __device__ void " << it.name << "(const ral_u64* __restrict__ slots, const ral_i64 t);\n";
+    }
     os << "#define RAL_BATCH_GRAB 8\n";
-    // dynamic shared memory: item prefix (n_programs + 1 long longs), then one function index per program
+    // dynamic shared memory: item prefix (n_programs + 1 long longs), one function index per
+    // program, then each warp's area for filter items
     os << "extern \"C\" __global__ void __launch_bounds__(256) " << gk.name
        << "(const ral_u64* __restrict__ descs, const int stride, const long long* __restrict__ item_prefix, "
           "const int* __restrict__ fn_index, const int np, unsigned int* counter, const long long total_items) {\n";
@@ -1008,6 +1036,11 @@ GeneratedKernel generate_batch_dispatch(const std::vector<std::string>& item_nam
     os << "    for (int i = threadIdx.x; i < np; i += blockDim.x) s_fn[i] = fn_index[i];\n";
     os << "    __syncthreads();\n";
     os << "    const int lane = threadIdx.x & 31;\n";
+    if (smem_words_per_warp > 0) {
+        os << "    const size_t head = ((size_t)(np + 1) * 8 + (size_t)np * 4 + 15) & ~(size_t)15;\n";
+        os << "    ral_u32* const wsm = reinterpret_cast<ral_u32*>(reinterpret_cast<char*>(s_prefix) + head) + "
+              "(threadIdx.x >> 5) * " << smem_words_per_warp << ";\n";
+    }
     os << "    for (;;) {\n";
     os << "        unsigned int got = 0;\n";
     os << "        if (lane == 0) got = atomicAdd(counter, (unsigned int)RAL_BATCH_GRAB);\n";
@@ -1024,7 +1057,9 @@ GeneratedKernel generate_batch_dispatch(const std::vector<std::string>& item_nam
     os << "            const ral_u64* slots = descs + (size_t)lo * stride;\n";
     os << "            const ral_i64 t = item - s_prefix[lo];\n";
     os << "            switch (s_fn[lo]) {\n";
-    for (int f = 0; f < NF; f++) os << "            case " << f << ": " << item_names[f] << "(slots, t); break;\n";
+    for (int f = 0; f < NF; f++)
+        os << "            case " << f << ": " << items[f].name << (items[f].filter ? "(slots, t, wsm)" : "(slots, t)")
+           << "; break;\n";
     os << "            default: break;\n";
     os << "            }\n";
     os << "        }\n";

@@ -49,6 +49,8 @@ struct GeneratedKernel {
     Shape shape;
     // filter kernels: scalar slots of the projection program
     std::vector<int> layout_project_lscalar, layout_project_rscalar;
+    // filter item functions: shared-memory words the function needs in its warp's area
+    int item_smem_words = 0;
 };
 
 // Batched and served launches run many programs in one persistent kernel.  Each program's warp
@@ -62,8 +64,23 @@ struct GeneratedKernel {
 //          int n_programs, unsigned int* counter, long long total_items)
 // descs holds `stride` slots per program; fn_index[q] indexes item_names.  Dynamic shared memory:
 // (n_programs + 1) * 8 + n_programs * 4 bytes.
+// Filter + project requests are batched the same way: their item function is the fused filter
+// kernel's chunk body (generate_filter_kernel with item = true),
+//   extern "C" __device__ void <name>(const ral_u64* slots, long long chunk, unsigned* warp_smem)
+// which also takes the calling warp's area of the dispatcher's dynamic shared memory.
 GeneratedKernel generate_batch_item(const Program& p, const Shape& s);
-GeneratedKernel generate_batch_dispatch(const std::vector<std::string>& item_names);
+struct DispatchEntry {
+    std::string name;
+    bool filter = false;  // takes the warp's shared-memory area
+};
+// smem_words_per_warp: largest item_smem_words over the filter items (0 if none).  The dynamic
+// shared memory is then (n_programs + 1) * 8 + n_programs * 4 (rounded up to 16) plus
+// 8 warps * smem_words_per_warp * 4 bytes.
+GeneratedKernel generate_batch_dispatch(const std::vector<DispatchEntry>& items, int smem_words_per_warp);
+inline size_t batch_dispatch_smem(int n_programs, int smem_words_per_warp) {
+    const size_t head = ((size_t)(n_programs + 1) * 8 + (size_t)n_programs * 4 + 15) & ~(size_t)15;
+    return head + (size_t)8 * smem_words_per_warp * 4;
+}
 
 // perform_operation: evaluate the program over n rows into the outputs.
 GeneratedKernel generate_eval_kernel(const Program& p, const Shape& s);
@@ -103,7 +120,7 @@ inline int64_t filter_tile_rows(const Shape& s) { return (int64_t)32 * s.G * s.J
 // Widest column the fused filter touches.
 int filter_max_width(const FilterSpec& f);
 
-GeneratedKernel generate_filter_kernel(const FilterSpec& f, const Shape& s);
+GeneratedKernel generate_filter_kernel(const FilterSpec& f, const Shape& s, bool item = false);
 
 // C type name of a column element.
 const char* element_ctype(gdf_dtype t);

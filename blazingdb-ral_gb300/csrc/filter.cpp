@@ -568,6 +568,87 @@ int process_filter(gdf_column* const* frame, int ncols, const char* query_part, 
     return process_filter_fused(frame, ncols, cond, outs, n_out, opt.stream);
 }
 
+int plan_filter_project(gdf_column* const* frame, int ncols, const char* filter_q, const char* project_q,
+                        std::unique_ptr<FilterPlan>& plan) {
+    if (!frame || ncols <= 0 || !filter_q || !project_q) return set_error(kInvalidArgument, "null argument");
+    for (int c = 0; c < ncols; c++) {
+        if (!frame[c]) return set_error(kInvalidArgument, "null frame column");
+        if (frame[c]->size != frame[0]->size) return set_error(kInvalidArgument, "frame columns differ in size");
+        if (gdf_dtype_size(frame[c]->dtype) == 0) return set_error(kUnsupported, "column dtype has no fixed width");
+    }
+    const std::string cond = named_expression(filter_q, "condition");
+    if (cond.empty()) return set_error(kParseError, "no condition=[...] in the LogicalFilter");
+    std::vector<gdf_dtype> fd(ncols);
+    for (int c = 0; c < ncols; c++) fd[c] = frame[c]->dtype;
+    const ProjectPlan& pp = cached_project_plan(project_q, fd);
+    auto p = std::make_unique<FilterPlan>();
+    frame_spec(frame, ncols, p->spec);
+    if (int e = predicate_spec(frame, ncols, cond, p->spec, p->pred, p->have_pred)) return e;
+    if (p->have_pred) p->spec.predicate = &p->pred;
+    const int n_outs = (int)pp.columns.size();
+    // stand-in output descriptors: only dtype and mask presence matter to the program
+    std::vector<gdf_column> stand(n_outs);
+    for (int i = 0; i < n_outs; i++) {
+        const bool ev = pp.columns[i].first;
+        stand[i].dtype = ev ? pp.eval_dtypes[pp.columns[i].second] : fd[pp.columns[i].second];
+        const bool mask = ev ? true : frame[pp.columns[i].second]->valid != nullptr;
+        stand[i].valid = mask ? (gdf_valid_type*)(uintptr_t)64 : nullptr;
+        stand[i].size = frame[0]->size;
+        p->out_dtypes.push_back(stand[i].dtype);
+        p->out_valid.push_back(mask);
+    }
+    p->have_proj = !pp.eval_dtypes.empty();
+    if (p->have_proj) {
+        std::vector<gdf_column*> evald;
+        for (int i = 0; i < n_outs; i++)
+            if (pp.columns[i].first) evald.push_back(&stand[i]);
+        std::vector<gdf_column*> ins;
+        for (int c : pp.input_columns) ins.push_back(frame[c]);
+        ProgramArrays pa{pp.pv.left.data(), pp.pv.right.data(), pp.pv.outs.data(), (int32_t)pp.pv.left.size(),
+                         pp.pv.final_pos.data(), pp.pv.bops.data(), pp.pv.uops.data(), pp.pv.lscalars.data(),
+                         pp.pv.rscalars.data()};
+        // as in filter_project: the filtered frame's masks are read whenever present
+        if (int e = build_program(p->proj, evald.data(), (int)evald.size(), ins.data(), (int)ins.size(), pa, true))
+            return e;
+        p->spec.project = &p->proj;
+        p->spec.project_cols = pp.input_columns;
+    }
+    for (int i = 0; i < n_outs; i++) {
+        FilterOutput o;
+        o.from_project = pp.columns[i].first;
+        o.index = pp.columns[i].second;
+        o.dtype = p->out_dtypes[i];
+        o.has_valid = p->out_valid[i];
+        p->spec.outputs.push_back(o);
+    }
+    plan = std::move(p);
+    return kSuccess;
+}
+
+void filter_fill_slots(const FilterPlan& plan, const GeneratedKernel& gk, gdf_column* const* frame, int64_t n_rows,
+                       void* const* out_data, void* const* out_valid, void* scratch, std::vector<uint64_t>& slots) {
+    const ParamLayout& L = gk.layout;
+    const FilterSpec& spec = plan.spec;
+    slots.assign(L.total, 0);
+    slots[L.n_rows] = (uint64_t)n_rows;
+    for (int c = 0; c < spec.n_frame; c++) {
+        slots[L.in_data + c] = (uint64_t)(uintptr_t)frame[c]->data;
+        slots[L.in_valid + c] = (uint64_t)(uintptr_t)frame[c]->valid;
+    }
+    for (size_t q = 0; q < spec.outputs.size(); q++) {
+        slots[L.out_data + q] = (uint64_t)(uintptr_t)out_data[q];
+        slots[L.out_valid + q] = (uint64_t)(uintptr_t)out_valid[q];
+    }
+    slots[L.scratch] = (uint64_t)(uintptr_t)scratch;
+    if (plan.have_pred) fill_scalars(plan.pred, L, slots);
+    if (plan.have_proj) {
+        ParamLayout QL;
+        QL.lscalar_slot = gk.layout_project_lscalar;
+        QL.rscalar_slot = gk.layout_project_rscalar;
+        fill_scalars(plan.proj, QL, slots);
+    }
+}
+
 int filter_project(gdf_column* const* frame, int ncols, const char* filter_q, const char* project_q,
                    gdf_column* const* outs, int n_outs, gdf_size_type* n_out, const FilterOptions& opt) {
     if (!frame || ncols <= 0 || !filter_q || !project_q || !outs || !n_out)

@@ -3,8 +3,12 @@
 
 #include <cuda_runtime.h>
 
+#include <memory>
 #include <string>
+#include <vector>
 
+#include "codegen.h"
+#include "program.h"
 #include "ral/gdf_compat.h"
 
 namespace ral {
@@ -28,5 +32,22 @@ int debug_filter_source(gdf_column* const* frame, int num_columns, const char* f
 int filter_project(gdf_column* const* frame, int num_columns, const char* filter_query_part,
                    const char* project_query_part, gdf_column* const* out_columns, int num_out_columns,
                    gdf_size_type* num_rows_out, const FilterOptions& opt);
+
+// A LogicalProject over a LogicalFilter, planned for a frame: the fused filter's spec and the
+// dtype / mask presence of every output (evaluated outputs carry a mask; a pass-through output
+// carries one exactly when its frame column does).  Holds the programs the spec points to.
+struct FilterPlan {
+    FilterSpec spec;
+    Program pred, proj;
+    bool have_pred = false, have_proj = false;
+    std::vector<gdf_dtype> out_dtypes;
+    std::vector<bool> out_valid;
+};
+int plan_filter_project(gdf_column* const* frame, int ncols, const char* filter_query_part,
+                        const char* project_query_part, std::unique_ptr<FilterPlan>& plan);
+
+// Parameter slots of a fused filter launch (kernel or batch item) of the plan.
+void filter_fill_slots(const FilterPlan& plan, const GeneratedKernel& gk, gdf_column* const* frame, int64_t n_rows,
+                       void* const* out_data, void* const* out_valid, void* scratch, std::vector<uint64_t>& slots);
 
 }  // namespace ral

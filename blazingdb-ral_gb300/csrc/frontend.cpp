@@ -396,7 +396,11 @@ std::vector<std::pair<std::string, std::string>> project_expressions(const std::
     if (open == std::string::npos || close == std::string::npos || close <= open)
         throw ParseError("not a LogicalProject: " + q);
     std::string all = q.substr(open + 1, close - open - 1);
+    // get_expressions_from_expression_list's rewrites, CalciteExpressionParsing.cpp:818-830, in its
+    // order: after the CASE(IS NOT NULL ...) -> COALESCE rewrite it drops every " NOT NULL", so an
+    // IS NOT NULL left in a projection becomes the unknown operator "IS" and is rejected, as there
     all = std::regex_replace(all, coalesce_re(), "COALESCE($1, $2)");
+    replace_all(all, " NOT NULL", "");
     std::vector<std::string> parts;
     int pd = 0, sd = 0;
     bool inq = false;

@@ -1,0 +1,138 @@
+// server.h — the served form of the expression path: a request loop over HBM-resident tables.
+//
+// Clients register tables (columns stay where the caller put them, in device memory) and
+// filter + project queries over them, then submit requests (one run of one query).  A
+// scheduler thread admits requests while the working set (resident tables plus the outputs
+// and scratch of admitted requests) stays under a byte budget, and launches every admitted
+// request that is waiting as one wave: one launch of the persistent dispatcher whose warps pull
+// (request, chunk) work items.  Up to max_waves waves are in flight on their own streams, so
+// requests that arrive while a wave runs are admitted and launched as soon as memory and a
+// wave slot free up, and their work overlaps the running wave's tail on the device.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <atomic>
+#include <condition_variable>
+#include <cstdint>
+#include <deque>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <thread>
+#include <unordered_map>
+#include <vector>
+
+#include "codegen.h"
+#include "filter.h"
+#include "jit.h"
+
+namespace ral {
+
+struct ServerTable {
+    std::vector<gdf_column> cols;
+    int64_t rows = 0;
+    size_t bytes = 0;
+};
+
+struct ServerQuery {
+    int table = -1;
+    std::unique_ptr<FilterPlan> plan;
+    GeneratedKernel item;
+    int fn = -1;               // index in the dispatcher's function list
+    size_t reserve = 0;        // output + scratch bytes of one request (every row kept)
+    int64_t chunks = 0;        // work items of one request
+};
+
+struct ServerRequest {
+    int64_t id = 0;
+    int query = -1;
+    bool keep = false;         // keep the outputs for ral_server_result (else freed at completion)
+    double t_submit = 0, t_launch = 0, t_done = 0;  // seconds on the server's clock
+    int64_t rows_out = -1;
+    int status = 0;
+    std::vector<void*> out_data, out_valid;
+    std::vector<int64_t> null_counts;
+    void* scratch = nullptr;
+    bool done = false;
+};
+
+struct ServerStats {
+    int64_t submitted = 0, completed = 0, waves = 0, max_wave_requests = 0;
+    size_t peak_reserved = 0;
+    double busy_s = 0;         // wall time with at least one wave in flight
+};
+
+class Server {
+public:
+    Server(size_t budget_bytes, int max_waves, int max_wave_requests);
+    ~Server();
+    int add_table(gdf_column* const* cols, int ncols, int* table_id);
+    int add_query(int table_id, const char* filter_q, const char* project_q, int* query_id);
+    // Output dtypes and mask presence of a query.
+    int query_outputs(int query_id, std::vector<gdf_dtype>& dtypes, std::vector<bool>& valid) const;
+    // Compiles every query's item function (host thread pool), links the dispatcher and starts
+    // the scheduler thread.  Queries added later trigger a relink before their first wave.
+    int start();
+    // Compiles the item functions and links the dispatcher without loading it (no GPU needed).
+    int debug_compile(std::string& log);
+    int submit(int query_id, bool keep, int64_t* request_id);
+    // Waits (up to timeout_s) for a request; fills rows out and latency (submit to completion).
+    int wait(int64_t request_id, double timeout_s, int64_t* rows_out, double* latency_s);
+    // A kept request's outputs (device pointers owned by the server until release).
+    int result(int64_t request_id, gdf_column* out_cols, int n_out);
+    int release(int64_t request_id);
+    // Runs a trace: request k of query q[k] submitted at start + arrival_s[k]; blocks until all
+    // are done and fills each latency and kept row count.
+    int run_trace(int n, const int32_t* queries, const double* arrival_s, double* latency_s, int64_t* rows_out,
+                  double* makespan_s);
+    int stop();
+    ServerStats stats() const;
+    double now() const;
+
+private:
+    struct Wave {
+        cudaStream_t stream = nullptr;
+        cudaEvent_t done = nullptr;
+        void* d_desc = nullptr;        // descs | prefix | fn | counter, one allocation
+        void* h_desc = nullptr;        // pinned staging of the same
+        void* h_head = nullptr;        // pinned: scratch headers copied back
+        size_t desc_bytes = 0;
+        std::vector<int64_t> reqs;
+        bool busy = false;
+        double t_launch = 0;
+    };
+    int ensure_linked();
+    int launch_wave(Wave& w, std::vector<int64_t>& batch);
+    void finish_wave(Wave& w);
+    void loop();
+
+    size_t budget_;
+    int max_waves_, max_wave_requests_;
+    std::vector<ServerTable> tables_;
+    std::vector<std::unique_ptr<ServerQuery>> queries_;
+    size_t tables_bytes_ = 0;
+    const CompiledKernel* kernel_ = nullptr;
+    int linked_queries_ = 0;
+    int stride_ = 1, smem_words_ = 0, grid_ = 0;
+    int device_ = 0;
+
+    mutable std::mutex mu_;
+    std::condition_variable cv_, done_cv_;
+    std::deque<int64_t> pending_;
+    std::unordered_map<int64_t, std::unique_ptr<ServerRequest>> requests_;
+    int64_t next_id_ = 1;
+    size_t reserved_ = 0;
+    std::vector<Wave> waves_;
+    std::thread thread_;
+    std::atomic<bool> stop_{false};
+    bool started_ = false;
+    int fatal_ = 0;
+    std::string fatal_msg_;
+    ServerStats stats_;
+    double t0_ = 0;
+    double busy_since_ = -1;
+    int inflight_ = 0;
+};
+
+}  // namespace ral

@@ -59,6 +59,21 @@ _SIGS = {
     "ral_batch_debug_source": (C.c_int, [P, C.c_int32, C.c_char_p, C.c_int64, C.c_char_p, C.c_int64]),
     "ral_batch_destroy": (C.c_int, [P]),
     "ral_batch_kernel_info": (C.c_int, [P, I32P, I32P, I32P]),
+    "ral_server_create": (C.c_int, [C.c_int64, C.c_int32, C.c_int32, C.POINTER(C.c_void_p)]),
+    "ral_server_add_table": (C.c_int, [P, COLPP, C.c_int32, I32P]),
+    "ral_server_add_query": (C.c_int, [P, C.c_int32, C.c_char_p, C.c_char_p, I32P]),
+    "ral_server_query_outputs": (C.c_int, [P, C.c_int32, I32P, I32P, C.c_int32, I32P]),
+    "ral_server_start": (C.c_int, [P]),
+    "ral_server_debug_compile": (C.c_int, [P, C.c_char_p, C.c_int64]),
+    "ral_server_submit": (C.c_int, [P, C.c_int32, C.c_int32, C.POINTER(C.c_int64)]),
+    "ral_server_wait": (C.c_int, [P, C.c_int64, C.c_double, C.POINTER(C.c_int64), C.POINTER(C.c_double)]),
+    "ral_server_result": (C.c_int, [P, C.c_int64, C.POINTER(GdfColumn), C.c_int32]),
+    "ral_server_release": (C.c_int, [P, C.c_int64]),
+    "ral_server_copy_result": (C.c_int, [P, C.c_int64, COLPP, C.c_int32]),
+    "ral_server_run_trace": (C.c_int, [P, C.c_int32, I32P, C.POINTER(C.c_double), C.POINTER(C.c_double),
+                                       C.POINTER(C.c_int64), C.POINTER(C.c_double)]),
+    "ral_server_stats": (C.c_int, [P, C.POINTER(C.c_int64)]),
+    "ral_server_destroy": (C.c_int, [P]),
     "ral_batch_tune_key": (C.c_int, [COLPP, C.c_int32, COLPP, C.c_int32, I16P, I16P, I16P, C.c_int32, I16P, I32P, I32P,
                                      SCP, SCP, C.c_char_p, C.c_int64]),
     "ral_autotune_program": (C.c_int, [COLPP, C.c_int32, COLPP, C.c_int32, I16P, I16P, I16P, C.c_int32, I16P, I32P,
@@ -486,3 +501,101 @@ def autotune_program(output_columns: List[Column], input_columns: List[Column], 
     _check(lib().ral_autotune_program(oa, len(output_columns), ia, len(input_columns), _p16(l), _p16(r), _p16(o),
                                       len(l), _p16(f), _p32(b), _p32(u), ls, rs, C.byref(J), C.byref(U), C.byref(ms)))
     return J.value, U.value, ms.value
+
+
+class Server:
+    """Served execution: resident tables, prepared filter + project queries, requests run with
+    continuous batching by a scheduler thread in the library (include/ral/ral_c.h)."""
+
+    def __init__(self, budget_bytes: int = 120 << 30, max_waves: int = 2, max_wave_requests: int = 1024):
+        h = C.c_void_p()
+        _check(lib().ral_server_create(int(budget_bytes), max_waves, max_wave_requests, C.byref(h)))
+        self._h = h
+        self._tables = []
+
+    def add_table(self, columns: List[Column]) -> int:
+        arr, structs = _colarray(columns)
+        tid = C.c_int32(-1)
+        _check(lib().ral_server_add_table(self._h, arr, len(columns), C.byref(tid)))
+        self._tables.append(list(columns))   # the server reads these buffers: keep them alive
+        return tid.value
+
+    def add_query(self, table_id: int, filter_query_part: str, project_query_part: str) -> int:
+        qid = C.c_int32(-1)
+        _check(lib().ral_server_add_query(self._h, table_id, filter_query_part.encode(), project_query_part.encode(),
+                                          C.byref(qid)))
+        return qid.value
+
+    def query_outputs(self, query_id: int) -> Tuple[List[int], List[bool]]:
+        cap = 64
+        dt = np.zeros(cap, dtype=np.int32)
+        hv = np.zeros(cap, dtype=np.int32)
+        n = C.c_int32(0)
+        _check(lib().ral_server_query_outputs(self._h, query_id, _p32(dt), _p32(hv), cap, C.byref(n)))
+        return [int(x) for x in dt[:n.value]], [bool(x) for x in hv[:n.value]]
+
+    def start(self) -> None:
+        _check(lib().ral_server_start(self._h))
+
+    def debug_compile(self) -> str:
+        """Compiles every query's chunk function and links the dispatcher (no GPU needed)."""
+        log = C.create_string_buffer(1 << 20)
+        _check(lib().ral_server_debug_compile(self._h, log, len(log)))
+        return log.value.decode()
+
+    def submit(self, query_id: int, keep: bool = False) -> int:
+        rid = C.c_int64(0)
+        _check(lib().ral_server_submit(self._h, query_id, 1 if keep else 0, C.byref(rid)))
+        return rid.value
+
+    def wait(self, request_id: int, timeout_s: float = 120.0) -> Tuple[int, float]:
+        rows, lat = C.c_int64(0), C.c_double(0)
+        _check(lib().ral_server_wait(self._h, request_id, timeout_s, C.byref(rows), C.byref(lat)))
+        return rows.value, lat.value
+
+    def release(self, request_id: int) -> None:
+        """Forgets a finished request (and frees its outputs if they were kept)."""
+        _check(lib().ral_server_release(self._h, request_id))
+
+    def result(self, request_id: int, query_id: int, release: bool = True) -> List[Column]:
+        """Copies of a kept request's outputs (the server's buffers are released afterwards)."""
+        dts, hv = self.query_outputs(query_id)
+        rows = C.c_int64(0)
+        _check(lib().ral_server_wait(self._h, request_id, 600.0, C.byref(rows), None))
+        out = [Column.empty(dt, int(rows.value), with_valid=v) for dt, v in zip(dts, hv)]
+        arr, structs = _colarray(out)
+        _check(lib().ral_server_copy_result(self._h, request_id, arr, len(out)))
+        for col, st in zip(out, structs):
+            col.sync_from_c(st)
+        if release:
+            _check(lib().ral_server_release(self._h, request_id))
+        return out
+
+    def run_trace(self, queries, arrival_s) -> Tuple[np.ndarray, np.ndarray, float]:
+        q = _i32(queries)
+        a = np.ascontiguousarray(np.asarray(arrival_s, dtype=np.float64))
+        lat = np.zeros(len(q), dtype=np.float64)
+        rows = np.zeros(len(q), dtype=np.int64)
+        mk = C.c_double(0)
+        _check(lib().ral_server_run_trace(self._h, len(q), _p32(q), a.ctypes.data_as(C.POINTER(C.c_double)),
+                                          lat.ctypes.data_as(C.POINTER(C.c_double)),
+                                          rows.ctypes.data_as(C.POINTER(C.c_int64)), C.byref(mk)))
+        return lat, rows, mk.value
+
+    def stats(self) -> dict:
+        st = (C.c_int64 * 6)()
+        _check(lib().ral_server_stats(self._h, st))
+        return dict(submitted=st[0], completed=st[1], waves=st[2], max_wave_requests=st[3], peak_reserved=st[4],
+                    busy_s=st[5] / 1e6)
+
+    def close(self) -> None:
+        if self._h:
+            lib().ral_server_destroy(self._h)
+            self._h = None
+            self._tables = []
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

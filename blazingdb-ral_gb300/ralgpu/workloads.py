@@ -196,7 +196,9 @@ BATCH_DTYPES = [D.GDF_INT32, D.GDF_INT64, D.GDF_FLOAT32, D.GDF_FLOAT64]
 BATCH_ARITH = ["+", "-", "*", "/", "MOD"]
 BATCH_COMPARE = ["=", "<>", "<", ">", "<=", ">="]
 BATCH_LOGICAL = ["AND", "OR", "NOT"]
-BATCH_UNARY = ["FLOOR", "CEIL", "ABS", "SIN", "COS", "IS NULL", "IS NOT NULL"]
+# IS NOT NULL is left out: inside a LogicalProject the reference's expression-list rewrite
+# turns it into an unknown operator (only CASE(IS NOT NULL(x), x, y) survives, as COALESCE)
+BATCH_UNARY = ["FLOOR", "CEIL", "ABS", "SIN", "COS", "IS NULL"]
 
 
 @dataclass
@@ -223,7 +225,7 @@ def random_rex(rng, k: int, n_cols: int, literal_ok: bool = True) -> str:
         op = "NOT" if cat == 2 else BATCH_UNARY[int(rng.integers(0, len(BATCH_UNARY)))]
         if op.startswith("IS ") and k > 1:
             # the VM tests the mask of an input column, not of an intermediate register
-            op = BATCH_UNARY[int(rng.integers(0, len(BATCH_UNARY) - 2))]
+            op = BATCH_UNARY[int(rng.integers(0, len(BATCH_UNARY) - 1))]
         return f"{op}({random_rex(rng, k - 1, n_cols, False)})"
     ops = BATCH_ARITH if cat == 0 else BATCH_COMPARE if cat == 1 else ["AND", "OR"]
     op = ops[int(rng.integers(0, len(ops)))]
@@ -297,5 +299,135 @@ def batched_table_device(t: BatchTable, device="cuda"):
             valid, nulls = random_valid_mask(n, nr, g, device)
         else:
             valid, nulls = None, 0
+        cols.append((dt, v, valid, nulls))
+    return cols
+
+
+# ---- served: prepared filter + project queries over resident tables -------------------------
+
+SERVED_DTYPES = [D.GDF_INT32, D.GDF_INT64, D.GDF_FLOAT32, D.GDF_FLOAT64, D.GDF_DATE32]
+SERVED_NULL_RATE = 0.05
+
+
+@dataclass
+class ServedTable:
+    rows: int
+    dtypes: List[int]
+    seed: int
+
+
+@dataclass
+class ServedQuery:
+    table: int
+    filter: str
+    project: str
+    n_ops: int
+
+
+def served_tables(n_tables: int = 24, seed: int = SEED, min_rows: float = 1e4, max_rows: float = 1e8) -> List[ServedTable]:
+    """Resident tables: log-uniform row counts, 4-8 columns of int32/int64/float32/float64/date32."""
+    rng = np.random.default_rng(seed + 1)
+    out = []
+    for _ in range(n_tables):
+        rows = int(round(math.exp(rng.uniform(math.log(min_rows), math.log(max_rows)))))
+        nc = int(rng.integers(4, 9))
+        dts = [SERVED_DTYPES[int(i)] for i in rng.integers(0, len(SERVED_DTYPES), nc)]
+        out.append(ServedTable(rows, dts, int(rng.integers(0, 2**31))))
+    return out
+
+
+def _served_literal(rng, dtype: int) -> str:
+    """A literal inside the column's value range, so that comparisons keep a fraction of rows."""
+    if dtype == D.GDF_INT32:
+        return str(int(rng.integers(-900, 900)))
+    if dtype == D.GDF_INT64:
+        return str(int(rng.integers(-(1 << 19), 1 << 19)))
+    if dtype == D.GDF_DATE32:
+        return str(int(rng.integers(1000, 19000)))
+    if dtype == D.GDF_FLOAT32:
+        return f"{rng.uniform(-90, 90):.2f}"
+    return f"{rng.normal(0, 60):.2f}"
+
+
+def random_predicate(rng, k: int, dtypes: List[int]) -> str:
+    """A condition with exactly k operators whose root is a comparison or AND / OR."""
+    if k == 1:
+        c = int(rng.integers(0, len(dtypes)))
+        op = BATCH_COMPARE[int(rng.integers(2, 6))]
+        return f"{op}(${c}, {_served_literal(rng, dtypes[c])})"
+    if k >= 3 and rng.random() < 0.5:
+        a = int(rng.integers(1, k - 1))
+        op = "AND" if rng.random() < 0.6 else "OR"
+        return f"{op}({random_predicate(rng, a, dtypes)}, {random_predicate(rng, k - 1 - a, dtypes)})"
+    op = BATCH_COMPARE[int(rng.integers(2, 6))]
+    return f"{op}({random_rex(rng, k - 1, len(dtypes), False)}, {int(rng.integers(-50, 50))})"
+
+
+def served_queries(tables: List[ServedTable], n_queries: int = 96, seed: int = SEED, min_ops: int = 4,
+                   max_ops: int = 32) -> List[ServedQuery]:
+    """Prepared queries: a LogicalFilter and a LogicalProject over one table, 4-32 operators in
+    all (1 or more in the condition, the rest over 1-3 projected expressions), plus at times a
+    column passed through."""
+    rng = np.random.default_rng(seed + 2)
+    out = []
+    for _ in range(n_queries):
+        ti = int(rng.integers(0, len(tables)))
+        dts = tables[ti].dtypes
+        n_ops = int(rng.integers(min_ops, max_ops + 1))
+        kf = int(rng.integers(1, min(8, n_ops - 1) + 1))
+        kp = n_ops - kf
+        n_expr = int(rng.integers(1, min(3, kp) + 1))
+        cuts = sorted(rng.choice(np.arange(1, kp), n_expr - 1, replace=False).tolist()) if n_expr > 1 else []
+        parts = np.diff([0] + cuts + [kp]).tolist()
+        exprs = [f"e{i}=[{random_rex(rng, int(k), len(dts))}]" for i, k in enumerate(parts)]
+        if rng.random() < 0.5:
+            exprs.append(f"c{len(exprs)}=[${int(rng.integers(0, len(dts)))}]")
+        out.append(ServedQuery(ti, f"LogicalFilter(condition=[{random_predicate(rng, kf, dts)}])",
+                               "LogicalProject(" + ", ".join(exprs) + ")", n_ops))
+    return out
+
+
+def served_trace(n_requests: int, rate: float, n_queries: int, seed: int = SEED):
+    """Poisson arrivals at `rate` requests/s; each request runs a query drawn uniformly."""
+    rng = np.random.default_rng(seed + 3)
+    gaps = rng.exponential(1.0 / rate, n_requests)
+    arrivals = np.cumsum(gaps) - gaps[0]
+    queries = rng.integers(0, n_queries, n_requests).astype(np.int32)
+    return queries, arrivals
+
+
+def served_table_host(t: ServedTable, rows: Optional[int] = None):
+    """Host columns of a served table: list of (dtype, values, valid bools)."""
+    rng = np.random.default_rng(t.seed)
+    n = t.rows if rows is None else rows
+    cols = []
+    for dt in t.dtypes:
+        if dt == D.GDF_DATE32:
+            v = rng.integers(0, 20000, n, dtype=np.int32)
+        else:
+            v = _batch_values_np(rng, dt, n)
+        cols.append((dt, v, rng.random(n) >= SERVED_NULL_RATE))
+    return cols
+
+
+def served_table_device(t: ServedTable, device="cuda"):
+    """Device columns of a served table: list of (dtype, tensor, packed mask, null count)."""
+    import torch
+    g = torch.Generator(device=device)
+    g.manual_seed(t.seed)
+    n = t.rows
+    cols = []
+    for dt in t.dtypes:
+        if dt == D.GDF_INT32:
+            v = torch.randint(-1000, 1000, (n,), generator=g, device=device, dtype=torch.int32)
+        elif dt == D.GDF_DATE32:
+            v = torch.randint(0, 20000, (n,), generator=g, device=device, dtype=torch.int32)
+        elif dt == D.GDF_INT64:
+            v = torch.randint(-(1 << 20), 1 << 20, (n,), generator=g, device=device, dtype=torch.int64)
+        elif dt == D.GDF_FLOAT32:
+            v = torch.rand(n, generator=g, device=device, dtype=torch.float32) * 200 - 100
+        else:
+            v = torch.randn(n, generator=g, device=device, dtype=torch.float64) * 100
+        valid, nulls = random_valid_mask(n, SERVED_NULL_RATE, g, device)
         cols.append((dt, v, valid, nulls))
     return cols

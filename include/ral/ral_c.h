@@ -275,6 +275,47 @@ int64_t ral_kernel_launches(void);
 /* JIT counters: kernels compiled, disk-cache hits, memory-cache hits, total compile ms. */
 int ral_jit_stats(int64_t *compiles, int64_t *disk_hits, int64_t *memory_hits, double *compile_ms);
 
+/*
+ * Served execution (no reference counterpart: the reference runs one query at a time).  A
+ * server keeps registered tables resident (the caller's device columns, not copied), plans
+ * filter + project queries over them, and runs submitted requests with continuous batching:
+ * a scheduler thread admits requests while resident tables plus the outputs of admitted
+ * requests stay under budget_bytes, and launches every admitted request as one wave of the
+ * persistent dispatcher; up to max_waves waves are in flight at once.
+ */
+typedef struct ral_server_s ral_server;
+int ral_server_create(int64_t budget_bytes, int32_t max_waves, int32_t max_wave_requests, ral_server **server);
+int ral_server_add_table(ral_server *server, gdf_column *const *columns, int32_t num_columns, int32_t *table_id);
+/* filter_query_part: "LogicalFilter(condition=[...])"; project_query_part: "LogicalProject(...)". */
+int ral_server_add_query(ral_server *server, int32_t table_id, const char *filter_query_part,
+                         const char *project_query_part, int32_t *query_id);
+/* dtype and mask presence (0/1) of each projected column; *num_outputs receives the count. */
+int ral_server_query_outputs(ral_server *server, int32_t query_id, gdf_dtype *dtypes, int32_t *has_valid,
+                             int32_t capacity, int32_t *num_outputs);
+/* Compiles every query's chunk function and links the dispatcher without loading it (no GPU
+ * needed); the ptxas / link log goes to log_out. */
+int ral_server_debug_compile(ral_server *server, char *log_out, int64_t log_capacity);
+/* Compiles every query, links the dispatcher and starts the scheduler thread. */
+int ral_server_start(ral_server *server);
+/* keep != 0: the outputs stay allocated for ral_server_result until ral_server_release. */
+int ral_server_submit(ral_server *server, int32_t query_id, int32_t keep, int64_t *request_id);
+/* Blocks up to timeout_s; *latency_s is submit-to-completion on the server's clock. */
+int ral_server_wait(ral_server *server, int64_t request_id, double timeout_s, int64_t *rows_out, double *latency_s);
+/* Descriptors of a kept request's outputs (device memory owned by the server). */
+int ral_server_result(ral_server *server, int64_t request_id, gdf_column *out_columns, int32_t num_outputs);
+/* Copies a kept request's outputs into the caller's columns (device buffers of at least the
+ * kept row count; masks 64-byte padded) and sets their size and null_count. */
+int ral_server_copy_result(ral_server *server, int64_t request_id, gdf_column *const *out_columns,
+                           int32_t num_outputs);
+int ral_server_release(ral_server *server, int64_t request_id);
+/* Submits request k (query queries[k]) at arrival_s[k] seconds after the call starts, waits for
+ * all, and fills each latency (from the scheduled arrival to completion) and kept row count. */
+int ral_server_run_trace(ral_server *server, int32_t num_requests, const int32_t *queries, const double *arrival_s,
+                         double *latency_s, int64_t *rows_out, double *makespan_s);
+/* stats: submitted, completed, waves, largest wave, peak reserved bytes, busy microseconds. */
+int ral_server_stats(ral_server *server, int64_t *stats6);
+int ral_server_destroy(ral_server *server);
+
 #ifdef __cplusplus
 }
 #endif

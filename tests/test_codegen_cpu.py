@@ -89,7 +89,7 @@ FILTER_CASES = [
      None),
     ("is null + coalesce projection", [D.GDF_INT32, D.GDF_FLOAT64, D.GDF_INT64], [1, 1, 0],
      "LogicalFilter(condition=[AND(IS NULL($0), >($2, 5))])",
-     "LogicalProject(a=[$2], b=[CASE(IS NOT NULL($0), $0, -1)], c=[IS NOT NULL($1)], d=[*($1, 2.5)])"),
+     "LogicalProject(a=[$2], b=[CASE(IS NOT NULL($0), $0, -1)], c=[IS NULL($1)], d=[*($1, 2.5)])"),
 ]
 
 

@@ -133,3 +133,19 @@ def test_project_output_types():
     for kind, v in pp.columns:
         exp.append(pp.output_types[v] if kind == "expr" else frame[v])
     assert types == exp
+
+
+def test_is_not_null_in_a_projection_is_rejected_like_the_reference():
+    """The reference's projection rewrite drops " NOT NULL" before parsing, so IS NOT NULL outside
+    the CASE(IS NOT NULL(x), x, y) pattern is an unknown operator there; both sides reject it."""
+    import ralgpu
+    from oracle import frontend as fe
+    frame = [ralgpu.dtypes.GDF_INT64, ralgpu.dtypes.GDF_FLOAT64]
+    q = "LogicalProject(a=[+($0, 1)], b=[IS NOT NULL($1)])"
+    with pytest.raises(ralgpu.RalError):
+        ralgpu.parse_project_plan(frame, q)
+    with pytest.raises(fe.FrontendError):
+        fe.parse_project_plan(frame, q)
+    ok = "LogicalProject(a=[CASE(IS NOT NULL($1), $1, 0)], b=[IS NULL($1)])"
+    assert len(ralgpu.parse_project_plan(frame, ok)["evaluated_dtypes"]) == 2
+    assert len(fe.parse_project_plan(frame, ok).output_types) == 2

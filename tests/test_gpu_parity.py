@@ -485,3 +485,22 @@ def test_filter_unaligned_frame(filter_mode):
     exp = O.process_filter([O.make_column(v[1:], t) for t, v, _ in base], q)
     for g, e in zip(got, exp):
         H.assert_columns_equal(g, e)
+
+
+def test_integer_division_by_zero_and_overflow_are_defined():
+    """x / 0, x % 0, INT64_MIN / -1 and x % -1 are undefined in the reference; both sides define
+    them the same way (0, 0, INT64_MIN, 0), so every kernel and the oracle agree bit for bit."""
+    n = 4096
+    rng = np.random.default_rng(77)
+    a = rng.integers(-(1 << 62), 1 << 62, n, dtype=np.int64)
+    b = rng.choice(np.array([0, -1, 1, 7, -3, np.iinfo(np.int64).min], dtype=np.int64), n)
+    a[:64] = np.iinfo(np.int64).min
+    b[:32] = -1
+    spec = [(D.GDF_INT64, a, None), (D.GDF_INT64, b, (rng.random(n) > 0.1))]
+    J = (D.GDF_INT32, 0)
+    prog = dict(left=[0, 0, 0], right=[1, 1, 1], outputs=[2, 3, 4], final=[2, 3, 4],
+                ops=[D.GDF_DIV, D.GDF_MOD, D.GDF_FLOOR_DIV], uops=[D.BLZ_INVALID_UNARY] * 3,
+                lscalars=[J] * 3, rscalars=[J] * 3)
+    dev, ora = H.run_program_both(spec, [D.GDF_INT64, D.GDF_INT64, D.GDF_INT64], prog)
+    for k, (g, e) in enumerate(zip(dev, ora)):
+        H.assert_columns_equal(g, e, what=f"output {k}", check_null_count=False)

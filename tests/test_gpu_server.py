@@ -1,0 +1,123 @@
+"""Served execution on the GPU: a request gives the same bits alone, in a mix of concurrent
+requests and under a tight memory budget, equal to the plain fused filter_project call and,
+for queries without transcendental operators, to the oracle."""
+import numpy as np
+import pytest
+
+import helpers as H
+import oracle as O
+import ralgpu as R
+from ralgpu import workloads as W
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def served():
+    tabs = W.served_tables(6, seed=41, min_rows=1_000, max_rows=300_000)
+    qs = W.served_queries(tabs, 16, seed=41)
+    host = [W.served_table_host(t) for t in tabs]
+    dev = [H.to_device(h) for h in host]
+    return tabs, qs, host, dev
+
+
+def _server(tabs, qs, dev, budget=8 << 30, waves=2):
+    srv = R.Server(budget_bytes=budget, max_waves=waves, max_wave_requests=256)
+    tids = [srv.add_table(d) for d in dev]
+    qids = [srv.add_query(tids[q.table], q.filter, q.project) for q in qs]
+    srv.start()
+    return srv, qids
+
+
+def _same_bits(a: R.Column, b: R.Column, what: str):
+    assert a.size == b.size, f"{what}: {a.size} rows vs {b.size}"
+    assert (a.valid is None) == (b.valid is None), f"{what}: mask presence"
+    va, vb = a.valid_bools(), b.valid_bools()
+    assert np.array_equal(va, vb), f"{what}: masks differ"
+    x, y = a.to_numpy()[va], b.to_numpy()[va]
+    assert np.array_equal(x.view(np.uint8), y.view(np.uint8)), f"{what}: data differ"
+    assert a.null_count == b.null_count, f"{what}: null_count {a.null_count} vs {b.null_count}"
+
+
+def _alone(srv, qid):
+    rid = srv.submit(qid, keep=True)
+    return srv.result(rid, qid)
+
+
+def _transcendental(q):
+    return "SIN(" in q.project or "COS(" in q.project or "SIN(" in q.filter or "COS(" in q.filter
+
+
+def test_each_query_alone_matches_filter_project_and_oracle(served):
+    tabs, qs, host, dev = served
+    srv, qids = _server(tabs, qs, dev)
+    checked = 0
+    for i, (q, qid) in enumerate(zip(qs, qids)):
+        got = _alone(srv, qid)
+        plain = R.filter_project(dev[q.table], q.filter, q.project)
+        assert len(got) == len(plain)
+        for k, (g, p) in enumerate(zip(got, plain)):
+            _same_bits(g, p, f"query {i} output {k} vs filter_project")
+        if _transcendental(q):
+            continue
+        ef = O.process_filter(H.to_oracle(host[q.table]), q.filter)
+        ep = O.execute_project_plan(ef, q.project)
+        for k, (g, e) in enumerate(zip(got, ep)):
+            H.assert_columns_equal(g, e, what=f"query {i} output {k} vs oracle")
+        checked += 1
+    assert checked >= 4
+    srv.close()
+
+
+def test_results_are_the_same_alone_and_in_the_mix(served):
+    tabs, qs, host, dev = served
+    srv, qids = _server(tabs, qs, dev)
+    alone = {i: _alone(srv, qids[i]) for i in range(len(qs))}
+    rng = np.random.default_rng(3)
+    picks = rng.integers(0, len(qs), 400)
+    keep = rng.random(400) < 0.15
+    rids = [srv.submit(qids[p], keep=bool(k)) for p, k in zip(picks, keep)]   # all in flight together
+    for rid, p, k in zip(rids, picks, keep):
+        rows, lat = srv.wait(rid)
+        assert rows == alone[p][0].size and lat > 0
+        if k:
+            got = srv.result(rid, qids[p])
+            for j, (g, a) in enumerate(zip(got, alone[p])):
+                _same_bits(g, a, f"query {p} output {j} in the mix")
+        else:
+            srv.release(rid)
+    st = srv.stats()
+    assert st["completed"] >= 400 + len(qs)
+    assert st["waves"] < st["completed"]          # requests shared waves
+    srv.close()
+
+
+def test_tight_budget_admits_fewer_requests_and_changes_nothing(served):
+    tabs, qs, host, dev = served
+    srv0, qids0 = _server(tabs, qs, dev)
+    alone = {i: _alone(srv0, qids0[i]) for i in range(len(qs))}
+    srv0.close()
+    table_bytes = sum(c.size * R.dtypes.WIDTH[c.dtype] + R.valid_alloc_size(c.size) for d in dev for c in d)
+    # room for about two of the largest requests at a time
+    biggest = max(t.rows for t in tabs) * 64
+    budget = table_bytes + 2 * biggest
+    srv, qids = _server(tabs, qs, dev, budget=budget, waves=3)
+    rids = [(srv.submit(qids[i % len(qs)], keep=True), i % len(qs)) for i in range(3 * len(qs))]
+    for rid, i in rids:
+        got = srv.result(rid, qids[i])
+        for j, (g, a) in enumerate(zip(got, alone[i])):
+            _same_bits(g, a, f"query {i} output {j} under the budget")
+    st = srv.stats()
+    assert st["peak_reserved"] <= budget - table_bytes
+    srv.close()
+
+
+def test_trace_reports_latency_and_rows(served):
+    tabs, qs, host, dev = served
+    srv, qids = _server(tabs, qs, dev)
+    alone_rows = [_alone(srv, q)[0].size for q in qids]
+    qi, arr = W.served_trace(300, 2000.0, len(qs), seed=5)
+    lat, rows, makespan = srv.run_trace([qids[i] for i in qi], arr)
+    assert np.all(lat > 0) and makespan > 0
+    assert [int(r) for r in rows] == [alone_rows[i] for i in qi]
+    srv.close()
