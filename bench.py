@@ -685,7 +685,8 @@ def run_served(args):
     torch.cuda.synchronize()
     gen_s = time.perf_counter() - t0
     budget = int(args.budget_gb * (1 << 30))
-    srv = R.Server(budget_bytes=budget, max_waves=args.waves, max_wave_requests=1024)
+    srv = R.Server(budget_bytes=budget, max_waves=args.waves, max_wave_requests=1024,
+                   wave_rows=args.wave_rows)
     tids = [srv.add_table(f) for f in frames]
     qids = [srv.add_query(tids[q.table], q.filter, q.project) for q in qs]
     t0 = time.perf_counter()
@@ -714,8 +715,9 @@ def run_served(args):
     wq, wa = W.served_trace(min(500, n_rate), 1e9, len(qs), seed=args.seed + 99)
     srv.run_trace(wq, np.zeros(len(wq)))
     cq, _ = W.served_trace(min(4000, 2 * n_rate), 1.0, len(qs), seed=args.seed + 7)
-    lat, rows, mk = srv.run_trace(cq, np.zeros(len(cq)))
-    capacity = len(cq) / mk
+    lat, rows, cap_mk = srv.run_trace(cq, np.zeros(len(cq)))
+    capacity = len(cq) / cap_mk
+    serial_mk = float(service[cq].sum())          # the same requests, one at a time
     sampler = ClockSampler(local)
     sampler.start()
     launches0 = R.kernel_launches()
@@ -745,7 +747,6 @@ def run_served(args):
     clocks = sampler.stop()
     launches = R.kernel_launches() - launches0
     st = srv.stats()
-    serial_capacity = 1.0 / float(service.mean())
     top = per_rate[-1]
     out = {
         "metric": METRIC, "value": top["served"]["rows_per_s"], "unit": "rows/s", "n_gpus": world,
@@ -755,11 +756,14 @@ def run_served(args):
         "config": {"workload": "served", "tables": len(tabs), "rows_resident": int(sum(t.rows for t in tabs)),
                    "queries": len(qs), "ops": "4-32 per request (filter + project)", "nulls": "5% per column",
                    "requests": int(n_rate * len(per_rate)), "arrivals": "Poisson, 5 rates",
-                   "budget_gb": args.budget_gb, "max_waves": args.waves, "parallelism": f"replicas x{world}",
+                   "budget_gb": args.budget_gb, "max_waves": args.waves, "wave_rows": args.wave_rows or "default",
+                   "parallelism": f"replicas x{world}",
                    "l2": "tables of up to 1e8 rows exceed L2; no flush"},
-        "served_capacity_rps": capacity, "serial_plain_capacity_rps": serial_capacity,
-        "served_rows_per_s_at_capacity": float(q_rows[cq].sum() / mk),
-        "serial_plain_rows_per_s": float(q_rows.mean() / service.mean()),
+        "capacity": {"requests": int(len(cq)), "arrivals": "all at once",
+                     "served_rps": capacity, "serial_plain_rps": len(cq) / serial_mk,
+                     "served_rows_per_s": float(q_rows[cq].sum() / cap_mk),
+                     "serial_plain_rows_per_s": float(q_rows[cq].sum() / serial_mk),
+                     "speedup_vs_serial_plain": serial_mk / cap_mk},
         "per_rate": per_rate,
         "server": dict(st, start_s=round(start_s, 2), generate_s=round(gen_s, 2)),
         "gpu_launches": int(launches), "clocks": clocks, "e2e": None,
@@ -832,6 +836,7 @@ def main():
     ap.add_argument("--requests", type=int, default=50_000)
     ap.add_argument("--budget-gb", type=float, default=120.0)
     ap.add_argument("--waves", type=int, default=2)
+    ap.add_argument("--wave-rows", type=int, default=0, help="served: rows per wave (0: the library default)")
     ap.add_argument("--programs", type=int, default=256)
     ap.add_argument("--seed", type=int, default=20261203)
     ap.add_argument("--plain-steps", type=int, default=3)

@@ -348,8 +348,9 @@ int Batch::launch(cudaStream_t st) {
     unsigned int* counter = d_counter_;
     long long total = total_items_;
     const void* fn = d_fn_;
+    const void* base = nullptr;
     int stride = stride_;
-    void* args[] = {&descs, &stride, &prefix, &fn, &np, &counter, &total};
+    void* args[] = {&descs, &stride, &prefix, &base, &fn, &np, &counter, &total};
     return check_cuda(cudaLaunchKernel((const void*)kernel_->kernel, dim3(grid_), dim3(256), args, smem_, st),
                       "launch of the batch kernel");
 }

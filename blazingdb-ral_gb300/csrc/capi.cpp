@@ -426,7 +426,7 @@ int ral_debug_filter_source(const gdf_dtype* frame_dtypes, const int32_t* frame_
 
 struct ral_server_s {
     ral::Server s;
-    ral_server_s(size_t b, int w, int m) : s(b, w, m) {}
+    ral_server_s(size_t b, int w, int m, int64_t r) : s(b, w, m, r) {}
 };
 
 struct ral_batch_s {
@@ -600,10 +600,11 @@ int ral_jit_stats(int64_t* compiles, int64_t* disk_hits, int64_t* memory_hits, d
     return 0;
 }
 
-int ral_server_create(int64_t budget_bytes, int32_t max_waves, int32_t max_wave_requests, ral_server** server) {
+int ral_server_create(int64_t budget_bytes, int32_t max_waves, int32_t max_wave_requests, int64_t wave_rows,
+                      ral_server** server) {
     return guarded([&] {
-        if (!server || budget_bytes <= 0) return set_error(kInvalidArgument, "bad argument");
-        *server = new ral_server_s((size_t)budget_bytes, max_waves, max_wave_requests);
+        if (!server || budget_bytes <= 0 || wave_rows < 0) return set_error(kInvalidArgument, "bad argument");
+        *server = new ral_server_s((size_t)budget_bytes, max_waves, max_wave_requests, wave_rows);
         return (int)kSuccess;
     });
 }

@@ -1006,10 +1006,11 @@ GeneratedKernel generate_batch_item(const Program& p, const Shape& sh) {
     return gk;
 }
 
-GeneratedKernel generate_batch_dispatch(const std::vector<DispatchEntry>& items, int smem_words_per_warp) {
+GeneratedKernel generate_batch_dispatch(const std::vector<DispatchEntry>& items, int smem_words_per_warp, int grab) {
     GeneratedKernel gk;
+    grab = std::max(1, std::min(grab, 64));
     std::ostringstream key;
-    key << "dispatch|" << smem_words_per_warp << "|";
+    key << "dispatch|" << smem_words_per_warp << "|g" << grab << "|";
     for (const auto& it : items) key << it.name << (it.filter ? "f" : "") << ";";
     char hex[32];
     snprintf(hex, sizeof hex, "%016llx", (unsigned long long)fnv1a(key.str()));
@@ -1024,20 +1025,24 @@ GeneratedKernel generate_batch_dispatch(const std::vector<DispatchEntry>& items,
         else
             os << "extern \"C\" __device__ void " << it.name << "(const ral_u64* __restrict__ slots, const ral_i64 t);\n";
     }
-    os << "#define RAL_BATCH_GRAB 8\n";
+    os << "#define RAL_BATCH_GRAB " << grab << "\n";
     // dynamic shared memory: item prefix (n_programs + 1 long longs), one function index per
     // program, then each warp's area for filter items
     os << "extern \"C\" __global__ void __launch_bounds__(256) " << gk.name
        << "(const ral_u64* __restrict__ descs, const int stride, const long long* __restrict__ item_prefix, "
-          "const int* __restrict__ fn_index, const int np, unsigned int* counter, const long long total_items) {\n";
+          "const long long* __restrict__ item_base, const int* __restrict__ fn_index, const int np, "
+          "unsigned int* counter, const long long total_items) {\n";
     os << "    extern __shared__ long long s_prefix[];\n";
-    os << "    int* s_fn = reinterpret_cast<int*>(s_prefix + np + 1);\n";
+    os << "    long long* s_base = s_prefix + np + 1;\n";
+    os << "    int* s_fn = reinterpret_cast<int*>(s_base + np);\n";
     os << "    for (int i = threadIdx.x; i <= np; i += blockDim.x) s_prefix[i] = item_prefix[i];\n";
+    // item t of entry q is the entry's tile / chunk item_base[q] + t (0 without item_base)
+    os << "    for (int i = threadIdx.x; i < np; i += blockDim.x) s_base[i] = item_base ? item_base[i] : 0;\n";
     os << "    for (int i = threadIdx.x; i < np; i += blockDim.x) s_fn[i] = fn_index[i];\n";
     os << "    __syncthreads();\n";
     os << "    const int lane = threadIdx.x & 31;\n";
     if (smem_words_per_warp > 0) {
-        os << "    const size_t head = ((size_t)(np + 1) * 8 + (size_t)np * 4 + 15) & ~(size_t)15;\n";
+        os << "    const size_t head = ((size_t)(np + 1) * 8 + (size_t)np * 12 + 15) & ~(size_t)15;\n";
         os << "    ral_u32* const wsm = reinterpret_cast<ral_u32*>(reinterpret_cast<char*>(s_prefix) + head) + "
               "(threadIdx.x >> 5) * " << smem_words_per_warp << ";\n";
     }
@@ -1055,7 +1060,7 @@ GeneratedKernel generate_batch_dispatch(const std::vector<DispatchEntry>& items,
     os << "                while (hi - lo > 1) { const int mid = (lo + hi) >> 1; if (s_prefix[mid] <= item) lo = mid; else hi = mid; }\n";
     os << "            }\n";
     os << "            const ral_u64* slots = descs + (size_t)lo * stride;\n";
-    os << "            const ral_i64 t = item - s_prefix[lo];\n";
+    os << "            const ral_i64 t = item - s_prefix[lo] + s_base[lo];\n";
     os << "            switch (s_fn[lo]) {\n";
     for (int f = 0; f < NF; f++)
         os << "            case " << f << ": " << items[f].name << (items[f].filter ? "(slots, t, wsm)" : "(slots, t)")

@@ -60,10 +60,11 @@ struct GeneratedKernel {
 // with slots laid out as gk.layout.  A dispatcher kernel, linked with the item functions, takes
 // work items (program, tile) from a device counter in chunks, finds the program by binary search
 // over the item prefix (in shared memory) and calls its function:
-//   <name>(const ral_u64* descs, int stride, const long long* item_prefix, const int* fn_index,
-//          int n_programs, unsigned int* counter, long long total_items)
-// descs holds `stride` slots per program; fn_index[q] indexes item_names.  Dynamic shared memory:
-// (n_programs + 1) * 8 + n_programs * 4 bytes.
+//   <name>(const ral_u64* descs, int stride, const long long* item_prefix, const long long* item_base,
+//          const int* fn_index, int n_programs, unsigned int* counter, long long total_items)
+// descs holds `stride` slots per program; fn_index[q] indexes the item functions; item t of
+// program q runs tile item_base[q] + t (item_base may be null: all 0), so a request's chunks can
+// be spread over several launches.
 // Filter + project requests are batched the same way: their item function is the fused filter
 // kernel's chunk body (generate_filter_kernel with item = true),
 //   extern "C" __device__ void <name>(const ral_u64* slots, long long chunk, unsigned* warp_smem)
@@ -74,11 +75,15 @@ struct DispatchEntry {
     bool filter = false;  // takes the warp's shared-memory area
 };
 // smem_words_per_warp: largest item_smem_words over the filter items (0 if none).  The dynamic
-// shared memory is then (n_programs + 1) * 8 + n_programs * 4 (rounded up to 16) plus
-// 8 warps * smem_words_per_warp * 4 bytes.
-GeneratedKernel generate_batch_dispatch(const std::vector<DispatchEntry>& items, int smem_words_per_warp);
+// shared memory is then (n_programs + 1) * 8 + n_programs * 12 (rounded up to 16) plus
+// 8 warps * smem_words_per_warp * 4 bytes.  A warp takes `grab` consecutive items per atomic
+// and runs them in order.  Filter items need grab = 1: a chunk's look-back waits on the chunk
+// before it, so a warp holding several consecutive chunks would make the next warp wait for
+// all of them and the chunks of a request would run one warp after another.
+GeneratedKernel generate_batch_dispatch(const std::vector<DispatchEntry>& items, int smem_words_per_warp,
+                                        int grab = 8);
 inline size_t batch_dispatch_smem(int n_programs, int smem_words_per_warp) {
-    const size_t head = ((size_t)(n_programs + 1) * 8 + (size_t)n_programs * 4 + 15) & ~(size_t)15;
+    const size_t head = ((size_t)(n_programs + 1) * 8 + (size_t)n_programs * 12 + 15) & ~(size_t)15;
     return head + (size_t)8 * smem_words_per_warp * 4;
 }
 

@@ -60,9 +60,10 @@ RequestLayout request_layout(const ServerQuery& q, int64_t rows) {
 
 }  // namespace
 
-Server::Server(size_t budget_bytes, int max_waves, int max_wave_requests)
+Server::Server(size_t budget_bytes, int max_waves, int max_wave_requests, int64_t wave_rows)
     : budget_(budget_bytes), max_waves_(std::max(1, std::min(max_waves, 8))),
       max_wave_requests_(std::max(1, std::min(max_wave_requests, 4096))) {
+    wave_rows_ = wave_rows > 0 ? wave_rows : ((int64_t)32 << 20);
     t0_ = 0;
     t0_ = now();
 }
@@ -119,7 +120,8 @@ int Server::add_query(int table_id, const char* filter_q, const char* project_q,
     if (int e = plan_filter_project(frame.data(), (int)frame.size(), filter_q, project_q, q->plan)) return e;
     const Shape sh = query_shape(*q->plan, al);
     q->item = generate_filter_kernel(q->plan->spec, sh, true);
-    q->chunks = (t.rows + filter_tile_rows(sh) - 1) / filter_tile_rows(sh);
+    // at least one chunk, so that an empty table's request still runs (and finishes) once
+    q->chunks = std::max<int64_t>(1, (t.rows + filter_tile_rows(sh) - 1) / filter_tile_rows(sh));
     q->reserve = request_layout(*q, t.rows).total;
     if (q->plan->out_dtypes.size() > 64) return set_error(kUnsupported, "more than 64 projected columns");
     if (tables_bytes_ + q->reserve > budget_)
@@ -152,7 +154,7 @@ int Server::ensure_linked() {
         stride = std::max(stride, queries_[i]->item.layout.total);
         smem = std::max(smem, queries_[i]->item.item_smem_words);
     }
-    GeneratedKernel disp = generate_batch_dispatch(entries, smem);
+    GeneratedKernel disp = generate_batch_dispatch(entries, smem, 1);
     tus.push_back(disp);
     std::vector<const std::vector<char>*> objs;
     if (int e = compile_items(tus, objs, nullptr)) return e;
@@ -175,9 +177,10 @@ int Server::ensure_linked() {
     stride_ = stride;
     smem_words_ = smem;
     linked_queries_ = (int)queries_.size();
-    // wave buffers: descs | prefix | fn | counter
+    // wave buffers: descs | prefix | base | fn | counter
     const size_t M = (size_t)max_wave_requests_;
-    const size_t bytes = round_up(M * stride_ * 8, 16) + round_up((M + 1) * 8, 16) + round_up(M * 4, 16) + 16;
+    const size_t bytes =
+        round_up(M * stride_ * 8, 16) + round_up((M + 1) * 8, 16) + round_up(M * 8, 16) + round_up(M * 4, 16) + 16;
     if (waves_.empty()) waves_.resize(max_waves_);
     for (auto& w : waves_) {
         if (!w.stream && check_cuda(cudaStreamCreateWithFlags(&w.stream, cudaStreamNonBlocking), "cudaStreamCreate"))
@@ -212,7 +215,7 @@ int Server::debug_compile(std::string& log) {
         entries.push_back({q->item.name, true});
         smem = std::max(smem, q->item.item_smem_words);
     }
-    tus.push_back(generate_batch_dispatch(entries, smem));
+    tus.push_back(generate_batch_dispatch(entries, smem, 1));
     std::vector<const std::vector<char>*> objs;
     if (int e = compile_items(tus, objs, &log)) return e;
     std::string err, llog;
@@ -257,77 +260,92 @@ int Server::submit(int query_id, bool keep, int64_t* request_id) {
     return kSuccess;
 }
 
-int Server::launch_wave(Wave& w, std::vector<int64_t>& batch) {
-    const int NP = (int)batch.size();
+int Server::launch_wave(Wave& w, const std::vector<int64_t>& reqs, const std::vector<int64_t>& take) {
+    const int NP = (int)reqs.size();
     const size_t M = (size_t)max_wave_requests_;
     char* h = (char*)w.h_desc;
     uint64_t* descs = (uint64_t*)h;
     const size_t off_prefix = round_up(M * stride_ * 8, 16);
-    const size_t off_fn = off_prefix + round_up((M + 1) * 8, 16);
+    const size_t off_base = off_prefix + round_up((M + 1) * 8, 16);
+    const size_t off_fn = off_base + round_up(M * 8, 16);
     const size_t off_counter = off_fn + round_up(M * 4, 16);
     long long* prefix = (long long*)(h + off_prefix);
+    long long* base = (long long*)(h + off_base);
     int* fn = (int*)(h + off_fn);
     std::memset(h + off_counter, 0, 16);
     prefix[0] = 0;
     const double t = now();
     std::vector<uint64_t> slots;
+    w.last.assign(NP, 0);
     for (int k = 0; k < NP; k++) {
-        ServerRequest& r = *requests_[batch[k]];
+        ServerRequest& r = *requests_[reqs[k]];
         ServerQuery& q = *queries_[r.query];
         ServerTable& tb = tables_[q.table];
-        const RequestLayout L = request_layout(q, tb.rows);
-        void* base = nullptr;
-        if (int e = check_cuda(cudaMallocAsync(&base, L.total, w.stream), "cudaMallocAsync")) return e;
-        cudaMemsetAsync(base, 0, L.zero_bytes, w.stream);
-        r.scratch = base;
-        const int NO = (int)q.plan->out_dtypes.size();
-        r.out_data.assign(NO, nullptr);
-        r.out_valid.assign(NO, nullptr);
-        for (int o = 0; o < NO; o++) {
-            r.out_data[o] = (char*)base + L.data_off[o];
-            if (L.valid_off[o] != (size_t)-1) r.out_valid[o] = (char*)base + L.valid_off[o];
+        if (r.next_chunk == 0) {
+            // first slice: the request's outputs and scratch, zeroed where the kernel expects it
+            const RequestLayout L = request_layout(q, tb.rows);
+            void* mem = nullptr;
+            if (int e = check_cuda(cudaMallocAsync(&mem, L.total, w.stream), "cudaMallocAsync")) return e;
+            cudaMemsetAsync(mem, 0, L.zero_bytes, w.stream);
+            r.scratch = mem;
+            const int NO = (int)q.plan->out_dtypes.size();
+            r.out_data.assign(NO, nullptr);
+            r.out_valid.assign(NO, nullptr);
+            for (int o = 0; o < NO; o++) {
+                r.out_data[o] = (char*)mem + L.data_off[o];
+                if (L.valid_off[o] != (size_t)-1) r.out_valid[o] = (char*)mem + L.valid_off[o];
+            }
+            r.t_launch = t;
         }
         std::vector<gdf_column*> frame;
         for (auto& c : tb.cols) frame.push_back(&c);
-        filter_fill_slots(*q.plan, q.item, frame.data(), tb.rows, r.out_data.data(), r.out_valid.data(), base, slots);
+        filter_fill_slots(*q.plan, q.item, frame.data(), tb.rows, r.out_data.data(), r.out_valid.data(), r.scratch,
+                          slots);
         std::memset(descs + (size_t)k * stride_, 0, (size_t)stride_ * 8);
         std::memcpy(descs + (size_t)k * stride_, slots.data(), slots.size() * 8);
-        prefix[k + 1] = prefix[k] + q.chunks;
+        prefix[k + 1] = prefix[k] + take[k];
+        base[k] = r.next_chunk;
         fn[k] = q.fn;
-        r.t_launch = t;
+        r.next_chunk += take[k];
+        w.last[k] = r.next_chunk >= q.chunks;
+        r.in_wave = true;
     }
     const long long total = prefix[NP];
-    if (total > ((long long)1 << 31)) return set_error(kInvalidArgument, "wave too large: more than 2^31 chunks");
     char* d = (char*)w.d_desc;
     cudaMemcpyAsync(d, h, (size_t)NP * stride_ * 8, cudaMemcpyHostToDevice, w.stream);
     cudaMemcpyAsync(d + off_prefix, h + off_prefix, (size_t)(NP + 1) * 8, cudaMemcpyHostToDevice, w.stream);
+    cudaMemcpyAsync(d + off_base, h + off_base, (size_t)NP * 8, cudaMemcpyHostToDevice, w.stream);
     cudaMemcpyAsync(d + off_fn, h + off_fn, (size_t)NP * 4, cudaMemcpyHostToDevice, w.stream);
     cudaMemcpyAsync(d + off_counter, h + off_counter, 16, cudaMemcpyHostToDevice, w.stream);
     const void* a_descs = d;
     int a_stride = stride_;
     const void* a_prefix = d + off_prefix;
+    const void* a_base = d + off_base;
     const void* a_fn = d + off_fn;
     int a_np = NP;
     unsigned int* a_counter = (unsigned int*)(d + off_counter);
     long long a_total = total;
-    void* args[] = {&a_descs, &a_stride, &a_prefix, &a_fn, &a_np, &a_counter, &a_total};
-    const long long warps_needed = (total + 7) / 8;
-    const int grid = (int)std::max<long long>(1, std::min<long long>(grid_, (warps_needed + 7) / 8));
+    void* args[] = {&a_descs, &a_stride, &a_prefix, &a_base, &a_fn, &a_np, &a_counter, &a_total};
+    const int grid = (int)std::max<long long>(1, std::min<long long>(grid_, (total + 7) / 8));
     const size_t smem = batch_dispatch_smem(NP, smem_words_);
-    if (int e = check_cuda(cudaLaunchKernel((const void*)kernel_->kernel, dim3(grid), dim3(256), args, smem, w.stream),
-                           "launch of the served dispatcher"))
-        return e;
-    note_launch();
-    // scratch headers back to the host: error flag, kept rows, valid counts
+    if (total > 0) {
+        if (int e = check_cuda(cudaLaunchKernel((const void*)kernel_->kernel, dim3(grid), dim3(256), args, smem, w.stream),
+                               "launch of the served dispatcher"))
+            return e;
+        note_launch();
+    }
+    // scratch headers of the requests that finish in this wave: error flag, kept rows, valid counts
     uint64_t* hh = (uint64_t*)w.h_head;
     for (int k = 0; k < NP; k++) {
-        ServerRequest& r = *requests_[batch[k]];
+        if (!w.last[k]) continue;
+        ServerRequest& r = *requests_[reqs[k]];
         const int NO = (int)queries_[r.query]->plan->out_dtypes.size();
         cudaMemcpyAsync(hh + (size_t)k * 67, r.scratch, (size_t)filter_scratch_header(NO) * 8, cudaMemcpyDeviceToHost,
                         w.stream);
     }
     if (int e = check_cuda(cudaEventRecord(w.done, w.stream), "cudaEventRecord")) return e;
-    w.reqs = batch;
+    w.reqs = reqs;
+    w.take = take;
     w.busy = true;
     w.t_launch = t;
     if (inflight_ == 0) busy_since_ = t;
@@ -342,6 +360,8 @@ void Server::finish_wave(Wave& w) {
     const uint64_t* hh = (const uint64_t*)w.h_head;
     for (size_t k = 0; k < w.reqs.size(); k++) {
         ServerRequest& r = *requests_[w.reqs[k]];
+        r.in_wave = false;
+        if (!w.last[k]) continue;
         ServerQuery& q = *queries_[r.query];
         const uint64_t* head = hh + k * 67;
         const int NO = (int)q.plan->out_dtypes.size();
@@ -363,6 +383,7 @@ void Server::finish_wave(Wave& w) {
             reserved_ -= q.reserve;  // kept outputs stay reserved until release
         }
         r.done = true;
+        active_.erase(std::find(active_.begin(), active_.end(), r.id));
         stats_.completed++;
     }
     w.reqs.clear();
@@ -378,6 +399,7 @@ void Server::finish_wave(Wave& w) {
 void Server::loop() {
     cudaSetDevice(device_);
     std::unique_lock<std::mutex> lk(mu_);
+    double last_busy = now();
     while (true) {
         for (auto& w : waves_) {
             if (!w.busy) continue;
@@ -396,43 +418,77 @@ void Server::loop() {
                 done_cv_.notify_all();
             }
         }
-        if (stop_ && pending_.empty() && inflight_ == 0) break;
-        if (!pending_.empty() && !fatal_) {
-            Wave* free_w = nullptr;
-            for (auto& w : waves_)
-                if (!w.busy) { free_w = &w; break; }
-            const bool need_link = linked_queries_ < (int)queries_.size();
-            if (free_w && (!need_link || inflight_ == 0)) {
-                int rc = need_link ? ensure_linked() : 0;
-                std::vector<int64_t> batch;
-                const size_t cap = budget_ - tables_bytes_;
-                while (!rc && !pending_.empty() && (int)batch.size() < max_wave_requests_) {
-                    ServerRequest& r = *requests_[pending_.front()];
-                    const size_t need = queries_[r.query]->reserve;
-                    if (reserved_ + need > cap) break;  // admission: wait for memory to free up
-                    reserved_ += need;
-                    batch.push_back(pending_.front());
-                    pending_.pop_front();
+        if (stop_ && pending_.empty() && active_.empty() && inflight_ == 0) break;
+        Wave* free_w = nullptr;
+        for (auto& w : waves_)
+            if (!w.busy) { free_w = &w; break; }
+        const bool need_link = linked_queries_ < (int)queries_.size();
+        if (free_w && !fatal_ && (!pending_.empty() || !active_.empty()) && (!need_link || inflight_ == 0)) {
+            int rc = need_link ? ensure_linked() : 0;
+            // admission (FIFO): while the working set stays under the budget
+            const size_t cap = budget_ - tables_bytes_;
+            while (!rc && !pending_.empty()) {
+                ServerRequest& r = *requests_[pending_.front()];
+                const size_t need = queries_[r.query]->reserve;
+                if (reserved_ + need > cap) break;  // wait for memory to free up
+                reserved_ += need;
+                active_.push_back(r.id);
+                pending_.pop_front();
+            }
+            stats_.peak_reserved = std::max(stats_.peak_reserved, reserved_);
+            // the wave: requests not in flight share wave_rows_ rows equally (a request that needs
+            // less than its share finishes in this wave), oldest first; rows left over go to the
+            // oldest requests.  Small requests finish within a wave of arriving and large ones
+            // advance every wave instead of waiting for the queue ahead of them to drain.
+            std::vector<int64_t> reqs, take;
+            std::vector<int64_t> cand;
+            for (int64_t id : active_)
+                if (!requests_[id]->in_wave && (int)cand.size() < max_wave_requests_) cand.push_back(id);
+            if (!cand.empty()) {
+                const int64_t share = std::max<int64_t>(1, wave_rows_ / (int64_t)cand.size());
+                int64_t rows = 0;
+                for (int64_t id : cand) {
+                    const ServerRequest& r = *requests_[id];
+                    const ServerQuery& q = *queries_[r.query];
+                    const int64_t rpc = filter_tile_rows(q.item.shape);
+                    const int64_t left = q.chunks - r.next_chunk;
+                    const int64_t n = std::max<int64_t>(1, std::min<int64_t>(left, (share + rpc - 1) / rpc));
+                    reqs.push_back(id);
+                    take.push_back(n);
+                    rows += n * rpc;
                 }
-                stats_.peak_reserved = std::max(stats_.peak_reserved, reserved_);
-                if (!rc && !batch.empty()) rc = launch_wave(*free_w, batch);
-                if (rc) {
-                    fatal_ = rc;
-                    fatal_msg_ = last_error();
-                    for (int64_t id : batch) {
-                        requests_[id]->status = rc;
-                        requests_[id]->done = true;
+                for (size_t k = 0; k < reqs.size() && rows < wave_rows_; k++) {
+                    const ServerRequest& r = *requests_[reqs[k]];
+                    const ServerQuery& q = *queries_[r.query];
+                    const int64_t rpc = filter_tile_rows(q.item.shape);
+                    const int64_t more = std::min<int64_t>(q.chunks - r.next_chunk - take[k], (wave_rows_ - rows) / rpc);
+                    if (more > 0) {
+                        take[k] += more;
+                        rows += more * rpc;
                     }
-                    done_cv_.notify_all();
                 }
             }
+            if (!rc && !reqs.empty()) rc = launch_wave(*free_w, reqs, take);
+            if (rc) {
+                fatal_ = rc;
+                fatal_msg_ = last_error();
+                for (int64_t id : reqs) {
+                    requests_[id]->status = rc;
+                    requests_[id]->done = true;
+                }
+                done_cv_.notify_all();
+            }
         }
-        if (inflight_ > 0) {
+        if (inflight_ > 0 || now() - last_busy < 0.005) {
+            // waves in flight, or idle for less than 5 ms: poll (a yield, not a sleep, so that
+            // completions and new requests are noticed within microseconds)
+            if (inflight_ > 0 || !pending_.empty()) last_busy = now();
             lk.unlock();
-            std::this_thread::sleep_for(std::chrono::microseconds(20));
+            std::this_thread::yield();
             lk.lock();
         } else {
             cv_.wait_for(lk, std::chrono::milliseconds(2));
+            last_busy = now();
         }
     }
 }

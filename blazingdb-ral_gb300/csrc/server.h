@@ -3,11 +3,14 @@
 // Clients register tables (columns stay where the caller put them, in device memory) and
 // filter + project queries over them, then submit requests (one run of one query).  A
 // scheduler thread admits requests while the working set (resident tables plus the outputs
-// and scratch of admitted requests) stays under a byte budget, and launches every admitted
-// request that is waiting as one wave: one launch of the persistent dispatcher whose warps pull
-// (request, chunk) work items.  Up to max_waves waves are in flight on their own streams, so
-// requests that arrive while a wave runs are admitted and launched as soon as memory and a
-// wave slot free up, and their work overlaps the running wave's tail on the device.
+// and scratch of admitted requests) stays under a byte budget, and runs admitted requests in
+// waves: one launch of the persistent dispatcher whose warps pull (request, chunk) work items.
+// A wave carries about wave_rows rows, shared equally by the admitted requests not already in
+// flight; a large request is sliced over several waves (its look-back status words stay in its
+// scratch between them), so requests that arrive while a large one runs finish within a wave
+// or two instead of waiting for it, and large requests keep advancing.  Up to max_waves waves are in flight on their own
+// streams; a request is in at most one in-flight wave at a time, so no launch ever waits on
+// another.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -55,6 +58,8 @@ struct ServerRequest {
     std::vector<int64_t> null_counts;
     void* scratch = nullptr;
     bool done = false;
+    int64_t next_chunk = 0;    // chunks launched so far
+    bool in_wave = false;      // part of an in-flight wave
 };
 
 struct ServerStats {
@@ -65,7 +70,8 @@ struct ServerStats {
 
 class Server {
 public:
-    Server(size_t budget_bytes, int max_waves, int max_wave_requests);
+    // wave_rows: row budget of one wave (a request's slice is whole chunks; 0 = default 32M)
+    Server(size_t budget_bytes, int max_waves, int max_wave_requests, int64_t wave_rows = 0);
     ~Server();
     int add_table(gdf_column* const* cols, int ncols, int* table_id);
     int add_query(int table_id, const char* filter_q, const char* project_q, int* query_id);
@@ -99,11 +105,13 @@ private:
         void* h_head = nullptr;        // pinned: scratch headers copied back
         size_t desc_bytes = 0;
         std::vector<int64_t> reqs;
+        std::vector<int64_t> take;     // chunks of each request in this wave
+        std::vector<char> last;        // the wave runs the request's last chunk
         bool busy = false;
         double t_launch = 0;
     };
     int ensure_linked();
-    int launch_wave(Wave& w, std::vector<int64_t>& batch);
+    int launch_wave(Wave& w, const std::vector<int64_t>& reqs, const std::vector<int64_t>& take);
     void finish_wave(Wave& w);
     void loop();
 
@@ -119,7 +127,9 @@ private:
 
     mutable std::mutex mu_;
     std::condition_variable cv_, done_cv_;
-    std::deque<int64_t> pending_;
+    std::deque<int64_t> pending_;      // submitted, not admitted (FIFO)
+    std::vector<int64_t> active_;      // admitted, not finished
+    int64_t wave_rows_ = 0;
     std::unordered_map<int64_t, std::unique_ptr<ServerRequest>> requests_;
     int64_t next_id_ = 1;
     size_t reserved_ = 0;

@@ -59,7 +59,7 @@ _SIGS = {
     "ral_batch_debug_source": (C.c_int, [P, C.c_int32, C.c_char_p, C.c_int64, C.c_char_p, C.c_int64]),
     "ral_batch_destroy": (C.c_int, [P]),
     "ral_batch_kernel_info": (C.c_int, [P, I32P, I32P, I32P]),
-    "ral_server_create": (C.c_int, [C.c_int64, C.c_int32, C.c_int32, C.POINTER(C.c_void_p)]),
+    "ral_server_create": (C.c_int, [C.c_int64, C.c_int32, C.c_int32, C.c_int64, C.POINTER(C.c_void_p)]),
     "ral_server_add_table": (C.c_int, [P, COLPP, C.c_int32, I32P]),
     "ral_server_add_query": (C.c_int, [P, C.c_int32, C.c_char_p, C.c_char_p, I32P]),
     "ral_server_query_outputs": (C.c_int, [P, C.c_int32, I32P, I32P, C.c_int32, I32P]),
@@ -507,9 +507,10 @@ class Server:
     """Served execution: resident tables, prepared filter + project queries, requests run with
     continuous batching by a scheduler thread in the library (include/ral/ral_c.h)."""
 
-    def __init__(self, budget_bytes: int = 120 << 30, max_waves: int = 2, max_wave_requests: int = 1024):
+    def __init__(self, budget_bytes: int = 120 << 30, max_waves: int = 2, max_wave_requests: int = 1024,
+                 wave_rows: int = 0):
         h = C.c_void_p()
-        _check(lib().ral_server_create(int(budget_bytes), max_waves, max_wave_requests, C.byref(h)))
+        _check(lib().ral_server_create(int(budget_bytes), max_waves, max_wave_requests, int(wave_rows), C.byref(h)))
         self._h = h
         self._tables = []
 

@@ -280,11 +280,14 @@ int ral_jit_stats(int64_t *compiles, int64_t *disk_hits, int64_t *memory_hits, d
  * server keeps registered tables resident (the caller's device columns, not copied), plans
  * filter + project queries over them, and runs submitted requests with continuous batching:
  * a scheduler thread admits requests while resident tables plus the outputs of admitted
- * requests stay under budget_bytes, and launches every admitted request as one wave of the
- * persistent dispatcher; up to max_waves waves are in flight at once.
+ * requests stay under budget_bytes, and runs them in waves of the persistent dispatcher (up to
+ * wave_rows rows each, fewest rows left first, large requests sliced over several waves); up to
+ * max_waves waves are in flight at once.
  */
 typedef struct ral_server_s ral_server;
-int ral_server_create(int64_t budget_bytes, int32_t max_waves, int32_t max_wave_requests, ral_server **server);
+/* wave_rows: rows one wave may carry (a large request is sliced over several waves); 0 = 32M. */
+int ral_server_create(int64_t budget_bytes, int32_t max_waves, int32_t max_wave_requests, int64_t wave_rows,
+                      ral_server **server);
 int ral_server_add_table(ral_server *server, gdf_column *const *columns, int32_t num_columns, int32_t *table_id);
 /* filter_query_part: "LogicalFilter(condition=[...])"; project_query_part: "LogicalProject(...)". */
 int ral_server_add_query(ral_server *server, int32_t table_id, const char *filter_query_part,

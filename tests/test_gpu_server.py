@@ -121,3 +121,41 @@ def test_trace_reports_latency_and_rows(served):
     assert np.all(lat > 0) and makespan > 0
     assert [int(r) for r in rows] == [alone_rows[i] for i in qi]
     srv.close()
+
+
+def test_many_large_requests_in_one_wave():
+    """Requests of thousands of chunks each, all admitted into the same waves: every chunk's
+    look-back finds its predecessor running (no timeouts) and each count equals the alone run."""
+    tabs = W.served_tables(2, seed=77, min_rows=3_000_000, max_rows=5_000_000)
+    qs = W.served_queries(tabs, 6, seed=77)
+    dev = [H.to_device(W.served_table_host(t)) for t in tabs]
+    srv, qids = _server(tabs, qs, dev, budget=40 << 30)
+    alone = [srv.wait(srv.submit(q))[0] for q in qids]
+    rids = [(srv.submit(qids[i % len(qids)]), i % len(qids)) for i in range(96)]
+    for rid, i in rids:
+        rows, _ = srv.wait(rid, timeout_s=300.0)
+        assert rows == alone[i]
+        srv.release(rid)
+    st = srv.stats()
+    assert st["max_wave_requests"] > 8
+    srv.close()
+
+
+def test_requests_sliced_over_many_waves_give_the_same_bits(served):
+    """A wave budget far below one table: every request runs as many slices, each chunk's
+    look-back continuing from the status words a previous wave left."""
+    tabs, qs, host, dev = served
+    srv0, qids0 = _server(tabs, qs, dev)
+    alone = {i: _alone(srv0, qids0[i]) for i in range(len(qs))}
+    srv0.close()
+    srv = R.Server(budget_bytes=8 << 30, max_waves=3, max_wave_requests=64, wave_rows=5000)
+    tids = [srv.add_table(d) for d in dev]
+    qids = [srv.add_query(tids[q.table], q.filter, q.project) for q in qs]
+    srv.start()
+    rids = [(srv.submit(qids[i], keep=True), i) for i in range(len(qs))]
+    for rid, i in rids:
+        got = srv.result(rid, qids[i])
+        for j, (g, a) in enumerate(zip(got, alone[i])):
+            _same_bits(g, a, f"query {i} output {j} sliced")
+    assert srv.stats()["waves"] > 3 * len(qs)
+    srv.close()
