@@ -20,9 +20,9 @@ LIB = os.path.join(OUT, "libralgpu.so")
 CUDA = os.environ.get("CUDA_HOME", "/usr/local/cuda")
 NVCC = os.path.join(CUDA, "bin", "nvcc")
 
-CPP = ["program.cpp", "frontend.cpp", "codegen.cpp", "jit.cpp", "engine.cpp", "filter.cpp", "batch.cpp", "server.cpp", "capi.cpp"]
+CPP = ["program.cpp", "frontend.cpp", "codegen.cpp", "jit.cpp", "engine.cpp", "filter.cpp", "batch.cpp", "server.cpp", "selftest.cpp", "capi.cpp"]
 CU = ["kernels.cu", "noalloc.cu"]
-HEADERS = ["program.h", "frontend.h", "codegen.h", "jit.h", "engine.h", "filter.h", "batch.h", "server.h", "kernels.h", "device_rt.cuh"]
+HEADERS = ["program.h", "frontend.h", "codegen.h", "jit.h", "engine.h", "filter.h", "batch.h", "server.h", "kernels.h", "device_rt.cuh", "softfp.cuh"]
 INCLUDES = [f"-I{os.path.join(ROOT, 'include')}", f"-I{CSRC}", f"-I{os.path.join(CUDA, 'include')}"]
 GENCODE = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
@@ -38,9 +38,10 @@ def _deps_mtime() -> float:
 
 
 def _embed_prelude() -> str:
-    src = open(os.path.join(CSRC, "device_rt.cuh")).read()
+    # softfp.cuh first: device_rt.cuh then skips its #include of it (NVRTC has no include path)
+    src = open(os.path.join(CSRC, "softfp.cuh")).read() + "\n" + open(os.path.join(CSRC, "device_rt.cuh")).read()
     out = os.path.join(OUT, "prelude_embed.cpp")
-    text = ('// generated from csrc/device_rt.cuh by build.py\n'
+    text = ('// generated from csrc/softfp.cuh and csrc/device_rt.cuh by build.py\n'
             'extern "C" const char* const ral_prelude_source;\n'
             'extern "C" const char* const ral_prelude_source = R"RALPRELUDE(' + src + ')RALPRELUDE";\n')
     if not os.path.exists(out) or open(out).read() != text:

@@ -17,6 +17,10 @@
 
 using namespace ral;
 
+namespace ral {
+int softfp_selftest(long long n, unsigned long long seed, long long* counts, unsigned long long* first_operands);
+}
+
 namespace {
 
 template <typename F>
@@ -740,6 +744,18 @@ int ral_server_stats(ral_server* server, int64_t* stats6) {
 int ral_server_destroy(ral_server* server) {
     delete server;
     return kSuccess;
+}
+
+int ral_softfp_selftest(int64_t n, uint64_t seed, int64_t* mismatches, uint64_t* first_operands) {
+    return guarded([&] {
+        if (!mismatches || !first_operands || n < 0) return set_error(kInvalidArgument, "bad argument");
+        std::vector<long long> c(16);
+        std::vector<unsigned long long> f(32);
+        int rc = softfp_selftest((long long)n, (unsigned long long)seed, c.data(), f.data());
+        for (int i = 0; i < 16; i++) mismatches[i] = c[i];
+        for (int i = 0; i < 32; i++) first_operands[i] = f[i];
+        return rc;
+    });
 }
 
 }  // extern "C"

@@ -51,7 +51,7 @@ std::string conv(const std::string& x, Kind from, Kind to) {
 std::string to_d(const std::string& x, Kind k) { return conv(x, k, Kind::F64); }
 std::string to_i(const std::string& x, Kind k) { return conv(x, k, Kind::I64); }
 std::string conv_bool(const std::string& b, Kind to) {
-    return to == Kind::F64 ? "((double)(" + b + "))" : "((ral_i64)(" + b + "))";
+    return to == Kind::F64 ? "((" + b + ") ? 1.0 : 0.0)" : "((ral_i64)(" + b + "))";
 }
 
 // Data-path op emission shared by every kernel kind.
@@ -109,15 +109,17 @@ struct OpEmitter {
                     if (f) return conv(std::string(dop) + "(" + to_d(l, lk) + ", " + to_d(r, rk) + ")", Kind::F64, ok);
                     return conv(std::string(iop) + "(" + l + ", " + r + ")", Kind::I64, ok);
                 };
-                auto cmp = [&](const char* c) {
-                    if (f) return conv_bool(to_d(l, lk) + " " + c + " " + to_d(r, rk), ok);
+                // double comparisons go through the prelude's ral_d* functions (integer-pipe
+                // versions unless RAL_SOFT_FP is 0)
+                auto cmp = [&](const char* c, const char* dfn) {
+                    if (f) return conv_bool(std::string(dfn) + "(" + to_d(l, lk) + ", " + to_d(r, rk) + ")", ok);
                     return conv_bool(l + " " + c + " " + r, ok);
                 };
                 switch (op.bop) {
                 case GDF_ADD: e = arith("__dadd_rn", "ral_addi"); break;
                 case GDF_SUB: e = arith("__dsub_rn", "ral_subi"); break;
                 case GDF_MUL: e = arith("__dmul_rn", "ral_muli"); break;
-                case GDF_DIV: case GDF_FLOOR_DIV: e = arith("__ddiv_rn", "ral_divi"); break;
+                case GDF_DIV: case GDF_FLOOR_DIV: e = arith("ral_ddiv", "ral_divi"); break;
                 case GDF_MOD: e = conv("ral_modi(" + to_i(l, lk) + ", " + to_i(r, rk) + ")", Kind::I64, ok); break;
                 case GDF_POW:
                     if (dtype_is_float(op.ltype) || dtype_is_float(op.rtype))
@@ -125,12 +127,12 @@ struct OpEmitter {
                     else
                         e = conv("ral_powi(" + l + ", " + r + ")", Kind::I64, ok);
                     break;
-                case GDF_EQUAL: e = cmp("=="); break;
-                case GDF_NOT_EQUAL: e = cmp("!="); break;
-                case GDF_LESS: e = cmp("<"); break;
-                case GDF_GREATER: e = cmp(">"); break;
-                case GDF_LESS_EQUAL: e = cmp("<="); break;
-                case GDF_GREATER_EQUAL: e = cmp(">="); break;
+                case GDF_EQUAL: e = cmp("==", "ral_deq"); break;
+                case GDF_NOT_EQUAL: e = cmp("!=", "ral_dne"); break;
+                case GDF_LESS: e = cmp("<", "ral_dlt"); break;
+                case GDF_GREATER: e = cmp(">", "ral_dgt"); break;
+                case GDF_LESS_EQUAL: e = cmp("<=", "ral_dle"); break;
+                case GDF_GREATER_EQUAL: e = cmp(">=", "ral_dge"); break;
                 case GDF_COALESCE:
                     e = "(rb" + std::to_string(op.left) + " ? " + conv(l, lk, ok) + " : " + conv(r, rk, ok) + ")";
                     break;
@@ -141,19 +143,19 @@ struct OpEmitter {
                 const bool d32 = op.ltype == GDF_DATE32;
                 auto math = [&](const std::string& fn) { return conv(fn + "(" + d + ")", Kind::F64, ok); };
                 switch (op.uop) {
-                case BLZ_FLOOR: e = math("floor"); break;
-                case BLZ_CEIL: e = math("ceil"); break;
+                case BLZ_FLOOR: e = math("ral_dfloor"); break;
+                case BLZ_CEIL: e = math("ral_dceil"); break;
                 case BLZ_SIN: e = math("sin"); break;
                 case BLZ_COS: e = math("cos"); break;
                 case BLZ_ASIN: e = math("asin"); break;
                 case BLZ_ACOS: e = math("acos"); break;
                 case BLZ_TAN: e = math("tan"); break;
-                case BLZ_COTAN: e = conv("__ddiv_rn(cos(" + d + "), sin(" + d + "))", Kind::F64, ok); break;
+                case BLZ_COTAN: e = conv("ral_ddiv(cos(" + d + "), sin(" + d + "))", Kind::F64, ok); break;
                 case BLZ_ATAN: e = math("atan"); break;
-                case BLZ_ABS: e = math("fabs"); break;
+                case BLZ_ABS: e = math("ral_dfabs"); break;
                 case BLZ_LN: e = math("log"); break;
                 case BLZ_LOG: e = math("log10"); break;
-                case BLZ_NOT: e = conv_bool(lk == Kind::F64 ? "(" + l + " == 0.0)" : "(" + l + " == 0)", ok); break;
+                case BLZ_NOT: e = conv_bool(lk == Kind::F64 ? "ral_dzero(" + l + ")" : "(" + l + " == 0)", ok); break;
                 case BLZ_YEAR: e = conv(std::string(d32 ? "ral_year32(" : "ral_year64(") + to_i(l, lk) + ")", Kind::I64, ok); break;
                 case BLZ_MONTH: e = conv(std::string(d32 ? "ral_month32(" : "ral_month64(") + to_i(l, lk) + ")", Kind::I64, ok); break;
                 case BLZ_DAY: e = conv(std::string(d32 ? "ral_day32(" : "ral_day64(") + to_i(l, lk) + ")", Kind::I64, ok); break;
@@ -216,6 +218,7 @@ struct ValidEmitter {
 };
 
 std::string widen(const std::string& x, gdf_dtype t) {
+    if (t == GDF_FLOAT32) return "ral_f2d(" + x + ")";
     return dtype_is_float(t) ? "((double)(" + x + "))" : "((ral_i64)(" + x + "))";
 }
 
@@ -225,7 +228,7 @@ std::string narrow(const std::string& v, Kind k, gdf_dtype t) {
     const std::string et = element_ctype(t);
     if (dtype_is_float(t)) {
         std::string d = k == Kind::F64 ? v : "ral_bits_d(" + v + ")";
-        if (t == GDF_FLOAT32) return "__double2float_rn(" + d + ")";
+        if (t == GDF_FLOAT32) return "ral_d2f(" + d + ")";
         return d;
     }
     std::string bits = k == Kind::I64 ? v : "ral_d_bits(" + v + ")";

@@ -1,9 +1,9 @@
 // device_rt.cuh — device-side building blocks of the generated expression kernels.
 //
 // This file is compiled twice: by NVRTC as the prelude of every generated
-// kernel (embedded into the library as a string at build time), and by nvcc
-// as part of the ahead-of-time kernels.  It includes no headers so that NVRTC
-// needs no include path.
+// kernel (embedded into the library as a string at build time, after
+// softfp.cuh), and by nvcc as part of the ahead-of-time kernels.  Under NVRTC
+// it includes nothing, so that NVRTC needs no include path.
 //
 // Arithmetic follows the reference interpreter's C++ semantics on {int64,
 // double} registers (src/Interpreter/interpreter_ops.cuh:574-838): explicit
@@ -19,9 +19,47 @@ typedef unsigned int ral_u32;
 
 #define RAL_FI __device__ __forceinline__
 
-// ---- conversions ---------------------------------------------------------------------------
+// ---- double operations that have integer-pipe versions -----------------------------------
+// RAL_SOFT_FP 1 (the default): division, floor / ceil / fabs, comparisons and the conversions
+// run as the exact integer-arithmetic versions of softfp.cuh, which leave the FP64 pipe to add,
+// subtract and multiply; 0: the hardware instructions.  Both give the same bits.
+#ifndef RAL_SOFT_FP
+#define RAL_SOFT_FP 1
+#endif
+#ifndef RAL_SOFTFP_CUH_
+#include "softfp.cuh"
+#endif
+#if RAL_SOFT_FP
+RAL_FI ral_i64 ral_d2i(double d) { return ral_sf_d2i(d); }
+RAL_FI double ral_i2d(ral_i64 x) { return ral_sf_i2d(x); }
+RAL_FI double ral_ddiv(double a, double b) { return ral_sf_div(a, b); }
+RAL_FI double ral_dfloor(double x) { return ral_sf_floor(x); }
+RAL_FI double ral_dceil(double x) { return ral_sf_ceil(x); }
+RAL_FI bool ral_dlt(double a, double b) { return ral_sf_lt(a, b); }
+RAL_FI bool ral_dle(double a, double b) { return ral_sf_le(a, b); }
+RAL_FI bool ral_dgt(double a, double b) { return ral_sf_gt(a, b); }
+RAL_FI bool ral_dge(double a, double b) { return ral_sf_ge(a, b); }
+RAL_FI bool ral_deq(double a, double b) { return ral_sf_eq(a, b); }
+RAL_FI bool ral_dne(double a, double b) { return ral_sf_ne(a, b); }
+RAL_FI double ral_f2d(float f) { return ral_sf_f2d(f); }
+RAL_FI float ral_d2f(double d) { return ral_sf_d2f(d); }
+#else
 RAL_FI ral_i64 ral_d2i(double d) { return __double2ll_rz(d); }
 RAL_FI double ral_i2d(ral_i64 x) { return __ll2double_rn(x); }
+RAL_FI double ral_ddiv(double a, double b) { return __ddiv_rn(a, b); }
+RAL_FI double ral_dfloor(double x) { return floor(x); }
+RAL_FI double ral_dceil(double x) { return ceil(x); }
+RAL_FI bool ral_dlt(double a, double b) { return a < b; }
+RAL_FI bool ral_dle(double a, double b) { return a <= b; }
+RAL_FI bool ral_dgt(double a, double b) { return a > b; }
+RAL_FI bool ral_dge(double a, double b) { return a >= b; }
+RAL_FI bool ral_deq(double a, double b) { return a == b; }
+RAL_FI bool ral_dne(double a, double b) { return a != b; }
+RAL_FI double ral_f2d(float f) { return (double)f; }
+RAL_FI float ral_d2f(double d) { return __double2float_rn(d); }
+#endif
+RAL_FI double ral_dfabs(double x) { return ral_sf_fabs(x); }
+RAL_FI bool ral_dzero(double x) { return ral_sf_is_zero(x); }
 RAL_FI double ral_bits_d(ral_i64 b) { return __longlong_as_double(b); }
 RAL_FI ral_i64 ral_d_bits(double d) { return __double_as_longlong(d); }
 

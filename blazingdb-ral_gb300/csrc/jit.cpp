@@ -39,8 +39,18 @@ uint64_t fnv1a(const std::string& s, uint64_t h = 1469598103934665603ull) {
     return h;
 }
 
+// RAL_SOFT_FP=0 selects the hardware FP64 instructions for the operations that otherwise run
+// on the integer pipes (same results; for comparison and diagnosis)
+const std::string& soft_fp_define() {
+    static const std::string d = [] {
+        const char* e = std::getenv("RAL_SOFT_FP");
+        return std::string("#define RAL_SOFT_FP ") + ((e && std::string(e) == "0") ? "0" : "1") + "\n";
+    }();
+    return d;
+}
+
 std::string full_source(const GeneratedKernel& gk) {
-    return std::string(ral_prelude_source) + "\n" + gk.source;
+    return soft_fp_define() + std::string(ral_prelude_source) + "\n" + gk.source;
 }
 
 std::string cache_dir() {

@@ -1,0 +1,328 @@
+// softfp.cuh — exactly rounded IEEE-754 binary64 operations on the integer pipes.
+//
+// GB300 issues about two FP64 instructions per clock per SM against 64+ integer instructions,
+// and an IEEE double division alone is a sequence of about nine FP64-pipe instructions.  The
+// expression kernels are FP64-bound long before they are HBM-bound, so the operations below
+// compute the same bits as the hardware instructions (division, floor / ceil, comparisons and
+// the int64 / float32 <-> double conversions) with integer arithmetic instead, leaving the FP64
+// pipe to add, subtract and multiply.
+//
+// Every function returns exactly what the IEEE operation (round to nearest even) returns for
+// every input, including -0, infinities and NaN (NaN results are the default quiet NaN or the
+// input NaN, as the hardware produces them; callers compare NaNs as NaN).  Inputs outside a
+// function's fast path (zero, subnormal, infinite or NaN operands, subnormal or overflowing
+// quotients) fall back to the hardware instruction.
+//
+// Methods: division by a Newton-Raphson reciprocal in 64-bit fixed point seeded from a
+// single-precision reciprocal estimate, then an exact remainder correction of the quotient and
+// round-to-nearest-even from the remainder (the schoolbook method of e.g. Muller et al.,
+// "Handbook of Floating-Point Arithmetic", ch. 9); comparisons on the sign-magnitude keys of the
+// bit patterns; conversions by normalising shifts with explicit round-to-nearest-even.
+//
+// The file compiles as CUDA device code (NVRTC prelude, nvcc) and as plain C++ on the host,
+// where the tests check it bit for bit against the host's own IEEE operations.
+#ifndef RAL_SOFTFP_CUH_
+#define RAL_SOFTFP_CUH_
+
+#if defined(__CUDACC__)
+#define RAL_SF __host__ __device__ __forceinline__
+#else
+#define RAL_SF static inline
+#endif
+
+#define RAL_SF_SIGN 0x8000000000000000ull
+#define RAL_SF_EXP 0x7ff0000000000000ull
+#define RAL_SF_FRAC 0x000fffffffffffffull
+#define RAL_SF_IMPL 0x0010000000000000ull
+
+RAL_SF unsigned long long ral_sf_bits(double d) {
+#if defined(__CUDA_ARCH__)
+    return (unsigned long long)__double_as_longlong(d);
+#else
+    unsigned long long b;
+    __builtin_memcpy(&b, &d, 8);
+    return b;
+#endif
+}
+
+RAL_SF double ral_sf_double(unsigned long long b) {
+#if defined(__CUDA_ARCH__)
+    return __longlong_as_double((long long)b);
+#else
+    double d;
+    __builtin_memcpy(&d, &b, 8);
+    return d;
+#endif
+}
+
+RAL_SF unsigned int ral_sf_fbits(float f) {
+#if defined(__CUDA_ARCH__)
+    return (unsigned int)__float_as_uint(f);
+#else
+    unsigned int b;
+    __builtin_memcpy(&b, &f, 4);
+    return b;
+#endif
+}
+
+RAL_SF float ral_sf_float(unsigned int b) {
+#if defined(__CUDA_ARCH__)
+    return __uint_as_float(b);
+#else
+    float f;
+    __builtin_memcpy(&f, &b, 4);
+    return f;
+#endif
+}
+
+RAL_SF unsigned long long ral_sf_umulh(unsigned long long a, unsigned long long b) {
+#if defined(__CUDA_ARCH__)
+    return __umul64hi(a, b);
+#else
+    return (unsigned long long)(((unsigned __int128)a * b) >> 64);
+#endif
+}
+
+RAL_SF int ral_sf_clz64(unsigned long long x) {  // x != 0
+#if defined(__CUDA_ARCH__)
+    return __clzll((long long)x);
+#else
+    return __builtin_clzll(x);
+#endif
+}
+
+// 1/x to about 22 bits for x in [2^23, 2^24) (an exact float of the divisor's top bits)
+RAL_SF float ral_sf_rcp_estimate(float x) {
+#if defined(__CUDA_ARCH__)
+    float r;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+#else
+    return 1.0f / x;
+#endif
+}
+
+// ---- hardware fallbacks for the inputs outside the fast paths -----------------------------
+
+RAL_SF double ral_sf_hw_div(double a, double b) {
+#if defined(__CUDA_ARCH__)
+    return __ddiv_rn(a, b);
+#else
+    return a / b;
+#endif
+}
+
+// ---- division --------------------------------------------------------------------------------
+
+// a / b rounded to nearest even.
+RAL_SF double ral_sf_div(double a, double b) {
+    const unsigned long long A = ral_sf_bits(a), B = ral_sf_bits(b);
+    const unsigned ea = (unsigned)(A >> 52) & 0x7ffu, eb = (unsigned)(B >> 52) & 0x7ffu;
+    // fast path: both operands normal and finite
+    if (ea - 1u >= 2046u || eb - 1u >= 2046u) return ral_sf_hw_div(a, b);
+    unsigned long long ma = (A & RAL_SF_FRAC) | RAL_SF_IMPL;
+    const unsigned long long mb = (B & RAL_SF_FRAC) | RAL_SF_IMPL;
+    int e = (int)ea - (int)eb + 1023;
+    if (ma < mb) {  // quotient of the significands in [1, 2)
+        ma <<= 1;
+        e -= 1;
+    }
+    // reciprocal y ~ 2^116 / mb in (2^63, 2^64]: float seed, then two Newton steps
+    const float seed = ral_sf_rcp_estimate((float)(unsigned)(mb >> 29));  // ~ 2^29 / mb
+    const float ys = seed * 0x1p87f;
+    unsigned long long y = ys >= 0x1p64f ? 0xffffffffffffffffull : (unsigned long long)ys;
+#pragma unroll
+    for (int it = 0; it < 2; ++it) {
+        // err = 2^116 - mb * y, as a signed value scaled by 2^-52
+        const unsigned long long plo = mb * y, phi = ral_sf_umulh(mb, y);
+        // (2^116 - P) >> 52 = (2^64 - (P >> 52)) using the 128-bit P = phi:plo
+        const unsigned long long p52 = (phi << 12) | (plo >> 52);  // P >> 52 (P < 2^117: fits)
+        const long long err = (long long)(0ull - p52);               // 2^64 - p52 mod 2^64, small
+        // y += y * err / 2^64
+        const unsigned long long mag = err < 0 ? (0ull - (unsigned long long)err) : (unsigned long long)err;
+        const unsigned long long corr = ral_sf_umulh(y, mag);
+        y = err < 0 ? y - corr : y + corr;
+    }
+    // Q ~ ma * 2^53 / mb = (ma * y) >> 63, then exact correction from the remainder
+    const unsigned long long qlo = ma * y, qhi = ral_sf_umulh(ma, y);
+    unsigned long long q = (qhi << 1) | (qlo >> 63);
+    // R = ma * 2^53 - q * mb (small: the low 64 bits of both products suffice)
+    long long r = (long long)((ma << 53) - q * mb);
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        if (r < 0) {
+            q -= 1;
+            r += (long long)mb;
+        }
+    }
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        if (r >= (long long)mb) {
+            q += 1;
+            r -= (long long)mb;
+        }
+    }
+    // q in [2^53, 2^54): 53 significand bits, one rounding bit, sticky = r != 0
+    unsigned long long m = q >> 1;
+    const unsigned rb = (unsigned)(q & 1u);
+    if (rb && (r != 0 || (m & 1u))) m += 1;
+    if (m == (1ull << 53)) {
+        m >>= 1;
+        e += 1;
+    }
+    if (e <= 0 || e >= 2047) return ral_sf_hw_div(a, b);  // subnormal or overflowing quotient
+    return ral_sf_double(((A ^ B) & RAL_SF_SIGN) | ((unsigned long long)e << 52) | (m & RAL_SF_FRAC));
+}
+
+// ---- rounding to an integer ------------------------------------------------------------------
+
+RAL_SF double ral_sf_floor(double x) {
+    unsigned long long A = ral_sf_bits(x);
+    const int e = (int)((A >> 52) & 0x7ff);
+    if (e >= 1075) return x;  // integral, infinite or NaN
+    if (e < 1023) {           // |x| < 1
+        if ((A << 1) == 0) return x;                                    // +-0
+        return (A >> 63) ? ral_sf_double(0xbff0000000000000ull) : 0.0;  // -1 or +0
+    }
+    const unsigned long long mask = RAL_SF_FRAC >> (e - 1023);
+    if ((A & mask) == 0) return x;
+    A = (A >> 63) ? (A | mask) + 1 : (A & ~mask);  // negative: away from zero (carries into the exponent)
+    return ral_sf_double(A);
+}
+
+RAL_SF double ral_sf_ceil(double x) {
+    unsigned long long A = ral_sf_bits(x);
+    const int e = (int)((A >> 52) & 0x7ff);
+    if (e >= 1075) return x;
+    if (e < 1023) {
+        if ((A << 1) == 0) return x;
+        return (A >> 63) ? ral_sf_double(RAL_SF_SIGN) : 1.0;  // -0 or 1
+    }
+    const unsigned long long mask = RAL_SF_FRAC >> (e - 1023);
+    if ((A & mask) == 0) return x;
+    A = (A >> 63) ? (A & ~mask) : (A | mask) + 1;
+    return ral_sf_double(A);
+}
+
+RAL_SF double ral_sf_fabs(double x) { return ral_sf_double(ral_sf_bits(x) & ~RAL_SF_SIGN); }
+
+// ---- comparisons -------------------------------------------------------------------------------
+
+RAL_SF bool ral_sf_isnan_bits(unsigned long long A) { return (A & ~RAL_SF_SIGN) > RAL_SF_EXP; }
+
+// Order-preserving signed key of a non-NaN double; -0 and +0 share the key 0.
+RAL_SF long long ral_sf_key(unsigned long long A) {
+    if ((A << 1) == 0) return 0;
+    return (long long)((A >> 63) ? (A ^ 0x7fffffffffffffffull) : A);
+}
+
+RAL_SF bool ral_sf_lt(double a, double b) {
+    const unsigned long long A = ral_sf_bits(a), B = ral_sf_bits(b);
+    return !ral_sf_isnan_bits(A) && !ral_sf_isnan_bits(B) && ral_sf_key(A) < ral_sf_key(B);
+}
+RAL_SF bool ral_sf_le(double a, double b) {
+    const unsigned long long A = ral_sf_bits(a), B = ral_sf_bits(b);
+    return !ral_sf_isnan_bits(A) && !ral_sf_isnan_bits(B) && ral_sf_key(A) <= ral_sf_key(B);
+}
+RAL_SF bool ral_sf_gt(double a, double b) { return ral_sf_lt(b, a); }
+RAL_SF bool ral_sf_ge(double a, double b) { return ral_sf_le(b, a); }
+RAL_SF bool ral_sf_eq(double a, double b) {
+    const unsigned long long A = ral_sf_bits(a), B = ral_sf_bits(b);
+    return !ral_sf_isnan_bits(A) && !ral_sf_isnan_bits(B) && ral_sf_key(A) == ral_sf_key(B);
+}
+RAL_SF bool ral_sf_ne(double a, double b) { return !ral_sf_eq(a, b); }
+// x == 0.0 (either zero; NaN is not zero)
+RAL_SF bool ral_sf_is_zero(double x) { return (ral_sf_bits(x) << 1) == 0; }
+
+// ---- conversions -----------------------------------------------------------------------------
+
+// int64 -> double, rounded to nearest even
+RAL_SF double ral_sf_i2d(long long x) {
+    if (x == 0) return 0.0;
+    const unsigned long long s = x < 0 ? RAL_SF_SIGN : 0ull;
+    const unsigned long long u = x < 0 ? 0ull - (unsigned long long)x : (unsigned long long)x;
+    const int lz = ral_sf_clz64(u);
+    const unsigned long long n = u << lz;  // top bit set
+    unsigned long long m = n >> 11;        // 53 bits
+    const unsigned long long rest = n & 0x7ffull;
+    int e = 1086 - lz;
+    if (rest > 0x400ull || (rest == 0x400ull && (m & 1u))) {
+        m += 1;
+        if (m == (1ull << 53)) {
+            m >>= 1;
+            e += 1;
+        }
+    }
+    return ral_sf_double(s | ((unsigned long long)e << 52) | (m & RAL_SF_FRAC));
+}
+
+// double -> int64, truncating; NaN -> 0, out of range saturates (cvt.rzi.s64.f64)
+RAL_SF long long ral_sf_d2i(double d) {
+    const unsigned long long A = ral_sf_bits(d);
+    const int e = (int)((A >> 52) & 0x7ff);
+    if (ral_sf_isnan_bits(A)) return 0;
+    if (e < 1023) return 0;
+    const bool neg = (A >> 63) != 0;
+    if (e >= 1023 + 63) return neg ? (long long)RAL_SF_SIGN : 0x7fffffffffffffffll;
+    const unsigned long long m = (A & RAL_SF_FRAC) | RAL_SF_IMPL;
+    const int sh = e - 1075;
+    const unsigned long long v = sh >= 0 ? (m << sh) : (m >> (-sh));
+    return neg ? (long long)(0ull - v) : (long long)v;
+}
+
+// float -> double (exact)
+RAL_SF double ral_sf_f2d(float f) {
+    const unsigned int F = ral_sf_fbits(f);
+    const unsigned long long s = (unsigned long long)(F >> 31) << 63;
+    const unsigned int e = (F >> 23) & 0xffu;
+    unsigned long long m = F & 0x7fffffu;
+    if (e == 0xffu) {
+        // infinity, or NaN made quiet with its payload kept in the top fraction bits
+        return ral_sf_double(s | RAL_SF_EXP | (m << 29) | (m ? (1ull << 51) : 0ull));
+    }
+    if (e == 0) {
+        if (m == 0) return ral_sf_double(s);
+        // subnormal float: m * 2^-149 with the leading one at bit p
+        const int p = 63 - ral_sf_clz64(m);
+        const unsigned long long frac = (m << (52 - p)) & RAL_SF_FRAC;
+        return ral_sf_double(s | ((unsigned long long)(p - 149 + 1023) << 52) | frac);
+    }
+    return ral_sf_double(s | ((unsigned long long)(e + 896) << 52) | (m << 29));
+}
+
+// v >> sh rounded to nearest even (sh in 1..63)
+RAL_SF unsigned long long ral_sf_shift_rne(unsigned long long v, int sh) {
+    const unsigned long long q = v >> sh;
+    const unsigned long long rest = v & ((1ull << sh) - 1);
+    const unsigned long long half = 1ull << (sh - 1);
+    return q + ((rest > half || (rest == half && (q & 1u))) ? 1u : 0u);
+}
+
+// double -> float, rounded to nearest even (overflow to infinity, subnormal results)
+RAL_SF float ral_sf_d2f(double d) {
+    const unsigned long long A = ral_sf_bits(d);
+    const unsigned int s = (unsigned int)(A >> 63) << 31;
+    const int e = (int)((A >> 52) & 0x7ff);
+    const unsigned long long frac = A & RAL_SF_FRAC;
+    if (e == 0x7ff) {
+        // infinity, or quiet NaN with the top payload bits
+        return ral_sf_float(s | 0x7f800000u | (frac ? (0x400000u | (unsigned int)(frac >> 29)) : 0u));
+    }
+    if (e == 0) return ral_sf_float(s);  // zero or a double subnormal (far below the float range)
+    const unsigned long long m = frac | RAL_SF_IMPL;  // 53 bits
+    const int ef = e - 1023 + 127;
+    if (ef >= 255) return ral_sf_float(s | 0x7f800000u);
+    if (ef >= 1) {
+        const unsigned long long r = ral_sf_shift_rne(m, 29);  // 24 bits, or 2^24 after a carry
+        // a carry out of the significand bumps the exponent through the add; 255 means infinity
+        const unsigned long long bits = ((unsigned long long)ef << 23) + (r - (1ull << 23));
+        return ral_sf_float(s | (bits >= 0x7f800000ull ? 0x7f800000u : (unsigned int)bits));
+    }
+    // subnormal float result: value = m * 2^(e - 1075), float subnormal unit 2^-149
+    const int sh = 29 + (1 - ef);
+    if (sh > 63) return ral_sf_float(s);
+    const unsigned long long r = ral_sf_shift_rne(m, sh);  // may round up to the smallest normal
+    return ral_sf_float(s | (unsigned int)r);
+}
+
+#endif  // RAL_SOFTFP_CUH_

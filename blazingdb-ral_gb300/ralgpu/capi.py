@@ -74,6 +74,7 @@ _SIGS = {
                                        C.POINTER(C.c_int64), C.POINTER(C.c_double)]),
     "ral_server_stats": (C.c_int, [P, C.POINTER(C.c_int64)]),
     "ral_server_destroy": (C.c_int, [P]),
+    "ral_softfp_selftest": (C.c_int, [C.c_int64, C.c_uint64, C.POINTER(C.c_int64), C.POINTER(C.c_uint64)]),
     "ral_batch_tune_key": (C.c_int, [COLPP, C.c_int32, COLPP, C.c_int32, I16P, I16P, I16P, C.c_int32, I16P, I32P, I32P,
                                      SCP, SCP, C.c_char_p, C.c_int64]),
     "ral_autotune_program": (C.c_int, [COLPP, C.c_int32, COLPP, C.c_int32, I16P, I16P, I16P, C.c_int32, I16P, I32P,
@@ -600,3 +601,15 @@ class Server:
             self.close()
         except Exception:
             pass
+
+
+SOFTFP_OPS = ["div", "floor", "ceil", "compare", "i2d", "d2i", "f2d", "d2f", "is_zero", "fabs"]
+
+
+def softfp_selftest(n: int = 1 << 24, seed: int = 1) -> dict:
+    """Runs the device self-test of the integer-pipe double operations; returns
+    {op: (mismatches, first operand bits)}."""
+    cnt = (C.c_int64 * 16)()
+    first = (C.c_uint64 * 32)()
+    _check(lib().ral_softfp_selftest(n, seed, cnt, first))
+    return {op: (int(cnt[i]), (int(first[2 * i]), int(first[2 * i + 1]))) for i, op in enumerate(SOFTFP_OPS)}

@@ -1,0 +1,139 @@
+// Host check of softfp.cuh: every function against the host's IEEE-754 operations, bit for bit,
+// on edge cases and random inputs.  Prints one line per function: name, cases, mismatches, and
+// the first mismatch.  Built and run by tests/test_softfp_cpu.py.
+#include <cmath>
+#include <cstdint>
+#include <cstdio>
+#include <cstring>
+#include <limits>
+#include <random>
+#include <vector>
+
+#include "softfp.cuh"
+
+static uint64_t bits(double d) { uint64_t b; std::memcpy(&b, &d, 8); return b; }
+static double dbl(uint64_t b) { double d; std::memcpy(&d, &b, 8); return d; }
+static uint32_t fbits(float f) { uint32_t b; std::memcpy(&b, &f, 4); return b; }
+static float flt(uint32_t b) { float f; std::memcpy(&f, &b, 4); return f; }
+
+// same value, or both NaN
+static bool same_d(double a, double b) { return (std::isnan(a) && std::isnan(b)) || bits(a) == bits(b); }
+static bool same_f(float a, float b) { return (std::isnan(a) && std::isnan(b)) || fbits(a) == fbits(b); }
+
+// the host's comparisons, kept out of line so that they are evaluated as written
+__attribute__((noinline)) static unsigned host_compare(double a, double b) {
+    return (unsigned)(a < b) | (unsigned)(a <= b) << 1 | (unsigned)(a > b) << 2 | (unsigned)(a >= b) << 3 |
+           (unsigned)(a == b) << 4 | (unsigned)(a != b) << 5;
+}
+
+struct Counter {
+    const char* name;
+    long long n = 0, bad = 0;
+    char first[256] = "";
+    void report() { std::printf("%s %lld %lld %s\n", name, n, bad, first); }
+};
+
+static std::vector<double> special_doubles() {
+    std::vector<double> v = {0.0, -0.0, 1.0, -1.0, 0.5, -0.5, 1.5, -1.5, 2.0, 3.0, -3.0, 0.1, -0.1, 1e308, -1e308,
+                             1e-308, -1e-308, 4.9e-324, -4.9e-324, 2.2250738585072014e-308,
+                             std::numeric_limits<double>::infinity(), -std::numeric_limits<double>::infinity(),
+                             std::numeric_limits<double>::quiet_NaN(), 9007199254740992.0, 9007199254740993.0,
+                             -9007199254740992.0, 4503599627370496.5, 4503599627370495.5, 9.2233720368547758e18,
+                             -9.2233720368547758e18, 9.2233720368547748e18, 0.49999999999999994, -0.49999999999999994,
+                             1.7976931348623157e308, 3.4028234663852886e38, 3.4028235677973366e38, 1.401298464324817e-45,
+                             7.006492321624085e-46, 7.006492321624087e-46, 1.1754943508222875e-38,
+                             1.1754942807573643e-38, 1.1754943157898259e-38};
+    return v;
+}
+
+int main(int argc, char** argv) {
+    const long long N = argc > 1 ? atoll(argv[1]) : 2000000;
+    std::mt19937_64 rng(12345);
+    auto rand_double = [&]() -> double {
+        switch (rng() % 6) {
+        case 0: return dbl(rng());                                       // any bit pattern
+        case 1: return (double)(int64_t)(rng() >> (rng() % 64));          // integers of all sizes
+        case 2: return std::ldexp((double)(rng() >> 11), (int)(rng() % 120) - 60);  // moderate range
+        case 3: return (double)(int32_t)rng() / (double)(1 + (rng() % 1000));
+        case 4: return std::ldexp(1.0, (int)(rng() % 2100) - 1075) * (rng() & 1 ? -1 : 1);
+        default: return (double)(float)dbl(rng());
+        }
+    };
+    std::vector<double> sp = special_doubles();
+
+    Counter cdiv{"div"}, cfloor{"floor"}, cceil{"ceil"}, cabs{"fabs"}, ccmp{"compare"}, ci2d{"i2d"}, cd2i{"d2i"},
+        cf2d{"f2d"}, cd2f{"d2f"}, czero{"is_zero"};
+    auto check_div = [&](double a, double b) {
+        cdiv.n++;
+        const double w = a / b, g = ral_sf_div(a, b);
+        if (!same_d(w, g) && cdiv.bad++ == 0)
+            std::snprintf(cdiv.first, sizeof cdiv.first, "%a/%a want %a got %a", a, b, w, g);
+    };
+    auto check_unary = [&](double x) {
+        cfloor.n++; cceil.n++; cabs.n++; czero.n++; cd2f.n++;
+        if (!same_d(std::floor(x), ral_sf_floor(x)) && cfloor.bad++ == 0)
+            std::snprintf(cfloor.first, sizeof cfloor.first, "%a want %a got %a", x, std::floor(x), ral_sf_floor(x));
+        if (!same_d(std::ceil(x), ral_sf_ceil(x)) && cceil.bad++ == 0)
+            std::snprintf(cceil.first, sizeof cceil.first, "%a want %a got %a", x, std::ceil(x), ral_sf_ceil(x));
+        if (!same_d(std::fabs(x), ral_sf_fabs(x)) && cabs.bad++ == 0)
+            std::snprintf(cabs.first, sizeof cabs.first, "%a", x);
+        if ((x == 0.0) != ral_sf_is_zero(x) && czero.bad++ == 0)
+            std::snprintf(czero.first, sizeof czero.first, "%a", x);
+        if (!same_f((float)x, ral_sf_d2f(x)) && cd2f.bad++ == 0)
+            std::snprintf(cd2f.first, sizeof cd2f.first, "%a want %a got %a", x, (double)(float)x, (double)ral_sf_d2f(x));
+        // double -> int64 as cvt.rzi.s64.f64: NaN -> 0, saturating
+        cd2i.n++;
+        long long w;
+        if (std::isnan(x)) w = 0;
+        else if (x >= 9223372036854775808.0) w = INT64_MAX;
+        else if (x <= -9223372036854775808.0) w = INT64_MIN;
+        else w = (long long)x;
+        if (w != ral_sf_d2i(x) && cd2i.bad++ == 0)
+            std::snprintf(cd2i.first, sizeof cd2i.first, "%a want %lld got %lld", x, w, ral_sf_d2i(x));
+    };
+    auto check_cmp = [&](double a, double b) {
+        ccmp.n++;
+        const unsigned want = host_compare(a, b);
+        const unsigned got = (unsigned)ral_sf_lt(a, b) | (unsigned)ral_sf_le(a, b) << 1 | (unsigned)ral_sf_gt(a, b) << 2 |
+                             (unsigned)ral_sf_ge(a, b) << 3 | (unsigned)ral_sf_eq(a, b) << 4 |
+                             (unsigned)ral_sf_ne(a, b) << 5;
+        if (want != got && ccmp.bad++ == 0)
+            std::snprintf(ccmp.first, sizeof ccmp.first, "%a vs %a (%llx %llx): want %x got %x", a, b,
+                          (unsigned long long)bits(a), (unsigned long long)bits(b), want, got);
+    };
+    for (double a : sp) {
+        check_unary(a);
+        for (double b : sp) {
+            check_div(a, b);
+            check_cmp(a, b);
+        }
+    }
+    for (long long k = 0; k < N; k++) {
+        const double a = rand_double(), b = rand_double();
+        check_div(a, b);
+        check_cmp(a, b);
+        check_cmp(a, a);
+        check_unary(a);
+        // quotients near 1 and exact quotients exercise the rounding boundaries
+        check_div(a, a * (1.0 + std::ldexp((double)(rng() % 64) - 32, -52)));
+        const double q = std::ldexp((double)(rng() >> 11), -(int)(rng() % 40));
+        check_div(q * b, b);
+        // int64 -> double
+        ci2d.n++;
+        const long long x = (long long)(rng() >> (rng() % 64)) * ((rng() & 1) ? -1 : 1);
+        if (!same_d((double)x, ral_sf_i2d(x)) && ci2d.bad++ == 0)
+            std::snprintf(ci2d.first, sizeof ci2d.first, "%lld want %a got %a", x, (double)x, ral_sf_i2d(x));
+        // float -> double
+        cf2d.n++;
+        const float f = flt((uint32_t)rng());
+        if (!same_d((double)f, ral_sf_f2d(f)) && cf2d.bad++ == 0)
+            std::snprintf(cf2d.first, sizeof cf2d.first, "%a", (double)f);
+    }
+    for (long long x : std::vector<long long>{0ll, 1ll, -1ll, (long long)INT64_MAX, (long long)INT64_MIN, (1ll << 53) + 1, -(1ll << 53) - 1, (1ll << 62) + 3}) {
+        ci2d.n++;
+        if (!same_d((double)x, ral_sf_i2d(x)) && ci2d.bad++ == 0)
+            std::snprintf(ci2d.first, sizeof ci2d.first, "%lld", x);
+    }
+    for (Counter* c : {&cdiv, &cfloor, &cceil, &cabs, &ccmp, &ci2d, &cd2i, &cf2d, &cd2f, &czero}) c->report();
+    return 0;
+}
