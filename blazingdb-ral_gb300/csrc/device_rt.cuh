@@ -9,7 +9,7 @@
 // double} registers (src/Interpreter/interpreter_ops.cuh:574-838): explicit
 // _rn intrinsics keep every double operation separately rounded (never
 // contracted into an FMA), integer add/sub/mul wrap, double->int64 truncates
-// and saturates with NaN -> 0 (cvt.rzi.s64.f64).
+// and saturates with NaN -> INT64_MIN (cvt.rzi.s64.f64 on the GPU).
 #ifndef RAL_DEVICE_RT_CUH_
 #define RAL_DEVICE_RT_CUH_
 

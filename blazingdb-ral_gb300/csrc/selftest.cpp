@@ -59,7 +59,7 @@ extern "C" __global__ void ral_softfp_selftest(unsigned long long* out, long lon
         if (hw != sw) st_bad(out, 3, a, b0);
         const long long x = (long long)(r1 >> (r0 % 64)) * ((r0 & 64) ? -1 : 1);
         if (!st_same(ral_sf_i2d(x), __ll2double_rn(x))) st_bad(out, 4, __longlong_as_double(x), 0.0);
-        if (ral_sf_d2i(a) != __double2ll_rz(a)) st_bad(out, 5, a, 0.0);
+        if (ral_sf_d2i(a) != __double2ll_rz(a)) st_bad(out, 5, a, __longlong_as_double(__double2ll_rz(a)));
         const float f = __uint_as_float((unsigned)r3);
         if (!st_same(ral_sf_f2d(f), (double)f)) st_bad(out, 6, (double)f, 0.0);
         const float g1 = ral_sf_d2f(a), g2 = __double2float_rn(a);

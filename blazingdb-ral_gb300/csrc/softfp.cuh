@@ -256,11 +256,12 @@ RAL_SF double ral_sf_i2d(long long x) {
     return ral_sf_double(s | ((unsigned long long)e << 52) | (m & RAL_SF_FRAC));
 }
 
-// double -> int64, truncating; NaN -> 0, out of range saturates (cvt.rzi.s64.f64)
+// double -> int64 as cvt.rzi.s64.f64 does it on the GPU: truncating, out of range saturates,
+// NaN -> INT64_MIN
 RAL_SF long long ral_sf_d2i(double d) {
     const unsigned long long A = ral_sf_bits(d);
     const int e = (int)((A >> 52) & 0x7ff);
-    if (ral_sf_isnan_bits(A)) return 0;
+    if (ral_sf_isnan_bits(A)) return (long long)RAL_SF_SIGN;
     if (e < 1023) return 0;
     const bool neg = (A >> 63) != 0;
     if (e >= 1023 + 63) return neg ? (long long)RAL_SF_SIGN : 0x7fffffffffffffffll;

@@ -148,9 +148,10 @@ uint64_t scalar_slot_bits(const Scalar& s, bool float_literal_compat) {
     return (uint64_t)v;
 }
 
-// double -> int64 as the GPU's cvt.rzi.s64.f64 does it: truncate, saturate, NaN -> 0.
+// static_cast<int64_t> of a double in the reference's device code: cvt.rzi.s64.f64, which
+// truncates, saturates out-of-range values and turns NaN into INT64_MIN (measured on the GPU)
 inline int64_t d2i(double d) {
-    if (std::isnan(d)) return 0;
+    if (std::isnan(d)) return INT64_MIN;
     if (d >= 9223372036854775808.0) return INT64_MAX;
     if (d <= -9223372036854775808.0) return INT64_MIN;
     return (int64_t)d;

@@ -81,10 +81,10 @@ int main(int argc, char** argv) {
             std::snprintf(czero.first, sizeof czero.first, "%a", x);
         if (!same_f((float)x, ral_sf_d2f(x)) && cd2f.bad++ == 0)
             std::snprintf(cd2f.first, sizeof cd2f.first, "%a want %a got %a", x, (double)(float)x, (double)ral_sf_d2f(x));
-        // double -> int64 as cvt.rzi.s64.f64: NaN -> 0, saturating
+        // double -> int64 as cvt.rzi.s64.f64 on the GPU: NaN -> INT64_MIN, saturating
         cd2i.n++;
         long long w;
-        if (std::isnan(x)) w = 0;
+        if (std::isnan(x)) w = INT64_MIN;
         else if (x >= 9223372036854775808.0) w = INT64_MAX;
         else if (x <= -9223372036854775808.0) w = INT64_MIN;
         else w = (long long)x;
