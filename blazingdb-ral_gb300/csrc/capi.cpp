@@ -392,7 +392,7 @@ int ral_debug_program_source(const gdf_dtype* input_dtypes, const int32_t* input
         if (!p.build(ins, ot, ov, left_inputs, right_inputs, outputs, num_operations, final_output_positions,
                      operators, unary_operators, left_scalars, right_scalars, err))
             return set_error(kUnsupported, err);
-        GeneratedKernel gk = generate_eval_kernel(p, default_shape(p));
+        GeneratedKernel gk = generate_eval_kernel(p, eval_shape(p));
         copy_out(std::string(jit_prelude()) + "\n" + gk.source, source_out, source_capacity);
         if (compile) {
             size_t bytes = 0;

@@ -3,6 +3,7 @@
 
 #include <algorithm>
 #include <functional>
+#include <cstdlib>
 #include <sstream>
 #include <stdexcept>
 
@@ -37,8 +38,30 @@ Shape default_shape(const Program& p) {
     s.G = 16 / max_width(p);
     s.J = std::max(1, 4 / s.G);
     s.threads = 256;
-    s.min_blocks = 1;
+    // four resident blocks (at most 64 registers a thread): the latency of the loads and of the
+    // integer-pipe double operations is hidden by more warps, not by more registers
+    s.min_blocks = 4;
     return s;
+}
+
+void apply_shape_tune(Shape& sh, const std::string& t) {
+    size_t i = 0;
+    while (i < t.size()) {
+        size_t e = t.find(',', i);
+        if (e == std::string::npos) e = t.size();
+        const std::string kv = t.substr(i, e - i);
+        const size_t eq = kv.find('=');
+        if (eq != std::string::npos) {
+            const std::string k = kv.substr(0, eq);
+            const int v = std::atoi(kv.c_str() + eq + 1);
+            if (k == "J" && v >= 1 && v * sh.G <= 2048) sh.J = v;
+            else if (k == "U" && v >= 1 && v <= 64) sh.unroll = v;
+            else if (k == "T" && (v == 128 || v == 256 || v == 512)) sh.threads = v;
+            else if (k == "B" && v >= 1 && v <= 16) sh.min_blocks = v;
+            else if (k == "S") sh.stage = v != 0;
+        }
+        i = e + 1;
+    }
 }
 
 namespace {

@@ -41,6 +41,9 @@ struct ParamLayout {
 int max_width(const Program& p);
 // Default shape for a program: G = 16 / widest column, J so that a lane covers 4 rows.
 Shape default_shape(const Program& p);
+// Applies "J=8,U=2,T=128,B=3,S=1" style overrides (slices, unroll, threads, min blocks per SM,
+// staging) to a shape; unknown keys and out-of-range values are ignored.
+void apply_shape_tune(Shape& sh, const std::string& t);
 
 struct GeneratedKernel {
     std::string name;

@@ -47,6 +47,17 @@ Config& config() {
     return c;
 }
 
+Shape eval_shape(const Program& p) {
+    Shape s = default_shape(p);
+    // RAL_EVAL_TUNE: shape overrides for the eval kernels ("J=4,B=3,T=128")
+    static const std::string tune = [] {
+        const char* e = std::getenv("RAL_EVAL_TUNE");
+        return std::string(e ? e : "");
+    }();
+    if (!tune.empty()) apply_shape_tune(s, tune);
+    return s;
+}
+
 int build_program(Program& p, gdf_column* const* outputs, int n_out, gdf_column* const* inputs, int n_in,
                   const ProgramArrays& pa, bool ignore_null_count) {
     if (n_in <= 0 || inputs == nullptr) return set_error(kInvalidArgument, "no input columns");
@@ -166,7 +177,7 @@ int perform_operation(gdf_column* const* outputs, int n_out, gdf_column* const* 
     for (int o = 0; o < n_out; o++)
         if (outputs[o]->size < n) return set_error(kInvalidArgument, "output column shorter than the input");
 
-    Shape s = opt.shape.G > 0 ? opt.shape : default_shape(p);
+    Shape s = opt.shape.G > 0 ? opt.shape : eval_shape(p);
     // vector loads need every touched buffer aligned to G elements
     const auto ref = p.inputs_referenced();
     bool ok_align = true;

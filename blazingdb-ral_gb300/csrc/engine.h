@@ -45,6 +45,9 @@ struct ProgramArrays {
     const gdf_scalar* rscalars;
 };
 
+// Launch shape of a perform_operation kernel: the default, with RAL_EVAL_TUNE's overrides.
+Shape eval_shape(const Program& p);
+
 struct EvalOptions {
     cudaStream_t stream = nullptr;
     bool sync = true;

@@ -319,25 +319,7 @@ std::string filter_tune() {
     return v ? std::string(v) : std::string();
 }
 
-void apply_tune(Shape& sh, const std::string& t) {
-    size_t i = 0;
-    while (i < t.size()) {
-        size_t e = t.find(',', i);
-        if (e == std::string::npos) e = t.size();
-        const std::string kv = t.substr(i, e - i);
-        const size_t eq = kv.find('=');
-        if (eq != std::string::npos) {
-            const std::string k = kv.substr(0, eq);
-            const int v = std::atoi(kv.c_str() + eq + 1);
-            if (k == "J" && v >= 1 && v * sh.G <= 2048) sh.J = v;
-            else if (k == "U" && v >= 1 && v <= 64) sh.unroll = v;
-            else if (k == "T" && (v == 128 || v == 256 || v == 512)) sh.threads = v;
-            else if (k == "B" && v >= 1 && v <= 16) sh.min_blocks = v;
-            else if (k == "S") sh.stage = v != 0;
-        }
-        i = e + 1;
-    }
-}
+void apply_tune(Shape& sh, const std::string& t) { apply_shape_tune(sh, t); }
 
 // Finishes a PreparedFilter whose spec (frame, predicate, projection, outputs) is filled in.
 int prepare_kernel(PreparedFilter& pf, bool aligned16, int64_t n) {

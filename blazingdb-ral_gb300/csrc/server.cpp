@@ -20,6 +20,10 @@ namespace {
 
 size_t round_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
 
+// Waiting credit of the wave order: a request that has waited 1 ms ranks as if it had 10M rows
+// fewer left (about the rows the GPU scans in that time), so that large requests are not starved.
+constexpr double kAgeRowsPerSecond = 1e10;
+
 // Item shape of a query: vector width from the widest column, 1024-row chunks at G = 2.
 Shape query_shape(const FilterPlan& plan, bool aligned16) {
     Shape sh;
@@ -275,7 +279,6 @@ int Server::launch_wave(Wave& w, const std::vector<int64_t>& reqs, const std::ve
     std::memset(h + off_counter, 0, 16);
     prefix[0] = 0;
     const double t = now();
-    std::vector<uint64_t> slots;
     w.last.assign(NP, 0);
     for (int k = 0; k < NP; k++) {
         ServerRequest& r = *requests_[reqs[k]];
@@ -297,12 +300,13 @@ int Server::launch_wave(Wave& w, const std::vector<int64_t>& reqs, const std::ve
             }
             r.t_launch = t;
         }
-        std::vector<gdf_column*> frame;
-        for (auto& c : tb.cols) frame.push_back(&c);
-        filter_fill_slots(*q.plan, q.item, frame.data(), tb.rows, r.out_data.data(), r.out_valid.data(), r.scratch,
-                          slots);
-        std::memset(descs + (size_t)k * stride_, 0, (size_t)stride_ * 8);
-        std::memcpy(descs + (size_t)k * stride_, slots.data(), slots.size() * 8);
+        if (r.slots.empty()) {
+            std::vector<gdf_column*> frame;
+            for (auto& c : tb.cols) frame.push_back(&c);
+            filter_fill_slots(*q.plan, q.item, frame.data(), tb.rows, r.out_data.data(), r.out_valid.data(), r.scratch,
+                              r.slots);
+        }
+        std::memcpy(descs + (size_t)k * stride_, r.slots.data(), r.slots.size() * 8);
         prefix[k + 1] = prefix[k] + take[k];
         base[k] = r.next_chunk;
         fn[k] = q.fn;
@@ -436,37 +440,32 @@ void Server::loop() {
                 pending_.pop_front();
             }
             stats_.peak_reserved = std::max(stats_.peak_reserved, reserved_);
-            // the wave: requests not in flight share wave_rows_ rows equally (a request that needs
-            // less than its share finishes in this wave), oldest first; rows left over go to the
-            // oldest requests.  Small requests finish within a wave of arriving and large ones
-            // advance every wave instead of waiting for the queue ahead of them to drain.
+            // the wave: requests not in flight, fewest rows left (less a waiting credit) first,
+            // each with at most a quarter of the wave, up to wave_rows_ rows
             std::vector<int64_t> reqs, take;
-            std::vector<int64_t> cand;
-            for (int64_t id : active_)
-                if (!requests_[id]->in_wave && (int)cand.size() < max_wave_requests_) cand.push_back(id);
-            if (!cand.empty()) {
-                const int64_t share = std::max<int64_t>(1, wave_rows_ / (int64_t)cand.size());
-                int64_t rows = 0;
-                for (int64_t id : cand) {
-                    const ServerRequest& r = *requests_[id];
-                    const ServerQuery& q = *queries_[r.query];
-                    const int64_t rpc = filter_tile_rows(q.item.shape);
-                    const int64_t left = q.chunks - r.next_chunk;
-                    const int64_t n = std::max<int64_t>(1, std::min<int64_t>(left, (share + rpc - 1) / rpc));
-                    reqs.push_back(id);
-                    take.push_back(n);
-                    rows += n * rpc;
-                }
-                for (size_t k = 0; k < reqs.size() && rows < wave_rows_; k++) {
-                    const ServerRequest& r = *requests_[reqs[k]];
-                    const ServerQuery& q = *queries_[r.query];
-                    const int64_t rpc = filter_tile_rows(q.item.shape);
-                    const int64_t more = std::min<int64_t>(q.chunks - r.next_chunk - take[k], (wave_rows_ - rows) / rpc);
-                    if (more > 0) {
-                        take[k] += more;
-                        rows += more * rpc;
-                    }
-                }
+            std::vector<std::pair<double, int64_t>> cand;  // (priority, id)
+            const double tnow = now();
+            for (int64_t id : active_) {
+                const ServerRequest& r = *requests_[id];
+                if (r.in_wave) continue;
+                const ServerQuery& q = *queries_[r.query];
+                const double left = (double)(q.chunks - r.next_chunk) * (double)filter_tile_rows(q.item.shape);
+                cand.push_back({left - (tnow - r.t_submit) * kAgeRowsPerSecond, id});
+            }
+            std::sort(cand.begin(), cand.end());
+            const int64_t slice = std::max<int64_t>(1, wave_rows_ / 4);
+            int64_t rows = 0;
+            for (auto& c : cand) {
+                if ((int)reqs.size() >= max_wave_requests_ || rows >= wave_rows_) break;
+                const ServerRequest& r = *requests_[c.second];
+                const ServerQuery& q = *queries_[r.query];
+                const int64_t rpc = filter_tile_rows(q.item.shape);
+                const int64_t left = q.chunks - r.next_chunk;
+                const int64_t cap_rows = std::min(slice, wave_rows_ - rows);
+                const int64_t n = std::max<int64_t>(1, std::min<int64_t>(left, (cap_rows + rpc - 1) / rpc));
+                reqs.push_back(c.second);
+                take.push_back(n);
+                rows += n * rpc;
             }
             if (!rc && !reqs.empty()) rc = launch_wave(*free_w, reqs, take);
             if (rc) {

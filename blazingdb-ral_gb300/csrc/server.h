@@ -5,10 +5,12 @@
 // scheduler thread admits requests while the working set (resident tables plus the outputs
 // and scratch of admitted requests) stays under a byte budget, and runs admitted requests in
 // waves: one launch of the persistent dispatcher whose warps pull (request, chunk) work items.
-// A wave carries about wave_rows rows, shared equally by the admitted requests not already in
-// flight; a large request is sliced over several waves (its look-back status words stay in its
-// scratch between them), so requests that arrive while a large one runs finish within a wave
-// or two instead of waiting for it, and large requests keep advancing.  Up to max_waves waves are in flight on their own
+// A wave carries about wave_rows rows.  Admitted requests not already in flight enter it in
+// order of fewest rows left, less a credit that grows with the time they have waited, each
+// with at most a quarter of the wave; a large request is sliced over several waves (its
+// look-back status words stay in its scratch between them).  So requests that arrive while a
+// large one runs finish within a wave or two instead of waiting for it, and large requests
+// keep advancing instead of starving under a stream of small ones.  Up to max_waves waves are in flight on their own
 // streams; a request is in at most one in-flight wave at a time, so no launch ever waits on
 // another.
 #pragma once
@@ -60,6 +62,7 @@ struct ServerRequest {
     bool done = false;
     int64_t next_chunk = 0;    // chunks launched so far
     bool in_wave = false;      // part of an in-flight wave
+    std::vector<uint64_t> slots;  // the request's parameter slots (after its first slice)
 };
 
 struct ServerStats {

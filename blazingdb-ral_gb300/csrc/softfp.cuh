@@ -128,9 +128,13 @@ RAL_SF double ral_sf_div(double a, double b) {
         e -= 1;
     }
     // reciprocal y ~ 2^116 / mb in (2^63, 2^64]: float seed, then two Newton steps
-    const float seed = ral_sf_rcp_estimate((float)(unsigned)(mb >> 29));  // ~ 2^29 / mb
-    const float ys = seed * 0x1p87f;
-    unsigned long long y = ys >= 0x1p64f ? 0xffffffffffffffffull : (unsigned long long)ys;
+    const float seed = ral_sf_rcp_estimate((float)(unsigned)(mb >> 29));  // ~ 2^29 / mb, in (2^-24, 2^-23]
+    // y0 = seed * 2^87 assembled from the float's fields (no float -> int64 conversion, which
+    // would run on the FP64 pipe)
+    const unsigned sb = ral_sf_fbits(seed);
+    const int sh = (int)((sb >> 23) & 0xffu) - 63;  // 40 for seeds below 2^-23
+    const unsigned long long sm = (unsigned long long)((sb & 0x7fffffu) | 0x800000u);
+    unsigned long long y = sh >= 41 ? 0xffffffffffffffffull : (sh <= 0 ? sm : sm << sh);
 #pragma unroll
     for (int it = 0; it < 2; ++it) {
         // err = 2^116 - mb * y, as a signed value scaled by 2^-52
