@@ -71,12 +71,25 @@ RAL_FI ral_i64 ral_muli(ral_i64 a, ral_i64 b) { return (ral_i64)((ral_u64)a * (r
 // and `%` in device code).  Here they are defined, identically in every kernel: x / 0 = 0,
 // x % 0 = 0, INT64_MIN / -1 = INT64_MIN (wrap), x % -1 = 0.  Without the guards the result
 // would depend on how the compiler happened to treat the undefined case.
+// The quotient and remainder themselves come from the integer-pipe division of softfp.cuh
+// (RAL_SOFT_FP) or from the compiler's 64-bit division; both are exact.
 RAL_FI ral_i64 ral_divi(ral_i64 a, ral_i64 b) {
     if (b == 0) return 0;
     if (b == -1) return (ral_i64)(0ull - (ral_u64)a);
+#if RAL_SOFT_FP
+    return ral_sf_div64(a, b);
+#else
     return a / b;
+#endif
 }
-RAL_FI ral_i64 ral_modi(ral_i64 a, ral_i64 b) { return (b == 0 || b == -1) ? 0 : a % b; }
+RAL_FI ral_i64 ral_modi(ral_i64 a, ral_i64 b) {
+    if (b == 0 || b == -1) return 0;
+#if RAL_SOFT_FP
+    return ral_sf_mod64(a, b);
+#else
+    return a % b;
+#endif
+}
 // Integer POWER: the reference multiplies `base` into 1, `e` times (e <= 0 -> 1);
 // square-and-multiply gives the same value modulo 2^64.
 RAL_FI ral_i64 ral_powi(ral_i64 base, ral_i64 e) {

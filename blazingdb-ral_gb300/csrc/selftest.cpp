@@ -66,6 +66,11 @@ extern "C" __global__ void ral_softfp_selftest(unsigned long long* out, long lon
         if (!((g1 != g1 && g2 != g2) || __float_as_uint(g1) == __float_as_uint(g2))) st_bad(out, 7, a, 0.0);
         if (ral_sf_is_zero(a) != (a == 0.0)) st_bad(out, 8, a, 0.0);
         if (!st_same(ral_sf_fabs(a), fabs(a))) st_bad(out, 9, a, 0.0);
+        const long long ia = (long long)(r0 >> (r1 % 64)) * ((r1 & 128) ? -1 : 1);
+        long long ib = (r2 & 1) ? (long long)(r3 >> (r2 % 64)) * ((r3 & 128) ? -1 : 1) : (long long)(1 + r3 % 1000);
+        if (ib == 0 || ib == -1) ib = 7;
+        if (ral_sf_div64(ia, ib) != ia / ib || ral_sf_mod64(ia, ib) != ia % ib)
+            st_bad(out, 10, __longlong_as_double(ia), __longlong_as_double(ib));
     }
 }
 )RALSRC";

@@ -330,4 +330,78 @@ RAL_SF float ral_sf_d2f(double d) {
     return ral_sf_float(s | (unsigned int)r);
 }
 
+// ---- 64-bit integer division ------------------------------------------------------------------
+
+// n / d and n % d for d >= 1, exactly, by the same reciprocal method: a float seed for
+// 2^127 / (d normalised), two Newton steps in 64-bit fixed point, a quotient estimate within a
+// few units and an exact correction from the remainder.
+RAL_SF void ral_sf_udivmod64(unsigned long long n, unsigned long long d, unsigned long long* q_out,
+                             unsigned long long* r_out) {
+    if (d > n) {
+        *q_out = 0;
+        *r_out = n;
+        return;
+    }
+    if ((n >> 32) == 0) {  // both fit in 32 bits: the 32-bit division
+        const unsigned q32 = (unsigned)n / (unsigned)d;
+        *q_out = q32;
+        *r_out = n - (unsigned long long)q32 * d;
+        return;
+    }
+    if (d >> 63) {  // d >= 2^63 and d <= n: the quotient is 1
+        *q_out = 1;
+        *r_out = n - d;
+        return;
+    }
+    const int s = ral_sf_clz64(d);  // >= 1
+    const unsigned long long dn = d << s;
+    const float seed = ral_sf_rcp_estimate((float)(unsigned)(dn >> 40));  // ~ 2^40 / dn
+    const unsigned sb = ral_sf_fbits(seed);
+    const int sh = (int)((sb >> 23) & 0xffu) - 63;
+    const unsigned long long sm = (unsigned long long)((sb & 0x7fffffu) | 0x800000u);
+    unsigned long long y = sh >= 41 ? 0xffffffffffffffffull : (sh <= 0 ? sm : sm << sh);  // ~ 2^127 / dn
+#pragma unroll
+    for (int it = 0; it < 2; ++it) {
+        const unsigned long long plo = dn * y, phi = ral_sf_umulh(dn, y);
+        const unsigned long long p63 = (phi << 1) | (plo >> 63);  // (dn * y) >> 63, mod 2^64
+        const long long err = (long long)(0ull - p63);            // (2^127 - dn * y) >> 63
+        const unsigned long long mag = err < 0 ? (0ull - (unsigned long long)err) : (unsigned long long)err;
+        const unsigned long long corr = ral_sf_umulh(y, mag);
+        y = err < 0 ? y - corr : y + corr;
+    }
+    // n / d = n * 2^s / dn ~ (n * y) >> (127 - s)
+    unsigned long long q = ral_sf_umulh(n, y) >> (63 - s);
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {  // too large: q * d > n
+        if (ral_sf_umulh(q, d) != 0 || q * d > n) q -= 1;
+    }
+    unsigned long long r = n - q * d;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        if (r >= d) {
+            q += 1;
+            r -= d;
+        }
+    }
+    *q_out = q;
+    *r_out = r;
+}
+
+// Signed quotient and remainder with C semantics (truncation; the remainder takes the
+// dividend's sign); d == 0 and d == -1 are left to the caller.
+RAL_SF long long ral_sf_div64(long long a, long long b) {
+    const unsigned long long ua = a < 0 ? 0ull - (unsigned long long)a : (unsigned long long)a;
+    const unsigned long long ub = b < 0 ? 0ull - (unsigned long long)b : (unsigned long long)b;
+    unsigned long long q, r;
+    ral_sf_udivmod64(ua, ub, &q, &r);
+    return ((a < 0) != (b < 0)) ? (long long)(0ull - q) : (long long)q;
+}
+RAL_SF long long ral_sf_mod64(long long a, long long b) {
+    const unsigned long long ua = a < 0 ? 0ull - (unsigned long long)a : (unsigned long long)a;
+    const unsigned long long ub = b < 0 ? 0ull - (unsigned long long)b : (unsigned long long)b;
+    unsigned long long q, r;
+    ral_sf_udivmod64(ua, ub, &q, &r);
+    return a < 0 ? (long long)(0ull - r) : (long long)r;
+}
+
 #endif  // RAL_SOFTFP_CUH_

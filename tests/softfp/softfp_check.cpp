@@ -61,6 +61,14 @@ int main(int argc, char** argv) {
     };
     std::vector<double> sp = special_doubles();
 
+    Counter cdiv64{"div64"};
+    auto check_div64 = [&](long long a, long long b) {
+        if (b == 0 || b == -1) return;
+        cdiv64.n++;
+        if ((a / b != ral_sf_div64(a, b) || a % b != ral_sf_mod64(a, b)) && cdiv64.bad++ == 0)
+            std::snprintf(cdiv64.first, sizeof cdiv64.first, "%lld / %lld: want %lld %lld got %lld %lld", a, b, a / b,
+                          a % b, ral_sf_div64(a, b), ral_sf_mod64(a, b));
+    };
     Counter cdiv{"div"}, cfloor{"floor"}, cceil{"ceil"}, cabs{"fabs"}, ccmp{"compare"}, ci2d{"i2d"}, cd2i{"d2i"},
         cf2d{"f2d"}, cd2f{"d2f"}, czero{"is_zero"};
     auto check_div = [&](double a, double b) {
@@ -123,6 +131,15 @@ int main(int argc, char** argv) {
         const long long x = (long long)(rng() >> (rng() % 64)) * ((rng() & 1) ? -1 : 1);
         if (!same_d((double)x, ral_sf_i2d(x)) && ci2d.bad++ == 0)
             std::snprintf(ci2d.first, sizeof ci2d.first, "%lld want %a got %a", x, (double)x, ral_sf_i2d(x));
+        // 64-bit integer division: operands of every magnitude, divisors near powers of two
+        const long long xa = (long long)(rng() >> (rng() % 64)) * ((rng() & 1) ? -1 : 1);
+        long long xb = (long long)(rng() >> (rng() % 64)) * ((rng() & 1) ? -1 : 1);
+        check_div64(xa, xb);
+        check_div64(xa, (long long)(1 + rng() % 1000));
+        xb = (long long)(1ull << (rng() % 63)) + (long long)(rng() % 3) - 1;
+        check_div64(xa, xb);
+        check_div64(INT64_MIN, xb);
+        check_div64(INT64_MAX, xb);
         // float -> double
         cf2d.n++;
         const float f = flt((uint32_t)rng());
@@ -134,6 +151,6 @@ int main(int argc, char** argv) {
         if (!same_d((double)x, ral_sf_i2d(x)) && ci2d.bad++ == 0)
             std::snprintf(ci2d.first, sizeof ci2d.first, "%lld", x);
     }
-    for (Counter* c : {&cdiv, &cfloor, &cceil, &cabs, &ccmp, &ci2d, &cd2i, &cf2d, &cd2f, &czero}) c->report();
+    for (Counter* c : {&cdiv64, &cdiv, &cfloor, &cceil, &cabs, &ccmp, &ci2d, &cd2i, &cf2d, &cd2f, &czero}) c->report();
     return 0;
 }
