@@ -5,6 +5,8 @@ nullable inputs and 3 outputs (f1, f2 float64; i1 int64), evaluated by
 ral_perform_operation_async on HBM-resident columns.  Other workloads:
   --workload plain_vm          1M-row filter + project (fused)
   --workload filter_gather     500M-row filter + compaction + gather, --selectivity 0.01/0.5/0.99
+  --workload filter_project    200M-row fused filter + project: the fused_project columns and its
+                               projection (as RexNode text) behind a filter on k, --selectivity s
   --workload batched           256 programs of 4-48 ops over tables of log-uniform [1e3, 5e7] rows,
                                all in one persistent launch replayed as a CUDA graph, against the
                                same 256 programs as plain synchronous perform_operation calls
@@ -195,9 +197,21 @@ def cpu_filter_gather(rows: int, threads: int, selectivity: float):
     return time.perf_counter() - t0
 
 
+def cpu_filter_project(rows: int, threads: int, selectivity: float):
+    import oracle as O
+    from ralgpu import workloads as W
+    frame = [O.make_column(v, t, m) for t, v, m in W.fused_project_host(rows, seed=99)]
+    t0 = time.perf_counter()
+    f = O.process_filter(frame, W.filter_project_filter(selectivity), nthreads=threads)
+    O.execute_project_plan(f, W.FILTER_PROJECT_PROJECT, nthreads=threads)
+    return time.perf_counter() - t0
+
+
 def cpu_time(workload, rows, threads, selectivity):
     if workload == "fused_project":
         return cpu_fused_project(rows, threads)
+    if workload == "filter_project":
+        return cpu_filter_project(rows, threads, selectivity)
     if workload == "plain_vm":
         return cpu_plain_vm(rows, threads)
     return cpu_filter_gather(rows, threads, selectivity)
@@ -342,7 +356,20 @@ def filter_setup(workload, n, selectivity, device):
     import ralgpu as R
     from ralgpu import workloads as W
     L = R.lib()
-    if workload == "plain_vm":
+    if workload == "filter_project":
+        frame = []
+        for t, data, valid, nulls in W.fused_project_device(n, device=device):
+            frame.append(R.Column(data, valid, t, size=n, null_count=nulls))
+        fq, pq = W.filter_project_filter(selectivity), W.FILTER_PROJECT_PROJECT
+        types, evald = R.project_output_types([c.dtype for c in frame], pq)
+        outs = [R.Column.empty(t, n) for t in types]
+        in_b = [R.dtypes.WIDTH[c.dtype] + 1 / 8 for c in frame]   # every column (+ mask) is read
+        out_b = sum(R.dtypes.WIDTH[t] + 1 / 8 for t in types)
+        cfg = {"workload": "filter_project", "rows": n, "selectivity": selectivity,
+               "filter": f"k < {int(round(1000 * selectivity))}", "project": "f1, f2, i1 of the 12-op program",
+               "inputs": "a,b int64; x,y float64; k int32; 5% nulls", "fused": "filter+project in one kernel",
+               "l2": "inputs exceed L2; no flush"}
+    elif workload == "plain_vm":
         spec = W.plain_vm_host(n)
         frame = [R.Column.from_numpy(v, t, m) for t, v, m in spec]
         fq, pq = W.PLAIN_VM_FILTER, W.PLAIN_VM_PROJECT
@@ -429,7 +456,8 @@ def run_ours(args):
     world, rank, local = dist_setup(args)
     torch.cuda.set_device(local)
     device = f"cuda:{local}"
-    n = args.rows or {"fused_project": 200_000_000, "plain_vm": 1_000_000, "filter_gather": 500_000_000}[args.workload]
+    n = args.rows or {"fused_project": 200_000_000, "plain_vm": 1_000_000, "filter_gather": 500_000_000,
+                      "filter_project": 200_000_000}[args.workload]
     if args.workload == "fused_project":
         ctx = fused_project_setup(n, device)
     else:
@@ -466,7 +494,8 @@ def run_ours(args):
     peak, peak_kind = load_peaks()
     alg = ctx["alg_bytes"] if "alg_bytes" in ctx else ctx["alg_bytes_fn"]()
     achieved = alg / (kernel_ms / 1e3) / 1e9
-    traffic_key = args.workload if args.workload != "filter_gather" else f"filter_gather_{args.selectivity}"
+    traffic_key = args.workload if args.workload not in ("filter_gather", "filter_project") \
+        else f"{args.workload}_{args.selectivity}"
     traffic = load_traffic(traffic_key)
     out = {
         "metric": METRIC, "value": value, "unit": "rows/s", "n_gpus": world, "steps": args.steps,
@@ -802,7 +831,8 @@ def run_reference(args):
                "e2e": {"value": v, "unit": "rows/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
         print(json.dumps(out), flush=True)
         return
-    n = args.rows or {"fused_project": 200_000_000, "plain_vm": 1_000_000, "filter_gather": 500_000_000}[args.workload]
+    n = args.rows or {"fused_project": 200_000_000, "plain_vm": 1_000_000, "filter_gather": 500_000_000,
+                      "filter_project": 200_000_000}[args.workload]
     threads = os.cpu_count() or 1
     # bounded sample per step, sized from a probe so the whole run stays within a few minutes
     probe = min(n, 1_000_000)
@@ -830,7 +860,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="fused_project",
-                    choices=["fused_project", "plain_vm", "filter_gather", "batched", "served"])
+                    choices=["fused_project", "plain_vm", "filter_gather", "filter_project", "batched", "served"])
     ap.add_argument("--tables", type=int, default=24)
     ap.add_argument("--queries", type=int, default=96)
     ap.add_argument("--requests", type=int, default=50_000)

@@ -96,6 +96,18 @@ def fused_project_program() -> ProgramSpec:
         lscalars=[J] * len(L), rscalars=RS)
 
 
+# The same projection as RexNode text over the same five columns ($0=a $1=b $2=x $3=y $4=k), behind
+# a LogicalFilter on k: the fused filter + project at 200M rows.
+FILTER_PROJECT_PROJECT = ("LogicalProject(f1=[+(*($2, $3), /($2, $3))], "
+                          "f2=[+(ABS(-($3, $2)), *(>($1, 0), -(FLOOR($2), ABS(-($3, $2)))))], "
+                          "i1=[MOD($0, +($4, 1))])")
+
+
+def filter_project_filter(selectivity: float) -> str:
+    """k is uniform in [0, 1000): <($4, 1000 s) keeps a fraction s of the rows."""
+    return f"LogicalFilter(condition=[<($4, {int(round(1000 * selectivity))})])"
+
+
 def fused_project_host(n: int, seed: int = SEED, null_rate: float = 0.05):
     rng = np.random.default_rng(seed)
     lim = 1 << 40

@@ -520,3 +520,15 @@ def test_nan_to_integer_is_int64_min_as_on_the_gpu():
     # row 2: INT64_MIN % 3 = -2
     assert ora[0].data[2] == -2.0
     H.assert_columns_equal(dev[0], ora[0], what="MOD of NaN", check_null_count=False)
+
+
+@pytest.mark.parametrize("sel", [0.01, 0.5, 0.99])
+def test_filter_project_workload_matches_oracle(sel, filter_mode):
+    """The 200M-row fused filter + project workload's query, at 300k rows."""
+    spec = W.fused_project_host(300_001, seed=8)
+    got = R.filter_project(H.to_device(spec), W.filter_project_filter(sel), W.FILTER_PROJECT_PROJECT)
+    ef = O.process_filter(H.to_oracle(spec), W.filter_project_filter(sel))
+    ep = O.execute_project_plan(ef, W.FILTER_PROJECT_PROJECT)
+    assert len(got) == len(ep) == 3
+    for k, (g, e) in enumerate(zip(got, ep)):
+        H.assert_columns_equal(g, e, what=f"projection {k}")
