@@ -71,27 +71,35 @@ RAL_FI ral_i64 ral_muli(ral_i64 a, ral_i64 b) { return (ral_i64)((ral_u64)a * (r
 // and `%` in device code).  Here they are defined, identically in every kernel: x / 0 = 0,
 // x % 0 = 0, INT64_MIN / -1 = INT64_MIN (wrap), x % -1 = 0.  Without the guards the result
 // would depend on how the compiler happened to treat the undefined case.
-// The quotient and remainder themselves come from the compiler's 64-bit division, or with
-// RAL_SOFT_INT_DIV=1 from the integer-only division of softfp.cuh.  Both are exact; on GB300
-// the compiler's is faster overall (measured on the 12-op projection: the integer-only version
-// takes the FP64 pipe from 76% to 49% busy but the ALU pipe from 54% to 61% and the kernel from
-// 388 to 464 us), so it is the default.
+// The quotient and remainder themselves: RAL_SOFT_INT_DIV 2 (the default) divides by a divisor
+// that fits in 32 bits with the integer-only word division of softfp.cuh and by larger ones with
+// the compiler's 64-bit division, whose reciprocal step uses the FP64 pipe; 1 uses the integer-only
+// division for every divisor (slower on GB300: its 64-bit Newton steps cost more integer work than
+// they save); 0 the compiler's division for every divisor.  All are exact.
 #ifndef RAL_SOFT_INT_DIV
-#define RAL_SOFT_INT_DIV 0
+#define RAL_SOFT_INT_DIV 2
 #endif
+RAL_FI bool ral_small_divisor(ral_i64 b) {
+    const ral_u64 m = b < 0 ? 0ull - (ral_u64)b : (ral_u64)b;
+    return m <= 0xffffffffull;
+}
 RAL_FI ral_i64 ral_divi(ral_i64 a, ral_i64 b) {
     if (b == 0) return 0;
     if (b == -1) return (ral_i64)(0ull - (ral_u64)a);
-#if RAL_SOFT_INT_DIV
+#if RAL_SOFT_INT_DIV == 1
     return ral_sf_div64(a, b);
+#elif RAL_SOFT_INT_DIV == 2
+    return ral_small_divisor(b) ? ral_sf_div64(a, b) : a / b;
 #else
     return a / b;
 #endif
 }
 RAL_FI ral_i64 ral_modi(ral_i64 a, ral_i64 b) {
     if (b == 0 || b == -1) return 0;
-#if RAL_SOFT_INT_DIV
+#if RAL_SOFT_INT_DIV == 1
     return ral_sf_mod64(a, b);
+#elif RAL_SOFT_INT_DIV == 2
+    return ral_small_divisor(b) ? ral_sf_mod64(a, b) : a % b;
 #else
     return a % b;
 #endif

@@ -332,6 +332,78 @@ RAL_SF float ral_sf_d2f(double d) {
 
 // ---- 64-bit integer division ------------------------------------------------------------------
 
+// n / d and n % d for 1 <= d < 2^32: two 2-by-1 word divisions with a 32-bit reciprocal of the
+// normalised divisor (Moller and Granlund, "Improved division by invariant integers", IEEE Trans.
+// Computers 60(2), 2011, algorithm 4); the reciprocal floor((2^64 - 1) / d) - 2^32 comes from a float
+// estimate and an exact integer correction.
+RAL_SF unsigned int ral_sf_clz32(unsigned int x) {  // x != 0
+#if defined(__CUDA_ARCH__)
+    return (unsigned int)__clz((int)x);
+#else
+    return (unsigned int)__builtin_clz(x);
+#endif
+}
+
+RAL_SF void ral_sf_div_2by1(unsigned int u1, unsigned int u0, unsigned int d, unsigned int v, unsigned int* q,
+                            unsigned int* r) {
+    const unsigned long long p = (unsigned long long)v * u1 + (((unsigned long long)u1 << 32) | u0);
+    unsigned int q1 = (unsigned int)(p >> 32) + 1u;
+    const unsigned int q0 = (unsigned int)p;
+    unsigned int rr = u0 - q1 * d;
+    if (rr > q0) {
+        q1 -= 1u;
+        rr += d;
+    }
+    if (rr >= d) {
+        q1 += 1u;
+        rr -= d;
+    }
+    *q = q1;
+    *r = rr;
+}
+
+RAL_SF void ral_sf_udivmod64_32(unsigned long long n, unsigned int d, unsigned long long* q_out,
+                                unsigned long long* r_out) {
+    const unsigned int s = ral_sf_clz32(d);
+    const unsigned int dn = d << s;  // top bit set
+    // v0 ~ 2^64 / dn - 2^32 from a float reciprocal, assembled from its fields
+    const float f = ral_sf_rcp_estimate((float)dn);                 // ~ 1 / dn, in (2^-32, 2^-31]
+    const unsigned fb = ral_sf_fbits(f);
+    const int sh = (int)((fb >> 23) & 0xffu) - 86;                  // f * 2^64 = (2^23 + M) << sh
+    const unsigned long long big = (unsigned long long)((fb & 0x7fffffu) | 0x800000u) << (sh > 0 ? sh : 0);
+    unsigned long long v0 = big > 0x1ffffffffull ? 0xffffffffull : (big < 0x100000000ull ? 0ull : big - 0x100000000ull);
+    // exact: v = floor((2^64 - 1) / dn) - 2^32, i.e. e = 2^64 - 1 - (2^32 + v) dn in [0, dn)
+    const unsigned long long A = ~((unsigned long long)dn << 32);
+    long long e = (long long)(A - v0 * dn);
+    const int adj = (int)((float)e * f);                            // ~ e / dn, |adj| < 2^13
+    v0 = (unsigned long long)((long long)v0 + adj);
+    e = (long long)(A - v0 * dn);
+#pragma unroll
+    for (int k = 0; k < 2; ++k) {
+        if (e < 0) {
+            v0 -= 1;
+            e += dn;
+        }
+    }
+#pragma unroll
+    for (int k = 0; k < 2; ++k) {
+        if (e >= (long long)dn) {
+            v0 += 1;
+            e -= dn;
+        }
+    }
+    const unsigned int v = (unsigned int)v0;
+    // numerator n << s as three words; the top word is below dn
+    const unsigned long long ns = n << s;
+    const unsigned int w2 = s ? (unsigned int)(n >> (64 - s)) : 0u;
+    unsigned int q1, q0, r;
+    ral_sf_div_2by1(w2, (unsigned int)(ns >> 32), dn, v, &q1, &r);
+    ral_sf_div_2by1(r, (unsigned int)ns, dn, v, &q0, &r);
+    *q_out = ((unsigned long long)q1 << 32) | q0;
+    *r_out = r >> s;
+}
+
+
 // n / d and n % d for d >= 1, exactly, by the same reciprocal method: a float seed for
 // 2^127 / (d normalised), two Newton steps in 64-bit fixed point, a quotient estimate within a
 // few units and an exact correction from the remainder.
@@ -346,6 +418,10 @@ RAL_SF void ral_sf_udivmod64(unsigned long long n, unsigned long long d, unsigne
         const unsigned q32 = (unsigned)n / (unsigned)d;
         *q_out = q32;
         *r_out = n - (unsigned long long)q32 * d;
+        return;
+    }
+    if ((d >> 32) == 0) {  // 32-bit divisor: two word divisions
+        ral_sf_udivmod64_32(n, (unsigned int)d, q_out, r_out);
         return;
     }
     if (d >> 63) {  // d >= 2^63 and d <= n: the quotient is 1

@@ -69,6 +69,15 @@ int main(int argc, char** argv) {
             std::snprintf(cdiv64.first, sizeof cdiv64.first, "%lld / %lld: want %lld %lld got %lld %lld", a, b, a / b,
                           a % b, ral_sf_div64(a, b), ral_sf_mod64(a, b));
     };
+    Counter cd32{"div64_32"};
+    auto check_d32 = [&](unsigned long long n, unsigned int d) {
+        if (d == 0) return;
+        cd32.n++;
+        unsigned long long q, r;
+        ral_sf_udivmod64_32(n, d, &q, &r);
+        if ((q != n / d || r != n % d) && cd32.bad++ == 0)
+            std::snprintf(cd32.first, sizeof cd32.first, "%llu / %u: want %llu %llu got %llu %llu", n, d, n / d, n % d, q, r);
+    };
     Counter cdiv{"div"}, cfloor{"floor"}, cceil{"ceil"}, cabs{"fabs"}, ccmp{"compare"}, ci2d{"i2d"}, cd2i{"d2i"},
         cf2d{"f2d"}, cd2f{"d2f"}, czero{"is_zero"};
     auto check_div = [&](double a, double b) {
@@ -139,6 +148,10 @@ int main(int argc, char** argv) {
         xb = (long long)(1ull << (rng() % 63)) + (long long)(rng() % 3) - 1;
         check_div64(xa, xb);
         check_div64(INT64_MIN, xb);
+        check_d32(rng() >> (rng() % 64), (unsigned)(rng() >> (32 + rng() % 32)));
+        check_d32(rng(), (unsigned)(1 + rng() % 1000));
+        check_d32(rng(), 0xffffffffu - (unsigned)(rng() % 3));
+        check_d32(rng(), (1u << (rng() % 32)) + (unsigned)(rng() % 3) - 1u);
         check_div64(INT64_MAX, xb);
         // float -> double
         cf2d.n++;
@@ -151,6 +164,6 @@ int main(int argc, char** argv) {
         if (!same_d((double)x, ral_sf_i2d(x)) && ci2d.bad++ == 0)
             std::snprintf(ci2d.first, sizeof ci2d.first, "%lld", x);
     }
-    for (Counter* c : {&cdiv64, &cdiv, &cfloor, &cceil, &cabs, &ccmp, &ci2d, &cd2i, &cf2d, &cd2f, &czero}) c->report();
+    for (Counter* c : {&cd32, &cdiv64, &cdiv, &cfloor, &cceil, &cabs, &ccmp, &ci2d, &cd2i, &cf2d, &cd2f, &czero}) c->report();
     return 0;
 }
