@@ -44,7 +44,11 @@ uint64_t fnv1a(const std::string& s, uint64_t h = 1469598103934665603ull) {
 const std::string& soft_fp_define() {
     static const std::string d = [] {
         const char* e = std::getenv("RAL_SOFT_FP");
-        return std::string("#define RAL_SOFT_FP ") + ((e && std::string(e) == "0") ? "0" : "1") + "\n";
+        std::string out = std::string("#define RAL_SOFT_FP ") + ((e && std::string(e) == "0") ? "0" : "1") + "\n";
+        // RAL_SOFT_INT_DIV=1|2: integer-only 64-bit division for every / for 32-bit divisors
+        const char* i = std::getenv("RAL_SOFT_INT_DIV");
+        if (i && (std::string(i) == "1" || std::string(i) == "2")) out += std::string("#define RAL_SOFT_INT_DIV ") + i + "\n";
+        return out;
     }();
     return d;
 }
