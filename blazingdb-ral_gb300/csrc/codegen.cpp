@@ -579,6 +579,7 @@ GeneratedKernel generate_filter_kernel(const FilterSpec& f, const Shape& s, bool
     char hex[32];
     snprintf(hex, sizeof hex, "%016llx", (unsigned long long)fnv1a(key.str()));
     gk.name = std::string(item ? "ral_fitem_" : "ral_filter_") + hex;
+    gk.soft_fp = !item;
 
     std::ostringstream os;
     os << "// generated: " << key.str() << "\n";
@@ -920,6 +921,7 @@ GeneratedKernel generate_batch_item(const Program& p, const Shape& sh) {
     char hex[32];
     snprintf(hex, sizeof hex, "%016llx", (unsigned long long)fnv1a(key.str()));
     gk.name = std::string("ral_item_") + hex;
+    gk.soft_fp = false;
     const std::string sfx = hex;
 
     std::ostringstream os;

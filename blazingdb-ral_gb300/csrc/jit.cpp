@@ -40,8 +40,11 @@ uint64_t fnv1a(const std::string& s, uint64_t h = 1469598103934665603ull) {
 }
 
 // RAL_SOFT_FP=0 selects the hardware FP64 instructions for the operations that otherwise run
-// on the integer pipes (same results; for comparison and diagnosis)
-const std::string& soft_fp_define() {
+// on the integer pipes (same results; for comparison and diagnosis); kernels whose
+// GeneratedKernel::soft_fp is false always use them
+const std::string& soft_fp_define(bool soft) {
+    static const std::string off = "#define RAL_SOFT_FP 0\n";
+    if (!soft) return off;
     static const std::string d = [] {
         const char* e = std::getenv("RAL_SOFT_FP");
         std::string out = std::string("#define RAL_SOFT_FP ") + ((e && std::string(e) == "0") ? "0" : "1") + "\n";
@@ -54,7 +57,7 @@ const std::string& soft_fp_define() {
 }
 
 std::string full_source(const GeneratedKernel& gk) {
-    return soft_fp_define() + std::string(ral_prelude_source) + "\n" + gk.source;
+    return soft_fp_define(gk.soft_fp) + std::string(ral_prelude_source) + "\n" + gk.source;
 }
 
 std::string cache_dir() {
