@@ -576,8 +576,8 @@ def run_batched(args):
             if k not in keys or p["rows"] > keys[k]["rows"]:
                 keys[k] = p
         for k, p in keys.items():
-            J, U, ms = R.autotune_program(p["outs"], p["ins"], *p["args"])
-            tuned[k] = [J, U, round(ms, 4)]
+            J, U, soft, ms = R.autotune_program(p["outs"], p["ins"], *p["args"])
+            tuned[k] = [J, U, int(soft), round(ms, 4)]
     tune_s = time.perf_counter() - t0
     t0 = time.perf_counter()
     b = R.Batch()
@@ -646,6 +646,7 @@ def run_batched(args):
         "batched": {"launch": "one persistent kernel per step, replayed as a CUDA graph",
                     "kernel": info, "ms_per_step": ms_per_step,
                     "prepare_s": round(prep_s, 2), "autotune_s": round(tune_s, 2), "tuned_keys": len(tuned),
+                    "tuned_integer_pipe_keys": sum(v[2] for v in tuned.values()),
                     "generate_s": round(gen_s, 2)},
         "plain_per_call": plain,
         "speedup_vs_plain": value / plain["value"] if plain else None,

@@ -25,7 +25,7 @@ namespace {
 
 std::mutex g_tune_mu;
 struct TuneEntry {
-    int J = 0, U = 1;
+    int J = 0, U = 1, S = 0;
     double ms = 0;
 };
 std::map<std::string, TuneEntry> g_tune;
@@ -42,7 +42,7 @@ std::string tune_path() {
     return dir + "/autotune.json";
 }
 
-// The table is a flat JSON object {"key": [J, U, ms], ...}; keys contain no quotes.
+// The table is a flat JSON object {"key": [J, U, ms, S], ...}; keys contain no quotes.
 void load_tune_locked() {
     if (g_tune_loaded) return;
     g_tune_loaded = true;
@@ -59,9 +59,11 @@ void load_tune_locked() {
         const size_t lb = t.find('[', e), rb = t.find(']', e);
         if (lb == std::string::npos || rb == std::string::npos) break;
         TuneEntry te;
-        if (std::sscanf(t.c_str() + lb + 1, "%d , %d , %lf", &te.J, &te.U, &te.ms) == 3 && te.J >= 1 && te.J <= 64 &&
-            te.U >= 1 && te.U <= 64)
+        const int got = std::sscanf(t.c_str() + lb + 1, "%d , %d , %lf , %d", &te.J, &te.U, &te.ms, &te.S);
+        if (got >= 3 && te.J >= 1 && te.J <= 64 && te.U >= 1 && te.U <= 64) {
+            if (got < 4) te.S = 0;
             g_tune[key] = te;
+        }
         i = rb + 1;
     }
 }
@@ -73,7 +75,8 @@ void save_tune_locked() {
     f << "{\n";
     size_t k = 0;
     for (const auto& kv : g_tune) {
-        f << "  \"" << kv.first << "\": [" << kv.second.J << ", " << kv.second.U << ", " << kv.second.ms << "]"
+        f << "  \"" << kv.first << "\": [" << kv.second.J << ", " << kv.second.U << ", " << kv.second.ms << ", "
+          << kv.second.S << "]"
           << (++k < g_tune.size() ? ",\n" : "\n");
     }
     f << "}\n";
@@ -136,16 +139,18 @@ Shape tuned_shape(const Program& p, int G) {
     if (it != g_tune.end()) {
         s.J = it->second.J;
         s.unroll = it->second.U;
+        s.soft = it->second.S != 0;
     }
     return s;
 }
 
-void record_tuned_shape(const Program& p, int G, int J, int U, double ms) {
+void record_tuned_shape(const Program& p, int G, int J, int U, bool soft, double ms) {
     std::lock_guard<std::mutex> lock(g_tune_mu);
     load_tune_locked();
     TuneEntry te;
     te.J = J;
     te.U = U;
+    te.S = soft ? 1 : 0;
     te.ms = ms;
     g_tune[tune_key(p, G)] = te;
     save_tune_locked();
@@ -209,6 +214,7 @@ int Batch::prepare(cudaStream_t st) {
         if (forced_J_ > 0) {
             s.J = forced_J_;
             s.unroll = forced_U_;
+            s.soft = forced_S_;
         }
         e->shape = s;
         e->items = (e->rows + 32LL * s.G * s.J - 1) / (32LL * s.G * s.J);

@@ -41,7 +41,7 @@ public:
     // Generated source (and an NVRTC-only compile) for the programs added so far.
     int debug_source(bool compile, std::string& source, std::string& log) const;
     // Every program of the batch at this tile shape instead of the tuned one (autotuning).
-    void force_shape(int J, int U) { forced_J_ = J; forced_U_ = U; }
+    void force_shape(int J, int U, bool soft) { forced_J_ = J; forced_U_ = U; forced_S_ = soft; }
 
 private:
     int launch(cudaStream_t stream);
@@ -62,15 +62,16 @@ private:
     cudaGraphExec_t graph_exec_ = nullptr;
     bool prepared_ = false;
     int forced_J_ = 0, forced_U_ = 1;
+    bool forced_S_ = false;
 };
 
-// Tile shape of a program's batch item: slices per warp tile J and the unroll of the slice loop,
-// from the autotuner's table (keyed by dtype mix and program length) or the default
-// (J = 8 / G, no unroll).
+// Tile shape of a program's batch item: slices per warp tile J, the unroll of the slice loop and
+// whether its double operations run on the integer pipes, from the autotuner's table (keyed by
+// dtype mix and program length) or the default (J = 8 / G, no unroll, FP64 instructions).
 Shape tuned_shape(const Program& p, int G);
 // Records a measured best for the program's key in the autotuner's table (persisted as JSON
 // in the JIT cache directory).
-void record_tuned_shape(const Program& p, int G, int J, int U, double ms);
+void record_tuned_shape(const Program& p, int G, int J, int U, bool soft, double ms);
 std::string tune_key(const Program& p, int G);
 
 // Compiles generated relocatable TUs on a pool of host threads (cached per name); appends the

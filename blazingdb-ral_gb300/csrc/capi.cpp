@@ -532,7 +532,7 @@ int ral_autotune_program(gdf_column* const* output_columns, int32_t num_outputs,
                          int32_t num_operations, const column_index_type* final_output_positions,
                          const int32_t* operators, const int32_t* unary_operators, const gdf_scalar* left_scalars,
                          const gdf_scalar* right_scalars, int32_t* best_slices, int32_t* best_unroll,
-                         double* best_ms) {
+                         int32_t* best_soft_fp, double* best_ms) {
     return guarded([&] {
         ProgramArrays pa{left_inputs, right_inputs, outputs, num_operations, final_output_positions,
                          operators, unary_operators, left_scalars, right_scalars};
@@ -540,24 +540,27 @@ int ral_autotune_program(gdf_column* const* output_columns, int32_t num_outputs,
         if (int e = build_program(p, output_columns, num_outputs, input_columns, num_inputs, pa, false)) return e;
         const int G = 16 / max_width(p);
         // candidates: rows per item 32*G*J, slice loop unrolled U times; all compiled up front
-        std::vector<std::pair<int, int>> cand;
-        for (int J : {2, 4, 8, 16})
-            for (int U : {1, 2})
-                if (U <= J && (int64_t)32 * G * J <= 8192) cand.push_back({J, U});
+        struct Cand { int J, U; bool S; };
+        std::vector<Cand> cand;
+        for (int S : {0, 1})
+            for (int J : {2, 4, 8, 16})
+                for (int U : {1, 2})
+                    if (U <= J && (int64_t)32 * G * J <= 8192) cand.push_back({J, U, S != 0});
         std::vector<std::unique_ptr<ral_batch_s>> bs;
         for (auto& c : cand) {
             auto b = std::make_unique<ral_batch_s>();
             const int idx = b->b.add(output_columns, num_outputs, input_columns, num_inputs, pa);
             if (idx < 0) return -idx;
-            b->b.force_shape(c.first, c.second);
+            b->b.force_shape(c.J, c.U, c.S);
             bs.push_back(std::move(b));
         }
         {   // compile every candidate's item and dispatcher at once, on the host thread pool
             std::vector<GeneratedKernel> tus;
             for (auto& c : cand) {
                 Shape sh = tuned_shape(p, G);
-                sh.J = c.first;
-                sh.unroll = c.second;
+                sh.J = c.J;
+                sh.unroll = c.U;
+                sh.soft = c.S;
                 tus.push_back(generate_batch_item(p, sh));
                 tus.push_back(generate_batch_dispatch({{tus.back().name, false}}, 0));
             }
@@ -585,9 +588,10 @@ int ral_autotune_program(gdf_column* const* output_columns, int32_t num_outputs,
         }
         cudaEventDestroy(e0);
         cudaEventDestroy(e1);
-        record_tuned_shape(p, G, cand[bi].first, cand[bi].second, best);
-        if (best_slices) *best_slices = cand[bi].first;
-        if (best_unroll) *best_unroll = cand[bi].second;
+        record_tuned_shape(p, G, cand[bi].J, cand[bi].U, cand[bi].S, best);
+        if (best_slices) *best_slices = cand[bi].J;
+        if (best_unroll) *best_unroll = cand[bi].U;
+        if (best_soft_fp) *best_soft_fp = cand[bi].S ? 1 : 0;
         if (best_ms) *best_ms = best;
         return check_cuda(cudaGetLastError(), "autotune");
     });

@@ -917,11 +917,11 @@ GeneratedKernel generate_batch_item(const Program& p, const Shape& sh) {
     gk.layout = make_layout(p, 0);
     const ParamLayout& L = gk.layout;
     std::ostringstream key;
-    key << "item|" << p.structure_key() << "#" << sh.G << "/" << sh.J << "/" << sh.unroll;
+    key << "item|" << p.structure_key() << "#" << sh.G << "/" << sh.J << "/" << sh.unroll << (sh.soft ? "/s" : "");
     char hex[32];
     snprintf(hex, sizeof hex, "%016llx", (unsigned long long)fnv1a(key.str()));
     gk.name = std::string("ral_item_") + hex;
-    gk.soft_fp = false;
+    gk.soft_fp = sh.soft;
     const std::string sfx = hex;
 
     std::ostringstream os;

@@ -24,6 +24,7 @@ struct Shape {
     int min_blocks = 1;  // __launch_bounds__ minimum resident blocks per SM
     int unroll = 4;    // filter kernels: unroll of the predicate pass over slices
     bool stage = false;  // filter kernels: dense slices written through a shared-memory stage
+    bool soft = false;   // batch items: integer-pipe double operations (the autotuner decides)
 };
 
 // Slot order of the kernel's parameter block (all 8-byte slots).
@@ -54,10 +55,11 @@ struct GeneratedKernel {
     std::vector<int> layout_project_lscalar, layout_project_rscalar;
     // filter item functions: shared-memory words the function needs in its warp's area
     int item_smem_words = 0;
-    // integer-pipe double operations (softfp.cuh) unless RAL_SOFT_FP=0.  Batched and served item
-    // functions use the FP64 instructions instead: hundreds of programs run side by side there,
-    // and the larger integer-pipe code of each one costs more in instruction-cache misses than
-    // it saves (measured: 256 programs over tables capped at 1M rows, 31.6 ms against 16.9 ms).
+    // integer-pipe double operations (softfp.cuh) unless RAL_SOFT_FP=0.  Batched item functions
+    // take it from their shape (the autotuner's choice; by default the FP64 instructions, since
+    // under the items' 64-register cap the larger integer-pipe code spills: 256 programs over
+    // tables capped at 1M rows ran 31.6 ms with it against 20.4 ms without); served chunk
+    // functions use the FP64 instructions.
     bool soft_fp = true;
 };
 

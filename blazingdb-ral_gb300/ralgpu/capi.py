@@ -78,7 +78,7 @@ _SIGS = {
     "ral_batch_tune_key": (C.c_int, [COLPP, C.c_int32, COLPP, C.c_int32, I16P, I16P, I16P, C.c_int32, I16P, I32P, I32P,
                                      SCP, SCP, C.c_char_p, C.c_int64]),
     "ral_autotune_program": (C.c_int, [COLPP, C.c_int32, COLPP, C.c_int32, I16P, I16P, I16P, C.c_int32, I16P, I32P,
-                                       I32P, SCP, SCP, I32P, I32P, C.POINTER(C.c_double)]),
+                                       I32P, SCP, SCP, I32P, I32P, I32P, C.POINTER(C.c_double)]),
 }
 
 
@@ -489,19 +489,21 @@ def batch_tune_key(output_columns: List[Column], input_columns: List[Column], le
 
 def autotune_program(output_columns: List[Column], input_columns: List[Column], left_inputs, right_inputs, outputs,
                      final_output_positions, operators, unary_operators, left_scalars,
-                     right_scalars) -> Tuple[int, int, float]:
+                     right_scalars) -> Tuple[int, int, bool, float]:
     """Times the program as a one-program batch at each candidate tile shape and records the
-    best in the autotuner's table (used by batches); returns (slices, unroll, ms per launch)."""
+    best in the autotuner's table (used by batches); returns (slices, unroll, integer-pipe double
+    operations, ms per launch)."""
     oa, _os = _colarray(output_columns)
     ia, _is = _colarray(input_columns)
     l, r, o, f = _i16(left_inputs), _i16(right_inputs), _i16(outputs), _i16(final_output_positions)
     b, u = _i32(operators), _i32(unary_operators)
     ls = _scalars([_as_scalar(s) for s in left_scalars])
     rs = _scalars([_as_scalar(s) for s in right_scalars])
-    J, U, ms = C.c_int32(0), C.c_int32(0), C.c_double(0)
+    J, U, S, ms = C.c_int32(0), C.c_int32(0), C.c_int32(0), C.c_double(0)
     _check(lib().ral_autotune_program(oa, len(output_columns), ia, len(input_columns), _p16(l), _p16(r), _p16(o),
-                                      len(l), _p16(f), _p32(b), _p32(u), ls, rs, C.byref(J), C.byref(U), C.byref(ms)))
-    return J.value, U.value, ms.value
+                                      len(l), _p16(f), _p32(b), _p32(u), ls, rs, C.byref(J), C.byref(U), C.byref(S),
+                                      C.byref(ms)))
+    return J.value, U.value, bool(S.value), ms.value
 
 
 class Server:

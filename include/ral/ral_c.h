@@ -248,11 +248,11 @@ int ral_batch_tune_key(gdf_column *const *output_columns, int32_t num_outputs, g
 
 /*
  * Autotuner: runs the perform_operation program as a one-program batch at each candidate tile
- * shape (rows per warp tile 32*G*J for J in 2, 4, 8, 16; slice loop unrolled 1 or 2 times),
- * times it and records the fastest in the tuning table (keyed by dtype mix and program length;
- * persisted as JSON in the JIT cache directory), which batches consult.  Writes the program's
- * outputs as a side effect.  *best_slices / *best_unroll receive the chosen shape and *best_ms
- * its kernel time.
+ * shape (rows per warp tile 32*G*J for J in 2, 4, 8, 16; slice loop unrolled 1 or 2 times; double
+ * operations on the integer pipes or as FP64 instructions), times it and records the fastest in
+ * the tuning table (keyed by dtype mix and program length; persisted as JSON in the JIT cache
+ * directory), which batches consult.  Writes the program's outputs as a side effect.
+ * *best_slices / *best_unroll / *best_soft_fp receive the chosen shape and *best_ms its kernel time.
  */
 int ral_autotune_program(gdf_column *const *output_columns, int32_t num_outputs, gdf_column *const *input_columns,
                          int32_t num_inputs, const column_index_type *left_inputs,
@@ -260,7 +260,7 @@ int ral_autotune_program(gdf_column *const *output_columns, int32_t num_outputs,
                          int32_t num_operations, const column_index_type *final_output_positions,
                          const int32_t *operators, const int32_t *unary_operators, const gdf_scalar *left_scalars,
                          const gdf_scalar *right_scalars, int32_t *best_slices, int32_t *best_unroll,
-                         double *best_ms);
+                         int32_t *best_soft_fp, double *best_ms);
 
 /* Generated source of the fused LogicalFilter kernel (optionally NVRTC-compiled, no GPU
  * needed) for a frame described by dtypes and mask presence; project_query_part may be

@@ -139,8 +139,8 @@ def test_autotune_records_a_shape_and_batch_still_matches():
     mix = W.batched_mix(4, seed=11, min_rows=100_000, max_rows=400_000)
     progs = _build(mix)
     p = progs[0]
-    J, U, ms = R.autotune_program(p["outs_b"], p["dev_in"], *_args(p["pp"]))
-    assert J in (2, 4, 8, 16) and U in (1, 2) and ms > 0
+    J, U, soft, ms = R.autotune_program(p["outs_b"], p["dev_in"], *_args(p["pp"]))
+    assert J in (2, 4, 8, 16) and U in (1, 2) and soft in (False, True) and ms > 0
     b = R.Batch()
     for p in progs:
         b.add(p["outs_b"], p["dev_in"], *_args(p["pp"]))
