@@ -168,12 +168,12 @@ struct OpEmitter {
                 switch (op.uop) {
                 case BLZ_FLOOR: e = math("ral_dfloor"); break;
                 case BLZ_CEIL: e = math("ral_dceil"); break;
-                case BLZ_SIN: e = math("sin"); break;
-                case BLZ_COS: e = math("cos"); break;
+                case BLZ_SIN: e = math("ral_dsin"); break;
+                case BLZ_COS: e = math("ral_dcos"); break;
                 case BLZ_ASIN: e = math("asin"); break;
                 case BLZ_ACOS: e = math("acos"); break;
                 case BLZ_TAN: e = math("tan"); break;
-                case BLZ_COTAN: e = conv("ral_ddiv(cos(" + d + "), sin(" + d + "))", Kind::F64, ok); break;
+                case BLZ_COTAN: e = conv("ral_ddiv(ral_dcos(" + d + "), ral_dsin(" + d + "))", Kind::F64, ok); break;
                 case BLZ_ATAN: e = math("atan"); break;
                 case BLZ_ABS: e = math("ral_dfabs"); break;
                 case BLZ_LN: e = math("log"); break;

@@ -58,6 +58,19 @@ RAL_FI bool ral_dne(double a, double b) { return a != b; }
 RAL_FI double ral_f2d(float f) { return (double)f; }
 RAL_FI float ral_d2f(double d) { return __double2float_rn(d); }
 #endif
+// sin / cos: RAL_SOFT_TRIG 1 (the default) evaluates them on the integer pipes (softfp.cuh,
+// within one ulp), 0 with the library functions.  Unlike the exact operations above the two
+// differ in the last bit, so the choice is the same for every kernel of a process.
+#ifndef RAL_SOFT_TRIG
+#define RAL_SOFT_TRIG 1
+#endif
+#if RAL_SOFT_TRIG
+RAL_FI double ral_dsin(double x) { return ral_sf_sin(x); }
+RAL_FI double ral_dcos(double x) { return ral_sf_cos(x); }
+#else
+RAL_FI double ral_dsin(double x) { return sin(x); }
+RAL_FI double ral_dcos(double x) { return cos(x); }
+#endif
 RAL_FI double ral_dfabs(double x) { return ral_sf_fabs(x); }
 RAL_FI bool ral_dzero(double x) { return ral_sf_is_zero(x); }
 RAL_FI double ral_bits_d(ral_i64 b) { return __longlong_as_double(b); }

@@ -42,6 +42,16 @@ uint64_t fnv1a(const std::string& s, uint64_t h = 1469598103934665603ull) {
 // RAL_SOFT_FP=0 selects the hardware FP64 instructions for the operations that otherwise run
 // on the integer pipes (same results; for comparison and diagnosis); kernels whose
 // GeneratedKernel::soft_fp is false always use them
+const std::string& trig_define() {
+    // RAL_SOFT_TRIG=0: the library sin / cos in every kernel (the same choice everywhere, since
+    // the two differ in the last bit)
+    static const std::string d = [] {
+        const char* e = std::getenv("RAL_SOFT_TRIG");
+        return std::string("#define RAL_SOFT_TRIG ") + ((e && std::string(e) == "0") ? "0" : "1") + "\n";
+    }();
+    return d;
+}
+
 const std::string& soft_fp_define(bool soft) {
     static const std::string off = "#define RAL_SOFT_FP 0\n";
     if (!soft) return off;
@@ -57,7 +67,7 @@ const std::string& soft_fp_define(bool soft) {
 }
 
 std::string full_source(const GeneratedKernel& gk) {
-    return soft_fp_define(gk.soft_fp) + std::string(ral_prelude_source) + "\n" + gk.source;
+    return trig_define() + soft_fp_define(gk.soft_fp) + std::string(ral_prelude_source) + "\n" + gk.source;
 }
 
 std::string cache_dir() {

@@ -29,6 +29,12 @@ RAL_FI double st_double(ral_u64 r, ral_u64 r2) {
     default: return (double)__uint_as_float((unsigned)r);
     }
 }
+RAL_FI long long st_ulps(double a, double b) {
+    long long x = __double_as_longlong(a), y = __double_as_longlong(b);
+    x = x < 0 ? -(x & 0x7fffffffffffffffll) : x;
+    y = y < 0 ? -(y & 0x7fffffffffffffffll) : y;
+    return x > y ? x - y : y - x;
+}
 RAL_FI bool st_same(double a, double b) {
     return (a != a && b != b) || __double_as_longlong(a) == __double_as_longlong(b);
 }
@@ -71,6 +77,11 @@ extern "C" __global__ void ral_softfp_selftest(unsigned long long* out, long lon
         if (ib == 0 || ib == -1) ib = 7;
         if (ral_sf_div64(ia, ib) != ia / ib || ral_sf_mod64(ia, ib) != ia % ib)
             st_bad(out, 10, __longlong_as_double(ia), __longlong_as_double(ib));
+        // sin / cos: approximations on both sides, so within 2 ulp of the library's
+        const double t = (r3 & 1) ? a : ldexp((double)(r0 >> 11), -53) * 2e6 * ((r1 & 1) ? -1.0 : 1.0);
+        if (t == t && t - t == 0.0) {
+            if (st_ulps(ral_sf_sin(t), sin(t)) > 2 || st_ulps(ral_sf_cos(t), cos(t)) > 2) st_bad(out, 11, t, 0.0);
+        }
     }
 }
 )RALSRC";

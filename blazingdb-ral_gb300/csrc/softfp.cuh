@@ -480,4 +480,151 @@ RAL_SF long long ral_sf_mod64(long long a, long long b) {
     return a < 0 ? (long long)(0ull - r) : (long long)r;
 }
 
+// ---- sine and cosine ---------------------------------------------------------------------------
+
+// 64-bit value V (a leading one anywhere) times 2^E, rounded to nearest even as a double (normal
+// results only; the callers' values lie in [2^-30, 2])
+RAL_SF double ral_sf_pack(unsigned long long V, int E, unsigned long long sign) {
+    const int lz = ral_sf_clz64(V);
+    V <<= lz;
+    E -= lz;
+    unsigned long long m = V >> 11;
+    const unsigned long long rest = V & 0x7ffull;
+    if (rest > 0x400ull || (rest == 0x400ull && (m & 1u))) m += 1;
+    int be = E + 63 + 1023;
+    if (m == (1ull << 53)) {
+        m >>= 1;
+        be += 1;
+    }
+    return ral_sf_double(sign | ((unsigned long long)be << 52) | (m & RAL_SF_FRAC));
+}
+
+// Fixed-point constants, each the nearest (or, for 2/pi and pi/2, the truncated) value:
+// 2/pi * 2^192 in three words, pi/2 * 2^127 in two words, and 2^63 / n! for the Taylor series
+// sin(r)/r = sum (-1)^n r^(2n) / (2n+1)!  and  cos(r) = sum (-1)^n r^(2n) / (2n)!.
+#define RAL_SF_2PI_W2 0xa2f9836e4e441529ull
+#define RAL_SF_2PI_W1 0xfc2757d1f534ddc0ull
+#define RAL_SF_2PI_W0 0xdb6295993c439041ull
+#define RAL_SF_PI2_HI 0xc90fdaa22168c234ull
+#define RAL_SF_PI2_LO 0xc4c6628b80dc1cd1ull
+
+// sin(|r|) (want_cos false) or cos(|r|) for r = rm * 2^-(64 + sr), rm normalised, |r| <= pi/4
+RAL_SF double ral_sf_sincos_poly(unsigned long long rm, int sr, bool want_cos, unsigned long long sign) {
+    const unsigned long long zz = ral_sf_umulh(rm, rm);  // r^2 * 2^(64 + 2 sr)
+    const unsigned long long z = 2 * sr >= 64 ? 0ull : (zz >> (2 * sr));  // r^2 in Q0.64
+    if (want_cos) {
+        // 2^63 / (2n)!, n = 10 .. 0
+        const unsigned long long c[11] = {0x8000000000000000ull, 0x4000000000000000ull, 0x0555555555555555ull,
+                                          0x002d82d82d82d82eull, 0x0000d00d00d00d01ull, 0x0000024fc9f6ef14ull,
+                                          0x000000047bb63bfeull, 0x00000000064e5d2aull, 0x000000000006b9fdull,
+                                          0x00000000000005a1ull, 0x0000000000000004ull};
+        unsigned long long p = c[10];
+#pragma unroll
+        for (int n = 9; n >= 0; --n) p = c[n] - ral_sf_umulh(p, z);
+        return ral_sf_pack(p, -63, sign);
+    }
+    // 2^63 / (2n+1)!, n = 9 .. 0
+    const unsigned long long c[10] = {0x8000000000000000ull, 0x1555555555555555ull, 0x0111111111111111ull,
+                                      0x0006806806806807ull, 0x0000171de3a556c7ull, 0x00000035cc8acfebull,
+                                      0x000000005849184full, 0x00000000006b9fd0ull, 0x000000000000654bull,
+                                      0x000000000000004cull};
+    unsigned long long p = c[9];
+#pragma unroll
+    for (int n = 8; n >= 0; --n) p = c[n] - ral_sf_umulh(p, z);
+    // sin(r) = r * p: value = umulh(rm, p) * 2^(-63 - sr)
+    return ral_sf_pack(ral_sf_umulh(rm, p), -63 - sr, sign);
+}
+
+RAL_SF double ral_sf_hw_sin(double x) {
+#if defined(__CUDA_ARCH__)
+    return sin(x);
+#else
+    return __builtin_sin(x);
+#endif
+}
+RAL_SF double ral_sf_hw_cos(double x) {
+#if defined(__CUDA_ARCH__)
+    return cos(x);
+#else
+    return __builtin_cos(x);
+#endif
+}
+
+// sin(x) (want_cos false) or cos(x) within one ulp, for 2^-26 <= |x| < 2^20; other inputs use
+// the library functions.  Method: Payne-Hanek-style reduction x * 2/pi = k + f with a 192-bit
+// fixed-point 2/pi (exact product with the 53-bit significand), r = f * pi/2 to 128 bits, then
+// the Taylor series of sin(r)/r or cos(r) in 64-bit fixed point by Horner's rule.
+RAL_SF double ral_sf_sincos(double x, bool want_cos) {
+    const unsigned long long X = ral_sf_bits(x);
+    const int ex = (int)((X >> 52) & 0x7ff);
+    const unsigned long long xsign = X & RAL_SF_SIGN;
+    if (ex < 1023 - 26 || ex >= 1023 + 20) return want_cos ? ral_sf_hw_cos(x) : ral_sf_hw_sin(x);
+    const unsigned long long m = (X & RAL_SF_FRAC) | RAL_SF_IMPL;
+    const int e2 = ex - 1075;  // x = m * 2^e2
+    unsigned long long rm;
+    int sr;
+    unsigned q;
+    bool rneg = false;
+    if ((X & ~RAL_SF_SIGN) < 0x3fe921fb54442d18ull) {  // |x| < pi/4: r = x exactly
+        rm = m << 11;
+        sr = -53 - e2;
+        q = 0;
+    } else {
+        // P = m * (2/pi * 2^192), four words
+        const unsigned long long t0 = m * RAL_SF_2PI_W0, h0 = ral_sf_umulh(m, RAL_SF_2PI_W0);
+        const unsigned long long t1 = m * RAL_SF_2PI_W1, h1 = ral_sf_umulh(m, RAL_SF_2PI_W1);
+        const unsigned long long t2 = m * RAL_SF_2PI_W2, h2 = ral_sf_umulh(m, RAL_SF_2PI_W2);
+        (void)t0;
+        const unsigned long long p1 = h0 + t1;
+        const unsigned long long a1 = p1 < h0 ? 1ull : 0ull;
+        const unsigned long long s2 = h1 + t2;
+        const unsigned long long a2a = s2 < h1 ? 1ull : 0ull;
+        const unsigned long long p2 = s2 + a1;
+        const unsigned long long a2 = a2a + (p2 < s2 ? 1ull : 0ull);
+        const unsigned long long p3 = h2 + a2;
+        // x * 2/pi = P * 2^(e2 - 192): sh = 192 - e2 fraction bits, v = sh - 192 in [33, 53]
+        const int v = -e2;
+        unsigned long long k = p3 >> v;
+        unsigned long long fhi = (p2 >> v) | (p3 << (64 - v));
+        unsigned long long flo = (p1 >> v) | (p2 << (64 - v));
+        if (fhi >> 63) {  // f >= 1/2: the nearer quadrant is k + 1, and r = (f - 1) pi/2 < 0
+            k += 1;
+            flo = 0ull - flo;
+            fhi = ~fhi + (flo == 0 ? 1ull : 0ull);
+            rneg = true;
+        }
+        q = (unsigned)(k & 3u);
+        // r = f * pi/2 in Q0.128: (f * pi2) >> 127, from the three high partial products
+        const unsigned long long ac_lo = fhi * RAL_SF_PI2_HI, ac_hi = ral_sf_umulh(fhi, RAL_SF_PI2_HI);
+        const unsigned long long ad = ral_sf_umulh(fhi, RAL_SF_PI2_LO), bc = ral_sf_umulh(flo, RAL_SF_PI2_HI);
+        unsigned long long lo = ac_lo + ad;
+        unsigned long long hi = ac_hi + (lo < ac_lo ? 1ull : 0ull);
+        const unsigned long long lo2 = lo + bc;
+        hi += lo2 < lo ? 1ull : 0ull;
+        lo = lo2;
+        const unsigned long long rhi = (hi << 1) | (lo >> 63), rlo = lo << 1;
+        if (rhi != 0) {
+            const int lz = ral_sf_clz64(rhi);
+            rm = lz ? ((rhi << lz) | (rlo >> (64 - lz))) : rhi;
+            sr = lz;
+        } else {
+            if (rlo == 0) return want_cos ? ral_sf_hw_cos(x) : ral_sf_hw_sin(x);
+            const int lz = ral_sf_clz64(rlo);
+            rm = rlo << lz;
+            sr = 64 + lz;
+        }
+    }
+    // quadrant: sin(x) = [s, c, -s, -c][q], cos(x) = [c, -s, -c, s][q] with s = sin r, c = cos r
+    const bool use_cos = want_cos ? (q & 1u) == 0 : (q & 1u) == 1;
+    bool neg;
+    if (want_cos) neg = (q == 1 || q == 2);
+    else neg = (q >= 2);
+    if (!use_cos && rneg) neg = !neg;               // sin(-|r|) = -sin|r|
+    if (!want_cos && xsign) neg = !neg;             // sin(-x) = -sin x; cos is even
+    return ral_sf_sincos_poly(rm, sr, use_cos, neg ? RAL_SF_SIGN : 0ull);
+}
+
+RAL_SF double ral_sf_sin(double x) { return ral_sf_sincos(x, false); }
+RAL_SF double ral_sf_cos(double x) { return ral_sf_sincos(x, true); }
+
 #endif  // RAL_SOFTFP_CUH_

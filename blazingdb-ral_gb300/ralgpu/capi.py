@@ -605,7 +605,7 @@ class Server:
             pass
 
 
-SOFTFP_OPS = ["div", "floor", "ceil", "compare", "i2d", "d2i", "f2d", "d2f", "is_zero", "fabs", "div64"]
+SOFTFP_OPS = ["div", "floor", "ceil", "compare", "i2d", "d2i", "f2d", "d2f", "is_zero", "fabs", "div64", "sincos"]
 
 
 def softfp_selftest(n: int = 1 << 24, seed: int = 1) -> dict:

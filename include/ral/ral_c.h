@@ -323,8 +323,8 @@ int ral_server_destroy(ral_server *server);
  * Device self-test of the integer-pipe double operations against the GPU's FP64 instructions
  * (no reference counterpart): n random operand sets from seed; mismatches[16] receives the
  * mismatch count of each operation (0 div, 1 floor, 2 ceil, 3 compares, 4 int64->double,
- * 5 double->int64, 6 float->double, 7 double->float, 8 == 0, 9 fabs, 10 int64 / and %) and
- * first_operands[32]
+ * 5 double->int64, 6 float->double, 7 double->float, 8 == 0, 9 fabs, 10 int64 / and %,
+ * 11 sin / cos beyond 2 ulp of the library's) and first_operands[32]
  * the bits of each operation's first mismatching operands.
  */
 int ral_softfp_selftest(int64_t n, uint64_t seed, int64_t *mismatches, uint64_t *first_operands);

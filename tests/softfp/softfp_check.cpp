@@ -16,6 +16,13 @@ static double dbl(uint64_t b) { double d; std::memcpy(&d, &b, 8); return d; }
 static uint32_t fbits(float f) { uint32_t b; std::memcpy(&b, &f, 4); return b; }
 static float flt(uint32_t b) { float f; std::memcpy(&f, &b, 4); return f; }
 
+// distance in units in the last place (finite doubles)
+static long long ulps(double a, double b) {
+    auto ord = [](double d) { long long v; std::memcpy(&v, &d, 8); return v < 0 ? -(v & 0x7fffffffffffffffll) : v; };
+    const long long d = ord(a) - ord(b);
+    return d < 0 ? -d : d;
+}
+
 // same value, or both NaN
 static bool same_d(double a, double b) { return (std::isnan(a) && std::isnan(b)) || bits(a) == bits(b); }
 static bool same_f(float a, float b) { return (std::isnan(a) && std::isnan(b)) || fbits(a) == fbits(b); }
@@ -77,6 +84,15 @@ int main(int argc, char** argv) {
         ral_sf_udivmod64_32(n, d, &q, &r);
         if ((q != n / d || r != n % d) && cd32.bad++ == 0)
             std::snprintf(cd32.first, sizeof cd32.first, "%llu / %u: want %llu %llu got %llu %llu", n, d, n / d, n % d, q, r);
+    };
+    // sin / cos: within one ulp of the host's libm (which is within one ulp of the exact value)
+    Counter csin{"sincos"};
+    auto check_trig = [&](double x) {
+        csin.n++;
+        const long long a = ulps(std::sin(x), ral_sf_sin(x)), b = ulps(std::cos(x), ral_sf_cos(x));
+        const bool nan_ok = std::isnan(x) ? (std::isnan(ral_sf_sin(x)) && std::isnan(ral_sf_cos(x))) : true;
+        if ((!nan_ok || (!std::isnan(x) && !std::isinf(x) && (a > 1 || b > 1))) && csin.bad++ == 0)
+            std::snprintf(csin.first, sizeof csin.first, "%a: sin %lld ulp, cos %lld ulp", x, a, b);
     };
     Counter cdiv{"div"}, cfloor{"floor"}, cceil{"ceil"}, cabs{"fabs"}, ccmp{"compare"}, ci2d{"i2d"}, cd2i{"d2i"},
         cf2d{"f2d"}, cd2f{"d2f"}, czero{"is_zero"};
@@ -148,6 +164,14 @@ int main(int argc, char** argv) {
         xb = (long long)(1ull << (rng() % 63)) + (long long)(rng() % 3) - 1;
         check_div64(xa, xb);
         check_div64(INT64_MIN, xb);
+        check_trig(a);
+        check_trig(std::ldexp((double)(rng() >> 11), -53) * 2e6 * ((rng() & 1) ? -1 : 1));
+        check_trig(std::ldexp(1.0 + (double)(rng() >> 11) * 0x1p-53, (int)(rng() % 50) - 28));
+        // next to multiples of pi/2, where the reduced argument is smallest
+        const double kpi2 = (double)(long long)(rng() % 600000) * 1.5707963267948966;
+        check_trig(std::nextafter(kpi2, 0.0));
+        check_trig(kpi2);
+        check_trig(std::nextafter(kpi2, 1e300));
         check_d32(rng() >> (rng() % 64), (unsigned)(rng() >> (32 + rng() % 32)));
         check_d32(rng(), (unsigned)(1 + rng() % 1000));
         check_d32(rng(), 0xffffffffu - (unsigned)(rng() % 3));
@@ -164,6 +188,10 @@ int main(int argc, char** argv) {
         if (!same_d((double)x, ral_sf_i2d(x)) && ci2d.bad++ == 0)
             std::snprintf(ci2d.first, sizeof ci2d.first, "%lld", x);
     }
-    for (Counter* c : {&cd32, &cdiv64, &cdiv, &cfloor, &cceil, &cabs, &ccmp, &ci2d, &cd2i, &cf2d, &cd2f, &czero}) c->report();
+    for (double v : sp) check_trig(v);
+    for (double v : {0.7853981633974483, 0.7853981633974482, 0.7853981633974484, 0x1p-26, 0x1p-27, 0x1p20,
+                     0x1.fffffffffffffp19, 3.141592653589793, 1.5707963267948966, 1e6, -1e6})
+        check_trig(v);
+    for (Counter* c : {&csin, &cd32, &cdiv64, &cdiv, &cfloor, &cceil, &cabs, &ccmp, &ci2d, &cd2i, &cf2d, &cd2f, &czero}) c->report();
     return 0;
 }
