@@ -43,11 +43,11 @@ uint64_t fnv1a(const std::string& s, uint64_t h = 1469598103934665603ull) {
 // on the integer pipes (same results; for comparison and diagnosis); kernels whose
 // GeneratedKernel::soft_fp is false always use them
 const std::string& trig_define() {
-    // RAL_SOFT_TRIG=0: the library sin / cos in every kernel (the same choice everywhere, since
-    // the two differ in the last bit)
+    // RAL_SOFT_TRIG=1: the integer-pipe sin / cos in every kernel (the same choice everywhere,
+    // since the two differ in the last bit)
     static const std::string d = [] {
         const char* e = std::getenv("RAL_SOFT_TRIG");
-        return std::string("#define RAL_SOFT_TRIG ") + ((e && std::string(e) == "0") ? "0" : "1") + "\n";
+        return std::string("#define RAL_SOFT_TRIG ") + ((e && std::string(e) == "1") ? "1" : "0") + "\n";
     }();
     return d;
 }
