@@ -9,6 +9,7 @@
 
 #include <algorithm>
 #include <chrono>
+#include <cstdlib>
 #include <cstring>
 
 #include "batch.h"
@@ -68,6 +69,9 @@ Server::Server(size_t budget_bytes, int max_waves, int max_wave_requests, int64_
     : budget_(budget_bytes), max_waves_(std::max(1, std::min(max_waves, 8))),
       max_wave_requests_(std::max(1, std::min(max_wave_requests, 4096))) {
     wave_rows_ = wave_rows > 0 ? wave_rows : ((int64_t)32 << 20);
+    // RAL_SERVER_SLICE_DIV: a request takes at most wave_rows / this of one wave (default 4)
+    const char* sd = std::getenv("RAL_SERVER_SLICE_DIV");
+    slice_div_ = sd && std::atoi(sd) >= 1 && std::atoi(sd) <= 64 ? std::atoi(sd) : 4;
     t0_ = 0;
     t0_ = now();
 }
@@ -329,7 +333,8 @@ int Server::launch_wave(Wave& w, const std::vector<int64_t>& reqs, const std::ve
     int a_np = NP;
     unsigned int* a_counter = (unsigned int*)(d + off_counter);
     long long a_total = total;
-    void* args[] = {&a_descs, &a_stride, &a_prefix, &a_base, &a_fn, &a_np, &a_counter, &a_total};
+    const void* a_list = nullptr;  // chunks of a request must run in order: no item list
+    void* args[] = {&a_descs, &a_stride, &a_prefix, &a_base, &a_fn, &a_np, &a_counter, &a_total, &a_list};
     const int grid = (int)std::max<long long>(1, std::min<long long>(grid_, (total + 7) / 8));
     const size_t smem = batch_dispatch_smem(NP, smem_words_);
     if (total > 0) {
@@ -453,7 +458,7 @@ void Server::loop() {
                 cand.push_back({left - (tnow - r.t_submit) * kAgeRowsPerSecond, id});
             }
             std::sort(cand.begin(), cand.end());
-            const int64_t slice = std::max<int64_t>(1, wave_rows_ / 4);
+            const int64_t slice = std::max<int64_t>(1, wave_rows_ / slice_div_);
             int64_t rows = 0;
             for (auto& c : cand) {
                 if ((int)reqs.size() >= max_wave_requests_ || rows >= wave_rows_) break;

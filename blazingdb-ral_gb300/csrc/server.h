@@ -133,6 +133,7 @@ private:
     std::deque<int64_t> pending_;      // submitted, not admitted (FIFO)
     std::vector<int64_t> active_;      // admitted, not finished
     int64_t wave_rows_ = 0;
+    int slice_div_ = 4;
     std::unordered_map<int64_t, std::unique_ptr<ServerRequest>> requests_;
     int64_t next_id_ = 1;
     size_t reserved_ = 0;
