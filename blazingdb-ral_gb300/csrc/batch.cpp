@@ -15,7 +15,6 @@
 #include <cstdlib>
 #include <fstream>
 #include <map>
-#include <queue>
 #include <mutex>
 #include <sstream>
 #include <thread>
@@ -91,11 +90,6 @@ int64_t bucket(int64_t x) {
     return b;
 }
 
-bool interleave_items() {
-    const char* e = std::getenv("RAL_BATCH_INTERLEAVE");
-    return !(e && std::string(e) == "0");
-}
-
 }  // namespace
 
 int compile_items(const std::vector<GeneratedKernel>& items, std::vector<const std::vector<char>*>& objects,
@@ -168,7 +162,6 @@ Batch::~Batch() {
     if (d_descs_) cudaFree(d_descs_);
     if (d_prefix_) cudaFree(d_prefix_);
     if (d_fn_) cudaFree(d_fn_);
-    if (d_items_) cudaFree(d_items_);
     if (d_counter_) cudaFree(d_counter_);
 }
 
@@ -291,31 +284,6 @@ int Batch::prepare(cudaStream_t st) {
     cudaMemcpyAsync(d_fn_, fn.data(), fn.size() * sizeof(int), cudaMemcpyHostToDevice, st);
     if (int e = check_cuda(cudaStreamSynchronize(st), "batch upload")) return e;
     smem_ = batch_dispatch_smem(NP, 0);
-    // Interleaved work items (RAL_BATCH_INTERLEAVE, default on): every program's tiles spread
-    // evenly over the item sequence (merged by fractional position (t + 1/2) / tiles), so that
-    // memory-bound and FP64-bound programs run side by side instead of one after another.
-    if (interleave_items()) {
-        std::vector<uint64_t> order;
-        order.reserve((size_t)total_items_);
-        struct Head { double key; int q; long long t; };
-        auto later = [](const Head& a, const Head& b) { return a.key > b.key; };
-        std::priority_queue<Head, std::vector<Head>, decltype(later)> pq(later);
-        for (int q = 0; q < NP; q++)
-            if (entries_[q]->items > 0) pq.push({0.5 / (double)entries_[q]->items, q, 0});
-        while (!pq.empty()) {
-            Head h = pq.top();
-            pq.pop();
-            order.push_back(((uint64_t)h.q << 40) | (uint64_t)h.t);
-            if (++h.t < entries_[h.q]->items) {
-                h.key = ((double)h.t + 0.5) / (double)entries_[h.q]->items;
-                pq.push(h);
-            }
-        }
-        if (int e = check_cuda(cudaMalloc(&d_items_, order.size() * 8), "cudaMalloc")) return e;
-        if (int e = check_cuda(cudaMemcpy(d_items_, order.data(), order.size() * 8, cudaMemcpyHostToDevice),
-                               "item list upload"))
-            return e;
-    }
     if (smem_ > 48 * 1024 &&
         check_cuda(cudaFuncSetAttribute((const void*)kernel_->kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_),
                    "cudaFuncSetAttribute"))
@@ -387,9 +355,8 @@ int Batch::launch(cudaStream_t st) {
     long long total = total_items_;
     const void* fn = d_fn_;
     const void* base = nullptr;
-    const void* list = d_items_;
     int stride = stride_;
-    void* args[] = {&descs, &stride, &prefix, &base, &fn, &np, &counter, &total, &list};
+    void* args[] = {&descs, &stride, &prefix, &base, &fn, &np, &counter, &total};
     return check_cuda(cudaLaunchKernel((const void*)kernel_->kernel, dim3(grid_), dim3(256), args, smem_, st),
                       "launch of the batch kernel");
 }

@@ -53,7 +53,6 @@ private:
     void* d_descs_ = nullptr;
     void* d_prefix_ = nullptr;
     void* d_fn_ = nullptr;
-    void* d_items_ = nullptr;  // interleaved (program << 40 | tile) list, or null
     unsigned int* d_counter_ = nullptr;
     int64_t total_items_ = 0;
     int grid_ = 0;

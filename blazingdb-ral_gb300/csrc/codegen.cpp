@@ -1059,7 +1059,7 @@ GeneratedKernel generate_batch_dispatch(const std::vector<DispatchEntry>& items,
     os << "extern \"C\" __global__ void __launch_bounds__(256) " << gk.name
        << "(const ral_u64* __restrict__ descs, const int stride, const long long* __restrict__ item_prefix, "
           "const long long* __restrict__ item_base, const int* __restrict__ fn_index, const int np, "
-          "unsigned int* counter, const long long total_items, const ral_u64* __restrict__ item_list) {\n";
+          "unsigned int* counter, const long long total_items) {\n";
     os << "    extern __shared__ long long s_prefix[];\n";
     os << "    long long* s_base = s_prefix + np + 1;\n";
     os << "    int* s_fn = reinterpret_cast<int*>(s_base + np);\n";
@@ -1082,21 +1082,12 @@ GeneratedKernel generate_batch_dispatch(const std::vector<DispatchEntry>& items,
     os << "        const long long last = first + RAL_BATCH_GRAB < total_items ? first + RAL_BATCH_GRAB : total_items;\n";
     os << "        int lo = 0;\n";
     os << "        for (long long item = first; item < last; ++item) {\n";
-    os << "            ral_i64 t;\n";
-    // with an item list, entry i names (program << 40 | tile) directly (any order of the items);
-    // otherwise items run in program order: largest q with s_prefix[q] <= item, and since the
-    // items of one grab are consecutive the search starts from the last q
-    os << "            if (item_list) {\n";
-    os << "                const ral_u64 e = item_list[item];\n";
-    os << "                lo = (int)(e >> 40);\n";
-    os << "                t = (ral_i64)(e & 0xffffffffffull) + s_base[lo];\n";
-    os << "            } else {\n";
-    os << "                if (s_prefix[lo + 1] <= item) {\n";
-    os << "                    int hi = np;\n";
-    os << "                    while (hi - lo > 1) { const int mid = (lo + hi) >> 1; if (s_prefix[mid] <= item) lo = mid; else hi = mid; }\n";
-    os << "                }\n";
-    os << "                t = item - s_prefix[lo] + s_base[lo];\n";
+    // largest q with s_prefix[q] <= item; items of one grab are consecutive, so start from the last q
+    os << "            if (s_prefix[lo + 1] <= item) {\n";
+    os << "                int hi = np;\n";
+    os << "                while (hi - lo > 1) { const int mid = (lo + hi) >> 1; if (s_prefix[mid] <= item) lo = mid; else hi = mid; }\n";
     os << "            }\n";
+    os << "            const ral_i64 t = item - s_prefix[lo] + s_base[lo];\n";
     os << "            const ral_u64* slots = descs + (size_t)lo * stride;\n";
     os << "            switch (s_fn[lo]) {\n";
     for (int f = 0; f < NF; f++)

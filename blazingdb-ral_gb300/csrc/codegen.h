@@ -71,12 +71,12 @@ struct GeneratedKernel {
 // work items (program, tile) from a device counter in chunks, finds the program by binary search
 // over the item prefix (in shared memory) and calls its function:
 //   <name>(const ral_u64* descs, int stride, const long long* item_prefix, const long long* item_base,
-//          const int* fn_index, int n_programs, unsigned int* counter, long long total_items,
-//          const ral_u64* item_list)
+//          const int* fn_index, int n_programs, unsigned int* counter, long long total_items)
 // descs holds `stride` slots per program; fn_index[q] indexes the item functions; item t of
 // program q runs tile item_base[q] + t (item_base may be null: all 0), so a request's chunks can
-// be spread over several launches.  item_list (may be null) lists the items as (q << 40 | t) in
-// any order; without it they run in program order.
+// be spread over several launches.  Items run in program order: interleaving the programs' tiles
+// (tried: every program's tiles spread evenly over the sequence) made the 256-program batch 14x
+// slower, each warp's consecutive items then touching different code and different tables.
 // Filter + project requests are batched the same way: their item function is the fused filter
 // kernel's chunk body (generate_filter_kernel with item = true),
 //   extern "C" __device__ void <name>(const ral_u64* slots, long long chunk, unsigned* warp_smem)

@@ -69,9 +69,10 @@ Server::Server(size_t budget_bytes, int max_waves, int max_wave_requests, int64_
     : budget_(budget_bytes), max_waves_(std::max(1, std::min(max_waves, 8))),
       max_wave_requests_(std::max(1, std::min(max_wave_requests, 4096))) {
     wave_rows_ = wave_rows > 0 ? wave_rows : ((int64_t)32 << 20);
-    // RAL_SERVER_SLICE_DIV: a request takes at most wave_rows / this of one wave (default 4)
+    // RAL_SERVER_SLICE_DIV: a request takes at most wave_rows / this of one wave (default 2;
+    // measured at 90% load: 4 gives p50 / p99 3.6 / 41.6 ms, 1 gives 6.3 / 31.3 ms)
     const char* sd = std::getenv("RAL_SERVER_SLICE_DIV");
-    slice_div_ = sd && std::atoi(sd) >= 1 && std::atoi(sd) <= 64 ? std::atoi(sd) : 4;
+    slice_div_ = sd && std::atoi(sd) >= 1 && std::atoi(sd) <= 64 ? std::atoi(sd) : 2;
     t0_ = 0;
     t0_ = now();
 }
@@ -333,8 +334,7 @@ int Server::launch_wave(Wave& w, const std::vector<int64_t>& reqs, const std::ve
     int a_np = NP;
     unsigned int* a_counter = (unsigned int*)(d + off_counter);
     long long a_total = total;
-    const void* a_list = nullptr;  // chunks of a request must run in order: no item list
-    void* args[] = {&a_descs, &a_stride, &a_prefix, &a_base, &a_fn, &a_np, &a_counter, &a_total, &a_list};
+    void* args[] = {&a_descs, &a_stride, &a_prefix, &a_base, &a_fn, &a_np, &a_counter, &a_total};
     const int grid = (int)std::max<long long>(1, std::min<long long>(grid_, (total + 7) / 8));
     const size_t smem = batch_dispatch_smem(NP, smem_words_);
     if (total > 0) {

@@ -7,7 +7,7 @@
 // waves: one launch of the persistent dispatcher whose warps pull (request, chunk) work items.
 // A wave carries about wave_rows rows.  Admitted requests not already in flight enter it in
 // order of fewest rows left, less a credit that grows with the time they have waited, each
-// with at most a quarter of the wave; a large request is sliced over several waves (its
+// with at most half of the wave; a large request is sliced over several waves (its
 // look-back status words stay in its scratch between them).  So requests that arrive while a
 // large one runs finish within a wave or two instead of waiting for it, and large requests
 // keep advancing instead of starving under a stream of small ones.  Up to max_waves waves are in flight on their own
@@ -133,7 +133,7 @@ private:
     std::deque<int64_t> pending_;      // submitted, not admitted (FIFO)
     std::vector<int64_t> active_;      // admitted, not finished
     int64_t wave_rows_ = 0;
-    int slice_div_ = 4;
+    int slice_div_ = 2;
     std::unordered_map<int64_t, std::unique_ptr<ServerRequest>> requests_;
     int64_t next_id_ = 1;
     size_t reserved_ = 0;
