@@ -92,6 +92,13 @@ int64_t bucket(int64_t x) {
 
 }  // namespace
 
+// RAL_BATCH_GRAB: consecutive work items a warp takes per atomic (default 8)
+int batch_grab() {
+    const char* e = std::getenv("RAL_BATCH_GRAB");
+    const int v = e ? std::atoi(e) : 0;
+    return v >= 1 && v <= 64 ? v : 8;
+}
+
 int compile_items(const std::vector<GeneratedKernel>& items, std::vector<const std::vector<char>*>& objects,
                   std::string* logs) {
     const size_t n = items.size();
@@ -240,7 +247,7 @@ int Batch::prepare(cudaStream_t st) {
     }
     std::vector<DispatchEntry> names;
     for (const auto& it : items) names.push_back({it.name, false});
-    GeneratedKernel disp = generate_batch_dispatch(names, 0);
+    GeneratedKernel disp = generate_batch_dispatch(names, 0, batch_grab());
     items.push_back(disp);
     std::vector<const std::vector<char>*> objects;
     if (int e = compile_items(items, objects, nullptr)) return e;
@@ -301,7 +308,7 @@ int Batch::prepare(cudaStream_t st) {
     if (cudaFuncGetAttributes(&fa, (const void*)kernel_->kernel) == cudaSuccess) registers_ = fa.numRegs;
     else cudaGetLastError();
     grid_ = std::max(1, sms * std::max(1, per_sm));
-    const int64_t warps_needed = (total_items_ + 7) / 8;
+    const int64_t warps_needed = (total_items_ + batch_grab() - 1) / batch_grab();
     grid_ = (int)std::max<int64_t>(1, std::min<int64_t>(grid_, (warps_needed + 7) / 8));
 
     // capture the launch (counter reset + kernel) once
@@ -332,7 +339,7 @@ int Batch::debug_source(bool compile, std::string& source, std::string& log) con
     }
     std::vector<DispatchEntry> names;
     for (const auto& it : items) names.push_back({it.name, false});
-    items.push_back(generate_batch_dispatch(names, 0));
+    items.push_back(generate_batch_dispatch(names, 0, batch_grab()));
     source.clear();
     for (const auto& it : items) source += "// ---- " + it.name + "\n" + it.source + "\n";
     if (compile) {

@@ -562,7 +562,7 @@ int ral_autotune_program(gdf_column* const* output_columns, int32_t num_outputs,
                 sh.unroll = c.U;
                 sh.soft = c.S;
                 tus.push_back(generate_batch_item(p, sh));
-                tus.push_back(generate_batch_dispatch({{tus.back().name, false}}, 0));
+                tus.push_back(generate_batch_dispatch({{tus.back().name, false}}, 0, batch_grab()));
             }
             std::vector<const std::vector<char>*> objs;
             if (int e = compile_items(tus, objs, nullptr)) return e;
