@@ -107,13 +107,14 @@ double work_estimate(const BatchEntry& e) {
     return per_row * (double)e.rows;
 }
 
-// RAL_BATCH_GRAB: consecutive work items a warp takes per atomic (default 2: measured 122 ms
-// against 125 / 131 / 159 ms at 4 / 8 / 32 on the 256-program mix, and 15.7 ms against 17.1 /
-// 24.0 / 70.6 with tables capped at 1M rows -- smaller grabs end the launch more evenly)
+// RAL_BATCH_GRAB: consecutive work items a warp takes per atomic (default 1: measured 121 ms
+// against 122 / 124 / 131 / 159 ms at 2 / 4 / 8 / 32 on the 256-program mix, and 15.0 ms against
+// 15.9 / 18.0 / 24.0 / 70.6 with tables capped at 1M rows -- smaller grabs end the launch more
+// evenly, and one atomic per warp tile is far below the counter's rate)
 int batch_grab() {
     const char* e = std::getenv("RAL_BATCH_GRAB");
     const int v = e ? std::atoi(e) : 0;
-    return v >= 1 && v <= 64 ? v : 2;
+    return v >= 1 && v <= 64 ? v : 1;
 }
 
 int compile_items(const std::vector<GeneratedKernel>& items, std::vector<const std::vector<char>*>& objects,

@@ -74,7 +74,7 @@ Shape tuned_shape(const Program& p, int G);
 void record_tuned_shape(const Program& p, int G, int J, int U, bool soft, double ms);
 std::string tune_key(const Program& p, int G);
 
-// Consecutive work items a batch warp takes per atomic (RAL_BATCH_GRAB, default 2).
+// Consecutive work items a batch warp takes per atomic (RAL_BATCH_GRAB, default 1).
 int batch_grab();
 
 // Compiles generated relocatable TUs on a pool of host threads (cached per name); appends the
