@@ -554,6 +554,47 @@ def batched_setup(n_programs, seed, device, max_rows=0):
     return progs, alg
 
 
+def batched_capped(R, progs, cap, stream, plain_steps):
+    """Batched vs plain calls for the same programs over the first `cap` rows of every table."""
+    import torch
+    views = []
+    for p in progs:
+        n = min(p["rows"], cap)
+        ins = [R.Column(c.data[:n], c.valid, c.dtype, n, c.null_count) for c in p["ins"]]
+        outs = [R.Column(c.data[:n], c.valid, c.dtype, n) for c in p["outs"]]
+        views.append((ins, outs, p["args"], n))
+    rows = sum(v[3] for v in views)
+    b = R.Batch()
+    for ins, outs, a, n in views:
+        b.add(outs, ins, *a)
+    b.prepare()
+    for _ in range(3):
+        b.run(stream)
+    torch.cuda.synchronize()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(5)]
+    for s_, e_ in ev:
+        s_.record(stream)
+        b.run(stream)
+        e_.record(stream)
+    torch.cuda.synchronize()
+    bms = statistics.mean(s_.elapsed_time(e_) for s_, e_ in ev)
+    b.close()
+    for ins, outs, a, n in views:
+        R.perform_operation(outs, ins, *a)
+    torch.cuda.synchronize()
+    times = []
+    for _ in range(plain_steps):
+        t0 = time.perf_counter()
+        for ins, outs, a, n in views:
+            R.perform_operation(outs, ins, *a)
+        torch.cuda.synchronize()
+        times.append(time.perf_counter() - t0)
+    pms = statistics.median(times) * 1e3
+    return {"cap_rows": cap, "rows": rows, "batched_ms": bms, "plain_ms": pms,
+            "batched_rows_per_s": rows / (bms / 1e3), "plain_rows_per_s": rows / (pms / 1e3),
+            "speedup_vs_plain": pms / bms}
+
+
 def run_batched(args):
     import concurrent.futures as cf
     import torch
@@ -632,6 +673,12 @@ def run_batched(args):
                  "timing": "host clock around synchronous ral_perform_operation calls, one per program",
                  "first_compile_s": round(plain_compile_s, 2)}
 
+    # the same 256 programs over the first cap rows of each table (views of the same columns):
+    # where per-call cost, not the FP64 work of the few largest tables, decides
+    capped = None
+    if args.plain_steps > 0 and args.capped_rows > 0:
+        capped = batched_capped(R, progs, args.capped_rows, stream, args.plain_steps)
+
     peak, peak_kind = load_peaks()
     achieved = alg / (ms_per_step / 1e3) / 1e9
     out = {
@@ -650,6 +697,7 @@ def run_batched(args):
                     "generate_s": round(gen_s, 2)},
         "plain_per_call": plain,
         "speedup_vs_plain": value / plain["value"] if plain else None,
+        "capped_tables": capped,
         "hbm_gbs": achieved,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "peak_kind": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else peak_kind,
@@ -873,6 +921,8 @@ def main():
     ap.add_argument("--plain-steps", type=int, default=3)
     ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--max-rows", type=int, default=0, help="batched: cap every table (profiling captures)")
+    ap.add_argument("--capped-rows", type=int, default=1_000_000,
+                    help="batched: also compare batch and plain calls over the first N rows of every table")
     ap.add_argument("--selectivity", type=float, default=0.5)
     ap.add_argument("--rows", type=int, default=0)
     ap.add_argument("--skip-e2e", action="store_true")
