@@ -575,11 +575,11 @@ GeneratedKernel generate_filter_kernel(const FilterSpec& f, const Shape& s, bool
     key << "|O";
     for (const FilterOutput& o : f.outputs) key << (o.from_project ? "p" : "g") << o.index << ":" << (int)o.dtype << (o.has_valid ? "v" : "") << ",";
     key << "|G" << s.G << "J" << s.J << "T" << s.threads << "B" << s.min_blocks << "U" << s.unroll << "S" << s.stage;
-    if (item) key << "|item";
+    if (item) key << "|item" << (s.soft ? "s" : "");
     char hex[32];
     snprintf(hex, sizeof hex, "%016llx", (unsigned long long)fnv1a(key.str()));
     gk.name = std::string(item ? "ral_fitem_" : "ral_filter_") + hex;
-    gk.soft_fp = !item;
+    gk.soft_fp = item ? s.soft : true;
 
     std::ostringstream os;
     os << "// generated: " << key.str() << "\n";

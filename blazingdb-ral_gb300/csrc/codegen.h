@@ -57,10 +57,11 @@ struct GeneratedKernel {
     int item_smem_words = 0;
     // integer-pipe double operations (softfp.cuh) unless RAL_SOFT_FP=0.  Batched item functions
     // take it from their shape (the autotuner's choice; by default the FP64 instructions, since
-    // under the items' 64-register cap the larger integer-pipe code spills: 256 programs over
-    // tables capped at 1M rows ran 31.6 ms with it against 20.4 ms without); served chunk
-    // functions use the FP64 instructions.
+    // under the items' register cap the larger integer-pipe code spills: 256 programs over tables
+    // capped at 1M rows ran 31.6 ms with it against 20.4 ms without).
     bool soft_fp = true;
+    // relocatable item functions: register cap (0: RAL_BATCH_MAXRREG's)
+    int max_registers = 0;
 };
 
 // Batched and served launches run many programs in one persistent kernel.  Each program's warp

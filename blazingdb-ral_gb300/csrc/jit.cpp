@@ -119,7 +119,7 @@ bool compile(const GeneratedKernel& gk, std::vector<char>& cubin, std::string& l
         opts.push_back("--relocatable-device-code=true");
         // item functions are compiled apart from the kernel that calls them, so launch bounds do
         // not reach them: cap their registers so the linked kernel keeps its occupancy
-        maxreg = "--maxrregcount=" + std::to_string(relocatable_max_registers());
+        maxreg = "--maxrregcount=" + std::to_string(gk.max_registers > 0 ? gk.max_registers : relocatable_max_registers());
         opts.push_back(maxreg.c_str());
     }
     rc = nvrtcCompileProgram(prog, (int)opts.size(), opts.data());
@@ -277,7 +277,8 @@ const std::vector<char>* jit_object(const GeneratedKernel& gk, std::string& err,
     }
     auto obj = std::make_unique<std::vector<char>>();
     const std::string dir = cache_dir();
-    const std::string path = dir + "/" + disk_key(gk) + ".r" + std::to_string(relocatable_max_registers()) + ".rdc";
+    const std::string path = dir + "/" + disk_key(gk) + ".r" +
+                             std::to_string(gk.max_registers > 0 ? gk.max_registers : relocatable_max_registers()) + ".rdc";
     bool from_disk = false;
     {
         std::ifstream f(path, std::ios::binary);

@@ -25,16 +25,30 @@ size_t round_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
 // fewer left (about the rows the GPU scans in that time), so that large requests are not starved.
 constexpr double kAgeRowsPerSecond = 1e10;
 
-// Item shape of a query: vector width from the widest column, 1024-row chunks at G = 2.
+// Item shape of a query: vector width from the widest column, chunks of RAL_SERVER_CHUNK rows
+// (default 2048, the single-launch filter's), predicate unroll 2 and the integer-pipe double
+// operations (RAL_SERVER_SOFT_FP, default on) as in the single-launch filter + project kernel.
 Shape query_shape(const FilterPlan& plan, bool aligned16) {
     Shape sh;
     sh.G = aligned16 ? 16 / filter_max_width(plan.spec) : 1;
-    sh.J = std::max(1, 32 / sh.G);
+    const char* c = std::getenv("RAL_SERVER_CHUNK");
+    const int rows = c && std::atoi(c) >= 32 && std::atoi(c) <= 8192 ? std::atoi(c) : 2048;
+    sh.J = std::max(1, rows / (32 * sh.G));
     sh.threads = 256;
     sh.min_blocks = 1;
-    sh.unroll = 4;
+    sh.unroll = 2;
     sh.stage = false;
+    const char* f = std::getenv("RAL_SERVER_SOFT_FP");
+    sh.soft = !(f && std::string(f) == "0");
     return sh;
+}
+
+// Register cap of the served chunk functions (RAL_SERVER_MAXRREG, default 64: four blocks per
+// SM, as the single-launch filter + project kernel runs fastest).
+int server_max_registers() {
+    const char* e = std::getenv("RAL_SERVER_MAXRREG");
+    const int v = e ? std::atoi(e) : 0;
+    return v >= 32 && v <= 255 ? v : 64;
 }
 
 // Layout of one request's allocation: scratch | output masks | output data (each 256-aligned),
@@ -129,6 +143,7 @@ int Server::add_query(int table_id, const char* filter_q, const char* project_q,
     if (int e = plan_filter_project(frame.data(), (int)frame.size(), filter_q, project_q, q->plan)) return e;
     const Shape sh = query_shape(*q->plan, al);
     q->item = generate_filter_kernel(q->plan->spec, sh, true);
+    q->item.max_registers = server_max_registers();
     // at least one chunk, so that an empty table's request still runs (and finishes) once
     q->chunks = std::max<int64_t>(1, (t.rows + filter_tile_rows(sh) - 1) / filter_tile_rows(sh));
     q->reserve = request_layout(*q, t.rows).total;
@@ -164,6 +179,7 @@ int Server::ensure_linked() {
         smem = std::max(smem, queries_[i]->item.item_smem_words);
     }
     GeneratedKernel disp = generate_batch_dispatch(entries, smem, 1);
+    disp.max_registers = server_max_registers();
     tus.push_back(disp);
     std::vector<const std::vector<char>*> objs;
     if (int e = compile_items(tus, objs, nullptr)) return e;
@@ -225,6 +241,7 @@ int Server::debug_compile(std::string& log) {
         smem = std::max(smem, q->item.item_smem_words);
     }
     tus.push_back(generate_batch_dispatch(entries, smem, 1));
+    tus.back().max_registers = server_max_registers();
     std::vector<const std::vector<char>*> objs;
     if (int e = compile_items(tus, objs, &log)) return e;
     std::string err, llog;
