@@ -59,6 +59,7 @@ void apply_shape_tune(Shape& sh, const std::string& t) {
             else if (k == "T" && (v == 128 || v == 256 || v == 512)) sh.threads = v;
             else if (k == "B" && v >= 1 && v <= 16) sh.min_blocks = v;
             else if (k == "S") sh.stage = v != 0;
+            else if (k == "P" && v >= 0 && v <= 64) sh.prefetch = v;
         }
         i = e + 1;
     }
@@ -574,7 +575,8 @@ GeneratedKernel generate_filter_kernel(const FilterSpec& f, const Shape& s, bool
     }
     key << "|O";
     for (const FilterOutput& o : f.outputs) key << (o.from_project ? "p" : "g") << o.index << ":" << (int)o.dtype << (o.has_valid ? "v" : "") << ",";
-    key << "|G" << s.G << "J" << s.J << "T" << s.threads << "B" << s.min_blocks << "U" << s.unroll << "S" << s.stage;
+    key << "|G" << s.G << "J" << s.J << "T" << s.threads << "B" << s.min_blocks << "U" << s.unroll << "S" << s.stage
+        << "P" << s.prefetch;
     if (item) key << "|item" << (s.soft ? "s" : "");
     char hex[32];
     snprintf(hex, sizeof hex, "%016llx", (unsigned long long)fnv1a(key.str()));
@@ -761,8 +763,48 @@ GeneratedKernel generate_filter_kernel(const FilterSpec& f, const Shape& s, bool
         os << "        const ral_u64 a0 = excl & ~31ull;\n";
     }
     if (any_proj && !proj_vouts.empty()) os << "        ral_u32 pw[" << proj_vouts.size() << "];\n";
+    // L2 prefetch of the columns pass 2 reads (not the predicate's, which pass 1 just read), a
+    // block of PF slices ahead, when the chunk keeps enough rows for the data to be needed: one
+    // cp.async.bulk.prefetch per column and block, issued by one lane each
+    std::vector<int> pf_cols;
+    if (s.prefetch > 0 && s.G > 1) {
+        std::vector<bool> want(NF, false);
+        for (const FilterOutput& o : f.outputs)
+            if (!o.from_project) want[o.index] = true;
+        for (size_t c = 0; c < f.project_cols.size(); c++)
+            if (proj_ref[c]) want[f.project_cols[c]] = true;
+        for (int c = 0; c < NF; c++)
+            if (want[c] && !pred_col[c]) pf_cols.push_back(c);
+        if ((int)pf_cols.size() > 32) pf_cols.resize(32);
+    }
+    const int PF = s.prefetch;
+    auto emit_prefetch = [&](const std::string& ind, const std::string& first_slice) {
+        if (pf_cols.empty()) return;
+        os << ind << "if (pf_on) {\n";
+        os << ind << "    const ral_i64 s0 = base + (ral_i64)(" << first_slice << ") * 32 * RAL_G;\n";
+        os << ind << "    if (s0 < n) {\n";
+        os << ind << "        const ral_i64 rows = (n - s0) < (ral_i64)" << PF << " * 32 * RAL_G ? (n - s0) : (ral_i64)" << PF
+           << " * 32 * RAL_G;\n";
+        for (size_t i = 0; i < pf_cols.size(); i++) {
+            const int c = pf_cols[i];
+            const int w = gdf_dtype_size(f.frame_dtypes[c]);
+            os << ind << "        if (lane == " << i << ") ral_prefetch_l2(" << fdata(c) << " + s0, (unsigned)((rows * " << w
+               << ") & ~15ll));\n";
+        }
+        os << ind << "    }\n" << ind << "}\n";
+    };
     os << "        ral_u64 sbase = excl;\n";
+    if (!pf_cols.empty()) {
+        os << "        const bool pf_on = (ral_u64)total * 8u >= (ral_u64)WT;\n";
+        emit_prefetch("        ", "0");
+        emit_prefetch("        ", std::to_string(PF));
+    }
     os << "#pragma unroll 2\n        for (int j = 0; j < RAL_J; ++j) {\n";
+    if (!pf_cols.empty()) {
+        os << "            if (j % " << PF << " == 0 && j + " << 2 * PF << " < RAL_J) {\n";
+        emit_prefetch("                ", "j + " + std::to_string(2 * PF));
+        os << "            }\n";
+    }
     os << "            const ral_u32 kb = (kbw[(j * RAL_G) >> 5] >> ((j * RAL_G) & 31)) & GMASK;\n";
     os << "            const ral_u32 c = __popc(kb);\n";
     os << "            ral_u32 inc = c;\n";

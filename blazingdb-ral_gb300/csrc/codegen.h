@@ -25,6 +25,7 @@ struct Shape {
     int unroll = 4;    // filter kernels: unroll of the predicate pass over slices
     bool stage = false;  // filter kernels: dense slices written through a shared-memory stage
     bool soft = false;   // batch items: integer-pipe double operations (the autotuner decides)
+    int prefetch = 8;    // filter kernels: slices of pass 2 prefetched into L2 ahead (0: none)
 };
 
 // Slot order of the kernel's parameter block (all 8-byte slots).
@@ -42,8 +43,8 @@ struct ParamLayout {
 int max_width(const Program& p);
 // Default shape for a program: G = 16 / widest column, J so that a lane covers 4 rows.
 Shape default_shape(const Program& p);
-// Applies "J=8,U=2,T=128,B=3,S=1" style overrides (slices, unroll, threads, min blocks per SM,
-// staging) to a shape; unknown keys and out-of-range values are ignored.
+// Applies "J=8,U=2,T=128,B=3,S=1,P=8" style overrides (slices, unroll, threads, min blocks per
+// SM, staging, L2 prefetch distance) to a shape; unknown keys and out-of-range values are ignored.
 void apply_shape_tune(Shape& sh, const std::string& t);
 
 struct GeneratedKernel {

@@ -181,6 +181,15 @@ RAL_FI ral_i64 ral_second64(ral_i64 t) {
     return t >= 0 ? ((t % RAL_MS_MINUTE) / RAL_MS_SECOND) : ((RAL_MS_MINUTE + (t % RAL_MS_MINUTE)) / RAL_MS_SECOND);
 }
 
+// ---- L2 prefetch of a contiguous range (one bulk request; 16-byte aligned start, size a
+// multiple of 16, within the allocation) -----------------------------------------------------
+RAL_FI void ral_prefetch_l2(const void* p, unsigned bytes) {
+    if (bytes < 16u) return;
+    unsigned long long g;
+    asm("cvta.to.global.u64 %0, %1;" : "=l"(g) : "l"(p));
+    asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(g), "r"(bytes) : "memory");
+}
+
 // ---- vector loads / stores of G consecutive elements ---------------------------------------
 template <int BYTES> struct RalVecT;
 template <> struct RalVecT<16> { typedef uint4 T; };
