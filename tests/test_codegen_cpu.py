@@ -93,7 +93,7 @@ FILTER_CASES = [
 ]
 
 
-@pytest.mark.parametrize("tune", ["", "S=1", "J=8,U=2,T=128,B=4", "J=64,U=8,T=512,B=1,S=1"])
+@pytest.mark.parametrize("tune", ["", "S=1", "J=8,U=2,T=128,B=4", "J=64,U=8,T=512,B=1,S=1", "P=8", "P=4,J=16"])
 @pytest.mark.parametrize("case", FILTER_CASES, ids=[c[0] for c in FILTER_CASES])
 def test_filter_kernels_compile(case, tune, monkeypatch):
     _, dtypes, nullable, fq, pq = case

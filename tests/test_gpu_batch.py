@@ -150,3 +150,24 @@ def test_autotune_records_a_shape_and_batch_still_matches():
         R.perform_operation(p["outs_p"], p["dev_in"], *_args(p["pp"]))
         for k, (x, y) in enumerate(zip(p["outs_b"], p["outs_p"])):
             _assert_same_bits(x, y, f"program {q} output {k}")
+
+
+def test_batch_with_empty_tables():
+    """Programs over empty tables contribute no work items; the others still run."""
+    import torch
+    mix = W.batched_mix(6, seed=13, min_rows=100, max_rows=5000)
+    mix[1].rows = 0
+    mix[4].rows = 0
+    progs = _build(mix)
+    b = R.Batch()
+    for p in progs:
+        b.add(p["outs_b"], p["dev_in"], *_args(p["pp"]))
+    b.run()
+    torch.cuda.synchronize()
+    assert b.info()["rows"] == sum(p["n"] for p in progs)
+    for q, p in enumerate(progs):
+        if p["n"] == 0:
+            continue
+        R.perform_operation(p["outs_p"], p["dev_in"], *_args(p["pp"]))
+        for k, (x, y) in enumerate(zip(p["outs_b"], p["outs_p"])):
+            _assert_same_bits(x, y, f"program {q} output {k}")

@@ -159,3 +159,24 @@ def test_requests_sliced_over_many_waves_give_the_same_bits(served):
             _same_bits(g, a, f"query {i} output {j} sliced")
     assert srv.stats()["waves"] > 3 * len(qs)
     srv.close()
+
+
+def test_empty_and_one_row_tables():
+    """A request over an empty table keeps 0 rows; over a one-row table, the row or nothing."""
+    import numpy as np
+    from ralgpu import dtypes as D
+    t0 = [R.Column.from_numpy(np.zeros(0, dtype=np.int32), D.GDF_INT32, np.zeros(0, dtype=bool)),
+          R.Column.from_numpy(np.zeros(0), D.GDF_FLOAT64, None)]
+    t1 = [R.Column.from_numpy(np.array([7], dtype=np.int32), D.GDF_INT32, np.array([True])),
+          R.Column.from_numpy(np.array([2.5]), D.GDF_FLOAT64, None)]
+    srv = R.Server(budget_bytes=1 << 30)
+    a, b = srv.add_table(t0), srv.add_table(t1)
+    fq, pq = "LogicalFilter(condition=[>($0, 5)])", "LogicalProject(x=[*($1, 2)], y=[$0])"
+    qa, qb = srv.add_query(a, fq, pq), srv.add_query(b, fq, pq)
+    qc = srv.add_query(b, "LogicalFilter(condition=[<($0, 5)])", pq)
+    srv.start()
+    assert srv.wait(srv.submit(qa))[0] == 0
+    got = srv.result(srv.submit(qb, keep=True), qb)
+    assert got[0].size == 1 and got[0].to_numpy()[0] == 5.0 and got[1].to_numpy()[0] == 7
+    assert srv.wait(srv.submit(qc))[0] == 0
+    srv.close()
