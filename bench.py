@@ -136,7 +136,9 @@ def dist_setup(args):
     local = int(os.environ.get("LOCAL_RANK", "0"))
     if world > 1:
         import torch.distributed as dist
-        backend = "nccl" if args.impl != "reference" else "gloo"
+        # replicas only exchange their timings: NCCL on GPUs, gloo for the CPU reference arm (and
+        # for CPU tests of this coordination, RAL_DIST_BACKEND=gloo)
+        backend = os.environ.get("RAL_DIST_BACKEND") or ("nccl" if args.impl != "reference" else "gloo")
         dist.init_process_group(backend=backend)
     return world, rank, local
 
@@ -152,9 +154,15 @@ def max_over_ranks(world, v):
         return v
     import torch
     import torch.distributed as dist
-    t = torch.tensor([v], dtype=torch.float64, device="cuda")
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([v], dtype=torch.float64, device=dev)
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
+
+
+def job_rate(world, units_per_rank, ms_per_step):
+    """Whole-job throughput of N replicas: every rank's units over the slowest rank's time."""
+    return world * units_per_rank / (ms_per_step / 1e3)
 
 
 # ---- CPU oracle timing --------------------------------------------------------------------------
@@ -490,7 +498,7 @@ def run_ours(args):
     total_ms = max_over_ranks(world, total_ms)
     kernel_ms = statistics.mean(s.elapsed_time(e) for s, e in events)
     ms_per_step = total_ms / args.steps
-    value = world * n / (ms_per_step / 1e3)
+    value = job_rate(world, n, ms_per_step)
     peak, peak_kind = load_peaks()
     alg = ctx["alg_bytes"] if "alg_bytes" in ctx else ctx["alg_bytes_fn"]()
     achieved = alg / (kernel_ms / 1e3) / 1e9
@@ -647,7 +655,7 @@ def run_batched(args):
     clocks = sampler.stop()
     step_ms = [s_.elapsed_time(e_) for s_, e_ in events]
     ms_per_step = max_over_ranks(world, statistics.mean(step_ms))
-    value = world * rows / (ms_per_step / 1e3)
+    value = job_rate(world, rows, ms_per_step)
 
     # the same programs as plain per-call launches: one synchronous ral_perform_operation each
     plain = None
