@@ -762,4 +762,49 @@ int ral_softfp_selftest(int64_t n, uint64_t seed, int64_t* mismatches, uint64_t*
     });
 }
 
+int ral_debug_lookback_timeout(int64_t n_rows, int32_t* status, int64_t* kept_after) {
+    return guarded([&] {
+        if (n_rows <= (int64_t)kCompactTileRows || n_rows > ((int64_t)64 << 20) || !status || !kept_after)
+            return set_error(kInvalidArgument, "n_rows must be above one tile and at most 64M");
+        cudaStream_t st = cudaStreamPerThread;
+        const int64_t words = compact_scratch_words(n_rows);
+        int8_t* stencil = nullptr;
+        int32_t* idx = nullptr;
+        unsigned long long* scratch = nullptr;
+        auto cleanup = [&] {
+            if (stencil) cudaFree(stencil);
+            if (idx) cudaFree(idx);
+            if (scratch) cudaFree(scratch);
+        };
+        if (check_cuda(cudaMalloc(&stencil, (size_t)n_rows), "cudaMalloc") ||
+            check_cuda(cudaMalloc(&idx, (size_t)n_rows * 4), "cudaMalloc") ||
+            check_cuda(cudaMalloc(&scratch, (size_t)words * 8), "cudaMalloc")) {
+            cleanup();
+            return (int)kCudaError;
+        }
+        cudaMemsetAsync(stencil, 1, (size_t)n_rows, st);
+        // the ticket counter starts at 1: tile 0 is never taken, so tile 1's look-back waits on a
+        // status word that nothing writes until its spin limit ends the wait
+        cudaMemsetAsync(scratch, 0, (size_t)words * 8, st);
+        const unsigned long long one = 1;
+        cudaMemcpyAsync(scratch, &one, 8, cudaMemcpyHostToDevice, st);
+        int rc = check_cuda(launch_compact_stencil(stencil, nullptr, n_rows, idx, scratch, st), "compaction");
+        unsigned long long err = 0;
+        if (!rc) cudaMemcpyAsync(&err, scratch + 1, 8, cudaMemcpyDeviceToHost, st);
+        if (!rc) rc = check_cuda(cudaStreamSynchronize(st), "compaction with an unclaimed tile");
+        *status = err ? (int32_t)kTimeout : (int32_t)kSuccess;
+        // the context is still usable: the same compaction with every tile taken
+        unsigned long long kept = 0;
+        if (!rc) {
+            cudaMemsetAsync(scratch, 0, (size_t)words * 8, st);
+            rc = check_cuda(launch_compact_stencil(stencil, nullptr, n_rows, idx, scratch, st), "compaction");
+            if (!rc) cudaMemcpyAsync(&kept, scratch + 2, 8, cudaMemcpyDeviceToHost, st);
+            if (!rc) rc = check_cuda(cudaStreamSynchronize(st), "compaction");
+        }
+        *kept_after = (int64_t)kept;
+        cleanup();
+        return rc;
+    });
+}
+
 }  // extern "C"

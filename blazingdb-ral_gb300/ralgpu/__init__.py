@@ -11,7 +11,8 @@ from .capi import (RalError, lib, perform_operation, perform_operation_async, ev
                    process_filter, execute_project_plan, filter_project, project_output_types,
                    materialize_column, apply_boolean_mask, add_expression_to_plan, get_output_type_expression,
                    debug_program_source, debug_filter_source, jit_stats, kernel_launches, version,
-                   parse_project_plan, Batch, autotune_program, batch_tune_key, Server, softfp_selftest)
+                   parse_project_plan, Batch, autotune_program, batch_tune_key, Server, softfp_selftest,
+                   debug_lookback_timeout)
 from .column import Column, Scalar, valid_alloc_size
 from . import dtypes
 
@@ -20,5 +21,5 @@ __all__ = [
     "process_filter", "execute_project_plan", "filter_project", "project_output_types",
     "materialize_column", "apply_boolean_mask", "add_expression_to_plan", "get_output_type_expression",
     "debug_program_source", "debug_filter_source", "jit_stats", "kernel_launches", "version", "Column", "Scalar",
-    "valid_alloc_size", "dtypes", "parse_project_plan", "Batch", "autotune_program", "batch_tune_key", "Server", "softfp_selftest",
+    "valid_alloc_size", "dtypes", "parse_project_plan", "Batch", "autotune_program", "batch_tune_key", "Server", "softfp_selftest", "debug_lookback_timeout",
 ]

@@ -75,6 +75,7 @@ _SIGS = {
     "ral_server_stats": (C.c_int, [P, C.POINTER(C.c_int64)]),
     "ral_server_destroy": (C.c_int, [P]),
     "ral_softfp_selftest": (C.c_int, [C.c_int64, C.c_uint64, C.POINTER(C.c_int64), C.POINTER(C.c_uint64)]),
+    "ral_debug_lookback_timeout": (C.c_int, [C.c_int64, I32P, C.POINTER(C.c_int64)]),
     "ral_batch_tune_key": (C.c_int, [COLPP, C.c_int32, COLPP, C.c_int32, I16P, I16P, I16P, C.c_int32, I16P, I32P, I32P,
                                      SCP, SCP, C.c_char_p, C.c_int64]),
     "ral_autotune_program": (C.c_int, [COLPP, C.c_int32, COLPP, C.c_int32, I16P, I16P, I16P, C.c_int32, I16P, I32P,
@@ -615,3 +616,11 @@ def softfp_selftest(n: int = 1 << 24, seed: int = 1) -> dict:
     first = (C.c_uint64 * 32)()
     _check(lib().ral_softfp_selftest(n, seed, cnt, first))
     return {op: (int(cnt[i]), (int(first[2 * i]), int(first[2 * i + 1]))) for i, op in enumerate(SOFTFP_OPS)}
+
+
+def debug_lookback_timeout(n_rows: int = 3 * 4096) -> Tuple[int, int]:
+    """Runs a compaction whose first tile is never taken; returns (status of that run, kept rows of
+    a normal run right after)."""
+    st, kept = C.c_int32(0), C.c_int64(0)
+    _check(lib().ral_debug_lookback_timeout(n_rows, C.byref(st), C.byref(kept)))
+    return st.value, kept.value

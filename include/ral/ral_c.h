@@ -329,6 +329,16 @@ int ral_server_destroy(ral_server *server);
  */
 int ral_softfp_selftest(int64_t n, uint64_t seed, int64_t *mismatches, uint64_t *first_operands);
 
+/*
+ * Failure-detection check (no reference counterpart): runs the compaction over n_rows rows with its
+ * tile counter starting at 1, so that tile 1's look-back waits on a status word nothing writes;
+ * the bounded wait must end (about a second) with the error word set, reported as
+ * *status = RAL_ERROR_TIMEOUT, and the context must stay usable: the same compaction is then run
+ * normally and *kept_after receives its kept-row count (n_rows).  n_rows: one tile (4096) < n_rows
+ * <= 64M.
+ */
+int ral_debug_lookback_timeout(int64_t n_rows, int32_t *status, int64_t *kept_after);
+
 #ifdef __cplusplus
 }
 #endif
