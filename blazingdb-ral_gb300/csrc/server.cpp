@@ -164,6 +164,28 @@ int Server::query_outputs(int query_id, std::vector<gdf_dtype>& dtypes, std::vec
     return kSuccess;
 }
 
+// One translation unit and one dispatcher entry per distinct item function: queries whose
+// filter and projection generate the same code (same column types, masks and operators, any
+// table) share one function, because the linker accepts each extern symbol once.  Sets each
+// query's dispatcher index.
+void Server::collect_items(std::vector<GeneratedKernel>& tus, std::vector<DispatchEntry>& entries, int& stride,
+                           int& smem) {
+    std::unordered_map<std::string, int> index;
+    stride = 1;
+    smem = 0;
+    for (auto& q : queries_) {
+        auto it = index.find(q->item.name);
+        if (it == index.end()) {
+            it = index.emplace(q->item.name, (int)entries.size()).first;
+            tus.push_back(q->item);
+            entries.push_back({q->item.name, true});
+        }
+        q->fn = it->second;
+        stride = std::max(stride, q->item.layout.total);
+        smem = std::max(smem, q->item.item_smem_words);
+    }
+}
+
 // Compiles the item functions of all queries and links the dispatcher; (re)allocates the
 // wave buffers.  Called with mu_ held and no wave in flight.
 int Server::ensure_linked() {
@@ -172,13 +194,7 @@ int Server::ensure_linked() {
     std::vector<GeneratedKernel> tus;
     std::vector<DispatchEntry> entries;
     int stride = 1, smem = 0;
-    for (size_t i = 0; i < queries_.size(); i++) {
-        queries_[i]->fn = (int)i;
-        tus.push_back(queries_[i]->item);
-        entries.push_back({queries_[i]->item.name, true});
-        stride = std::max(stride, queries_[i]->item.layout.total);
-        smem = std::max(smem, queries_[i]->item.item_smem_words);
-    }
+    collect_items(tus, entries, stride, smem);
     GeneratedKernel disp = generate_batch_dispatch(entries, smem, 1);
     disp.max_registers = server_max_registers();
     tus.push_back(disp);
@@ -235,12 +251,8 @@ int Server::debug_compile(std::string& log) {
     if (queries_.empty()) return set_error(kInvalidArgument, "no queries");
     std::vector<GeneratedKernel> tus;
     std::vector<DispatchEntry> entries;
-    int smem = 0;
-    for (auto& q : queries_) {
-        tus.push_back(q->item);
-        entries.push_back({q->item.name, true});
-        smem = std::max(smem, q->item.item_smem_words);
-    }
+    int stride = 1, smem = 0;
+    collect_items(tus, entries, stride, smem);
     tus.push_back(generate_batch_dispatch(entries, smem, 1));
     tus.back().max_registers = server_max_registers();
     std::vector<const std::vector<char>*> objs;

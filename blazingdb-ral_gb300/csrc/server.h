@@ -114,6 +114,7 @@ private:
         double t_launch = 0;
     };
     int ensure_linked();
+    void collect_items(std::vector<GeneratedKernel>& tus, std::vector<DispatchEntry>& entries, int& stride, int& smem);
     int launch_wave(Wave& w, const std::vector<int64_t>& reqs, const std::vector<int64_t>& take);
     void finish_wave(Wave& w);
     void loop();

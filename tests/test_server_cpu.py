@@ -55,6 +55,25 @@ def test_query_chunk_functions_compile_and_link(tmp_path, monkeypatch):
     srv.close()
 
 
+def test_queries_with_identical_code_share_one_item_function(tmp_path, monkeypatch):
+    """The same filter and projection over tables with the same column types generate one item
+    function; it is linked once (a second copy is a duplicate symbol to the linker)."""
+    monkeypatch.setenv("RAL_JIT_CACHE_DIR", str(tmp_path))
+    D = ralgpu.dtypes
+    srv = ralgpu.Server(budget_bytes=1 << 30)
+    tids = [srv.add_table([ralgpu.Column.empty(D.GDF_INT32, n, with_valid=True, device="cpu"),
+                           ralgpu.Column.empty(D.GDF_FLOAT64, n, with_valid=False, device="cpu")])
+            for n in (0, 1, 1000)]
+    fq, pq = "LogicalFilter(condition=[>($0, 5)])", "LogicalProject(x=[*($1, 2)], y=[$0])"
+    for t in tids:
+        srv.add_query(t, fq, pq)
+        srv.add_query(t, fq, pq)
+    srv.add_query(tids[1], "LogicalFilter(condition=[<($0, 5)])", pq)
+    log = srv.debug_compile()
+    assert "Multiple definition" not in log
+    srv.close()
+
+
 def test_budget_rejects_a_query_whose_request_cannot_fit():
     tabs = W.served_tables(2, seed=5)
     n = 100_000
