@@ -60,6 +60,7 @@ void apply_shape_tune(Shape& sh, const std::string& t) {
             else if (k == "B" && v >= 1 && v <= 16) sh.min_blocks = v;
             else if (k == "S") sh.stage = v != 0;
             else if (k == "P" && v >= 0 && v <= 64) sh.prefetch = v;
+            else if (k == "D" && v >= -1 && v <= 1) sh.dense = v;
         }
         i = e + 1;
     }
@@ -575,8 +576,20 @@ GeneratedKernel generate_filter_kernel(const FilterSpec& f, const Shape& s, bool
     }
     key << "|O";
     for (const FilterOutput& o : f.outputs) key << (o.from_project ? "p" : "g") << o.index << ":" << (int)o.dtype << (o.has_valid ? "v" : "") << ",";
+    // dense pass 2 (see Shape::dense): per warp a u16 list of the chunk's kept rows and the
+    // projection's validity words of the chunk; kept to blocks whose static shared memory fits
+    bool any_gather = false, any_proj = false;
+    for (const FilterOutput& o : f.outputs) (o.from_project ? any_proj : any_gather) = true;
+    int n_proj_vouts = 0;
+    for (int k : vouts) n_proj_vouts += f.outputs[k].from_project ? 1 : 0;
+    bool dense = s.dense < 0 ? any_proj : s.dense > 0;
+    if (32 * s.G * s.J > 65536) dense = false;
+    {
+        const long per_warp = (long)NVO * (s.G * s.J + 2) * 4 + (dense ? (long)n_proj_vouts * s.G * s.J * 4 + 64L * s.G * s.J : 0);
+        if (dense && per_warp * (s.threads / 32) > 47 * 1024) dense = false;
+    }
     key << "|G" << s.G << "J" << s.J << "T" << s.threads << "B" << s.min_blocks << "U" << s.unroll << "S" << s.stage
-        << "P" << s.prefetch;
+        << "P" << s.prefetch << "D" << (dense ? 1 : 0);
     if (item) key << "|item" << (s.soft ? "s" : "");
     char hex[32];
     snprintf(hex, sizeof hex, "%016llx", (unsigned long long)fnv1a(key.str()));
@@ -652,11 +665,23 @@ GeneratedKernel generate_filter_kernel(const FilterSpec& f, const Shape& s, bool
            << "(const ral_u64* __restrict__ slots, const ral_i64 chunk_index, ral_u32* __restrict__ wsm) {\n";
         os << "    const RalParams& P = *reinterpret_cast<const RalParams*>(slots);\n";
         if (NVO) os << "    ral_u32 (*const s_vbw)[RAL_G * RAL_J + 2] = reinterpret_cast<ral_u32 (*)[RAL_G * RAL_J + 2]>(wsm);\n";
-        gk.item_smem_words = NVO * (s.G * s.J + 2);
+        int words = NVO * (s.G * s.J + 2);
+        if (dense) {
+            if (n_proj_vouts)
+                os << "    ral_u32 (*const s_pvw)[RAL_G * RAL_J] = reinterpret_cast<ral_u32 (*)[RAL_G * RAL_J]>(wsm + " << words << ");\n";
+            words += n_proj_vouts * s.G * s.J;
+            os << "    unsigned short* const s_lst = reinterpret_cast<unsigned short*>(wsm + " << words << ");\n";
+            words += 16 * s.G * s.J;
+        }
+        gk.item_smem_words = words;
     } else {
         os << "\nextern \"C\" __global__ void __launch_bounds__(RAL_THREADS, " << std::max(1, s.min_blocks) << ") " << gk.name
            << "(const __grid_constant__ RalParams P) {\n";
         if (NVO) os << "    __shared__ ral_u32 s_vb[RAL_WARPS][" << NVO << "][RAL_G * RAL_J + 2];\n";
+        if (dense) {
+            if (n_proj_vouts) os << "    __shared__ ral_u32 s_pv[RAL_WARPS][" << n_proj_vouts << "][RAL_G * RAL_J];\n";
+            os << "    __shared__ unsigned short s_ls[RAL_WARPS][32 * RAL_G * RAL_J];\n";
+        }
     }
     // per-warp staging of one slice's compacted values, so that stores are contiguous
     if (s.stage) os << "    __shared__ ral_u64 s_stage[RAL_WARPS][32 * RAL_G];\n";
@@ -681,6 +706,10 @@ GeneratedKernel generate_filter_kernel(const FilterSpec& f, const Shape& s, bool
         os << "    const int warp = threadIdx.x >> 5;\n";
         if (NVO) os << "    ral_u32 (*const s_vbw)[RAL_G * RAL_J + 2] = s_vb[warp];\n";
         if (s.stage) os << "    ral_u64* const s_stw = s_stage[warp];\n";
+        if (dense) {
+            if (n_proj_vouts) os << "    ral_u32 (*const s_pvw)[RAL_G * RAL_J] = s_pv[warp];\n";
+            os << "    unsigned short* const s_lst = s_ls[warp];\n";
+        }
     }
     os << "    const ral_i64 WT = 32 * RAL_G * RAL_J;\n";
     os << "    const ral_i64 nchunks = (n + WT - 1) / WT;\n";
@@ -698,8 +727,10 @@ GeneratedKernel generate_filter_kernel(const FilterSpec& f, const Shape& s, bool
     }
     os << "        const ral_i64 base = chunk * WT;\n";
     os << "        const bool full = base + WT <= n;\n";
-    os << "        ral_u32 kbw[" << KBW << "];\n";
-    os << "        for (int q = 0; q < " << KBW << "; ++q) kbw[q] = 0u;\n";
+    if (!dense) {
+        os << "        ral_u32 kbw[" << KBW << "];\n";
+        os << "        for (int q = 0; q < " << KBW << "; ++q) kbw[q] = 0u;\n";
+    }
     os << "        ral_u32 total = 0;\n";
 
     // ---- pass 1: predicate
@@ -743,16 +774,30 @@ GeneratedKernel generate_filter_kernel(const FilterSpec& f, const Shape& s, bool
     os << "            const ral_u32 word = __shfl_sync(0xffffffffu, sw, (lane * RAL_G) >> 5);\n";
     os << "            bits &= (word >> (int)(r & 31)) & GMASK;\n";
     os << "            if (!full) {\n#pragma unroll\n                for (int g = 0; g < RAL_G; ++g) if (r + g >= n) bits &= ~(1u << g);\n            }\n";
-    os << "            kbw[(j * RAL_G) >> 5] |= bits << ((j * RAL_G) & 31);\n";
-    os << "            total += __reduce_add_sync(0xffffffffu, __popc(bits));\n";
+    if (dense) {
+        // the lane's kept rows go to the chunk's list at their rank: rows of earlier slices,
+        // then of lower lanes in this slice
+        os << "            {\n";
+        os << "                const ral_u32 c = __popc(bits);\n";
+        os << "                ral_u32 inc = c;\n";
+        os << "                for (int off = 1; off < 32; off <<= 1) {\n";
+        os << "                    const ral_u32 t = __shfl_up_sync(0xffffffffu, inc, off);\n";
+        os << "                    if (lane >= off) inc += t;\n                }\n";
+        os << "                ral_u32 q = total + inc - c;\n";
+        os << "#pragma unroll\n                for (int g = 0; g < RAL_G; ++g)\n";
+        os << "                    if ((bits >> g) & 1u) s_lst[q++] = (unsigned short)(j * 32 * RAL_G + lane * RAL_G + g);\n";
+        os << "                total += __shfl_sync(0xffffffffu, inc, 31);\n";
+        os << "            }\n";
+    } else {
+        os << "            kbw[(j * RAL_G) >> 5] |= bits << ((j * RAL_G) & 31);\n";
+        os << "            total += __reduce_add_sync(0xffffffffu, __popc(bits));\n";
+    }
     os << "        }\n";
     os << "        const ral_u64 excl = ral_lookback(status, chunk, total, scratch + 1);\n";
     os << "        if (chunk == nchunks - 1 && lane == 0) scratch[2] = excl + total;\n";
     os << "        if (total == 0u) continue;\n";
 
     // ---- pass 2: ranks and outputs
-    bool any_gather = false, any_proj = false;
-    for (const FilterOutput& o : f.outputs) (o.from_project ? any_proj : any_gather) = true;
     if (NVO) {
         for (int i = 0; i < NVO; i++) os << "        if (lane < RAL_G * RAL_J + 2) s_vbw[" << i << "][lane] = 0u;\n";
         os << "        if (RAL_G * RAL_J + 2 > 32) {\n";
@@ -762,165 +807,244 @@ GeneratedKernel generate_filter_kernel(const FilterSpec& f, const Shape& s, bool
         os << "        __syncwarp();\n";
         os << "        const ral_u64 a0 = excl & ~31ull;\n";
     }
-    if (any_proj && !proj_vouts.empty()) os << "        ral_u32 pw[" << proj_vouts.size() << "];\n";
-    // L2 prefetch of the columns pass 2 reads (not the predicate's, which pass 1 just read), a
-    // block of PF slices ahead, when the chunk keeps enough rows for the data to be needed: one
-    // cp.async.bulk.prefetch per column and block, issued by one lane each
-    std::vector<int> pf_cols;
-    if (s.prefetch > 0 && s.G > 1) {
-        std::vector<bool> want(NF, false);
-        for (const FilterOutput& o : f.outputs)
-            if (!o.from_project) want[o.index] = true;
-        for (size_t c = 0; c < f.project_cols.size(); c++)
-            if (proj_ref[c]) want[f.project_cols[c]] = true;
-        for (int c = 0; c < NF; c++)
-            if (want[c] && !pred_col[c]) pf_cols.push_back(c);
-        if ((int)pf_cols.size() > 32) pf_cols.resize(32);
-    }
-    const int PF = s.prefetch;
-    auto emit_prefetch = [&](const std::string& ind, const std::string& first_slice) {
-        if (pf_cols.empty()) return;
-        os << ind << "if (pf_on) {\n";
-        os << ind << "    const ral_i64 s0 = base + (ral_i64)(" << first_slice << ") * 32 * RAL_G;\n";
-        os << ind << "    if (s0 < n) {\n";
-        os << ind << "        const ral_i64 rows = (n - s0) < (ral_i64)" << PF << " * 32 * RAL_G ? (n - s0) : (ral_i64)" << PF
-           << " * 32 * RAL_G;\n";
-        for (size_t i = 0; i < pf_cols.size(); i++) {
-            const int c = pf_cols[i];
-            const int w = gdf_dtype_size(f.frame_dtypes[c]);
-            os << ind << "        if (lane == " << i << ") ral_prefetch_l2(" << fdata(c) << " + s0, (unsigned)((rows * " << w
-               << ") & ~15ll));\n";
+    if (dense) {
+        // Dense pass 2: lane k of step k0 takes the chunk's kept row k0 + k from the list, so
+        // every lane evaluates a kept row (the last step excepted) and the stores of a step are
+        // contiguous.  The projection's validity words of the chunk are staged first; each masked
+        // output's bits of a step are one ballot, placed at the step's output positions.
+        if (n_proj_vouts) {
+            os << "        for (int wl = lane; wl < RAL_G * RAL_J; wl += 32) {\n";
+            os << "            const ral_i64 w = (base >> 5) + wl;\n";
+            os << "            ral_u32 pv[" << n_proj_vouts << "];\n";
+            os << "            for (int i = 0; i < " << n_proj_vouts << "; ++i) pv[i] = 0u;\n";
+            os << "            if ((w << 5) < n) ral_proj_vword(P, w, pv);\n";
+            for (int i = 0; i < n_proj_vouts; i++) os << "            s_pvw[" << i << "][wl] = pv[" << i << "];\n";
+            os << "        }\n";
         }
-        os << ind << "    }\n" << ind << "}\n";
-    };
-    os << "        ral_u64 sbase = excl;\n";
-    if (!pf_cols.empty()) {
-        os << "        const bool pf_on = (ral_u64)total * 8u >= (ral_u64)WT;\n";
-        emit_prefetch("        ", "0");
-        emit_prefetch("        ", std::to_string(PF));
-    }
-    os << "#pragma unroll 2\n        for (int j = 0; j < RAL_J; ++j) {\n";
-    if (!pf_cols.empty()) {
-        os << "            if (j % " << PF << " == 0 && j + " << 2 * PF << " < RAL_J) {\n";
-        emit_prefetch("                ", "j + " + std::to_string(2 * PF));
-        os << "            }\n";
-    }
-    os << "            const ral_u32 kb = (kbw[(j * RAL_G) >> 5] >> ((j * RAL_G) & 31)) & GMASK;\n";
-    os << "            const ral_u32 c = __popc(kb);\n";
-    os << "            ral_u32 inc = c;\n";
-    os << "            for (int off = 1; off < 32; off <<= 1) {\n";
-    os << "                const ral_u32 t = __shfl_up_sync(0xffffffffu, inc, off);\n";
-    os << "                if (lane >= off) inc += t;\n            }\n";
-    os << "            const ral_u32 stot = __shfl_sync(0xffffffffu, inc, 31);\n";
-    os << "            if (stot == 0u) continue;\n";
-    os << "            const ral_u64 pos0 = sbase + inc - c;\n";
-    os << "            const ral_i64 r = base + (ral_i64)j * 32 * RAL_G + lane * RAL_G;\n";
-    if (any_gather) {
-        // every gathered column of the slice is loaded first (all loads in flight together);
-        // a slice that keeps many rows is then written through the warp's stage as one
-        // contiguous run per column, a sparse slice with direct stores
+        os << "        __syncwarp();\n";
+        os << "        for (ral_u32 k0 = 0; k0 < total; k0 += 32) {\n";
+        os << "            const ral_u32 k = k0 + lane;\n";
+        os << "            const bool act = k < total;\n";
+        // an idle lane of the last step works on the step's first row and stores nothing
+        os << "            const ral_u32 off = s_lst[act ? k : k0];\n";
+        os << "            const ral_i64 row = base + off;\n";
+        os << "            const ral_u64 pos = excl + k;\n";
         for (int k = 0; k < NO; k++) {
             if (f.outputs[k].from_project) continue;
             const int c = f.outputs[k].index;
-            const char* et = element_ctype(f.frame_dtypes[c]);
-            os << "            " << et << " ga" << k << "[RAL_G];\n";
-            os << "            if (kb) {\n";
-            os << "                if (full) " << (pred_col[c] ? "ral_ldg_keep<" : "ral_ldg<") << et << ", RAL_G>(" << fdata(c)
-               << ", r, ga" << k << ");\n";
-            os << "                else {\n#pragma unroll\n                    for (int g = 0; g < RAL_G; ++g) ga" << k
-               << "[g] = (r + g < n) ? " << fdata(c) << "[r + g] : (" << et << ")0;\n                }\n";
+            os << "            {\n                const " << element_ctype(f.frame_dtypes[c]) << " v = " << fdata(c) << "[row];\n";
+            os << "                if (act) o" << k << "[pos] = v;\n            }\n";
+        }
+        if (any_proj) {
+            for (size_t c = 0; c < f.project_cols.size(); c++)
+                if (proj_ref[c])
+                    os << "            const " << element_ctype(f.frame_dtypes[f.project_cols[c]]) << " qa" << c << " = "
+                       << fdata(f.project_cols[c]) << "[row];\n";
+            for (size_t c = 0; c < f.project_cols.size(); c++)
+                if (proj_raw[c]) {
+                    const int fc = f.project_cols[c];
+                    if (f.frame_has_valid[fc]) os << "            const ral_u32 qw" << c << " = __ldg(" << fvalid(fc) << " + (row >> 5));\n";
+                    else os << "            const ral_u32 qw" << c << " = 0xffffffffu;\n";
+                }
+            for (int o = 0; o < f.project->n_out; o++) os << "            " << kind_ctype(proj_kind[o]) << " y" << o << ";\n";
+            os << "            ral_proj_row(P";
+            for (size_t c = 0; c < f.project_cols.size(); c++)
+                if (proj_ref[c]) os << ", " << widen("qa" + std::to_string(c), f.frame_dtypes[f.project_cols[c]]);
+            for (size_t c = 0; c < f.project_cols.size(); c++)
+                if (proj_raw[c]) os << ", (qw" << c << " >> (int)(row & 31)) & 1u";
+            for (int o = 0; o < f.project->n_out; o++) os << ", y" << o;
+            os << ");\n";
+            os << "            if (act) {\n";
+            for (int k = 0; k < NO; k++) {
+                if (!f.outputs[k].from_project) continue;
+                const int o = f.outputs[k].index;
+                os << "                o" << k << "[pos] = " << narrow("y" + std::to_string(o), proj_kind[o], f.outputs[k].dtype) << ";\n";
+            }
             os << "            }\n";
         }
-        if (s.stage) {
-            os << "            if (stot >= 16u) {\n";
+        for (int i = 0; i < NVO; i++) {
+            const int k = vouts[i];
+            const FilterOutput& o = f.outputs[k];
+            os << "            {\n";
+            if (o.from_project) {
+                int pi = 0;
+                for (size_t q = 0; q < proj_vouts.size(); q++)
+                    if (proj_vouts[q] == o.index) pi = (int)q;
+                os << "                const ral_u32 vw = s_pvw[" << pi << "][off >> 5];\n";
+            } else {
+                os << "                const ral_u32 vw = __ldg(" << fvalid(o.index) << " + (row >> 5));\n";
+            }
+            os << "                const ral_u32 bal = __ballot_sync(0xffffffffu, act && ((vw >> (off & 31u)) & 1u));\n";
+            os << "                if (lane == 0 && bal) {\n";
+            os << "                    vcnt[" << i << "] += __popc(bal);\n";
+            os << "                    const ral_u64 X = (ral_u64)bal << (excl & 31u);\n";
+            os << "                    s_vbw[" << i << "][k0 >> 5] |= (ral_u32)X;\n";
+            os << "                    s_vbw[" << i << "][(k0 >> 5) + 1] |= (ral_u32)(X >> 32);\n";
+            os << "                }\n";
+            os << "            }\n";
+        }
+        os << "        }\n";
+    } else {
+        if (any_proj && !proj_vouts.empty()) os << "        ral_u32 pw[" << proj_vouts.size() << "];\n";
+        // L2 prefetch of the columns pass 2 reads (not the predicate's, which pass 1 just read), a
+        // block of PF slices ahead, when the chunk keeps enough rows for the data to be needed: one
+        // cp.async.bulk.prefetch per column and block, issued by one lane each
+        std::vector<int> pf_cols;
+        if (s.prefetch > 0 && s.G > 1) {
+            std::vector<bool> want(NF, false);
+            for (const FilterOutput& o : f.outputs)
+                if (!o.from_project) want[o.index] = true;
+            for (size_t c = 0; c < f.project_cols.size(); c++)
+                if (proj_ref[c]) want[f.project_cols[c]] = true;
+            for (int c = 0; c < NF; c++)
+                if (want[c] && !pred_col[c]) pf_cols.push_back(c);
+            if ((int)pf_cols.size() > 32) pf_cols.resize(32);
+        }
+        const int PF = s.prefetch;
+        auto emit_prefetch = [&](const std::string& ind, const std::string& first_slice) {
+            if (pf_cols.empty()) return;
+            os << ind << "if (pf_on) {\n";
+            os << ind << "    const ral_i64 s0 = base + (ral_i64)(" << first_slice << ") * 32 * RAL_G;\n";
+            os << ind << "    if (s0 < n) {\n";
+            os << ind << "        const ral_i64 rows = (n - s0) < (ral_i64)" << PF << " * 32 * RAL_G ? (n - s0) : (ral_i64)" << PF
+               << " * 32 * RAL_G;\n";
+            for (size_t i = 0; i < pf_cols.size(); i++) {
+                const int c = pf_cols[i];
+                const int w = gdf_dtype_size(f.frame_dtypes[c]);
+                os << ind << "        if (lane == " << i << ") ral_prefetch_l2(" << fdata(c) << " + s0, (unsigned)((rows * " << w
+                   << ") & ~15ll));\n";
+            }
+            os << ind << "    }\n" << ind << "}\n";
+        };
+        os << "        ral_u64 sbase = excl;\n";
+        if (!pf_cols.empty()) {
+            os << "        const bool pf_on = (ral_u64)total * 8u >= (ral_u64)WT;\n";
+            emit_prefetch("        ", "0");
+            emit_prefetch("        ", std::to_string(PF));
+        }
+        os << "#pragma unroll 2\n        for (int j = 0; j < RAL_J; ++j) {\n";
+        if (!pf_cols.empty()) {
+            os << "            if (j % " << PF << " == 0 && j + " << 2 * PF << " < RAL_J) {\n";
+            emit_prefetch("                ", "j + " + std::to_string(2 * PF));
+            os << "            }\n";
+        }
+        os << "            const ral_u32 kb = (kbw[(j * RAL_G) >> 5] >> ((j * RAL_G) & 31)) & GMASK;\n";
+        os << "            const ral_u32 c = __popc(kb);\n";
+        os << "            ral_u32 inc = c;\n";
+        os << "            for (int off = 1; off < 32; off <<= 1) {\n";
+        os << "                const ral_u32 t = __shfl_up_sync(0xffffffffu, inc, off);\n";
+        os << "                if (lane >= off) inc += t;\n            }\n";
+        os << "            const ral_u32 stot = __shfl_sync(0xffffffffu, inc, 31);\n";
+        os << "            if (stot == 0u) continue;\n";
+        os << "            const ral_u64 pos0 = sbase + inc - c;\n";
+        os << "            const ral_i64 r = base + (ral_i64)j * 32 * RAL_G + lane * RAL_G;\n";
+        if (any_gather) {
+            // every gathered column of the slice is loaded first (all loads in flight together);
+            // a slice that keeps many rows is then written through the warp's stage as one
+            // contiguous run per column, a sparse slice with direct stores
             for (int k = 0; k < NO; k++) {
                 if (f.outputs[k].from_project) continue;
-                const char* et = element_ctype(f.frame_dtypes[f.outputs[k].index]);
-                os << "                {\n";
-                os << "                    " << et << "* const st = reinterpret_cast<" << et << "*>(s_stw);\n";
-                os << "                    ral_u32 q = inc - c;\n";
+                const int c = f.outputs[k].index;
+                const char* et = element_ctype(f.frame_dtypes[c]);
+                os << "            " << et << " ga" << k << "[RAL_G];\n";
+                os << "            if (kb) {\n";
+                os << "                if (full) " << (pred_col[c] ? "ral_ldg_keep<" : "ral_ldg<") << et << ", RAL_G>(" << fdata(c)
+                   << ", r, ga" << k << ");\n";
+                os << "                else {\n#pragma unroll\n                    for (int g = 0; g < RAL_G; ++g) ga" << k
+                   << "[g] = (r + g < n) ? " << fdata(c) << "[r + g] : (" << et << ")0;\n                }\n";
+                os << "            }\n";
+            }
+            if (s.stage) {
+                os << "            if (stot >= 16u) {\n";
+                for (int k = 0; k < NO; k++) {
+                    if (f.outputs[k].from_project) continue;
+                    const char* et = element_ctype(f.frame_dtypes[f.outputs[k].index]);
+                    os << "                {\n";
+                    os << "                    " << et << "* const st = reinterpret_cast<" << et << "*>(s_stw);\n";
+                    os << "                    ral_u32 q = inc - c;\n";
+                    os << "#pragma unroll\n                    for (int g = 0; g < RAL_G; ++g)\n";
+                    os << "                        if ((kb >> g) & 1u) st[q++] = ga" << k << "[g];\n";
+                    os << "                    __syncwarp();\n";
+                    os << "                    for (ral_u32 m = lane; m < stot; m += 32) o" << k << "[sbase + m] = st[m];\n";
+                    os << "                    __syncwarp();\n";
+                    os << "                }\n";
+                }
+                os << "            } else\n";
+            }
+            os << "            if (kb) {\n";
+            for (int k = 0; k < NO; k++) {
+                if (f.outputs[k].from_project) continue;
+                os << "                {\n                    ral_u64 pos = pos0;\n";
                 os << "#pragma unroll\n                    for (int g = 0; g < RAL_G; ++g)\n";
-                os << "                        if ((kb >> g) & 1u) st[q++] = ga" << k << "[g];\n";
-                os << "                    __syncwarp();\n";
-                os << "                    for (ral_u32 m = lane; m < stot; m += 32) o" << k << "[sbase + m] = st[m];\n";
-                os << "                    __syncwarp();\n";
+                os << "                        if ((kb >> g) & 1u) o" << k << "[pos++] = ga" << k << "[g];\n";
                 os << "                }\n";
             }
-            os << "            } else\n";
-        }
-        os << "            if (kb) {\n";
-        for (int k = 0; k < NO; k++) {
-            if (f.outputs[k].from_project) continue;
-            os << "                {\n                    ral_u64 pos = pos0;\n";
-            os << "#pragma unroll\n                    for (int g = 0; g < RAL_G; ++g)\n";
-            os << "                        if ((kb >> g) & 1u) o" << k << "[pos++] = ga" << k << "[g];\n";
-            os << "                }\n";
-        }
-        os << "            }\n";
-    }
-    if (any_proj) {
-        if (!proj_vouts.empty()) {
-            os << "            for (int i = 0; i < " << proj_vouts.size() << "; ++i) pw[i] = 0u;\n";
-            os << "            if (lane < RAL_G) {\n";
-            os << "                const ral_i64 w = (base >> 5) + (ral_i64)j * RAL_G + lane;\n";
-            os << "                if ((w << 5) < n) ral_proj_vword(P, w, pw);\n";
             os << "            }\n";
         }
-        os << "            if (kb) {\n";
-        for (size_t c = 0; c < f.project_cols.size(); c++)
-            if (proj_ref[c]) load(os, "                ", f.project_cols[c], "qa" + std::to_string(c));
-        for (size_t c = 0; c < f.project_cols.size(); c++)
-            if (proj_raw[c]) os << "                const ral_u32 qw" << c << " = " << raw_word(f.project_cols[c]) << ";\n";
-        os << "                ral_u64 pos = pos0;\n";
-        os << "#pragma unroll\n                for (int g = 0; g < RAL_G; ++g) {\n";
-        os << "                    if (((kb >> g) & 1u) == 0u) continue;\n";
-        for (int o = 0; o < f.project->n_out; o++) os << "                    " << kind_ctype(proj_kind[o]) << " y" << o << ";\n";
-        os << "                    ral_proj_row(P";
-        for (size_t c = 0; c < f.project_cols.size(); c++)
-            if (proj_ref[c]) os << ", " << widen("qa" + std::to_string(c) + "[g]", f.frame_dtypes[f.project_cols[c]]);
-        for (size_t c = 0; c < f.project_cols.size(); c++)
-            if (proj_raw[c]) os << ", (qw" << c << " >> ((int)(r & 31) + g)) & 1u";
-        for (int o = 0; o < f.project->n_out; o++) os << ", y" << o;
-        os << ");\n";
-        for (int k = 0; k < NO; k++) {
-            if (!f.outputs[k].from_project) continue;
-            const int o = f.outputs[k].index;
-            os << "                    o" << k << "[pos] = " << narrow("y" + std::to_string(o), proj_kind[o], f.outputs[k].dtype) << ";\n";
+        if (any_proj) {
+            if (!proj_vouts.empty()) {
+                os << "            for (int i = 0; i < " << proj_vouts.size() << "; ++i) pw[i] = 0u;\n";
+                os << "            if (lane < RAL_G) {\n";
+                os << "                const ral_i64 w = (base >> 5) + (ral_i64)j * RAL_G + lane;\n";
+                os << "                if ((w << 5) < n) ral_proj_vword(P, w, pw);\n";
+                os << "            }\n";
+            }
+            os << "            if (kb) {\n";
+            for (size_t c = 0; c < f.project_cols.size(); c++)
+                if (proj_ref[c]) load(os, "                ", f.project_cols[c], "qa" + std::to_string(c));
+            for (size_t c = 0; c < f.project_cols.size(); c++)
+                if (proj_raw[c]) os << "                const ral_u32 qw" << c << " = " << raw_word(f.project_cols[c]) << ";\n";
+            os << "                ral_u64 pos = pos0;\n";
+            os << "#pragma unroll\n                for (int g = 0; g < RAL_G; ++g) {\n";
+            os << "                    if (((kb >> g) & 1u) == 0u) continue;\n";
+            for (int o = 0; o < f.project->n_out; o++) os << "                    " << kind_ctype(proj_kind[o]) << " y" << o << ";\n";
+            os << "                    ral_proj_row(P";
+            for (size_t c = 0; c < f.project_cols.size(); c++)
+                if (proj_ref[c]) os << ", " << widen("qa" + std::to_string(c) + "[g]", f.frame_dtypes[f.project_cols[c]]);
+            for (size_t c = 0; c < f.project_cols.size(); c++)
+                if (proj_raw[c]) os << ", (qw" << c << " >> ((int)(r & 31) + g)) & 1u";
+            for (int o = 0; o < f.project->n_out; o++) os << ", y" << o;
+            os << ");\n";
+            for (int k = 0; k < NO; k++) {
+                if (!f.outputs[k].from_project) continue;
+                const int o = f.outputs[k].index;
+                os << "                    o" << k << "[pos] = " << narrow("y" + std::to_string(o), proj_kind[o], f.outputs[k].dtype) << ";\n";
+            }
+            os << "                    ++pos;\n                }\n";
+            os << "            }\n";
         }
-        os << "                    ++pos;\n                }\n";
-        os << "            }\n";
-    }
-    // validity of the masked outputs for this slice, staged in the warp's shared-memory buffer
-    for (int i = 0; i < NVO; i++) {
-        const int k = vouts[i];
-        const FilterOutput& o = f.outputs[k];
-        os << "            {\n";
-        if (o.from_project) {
-            int pi = 0;
-            for (size_t q = 0; q < proj_vouts.size(); q++)
-                if (proj_vouts[q] == o.index) pi = (int)q;
-            os << "                const ral_u32 vw = __shfl_sync(0xffffffffu, pw[" << pi << "], (lane * RAL_G) >> 5);\n";
-        } else {
-            os << "                const ral_u32 vw = kb ? __ldg(" << fvalid(o.index) << " + (r >> 5)) : 0u;\n";
+        // validity of the masked outputs for this slice, staged in the warp's shared-memory buffer
+        for (int i = 0; i < NVO; i++) {
+            const int k = vouts[i];
+            const FilterOutput& o = f.outputs[k];
+            os << "            {\n";
+            if (o.from_project) {
+                int pi = 0;
+                for (size_t q = 0; q < proj_vouts.size(); q++)
+                    if (proj_vouts[q] == o.index) pi = (int)q;
+                os << "                const ral_u32 vw = __shfl_sync(0xffffffffu, pw[" << pi << "], (lane * RAL_G) >> 5);\n";
+            } else {
+                os << "                const ral_u32 vw = kb ? __ldg(" << fvalid(o.index) << " + (r >> 5)) : 0u;\n";
+            }
+            os << "                ral_u32 lb = 0, t = 0;\n";
+            os << "#pragma unroll\n                for (int g = 0; g < RAL_G; ++g)\n";
+            os << "                    if ((kb >> g) & 1u) { lb |= ((vw >> ((int)(r & 31) + g)) & 1u) << t; ++t; }\n";
+            os << "                vcnt[" << i << "] += __popc(lb);\n";
+            os << "                const ral_u32 q = (ral_u32)(pos0 - a0);\n";
+            os << "                const ral_u64 X = (ral_u64)lb << (q & 31);\n";
+            os << "                const ral_u32 qw = q >> 5;\n";
+            os << "                const ral_u32 first = (ral_u32)(sbase - a0) >> 5;\n";
+            os << "#pragma unroll\n                for (int kk = 0; kk <= RAL_G; ++kk) {\n";
+            os << "                    const ral_u32 W = first + kk;\n";
+            os << "                    const ral_u32 part = (t == 0u) ? 0u : (qw == W ? (ral_u32)X : (qw + 1u == W ? (ral_u32)(X >> 32) : 0u));\n";
+            os << "                    const ral_u32 v = __reduce_or_sync(0xffffffffu, part);\n";
+            os << "                    if (lane == 0 && v) s_vbw[" << i << "][W] |= v;\n";
+            os << "                }\n";
+            os << "            }\n";
         }
-        os << "                ral_u32 lb = 0, t = 0;\n";
-        os << "#pragma unroll\n                for (int g = 0; g < RAL_G; ++g)\n";
-        os << "                    if ((kb >> g) & 1u) { lb |= ((vw >> ((int)(r & 31) + g)) & 1u) << t; ++t; }\n";
-        os << "                vcnt[" << i << "] += __popc(lb);\n";
-        os << "                const ral_u32 q = (ral_u32)(pos0 - a0);\n";
-        os << "                const ral_u64 X = (ral_u64)lb << (q & 31);\n";
-        os << "                const ral_u32 qw = q >> 5;\n";
-        os << "                const ral_u32 first = (ral_u32)(sbase - a0) >> 5;\n";
-        os << "#pragma unroll\n                for (int kk = 0; kk <= RAL_G; ++kk) {\n";
-        os << "                    const ral_u32 W = first + kk;\n";
-        os << "                    const ral_u32 part = (t == 0u) ? 0u : (qw == W ? (ral_u32)X : (qw + 1u == W ? (ral_u32)(X >> 32) : 0u));\n";
-        os << "                    const ral_u32 v = __reduce_or_sync(0xffffffffu, part);\n";
-        os << "                    if (lane == 0 && v) s_vbw[" << i << "][W] |= v;\n";
-        os << "                }\n";
-        os << "            }\n";
+        os << "            sbase += stot;\n";
+        os << "        }\n";
     }
-    os << "            sbase += stot;\n";
-    os << "        }\n";
     // flush the staged masks: edge words may be shared with neighbouring chunks
     if (NVO) {
         os << "        __syncwarp();\n";
@@ -936,6 +1060,8 @@ GeneratedKernel generate_filter_kernel(const FilterSpec& f, const Shape& s, bool
         }
         os << "        __syncwarp();\n";
     }
+    // the next chunk's pass 1 rewrites the list the lanes have just read
+    if (dense && !NVO) os << "        __syncwarp();\n";
     os << (item ? "    } while (0);\n" : "    }\n");  // chunk loop
 
     // ---- valid-bit counts: one atomic per warp and masked output

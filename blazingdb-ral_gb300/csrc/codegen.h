@@ -28,6 +28,10 @@ struct Shape {
     // filter kernels: slices of pass 2 prefetched into L2 ahead (0, the default: none -- measured
     // slower at 4, 8 and 16 slices: 500M rows at s = 0.5 ran 5.39 / 5.71 / 5.79 ms against 5.06)
     int prefetch = 0;
+    // filter kernels: pass 2 walks a shared-memory list of the chunk's kept rows, 32 at a time,
+    // so every lane evaluates a kept row and stores are contiguous (1), or evaluates its own G
+    // rows of each slice, skipping dropped ones (0); -1: 1 when the filter has a projection
+    int dense = -1;
 };
 
 // Slot order of the kernel's parameter block (all 8-byte slots).

@@ -58,9 +58,11 @@ const std::string& soft_fp_define(bool soft) {
     static const std::string d = [] {
         const char* e = std::getenv("RAL_SOFT_FP");
         std::string out = std::string("#define RAL_SOFT_FP ") + ((e && std::string(e) == "0") ? "0" : "1") + "\n";
-        // RAL_SOFT_INT_DIV=1|2: integer-only 64-bit division for every / for 32-bit divisors
+        // RAL_SOFT_INT_DIV=0|1|2|3: the compiler's 64-bit division / integer-only division for
+        // every divisor / for 32-bit divisors / for divisors below 2^16 (the default)
         const char* i = std::getenv("RAL_SOFT_INT_DIV");
-        if (i && (std::string(i) == "1" || std::string(i) == "2")) out += std::string("#define RAL_SOFT_INT_DIV ") + i + "\n";
+        if (i && (std::string(i) == "0" || std::string(i) == "1" || std::string(i) == "2" || std::string(i) == "3"))
+            out += std::string("#define RAL_SOFT_INT_DIV ") + i + "\n";
         return out;
     }();
     return d;

@@ -77,6 +77,9 @@ extern "C" __global__ void ral_softfp_selftest(unsigned long long* out, long lon
         if (ib == 0 || ib == -1) ib = 7;
         if (ral_sf_div64(ia, ib) != ia / ib || ral_sf_mod64(ia, ib) != ia % ib)
             st_bad(out, 10, __longlong_as_double(ia), __longlong_as_double(ib));
+        const long long ic = (long long)(1 + (r2 >> 40) % 65535) * ((r2 & 2) ? -1 : 1);
+        if (ral_sf_div64_16(ia, ic) != ia / ic || ral_sf_mod64_16(ia, ic) != ia % ic)
+            st_bad(out, 10, __longlong_as_double(ia), __longlong_as_double(ic));
         // sin / cos: approximations on both sides, so within 2 ulp of the library's
         const double t = (r3 & 1) ? a : ldexp((double)(r0 >> 11), -53) * 2e6 * ((r1 & 1) ? -1.0 : 1.0);
         if (t == t && t - t == 0.0) {

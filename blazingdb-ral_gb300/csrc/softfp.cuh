@@ -404,6 +404,59 @@ RAL_SF void ral_sf_udivmod64_32(unsigned long long n, unsigned int d, unsigned l
 }
 
 
+// n / d and n % d for 1 <= d < 2^16 with 32-bit operations only.  m = floor((2^32 - 1) / d) lies
+// in [2^32 / d - 1, 2^32 / d], so for any 32-bit x the high word of x * m is floor(x / d) or one
+// less (x * m / 2^32 > x / d - x / 2^32 > x / d - 1), and one remainder test corrects it.  The
+// dividend is taken as 32 + 16 + 16 bits, most significant first (long division in base 2^16
+// after the first word): each partial remainder is below d < 2^16, so the next partial dividend
+// (remainder << 16 | next 16 bits) stays below 2^32 and its quotient below 2^16.
+RAL_SF unsigned int ral_sf_umulhi32(unsigned int a, unsigned int b) {
+#if defined(__CUDA_ARCH__)
+    return __umulhi(a, b);
+#else
+    return (unsigned int)(((unsigned long long)a * b) >> 32);
+#endif
+}
+
+RAL_SF unsigned int ral_sf_divstep16(unsigned int x, unsigned int d, unsigned int m, unsigned int* r) {
+    unsigned int q = ral_sf_umulhi32(x, m);
+    unsigned int rr = x - q * d;  // in [0, 2d)
+    if (rr >= d) {
+        q += 1u;
+        rr -= d;
+    }
+    *r = rr;
+    return q;
+}
+
+RAL_SF void ral_sf_udivmod64_16(unsigned long long n, unsigned int d, unsigned long long* q_out,
+                                unsigned long long* r_out) {
+    const unsigned int m = 0xffffffffu / d;
+    unsigned int r;
+    const unsigned int q2 = ral_sf_divstep16((unsigned int)(n >> 32), d, m, &r);
+    const unsigned int lo = (unsigned int)n;
+    const unsigned int q1 = ral_sf_divstep16((r << 16) | (lo >> 16), d, m, &r);
+    const unsigned int q0 = ral_sf_divstep16((r << 16) | (lo & 0xffffu), d, m, &r);
+    *q_out = ((unsigned long long)q2 << 32) | ((unsigned long long)q1 << 16) | q0;
+    *r_out = r;
+}
+
+// Signed quotient and remainder (C semantics) for 1 <= |b| < 2^16; b == -1 is left to the caller.
+RAL_SF long long ral_sf_div64_16(long long a, long long b) {
+    const unsigned long long ua = a < 0 ? 0ull - (unsigned long long)a : (unsigned long long)a;
+    const unsigned int ub = (unsigned int)(b < 0 ? 0ll - b : b);
+    unsigned long long q, r;
+    ral_sf_udivmod64_16(ua, ub, &q, &r);
+    return ((a < 0) != (b < 0)) ? (long long)(0ull - q) : (long long)q;
+}
+RAL_SF long long ral_sf_mod64_16(long long a, long long b) {
+    const unsigned long long ua = a < 0 ? 0ull - (unsigned long long)a : (unsigned long long)a;
+    const unsigned int ub = (unsigned int)(b < 0 ? 0ll - b : b);
+    unsigned long long q, r;
+    ral_sf_udivmod64_16(ua, ub, &q, &r);
+    return a < 0 ? (long long)(0ull - r) : (long long)r;
+}
+
 // n / d and n % d for d >= 1, exactly, by the same reciprocal method: a float seed for
 // 2^127 / (d normalised), two Newton steps in 64-bit fixed point, a quotient estimate within a
 // few units and an exact correction from the remainder.

@@ -76,6 +76,13 @@ int main(int argc, char** argv) {
             std::snprintf(cdiv64.first, sizeof cdiv64.first, "%lld / %lld: want %lld %lld got %lld %lld", a, b, a / b,
                           a % b, ral_sf_div64(a, b), ral_sf_mod64(a, b));
     };
+    Counter cd16{"div64_16"};
+    auto check_d16 = [&](long long a, long long b) {  // 1 <= |b| < 2^16
+        cd16.n++;
+        if ((a / b != ral_sf_div64_16(a, b) || a % b != ral_sf_mod64_16(a, b)) && cd16.bad++ == 0)
+            std::snprintf(cd16.first, sizeof cd16.first, "%lld / %lld: want %lld %lld got %lld %lld", a, b, a / b,
+                          a % b, ral_sf_div64_16(a, b), ral_sf_mod64_16(a, b));
+    };
     Counter cd32{"div64_32"};
     auto check_d32 = [&](unsigned long long n, unsigned int d) {
         if (d == 0) return;
@@ -177,6 +184,16 @@ int main(int argc, char** argv) {
         check_d32(rng(), 0xffffffffu - (unsigned)(rng() % 3));
         check_d32(rng(), (1u << (rng() % 32)) + (unsigned)(rng() % 3) - 1u);
         check_div64(INT64_MAX, xb);
+        // divisors below 2^16: every size, powers of two and their neighbours, the extremes
+        const long long d16 = (long long)(1 + (rng() >> (48 + rng() % 16)) % 65535) * ((rng() & 1) ? -1 : 1);
+        const long long p16 = (long long)(1ull << (rng() % 16)) + (long long)(rng() % 3) - 1;
+        for (long long dd : {d16, p16 > 0 ? p16 : 1ll, 65535ll, -65535ll, 1ll, 2ll, -2ll}) {
+            if (dd == -1) continue;
+            check_d16(xa, dd);
+            check_d16(INT64_MIN, dd);
+            check_d16(INT64_MAX, dd);
+            check_d16((long long)rng(), dd);
+        }
         // float -> double
         cf2d.n++;
         const float f = flt((uint32_t)rng());
@@ -192,6 +209,6 @@ int main(int argc, char** argv) {
     for (double v : {0.7853981633974483, 0.7853981633974482, 0.7853981633974484, 0x1p-26, 0x1p-27, 0x1p20,
                      0x1.fffffffffffffp19, 3.141592653589793, 1.5707963267948966, 1e6, -1e6})
         check_trig(v);
-    for (Counter* c : {&csin, &cd32, &cdiv64, &cdiv, &cfloor, &cceil, &cabs, &ccmp, &ci2d, &cd2i, &cf2d, &cd2f, &czero}) c->report();
+    for (Counter* c : {&csin, &cd16, &cd32, &cdiv64, &cdiv, &cfloor, &cceil, &cabs, &ccmp, &ci2d, &cd2i, &cf2d, &cd2f, &czero}) c->report();
     return 0;
 }

@@ -93,7 +93,8 @@ FILTER_CASES = [
 ]
 
 
-@pytest.mark.parametrize("tune", ["", "S=1", "J=8,U=2,T=128,B=4", "J=64,U=8,T=512,B=1,S=1", "P=8", "P=4,J=16"])
+@pytest.mark.parametrize("tune", ["", "S=1", "J=8,U=2,T=128,B=4", "J=64,U=8,T=512,B=1,S=1", "P=8", "P=4,J=16",
+                                  "D=1", "D=0", "D=1,J=8,T=128"])
 @pytest.mark.parametrize("case", FILTER_CASES, ids=[c[0] for c in FILTER_CASES])
 def test_filter_kernels_compile(case, tune, monkeypatch):
     _, dtypes, nullable, fq, pq = case
@@ -101,3 +102,19 @@ def test_filter_kernels_compile(case, tune, monkeypatch):
     src, log = ralgpu.debug_filter_source(dtypes, nullable, fq, pq, compile=True)
     assert "ral_filter_" in src and "ral_lookback" in src
     assert spills(log) <= 64, log
+
+
+def test_dense_pass_two_is_the_default_with_a_projection_and_fits_shared_memory(monkeypatch):
+    """A projection makes pass 2 walk the kept-row list; a filter without one keeps the slice-wise
+    pass; a shape whose per-block lists would not fit static shared memory falls back to it."""
+    monkeypatch.delenv("RAL_FILTER_TUNE", raising=False)
+    p = W.fused_project_program()
+    src, _ = ralgpu.debug_filter_source(p.input_dtypes, [1] * 5, W.filter_project_filter(0.5),
+                                        W.FILTER_PROJECT_PROJECT)
+    assert "s_lst[act ? k : k0]" in src and "kbw[" not in src
+    src, _ = ralgpu.debug_filter_source(W.FILTER_GATHER_DTYPES, [1] * 6, W.filter_gather_query(0.5), None)
+    assert "s_lst" not in src and "kbw[" in src
+    monkeypatch.setenv("RAL_FILTER_TUNE", "J=64,T=512,B=1")
+    src, log = ralgpu.debug_filter_source(p.input_dtypes, [1] * 5, W.filter_project_filter(0.5),
+                                          W.FILTER_PROJECT_PROJECT, compile=True)
+    assert "s_lst" not in src and "kbw[" in src and spills(log) <= 64
