@@ -76,7 +76,7 @@ std::string conv(const std::string& x, Kind from, Kind to) {
 std::string to_d(const std::string& x, Kind k) { return conv(x, k, Kind::F64); }
 std::string to_i(const std::string& x, Kind k) { return conv(x, k, Kind::I64); }
 std::string conv_bool(const std::string& b, Kind to) {
-    return to == Kind::F64 ? "((" + b + ") ? 1.0 : 0.0)" : "((ral_i64)(" + b + "))";
+    return to == Kind::F64 ? "ral_b2d(" + b + ")" : "((ral_i64)(" + b + "))";
 }
 
 // Data-path op emission shared by every kernel kind.
@@ -85,6 +85,14 @@ struct OpEmitter {
     const ParamLayout& L;
     std::vector<std::string> name;   // current SSA value of each register
     std::vector<Kind> kind;
+    // registers whose current value is 0 or 1 (comparisons, NOT, IS [NOT] NULL, products of two
+    // such): converted to double by a select, and a double product with one skips the multiply
+    std::vector<bool> b01;
+    // ABS results not yet emitted: the operand's expression.  A double add, subtract or multiply
+    // reads fabs(operand), which the compiler folds into the instruction as a free modifier; any
+    // other reader (a stored output, a comparison, a division) gets the integer-pipe version,
+    // emitted once where first needed.
+    std::vector<std::string> absrc;
 
     OpEmitter(const Program& prog, const ParamLayout& layout) : p(prog), L(layout) {
         int maxreg = p.n_in;
@@ -92,6 +100,8 @@ struct OpEmitter {
         for (int16_t f : p.final_pos) maxreg = std::max<int>(maxreg, f);
         name.assign(maxreg + 1, "");
         kind.assign(maxreg + 1, Kind::I64);
+        b01.assign(maxreg + 1, false);
+        absrc.assign(maxreg + 1, "");
         for (int c = 0; c < p.n_in; c++) {
             name[c] = "x" + std::to_string(c);
             kind[c] = dtype_kind(p.inputs[c].dtype);
@@ -104,8 +114,25 @@ struct OpEmitter {
             const Op& op = p.ops[k];
             std::string l, r;
             Kind lk = op.lk, rk = op.rk;
+            const bool l01 = op.left >= 0 && b01[op.left];
+            const bool r01 = !op.unary && op.right >= 0 && b01[op.right];
+            // operands a deferred ABS may reach as fabs(): double add / subtract / multiply
+            // (not a multiply by a 0/1 value, which is integer work)
+            const bool farith = !op.unary && (lk == Kind::F64 || rk == Kind::F64) &&
+                                (op.bop == GDF_ADD || op.bop == GDF_SUB || (op.bop == GDF_MUL && l01 == r01));
+            auto fetch = [&](int reg, bool fold) -> std::string {
+                if (!absrc[reg].empty()) {
+                    if (fold) return "fabs(" + absrc[reg] + ")";
+                    const std::string t = "ta" + std::to_string(k) + "_" + std::to_string(reg);
+                    os << indent << "const double " << t << " = ral_dfabs(" << absrc[reg] << ");\n";
+                    name[reg] = t;
+                    absrc[reg].clear();
+                }
+                return name[reg];
+            };
+            const bool abs_op = op.unary && op.uop == BLZ_ABS && op.left >= 0 && lk == Kind::F64 && op.ok == Kind::F64;
             if (op.left >= 0) {
-                l = name[op.left];
+                l = fetch(op.left, (farith && lk == Kind::F64) || abs_op);
             } else if (op.left == SCALAR_INDEX) {
                 l = "sl" + std::to_string(k);
                 os << indent << "const " << kind_ctype(lk) << " " << l << " = "
@@ -114,9 +141,16 @@ struct OpEmitter {
             } else {
                 l = lk == Kind::F64 ? "0.0" : "((ral_i64)0)";
             }
+            if (abs_op) {  // deferred: see absrc
+                absrc[op.out] = l;
+                name[op.out].clear();
+                kind[op.out] = Kind::F64;
+                b01[op.out] = false;
+                continue;
+            }
             if (!op.unary) {
                 if (op.right >= 0) {
-                    r = name[op.right];
+                    r = fetch(op.right, farith && rk == Kind::F64);
                 } else if (op.right == SCALAR_INDEX) {
                     r = "sr" + std::to_string(k);
                     os << indent << "const " << kind_ctype(rk) << " " << r << " = "
@@ -128,22 +162,38 @@ struct OpEmitter {
             }
             const Kind ok = op.ok;
             std::string e;
+            bool res01 = false;
             if (!op.unary) {
                 const bool f = (lk == Kind::F64) || (rk == Kind::F64);
+                // a 0/1 operand as a double, and as a truth value
+                auto d01 = [&](const std::string& v, Kind k) {
+                    return k == Kind::I64 ? "ral_b2d((" + v + ") != 0)" : v;
+                };
+                auto t01 = [&](const std::string& v, Kind k) {
+                    return k == Kind::I64 ? "((" + v + ") != 0)" : "(!ral_dzero(" + v + "))";
+                };
+                const std::string ld = l01 ? d01(l, lk) : to_d(l, lk);
+                const std::string rd = r01 ? d01(r, rk) : to_d(r, rk);
                 auto arith = [&](const char* dop, const char* iop) {
-                    if (f) return conv(std::string(dop) + "(" + to_d(l, lk) + ", " + to_d(r, rk) + ")", Kind::F64, ok);
+                    if (f) return conv(std::string(dop) + "(" + ld + ", " + rd + ")", Kind::F64, ok);
                     return conv(std::string(iop) + "(" + l + ", " + r + ")", Kind::I64, ok);
                 };
                 // double comparisons go through the prelude's ral_d* functions (integer-pipe
                 // versions unless RAL_SOFT_FP is 0)
                 auto cmp = [&](const char* c, const char* dfn) {
-                    if (f) return conv_bool(std::string(dfn) + "(" + to_d(l, lk) + ", " + to_d(r, rk) + ")", ok);
+                    res01 = true;
+                    if (f) return conv_bool(std::string(dfn) + "(" + ld + ", " + rd + ")", ok);
                     return conv_bool(l + " " + c + " " + r, ok);
                 };
                 switch (op.bop) {
                 case GDF_ADD: e = arith("__dadd_rn", "ral_addi"); break;
                 case GDF_SUB: e = arith("__dsub_rn", "ral_subi"); break;
-                case GDF_MUL: e = arith("__dmul_rn", "ral_muli"); break;
+                case GDF_MUL:
+                    if (f && l01 && !r01) e = conv("ral_dmul01(" + t01(l, lk) + ", " + rd + ")", Kind::F64, ok);
+                    else if (f && r01 && !l01) e = conv("ral_dmul01(" + t01(r, rk) + ", " + ld + ")", Kind::F64, ok);
+                    else e = arith("__dmul_rn", "ral_muli");
+                    res01 = l01 && r01;
+                    break;
                 case GDF_DIV: case GDF_FLOOR_DIV: e = arith("ral_ddiv", "ral_divi"); break;
                 case GDF_MOD: e = conv("ral_modi(" + to_i(l, lk) + ", " + to_i(r, rk) + ")", Kind::I64, ok); break;
                 case GDF_POW:
@@ -164,7 +214,7 @@ struct OpEmitter {
                 default: throw std::runtime_error("codegen: unsupported binary operator");
                 }
             } else {
-                const std::string d = to_d(l, lk);
+                const std::string d = l01 && lk == Kind::I64 ? "ral_b2d((" + l + ") != 0)" : to_d(l, lk);
                 const bool d32 = op.ltype == GDF_DATE32;
                 auto math = [&](const std::string& fn) { return conv(fn + "(" + d + ")", Kind::F64, ok); };
                 switch (op.uop) {
@@ -180,22 +230,32 @@ struct OpEmitter {
                 case BLZ_ABS: e = math("ral_dfabs"); break;
                 case BLZ_LN: e = math("log"); break;
                 case BLZ_LOG: e = math("log10"); break;
-                case BLZ_NOT: e = conv_bool(lk == Kind::F64 ? "ral_dzero(" + l + ")" : "(" + l + " == 0)", ok); break;
+                case BLZ_NOT: e = conv_bool(lk == Kind::F64 ? "ral_dzero(" + l + ")" : "(" + l + " == 0)", ok); res01 = true; break;
                 case BLZ_YEAR: e = conv(std::string(d32 ? "ral_year32(" : "ral_year64(") + to_i(l, lk) + ")", Kind::I64, ok); break;
                 case BLZ_MONTH: e = conv(std::string(d32 ? "ral_month32(" : "ral_month64(") + to_i(l, lk) + ")", Kind::I64, ok); break;
                 case BLZ_DAY: e = conv(std::string(d32 ? "ral_day32(" : "ral_day64(") + to_i(l, lk) + ")", Kind::I64, ok); break;
                 case BLZ_HOUR: e = d32 ? conv("((ral_i64)0)", Kind::I64, ok) : conv("ral_hour64(" + to_i(l, lk) + ")", Kind::I64, ok); break;
                 case BLZ_MINUTE: e = d32 ? conv("((ral_i64)0)", Kind::I64, ok) : conv("ral_minute64(" + to_i(l, lk) + ")", Kind::I64, ok); break;
                 case BLZ_SECOND: e = d32 ? conv("((ral_i64)0)", Kind::I64, ok) : conv("ral_second64(" + to_i(l, lk) + ")", Kind::I64, ok); break;
-                case BLZ_IS_NULL: e = conv_bool("rb" + std::to_string(op.left) + " == 0u", ok); break;
-                case BLZ_IS_NOT_NULL: e = conv_bool("rb" + std::to_string(op.left) + " != 0u", ok); break;
-                default: e = conv(l, lk, ok); break;  // copy with conversion
+                case BLZ_IS_NULL: e = conv_bool("rb" + std::to_string(op.left) + " == 0u", ok); res01 = true; break;
+                case BLZ_IS_NOT_NULL: e = conv_bool("rb" + std::to_string(op.left) + " != 0u", ok); res01 = true; break;
+                default: e = conv(l, lk, ok); res01 = l01; break;  // copy with conversion
                 }
             }
             const std::string t = "t" + std::to_string(k);
             os << indent << "const " << kind_ctype(ok) << " " << t << " = " << e << ";\n";
             name[op.out] = t;
             kind[op.out] = ok;
+            b01[op.out] = res01;
+            absrc[op.out].clear();
+        }
+        // deferred ABS values that are outputs of the program
+        for (int16_t f : p.final_pos) {
+            if (f < 0 || absrc[f].empty()) continue;
+            const std::string t = "tf" + std::to_string(f);
+            os << indent << "const double " << t << " = ral_dfabs(" << absrc[f] << ");\n";
+            name[f] = t;
+            absrc[f].clear();
         }
     }
 };

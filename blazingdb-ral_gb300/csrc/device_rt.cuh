@@ -78,6 +78,21 @@ RAL_FI double ral_dfabs(double x) { return ral_sf_fabs(x); }
 RAL_FI bool ral_dzero(double x) { return ral_sf_is_zero(x); }
 RAL_FI double ral_bits_d(ral_i64 b) { return __longlong_as_double(b); }
 RAL_FI ral_i64 ral_d_bits(double d) { return __double_as_longlong(d); }
+// a truth value as 1.0 / 0.0 from the bits of 1.0 and an opaque mask (a select between the two
+// constants is turned into an integer -> double conversion on the FP64 pipe)
+RAL_FI double ral_b2d(bool b) {
+    return __longlong_as_double((long long)(ral_sf_opaque(0ull - (ral_u64)b) & 0x3ff0000000000000ull));
+}
+// (one ? 1.0 : 0.0) * x, the same bits as the multiply: a finite x times 1.0 is x and times 0.0
+// is a zero with x's sign; an infinite or NaN x takes the FP64 instruction (NaN, or inf * 1.0).
+// The 0/1 operand comes from a comparison or a logical operator of the program.  The rare case is
+// a call, so that the compiler does not issue its multiply, predicated off, for every row.
+static __device__ __noinline__ double ral_dmul_rare(double a, double b) { return __dmul_rn(a, b); }
+RAL_FI double ral_dmul01(bool one, double x) {
+    const ral_u64 b = ral_sf_bits(x);
+    if ((b & 0x7ff0000000000000ull) == 0x7ff0000000000000ull) return ral_dmul_rare(ral_b2d(one), x);
+    return one ? x : __longlong_as_double((long long)(b & 0x8000000000000000ull));
+}
 
 // ---- integer ops (two's complement wrap, as the GPU executes them) -------------------------
 RAL_FI ral_i64 ral_addi(ral_i64 a, ral_i64 b) { return (ral_i64)((ral_u64)a + (ral_u64)b); }

@@ -321,19 +321,28 @@ std::string filter_tune() {
 
 void apply_tune(Shape& sh, const std::string& t) { apply_shape_tune(sh, t); }
 
+// Launch shape of a fused filter over n rows (n < 0: large), before RAL_FILTER_TUNE.
+Shape default_filter_shape(const FilterSpec& spec, bool aligned16, int64_t n) {
+    const bool have_proj = spec.project != nullptr;
+    Shape sh;
+    sh.G = aligned16 ? 16 / filter_max_width(spec) : 1;
+    sh.threads = 256;
+    // With a projection pass 2 walks the chunk's kept-row list (Shape::dense): 1024-row chunks and
+    // six resident blocks (40 registers; the per-warp lists of 2048-row chunks would leave room for
+    // five) measured fastest -- 200M rows, s = 0.01 / 0.5 / 0.99: 0.86 / 2.09 / 3.41 ms against
+    // 0.91 / 2.24 / 3.52 with 2048-row chunks and four blocks.  A gather-only filter keeps the
+    // slice-wise pass 2 and is fastest at 2048-row chunks and two blocks.
+    const int jmax = std::max(1, (have_proj ? 32 : 64) / sh.G);
+    sh.J = n < 0 ? jmax : std::max(1, std::min(jmax, chunk_slices(n, sh.G)));
+    sh.min_blocks = have_proj ? 6 : 2;
+    sh.unroll = have_proj ? 2 : 4;
+    sh.stage = false;
+    return sh;
+}
+
 // Finishes a PreparedFilter whose spec (frame, predicate, projection, outputs) is filled in.
 int prepare_kernel(PreparedFilter& pf, bool aligned16, int64_t n) {
-    Shape sh;
-    sh.G = aligned16 ? 16 / filter_max_width(pf.spec) : 1;
-    sh.J = std::max(1, std::min(64 / sh.G, chunk_slices(n, sh.G)));
-    sh.threads = 256;
-    // a projection makes the kernel latency-bound (loads and the double operations of every kept
-    // row): four resident blocks and a shorter predicate unroll measured fastest with one
-    // (200M rows, s = 0.5 / 0.99: 36.7 / 36.4 G rows/s against 30.3 / 29.5 at two blocks);
-    // a gather-only filter is fastest at two blocks
-    sh.min_blocks = pf.have_proj ? 4 : 2;
-    sh.unroll = pf.have_proj ? 2 : 4;
-    sh.stage = false;
+    Shape sh = default_filter_shape(pf.spec, aligned16, n);
     apply_tune(sh, filter_tune());
     pf.gk = generate_filter_kernel(pf.spec, sh);
     std::string err;
@@ -519,12 +528,7 @@ int debug_filter_source(gdf_column* const* frame, int ncols, const char* filter_
             spec.outputs.push_back(o);
         }
     }
-    Shape sh;
-    sh.G = 16 / filter_max_width(spec);
-    sh.J = 64 / sh.G;
-    sh.threads = 256;
-    sh.min_blocks = spec.project ? 4 : 2;
-    sh.unroll = spec.project ? 2 : 4;
+    Shape sh = default_filter_shape(spec, true, -1);
     apply_tune(sh, filter_tune());
     GeneratedKernel gk = generate_filter_kernel(spec, sh);
     source = std::string(jit_prelude()) + "\n" + gk.source;

@@ -13,9 +13,9 @@
 // function's fast path (zero, subnormal, infinite or NaN operands, subnormal or overflowing
 // quotients) fall back to the hardware instruction.
 //
-// Methods: division by a Newton-Raphson reciprocal in 64-bit fixed point seeded from a
-// single-precision reciprocal estimate, then an exact remainder correction of the quotient and
-// round-to-nearest-even from the remainder (the schoolbook method of e.g. Muller et al.,
+// Methods: division by a Newton-Raphson reciprocal (one step in 32-bit, one in 64-bit fixed
+// point) seeded from a single-precision reciprocal estimate, then an exact remainder correction of
+// the quotient and round-to-nearest-even from the remainder (the schoolbook method of e.g. Muller et al.,
 // "Handbook of Floating-Point Arithmetic", ch. 9); comparisons on the sign-magnitude keys of the
 // bit patterns; conversions by normalising shifts with explicit round-to-nearest-even.
 //
@@ -42,6 +42,20 @@ RAL_SF unsigned long long ral_sf_bits(double d) {
     unsigned long long b;
     __builtin_memcpy(&b, &d, 8);
     return b;
+#endif
+}
+
+// The bits of a double through an opaque move, for the functions whose tests on the bits the
+// compiler would otherwise turn back into floating-point operations on the FP64 pipe (a zero test
+// into an FP64 compare, a sign mask into an FP64 absolute value, an exponent test into a NaN
+// compare).  Elsewhere the plain bits keep register pressure lower.
+RAL_SF unsigned long long ral_sf_obits(double d) {
+#if defined(__CUDA_ARCH__)
+    unsigned long long b;
+    asm("mov.b64 %0, %1;" : "=l"(b) : "d"(d));
+    return b;
+#else
+    return ral_sf_bits(d);
 #endif
 }
 
@@ -127,16 +141,24 @@ RAL_SF double ral_sf_div(double a, double b) {
         ma <<= 1;
         e -= 1;
     }
-    // reciprocal y ~ 2^116 / mb in (2^63, 2^64]: float seed, then two Newton steps
-    const float seed = ral_sf_rcp_estimate((float)(unsigned)(mb >> 29));  // ~ 2^29 / mb, in (2^-24, 2^-23]
-    // y0 = seed * 2^87 assembled from the float's fields (no float -> int64 conversion, which
-    // would run on the FP64 pipe)
+    // reciprocal y ~ 2^116 / mb in [2^63, 2^64): a float seed for the divisor's top 32 bits d32,
+    // one Newton step in 32-bit fixed point (v ~ 2^63 / d32 to ~31 bits), one in 64-bit (~60 bits)
+    const unsigned d32 = (unsigned)(mb >> 21);                        // in [2^31, 2^32)
+    const float seed = ral_sf_rcp_estimate((float)d32);              // ~ 1 / d32
+    // v0 = seed * 2^63 assembled from the float's fields (no float -> int conversion)
     const unsigned sb = ral_sf_fbits(seed);
-    const int sh = (int)((sb >> 23) & 0xffu) - 63;  // 40 for seeds below 2^-23
-    const unsigned long long sm = (unsigned long long)((sb & 0x7fffffu) | 0x800000u);
-    unsigned long long y = sh >= 41 ? 0xffffffffffffffffull : (sh <= 0 ? sm : sm << sh);
-#pragma unroll
-    for (int it = 0; it < 2; ++it) {
+    const int sh = (int)((sb >> 23) & 0xffu) - 87;                   // 7..9
+    unsigned long long v = (unsigned long long)((sb & 0x7fffffu) | 0x800000u) << (sh > 0 ? sh : 0);
+    if (v > 0xffffffffull) v = 0xffffffffull;
+    {
+        const long long e = (long long)((1ull << 63) - (unsigned long long)d32 * v);  // |e| < 2^43
+        long long v1 = (long long)v + (((long long)v * (e >> 21)) >> 42);
+        if (v1 > 0xffffffffll) v1 = 0xffffffffll;
+        if (v1 < 0x80000000ll) v1 = 0x80000000ll;
+        v = (unsigned long long)v1;
+    }
+    unsigned long long y = v << 32;
+    {
         // err = 2^116 - mb * y, as a signed value scaled by 2^-52
         const unsigned long long plo = mb * y, phi = ral_sf_umulh(mb, y);
         // (2^116 - P) >> 52 = (2^64 - (P >> 52)) using the 128-bit P = phi:plo
@@ -147,24 +169,18 @@ RAL_SF double ral_sf_div(double a, double b) {
         const unsigned long long corr = ral_sf_umulh(y, mag);
         y = err < 0 ? y - corr : y + corr;
     }
-    // Q ~ ma * 2^53 / mb = (ma * y) >> 63, then exact correction from the remainder
+    // Q ~ ma * 2^53 / mb = (ma * y) >> 63.  With y within ~2^-60 of 2^116 / mb the estimate is
+    // off by at most one either way, and one remainder test per direction corrects it.
     const unsigned long long qlo = ma * y, qhi = ral_sf_umulh(ma, y);
     unsigned long long q = (qhi << 1) | (qlo >> 63);
     // R = ma * 2^53 - q * mb (small: the low 64 bits of both products suffice)
     long long r = (long long)((ma << 53) - q * mb);
-#pragma unroll
-    for (int k = 0; k < 3; ++k) {
-        if (r < 0) {
-            q -= 1;
-            r += (long long)mb;
-        }
-    }
-#pragma unroll
-    for (int k = 0; k < 3; ++k) {
-        if (r >= (long long)mb) {
-            q += 1;
-            r -= (long long)mb;
-        }
+    if (r < 0) {
+        q -= 1;
+        r += (long long)mb;
+    } else if (r >= (long long)mb) {
+        q += 1;
+        r -= (long long)mb;
     }
     // q in [2^53, 2^54): 53 significand bits, one rounding bit, sticky = r != 0
     unsigned long long m = q >> 1;
@@ -178,15 +194,25 @@ RAL_SF double ral_sf_div(double a, double b) {
     return ral_sf_double(((A ^ B) & RAL_SF_SIGN) | ((unsigned long long)e << 52) | (m & RAL_SF_FRAC));
 }
 
+// An integer the compiler cannot see through.  A double chosen between two constants (0.0, 1.0,
+// -1.0) by a truth value is otherwise turned into an integer -> double conversion, which runs on
+// the FP64 pipe; the callers instead AND a constant's bits with an opaque mask.
+RAL_SF unsigned long long ral_sf_opaque(unsigned long long x) {
+#if defined(__CUDA_ARCH__)
+    asm("mov.b64 %0, %1;" : "=l"(x) : "l"(x));
+#endif
+    return x;
+}
+
 // ---- rounding to an integer ------------------------------------------------------------------
 
 RAL_SF double ral_sf_floor(double x) {
-    unsigned long long A = ral_sf_bits(x);
+    unsigned long long A = ral_sf_obits(x);
     const int e = (int)((A >> 52) & 0x7ff);
     if (e >= 1075) return x;  // integral, infinite or NaN
-    if (e < 1023) {           // |x| < 1
-        if ((A << 1) == 0) return x;                                    // +-0
-        return (A >> 63) ? ral_sf_double(0xbff0000000000000ull) : 0.0;  // -1 or +0
+    if (e < 1023) {  // |x| < 1: +-0 stays, otherwise -1 or +0
+        const unsigned long long neg = ral_sf_opaque((unsigned long long)((long long)A >> 63));
+        return ral_sf_double((A << 1) == 0 ? A : (neg & 0xbff0000000000000ull));
     }
     const unsigned long long mask = RAL_SF_FRAC >> (e - 1023);
     if ((A & mask) == 0) return x;
@@ -195,12 +221,12 @@ RAL_SF double ral_sf_floor(double x) {
 }
 
 RAL_SF double ral_sf_ceil(double x) {
-    unsigned long long A = ral_sf_bits(x);
+    unsigned long long A = ral_sf_obits(x);
     const int e = (int)((A >> 52) & 0x7ff);
     if (e >= 1075) return x;
-    if (e < 1023) {
-        if ((A << 1) == 0) return x;
-        return (A >> 63) ? ral_sf_double(RAL_SF_SIGN) : 1.0;  // -0 or 1
+    if (e < 1023) {  // |x| < 1: +-0 stays, otherwise -0 or 1
+        const unsigned long long neg = ral_sf_opaque((unsigned long long)((long long)A >> 63));
+        return ral_sf_double((A << 1) == 0 ? A : (0x3ff0000000000000ull ^ (neg & (0x3ff0000000000000ull ^ RAL_SF_SIGN))));
     }
     const unsigned long long mask = RAL_SF_FRAC >> (e - 1023);
     if ((A & mask) == 0) return x;
@@ -208,7 +234,7 @@ RAL_SF double ral_sf_ceil(double x) {
     return ral_sf_double(A);
 }
 
-RAL_SF double ral_sf_fabs(double x) { return ral_sf_double(ral_sf_bits(x) & ~RAL_SF_SIGN); }
+RAL_SF double ral_sf_fabs(double x) { return ral_sf_double(ral_sf_obits(x) & ~RAL_SF_SIGN); }
 
 // ---- comparisons -------------------------------------------------------------------------------
 
@@ -221,22 +247,22 @@ RAL_SF long long ral_sf_key(unsigned long long A) {
 }
 
 RAL_SF bool ral_sf_lt(double a, double b) {
-    const unsigned long long A = ral_sf_bits(a), B = ral_sf_bits(b);
+    const unsigned long long A = ral_sf_obits(a), B = ral_sf_obits(b);
     return !ral_sf_isnan_bits(A) && !ral_sf_isnan_bits(B) && ral_sf_key(A) < ral_sf_key(B);
 }
 RAL_SF bool ral_sf_le(double a, double b) {
-    const unsigned long long A = ral_sf_bits(a), B = ral_sf_bits(b);
+    const unsigned long long A = ral_sf_obits(a), B = ral_sf_obits(b);
     return !ral_sf_isnan_bits(A) && !ral_sf_isnan_bits(B) && ral_sf_key(A) <= ral_sf_key(B);
 }
 RAL_SF bool ral_sf_gt(double a, double b) { return ral_sf_lt(b, a); }
 RAL_SF bool ral_sf_ge(double a, double b) { return ral_sf_le(b, a); }
 RAL_SF bool ral_sf_eq(double a, double b) {
-    const unsigned long long A = ral_sf_bits(a), B = ral_sf_bits(b);
+    const unsigned long long A = ral_sf_obits(a), B = ral_sf_obits(b);
     return !ral_sf_isnan_bits(A) && !ral_sf_isnan_bits(B) && ral_sf_key(A) == ral_sf_key(B);
 }
 RAL_SF bool ral_sf_ne(double a, double b) { return !ral_sf_eq(a, b); }
 // x == 0.0 (either zero; NaN is not zero)
-RAL_SF bool ral_sf_is_zero(double x) { return (ral_sf_bits(x) << 1) == 0; }
+RAL_SF bool ral_sf_is_zero(double x) { return (ral_sf_obits(x) << 1) == 0; }
 
 // ---- conversions -----------------------------------------------------------------------------
 
@@ -263,7 +289,7 @@ RAL_SF double ral_sf_i2d(long long x) {
 // double -> int64 as cvt.rzi.s64.f64 does it on the GPU: truncating, out of range saturates,
 // NaN -> INT64_MIN
 RAL_SF long long ral_sf_d2i(double d) {
-    const unsigned long long A = ral_sf_bits(d);
+    const unsigned long long A = ral_sf_obits(d);
     const int e = (int)((A >> 52) & 0x7ff);
     if (ral_sf_isnan_bits(A)) return (long long)RAL_SF_SIGN;
     if (e < 1023) return 0;
@@ -305,7 +331,7 @@ RAL_SF unsigned long long ral_sf_shift_rne(unsigned long long v, int sh) {
 
 // double -> float, rounded to nearest even (overflow to infinity, subnormal results)
 RAL_SF float ral_sf_d2f(double d) {
-    const unsigned long long A = ral_sf_bits(d);
+    const unsigned long long A = ral_sf_obits(d);
     const unsigned int s = (unsigned int)(A >> 63) << 31;
     const int e = (int)((A >> 52) & 0x7ff);
     const unsigned long long frac = A & RAL_SF_FRAC;
@@ -608,7 +634,7 @@ RAL_SF double ral_sf_hw_cos(double x) {
 // fixed-point 2/pi (exact product with the 53-bit significand), r = f * pi/2 to 128 bits, then
 // the Taylor series of sin(r)/r or cos(r) in 64-bit fixed point by Horner's rule.
 RAL_SF double ral_sf_sincos(double x, bool want_cos) {
-    const unsigned long long X = ral_sf_bits(x);
+    const unsigned long long X = ral_sf_obits(x);
     const int ex = (int)((X >> 52) & 0x7ff);
     const unsigned long long xsign = X & RAL_SF_SIGN;
     if (ex < 1023 - 26 || ex >= 1023 + 20) return want_cos ? ral_sf_hw_cos(x) : ral_sf_hw_sin(x);
