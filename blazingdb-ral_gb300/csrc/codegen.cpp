@@ -61,6 +61,7 @@ void apply_shape_tune(Shape& sh, const std::string& t) {
             else if (k == "S") sh.stage = v != 0;
             else if (k == "P" && v >= 0 && v <= 64) sh.prefetch = v;
             else if (k == "D" && v >= -1 && v <= 1) sh.dense = v;
+            else if (k == "K" && v >= 1 && v <= 2) sh.dense_unroll = v;
         }
         i = e + 1;
     }
@@ -649,7 +650,7 @@ GeneratedKernel generate_filter_kernel(const FilterSpec& f, const Shape& s, bool
         if (dense && per_warp * (s.threads / 32) > 47 * 1024) dense = false;
     }
     key << "|G" << s.G << "J" << s.J << "T" << s.threads << "B" << s.min_blocks << "U" << s.unroll << "S" << s.stage
-        << "P" << s.prefetch << "D" << (dense ? 1 : 0);
+        << "P" << s.prefetch << "D" << (dense ? 1 : 0) << "K" << s.dense_unroll;
     if (item) key << "|item" << (s.soft ? "s" : "");
     char hex[32];
     snprintf(hex, sizeof hex, "%016llx", (unsigned long long)fnv1a(key.str()));
@@ -717,6 +718,23 @@ GeneratedKernel generate_filter_kernel(const FilterSpec& f, const Shape& s, bool
         if (!f.frame_has_valid[c]) return std::string("0xffffffffu");
         return "((r < n) ? __ldg(" + fvalid(c) + " + (r >> 5)) : 0xffffffffu)";
     };
+    // With the dense pass 2 the kept-row list decouples pass 1 from pass 2's slices: pass 1 then
+    // takes G1 = 16 / (widest column it reads) rows per lane and slice (4 for an int32 predicate
+    // column against pass 2's 2 for int64 / double outputs), reads the chunk's stencil validity
+    // words once (one per lane; a chunk of at most 32 words), and indexes the chunk with 32-bit
+    // offsets.
+    int p1_width = 0;
+    if (f.clone_stencil) p1_width = gdf_dtype_size(f.frame_dtypes[f.clone_column]);
+    for (size_t c = 0; c < f.predicate_cols.size(); c++)
+        if (!f.clone_stencil && pred_ref[c]) p1_width = std::max(p1_width, gdf_dtype_size(f.frame_dtypes[f.predicate_cols[c]]));
+    const int G1 = (s.G > 1 && p1_width > 0) ? 16 / p1_width : s.G;
+    const bool wide_p1 = dense && s.G * s.J <= 32 && G1 >= 1 && G1 <= 16 && (s.G * s.J) % G1 == 0;
+    // Pipelined chunks (a full kernel with the wide pass 1): a warp evaluates the predicate of its
+    // next chunk B and publishes B's count before it looks back for the chunk A it evaluated the
+    // round before, so A's predecessors have long published and the look-back rarely waits.
+    // Pass 1 then records the keep bits as the chunk's 32 mask words (two chunks per warp in
+    // shared memory) and pass 2 turns A's words into its kept-row list.
+    const bool pipe = wide_p1 && !item;
     const int KBW = (s.G * s.J + 31) / 32;  // packed keep-bit words per lane
     if (item) {
         // one chunk of a batched request: the dispatcher hands over the chunk index and this
@@ -742,6 +760,7 @@ GeneratedKernel generate_filter_kernel(const FilterSpec& f, const Shape& s, bool
             if (n_proj_vouts) os << "    __shared__ ral_u32 s_pv[RAL_WARPS][" << n_proj_vouts << "][RAL_G * RAL_J];\n";
             os << "    __shared__ unsigned short s_ls[RAL_WARPS][32 * RAL_G * RAL_J];\n";
         }
+        if (pipe) os << "    __shared__ ral_u32 s_kp[RAL_WARPS][2][32];\n";
     }
     // per-warp staging of one slice's compacted values, so that stores are contiguous
     if (s.stage) os << "    __shared__ ral_u64 s_stage[RAL_WARPS][32 * RAL_G];\n";
@@ -770,12 +789,27 @@ GeneratedKernel generate_filter_kernel(const FilterSpec& f, const Shape& s, bool
             if (n_proj_vouts) os << "    ral_u32 (*const s_pvw)[RAL_G * RAL_J] = s_pv[warp];\n";
             os << "    unsigned short* const s_lst = s_ls[warp];\n";
         }
+        if (pipe) os << "    ral_u32 (*const s_kpw)[32] = s_kp[warp];\n";
     }
     os << "    const ral_i64 WT = 32 * RAL_G * RAL_J;\n";
     os << "    const ral_i64 nchunks = (n + WT - 1) / WT;\n";
     os << "    const ral_u32 GMASK = (RAL_G == 32) ? 0xffffffffu : ((1u << RAL_G) - 1u);\n";
     if (NVO) os << "    ral_u32 vcnt[" << NVO << "];\n    for (int i = 0; i < " << NVO << "; ++i) vcnt[i] = 0;\n";
-    if (item) {
+    if (pipe) {
+        os << "    int chunkA = -1;\n    ral_u32 totalA = 0;\n    int bufA = 0;\n";
+        os << "    for (;;) {\n";
+        os << "        ral_u32 ticket = 0;\n";
+        os << "        if (lane == 0) ticket = atomicAdd((unsigned int*)scratch, 1u);\n";
+        os << "        const int chunkB = (int)__shfl_sync(0xffffffffu, ticket, 0);\n";
+        os << "        const bool moreB = (ral_i64)chunkB < nchunks;\n";
+        os << "        const int bufB = bufA ^ 1;\n";
+        os << "        ral_u32 totalB = 0;\n";
+        os << "        if (moreB) {\n";
+        os << "        const ral_i64 chunk = chunkB;\n";
+        os << "        ral_u32* const kp = s_kpw[bufB];\n";
+        os << "        kp[lane] = 0u;\n";
+        os << "        __syncwarp();\n";
+    } else if (item) {
         os << "    do {\n";
         os << "        const ral_i64 chunk = chunk_index;\n";
     } else {
@@ -794,6 +828,72 @@ GeneratedKernel generate_filter_kernel(const FilterSpec& f, const Shape& s, bool
     os << "        ral_u32 total = 0;\n";
 
     // ---- pass 1: predicate
+    if (wide_p1) {
+        os << "        ral_u32 swc = 0;\n";
+        os << "        if (lane < RAL_G * RAL_J) {\n";
+        os << "            const ral_i64 w = (base >> 5) + lane;\n";
+        if (f.clone_stencil) {
+            if (f.frame_has_valid[f.clone_column]) os << "            if ((w << 5) < n) swc = __ldg(" << fvalid(f.clone_column) << " + w);\n";
+            else os << "            if ((w << 5) < n) swc = 0xffffffffu;\n";
+        } else {
+            os << "            if ((w << 5) < n) swc = ral_pred_vword(P, w);\n";
+        }
+        os << "        }\n";
+        os << "#pragma unroll " << std::max(1, s.unroll) << "\n        for (int j = 0; j < (RAL_G * RAL_J) / " << G1 << "; ++j) {\n";
+        os << "            const ral_u32 lr = (ral_u32)j * " << 32 * G1 << "u + (ral_u32)lane * " << G1 << "u;\n";
+        os << "            const ral_i64 r = base + lr;\n";
+        auto load1 = [&](int c, const std::string& arr) {
+            const char* et = element_ctype(f.frame_dtypes[c]);
+            os << "            " << et << " " << arr << "[" << G1 << "];\n";
+            os << "            if (full) ral_ldg_keep<" << et << ", " << G1 << ">(" << fdata(c) << ", r, " << arr << ");\n";
+            os << "            else {\n#pragma unroll\n                for (int g = 0; g < " << G1 << "; ++g) " << arr << "[g] = (r + g < n) ? "
+               << fdata(c) << "[r + g] : (" << et << ")0;\n            }\n";
+        };
+        if (f.clone_stencil) {
+            load1(f.clone_column, "sa");
+        } else {
+            for (size_t c = 0; c < f.predicate_cols.size(); c++)
+                if (pred_ref[c]) load1(f.predicate_cols[c], "pa" + std::to_string(c));
+            for (size_t c = 0; c < f.predicate_cols.size(); c++)
+                if (pred_raw[c]) os << "            const ral_u32 rw" << c << " = " << raw_word(f.predicate_cols[c]) << ";\n";
+        }
+        os << "            ral_u32 bits = 0;\n";
+        os << "#pragma unroll\n            for (int g = 0; g < " << G1 << "; ++g) {\n";
+        if (f.clone_stencil) {
+            os << "                const signed char sv = (signed char)sa[g];\n";
+        } else {
+            os << "                " << kind_ctype(pred_kind[0]) << " y0;\n";
+            os << "                ral_pred_row(P";
+            for (size_t c = 0; c < f.predicate_cols.size(); c++)
+                if (pred_ref[c]) os << ", " << widen("pa" + std::to_string(c) + "[g]", f.frame_dtypes[f.predicate_cols[c]]);
+            for (size_t c = 0; c < f.predicate_cols.size(); c++)
+                if (pred_raw[c]) os << ", (rw" << c << " >> ((int)(r & 31) + g)) & 1u";
+            os << ", y0);\n";
+            os << "                const signed char sv = " << narrow("y0", pred_kind[0], GDF_INT8) << ";\n";
+        }
+        os << "                bits |= (sv != 0 ? 1u : 0u) << g;\n";
+        os << "            }\n";
+        os << "            const ral_u32 word = __shfl_sync(0xffffffffu, swc, (int)(lr >> 5));\n";
+        os << "            bits &= (word >> (lr & 31u)) & " << (G1 == 32 ? "0xffffffffu" : std::to_string((1u << G1) - 1u) + "u") << ";\n";
+        os << "            if (!full) {\n#pragma unroll\n                for (int g = 0; g < " << G1 << "; ++g) if (r + g >= n) bits &= ~(1u << g);\n            }\n";
+        if (pipe) {
+            os << "            if (bits) atomicOr(kp + (lr >> 5), bits << (lr & 31u));\n";
+            os << "            total += __reduce_add_sync(0xffffffffu, __popc(bits));\n";
+        } else {
+            os << "            {\n";
+            os << "                const ral_u32 c = __popc(bits);\n";
+            os << "                ral_u32 inc = c;\n";
+            os << "                for (int off = 1; off < 32; off <<= 1) {\n";
+            os << "                    const ral_u32 t = __shfl_up_sync(0xffffffffu, inc, off);\n";
+            os << "                    if (lane >= off) inc += t;\n                }\n";
+            os << "                ral_u32 q = total + inc - c;\n";
+            os << "#pragma unroll\n                for (int g = 0; g < " << G1 << "; ++g)\n";
+            os << "                    if ((bits >> g) & 1u) s_lst[q++] = (unsigned short)(lr + g);\n";
+            os << "                total += __shfl_sync(0xffffffffu, inc, 31);\n";
+            os << "            }\n";
+        }
+        os << "        }\n";
+    } else {
     os << "#pragma unroll " << std::max(1, s.unroll) << "\n        for (int j = 0; j < RAL_J; ++j) {\n";
     os << "            const ral_i64 r = base + (ral_i64)j * 32 * RAL_G + lane * RAL_G;\n";
     // stencil validity word of this slice for the lane's rows
@@ -853,9 +953,57 @@ GeneratedKernel generate_filter_kernel(const FilterSpec& f, const Shape& s, bool
         os << "            total += __reduce_add_sync(0xffffffffu, __popc(bits));\n";
     }
     os << "        }\n";
-    os << "        const ral_u64 excl = ral_lookback(status, chunk, total, scratch + 1);\n";
-    os << "        if (chunk == nchunks - 1 && lane == 0) scratch[2] = excl + total;\n";
-    os << "        if (total == 0u) continue;\n";
+    }  // pass 1 with pass 2's slices
+    if (dense && s.prefetch > 0 && s.G > 1) {
+        // the chunk's rows of the columns pass 2 reads (not the predicate's, which pass 1 just
+        // read) are prefetched into L2 while the warp waits in its look-back, when the chunk keeps
+        // at least an eighth of its rows; one cp.async.bulk.prefetch per column, one lane each
+        std::vector<bool> want(NF, false);
+        for (const FilterOutput& o : f.outputs)
+            if (!o.from_project) want[o.index] = true;
+        for (size_t c = 0; c < f.project_cols.size(); c++)
+            if (proj_ref[c]) want[f.project_cols[c]] = true;
+        std::vector<int> cols;
+        for (int c = 0; c < NF; c++)
+            if (want[c] && !pred_col[c] && (int)cols.size() < 32) cols.push_back(c);
+        if (!cols.empty()) {
+            os << "        if ((ral_u64)total * 8u >= (ral_u64)WT) {\n";
+            os << "            const ral_i64 rows = (n - base) < WT ? (n - base) : WT;\n";
+            for (size_t i = 0; i < cols.size(); i++) {
+                const int c = cols[i];
+                os << "            if (lane == " << i << ") ral_prefetch_l2(" << fdata(c) << " + base, (unsigned)((rows * "
+                   << gdf_dtype_size(f.frame_dtypes[c]) << ") & ~15ll));\n";
+            }
+            os << "        }\n";
+        }
+    }
+    if (pipe) {
+        os << "        ral_lookback_publish(status, chunk, total);\n";
+        os << "        totalB = total;\n";
+        os << "        }\n";  // chunk B
+        os << "        if (chunkA >= 0) {\n";
+        os << "        const ral_i64 chunk = chunkA;\n";
+        os << "        const ral_u32 total = totalA;\n";
+        os << "        const ral_i64 base = chunk * WT;\n";
+        os << "        const ral_u64 excl = ral_lookback_published(status, chunk, total, scratch + 1);\n";
+        os << "        if (chunk == nchunks - 1 && lane == 0) scratch[2] = excl + total;\n";
+        os << "        if (total != 0u) {\n";
+        // A's kept-row list from its mask words: lane w holds word w, ranks by a warp scan
+        os << "        {\n";
+        os << "            const ral_u32 kw = (lane < RAL_G * RAL_J) ? s_kpw[bufA][lane] : 0u;\n";
+        os << "            const ral_u32 c = __popc(kw);\n";
+        os << "            ral_u32 inc = c;\n";
+        os << "            for (int off = 1; off < 32; off <<= 1) {\n";
+        os << "                const ral_u32 t = __shfl_up_sync(0xffffffffu, inc, off);\n";
+        os << "                if (lane >= off) inc += t;\n            }\n";
+        os << "            ral_u32 q = inc - c;\n";
+        os << "            for (ral_u32 m = kw; m; m &= m - 1u) s_lst[q++] = (unsigned short)(lane * 32 + __ffs(m) - 1);\n";
+        os << "        }\n";
+    } else {
+        os << "        const ral_u64 excl = ral_lookback(status, chunk, total, scratch + 1);\n";
+        os << "        if (chunk == nchunks - 1 && lane == 0) scratch[2] = excl + total;\n";
+        os << "        if (total == 0u) continue;\n";
+    }
 
     // ---- pass 2: ranks and outputs
     if (NVO) {
@@ -882,66 +1030,98 @@ GeneratedKernel generate_filter_kernel(const FilterSpec& f, const Shape& s, bool
             os << "        }\n";
         }
         os << "        __syncwarp();\n";
-        os << "        for (ral_u32 k0 = 0; k0 < total; k0 += 32) {\n";
-        os << "            const ral_u32 k = k0 + lane;\n";
-        os << "            const bool act = k < total;\n";
-        // an idle lane of the last step works on the step's first row and stores nothing
-        os << "            const ral_u32 off = s_lst[act ? k : k0];\n";
-        os << "            const ral_i64 row = base + off;\n";
-        os << "            const ral_u64 pos = excl + k;\n";
-        for (int k = 0; k < NO; k++) {
-            if (f.outputs[k].from_project) continue;
-            const int c = f.outputs[k].index;
-            os << "            {\n                const " << element_ctype(f.frame_dtypes[c]) << " v = " << fdata(c) << "[row];\n";
-            os << "                if (act) o" << k << "[pos] = v;\n            }\n";
-        }
-        if (any_proj) {
-            for (size_t c = 0; c < f.project_cols.size(); c++)
-                if (proj_ref[c])
-                    os << "            const " << element_ctype(f.frame_dtypes[f.project_cols[c]]) << " qa" << c << " = "
-                       << fdata(f.project_cols[c]) << "[row];\n";
-            for (size_t c = 0; c < f.project_cols.size(); c++)
-                if (proj_raw[c]) {
-                    const int fc = f.project_cols[c];
-                    if (f.frame_has_valid[fc]) os << "            const ral_u32 qw" << c << " = __ldg(" << fvalid(fc) << " + (row >> 5));\n";
-                    else os << "            const ral_u32 qw" << c << " = 0xffffffffu;\n";
-                }
-            for (int o = 0; o < f.project->n_out; o++) os << "            " << kind_ctype(proj_kind[o]) << " y" << o << ";\n";
-            os << "            ral_proj_row(P";
-            for (size_t c = 0; c < f.project_cols.size(); c++)
-                if (proj_ref[c]) os << ", " << widen("qa" + std::to_string(c), f.frame_dtypes[f.project_cols[c]]);
-            for (size_t c = 0; c < f.project_cols.size(); c++)
-                if (proj_raw[c]) os << ", (qw" << c << " >> (int)(row & 31)) & 1u";
-            for (int o = 0; o < f.project->n_out; o++) os << ", y" << o;
-            os << ");\n";
-            os << "            if (act) {\n";
+        // one step's row and loads (suffix sx; the step's first list position kx)
+        auto step_loads = [&](const std::string& sx, const std::string& kx, const std::string& guard) {
+            os << "            const ral_u32 k" << sx << " = " << kx << " + lane;\n";
+            os << "            const bool act" << sx << " = " << guard << "k" << sx << " < total;\n";
+            // an idle lane works on the step's first row and stores nothing
+            os << "            const ral_u32 off" << sx << " = s_lst[act" << sx << " ? k" << sx << " : " << kx << "];\n";
+            os << "            const ral_i64 row" << sx << " = base + off" << sx << ";\n";
             for (int k = 0; k < NO; k++) {
-                if (!f.outputs[k].from_project) continue;
-                const int o = f.outputs[k].index;
-                os << "                o" << k << "[pos] = " << narrow("y" + std::to_string(o), proj_kind[o], f.outputs[k].dtype) << ";\n";
+                if (f.outputs[k].from_project) continue;
+                const int c = f.outputs[k].index;
+                os << "            const " << element_ctype(f.frame_dtypes[c]) << " gv" << k << sx << " = " << fdata(c) << "[row"
+                   << sx << "];\n";
             }
-            os << "            }\n";
-        }
-        for (int i = 0; i < NVO; i++) {
-            const int k = vouts[i];
-            const FilterOutput& o = f.outputs[k];
-            os << "            {\n";
-            if (o.from_project) {
-                int pi = 0;
-                for (size_t q = 0; q < proj_vouts.size(); q++)
-                    if (proj_vouts[q] == o.index) pi = (int)q;
-                os << "                const ral_u32 vw = s_pvw[" << pi << "][off >> 5];\n";
-            } else {
-                os << "                const ral_u32 vw = __ldg(" << fvalid(o.index) << " + (row >> 5));\n";
+            if (any_proj) {
+                for (size_t c = 0; c < f.project_cols.size(); c++)
+                    if (proj_ref[c])
+                        os << "            const " << element_ctype(f.frame_dtypes[f.project_cols[c]]) << " qa" << c << sx
+                           << " = " << fdata(f.project_cols[c]) << "[row" << sx << "];\n";
+                for (size_t c = 0; c < f.project_cols.size(); c++)
+                    if (proj_raw[c]) {
+                        const int fc = f.project_cols[c];
+                        if (f.frame_has_valid[fc])
+                            os << "            const ral_u32 qw" << c << sx << " = __ldg(" << fvalid(fc) << " + (row" << sx << " >> 5));\n";
+                        else
+                            os << "            const ral_u32 qw" << c << sx << " = 0xffffffffu;\n";
+                    }
             }
-            os << "                const ral_u32 bal = __ballot_sync(0xffffffffu, act && ((vw >> (off & 31u)) & 1u));\n";
-            os << "                if (lane == 0 && bal) {\n";
-            os << "                    vcnt[" << i << "] += __popc(bal);\n";
-            os << "                    const ral_u64 X = (ral_u64)bal << (excl & 31u);\n";
-            os << "                    s_vbw[" << i << "][k0 >> 5] |= (ral_u32)X;\n";
-            os << "                    s_vbw[" << i << "][(k0 >> 5) + 1] |= (ral_u32)(X >> 32);\n";
-            os << "                }\n";
+        };
+        // the step's outputs and validity bits
+        auto step_outputs = [&](const std::string& sx, const std::string& kx, const std::string& ind) {
+            os << ind << "const ral_u64 pos" << sx << " = excl + k" << sx << ";\n";
+            os << ind << "if (act" << sx << ") {\n";
+            for (int k = 0; k < NO; k++)
+                if (!f.outputs[k].from_project) os << ind << "    o" << k << "[pos" << sx << "] = gv" << k << sx << ";\n";
+            os << ind << "}\n";
+            if (any_proj) {
+                os << ind << "{\n";
+                for (int o = 0; o < f.project->n_out; o++) os << ind << "    " << kind_ctype(proj_kind[o]) << " y" << o << ";\n";
+                os << ind << "    ral_proj_row(P";
+                for (size_t c = 0; c < f.project_cols.size(); c++)
+                    if (proj_ref[c]) os << ", " << widen("qa" + std::to_string(c) + sx, f.frame_dtypes[f.project_cols[c]]);
+                for (size_t c = 0; c < f.project_cols.size(); c++)
+                    if (proj_raw[c]) os << ", (qw" << c << sx << " >> (int)(row" << sx << " & 31)) & 1u";
+                for (int o = 0; o < f.project->n_out; o++) os << ", y" << o;
+                os << ");\n";
+                os << ind << "    if (act" << sx << ") {\n";
+                for (int k = 0; k < NO; k++) {
+                    if (!f.outputs[k].from_project) continue;
+                    const int o = f.outputs[k].index;
+                    os << ind << "        o" << k << "[pos" << sx << "] = " << narrow("y" + std::to_string(o), proj_kind[o], f.outputs[k].dtype)
+                       << ";\n";
+                }
+                os << ind << "    }\n" << ind << "}\n";
+            }
+            for (int i = 0; i < NVO; i++) {
+                const int k = vouts[i];
+                const FilterOutput& o = f.outputs[k];
+                os << ind << "{\n";
+                if (o.from_project) {
+                    int pi = 0;
+                    for (size_t q = 0; q < proj_vouts.size(); q++)
+                        if (proj_vouts[q] == o.index) pi = (int)q;
+                    os << ind << "    const ral_u32 vw = s_pvw[" << pi << "][off" << sx << " >> 5];\n";
+                } else {
+                    os << ind << "    const ral_u32 vw = __ldg(" << fvalid(o.index) << " + (row" << sx << " >> 5));\n";
+                }
+                os << ind << "    const ral_u32 bal = __ballot_sync(0xffffffffu, act" << sx << " && ((vw >> (off" << sx << " & 31u)) & 1u));\n";
+                os << ind << "    if (lane == 0 && bal) {\n";
+                os << ind << "        vcnt[" << i << "] += __popc(bal);\n";
+                os << ind << "        const ral_u64 X = (ral_u64)bal << (excl & 31u);\n";
+                os << ind << "        s_vbw[" << i << "][(" << kx << ") >> 5] |= (ral_u32)X;\n";
+                os << ind << "        s_vbw[" << i << "][((" << kx << ") >> 5) + 1] |= (ral_u32)(X >> 32);\n";
+                os << ind << "    }\n";
+                os << ind << "}\n";
+            }
+        };
+        if (s.dense_unroll >= 2) {
+            // two steps per iteration: both steps' loads are in flight before either computes; the
+            // second step computes only when it holds rows (a warp-uniform test)
+            os << "        for (ral_u32 k0 = 0; k0 < total; k0 += 64) {\n";
+            os << "            const bool two = k0 + 32u < total;\n";
+            os << "            const ral_u32 k1 = two ? k0 + 32u : k0;\n";
+            step_loads("A", "k0", "");
+            step_loads("B", "k1", "two && ");
+            step_outputs("A", "k0", "            ");
+            os << "            if (two) {\n";
+            step_outputs("B", "k1", "                ");
             os << "            }\n";
+        } else {
+            os << "        for (ral_u32 k0 = 0; k0 < total; k0 += 32) {\n";
+            step_loads("A", "k0", "");
+            step_outputs("A", "k0", "            ");
         }
         os << "        }\n";
     } else {
@@ -1122,7 +1302,15 @@ GeneratedKernel generate_filter_kernel(const FilterSpec& f, const Shape& s, bool
     }
     // the next chunk's pass 1 rewrites the list the lanes have just read
     if (dense && !NVO) os << "        __syncwarp();\n";
-    os << (item ? "    } while (0);\n" : "    }\n");  // chunk loop
+    if (pipe) {
+        os << "        }\n";  // total != 0
+        os << "        }\n";  // chunk A
+        os << "        if (!moreB) break;\n";
+        os << "        chunkA = chunkB;\n        totalA = totalB;\n        bufA = bufB;\n";
+        os << "    }\n";
+    } else {
+        os << (item ? "    } while (0);\n" : "    }\n");  // chunk loop
+    }
 
     // ---- valid-bit counts: one atomic per warp and masked output
     if (NVO) {

@@ -26,12 +26,17 @@ struct Shape {
     bool stage = false;  // filter kernels: dense slices written through a shared-memory stage
     bool soft = false;   // batch items: integer-pipe double operations (the autotuner decides)
     // filter kernels: slices of pass 2 prefetched into L2 ahead (0, the default: none -- measured
-    // slower at 4, 8 and 16 slices: 500M rows at s = 0.5 ran 5.39 / 5.71 / 5.79 ms against 5.06)
+    // slower at 4, 8 and 16 slices: 500M rows at s = 0.5 ran 5.39 / 5.71 / 5.79 ms against 5.06).
+    // With the dense pass 2 any value > 0 prefetches the chunk's columns during the look-back
+    // (also slower: the 200M-row filter + project at s = 0.5 ran 2.53 ms against 2.09).
     int prefetch = 0;
     // filter kernels: pass 2 walks a shared-memory list of the chunk's kept rows, 32 at a time,
     // so every lane evaluates a kept row and stores are contiguous (1), or evaluates its own G
     // rows of each slice, skipping dropped ones (0); -1: 1 when the filter has a projection
     int dense = -1;
+    // dense pass 2: list steps whose loads are issued together (1 or 2; 2 measured no faster:
+    // 2.15 ms against 2.09 at s = 0.5, at five blocks per SM for its registers)
+    int dense_unroll = 1;
 };
 
 // Slot order of the kernel's parameter block (all 8-byte slots).

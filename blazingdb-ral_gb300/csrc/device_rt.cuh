@@ -278,16 +278,39 @@ RAL_FI ral_u32 ral_lanemask_lt() {
 #define RAL_FLAG_INCLUSIVE (2ull << 62)
 #define RAL_VALUE_MASK ((1ull << 62) - 1)
 #define RAL_LOOKBACK_SPIN_LIMIT (1l << 22)
-__device__ __forceinline__ ral_u64 ral_lookback(ral_u64* status, ral_i64 tile, ral_u64 aggregate, ral_u64* error_word) {
+// The two halves of a look-back: a tile's count is published as soon as it is known (tile 0's is
+// its inclusive prefix), and the exclusive prefix is looked up later -- a warp that holds two
+// tiles publishes the second before it looks back for the first.  A tile's status stays empty
+// only while its own warp evaluates it, which waits on nothing, so every wait ends.
+__device__ __forceinline__ void ral_lookback_publish(ral_u64* status, ral_i64 tile, ral_u64 aggregate) {
+    if ((threadIdx.x & 31) == 0)
+        ral_st_status(status + tile, (tile == 0 ? RAL_FLAG_INCLUSIVE : RAL_FLAG_AGGREGATE) | aggregate);
+}
+__device__ __forceinline__ ral_u64 ral_lookback_published(ral_u64* status, ral_i64 tile, ral_u64 aggregate,
+                                                          ral_u64* error_word) {
     const int lane = threadIdx.x & 31;
-    if (tile == 0) {
-        if (lane == 0) ral_st_status(status, RAL_FLAG_INCLUSIVE | aggregate);
-        return 0;
+    if (tile == 0) return 0;
+    // The nearest predecessor is usually still in its own pass 1 when a tile gets here: lane 0
+    // alone polls it until it has published, with a growing pause, so that a waiting warp costs
+    // one load per round instead of 32; then the warp reads 32 predecessors per round.
+    long spins = 0;
+    {
+        unsigned pause = 32;
+        for (;;) {
+            ral_u64 s0 = 0;
+            if (lane == 0) s0 = ral_ld_status(status + tile - 1);
+            s0 = __shfl_sync(0xffffffffu, s0, 0);
+            if (s0 & ~RAL_VALUE_MASK) break;
+            if (++spins > RAL_LOOKBACK_SPIN_LIMIT) {
+                if (lane == 0) atomicExch((unsigned long long*)error_word, 1ull);
+                break;
+            }
+            __nanosleep(pause);
+            if (pause < 256) pause <<= 1;
+        }
     }
-    if (lane == 0) ral_st_status(status + tile, RAL_FLAG_AGGREGATE | aggregate);
     ral_u64 excl = 0;
     ral_i64 j = tile - 1 - lane;
-    long spins = 0;
     for (;;) {
         const ral_u64 s = j >= 0 ? ral_ld_status(status + j) : RAL_FLAG_INCLUSIVE;
         const ral_u64 flag = s & ~RAL_VALUE_MASK;
@@ -311,6 +334,10 @@ __device__ __forceinline__ ral_u64 ral_lookback(ral_u64* status, ral_i64 tile, r
     }
     if (lane == 0) ral_st_status(status + tile, RAL_FLAG_INCLUSIVE | ((excl + aggregate) & RAL_VALUE_MASK));
     return excl;
+}
+__device__ __forceinline__ ral_u64 ral_lookback(ral_u64* status, ral_i64 tile, ral_u64 aggregate, ral_u64* error_word) {
+    ral_lookback_publish(status, tile, aggregate);
+    return ral_lookback_published(status, tile, aggregate, error_word);
 }
 
 #endif  // RAL_DEVICE_RT_CUH_

@@ -327,14 +327,15 @@ Shape default_filter_shape(const FilterSpec& spec, bool aligned16, int64_t n) {
     Shape sh;
     sh.G = aligned16 ? 16 / filter_max_width(spec) : 1;
     sh.threads = 256;
-    // With a projection pass 2 walks the chunk's kept-row list (Shape::dense): 1024-row chunks and
-    // six resident blocks (40 registers; the per-warp lists of 2048-row chunks would leave room for
-    // five) measured fastest -- 200M rows, s = 0.01 / 0.5 / 0.99: 0.86 / 2.09 / 3.41 ms against
-    // 0.91 / 2.24 / 3.52 with 2048-row chunks and four blocks.  A gather-only filter keeps the
-    // slice-wise pass 2 and is fastest at 2048-row chunks and two blocks.
+    // With a projection pass 2 walks the chunk's kept-row list (Shape::dense) and a warp pipelines
+    // two chunks (pass 1 of the next before the look-back of the last), which needs chunks of at
+    // most 32 mask words: 1024-row chunks.  Five resident blocks (47 registers) measured fastest --
+    // 200M rows, s = 0.01 / 0.5 / 0.99: 0.54 / 1.83 / 3.11 ms, against 0.63 / 1.81 / 3.12 at six
+    // blocks (whose 40-register cap spills) and 0.73 / 1.98 / 3.23 unpipelined.  A gather-only
+    // filter keeps the slice-wise pass 2 and is fastest at 2048-row chunks and two blocks.
     const int jmax = std::max(1, (have_proj ? 32 : 64) / sh.G);
     sh.J = n < 0 ? jmax : std::max(1, std::min(jmax, chunk_slices(n, sh.G)));
-    sh.min_blocks = have_proj ? 6 : 2;
+    sh.min_blocks = have_proj ? 5 : 2;
     sh.unroll = have_proj ? 2 : 4;
     sh.stage = false;
     return sh;

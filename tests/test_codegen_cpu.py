@@ -94,7 +94,7 @@ FILTER_CASES = [
 
 
 @pytest.mark.parametrize("tune", ["", "S=1", "J=8,U=2,T=128,B=4", "J=64,U=8,T=512,B=1,S=1", "P=8", "P=4,J=16",
-                                  "D=1", "D=0", "D=1,J=8,T=128"])
+                                  "D=1", "D=0", "D=1,J=8,T=128", "K=2,B=5", "P=1,K=2,B=4"])
 @pytest.mark.parametrize("case", FILTER_CASES, ids=[c[0] for c in FILTER_CASES])
 def test_filter_kernels_compile(case, tune, monkeypatch):
     _, dtypes, nullable, fq, pq = case
@@ -111,10 +111,25 @@ def test_dense_pass_two_is_the_default_with_a_projection_and_fits_shared_memory(
     p = W.fused_project_program()
     src, _ = ralgpu.debug_filter_source(p.input_dtypes, [1] * 5, W.filter_project_filter(0.5),
                                         W.FILTER_PROJECT_PROJECT)
-    assert "s_lst[act ? k : k0]" in src and "kbw[" not in src
+    assert "s_lst[actA ? kA : k0]" in src and "kbw[" not in src
     src, _ = ralgpu.debug_filter_source(W.FILTER_GATHER_DTYPES, [1] * 6, W.filter_gather_query(0.5), None)
     assert "s_lst" not in src and "kbw[" in src
     monkeypatch.setenv("RAL_FILTER_TUNE", "J=64,T=512,B=1")
     src, log = ralgpu.debug_filter_source(p.input_dtypes, [1] * 5, W.filter_project_filter(0.5),
                                           W.FILTER_PROJECT_PROJECT, compile=True)
     assert "s_lst" not in src and "kbw[" in src and spills(log) <= 64
+
+
+def test_projection_filter_pipelines_two_chunks_per_warp(monkeypatch):
+    """With a projection the kernel evaluates the next chunk's predicate before the look-back of
+    the last one (keep bits as mask words, two chunks per warp); a chunk size with more than 32
+    mask words falls back to one chunk at a time."""
+    monkeypatch.delenv("RAL_FILTER_TUNE", raising=False)
+    p = W.fused_project_program()
+    src, log = ralgpu.debug_filter_source(p.input_dtypes, [1] * 5, W.filter_project_filter(0.5),
+                                          W.FILTER_PROJECT_PROJECT, compile=True)
+    assert "ral_lookback_publish(status, chunk, total)" in src and "chunkA" in src and spills(log) == 0
+    monkeypatch.setenv("RAL_FILTER_TUNE", "J=32,B=4")
+    src, log = ralgpu.debug_filter_source(p.input_dtypes, [1] * 5, W.filter_project_filter(0.5),
+                                          W.FILTER_PROJECT_PROJECT, compile=True)
+    assert "chunkA" not in src and "s_lst[actA ? kA : k0]" in src and spills(log) == 0

@@ -532,3 +532,47 @@ def test_filter_project_workload_matches_oracle(sel, filter_mode):
     assert len(got) == len(ep) == 3
     for k, (g, e) in enumerate(zip(got, ep)):
         H.assert_columns_equal(g, e, what=f"projection {k}")
+
+
+@pytest.mark.parametrize("tune", ["D=0", "K=2,B=5", "P=1", "J=32,B=4", "D=1,J=4"])
+def test_filter_project_launch_variants_match_oracle(tune, monkeypatch):
+    """Every pass-2 form of the fused filter (slice-wise; kept-row list one or two steps at a time,
+    with or without the look-back prefetch; other chunk sizes) gives the oracle's bits."""
+    monkeypatch.setenv("RAL_FILTER_TUNE", tune)
+    n = 200_003
+    rng = np.random.default_rng(91)
+    spec = [(D.GDF_INT32, rng.integers(0, 100, n), rng.random(n) < 0.9),
+            (D.GDF_FLOAT64, rng.standard_normal(n), rng.random(n) < 0.8),
+            (D.GDF_INT64, rng.integers(-1000, 1000, n), None),
+            (D.GDF_INT8, rng.integers(-5, 5, n), rng.random(n) < 0.7)]
+    filt = "LogicalFilter(condition=[OR(<($0, 45), >($2, 700))])"
+    proj = ("LogicalProject(a=[$2], b=[*($1, 2.5)], c=[+($0, $3)], d=[$3], e=[IS NULL($1)], "
+            "f=[CASE(IS NOT NULL($0), $0, -1)], g=[FLOOR(/($1, 3))], h=[MOD($2, +($0, 1))])")
+    got = R.filter_project(H.to_device(spec), filt, proj)
+    ef = O.process_filter(H.to_oracle(spec), filt)
+    ep = O.execute_project_plan(ef, proj)
+    for k, (g, e) in enumerate(zip(got, ep)):
+        H.assert_columns_equal(g, e, what=f"{tune}: projection {k}")
+
+
+def test_multiply_by_comparison_and_abs_on_special_values():
+    """A double times a 0/1 comparison result skips the FP64 multiply and ABS may fold into its
+    consumer; infinities, NaN, signed zeros and subnormals give the multiply's results."""
+    specials = np.array([0.0, -0.0, 1.5, -2.25, np.inf, -np.inf, np.nan, 5e-324, -5e-324, 1e308, -1e-310],
+                        dtype=np.float64)
+    n = len(specials) * 4
+    x = np.tile(specials, 4)
+    b = np.repeat(np.array([-1, 0, 1, 7], dtype=np.int64), len(specials))
+    spec = [(D.GDF_FLOAT64, x, None), (D.GDF_INT64, b, None)]
+    J, I64 = (D.GDF_INT32, 0), (D.GDF_INT64, 0)
+    # registers: $0 = x, $1 = b, outputs 2..5, temporaries from 6
+    # c = b > 0 (6); m = c * x (5); a = |x| (7); s = a + m (2); d = |x| stored (3); z = m - a (4)
+    prog = dict(left=[1, 6, 0, 7, 0, 5], right=[-2, 0, -1, 5, -1, 7], outputs=[6, 5, 7, 2, 3, 4],
+                final=[2, 3, 4, 5],
+                ops=[D.GDF_GREATER, D.GDF_MUL, D.GDF_INVALID_BINARY, D.GDF_ADD, D.GDF_INVALID_BINARY, D.GDF_SUB],
+                uops=[D.BLZ_INVALID_UNARY, D.BLZ_INVALID_UNARY, D.BLZ_ABS, D.BLZ_INVALID_UNARY, D.BLZ_ABS,
+                      D.BLZ_INVALID_UNARY],
+                lscalars=[J] * 6, rscalars=[I64, J, J, J, J, J])
+    dev, ora = H.run_program_both(spec, [D.GDF_FLOAT64] * 4, prog)
+    for k, (g, e) in enumerate(zip(dev, ora)):
+        H.assert_columns_equal(g, e, what=f"output {k}", check_null_count=False)
