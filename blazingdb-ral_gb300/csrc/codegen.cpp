@@ -643,7 +643,7 @@ GeneratedKernel generate_filter_kernel(const FilterSpec& f, const Shape& s, bool
     for (const FilterOutput& o : f.outputs) (o.from_project ? any_proj : any_gather) = true;
     int n_proj_vouts = 0;
     for (int k : vouts) n_proj_vouts += f.outputs[k].from_project ? 1 : 0;
-    bool dense = s.dense < 0 ? any_proj : s.dense > 0;
+    bool dense = s.dense != 0;
     if (32 * s.G * s.J > 65536) dense = false;
     {
         const long per_warp = (long)NVO * (s.G * s.J + 2) * 4 + (dense ? (long)n_proj_vouts * s.G * s.J * 4 + 64L * s.G * s.J : 0);

@@ -31,8 +31,8 @@ struct Shape {
     // (also slower: the 200M-row filter + project at s = 0.5 ran 2.53 ms against 2.09).
     int prefetch = 0;
     // filter kernels: pass 2 walks a shared-memory list of the chunk's kept rows, 32 at a time,
-    // so every lane evaluates a kept row and stores are contiguous (1), or evaluates its own G
-    // rows of each slice, skipping dropped ones (0); -1: 1 when the filter has a projection
+    // so every lane evaluates or gathers a kept row and stores are contiguous (1, the default;
+    // -1 is the same), or takes its own G rows of each slice, skipping dropped ones (0)
     int dense = -1;
     // dense pass 2: list steps whose loads are issued together (1 or 2; 2 measured no faster:
     // 2.15 ms against 2.09 at s = 0.5, at five blocks per SM for its registers)

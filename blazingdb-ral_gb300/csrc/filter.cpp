@@ -323,20 +323,20 @@ void apply_tune(Shape& sh, const std::string& t) { apply_shape_tune(sh, t); }
 
 // Launch shape of a fused filter over n rows (n < 0: large), before RAL_FILTER_TUNE.
 Shape default_filter_shape(const FilterSpec& spec, bool aligned16, int64_t n) {
-    const bool have_proj = spec.project != nullptr;
     Shape sh;
     sh.G = aligned16 ? 16 / filter_max_width(spec) : 1;
     sh.threads = 256;
-    // With a projection pass 2 walks the chunk's kept-row list (Shape::dense) and a warp pipelines
-    // two chunks (pass 1 of the next before the look-back of the last), which needs chunks of at
-    // most 32 mask words: 1024-row chunks.  Five resident blocks (47 registers) measured fastest --
-    // 200M rows, s = 0.01 / 0.5 / 0.99: 0.54 / 1.83 / 3.11 ms, against 0.63 / 1.81 / 3.12 at six
-    // blocks (whose 40-register cap spills) and 0.73 / 1.98 / 3.23 unpipelined.  A gather-only
-    // filter keeps the slice-wise pass 2 and is fastest at 2048-row chunks and two blocks.
-    const int jmax = std::max(1, (have_proj ? 32 : 64) / sh.G);
+    // Pass 2 walks the chunk's kept-row list (Shape::dense) and a warp pipelines two chunks (pass 1
+    // of the next before the look-back of the last), which needs chunks of at most 32 mask words:
+    // 1024-row chunks, five resident blocks (47 registers with the 12-op projection).  Measured on
+    // the 200M-row filter + project, s = 0.01 / 0.5 / 0.99: 0.54 / 1.83 / 3.11 ms, against
+    // 0.63 / 1.81 / 3.12 at six blocks (whose 40-register cap spills) and 0.73 / 1.98 / 3.23
+    // unpipelined; on the 500M-row six-column gather 1.36 / 3.67 / 5.57 ms against 2.34 / 5.01 /
+    // 6.41 with the slice-wise pass 2 at 2048-row chunks and two blocks.
+    const int jmax = std::max(1, 32 / sh.G);
     sh.J = n < 0 ? jmax : std::max(1, std::min(jmax, chunk_slices(n, sh.G)));
-    sh.min_blocks = have_proj ? 5 : 2;
-    sh.unroll = have_proj ? 2 : 4;
+    sh.min_blocks = 5;
+    sh.unroll = spec.project != nullptr ? 2 : 4;
     sh.stage = false;
     return sh;
 }

@@ -104,14 +104,18 @@ def test_filter_kernels_compile(case, tune, monkeypatch):
     assert spills(log) <= 64, log
 
 
-def test_dense_pass_two_is_the_default_with_a_projection_and_fits_shared_memory(monkeypatch):
-    """A projection makes pass 2 walk the kept-row list; a filter without one keeps the slice-wise
-    pass; a shape whose per-block lists would not fit static shared memory falls back to it."""
+def test_dense_pass_two_is_the_default_and_fits_shared_memory(monkeypatch):
+    """Pass 2 walks the kept-row list by default, with a projection or gathers only; D=0 selects
+    the slice-wise pass; a shape whose per-block lists would not fit static shared memory falls
+    back to it."""
     monkeypatch.delenv("RAL_FILTER_TUNE", raising=False)
     p = W.fused_project_program()
     src, _ = ralgpu.debug_filter_source(p.input_dtypes, [1] * 5, W.filter_project_filter(0.5),
                                         W.FILTER_PROJECT_PROJECT)
     assert "s_lst[actA ? kA : k0]" in src and "kbw[" not in src
+    src, _ = ralgpu.debug_filter_source(W.FILTER_GATHER_DTYPES, [1] * 6, W.filter_gather_query(0.5), None)
+    assert "s_lst[actA ? kA : k0]" in src and "kbw[" not in src
+    monkeypatch.setenv("RAL_FILTER_TUNE", "D=0")
     src, _ = ralgpu.debug_filter_source(W.FILTER_GATHER_DTYPES, [1] * 6, W.filter_gather_query(0.5), None)
     assert "s_lst" not in src and "kbw[" in src
     monkeypatch.setenv("RAL_FILTER_TUNE", "J=64,T=512,B=1")
