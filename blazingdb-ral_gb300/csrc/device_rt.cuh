@@ -292,7 +292,9 @@ __device__ __forceinline__ ral_u64 ral_lookback_published(ral_u64* status, ral_i
     if (tile == 0) return 0;
     // The nearest predecessor is usually still in its own pass 1 when a tile gets here: lane 0
     // alone polls it until it has published, with a growing pause, so that a waiting warp costs
-    // one load per round instead of 32; then the warp reads 32 predecessors per round.
+    // one load per round instead of 32; then the warp reads 32 predecessors per round.  (Reading
+    // 4 or 8 predecessors per lane and round -- fewer rounds for long walks -- measured slower:
+    // the status words are written by other SMs, and most walks end within 64 tiles.)
     long spins = 0;
     {
         unsigned pause = 32;
