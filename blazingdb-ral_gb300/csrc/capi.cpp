@@ -84,6 +84,19 @@ int ral_perform_operation(gdf_column* const* output_columns, int32_t num_outputs
     });
 }
 
+int ral_perform_operation_host(gdf_column* const* output_columns, int32_t num_outputs, gdf_column* const* input_columns,
+                               int32_t num_inputs, const column_index_type* left_inputs,
+                               const column_index_type* right_inputs, const column_index_type* outputs,
+                               int32_t num_operations, const column_index_type* final_output_positions,
+                               const int32_t* operators, const int32_t* unary_operators, const gdf_scalar* left_scalars,
+                               const gdf_scalar* right_scalars, int64_t chunk_rows) {
+    return guarded([&] {
+        ProgramArrays pa{left_inputs, right_inputs, outputs, num_operations, final_output_positions,
+                         operators, unary_operators, left_scalars, right_scalars};
+        return perform_operation_host(output_columns, num_outputs, input_columns, num_inputs, pa, chunk_rows);
+    });
+}
+
 int ral_perform_operation_async(gdf_column* const* output_columns, int32_t num_outputs,
                                 gdf_column* const* input_columns, int32_t num_inputs,
                                 const column_index_type* left_inputs, const column_index_type* right_inputs,

@@ -224,7 +224,7 @@ int perform_operation(gdf_column* const* outputs, int n_out, gdf_column* const* 
         slots[L.out_data + o] = (uint64_t)(uintptr_t)outputs[o]->data;
         slots[L.out_valid + o] = (uint64_t)(uintptr_t)outputs[o]->valid;
     }
-    slots[L.counts] = (uint64_t)(uintptr_t)d_counts;
+    slots[L.counts] = (uint64_t)(uintptr_t)(d_counts ? d_counts : opt.device_valid_counts);
     fill_scalars(p, L, slots);
 
     if (n > 0) {
@@ -250,6 +250,147 @@ int perform_operation(gdf_column* const* outputs, int n_out, gdf_column* const* 
     }
     if (int e = check_cuda(cudaGetLastError(), "expression kernel")) return e;
     return kSuccess;
+}
+
+namespace {
+
+// Streams of the host-buffer path, per calling thread.
+struct HostStreams {
+    cudaStream_t s[3] = {nullptr, nullptr, nullptr};
+    cudaEvent_t ready = nullptr;
+    ~HostStreams() {
+        for (cudaStream_t& x : s)
+            if (x) cudaStreamDestroy(x);
+        if (ready) cudaEventDestroy(ready);
+    }
+};
+
+size_t round256(size_t b) { return (b + 255) & ~(size_t)255; }
+
+}  // namespace
+
+int perform_operation_host(gdf_column* const* outputs, int n_out, gdf_column* const* inputs, int n_in,
+                           const ProgramArrays& pa, int64_t chunk_rows) {
+    if (!outputs || !inputs || n_out <= 0 || n_in <= 0) return set_error(kInvalidArgument, "null or empty column list");
+    for (int c = 0; c < n_in; c++)
+        if (!inputs[c]) return set_error(kInvalidArgument, "null input column");
+    for (int o = 0; o < n_out; o++)
+        if (!outputs[o]) return set_error(kInvalidArgument, "null output column");
+    const int64_t n = inputs[0]->size;
+    for (int c = 0; c < n_in; c++)
+        if (inputs[c]->size != n) return set_error(kInvalidArgument, "input columns differ in size");
+    for (int o = 0; o < n_out; o++)
+        if (outputs[o]->size < n) return set_error(kInvalidArgument, "output column shorter than the input");
+    {
+        // the program is checked once up front (dtypes, registers, operators)
+        Program p;
+        if (int rc = build_program(p, outputs, n_out, inputs, n_in, pa, false)) return rc;
+    }
+    if (n == 0) {
+        for (int o = 0; o < n_out; o++) outputs[o]->null_count = 0;
+        return kSuccess;
+    }
+    // chunks start at multiples of 1024 rows: mask offsets are whole words and vector loads stay aligned
+    int64_t chunk = chunk_rows > 0 ? chunk_rows : ((int64_t)4 << 20);
+    chunk = std::max<int64_t>(1024, (chunk + 1023) / 1024 * 1024);
+    if (chunk > n) chunk = (n + 1023) / 1024 * 1024;
+    static thread_local HostStreams hs;
+    for (cudaStream_t& x : hs.s)
+        if (!x && check_cuda(cudaStreamCreateWithFlags(&x, cudaStreamNonBlocking), "cudaStreamCreate")) return kCudaError;
+    if (!hs.ready && check_cuda(cudaEventCreateWithFlags(&hs.ready, cudaEventDisableTiming), "cudaEventCreate"))
+        return kCudaError;
+    // one device area per stream: every input and output column's chunk (data, then mask)
+    auto mask_bytes = [](int64_t rows) { return round256((size_t)gdf_valid_allocation_size(rows)); };
+    size_t per_slot = 0;
+    for (int c = 0; c < n_in; c++)
+        per_slot += round256((size_t)chunk * gdf_dtype_size(inputs[c]->dtype)) + (inputs[c]->valid ? mask_bytes(chunk) : 0);
+    for (int o = 0; o < n_out; o++)
+        per_slot += round256((size_t)chunk * gdf_dtype_size(outputs[o]->dtype)) + (outputs[o]->valid ? mask_bytes(chunk) : 0);
+    char* area[3] = {nullptr, nullptr, nullptr};
+    uint64_t* d_counts = nullptr;
+    int rc = kSuccess;
+    auto release = [&]() {
+        for (int k = 0; k < 3; k++) {
+            cudaStreamSynchronize(hs.s[k]);
+            if (area[k]) cudaFreeAsync(area[k], hs.s[k]);
+        }
+        if (d_counts) cudaFreeAsync(d_counts, hs.s[0]);
+        cudaStreamSynchronize(hs.s[0]);
+    };
+    if ((rc = check_cuda(cudaMallocAsync((void**)&d_counts, sizeof(uint64_t) * n_out, hs.s[0]), "cudaMallocAsync")) ||
+        (rc = check_cuda(cudaMemsetAsync(d_counts, 0, sizeof(uint64_t) * n_out, hs.s[0]), "cudaMemsetAsync"))) {
+        release();
+        return rc;
+    }
+    cudaEventRecord(hs.ready, hs.s[0]);
+    for (int k = 0; k < 3; k++) {
+        if ((rc = check_cuda(cudaMallocAsync((void**)&area[k], per_slot, hs.s[k]), "cudaMallocAsync"))) {
+            release();
+            return rc;
+        }
+        cudaStreamWaitEvent(hs.s[k], hs.ready, 0);
+    }
+    std::vector<gdf_column> vin(n_in), vout(n_out);
+    std::vector<gdf_column*> pin(n_in), pout(n_out);
+    const int64_t nchunks = (n + chunk - 1) / chunk;
+    for (int64_t q = 0; q < nchunks && rc == kSuccess; q++) {
+        const int k = (int)(q % 3);
+        cudaStream_t st = hs.s[k];
+        const int64_t off = q * chunk;
+        const int64_t r = std::min(chunk, n - off);
+        const size_t mb = (size_t)((r + 7) / 8);
+        char* cur = area[k];
+        for (int c = 0; c < n_in; c++) {
+            const size_t w = gdf_dtype_size(inputs[c]->dtype);
+            vin[c] = *inputs[c];
+            vin[c].size = (gdf_size_type)r;
+            vin[c].data = cur;
+            cudaMemcpyAsync(cur, (const char*)inputs[c]->data + off * w, (size_t)r * w, cudaMemcpyHostToDevice, st);
+            cur += round256((size_t)chunk * w);
+            if (inputs[c]->valid) {
+                vin[c].valid = (gdf_valid_type*)cur;
+                cudaMemcpyAsync(cur, (const char*)inputs[c]->valid + off / 8, mb, cudaMemcpyHostToDevice, st);
+                cur += mask_bytes(chunk);
+            }
+            pin[c] = &vin[c];
+        }
+        for (int o = 0; o < n_out; o++) {
+            const size_t w = gdf_dtype_size(outputs[o]->dtype);
+            vout[o] = *outputs[o];
+            vout[o].size = (gdf_size_type)r;
+            vout[o].data = cur;
+            cur += round256((size_t)chunk * w);
+            if (outputs[o]->valid) {
+                vout[o].valid = (gdf_valid_type*)cur;
+                cur += mask_bytes(chunk);
+            }
+            pout[o] = &vout[o];
+        }
+        EvalOptions eo;
+        eo.stream = st;
+        eo.sync = false;
+        eo.device_valid_counts = d_counts;
+        if ((rc = perform_operation(pout.data(), n_out, pin.data(), n_in, pa, eo))) break;
+        for (int o = 0; o < n_out; o++) {
+            const size_t w = gdf_dtype_size(outputs[o]->dtype);
+            cudaMemcpyAsync((char*)outputs[o]->data + off * w, vout[o].data, (size_t)r * w, cudaMemcpyDeviceToHost, st);
+            if (outputs[o]->valid)
+                cudaMemcpyAsync((char*)outputs[o]->valid + off / 8, vout[o].valid, mb, cudaMemcpyDeviceToHost, st);
+        }
+    }
+    if (rc == kSuccess) {
+        for (int k = 1; k < 3; k++) {
+            cudaEventRecord(hs.ready, hs.s[k]);
+            cudaStreamWaitEvent(hs.s[0], hs.ready, 0);
+        }
+        std::vector<uint64_t> h(n_out, 0);
+        cudaMemcpyAsync(h.data(), d_counts, sizeof(uint64_t) * n_out, cudaMemcpyDeviceToHost, hs.s[0]);
+        if (!(rc = check_cuda(cudaStreamSynchronize(hs.s[0]), "host-buffer evaluation")))
+            for (int o = 0; o < n_out; o++) outputs[o]->null_count = outputs[o]->valid ? (gdf_size_type)(n - (int64_t)h[o]) : 0;
+    }
+    release();
+    if (rc == kSuccess) rc = check_cuda(cudaGetLastError(), "host-buffer evaluation");
+    return rc;
 }
 
 }  // namespace ral

@@ -59,7 +59,18 @@ struct EvalOptions {
     // treat every input's validity mask as possibly holding nulls, ignoring
     // null_count (fused filter+project semantics)
     bool ignore_null_count = false;
+    // when non-null (and null_counts is null): device array the kernel adds each output's
+    // number of valid rows to, without any synchronisation; the caller zeroes and reads it
+    uint64_t* device_valid_counts = nullptr;
 };
+
+// perform_operation over columns in host memory: the rows stream through the GPU in chunks of
+// chunk_rows (0: the default), each chunk's host-to-device copies, kernel and device-to-host copies
+// on one of three streams, so that copies in both directions overlap each other and the kernels.
+// Results and null counts are those of perform_operation over the whole columns; host buffers
+// should be page-locked for the copies to overlap.
+int perform_operation_host(gdf_column* const* outputs, int n_out, gdf_column* const* inputs, int n_in,
+                           const ProgramArrays& pa, int64_t chunk_rows);
 
 // perform_operation over gdf_columns.  Outputs are written in place.
 int perform_operation(gdf_column* const* outputs, int n_out, gdf_column* const* inputs, int n_in,

@@ -7,7 +7,7 @@ buffers are device memory held by torch tensors.  Every call goes through
 libralgpu.so (include/ral/ral_c.h); there is no CPU or torch fallback: if the
 library is missing the import of the first entry point raises.
 """
-from .capi import (RalError, lib, perform_operation, perform_operation_async, evaluate_expression,
+from .capi import (RalError, lib, perform_operation, perform_operation_async, perform_operation_host, evaluate_expression,
                    process_filter, execute_project_plan, filter_project, project_output_types,
                    materialize_column, apply_boolean_mask, add_expression_to_plan, get_output_type_expression,
                    debug_program_source, debug_filter_source, jit_stats, kernel_launches, version,
@@ -17,7 +17,7 @@ from .column import Column, Scalar, valid_alloc_size
 from . import dtypes
 
 __all__ = [
-    "RalError", "lib", "perform_operation", "perform_operation_async", "evaluate_expression",
+    "RalError", "lib", "perform_operation", "perform_operation_async", "perform_operation_host", "evaluate_expression",
     "process_filter", "execute_project_plan", "filter_project", "project_output_types",
     "materialize_column", "apply_boolean_mask", "add_expression_to_plan", "get_output_type_expression",
     "debug_program_source", "debug_filter_source", "jit_stats", "kernel_launches", "version", "Column", "Scalar",

@@ -26,6 +26,8 @@ _SIGS = {
     "ral_version": (C.c_char_p, []),
     "ral_perform_operation": (C.c_int, [COLPP, C.c_int32, COLPP, C.c_int32, I16P, I16P, I16P, C.c_int32, I16P,
                                         I32P, I32P, SCP, SCP, I16P, C.c_int32]),
+    "ral_perform_operation_host": (C.c_int, [COLPP, C.c_int32, COLPP, C.c_int32, I16P, I16P, I16P, C.c_int32, I16P,
+                                             I32P, I32P, SCP, SCP, C.c_int64]),
     "ral_perform_operation_async": (C.c_int, [COLPP, C.c_int32, COLPP, C.c_int32, I16P, I16P, I16P, C.c_int32,
                                               I16P, I32P, I32P, SCP, SCP, P, C.POINTER(C.c_int64)]),
     "ral_evaluate_expression": (C.c_int, [COLPP, C.c_int32, C.c_char_p, C.POINTER(GdfColumn)]),
@@ -165,6 +167,23 @@ def perform_operation(output_columns: List[Column], input_columns: List[Column],
     nii = _i16(new_input_indices if new_input_indices is not None else list(range(len(input_columns))))
     _check(lib().ral_perform_operation(oa, len(output_columns), ia, len(input_columns), _p16(l), _p16(r), _p16(o),
                                        len(l), _p16(f), _p32(b), _p32(u), ls, rs, _p16(nii), len(nii)))
+
+
+def perform_operation_host(output_columns: List[Column], input_columns: List[Column], left_inputs, right_inputs,
+                           outputs, final_output_positions, operators, unary_operators, left_scalars, right_scalars,
+                           chunk_rows: int = 0) -> None:
+    """perform_operation over columns whose buffers are in host memory (pinned for overlap); the
+    rows stream through the GPU in chunks.  Output null counts are filled in."""
+    oa, ostructs = _colarray(output_columns)
+    ia, _is = _colarray(input_columns)
+    l, r, o, f = _i16(left_inputs), _i16(right_inputs), _i16(outputs), _i16(final_output_positions)
+    b, u = _i32(operators), _i32(unary_operators)
+    ls = _scalars([_as_scalar(s) for s in left_scalars])
+    rs = _scalars([_as_scalar(s) for s in right_scalars])
+    _check(lib().ral_perform_operation_host(oa, len(output_columns), ia, len(input_columns), _p16(l), _p16(r),
+                                            _p16(o), len(l), _p16(f), _p32(b), _p32(u), ls, rs, int(chunk_rows)))
+    for c, st in zip(output_columns, ostructs):
+        c.null_count = st.null_count
 
 
 def perform_operation_async(output_columns: List[Column], input_columns: List[Column], left_inputs, right_inputs,

@@ -68,6 +68,24 @@ int ral_perform_operation_async(gdf_column *const *output_columns, int32_t num_o
                                 const gdf_scalar *right_scalars, void *stream, int64_t *null_counts);
 
 /*
+ * perform_operation over columns in HOST memory (no reference counterpart; the reference's
+ * perform_operation, src/Interpreter/interpreter_cpp.h:25-37, takes device columns).  The
+ * gdf_column data and valid pointers are host pointers; the rows stream through the GPU in chunks
+ * of chunk_rows (rounded up to a multiple of 1024; 0 = 4Mi rows), each chunk's copies to the
+ * device, kernel and copies back on one of three streams, so that copies in both directions
+ * overlap the kernels.  Same results as perform_operation over device copies of the columns;
+ * output null_count is filled in.  Page-locked host buffers are needed for the overlap.
+ * Synchronous.
+ */
+int ral_perform_operation_host(gdf_column *const *output_columns, int32_t num_outputs,
+                               gdf_column *const *input_columns, int32_t num_inputs,
+                               const column_index_type *left_inputs, const column_index_type *right_inputs,
+                               const column_index_type *outputs, int32_t num_operations,
+                               const column_index_type *final_output_positions, const int32_t *operators,
+                               const int32_t *unary_operators, const gdf_scalar *left_scalars,
+                               const gdf_scalar *right_scalars, int64_t chunk_rows);
+
+/*
  * evaluate_expression — src/LogicalFilter.h:20-23 (src/LogicalFilter.cpp:271-371).
  * Compiles one Calcite RexNode expression over the frame's columns and
  * evaluates it into `output` (caller-allocated, n rows).  For an expression

@@ -576,3 +576,34 @@ def test_multiply_by_comparison_and_abs_on_special_values():
     dev, ora = H.run_program_both(spec, [D.GDF_FLOAT64] * 4, prog)
     for k, (g, e) in enumerate(zip(dev, ora)):
         H.assert_columns_equal(g, e, what=f"output {k}", check_null_count=False)
+
+
+@pytest.mark.parametrize("pinned", [True, False])
+def test_host_buffer_evaluation_matches_device_columns(pinned):
+    """ral_perform_operation_host streams host columns through the GPU in chunks (here three
+    full chunks and a partial one, on three streams) and gives the device call's bits and null
+    counts; page-locked or not."""
+    n = 3_000_123
+    spec = W.fused_project_program()
+    host = W.fused_project_host(n, seed=5)
+    dev_in = H.to_device(host)
+    dev_out = [R.Column.empty(t, n) for t in spec.output_dtypes]
+    R.perform_operation(dev_out, dev_in, spec.left, spec.right, spec.outputs, spec.final, spec.ops, spec.uops,
+                        spec.lscalars, spec.rscalars)
+
+    def host_copy(t):
+        t = t.cpu()
+        return t.pin_memory() if pinned else t
+
+    hin = [R.Column(host_copy(c.data), host_copy(c.valid), c.dtype, size=n, null_count=c.null_count) for c in dev_in]
+    hout = []
+    for t in spec.output_dtypes:
+        c = R.Column.empty(t, n, device="cpu")
+        hout.append(R.Column(host_copy(c.data), host_copy(c.valid), t, size=n))
+    R.perform_operation_host(hout, hin, spec.left, spec.right, spec.outputs, spec.final, spec.ops, spec.uops,
+                             spec.lscalars, spec.rscalars, chunk_rows=1_000_000)
+    for k, (g, e) in enumerate(zip(hout, dev_out)):
+        ev = e.valid_bools()
+        assert np.array_equal(g.valid_bools(), ev), f"output {k}: masks differ"
+        assert np.array_equal(g.to_numpy()[ev].view(np.uint8), e.to_numpy()[ev].view(np.uint8)), f"output {k}: data"
+        assert g.null_count == int((~ev).sum())
