@@ -52,3 +52,28 @@ def test_invalid_program_rejected_without_gpu():
     rc = L.ral_perform_operation(arr, 1, arr, 0, None, None, None, 0, None, None, None, None, None, None, 0)
     assert rc == 1
     assert b"input" in L.ral_last_error()
+
+
+def test_host_buffer_evaluation_checks_arguments_before_any_cuda_call():
+    """ral_perform_operation_host validates columns and the program on the host; an empty frame
+    returns at once with zero null counts."""
+    import numpy as np
+    from ralgpu import dtypes as D
+    from ralgpu import workloads as W
+    spec = W.fused_project_program()
+    cols = [ralgpu.Column.from_numpy(np.zeros(8, dtype=np.int64 if t == D.GDF_INT64 else
+                                              (np.float64 if t == D.GDF_FLOAT64 else np.int32)), t, None, device="cpu")
+            for t in spec.input_dtypes]
+    outs = [ralgpu.Column.empty(t, 8, device="cpu") for t in spec.output_dtypes]
+    args = (spec.left, spec.right, spec.outputs, spec.final, spec.ops, spec.uops, spec.lscalars, spec.rscalars)
+    short = ralgpu.Column.from_numpy(np.zeros(4, dtype=np.int32), D.GDF_INT32, None, device="cpu")
+    with pytest.raises(ralgpu.RalError, match="differ in size"):
+        ralgpu.perform_operation_host(outs, cols[:4] + [short], *args)
+    with pytest.raises(ralgpu.RalError, match="shorter"):
+        ralgpu.perform_operation_host([ralgpu.Column.empty(t, 2, device="cpu") for t in spec.output_dtypes], cols, *args)
+    empty = [ralgpu.Column.from_numpy(np.zeros(0, dtype=c.to_numpy().dtype), c.dtype, None, device="cpu") for c in cols]
+    eouts = [ralgpu.Column.empty(t, 0, device="cpu") for t in spec.output_dtypes]
+    for c in eouts:
+        c.null_count = 5
+    ralgpu.perform_operation_host(eouts, empty, *args)
+    assert all(c.null_count == 0 for c in eouts)
