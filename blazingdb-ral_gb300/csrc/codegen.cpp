@@ -696,13 +696,15 @@ GeneratedKernel generate_filter_kernel(const FilterSpec& f, const Shape& s, bool
         }
     }
 
-    // ---- kernel: one warp-sized chunk of 32*G*J rows per ticket, no block-wide barriers.
-    // Pass 1 evaluates the predicate over the chunk into packed keep bits (G bits per lane and
-    // slice, in registers); the warp then publishes its kept count and looks back over the
-    // preceding chunks; pass 2 recomputes each slice's ranks from the bits and writes every
-    // output.  While one warp waits in its look-back the other warps of the SM keep loading.
-    // columns the predicate reads: loaded with normal eviction, so that a second read by the
-    // gather or the projection hits in cache instead of DRAM
+    // ---- kernel: warp-sized chunks of 32*G*J rows taken by ticket, no block-wide barriers.
+    // Pass 1 evaluates the predicate over a chunk into keep bits; the warp publishes the chunk's
+    // kept count and looks back over the preceding chunks for its output offset; pass 2 writes
+    // every output.  Pass 2 walks the chunk's kept-row list, 32 kept rows per step (dense, the
+    // default), or takes each slice's rows lane by lane from packed keep bits (D=0).  Dense full
+    // kernels with chunks of at most 32 mask words hold two chunks per warp: the next chunk's
+    // pass 1 and published count come before the look-back and pass 2 of the last one.
+    // Columns the predicate reads are loaded with normal eviction, so that a second read by the
+    // gather or the projection hits in cache instead of DRAM.
     std::vector<bool> pred_col(NF, false);
     if (f.clone_stencil) pred_col[f.clone_column] = true;
     for (size_t c = 0; c < f.predicate_cols.size(); c++)

@@ -26,7 +26,7 @@ size_t round_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
 constexpr double kAgeRowsPerSecond = 1e10;
 
 // Item shape of a query: vector width from the widest column, chunks of RAL_SERVER_CHUNK rows
-// (default 2048, the single-launch filter's), predicate unroll 2, and the FP64 instructions
+// (default 2048; 1024 measured the same), predicate unroll 2, and the FP64 instructions
 // (RAL_SERVER_SOFT_FP=1 for the integer-pipe double operations: measured 1656 requests/s at
 // capacity against 1756 with the FP64 instructions).
 Shape query_shape(const FilterPlan& plan, bool aligned16) {
@@ -44,8 +44,8 @@ Shape query_shape(const FilterPlan& plan, bool aligned16) {
     return sh;
 }
 
-// Register cap of the served chunk functions (RAL_SERVER_MAXRREG, default 64: four blocks per
-// SM, as the single-launch filter + project kernel runs fastest).
+// Register cap of the served chunk functions and their dispatcher (RAL_SERVER_MAXRREG, default
+// 64: four 256-thread blocks per SM).
 int server_max_registers() {
     const char* e = std::getenv("RAL_SERVER_MAXRREG");
     const int v = e ? std::atoi(e) : 0;
