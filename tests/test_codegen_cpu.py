@@ -137,3 +137,22 @@ def test_projection_filter_pipelines_two_chunks_per_warp(monkeypatch):
     src, log = ralgpu.debug_filter_source(p.input_dtypes, [1] * 5, W.filter_project_filter(0.5),
                                           W.FILTER_PROJECT_PROJECT, compile=True)
     assert "chunkA" not in src and "s_lst[actA ? kA : k0]" in src and spills(log) == 0
+
+
+def _registers(log: str) -> int:
+    m = re.findall(r"Used (\d+) registers", log)
+    return max(int(x) for x in m) if m else 0
+
+
+def test_default_shapes_keep_their_occupancy():
+    """The measured defaults rely on resident warps: the 12-op projection as two 512-thread blocks
+    per SM (at most 64 registers) and the fused filter + project as five 256-thread blocks (at most
+    51), both without spills."""
+    p = W.fused_project_program()
+    src, log = compile_spec(p)
+    assert "#define RAL_THREADS 512" in src and "__launch_bounds__(RAL_THREADS, 2)" in src
+    assert spills(log) == 0 and _registers(log) <= 64, log
+    src, log = ralgpu.debug_filter_source(p.input_dtypes, [1] * 5, W.filter_project_filter(0.5),
+                                          W.FILTER_PROJECT_PROJECT, compile=True)
+    assert "__launch_bounds__(RAL_THREADS, 5)" in src
+    assert spills(log) == 0 and _registers(log) <= 51, log
