@@ -96,19 +96,26 @@ class ClockSampler:
         self.t1 = time.monotonic()
 
     def stop(self):
+        """Ends sampling; summary of the window [mark_start, mark_end]."""
+        if self.proc is not None:
+            time.sleep(0.1)
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+        return self.window(self.t0, self.t1)
+
+    def window(self, t0, t1):
+        """Median SM clock, max clock and throttle reasons of the samples taken in [t0, t1]."""
         if self.proc is None:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"], "samples": 0}
-        time.sleep(0.1)
-        self.proc.terminate()
-        try:
-            self.proc.wait(timeout=5)
-        except Exception:
-            self.proc.kill()
-        inside = [ln for t, ln in self.lines if self.t0 is not None and self.t0 <= t <= self.t1 + 0.05]
+        lines = list(self.lines)
+        inside = [ln for t, ln in lines if t0 is not None and t0 <= t <= t1 + 0.05]
         window = "timed region"
         if not inside:
             # a very short timed region: take the samples nearest to it
-            near = sorted(self.lines, key=lambda x: abs(x[0] - (self.t0 or 0)))[:3]
+            near = sorted(lines, key=lambda x: abs(x[0] - (t0 or 0)))[:3]
             inside = [ln for _, ln in near]
             window = "nearest samples (timed region shorter than the sampling period)"
         sm, smax, power, reasons = [], [], [], set()
@@ -225,8 +232,22 @@ def cpu_time(workload, rows, threads, selectivity):
     return cpu_filter_gather(rows, threads, selectivity)
 
 
-def cpu_baseline(workload, full_rows, selectivity, budget_s=12.0):
-    """rows/s of the oracle on all cores over a bounded sample sized for about budget_s of work."""
+def cpu_model() -> str:
+    """The host CPU's model name (lscpu), for the record of where the CPU figures were taken."""
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for ln in out.splitlines():
+            if ln.strip().lower().startswith("model name"):
+                return ln.split(":", 1)[1].strip()
+    except Exception:
+        pass
+    import platform
+    return platform.processor() or platform.machine()
+
+
+def cpu_baseline(workload, full_rows, selectivity, budget_s=12.0, single_budget_s=4.0):
+    """rows/s of the oracle on all cores over a bounded sample sized for about budget_s of work, and
+    on one thread over a sample sized for about single_budget_s."""
     threads = os.cpu_count() or 1
     probe = min(full_rows, 2_000_000)
     dt = cpu_time(workload, probe, threads, selectivity)
@@ -234,8 +255,17 @@ def cpu_baseline(workload, full_rows, selectivity, budget_s=12.0):
     rows = int(min(full_rows, max(probe, rate * budget_s / 3)))
     times = [cpu_time(workload, rows, threads, selectivity) for _ in range(3)]
     t = statistics.median(times)
-    return {"value": rows / t, "unit": "rows/s", "cores": threads, "kind": "port",
-            "sample": f"{rows} of {full_rows} rows, median of 3 runs, {threads} threads"}
+    out = {"value": rows / t, "unit": "rows/s", "cores": threads, "kind": "port",
+           "sample": f"{rows} of {full_rows} rows, median of 3 runs, {threads} threads",
+           "cpu_model": cpu_model()}
+    if single_budget_s > 0:
+        p1 = min(full_rows, 200_000)
+        d1 = cpu_time(workload, p1, 1, selectivity)
+        r1 = int(min(full_rows, max(p1, (p1 / max(d1, 1e-9)) * single_budget_s / 3)))
+        t1 = statistics.median([cpu_time(workload, r1, 1, selectivity) for _ in range(3)])
+        out["single_thread"] = {"value": r1 / t1, "unit": "rows/s", "cores": 1,
+                                "sample": f"{r1} of {full_rows} rows, median of 3 runs, 1 thread"}
+    return out
 
 
 def cpu_batched(threads: int, n_programs: int, rows_cap: int, seed: int = 20261203):
@@ -288,6 +318,34 @@ def cpu_served(threads: int, n_queries: int, rows_cap: int, seed: int = 20261203
 
 # ---- GPU workloads --------------------------------------------------------------------------------
 
+DEFAULT_ROWS = {"fused_project": 200_000_000, "plain_vm": 1_000_000, "filter_gather": 500_000_000,
+                "filter_project": 200_000_000}
+
+
+def workload_config(workload, n, selectivity, world=1):
+    """The `config` object of a workload: the same dict on both arms of the benchmark."""
+    if workload == "fused_project":
+        cfg = {"workload": "fused_project", "rows": n, "inputs": "a,b int64; x,y float64; k int32; 5% nulls",
+               "program_ops": 12, "outputs": "f1,f2 float64; i1 int64",
+               "l2": "inputs (12.2 GB at 200M rows) exceed L2; no flush"}
+    elif workload == "filter_project":
+        cfg = {"workload": "filter_project", "rows": n, "selectivity": selectivity,
+               "filter": f"k < {int(round(1000 * selectivity))}", "project": "f1, f2, i1 of the 12-op program",
+               "inputs": "a,b int64; x,y float64; k int32; 5% nulls", "fused": "filter+project in one kernel",
+               "l2": "inputs exceed L2; no flush"}
+    elif workload == "plain_vm":
+        cfg = {"workload": "plain_vm", "rows": n, "filter": "((c2>=24 AND c1<0.05) OR c0%7=3) AND c3<1200",
+               "project": "c1*(1-c1)+c2", "fused": "filter+project in one kernel",
+               "l2": "1M rows (24 MB) fit in L2: per-call latency bound"}
+    else:
+        from ralgpu import workloads as W
+        cfg = {"workload": "filter_gather", "rows": n, "selectivity": selectivity,
+               "predicate": f"<($0, {W.FILTER_THRESHOLDS[selectivity]})", "gathered_columns": 6,
+               "l2": "inputs exceed L2; no flush"}
+    cfg["parallelism"] = f"replicas x{world}"
+    return cfg
+
+
 def fused_project_setup(n, device):
     import torch
     import ralgpu as R
@@ -305,10 +363,7 @@ def fused_project_setup(n, device):
         R.perform_operation_async(outs, cols, spec.left, spec.right, spec.outputs, spec.final, spec.ops, spec.uops,
                                   spec.lscalars, spec.rscalars, stream=stream)
 
-    return dict(step=step, alg_bytes=alg_bytes, cols=cols, outs=outs, spec=spec,
-                config={"workload": "fused_project", "rows": n, "inputs": "a,b int64; x,y float64; k int32; 5% nulls",
-                        "program_ops": len(spec.ops), "outputs": "f1,f2 float64; i1 int64",
-                        "l2": "inputs (12.2 GB at 200M rows) exceed L2; no flush"})
+    return dict(step=step, alg_bytes=alg_bytes, cols=cols, outs=outs, spec=spec)
 
 
 def fused_project_e2e(ctx, steps, device):
@@ -349,7 +404,7 @@ def _colarray(cols):
     return arr, structs
 
 
-def filter_setup(workload, n, selectivity, device):
+def filter_setup(workload, n, selectivity, device, null_rate=None):
     """plain_vm (fused filter + project) or filter_gather (fused filter over 6 columns)."""
     import ctypes
     import torch
@@ -365,10 +420,6 @@ def filter_setup(workload, n, selectivity, device):
         outs = [R.Column.empty(t, n) for t in types]
         in_b = [R.dtypes.WIDTH[c.dtype] + 1 / 8 for c in frame]   # every column (+ mask) is read
         out_b = sum(R.dtypes.WIDTH[t] + 1 / 8 for t in types)
-        cfg = {"workload": "filter_project", "rows": n, "selectivity": selectivity,
-               "filter": f"k < {int(round(1000 * selectivity))}", "project": "f1, f2, i1 of the 12-op program",
-               "inputs": "a,b int64; x,y float64; k int32; 5% nulls", "fused": "filter+project in one kernel",
-               "l2": "inputs exceed L2; no flush"}
     elif workload == "plain_vm":
         spec = W.plain_vm_host(n)
         frame = [R.Column.from_numpy(v, t, m) for t, v, m in spec]
@@ -377,19 +428,14 @@ def filter_setup(workload, n, selectivity, device):
         outs = [R.Column.empty(t, n) for t in types]
         in_b = [8 + 0, 8 + 1 / 8, 4, 4]          # c0, c1 (+mask), c2, c3 read by the predicate / projection
         out_b = 8 + 1 / 8
-        cfg = {"workload": "plain_vm", "rows": n, "filter": "((c2>=24 AND c1<0.05) OR c0%7=3) AND c3<1200",
-               "project": "c1*(1-c1)+c2", "fused": "filter+project in one kernel"}
     else:
         frame = []
-        for t, data, valid, nulls in W.filter_gather_device(n, device=device):
+        for t, data, valid, nulls in W.filter_gather_device(n, device=device, null_rate=null_rate):
             frame.append(R.Column(data, valid, t, size=n, null_count=nulls))
         fq, pq = W.filter_gather_query(selectivity), None
         outs = [R.Column.empty(c.dtype, n, with_valid=c.valid is not None) for c in frame]
         in_b = [R.dtypes.WIDTH[c.dtype] for c in frame]
         out_b = sum(in_b)
-        cfg = {"workload": "filter_gather", "rows": n, "selectivity": selectivity,
-               "predicate": f"<($0, {W.FILTER_THRESHOLDS[selectivity]})", "gathered_columns": 6,
-               "l2": "inputs exceed L2; no flush"}
     fa, fs = _colarray(frame)
     oa, os_ = _colarray(outs)
     nout = ctypes.c_int32(0)
@@ -406,7 +452,7 @@ def filter_setup(workload, n, selectivity, device):
         k = nout.value
         return n * sum(in_b) + k * out_b + 8
 
-    return dict(step=step, alg_bytes_fn=alg_bytes, nout=nout, cols=frame, outs=outs, config=cfg)
+    return dict(step=step, alg_bytes_fn=alg_bytes, nout=nout, cols=frame, outs=outs, out_structs=os_, fq=fq, pq=pq)
 
 
 def filter_e2e(ctx, steps):
@@ -450,21 +496,113 @@ def filter_e2e(ctx, steps):
             "ms_per_step": ms}
 
 
-def run_ours(args):
+# ---- full-size parity: the oracle as the checker, outside every timed region ----------------
+
+PARITY_CHUNK = 1 << 24   # input rows per oracle chunk (a multiple of 64: chunk masks start on a byte)
+
+
+def _bits_np(valid, s, e):
+    """Validity bits [s, e) of a packed device mask as a numpy bool array."""
+    import numpy as np
+    if valid is None:
+        return np.ones(e - s, dtype=bool)
+    raw = valid[s // 8:(e + 7) // 8].cpu().numpy()
+    return np.unpackbits(raw, bitorder="little")[s % 8:s % 8 + (e - s)].astype(bool)
+
+
+def _oracle_chunk(cols, s, e):
+    """Oracle columns holding rows [s, e) of device columns; each keeps its whole column's null count,
+    which the interpreter's validity pass reads (null_count == 0 means all-valid)."""
+    import numpy as np
+    import oracle as O
+    out = []
+    for c in cols:
+        data = np.ascontiguousarray(c.data[s:e].cpu().numpy())
+        if c.valid is None:
+            out.append(O.OColumn(data, None, c.dtype, 0))
+        else:
+            out.append(O.make_column(data, c.dtype, _bits_np(c.valid, s, e), null_count=c.null_count))
+    return out
+
+
+def _compare(gpu_col, g0, g1, oc, stats):
+    """Rows [g0, g1) of a device output against an oracle column: validity bits, and the data bits
+    of every valid row (data under a null is unspecified)."""
+    import numpy as np
+    gv = _bits_np(gpu_col.valid, g0, g1)
+    ov = oc.valid_bools()[:g1 - g0] if oc.valid is not None else np.ones(g1 - g0, dtype=bool)
+    if gpu_col.valid is not None or oc.valid is not None:
+        stats["valid"] += int((gv != ov).sum())
+    m = gv & ov
+    gd = gpu_col.data[g0:g1].cpu().numpy()
+    od = oc.data[:g1 - g0]
+    u = {1: np.uint8, 2: np.uint16, 4: np.uint32, 8: np.uint64}[gd.dtype.itemsize]
+    stats["data"] += int((gd.view(u)[m] != od.astype(gd.dtype, copy=False).view(u)[m]).sum())
+
+
+def parity_check(workload, ctx, selectivity):
+    """Runs the oracle over every input row of the last timed step (in chunks of PARITY_CHUNK rows on
+    all host threads) and compares every output row bit for bit: data of valid rows, validity bits,
+    null counts, the kept row count and row order."""
+    import oracle as O
+    from ralgpu import workloads as W
+    t0 = time.perf_counter()
+    threads = os.cpu_count() or 1
+    cols, outs = ctx["cols"], ctx["outs"]
+    n = cols[0].size
+    stats = {"valid": 0, "data": 0, "rows_out": 0, "null_count": 0}
+    kept = 0
+    nulls = [0] * len(outs)
+    for s in range(0, n, PARITY_CHUNK):
+        e = min(n, s + PARITY_CHUNK)
+        chunk = _oracle_chunk(cols, s, e)
+        if workload == "fused_project":
+            spec = ctx["spec"]
+            from oracle import frontend as fe
+            exp = [O.alloc_column(t, e - s) for t in spec.output_dtypes]
+            O.perform_operation(exp, chunk, spec.left, spec.right, spec.outputs, spec.final, spec.ops, spec.uops,
+                                [fe.Scalar(*x) for x in spec.lscalars], [fe.Scalar(*x) for x in spec.rscalars],
+                                nthreads=threads)
+            g0, k = s, e - s
+        else:
+            f = O.process_filter(chunk, ctx["fq"], nthreads=threads)
+            exp = f if ctx["pq"] is None else O.execute_project_plan(f, ctx["pq"], nthreads=threads)
+            k = exp[0].size
+            g0 = kept
+            for i, oc in enumerate(exp):
+                O.update_null_count(oc)
+                nulls[i] += oc.null_count
+        for gcol, oc in zip(outs, exp):
+            if k:
+                _compare(gcol, g0, g0 + k, oc, stats)
+        kept += k
+    out = {"rows": n, "chunks": (n + PARITY_CHUNK - 1) // PARITY_CHUNK, "oracle_threads": threads}
+    if "nout" in ctx:
+        got = ctx["nout"].value
+        stats["rows_out"] = abs(got - kept)
+        out["rows_out"] = got
+        for i, st in enumerate(ctx["out_structs"]):
+            stats["null_count"] += int(st.null_count != nulls[i])
+    out["mismatches"] = sum(stats.values())
+    out["detail"] = stats
+    out["checked"] = ("every output row, bit for bit: data of valid rows, validity bits"
+                      + (", null counts, kept row count and row order" if "nout" in ctx else ""))
+    out["seconds"] = round(time.perf_counter() - t0, 2)
+    return out
+
+
+def measure_workload(args, workload, n, selectivity, device, world, sampler, e2e=True, cpu=True, parity=True,
+                     cpu_budget_s=12.0):
+    """One workload: warm-up, the timed steps (CUDA events on the launching stream, max over ranks),
+    the roofline of its kernel, and on rank 0 the e2e, CPU baseline and full-size parity legs."""
     import torch
     import ralgpu as R
-    world, rank, local = dist_setup(args)
-    torch.cuda.set_device(local)
-    device = f"cuda:{local}"
-    n = args.rows or {"fused_project": 200_000_000, "plain_vm": 1_000_000, "filter_gather": 500_000_000,
-                      "filter_project": 200_000_000}[args.workload]
-    if args.workload == "fused_project":
+    rank = int(os.environ.get("RANK", "0"))
+    if workload == "fused_project":
         ctx = fused_project_setup(n, device)
     else:
-        ctx = filter_setup(args.workload, n, args.selectivity, device)
+        ctx = filter_setup(workload, n, selectivity, device)
     stream = torch.cuda.current_stream()
-    sampler = ClockSampler(local)
-    sampler.start()
     for _ in range(args.warmup):
         ctx["step"](stream)
     torch.cuda.synchronize()
@@ -474,7 +612,7 @@ def run_ours(args):
     torch.cuda.synchronize()
     t_start = torch.cuda.Event(enable_timing=True)
     t_end = torch.cuda.Event(enable_timing=True)
-    sampler.mark_start()
+    w0 = time.monotonic()
     t_start.record()
     for s, e in events:
         s.record()
@@ -482,48 +620,112 @@ def run_ours(args):
         e.record()
     t_end.record()
     torch.cuda.synchronize()
-    sampler.mark_end()
+    w1 = time.monotonic()
     launches = R.kernel_launches() - launches0
-    clocks = sampler.stop()
     barrier(world)
-    total_ms = t_start.elapsed_time(t_end)
-    total_ms = max_over_ranks(world, total_ms)
+    total_ms = max_over_ranks(world, t_start.elapsed_time(t_end))
     kernel_ms = statistics.mean(s.elapsed_time(e) for s, e in events)
     ms_per_step = total_ms / args.steps
-    value = job_rate(world, n, ms_per_step)
     peak, peak_kind = load_peaks()
     alg = ctx["alg_bytes"] if "alg_bytes" in ctx else ctx["alg_bytes_fn"]()
     achieved = alg / (kernel_ms / 1e3) / 1e9
-    traffic_key = args.workload if args.workload not in ("filter_gather", "filter_project") \
-        else f"{args.workload}_{args.selectivity}"
-    traffic = load_traffic(traffic_key)
+    traffic_key = workload if workload not in ("filter_gather", "filter_project") else f"{workload}_{selectivity}"
     out = {
-        "metric": METRIC, "value": value, "unit": "rows/s", "n_gpus": world, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded, generated on the GPU)",
-        "config": dict(ctx["config"], parallelism=f"replicas x{world}"),
-        "hbm_gbs": achieved,
+        "workload": workload, "value": job_rate(world, n, ms_per_step), "unit": "rows/s", "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_per_step,
+        "config": workload_config(workload, n, selectivity, world),
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "peak_kind": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else peak_kind,
-                     "frac_of_8tbs": achieved / 8000.0, "traffic": traffic,
+                     "frac_of_8tbs": achieved / 8000.0, "traffic": load_traffic(traffic_key),
                      "algorithmic_bytes_per_launch": alg, "kernel_ms": kernel_ms},
         "gpu_launches": int(launches),
-        "clocks": clocks,
+        "clocks": sampler.window(w0, w1),
     }
     if "nout" in ctx:
-        out["config"]["rows_out"] = ctx["nout"].value
-        out["dtype"] = "int32/int64/f32/f64/date32/bool8 gather" if args.workload == "filter_gather" else "f64+int"
+        out["rows_out"] = ctx["nout"].value
     if rank == 0:
-        if not args.skip_e2e and args.workload == "fused_project":
-            out["e2e"] = fused_project_e2e(ctx, max(2, min(args.steps, 3)), device)
-        elif not args.skip_e2e:
-            out["e2e"] = filter_e2e(ctx, max(2, min(args.steps, 3)))
-        if not args.skip_cpu:
-            out["cpu_baseline"] = cpu_baseline(args.workload, n, args.selectivity)
+        # the device outputs of the last timed step are checked before the e2e leg reuses the columns
+        if parity and not args.skip_parity:
+            out["parity"] = parity_check(workload, ctx, selectivity)
+        if e2e and not args.skip_e2e:
+            out["e2e"] = (fused_project_e2e(ctx, max(2, min(args.steps, 3)), device) if workload == "fused_project"
+                          else filter_e2e(ctx, max(2, min(args.steps, 3))))
+        if cpu and not args.skip_cpu:
+            out["cpu_baseline"] = cpu_baseline(workload, n, selectivity, budget_s=cpu_budget_s,
+                                               single_budget_s=cpu_budget_s / 3)
+    del ctx
+    torch.cuda.empty_cache()
+    return out
+
+
+# Workloads measured beside the default one in the same run: the 200M-row fused filter + project at
+# s = 0.5 (the target kernel) and the 500M-row filter + gather of six columns at s = 0.5.
+EXTRA_WORKLOADS = [("filter_project", 0.5), ("filter_gather", 0.5)]
+
+
+def run_ours(args):
+    import torch
+    world, rank, local = dist_setup(args)
+    torch.cuda.set_device(local)
+    device = f"cuda:{local}"
+    n = args.rows or DEFAULT_ROWS[args.workload]
+    sampler = ClockSampler(local)
+    sampler.start()
+    main = measure_workload(args, args.workload, n, args.selectivity, device, world, sampler)
+    extra = {}
+    if args.workload == "fused_project" and not args.rows and not args.no_extra:
+        for wl, sel in EXTRA_WORKLOADS:
+            extra[f"{wl}_s{sel}"] = measure_workload(args, wl, DEFAULT_ROWS[wl], sel, device, world, sampler,
+                                                     cpu_budget_s=6.0)
+    sampler.stop()
+    out = {
+        "metric": METRIC, "value": main["value"], "unit": "rows/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": main["ms_per_step"], "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": {"fused_project": "f64+int64", "filter_project": "f64+int64", "plain_vm": "f64+int64",
+                  "filter_gather": "int32/int64/f32/f64/date32/bool8 gather"}[args.workload],
+        "data": "synthetic (seeded, generated on the GPU)",
+        "config": main["config"],
+        "hbm_gbs": main["roofline"]["achieved"],
+        "roofline": main["roofline"],
+        "gpu_launches": main["gpu_launches"] + sum(b["gpu_launches"] for b in extra.values()),
+        "gpu_launches_main": main["gpu_launches"],
+        "clocks": main["clocks"],
+    }
+    for k in ("rows_out", "parity", "e2e", "cpu_baseline"):
+        if k in main:
+            out[k] = main[k]
+    if extra:
+        out["extra_workloads"] = extra
+    if rank == 0:
         print(json.dumps(out), flush=True)
     if world > 1:
         import torch.distributed as dist
         dist.destroy_process_group()
+
+
+def batched_config(args, world=1):
+    """`config` of the batched workload (the same dict on both arms)."""
+    from ralgpu import workloads as W
+    mix = W.batched_mix(args.programs, seed=args.seed)
+    rows = sum(min(t.rows, args.max_rows) if args.max_rows else t.rows for t in mix)
+    return {"workload": "batched", "programs": len(mix), "rows_total": int(rows), "ops": "4-48 per program",
+            "rows_per_table": "log-uniform [1e3, 5e7]", "columns": "2-8 of int32/int64/f32/f64, 0-20% nulls",
+            "seed": args.seed, "parallelism": f"replicas x{world}", "max_rows": args.max_rows or None,
+            "l2": "inputs of the whole batch (tens of GB) exceed L2; no flush"}
+
+
+def served_config(args, world=1):
+    """`config` of the served workload (the same dict on both arms)."""
+    from ralgpu import workloads as W
+    tabs = W.served_tables(args.tables, seed=args.seed, max_rows=args.max_rows or 1e8)
+    n_rate = max(50, args.requests // 5)
+    return {"workload": "served", "tables": len(tabs), "rows_resident": int(sum(t.rows for t in tabs)),
+            "queries": args.queries, "ops": "4-32 per request (filter + project)", "nulls": "5% per column",
+            "requests": int(n_rate * 5), "arrivals": "Poisson, 5 rates",
+            "budget_gb": args.budget_gb, "max_waves": args.waves, "wave_rows": args.wave_rows or "default",
+            "parallelism": f"replicas x{world}",
+            "l2": "tables of up to 1e8 rows exceed L2; no flush"}
 
 
 def batched_setup(n_programs, seed, device, max_rows=0):
@@ -686,10 +888,7 @@ def run_batched(args):
         "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "int32/int64/f32/f64 (VM registers int64/f64)",
         "data": "synthetic (seeded, generated on the GPU)",
-        "config": {"workload": "batched", "programs": len(progs), "rows_total": rows, "ops": "4-48 per program",
-                   "rows_per_table": "log-uniform [1e3, 5e7]", "columns": "2-8 of int32/int64/f32/f64, 0-20% nulls",
-                   "seed": args.seed, "parallelism": f"replicas x{world}", "max_rows": args.max_rows or None,
-                   "l2": "inputs of the whole batch (tens of GB) exceed L2; no flush"},
+        "config": batched_config(args, world),
         "batched": {"launch": "one persistent kernel per step, replayed as a CUDA graph",
                     "kernel": info, "ms_per_step": ms_per_step,
                     "prepare_s": round(prep_s, 2), "autotune_s": round(tune_s, 2), "tuned_keys": len(tuned),
@@ -831,12 +1030,7 @@ def run_served(args):
         "steps": len(per_rate), "warmup": 1, "ms_per_step": None, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "int32/int64/f32/f64/date32 (VM registers int64/f64)",
         "data": "synthetic (seeded, generated on the GPU)",
-        "config": {"workload": "served", "tables": len(tabs), "rows_resident": int(sum(t.rows for t in tabs)),
-                   "queries": len(qs), "ops": "4-32 per request (filter + project)", "nulls": "5% per column",
-                   "requests": int(n_rate * len(per_rate)), "arrivals": "Poisson, 5 rates",
-                   "budget_gb": args.budget_gb, "max_waves": args.waves, "wave_rows": args.wave_rows or "default",
-                   "parallelism": f"replicas x{world}",
-                   "l2": "tables of up to 1e8 rows exceed L2; no flush"},
+        "config": served_config(args, world),
         "capacity": {"requests": int(len(cq)), "arrivals": "all at once",
                      "served_rps": capacity, "serial_plain_rps": len(cq) / serial_mk,
                      "served_rows_per_s": float(q_rows[cq].sum() / cap_mk),
@@ -873,15 +1067,15 @@ def run_reference(args):
         out = {"metric": METRIC, "value": v, "unit": "rows/s", "n_gpus": world, "steps": args.steps,
                "warmup": args.warmup, "ms_per_step": t * 1e3, "higher_is_better": True, "scaling": "weak",
                "vs_baseline": None, "dtype": "int32/int64/f32/f64", "data": "synthetic (seeded)",
-               "impl": "reference", "config": {"workload": args.workload, "seed": args.seed},
+               "impl": "reference",
+               "config": batched_config(args, world) if args.workload == "batched" else served_config(args, world),
                "cpu_baseline": {"value": v, "unit": "rows/s", "cores": threads, "kind": "port",
                                 "sample": f"first {64 if args.workload == 'batched' else 32} {what}, "
                                           f"tables capped at 200000 rows ({rows} rows)"},
                "e2e": {"value": v, "unit": "rows/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
         print(json.dumps(out), flush=True)
         return
-    n = args.rows or {"fused_project": 200_000_000, "plain_vm": 1_000_000, "filter_gather": 500_000_000,
-                      "filter_project": 200_000_000}[args.workload]
+    n = args.rows or DEFAULT_ROWS[args.workload]
     threads = os.cpu_count() or 1
     # bounded sample per step, sized from a probe so the whole run stays within a few minutes
     probe = min(n, 1_000_000)
@@ -894,10 +1088,13 @@ def run_reference(args):
     v = rows / t
     out = {"metric": METRIC, "value": v, "unit": "rows/s", "n_gpus": world, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": t * 1e3, "higher_is_better": True, "scaling": "weak",
-           "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)", "impl": "reference",
-           "config": {"workload": args.workload, "rows": n},
+           "vs_baseline": None,
+           "dtype": {"fused_project": "f64+int64", "filter_project": "f64+int64", "plain_vm": "f64+int64",
+                     "filter_gather": "int32/int64/f32/f64/date32/bool8 gather"}[args.workload],
+           "data": "synthetic (seeded)", "impl": "reference",
+           "config": workload_config(args.workload, n, args.selectivity, world),
            "cpu_baseline": {"value": v, "unit": "rows/s", "cores": threads, "kind": "port",
-                            "sample": f"{rows} of {n} rows per step"},
+                            "sample": f"{rows} of {n} rows per step", "cpu_model": cpu_model()},
            "e2e": {"value": v, "unit": "rows/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(out), flush=True)
 
@@ -927,6 +1124,9 @@ def main():
     ap.add_argument("--rows", type=int, default=0)
     ap.add_argument("--skip-e2e", action="store_true")
     ap.add_argument("--skip-cpu", action="store_true")
+    ap.add_argument("--skip-parity", action="store_true", help="skip the full-size oracle check")
+    ap.add_argument("--no-extra", action="store_true",
+                    help="default run: measure only the default workload, not the extra blocks")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":
         args.warmup = 3

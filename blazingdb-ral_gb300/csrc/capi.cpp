@@ -1,4 +1,4 @@
-// capi.cpp — the extern "C" entry points declared in include/ral/ral_c.h.
+// capi.cpp — the extern "C" entry points declared in include/ral/ral_c.h and include/ral/ral_debug.h.
 #include <cuda_runtime.h>
 
 #include <cstring>
@@ -14,6 +14,7 @@
 #include "kernels.h"
 #include "server.h"
 #include "ral/ral_c.h"
+#include "ral/ral_debug.h"
 
 using namespace ral;
 
@@ -334,7 +335,10 @@ int ral_apply_boolean_mask(const gdf_column* stencil, gdf_column* out_indices, g
         const int64_t words = compact_scratch_words(n);
         unsigned long long* scratch = nullptr;
         if (int e = check_cuda(cudaMallocAsync((void**)&scratch, (size_t)words * 8, st), "cudaMallocAsync")) return e;
-        cudaMemsetAsync(scratch, 0, (size_t)words * 8, st);
+        if (int e = check_cuda(cudaMemsetAsync(scratch, 0, (size_t)words * 8, st), "cudaMemsetAsync")) {
+            cudaFreeAsync(scratch, st);
+            return e;
+        }
         int rc = check_cuda(launch_compact_stencil((const int8_t*)stencil->data, (const uint32_t*)stencil->valid, n,
                                                    (int32_t*)out_indices->data, scratch, st),
                             "compaction");

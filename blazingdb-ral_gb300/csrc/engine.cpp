@@ -11,6 +11,7 @@
 #include <atomic>
 #include <cstdlib>
 #include <cstring>
+#include <map>
 #include <mutex>
 #include <unordered_map>
 
@@ -294,7 +295,11 @@ int perform_operation_host(gdf_column* const* outputs, int n_out, gdf_column* co
     int64_t chunk = chunk_rows > 0 ? chunk_rows : ((int64_t)4 << 20);
     chunk = std::max<int64_t>(1024, (chunk + 1023) / 1024 * 1024);
     if (chunk > n) chunk = (n + 1023) / 1024 * 1024;
-    static thread_local HostStreams hs;
+    // streams belong to the device that was current when they were made: one set per device
+    int dev = 0;
+    if (check_cuda(cudaGetDevice(&dev), "cudaGetDevice")) return kCudaError;
+    static thread_local std::map<int, HostStreams> per_device;
+    HostStreams& hs = per_device[dev];
     for (cudaStream_t& x : hs.s)
         if (!x && check_cuda(cudaStreamCreateWithFlags(&x, cudaStreamNonBlocking), "cudaStreamCreate")) return kCudaError;
     if (!hs.ready && check_cuda(cudaEventCreateWithFlags(&hs.ready, cudaEventDisableTiming), "cudaEventCreate"))

@@ -9,14 +9,15 @@
 //
 // The array lives in every device's memory as soon as the library's module is
 // loaded there and stays until the process exits.  Its host-side name is only a
-// stand-in for the symbol, so the device address is looked up once per device
-// with cudaGetSymbolAddress and passed to the kernel.  All calls share the one
-// array: it is cleared before each use, and calls whose GPU work overlaps (two
-// threads, or two streams, at once) race on it.
+// stand-in for the symbol: each call looks up the array's device address on the
+// current device with cudaGetSymbolAddress and passes it to the kernel.  (The
+// address is not cached: after a cudaDeviceReset the module is loaded again and
+// the array may move.)  All calls share the one array: it is cleared before each
+// use, and calls whose GPU work overlaps (two threads, or two streams, at once)
+// race on it.
 #include <cuda_runtime.h>
 
 #include <cstdint>
-#include <mutex>
 #include <string>
 
 #include "engine.h"
@@ -33,22 +34,12 @@ static_assert(RAL_NOALLOC_MAX_ROWS == kMaxRows, "ral_c.h states a different limi
 
 static __device__ __align__(256) unsigned long long g_scratch[kScratchWords];
 
-constexpr int kMaxDevices = 64;
-std::mutex g_mu;
-unsigned long long* g_scratch_ptr[kMaxDevices] = {};
-
-// Device address of g_scratch on the current device (looked up on first use).
+// Device address of g_scratch on the current device.  The first lookup on a device loads the
+// library's module there.
 int scratch_on_current_device(unsigned long long** out) {
-    int dev = 0;
-    if (int e = ral::check_cuda(cudaGetDevice(&dev), "cudaGetDevice")) return e;
-    if (dev < 0 || dev >= kMaxDevices) return ral::set_error(ral::kInvalidArgument, "device ordinal out of range");
-    std::lock_guard<std::mutex> lock(g_mu);
-    if (!g_scratch_ptr[dev]) {
-        void* p = nullptr;
-        if (int e = ral::check_cuda(cudaGetSymbolAddress(&p, g_scratch), "cudaGetSymbolAddress")) return e;
-        g_scratch_ptr[dev] = static_cast<unsigned long long*>(p);
-    }
-    *out = g_scratch_ptr[dev];
+    void* p = nullptr;
+    if (int e = ral::check_cuda(cudaGetSymbolAddress(&p, g_scratch), "cudaGetSymbolAddress")) return e;
+    *out = static_cast<unsigned long long*>(p);
     return ral::kSuccess;
 }
 

@@ -184,8 +184,9 @@ int ral_apply_boolean_mask(const gdf_column *stencil, gdf_column *out_indices, g
  * scratch block comes from a fixed 256 KiB array compiled into the library,
  * which every GPU that loads the library holds until the process exits.
  * Limit: stencil->size <= RAL_NOALLOC_MAX_ROWS; larger stencils are rejected
- * with RAL_ERROR_INVALID_ARGUMENT.  The first call on a device looks up the
- * array's device address (cudaGetSymbolAddress); make that first call before
+ * with RAL_ERROR_INVALID_ARGUMENT.  Each call looks up the array's device
+ * address on the current device (cudaGetSymbolAddress); the first call on a
+ * device also loads the library's module there, so make that first call before
  * any stream capture.  All calls share the array: calls whose GPU work
  * overlaps (from several threads or streams at once) race on it.
  */
@@ -210,18 +211,6 @@ int ral_add_expression_to_plan(const char *expression, column_index_type express
 /* get_output_type_expression — src/CalciteExpressionParsing.cpp:420-481. */
 int ral_get_output_type_expression(const gdf_dtype *frame_dtypes, int32_t num_columns, const char *expression,
                                    gdf_dtype *dtype_out);
-
-/* Library introspection (no reference counterpart): generated CUDA source of
- * the kernel a program maps to, and an NVRTC-only compile check that needs
- * no GPU.  Buffers receive a NUL-terminated string truncated to capacity. */
-int ral_debug_program_source(const gdf_dtype *input_dtypes, const int32_t *input_nullable, int32_t num_inputs,
-                             const gdf_dtype *output_dtypes, const int32_t *output_nullable, int32_t num_outputs,
-                             const column_index_type *left_inputs, const column_index_type *right_inputs,
-                             const column_index_type *outputs, int32_t num_operations,
-                             const column_index_type *final_output_positions, const int32_t *operators,
-                             const int32_t *unary_operators, const gdf_scalar *left_scalars,
-                             const gdf_scalar *right_scalars, int32_t compile, char *source_out,
-                             int64_t source_capacity, char *log_out, int64_t log_capacity);
 
 /*
  * Batched execution — no single reference counterpart: the reference runs each program as its
@@ -251,10 +240,6 @@ int ral_batch_destroy(ral_batch *batch);
 /* Registers per thread, grid and resident blocks per SM of the prepared batch kernel (0 before
  * ral_batch_prepare). */
 int ral_batch_kernel_info(const ral_batch *batch, int32_t *registers, int32_t *grid, int32_t *blocks_per_sm);
-/* Generated source of the batch kernel for the programs added so far (and an NVRTC-only
- * compile when compile != 0); needs no GPU. */
-int ral_batch_debug_source(const ral_batch *batch, int32_t compile, char *source_out, int64_t source_capacity,
-                           char *log_out, int64_t log_capacity);
 
 /* The autotuner's table key of a perform_operation program (dtype mix and program length). */
 int ral_batch_tune_key(gdf_column *const *output_columns, int32_t num_outputs, gdf_column *const *input_columns,
@@ -279,13 +264,6 @@ int ral_autotune_program(gdf_column *const *output_columns, int32_t num_outputs,
                          const int32_t *operators, const int32_t *unary_operators, const gdf_scalar *left_scalars,
                          const gdf_scalar *right_scalars, int32_t *best_slices, int32_t *best_unroll,
                          int32_t *best_soft_fp, double *best_ms);
-
-/* Generated source of the fused LogicalFilter kernel (optionally NVRTC-compiled, no GPU
- * needed) for a frame described by dtypes and mask presence; project_query_part may be
- * NULL (process_filter) or a LogicalProject (ral_filter_project). */
-int ral_debug_filter_source(const gdf_dtype *frame_dtypes, const int32_t *frame_nullable, int32_t num_columns,
-                            const char *filter_query_part, const char *project_query_part, int32_t compile,
-                            char *source_out, int64_t source_capacity, char *log_out, int64_t log_capacity);
 
 /* Kernels launched by this library since load (all entry points). */
 int64_t ral_kernel_launches(void);
@@ -313,9 +291,6 @@ int ral_server_add_query(ral_server *server, int32_t table_id, const char *filte
 /* dtype and mask presence (0/1) of each projected column; *num_outputs receives the count. */
 int ral_server_query_outputs(ral_server *server, int32_t query_id, gdf_dtype *dtypes, int32_t *has_valid,
                              int32_t capacity, int32_t *num_outputs);
-/* Compiles every query's chunk function and links the dispatcher without loading it (no GPU
- * needed); the ptxas / link log goes to log_out. */
-int ral_server_debug_compile(ral_server *server, char *log_out, int64_t log_capacity);
 /* Compiles every query, links the dispatcher and starts the scheduler thread. */
 int ral_server_start(ral_server *server);
 /* keep != 0: the outputs stay allocated for ral_server_result until ral_server_release. */
@@ -336,26 +311,6 @@ int ral_server_run_trace(ral_server *server, int32_t num_requests, const int32_t
 /* stats: submitted, completed, waves, largest wave, peak reserved bytes, busy microseconds. */
 int ral_server_stats(ral_server *server, int64_t *stats6);
 int ral_server_destroy(ral_server *server);
-
-/*
- * Device self-test of the integer-pipe double operations against the GPU's FP64 instructions
- * (no reference counterpart): n random operand sets from seed; mismatches[16] receives the
- * mismatch count of each operation (0 div, 1 floor, 2 ceil, 3 compares, 4 int64->double,
- * 5 double->int64, 6 float->double, 7 double->float, 8 == 0, 9 fabs, 10 int64 / and %,
- * 11 sin / cos beyond 2 ulp of the library's) and first_operands[32]
- * the bits of each operation's first mismatching operands.
- */
-int ral_softfp_selftest(int64_t n, uint64_t seed, int64_t *mismatches, uint64_t *first_operands);
-
-/*
- * Failure-detection check (no reference counterpart): runs the compaction over n_rows rows with its
- * tile counter starting at 1, so that tile 1's look-back waits on a status word nothing writes;
- * the bounded wait must end (about a second) with the error word set, reported as
- * *status = RAL_ERROR_TIMEOUT, and the context must stay usable: the same compaction is then run
- * normally and *kept_after receives its kept-row count (n_rows).  n_rows: one tile (4096) < n_rows
- * <= 64M.
- */
-int ral_debug_lookback_timeout(int64_t n_rows, int32_t *status, int64_t *kept_after);
 
 #ifdef __cplusplus
 }

@@ -26,8 +26,10 @@
 //     tests/interpreter/interpreter_tests.cu:434-514 expects that); the
 //     shipped value-to-int64 conversion (interpreter_ops.cuh:167-168) is
 //     available with ORACLE_FLOAT_LITERAL_COMPAT.
-//   * double -> int64 conversions saturate and map NaN to 0, which is what the
-//     GPU's cvt.rzi.s64.f64 does (x86's cvttsd2si would give INT64_MIN).
+//   * double -> int64 conversions truncate, saturate out-of-range values and map
+//     NaN to INT64_MIN, which is what the GPU's cvt.rzi.s64.f64 does (measured
+//     on the GPU; a plain C++ cast of NaN or of an out-of-range value is
+//     undefined on the host).
 //   * Signed integer arithmetic wraps (two's complement), as on the GPU.
 //   * Integer division or remainder by zero has no pinned GPU value; the
 //     oracle returns 0 and counts the event so tests can exclude such rows.

@@ -28,8 +28,9 @@ def _entry():
     return f
 
 
-def _noalloc(stencil: R.Column) -> R.Column:
-    out = R.Column.empty(D.GDF_INT32, stencil.size, with_valid=False)
+def _noalloc(stencil: R.Column, out: R.Column = None) -> R.Column:
+    if out is None:
+        out = R.Column.empty(D.GDF_INT32, stencil.size, with_valid=False)
     sc, oc = stencil.to_c(), out.to_c()
     n = ctypes.c_int32(-1)
     rc = _entry()(ctypes.byref(sc), ctypes.byref(oc), ctypes.byref(n))
@@ -51,6 +52,51 @@ def test_noalloc_matches_allocating_entry_point_on_two_calls():
         exp = R.apply_boolean_mask(col)
         assert got.size == exp.size
         np.testing.assert_array_equal(got.to_numpy(), exp.to_numpy())
+
+
+def _cudart():
+    """The CUDA runtime the library links (for the default memory pool's counters)."""
+    import glob
+    import os
+    for name in ("libcudart.so.13", "libcudart.so"):
+        try:
+            return ctypes.CDLL(name)
+        except OSError:
+            pass
+    for cand in glob.glob(os.path.join(os.environ.get("CUDA_HOME", "/usr/local/cuda"), "lib64", "libcudart.so*")):
+        return ctypes.CDLL(cand)
+    pytest.skip("libcudart not found")
+
+
+def test_noalloc_makes_no_device_allocation():
+    """The property the entry point exists for: a warm call (and an empty one) leaves the device's
+    free memory and its default memory pool's high-water mark where they were."""
+    import torch
+    rt = _cudart()
+    pool = ctypes.c_void_p()
+    assert rt.cudaDeviceGetDefaultMemPool(ctypes.byref(pool), torch.cuda.current_device()) == 0
+    USED_HIGH = 8                           # cudaMemPoolAttrUsedMemHigh
+    rng = np.random.default_rng(5)
+    n = 2_000_003
+    col = R.Column.from_numpy((rng.random(n) < 0.5).astype(np.int8), D.GDF_INT8, rng.random(n) >= 0.1)
+    empty = R.Column.empty(D.GDF_INT8, 0, with_valid=False)
+    # outputs made up front: only the calls themselves run between the two readings
+    out = R.Column.empty(D.GDF_INT32, n, with_valid=False)
+    out0 = R.Column.empty(D.GDF_INT32, 0, with_valid=False)
+    _noalloc(col, out)                      # warm: module loaded, kernel resolved
+    torch.cuda.synchronize()
+    zero = ctypes.c_uint64(0)
+    assert rt.cudaMemPoolSetAttribute(pool, USED_HIGH, ctypes.byref(zero)) == 0
+    free0, _ = torch.cuda.mem_get_info()
+    got = _noalloc(col, out)
+    assert _noalloc(empty, out0).size == 0
+    torch.cuda.synchronize()
+    free1, _ = torch.cuda.mem_get_info()
+    high = ctypes.c_uint64(1)
+    assert rt.cudaMemPoolGetAttribute(pool, USED_HIGH, ctypes.byref(high)) == 0
+    assert high.value == 0, "the call allocated from the default memory pool"
+    assert free1 == free0, "device free memory changed across the call"
+    assert got.size == R.apply_boolean_mask(col).size
 
 
 def test_noalloc_rejects_stencils_beyond_the_limit():
