@@ -591,6 +591,47 @@ def parity_check(workload, ctx, selectivity):
     return out
 
 
+_LINK = None
+
+
+def host_link_peak(nbytes=1 << 30, reps=5):
+    """Pinned host <-> device copy bandwidth with plain cudaMemcpyAsync (torch copies): H2D alone,
+    D2H alone, and both directions at once on two streams (GB/s, best of reps).  Measured once."""
+    global _LINK
+    if _LINK is not None:
+        return _LINK
+    import torch
+    h_in = torch.empty(nbytes, dtype=torch.uint8).pin_memory()
+    h_out = torch.empty(nbytes, dtype=torch.uint8).pin_memory()
+    d_a = torch.empty(nbytes, dtype=torch.uint8, device="cuda")
+    d_b = torch.empty(nbytes, dtype=torch.uint8, device="cuda")
+    s1, s2 = torch.cuda.Stream(), torch.cuda.Stream()
+
+    def timed(fn):
+        best = 1e30
+        for _ in range(reps):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            fn()
+            torch.cuda.synchronize()
+            best = min(best, time.perf_counter() - t0)
+        return best
+
+    def both():
+        with torch.cuda.stream(s1):
+            d_a.copy_(h_in, non_blocking=True)
+        with torch.cuda.stream(s2):
+            h_out.copy_(d_b, non_blocking=True)
+
+    h2d = nbytes / timed(lambda: d_a.copy_(h_in, non_blocking=True)) / 1e9
+    d2h = nbytes / timed(lambda: h_out.copy_(d_b, non_blocking=True)) / 1e9
+    bi = 2 * nbytes / timed(both) / 1e9
+    _LINK = {"h2d_gbs": h2d, "d2h_gbs": d2h, "both_gbs": bi,
+             "how": f"pinned {nbytes >> 20} MiB cudaMemcpyAsync, best of {reps}; both = H2D and D2H at once"}
+    del h_in, h_out, d_a, d_b
+    return _LINK
+
+
 def measure_workload(args, workload, n, selectivity, device, world, sampler, e2e=True, cpu=True, parity=True,
                      cpu_budget_s=12.0):
     """One workload: warm-up, the timed steps (CUDA events on the launching stream, max over ranks),
@@ -644,12 +685,16 @@ def measure_workload(args, workload, n, selectivity, device, world, sampler, e2e
     if "nout" in ctx:
         out["rows_out"] = ctx["nout"].value
     if rank == 0:
-        # the device outputs of the last timed step are checked before the e2e leg reuses the columns
-        if parity and not args.skip_parity:
-            out["parity"] = parity_check(workload, ctx, selectivity)
         if e2e and not args.skip_e2e:
             out["e2e"] = (fused_project_e2e(ctx, max(2, min(args.steps, 3)), device) if workload == "fused_project"
                           else filter_e2e(ctx, max(2, min(args.steps, 3))))
+            link = host_link_peak()
+            moved = out["e2e"]["h2d_bytes_per_step"] + out["e2e"]["d2h_bytes_per_step"]
+            out["e2e"]["host_link"] = dict(link, e2e_gbs=moved / (out["e2e"]["ms_per_step"] / 1e3) / 1e9)
+            out["e2e"]["host_link"]["frac_of_link"] = out["e2e"]["host_link"]["e2e_gbs"] / link["both_gbs"]
+        # the device outputs (the e2e leg rewrote them with the same bits) against the oracle
+        if parity and not args.skip_parity:
+            out["parity"] = parity_check(workload, ctx, selectivity)
         if cpu and not args.skip_cpu:
             out["cpu_baseline"] = cpu_baseline(workload, n, selectivity, budget_s=cpu_budget_s,
                                                single_budget_s=cpu_budget_s / 3)

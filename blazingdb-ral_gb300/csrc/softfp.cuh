@@ -105,12 +105,25 @@ RAL_SF int ral_sf_clz64(unsigned long long x) {  // x != 0
 #endif
 }
 
-// 1/x to about 22 bits for x in [2^23, 2^24) (an exact float of the divisor's top bits)
+// 1/x to about 22 bits (rcp.approx on the GPU: at most one ulp from 1/x).  On the host the tests
+// can move the estimate by RAL_SF_TEST_RCP_ULPS ulps to show that every caller's refinement and
+// correction steps hold for an estimate several ulps off.
+#if !defined(__CUDA_ARCH__) && defined(RAL_SF_TEST_RCP_ULPS)
+extern int ral_sf_test_rcp_ulps;
+#endif
 RAL_SF float ral_sf_rcp_estimate(float x) {
 #if defined(__CUDA_ARCH__)
     float r;
     asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
     return r;
+#elif defined(RAL_SF_TEST_RCP_ULPS)
+    const float r = 1.0f / x;
+    unsigned b;
+    __builtin_memcpy(&b, &r, 4);
+    b = (unsigned)((int)b + ral_sf_test_rcp_ulps);
+    float o;
+    __builtin_memcpy(&o, &b, 4);
+    return o;
 #else
     return 1.0f / x;
 #endif
@@ -128,7 +141,30 @@ RAL_SF double ral_sf_hw_div(double a, double b) {
 
 // ---- division --------------------------------------------------------------------------------
 
+RAL_SF unsigned int ral_sf_umulhi32(unsigned int a, unsigned int b) {
+#if defined(__CUDA_ARCH__)
+    return __umulhi(a, b);
+#else
+    return (unsigned int)(((unsigned long long)a * b) >> 32);
+#endif
+}
+
 // a / b rounded to nearest even.
+//
+// With both operands normal, the significands ma, mb in [2^52, 2^53) (ma doubled when below mb,
+// so ma / mb is in [1, 2)) give the quotient Q = floor(ma * 2^53 / mb) in [2^53, 2^54) and the
+// remainder R = ma * 2^53 - Q * mb, from which the result rounds.  Q comes from schoolbook long
+// division in two digits with a 32-bit reciprocal v ~ 2^63 / dh of the divisor's top 32 bits
+// dh = mb >> 21 (Muller et al., "Handbook of Floating-Point Arithmetic", ch. 9):
+//   * v: the float reciprocal of mb's top 24 bits (assembled from the float's fields, no
+//     conversion instruction), then one Newton step in integer arithmetic: |v - 2^63 / dh| < 2;
+//   * digit 1: q1 = umulhi(ma >> 22, v) estimates T1 = ma * 2^30 / mb within [-4, +3] units (the
+//     reciprocal's error, the truncated dividend and divisor, the floor); taken 4 low, its
+//     remainder R1 = ma * 2^30 - q1 * mb lies in [mb, 8 mb] < 2^56 and is exact in 64 bits;
+//   * digit 2: q2 = umulhi(R1 >> 25, v) >> 4 estimates R1 * 2^23 / mb (below 2^26) within one
+//     unit either way, so R = R1 * 2^23 - q2 * mb (exact modulo 2^64, its true value small) needs
+//     one test per direction.
+// Only 32 x 32-bit products and 64-bit adds and shifts: no 64 x 64-bit multiply.
 RAL_SF double ral_sf_div(double a, double b) {
     const unsigned long long A = ral_sf_bits(a), B = ral_sf_bits(b);
     const unsigned ea = (unsigned)(A >> 52) & 0x7ffu, eb = (unsigned)(B >> 52) & 0x7ffu;
@@ -141,40 +177,28 @@ RAL_SF double ral_sf_div(double a, double b) {
         ma <<= 1;
         e -= 1;
     }
-    // reciprocal y ~ 2^116 / mb in [2^63, 2^64): a float seed for the divisor's top 32 bits d32,
-    // one Newton step in 32-bit fixed point (v ~ 2^63 / d32 to ~31 bits), one in 64-bit (~60 bits)
-    const unsigned d32 = (unsigned)(mb >> 21);                        // in [2^31, 2^32)
-    const float seed = ral_sf_rcp_estimate((float)d32);              // ~ 1 / d32
-    // v0 = seed * 2^63 assembled from the float's fields (no float -> int conversion)
-    const unsigned sb = ral_sf_fbits(seed);
-    const int sh = (int)((sb >> 23) & 0xffu) - 87;                   // 7..9
-    unsigned long long v = (unsigned long long)((sb & 0x7fffffu) | 0x800000u) << (sh > 0 ? sh : 0);
-    if (v > 0xffffffffull) v = 0xffffffffull;
+    const unsigned dh = (unsigned)(mb >> 21);  // in [2^31, 2^32)
+    unsigned v;
     {
-        const long long e = (long long)((1ull << 63) - (unsigned long long)d32 * v);  // |e| < 2^43
-        long long v1 = (long long)v + (((long long)v * (e >> 21)) >> 42);
+        // r ~ 2^31 / dh from the float 1.f of mb's top 24 bits; v0 = r * 2^32 from r's fields
+        const float r = ral_sf_rcp_estimate(ral_sf_float(0x3f800000u | ((unsigned)(mb >> 29) & 0x7fffffu)));
+        const unsigned rb = ral_sf_fbits(r);
+        const unsigned long long big = (unsigned long long)((rb & 0x7fffffu) | 0x800000u) << (((rb >> 23) & 0xffu) - 118u);
+        const unsigned v0 = big > 0xffffffffull ? 0xffffffffu : (unsigned)big;
+        // Newton: v1 = v0 + v0 * (2^63 - dh * v0) / 2^63, the error term (|err| < 2^43) scaled down
+        // to 22 bits so that its product with v0 is one 32 x 32-bit multiply
+        const long long err = (long long)((1ull << 63) - (unsigned long long)dh * v0);
+        const unsigned mag = (unsigned)((err < 0 ? 0ull - (unsigned long long)err : (unsigned long long)err) >> 21);
+        const unsigned long long corr = ((unsigned long long)mag * v0) >> 42;
+        long long v1 = err < 0 ? (long long)v0 - (long long)corr : (long long)v0 + (long long)corr;
         if (v1 > 0xffffffffll) v1 = 0xffffffffll;
-        if (v1 < 0x80000000ll) v1 = 0x80000000ll;
-        v = (unsigned long long)v1;
+        v = (unsigned)v1;
     }
-    unsigned long long y = v << 32;
-    {
-        // err = 2^116 - mb * y, as a signed value scaled by 2^-52
-        const unsigned long long plo = mb * y, phi = ral_sf_umulh(mb, y);
-        // (2^116 - P) >> 52 = (2^64 - (P >> 52)) using the 128-bit P = phi:plo
-        const unsigned long long p52 = (phi << 12) | (plo >> 52);  // P >> 52 (P < 2^117: fits)
-        const long long err = (long long)(0ull - p52);               // 2^64 - p52 mod 2^64, small
-        // y += y * err / 2^64
-        const unsigned long long mag = err < 0 ? (0ull - (unsigned long long)err) : (unsigned long long)err;
-        const unsigned long long corr = ral_sf_umulh(y, mag);
-        y = err < 0 ? y - corr : y + corr;
-    }
-    // Q ~ ma * 2^53 / mb = (ma * y) >> 63.  With y within ~2^-60 of 2^116 / mb the estimate is
-    // off by at most one either way, and one remainder test per direction corrects it.
-    const unsigned long long qlo = ma * y, qhi = ral_sf_umulh(ma, y);
-    unsigned long long q = (qhi << 1) | (qlo >> 63);
-    // R = ma * 2^53 - q * mb (small: the low 64 bits of both products suffice)
-    long long r = (long long)((ma << 53) - q * mb);
+    const unsigned q1 = ral_sf_umulhi32((unsigned)(ma >> 22), v) - 4u;
+    const unsigned long long r1 = (ma << 30) - (unsigned long long)q1 * mb;          // in [mb, 8 mb]
+    const unsigned q2 = ral_sf_umulhi32((unsigned)(r1 >> 25), v) >> 4;
+    unsigned long long q = ((unsigned long long)q1 << 23) + q2;
+    long long r = (long long)((r1 << 23) - (unsigned long long)q2 * mb);
     if (r < 0) {
         q -= 1;
         r += (long long)mb;
@@ -184,8 +208,8 @@ RAL_SF double ral_sf_div(double a, double b) {
     }
     // q in [2^53, 2^54): 53 significand bits, one rounding bit, sticky = r != 0
     unsigned long long m = q >> 1;
-    const unsigned rb = (unsigned)(q & 1u);
-    if (rb && (r != 0 || (m & 1u))) m += 1;
+    const unsigned rnd = (unsigned)(q & 1u);
+    if (rnd && (r != 0 || (m & 1u))) m += 1;
     if (m == (1ull << 53)) {
         m >>= 1;
         e += 1;
@@ -206,32 +230,34 @@ RAL_SF unsigned long long ral_sf_opaque(unsigned long long x) {
 
 // ---- rounding to an integer ------------------------------------------------------------------
 
+// floor and ceil by masking the fraction bits.  With e the biased exponent: e >= 1075 is already
+// integral (or infinite / NaN); below 1023 (|x| < 1) the mask covers every bit but the sign, and
+// the result is the signed zero or -1 / +1; otherwise the mask covers the fraction bits below the
+// binary point.  Rounding away from zero adds one unit at the binary point to the truncated bits
+// (the carry may move into the exponent).
 RAL_SF double ral_sf_floor(double x) {
-    unsigned long long A = ral_sf_obits(x);
-    const int e = (int)((A >> 52) & 0x7ff);
-    if (e >= 1075) return x;  // integral, infinite or NaN
-    if (e < 1023) {  // |x| < 1: +-0 stays, otherwise -1 or +0
-        const unsigned long long neg = ral_sf_opaque((unsigned long long)((long long)A >> 63));
-        return ral_sf_double((A << 1) == 0 ? A : (neg & 0xbff0000000000000ull));
-    }
-    const unsigned long long mask = RAL_SF_FRAC >> (e - 1023);
-    if ((A & mask) == 0) return x;
-    A = (A >> 63) ? (A | mask) + 1 : (A & ~mask);  // negative: away from zero (carries into the exponent)
-    return ral_sf_double(A);
+    const unsigned long long A = ral_sf_obits(x);
+    const unsigned e = (unsigned)(A >> 52) & 0x7ffu;
+    if (e >= 1075u) return x;  // integral, infinite or NaN
+    const bool small = e < 1023u;
+    const unsigned long long mask = small ? ~RAL_SF_SIGN : (RAL_SF_FRAC >> (e - 1023u));
+    if ((A & mask) == 0) return x;  // integral, or a zero
+    const unsigned long long t = A & ~mask;  // truncated toward zero (a signed zero when small)
+    if (!(A >> 63)) return ral_sf_double(t);
+    // negative with a fraction: one unit more in magnitude (-1.0 when small)
+    return ral_sf_double(small ? 0xbff0000000000000ull : t + ((mask + 1) & ~RAL_SF_SIGN));
 }
 
 RAL_SF double ral_sf_ceil(double x) {
-    unsigned long long A = ral_sf_obits(x);
-    const int e = (int)((A >> 52) & 0x7ff);
-    if (e >= 1075) return x;
-    if (e < 1023) {  // |x| < 1: +-0 stays, otherwise -0 or 1
-        const unsigned long long neg = ral_sf_opaque((unsigned long long)((long long)A >> 63));
-        return ral_sf_double((A << 1) == 0 ? A : (0x3ff0000000000000ull ^ (neg & (0x3ff0000000000000ull ^ RAL_SF_SIGN))));
-    }
-    const unsigned long long mask = RAL_SF_FRAC >> (e - 1023);
+    const unsigned long long A = ral_sf_obits(x);
+    const unsigned e = (unsigned)(A >> 52) & 0x7ffu;
+    if (e >= 1075u) return x;
+    const bool small = e < 1023u;
+    const unsigned long long mask = small ? ~RAL_SF_SIGN : (RAL_SF_FRAC >> (e - 1023u));
     if ((A & mask) == 0) return x;
-    A = (A >> 63) ? (A & ~mask) : (A | mask) + 1;
-    return ral_sf_double(A);
+    const unsigned long long t = A & ~mask;
+    if (A >> 63) return ral_sf_double(t);  // negative: truncation (-0.0 when small)
+    return ral_sf_double(small ? 0x3ff0000000000000ull : t + ((mask + 1) & ~RAL_SF_SIGN));
 }
 
 RAL_SF double ral_sf_fabs(double x) { return ral_sf_double(ral_sf_obits(x) & ~RAL_SF_SIGN); }
@@ -433,17 +459,9 @@ RAL_SF void ral_sf_udivmod64_32(unsigned long long n, unsigned int d, unsigned l
 // n / d and n % d for 1 <= d < 2^16 with 32-bit operations only.  m = floor((2^32 - 1) / d) lies
 // in [2^32 / d - 1, 2^32 / d], so for any 32-bit x the high word of x * m is floor(x / d) or one
 // less (x * m / 2^32 > x / d - x / 2^32 > x / d - 1), and one remainder test corrects it.  The
-// dividend is taken as 32 + 16 + 16 bits, most significant first (long division in base 2^16
-// after the first word): each partial remainder is below d < 2^16, so the next partial dividend
-// (remainder << 16 | next 16 bits) stays below 2^32 and its quotient below 2^16.
-RAL_SF unsigned int ral_sf_umulhi32(unsigned int a, unsigned int b) {
-#if defined(__CUDA_ARCH__)
-    return __umulhi(a, b);
-#else
-    return (unsigned int)(((unsigned long long)a * b) >> 32);
-#endif
-}
-
+// dividend is taken as 32 + 16 + 16 bits (32 + 16 below 2^48), most significant first (long
+// division in base 2^16 after the first word): each partial remainder is below d < 2^16, so the
+// next partial dividend (remainder << 16 | next 16 bits) stays below 2^32.
 RAL_SF unsigned int ral_sf_divstep16(unsigned int x, unsigned int d, unsigned int m, unsigned int* r) {
     unsigned int q = ral_sf_umulhi32(x, m);
     unsigned int rr = x - q * d;  // in [0, 2d)
@@ -459,6 +477,13 @@ RAL_SF void ral_sf_udivmod64_16(unsigned long long n, unsigned int d, unsigned l
                                 unsigned long long* r_out) {
     const unsigned int m = 0xffffffffu / d;
     unsigned int r;
+    if ((n >> 48) == 0) {  // a dividend below 2^48 (the common case) as 32 + 16 bits: two steps
+        const unsigned int q1 = ral_sf_divstep16((unsigned int)(n >> 16), d, m, &r);
+        const unsigned int q0 = ral_sf_divstep16((r << 16) | ((unsigned int)n & 0xffffu), d, m, &r);
+        *q_out = ((unsigned long long)q1 << 16) | q0;
+        *r_out = r;
+        return;
+    }
     const unsigned int q2 = ral_sf_divstep16((unsigned int)(n >> 32), d, m, &r);
     const unsigned int lo = (unsigned int)n;
     const unsigned int q1 = ral_sf_divstep16((r << 16) | (lo >> 16), d, m, &r);

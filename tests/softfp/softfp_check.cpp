@@ -1,6 +1,7 @@
 // Host check of softfp.cuh: every function against the host's IEEE-754 operations, bit for bit,
 // on edge cases and random inputs.  Prints one line per function: name, cases, mismatches, and
 // the first mismatch.  Built and run by tests/test_softfp_cpu.py.
+#include <algorithm>
 #include <cmath>
 #include <cstdint>
 #include <cstdio>
@@ -9,6 +10,10 @@
 #include <random>
 #include <vector>
 
+// every estimate of ral_sf_rcp_estimate can be moved by a number of ulps (0 except in the
+// division-under-perturbed-reciprocal check below)
+#define RAL_SF_TEST_RCP_ULPS 1
+int ral_sf_test_rcp_ulps = 0;
 #include "softfp.cuh"
 
 static uint64_t bits(double d) { uint64_t b; std::memcpy(&b, &d, 8); return b; }
@@ -200,6 +205,43 @@ int main(int argc, char** argv) {
         if (!same_d((double)f, ral_sf_f2d(f)) && cf2d.bad++ == 0)
             std::snprintf(cf2d.first, sizeof cf2d.first, "%a", (double)f);
     }
+    // division with the reciprocal estimate moved by -4 .. +4 ulps (the GPU's rcp.approx is within
+    // one), on divisors whose top 32 bits sit at the ends of their range and dividends at the ends of
+    // the quotient range [1, 2)
+    Counter cdivr{"div_rcp"};
+    for (int pert = -4; pert <= 4; ++pert) {
+        ral_sf_test_rcp_ulps = pert;
+        const long long per = std::max(1ll, N / 8);
+        for (long long k = 0; k < per; k++) {
+            unsigned long long dh;
+            switch (rng() % 4) {
+            case 0: dh = (1ull << 31) + rng() % 8; break;
+            case 1: dh = (1ull << 32) - 1 - rng() % 8; break;
+            case 2: dh = (1ull << 31) | (1ull << (rng() % 31)); break;
+            default: dh = (1ull << 31) | (rng() >> 33); break;
+            }
+            const unsigned long long dl = (rng() % 3 == 0) ? 0 : ((rng() % 2) ? (1ull << 21) - 1 : rng() >> 43);
+            const unsigned long long mb = (dh << 21) | dl;
+            unsigned long long ma;
+            switch (rng() % 5) {
+            case 0: ma = mb; break;
+            case 1: ma = mb - 1 - rng() % 4; break;                     // just below: doubled
+            case 2: ma = (mb + 1 + rng() % 4) & ((1ull << 53) - 1); break;
+            case 3: ma = (1ull << 53) - 1 - rng() % 4; break;
+            default: ma = rng() >> 11; break;
+            }
+            ma |= 1ull << 52;
+            const int ea = 900 + (int)(rng() % 200), eb = 900 + (int)(rng() % 200);
+            const double a = dbl(((unsigned long long)ea << 52) | (ma & ((1ull << 52) - 1)) | ((rng() & 1) << 63));
+            const double b = dbl(((unsigned long long)eb << 52) | (mb & ((1ull << 52) - 1)));
+            cdivr.n++;
+            const double w = a / b, g = ral_sf_div(a, b);
+            if (!same_d(w, g) && cdivr.bad++ == 0)
+                std::snprintf(cdivr.first, sizeof cdivr.first, "%a/%a (rcp %+d ulp) want %a got %a", a, b, pert, w, g);
+        }
+    }
+    ral_sf_test_rcp_ulps = 0;
+    cdivr.report();
     for (long long x : std::vector<long long>{0ll, 1ll, -1ll, (long long)INT64_MAX, (long long)INT64_MIN, (1ll << 53) + 1, -(1ll << 53) - 1, (1ll << 62) + 3}) {
         ci2d.n++;
         if (!same_d((double)x, ral_sf_i2d(x)) && ci2d.bad++ == 0)
