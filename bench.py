@@ -223,6 +223,8 @@ def cpu_filter_project(rows: int, threads: int, selectivity: float):
 
 
 def cpu_time(workload, rows, threads, selectivity):
+    if workload == "gather":
+        return cpu_gather(rows, threads)
     if workload == "fused_project":
         return cpu_fused_project(rows, threads)
     if workload == "filter_project":
@@ -319,7 +321,7 @@ def cpu_served(threads: int, n_queries: int, rows_cap: int, seed: int = 20261203
 # ---- GPU workloads --------------------------------------------------------------------------------
 
 DEFAULT_ROWS = {"fused_project": 200_000_000, "plain_vm": 1_000_000, "filter_gather": 500_000_000,
-                "filter_project": 200_000_000}
+                "filter_project": 200_000_000, "gather": 200_000_000}
 
 
 def workload_config(workload, n, selectivity, world=1):
@@ -333,6 +335,11 @@ def workload_config(workload, n, selectivity, world=1):
                "filter": f"k < {int(round(1000 * selectivity))}", "project": "f1, f2, i1 of the 12-op program",
                "inputs": "a,b int64; x,y float64; k int32; 5% nulls", "fused": "filter+project in one kernel",
                "l2": "inputs exceed L2; no flush"}
+    elif workload == "gather":
+        cfg = {"workload": "gather", "rows": n, "pattern": selectivity if isinstance(selectivity, str) else "permutation",
+               "columns": "int32, int64, float32, float64, date32, bool8; 5% nulls", "index": "int32",
+               "api": "ral_materialize_columns (all columns in one kernel)",
+               "l2": "columns (5.8 GB at 200M rows) exceed L2; no flush"}
     elif workload == "plain_vm":
         cfg = {"workload": "plain_vm", "rows": n, "filter": "((c2>=24 AND c1<0.05) OR c0%7=3) AND c3<1200",
                "project": "c1*(1-c1)+c2", "fused": "filter+project in one kernel",
@@ -453,6 +460,101 @@ def filter_setup(workload, n, selectivity, device, null_rate=None):
         return n * sum(in_b) + k * out_b + 8
 
     return dict(step=step, alg_bytes_fn=alg_bytes, nout=nout, cols=frame, outs=outs, out_structs=os_, fq=fq, pq=pq)
+
+
+def gather_setup(n, pattern, device, null_rate=0.05):
+    """Every column of the six-column frame of filter_gather (int32, int64, float32, float64, date32,
+    bool8; 5% nulls) gathered by one int32 index column: a permutation (order-by), random indices
+    with repetition (join) or sorted random indices (the kept rows of a filter)."""
+    import ctypes
+    import torch
+    import ralgpu as R
+    from ralgpu import dtypes as D
+    from ralgpu import workloads as W
+    L = R.lib()
+    frame = [R.Column(v, m, t, n, nn) for t, v, m, nn in W.filter_gather_device(n, device=device, null_rate=null_rate)]
+    g = torch.Generator(device=device)
+    g.manual_seed(W.SEED + 1)
+    if pattern == "permutation":
+        idx = torch.randperm(n, generator=g, device=device, dtype=torch.int32)
+    else:
+        idx = torch.randint(0, n, (n,), generator=g, device=device, dtype=torch.int32)
+        if pattern == "sorted":
+            idx = torch.sort(idx).values
+    icol = R.Column(idx, None, D.GDF_INT32, n)
+    outs = [R.Column.empty(c.dtype, n, with_valid=c.valid is not None, device=device) for c in frame]
+    fa, fs = _colarray(frame)
+    oa, os_ = _colarray(outs)
+    ic = icol.to_c()
+
+    def step(stream):
+        rc = L.ral_materialize_columns(ctypes.cast(fa, ctypes.c_void_p), ctypes.cast(oa, ctypes.c_void_p),
+                                       len(frame), ctypes.byref(ic))
+        if rc:
+            raise RuntimeError(L.ral_last_error().decode())
+
+    def per_column(stream):
+        for c, o in zip(fs, os_):
+            rc = L.ral_materialize_column(ctypes.byref(c), ctypes.byref(o), ctypes.byref(ic))
+            if rc:
+                raise RuntimeError(L.ral_last_error().decode())
+
+    widths = [D.WIDTH[c.dtype] for c in frame]
+    masked = [c.valid is not None for c in frame]
+    # algorithmic: the index, one element read and one written per column, masks read and written
+    alg = n * (4 + sum(2 * w for w in widths) + sum(2 / 8 for m in masked if m))
+    return dict(step=step, per_column=per_column, alg_bytes=alg, cols=frame, outs=outs, idx=icol,
+                out_structs=os_, pattern=pattern)
+
+
+def gather_parity(ctx):
+    """Every output row of every column against the oracle's materialize_column, in chunks of
+    output rows on all host threads."""
+    import concurrent.futures as cf
+    import numpy as np
+    import oracle as O
+    t0 = time.perf_counter()
+    threads = os.cpu_count() or 1
+    n = ctx["idx"].size
+    idx = ctx["idx"].data[:n].cpu().numpy()
+    stats = {"valid": 0, "data": 0, "null_count": 0}
+    chunk = PARITY_CHUNK
+    for c, (col, out, st) in enumerate(zip(ctx["cols"], ctx["outs"], ctx["out_structs"])):
+        host = _oracle_chunk([col], 0, col.size)[0]
+
+        def one(s):
+            e = min(n, s + chunk)
+            exp = O.materialize_column(host, idx[s:e])
+            local = {"valid": 0, "data": 0}
+            _compare(out, s, e, exp, local)
+            return local, (exp.null_count if exp.valid is not None else 0)
+
+        nulls = 0
+        with cf.ThreadPoolExecutor(max_workers=threads) as ex:
+            for local, nc in ex.map(one, range(0, n, chunk)):
+                stats["valid"] += local["valid"]
+                stats["data"] += local["data"]
+                nulls += nc
+        stats["null_count"] += int(st.null_count != nulls)
+        del host
+    return {"rows": n, "columns": len(ctx["cols"]), "mismatches": sum(stats.values()), "detail": stats,
+            "checked": "every output row of every column, bit for bit: data of valid rows, validity bits, null counts",
+            "oracle_threads": threads, "seconds": round(time.perf_counter() - t0, 2)}
+
+
+def cpu_gather(rows: int, threads: int):
+    """The oracle's materialize_column over every column of the frame, output chunks on threads."""
+    import concurrent.futures as cf
+    import numpy as np
+    import oracle as O
+    from ralgpu import workloads as W
+    frame = [O.make_column(v, t, m) for t, v, m in W.filter_gather_host(rows, seed=99, null_rate=0.05)]
+    idx = np.random.default_rng(5).permutation(rows).astype(np.int32)
+    step = max(1, (rows + threads - 1) // threads)
+    t0 = time.perf_counter()
+    with cf.ThreadPoolExecutor(max_workers=threads) as ex:
+        list(ex.map(lambda s: [O.materialize_column(c, idx[s:s + step]) for c in frame], range(0, rows, step)))
+    return time.perf_counter() - t0
 
 
 def filter_e2e(ctx, steps):
@@ -632,6 +734,60 @@ def host_link_peak(nbytes=1 << 30, reps=5):
     return _LINK
 
 
+def aggregate_oracle_chunked(cols, query):
+    """The oracle's process_aggregate over device columns of any size: rows in chunks of
+    PARITY_CHUNK on all host threads, partial results combined (integer sums modulo 2^64, exact float
+    sums of the partial sums, MIN / MAX, counts; AVG as the combined sum over the combined count)."""
+    import math
+    import numpy as np
+    import oracle as O
+    from oracle import frontend as fe
+    threads = os.cpu_count() or 1
+    n = cols[0].size
+    _, aggs = fe.parse_aggregate(query)
+    # per chunk: AVG reduced as SUM; its count is the evaluated row count or the bare valid count
+    chunk_q = query.replace("=[AVG(", "=[SUM(")
+    parts = [[] for _ in aggs]
+    counts = [0] * len(aggs)
+    for s0 in range(0, n, PARITY_CHUNK):
+        e0 = min(n, s0 + PARITY_CHUNK)
+        frame = []
+        for c in cols:
+            data = np.ascontiguousarray(c.data[s0:e0].cpu().numpy())
+            frame.append(O.OColumn(data, None, c.dtype, 0) if c.valid is None
+                         else O.make_column(data, c.dtype, _bits_np(c.valid, s0, e0)))
+        res = O.process_aggregate(frame, chunk_q, nthreads=threads)
+        for i, ((name, op, expr), r) in enumerate(zip(aggs, res)):
+            parts[i].append(r)
+            if op == fe.GDF_AVG:
+                col = None if fe.contains_evaluation(expr) else frame[fe.get_index(expr)]
+                counts[i] += (e0 - s0) if col is None else col.size - col.null_count
+    out = []
+    for i, (name, op, expr) in enumerate(aggs):
+        ps = parts[i]
+        valid = [p for p in ps if p.is_valid]
+        t = ps[0].dtype if ps else fe.GDF_INT64
+        if op == fe.GDF_COUNT:
+            out.append(O.AggResult(fe.GDF_INT64, True, sum(p.value for p in ps)))
+        elif not valid:
+            out.append(O.AggResult(fe.GDF_FLOAT64 if op == fe.GDF_AVG else t, False))
+        elif op in (fe.GDF_MIN, fe.GDF_MAX):
+            v = min(p.value for p in valid) if op == fe.GDF_MIN else max(p.value for p in valid)
+            out.append(O.AggResult(t, True, v))
+        else:
+            bound = sum(p.float_sum_bound for p in valid)
+            if isinstance(valid[0].value, float):
+                total = math.fsum(p.value for p in valid)
+            else:
+                total = int(np.array([p.value for p in valid], dtype=np.int64).astype(np.uint64)
+                            .sum(dtype=np.uint64).astype(np.int64))
+            if op == fe.GDF_SUM:
+                out.append(O.AggResult(t, True, total, bound))
+            else:
+                out.append(O.AggResult(fe.GDF_FLOAT64, True, float(total) / counts[i], bound / counts[i]))
+    return out
+
+
 def measure_workload(args, workload, n, selectivity, device, world, sampler, e2e=True, cpu=True, parity=True,
                      cpu_budget_s=12.0):
     """One workload: warm-up, the timed steps (CUDA events on the launching stream, max over ranks),
@@ -641,6 +797,8 @@ def measure_workload(args, workload, n, selectivity, device, world, sampler, e2e
     rank = int(os.environ.get("RANK", "0"))
     if workload == "fused_project":
         ctx = fused_project_setup(n, device)
+    elif workload == "gather":
+        ctx = gather_setup(n, selectivity, device)
     else:
         ctx = filter_setup(workload, n, selectivity, device)
     stream = torch.cuda.current_stream()
@@ -670,7 +828,7 @@ def measure_workload(args, workload, n, selectivity, device, world, sampler, e2e
     peak, peak_kind = load_peaks()
     alg = ctx["alg_bytes"] if "alg_bytes" in ctx else ctx["alg_bytes_fn"]()
     achieved = alg / (kernel_ms / 1e3) / 1e9
-    traffic_key = workload if workload not in ("filter_gather", "filter_project") else f"{workload}_{selectivity}"
+    traffic_key = workload if workload not in ("filter_gather", "filter_project", "gather") else f"{workload}_{selectivity}"
     out = {
         "workload": workload, "value": job_rate(world, n, ms_per_step), "unit": "rows/s", "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_per_step,
@@ -684,8 +842,29 @@ def measure_workload(args, workload, n, selectivity, device, world, sampler, e2e
     }
     if "nout" in ctx:
         out["rows_out"] = ctx["nout"].value
+    if workload == "gather":
+        # the same gather as one ral_materialize_column call per column (the reference's loop shape)
+        for _ in range(2):
+            ctx["per_column"](stream)
+        torch.cuda.synchronize()
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(5)]
+        for a, b in ev:
+            a.record()
+            ctx["per_column"](stream)
+            b.record()
+        torch.cuda.synchronize()
+        pc = statistics.mean(a.elapsed_time(b) for a, b in ev)
+        out["per_column_calls"] = {"ms_per_step": pc, "value": n / (pc / 1e3), "calls": len(ctx["cols"]),
+                                   "speedup_of_fused": pc / ms_per_step,
+                                   "api": "ral_materialize_column once per column, index read each time"}
+        # a random gather reads one 32-byte sector per element and mask word (inputs exceed L2)
+        if ctx["pattern"] != "sorted":
+            touched = n * (4 + sum(32 + w for w in (R.dtypes.WIDTH[c.dtype] for c in ctx["cols"]))
+                           + sum(32 + 1 / 8 for c in ctx["cols"] if c.valid is not None))
+            out["roofline"]["sector_model_bytes_per_launch"] = touched
+            out["roofline"]["sector_model_gbs"] = touched / (kernel_ms / 1e3) / 1e9
     if rank == 0:
-        if e2e and not args.skip_e2e:
+        if e2e and not args.skip_e2e and workload != "gather":
             out["e2e"] = (fused_project_e2e(ctx, max(2, min(args.steps, 3)), device) if workload == "fused_project"
                           else filter_e2e(ctx, max(2, min(args.steps, 3))))
             link = host_link_peak()
@@ -694,7 +873,7 @@ def measure_workload(args, workload, n, selectivity, device, world, sampler, e2e
             out["e2e"]["host_link"]["frac_of_link"] = out["e2e"]["host_link"]["e2e_gbs"] / link["both_gbs"]
         # the device outputs (the e2e leg rewrote them with the same bits) against the oracle
         if parity and not args.skip_parity:
-            out["parity"] = parity_check(workload, ctx, selectivity)
+            out["parity"] = gather_parity(ctx) if workload == "gather" else parity_check(workload, ctx, selectivity)
         if cpu and not args.skip_cpu:
             out["cpu_baseline"] = cpu_baseline(workload, n, selectivity, budget_s=cpu_budget_s,
                                                single_budget_s=cpu_budget_s / 3)
@@ -705,7 +884,7 @@ def measure_workload(args, workload, n, selectivity, device, world, sampler, e2e
 
 # Workloads measured beside the default one in the same run: the 200M-row fused filter + project at
 # s = 0.5 (the target kernel) and the 500M-row filter + gather of six columns at s = 0.5.
-EXTRA_WORKLOADS = [("filter_project", 0.5), ("filter_gather", 0.5)]
+EXTRA_WORKLOADS = [("filter_project", 0.5), ("filter_gather", 0.5), ("gather", "permutation")]
 
 
 def run_ours(args):
@@ -716,19 +895,21 @@ def run_ours(args):
     n = args.rows or DEFAULT_ROWS[args.workload]
     sampler = ClockSampler(local)
     sampler.start()
-    main = measure_workload(args, args.workload, n, args.selectivity, device, world, sampler)
+    sel = args.pattern if args.workload == "gather" else args.selectivity
+    main = measure_workload(args, args.workload, n, sel, device, world, sampler)
     extra = {}
     if args.workload == "fused_project" and not args.rows and not args.no_extra:
         for wl, sel in EXTRA_WORKLOADS:
-            extra[f"{wl}_s{sel}"] = measure_workload(args, wl, DEFAULT_ROWS[wl], sel, device, world, sampler,
-                                                     cpu_budget_s=6.0)
+            key = f"{wl}_{sel}" if isinstance(sel, str) else f"{wl}_s{sel}"
+            extra[key] = measure_workload(args, wl, DEFAULT_ROWS[wl], sel, device, world, sampler, cpu_budget_s=6.0)
     sampler.stop()
     out = {
         "metric": METRIC, "value": main["value"], "unit": "rows/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": main["ms_per_step"], "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None,
         "dtype": {"fused_project": "f64+int64", "filter_project": "f64+int64", "plain_vm": "f64+int64",
-                  "filter_gather": "int32/int64/f32/f64/date32/bool8 gather"}[args.workload],
+                  "filter_gather": "int32/int64/f32/f64/date32/bool8 gather",
+                  "gather": "int32/int64/f32/f64/date32/bool8 gather"}[args.workload],
         "data": "synthetic (seeded, generated on the GPU)",
         "config": main["config"],
         "hbm_gbs": main["roofline"]["achieved"],
@@ -1123,21 +1304,23 @@ def run_reference(args):
     n = args.rows or DEFAULT_ROWS[args.workload]
     threads = os.cpu_count() or 1
     # bounded sample per step, sized from a probe so the whole run stays within a few minutes
+    sel = args.pattern if args.workload == "gather" else args.selectivity
     probe = min(n, 1_000_000)
-    dt = cpu_time(args.workload, probe, threads, args.selectivity)
+    dt = cpu_time(args.workload, probe, threads, sel)
     rows = int(min(n, max(probe, (probe / max(dt, 1e-9)) * 4.0)))
     for _ in range(args.warmup):
-        cpu_time(args.workload, min(rows, probe), threads, args.selectivity)
-    times = [cpu_time(args.workload, rows, threads, args.selectivity) for _ in range(args.steps)]
+        cpu_time(args.workload, min(rows, probe), threads, sel)
+    times = [cpu_time(args.workload, rows, threads, sel) for _ in range(args.steps)]
     t = sum(times) / len(times)
     v = rows / t
     out = {"metric": METRIC, "value": v, "unit": "rows/s", "n_gpus": world, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": t * 1e3, "higher_is_better": True, "scaling": "weak",
            "vs_baseline": None,
            "dtype": {"fused_project": "f64+int64", "filter_project": "f64+int64", "plain_vm": "f64+int64",
-                     "filter_gather": "int32/int64/f32/f64/date32/bool8 gather"}[args.workload],
+                     "filter_gather": "int32/int64/f32/f64/date32/bool8 gather",
+                  "gather": "int32/int64/f32/f64/date32/bool8 gather"}[args.workload],
            "data": "synthetic (seeded)", "impl": "reference",
-           "config": workload_config(args.workload, n, args.selectivity, world),
+           "config": workload_config(args.workload, n, sel, world),
            "cpu_baseline": {"value": v, "unit": "rows/s", "cores": threads, "kind": "port",
                             "sample": f"{rows} of {n} rows per step", "cpu_model": cpu_model()},
            "e2e": {"value": v, "unit": "rows/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -1151,7 +1334,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="fused_project",
-                    choices=["fused_project", "plain_vm", "filter_gather", "filter_project", "batched", "served"])
+                    choices=["fused_project", "plain_vm", "filter_gather", "filter_project", "gather", "batched",
+                             "served"])
     ap.add_argument("--tables", type=int, default=24)
     ap.add_argument("--queries", type=int, default=96)
     ap.add_argument("--requests", type=int, default=50_000)
@@ -1166,6 +1350,8 @@ def main():
     ap.add_argument("--capped-rows", type=int, default=1_000_000,
                     help="batched: also compare batch and plain calls over the first N rows of every table")
     ap.add_argument("--selectivity", type=float, default=0.5)
+    ap.add_argument("--pattern", default="permutation", choices=["permutation", "random", "sorted"],
+                    help="gather: the index column's pattern")
     ap.add_argument("--rows", type=int, default=0)
     ap.add_argument("--skip-e2e", action="store_true")
     ap.add_argument("--skip-cpu", action="store_true")

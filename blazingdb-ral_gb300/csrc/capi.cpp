@@ -318,6 +318,89 @@ int ral_materialize_column(const gdf_column* input, gdf_column* output, const gd
     });
 }
 
+int ral_materialize_columns(const gdf_column* const* inputs, gdf_column* const* outputs, int32_t num_columns,
+                            const gdf_column* row_indices) {
+    return guarded([&] {
+        if (!row_indices || (num_columns > 0 && (!inputs || !outputs))) return set_error(kInvalidArgument, "null argument");
+        if (num_columns < 0 || num_columns > kMaxGatherColumns)
+            return set_error(kInvalidArgument, "materialize_columns: 0.." + std::to_string(kMaxGatherColumns) + " columns");
+        const int iw = gdf_dtype_size(row_indices->dtype);
+        if (iw == 0 || dtype_is_float(row_indices->dtype))
+            return set_error(kInvalidArgument, "materialize_columns: row_indices must be an INT8/16/32/64 column");
+        const int64_t n = row_indices->size;
+        if (n < 0) return set_error(kInvalidArgument, "materialize_columns: negative row count");
+        if (n > 0 && !row_indices->data) return set_error(kInvalidArgument, "materialize_columns: row_indices without data");
+        GatherColumnsParams p{};
+        p.idx = row_indices->data;
+        p.idx_width = iw;
+        p.n_out = n;
+        p.num_columns = num_columns;
+        int64_t n_in = -1;
+        for (int c = 0; c < num_columns; c++) {
+            const gdf_column* in = inputs[c];
+            gdf_column* out = outputs[c];
+            if (!in || !out) return set_error(kInvalidArgument, "materialize_columns: null column");
+            const int w = gdf_dtype_size(in->dtype);
+            if (w == 0) return set_error(kInvalidArgument, "materialize_columns: unsupported dtype of column " + std::to_string(c));
+            if (gdf_dtype_size(out->dtype) != w)
+                return set_error(kInvalidArgument, "materialize_columns: width mismatch in column " + std::to_string(c));
+            if (n_in < 0) n_in = in->size;
+            if (in->size != n_in) return set_error(kInvalidArgument, "materialize_columns: input columns differ in size");
+            if (n > 0 && ((in->size > 0 && !in->data) || !out->data))
+                return set_error(kInvalidArgument, "materialize_columns: column without data");
+            if (((uintptr_t)in->valid & 3) || ((uintptr_t)out->valid & 3))
+                return set_error(kInvalidArgument, "materialize_columns: masks must be 4-byte aligned");
+            p.col[c] = GatherColumn{in->data, (const uint32_t*)in->valid, out->data, (uint32_t*)out->valid, w, 0};
+        }
+        p.n_in = n_in < 0 ? 0 : n_in;
+        cudaStream_t st = cudaStreamPerThread;
+        std::vector<unsigned long long> h(num_columns > 0 ? num_columns : 1, 0);
+        if (n > 0 && num_columns > 0) {
+            unsigned long long* d = nullptr;
+            if (int e = check_cuda(cudaMallocAsync((void**)&d, sizeof(unsigned long long) * num_columns, st), "cudaMallocAsync")) return e;
+            int rc = check_cuda(cudaMemsetAsync(d, 0, sizeof(unsigned long long) * num_columns, st), "cudaMemsetAsync");
+            p.valid_counts = d;
+            if (!rc) rc = check_cuda(launch_gather_columns(p, st), "gather_columns");
+            if (!rc) rc = check_cuda(cudaMemcpyAsync(h.data(), d, sizeof(unsigned long long) * num_columns,
+                                                     cudaMemcpyDeviceToHost, st), "cudaMemcpyAsync");
+            cudaFreeAsync(d, st);
+            if (int e = check_cuda(cudaStreamSynchronize(st), "materialize_columns")) return e;
+            if (rc) return rc;
+        }
+        for (int c = 0; c < num_columns; c++) {
+            outputs[c]->size = (gdf_size_type)n;
+            outputs[c]->null_count = outputs[c]->valid ? (gdf_size_type)(n - (int64_t)h[c]) : 0;
+        }
+        return (int)kSuccess;
+    });
+}
+
+int ral_process_aggregate(gdf_column* const* frame_columns, int32_t num_columns, const char* query_part,
+                          gdf_scalar* results, int32_t capacity, int32_t* num_results) {
+    return guarded([&] {
+        int n = 0;
+        const int rc = process_aggregate(frame_columns, num_columns, query_part, results, capacity, &n,
+                                         cudaStreamPerThread);
+        if (num_results) *num_results = n;
+        return rc;
+    });
+}
+
+int ral_debug_aggregate_source(const gdf_dtype* frame_dtypes, const int32_t* frame_nullable,
+                               const int64_t* frame_null_counts, int32_t num_columns, const char* query_part,
+                               int32_t compile, char* source_out, int64_t source_capacity, char* log_out,
+                               int64_t log_capacity) {
+    return guarded([&] {
+        if (!frame_dtypes || num_columns <= 0 || !query_part) return set_error(kInvalidArgument, "null argument");
+        std::string src, log;
+        const int rc = aggregate_source(frame_dtypes, frame_nullable, frame_null_counts, num_columns, query_part,
+                                        compile != 0, src, log);
+        copy_out(src, source_out, source_capacity);
+        copy_out(log, log_out, log_capacity);
+        return rc;
+    });
+}
+
 int ral_apply_boolean_mask(const gdf_column* stencil, gdf_column* out_indices, gdf_size_type* num_rows_out) {
     return guarded([&] {
         if (!stencil || !out_indices || !num_rows_out) return set_error(kInvalidArgument, "null argument");

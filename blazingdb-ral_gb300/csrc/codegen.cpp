@@ -538,6 +538,241 @@ GeneratedKernel generate_eval_kernel(const Program& p, const Shape& s) {
     return gk;
 }
 
+namespace {
+
+bool slot_float(const AggregateSlot& a) { return dtype_is_float(a.dtype); }
+
+// cudf's reduction identities in the reduced column's type (numeric_limits max / lowest), as
+// literals of the accumulator type
+std::string slot_identity(const AggregateSlot& a) {
+    if (a.op == GDF_SUM) return slot_float(a) ? "0.0" : "0ll";
+    const bool mn = a.op == GDF_MIN;
+    switch (a.dtype) {
+    case GDF_FLOAT32: return mn ? "3.4028234663852886e+38" : "-3.4028234663852886e+38";
+    case GDF_FLOAT64: return mn ? "1.7976931348623157e+308" : "-1.7976931348623157e+308";
+    case GDF_INT8: case GDF_BOOL8: return mn ? "127ll" : "-128ll";
+    case GDF_INT16: return mn ? "32767ll" : "-32768ll";
+    case GDF_INT32: case GDF_DATE32: case GDF_CATEGORY: case GDF_STRING_CATEGORY:
+        return mn ? "2147483647ll" : "(-2147483647ll - 1)";
+    default: return mn ? "9223372036854775807ll" : "(-9223372036854775807ll - 1)";
+    }
+}
+
+// acc = fold(acc, v): wrapping int64 add, IEEE double add, or std::min / std::max (which keep the
+// accumulator unless the new value compares below / above it)
+std::string slot_fold(const AggregateSlot& a, const std::string& acc, const std::string& v) {
+    const bool f = slot_float(a);
+    if (a.op == GDF_SUM)
+        return f ? "__dadd_rn(" + acc + ", " + v + ")" : "ral_addi(" + acc + ", " + v + ")";
+    if (a.op == GDF_MIN)
+        return f ? "(ral_dlt(" + v + ", " + acc + ") ? " + v + " : " + acc + ")" : "(" + v + " < " + acc + " ? " + v + " : " + acc + ")";
+    return f ? "(ral_dlt(" + acc + ", " + v + ") ? " + v + " : " + acc + ")" : "(" + acc + " < " + v + " ? " + v + " : " + acc + ")";
+}
+
+// A column element as the accumulator's type: ints sign-extended to int64, floats to double.
+std::string slot_value(const std::string& elem, gdf_dtype t) {
+    if (t == GDF_FLOAT32) return "ral_f2d(" + elem + ")";
+    if (t == GDF_FLOAT64) return "(" + elem + ")";
+    return "((ral_i64)(" + elem + "))";
+}
+
+}  // namespace
+
+GeneratedKernel generate_aggregate_kernel(const Program& p, const std::vector<AggregateSlot>& slots,
+                                          const std::vector<ColumnDesc>& bare, const Shape& s) {
+    GeneratedKernel gk;
+    gk.shape = s;
+    const int NB = (int)bare.size();
+    gk.layout = make_layout(p, 1 + 2 * NB);
+    const ParamLayout& L = gk.layout;
+    const int scratch_slot = L.counts + 1;
+    const int bare_data = scratch_slot + 1, bare_valid = bare_data + NB;
+    const int S = (int)slots.size();
+    const bool has_prog = p.n_out > 0;
+    const std::vector<bool> load = has_prog ? p.inputs_referenced() : std::vector<bool>(p.n_in, false);
+    const auto raw = has_prog ? p.inputs_raw_valid() : std::vector<bool>(p.n_in, false);
+    std::vector<bool> mask(NB, false);  // bare columns whose null rows are skipped
+    for (const auto& a : slots)
+        if (!a.evaluated && a.skip_nulls) mask[a.index] = true;
+    const auto fk = has_prog ? final_kinds(p, L) : std::vector<Kind>();
+
+    std::ostringstream key;
+    key << "agg|" << (has_prog ? p.structure_key() : std::string("-")) << "|";
+    for (const auto& b : bare) key << (int)b.dtype << (b.has_valid ? "v" : "n") << ",";
+    key << "|";
+    for (const auto& a : slots)
+        key << a.op << (a.evaluated ? "e" : "c") << a.index << ":" << (int)a.dtype << (a.skip_nulls ? "s" : "") << ";";
+    key << "|G" << s.G << "J" << s.J << "T" << s.threads << "B" << s.min_blocks;
+    char hex[32];
+    snprintf(hex, sizeof hex, "%016llx", (unsigned long long)fnv1a(key.str()));
+    gk.name = std::string("ral_agg_") + hex;
+
+    std::ostringstream os;
+    os << "// generated: " << key.str() << "\n";
+    os << "#define RAL_G " << s.G << "\n#define RAL_J " << s.J << "\n#define RAL_THREADS " << s.threads << "\n";
+    os << "struct RalParams { ral_u64 s[" << L.total << "]; };\n\n";
+    if (has_prog) emit_row_function(os, p, L, "ral_row");
+    auto acc_t = [&](const AggregateSlot& a) { return slot_float(a) ? "double" : "ral_i64"; };
+    auto to_u64 = [&](const AggregateSlot& a, const std::string& v) {
+        return slot_float(a) ? "(ral_u64)__double_as_longlong(" + v + ")" : "(ral_u64)(" + v + ")";
+    };
+    auto from_u64 = [&](const AggregateSlot& a, const std::string& v) {
+        return slot_float(a) ? "__longlong_as_double((long long)(" + v + "))" : "(ral_i64)(" + v + ")";
+    };
+    // the per-row fold: elem / bit give a program input's element and raw validity bit, belem /
+    // bbit a bare column's
+    auto emit_folds = [&](const std::string& ind, const std::function<std::string(int)>& elem,
+                          const std::function<std::string(int)>& bit, const std::function<std::string(int)>& belem,
+                          const std::function<std::string(int)>& bbit) {
+        std::ostringstream o;
+        if (has_prog) {
+            for (int q = 0; q < p.n_out; q++) o << ind << kind_ctype(fk[q]) << " y" << q << ";\n";
+            o << ind << "ral_row(P";
+            for (int c = 0; c < p.n_in; c++)
+                if (p.inputs_referenced()[c]) o << ", " << widen(elem(c), p.inputs[c].dtype);
+            for (int c = 0; c < p.n_in; c++)
+                if (raw[c]) o << ", " << bit(c);
+            for (int q = 0; q < p.n_out; q++) o << ", y" << q;
+            o << ");\n";
+        }
+        for (int k = 0; k < S; k++) {
+            const auto& a = slots[k];
+            std::string v;
+            if (a.evaluated)
+                v = slot_value(narrow("y" + std::to_string(a.index), fk[a.index], a.dtype), a.dtype);
+            else
+                v = slot_value(belem(a.index), a.dtype);
+            const std::string acc = "acc" + std::to_string(k);
+            if (!a.evaluated && a.skip_nulls)
+                o << ind << "if (" << bbit(a.index) << ") " << acc << " = " << slot_fold(a, acc, v) << ";\n";
+            else
+                o << ind << acc << " = " << slot_fold(a, acc, v) << ";\n";
+        }
+        return o.str();
+    };
+
+    os << "\nextern \"C\" __global__ void __launch_bounds__(RAL_THREADS, " << s.min_blocks << ") " << gk.name
+       << "(const __grid_constant__ RalParams P) {\n";
+    os << "    const ral_i64 n = (ral_i64)P.s[" << L.n_rows << "];\n";
+    for (int c = 0; c < p.n_in; c++) {
+        if (load[c])
+            os << "    const " << element_ctype(p.inputs[c].dtype) << "* __restrict__ pin" << c << " = (const "
+               << element_ctype(p.inputs[c].dtype) << "*)P.s[" << L.in_data + c << "];\n";
+        if (raw[c] && p.inputs[c].has_valid)
+            os << "    const ral_u32* __restrict__ pvr" << c << " = (const ral_u32*)P.s[" << L.in_valid + c << "];\n";
+    }
+    for (int c = 0; c < NB; c++) {
+        os << "    const " << element_ctype(bare[c].dtype) << "* __restrict__ pbx" << c << " = (const "
+           << element_ctype(bare[c].dtype) << "*)P.s[" << bare_data + c << "];\n";
+        if (mask[c] && bare[c].has_valid)
+            os << "    const ral_u32* __restrict__ pbv" << c << " = (const ral_u32*)P.s[" << bare_valid + c << "];\n";
+    }
+    for (int k = 0; k < S; k++) os << "    " << acc_t(slots[k]) << " acc" << k << " = " << slot_identity(slots[k]) << ";\n";
+    os << "    const int lane = threadIdx.x & 31;\n";
+    os << "    const ral_i64 gwarp = ((ral_i64)blockIdx.x * RAL_THREADS + threadIdx.x) >> 5;\n";
+    os << "    const ral_i64 nwarp = ((ral_i64)gridDim.x * RAL_THREADS) >> 5;\n";
+    os << "    const ral_i64 TILE = 32 * RAL_G * RAL_J;\n";
+    os << "    const ral_i64 ntiles = n / TILE;\n";
+    os << "    for (ral_i64 t = gwarp; t < ntiles; t += nwarp) {\n";
+    os << "        const ral_i64 base = t * TILE;\n";
+    os << "#pragma unroll\n";
+    os << "        for (int j = 0; j < RAL_J; ++j) {\n";
+    os << "            const ral_i64 r = base + (ral_i64)j * 32 * RAL_G + lane * RAL_G;\n";
+    for (int c = 0; c < p.n_in; c++) {
+        if (!load[c]) continue;
+        const char* et = element_ctype(p.inputs[c].dtype);
+        os << "            " << et << " a" << c << "[RAL_G]; ral_ldg<" << et << ", RAL_G>(pin" << c << ", r, a" << c << ");\n";
+    }
+    for (int c = 0; c < NB; c++) {
+        const char* et = element_ctype(bare[c].dtype);
+        os << "            " << et << " e" << c << "[RAL_G]; ral_ldg<" << et << ", RAL_G>(pbx" << c << ", r, e" << c << ");\n";
+    }
+    for (int c = 0; c < p.n_in; c++) {
+        if (!raw[c]) continue;
+        if (p.inputs[c].has_valid) os << "            const ral_u32 rw" << c << " = __ldg(pvr" << c << " + (r >> 5));\n";
+        else os << "            const ral_u32 rw" << c << " = 0xffffffffu;\n";
+    }
+    for (int c = 0; c < NB; c++) {
+        if (!mask[c]) continue;
+        if (bare[c].has_valid) os << "            const ral_u32 bw" << c << " = __ldg(pbv" << c << " + (r >> 5));\n";
+        else os << "            const ral_u32 bw" << c << " = 0xffffffffu;\n";
+    }
+    os << "#pragma unroll\n";
+    os << "            for (int g = 0; g < RAL_G; ++g) {\n";
+    os << emit_folds("                ", [](int c) { return "a" + std::to_string(c) + "[g]"; },
+                     [](int c) { return "((rw" + std::to_string(c) + " >> ((int)(r & 31) + g)) & 1u)"; },
+                     [](int c) { return "e" + std::to_string(c) + "[g]"; },
+                     [](int c) { return "((bw" + std::to_string(c) + " >> ((int)(r & 31) + g)) & 1u)"; });
+    os << "            }\n";
+    os << "        }\n";
+    os << "    }\n";
+    // tail rows, one warp
+    os << "    const ral_i64 tail0 = ntiles * TILE;\n";
+    os << "    if (tail0 < n && gwarp == (ntiles % nwarp)) {\n";
+    os << "        for (ral_i64 r = tail0 + lane; r < n; r += 32) {\n";
+    for (int c = 0; c < p.n_in; c++) {
+        if (!raw[c]) continue;
+        if (p.inputs[c].has_valid) os << "            const ral_u32 rw" << c << " = __ldg(pvr" << c << " + (r >> 5));\n";
+        else os << "            const ral_u32 rw" << c << " = 0xffffffffu;\n";
+    }
+    for (int c = 0; c < NB; c++) {
+        if (!mask[c]) continue;
+        if (bare[c].has_valid) os << "            const ral_u32 bw" << c << " = __ldg(pbv" << c << " + (r >> 5));\n";
+        else os << "            const ral_u32 bw" << c << " = 0xffffffffu;\n";
+    }
+    os << emit_folds("            ", [](int c) { return "pin" + std::to_string(c) + "[r]"; },
+                     [](int c) { return "((rw" + std::to_string(c) + " >> (int)(r & 31)) & 1u)"; },
+                     [](int c) { return "pbx" + std::to_string(c) + "[r]"; },
+                     [](int c) { return "((bw" + std::to_string(c) + " >> (int)(r & 31)) & 1u)"; });
+    os << "        }\n";
+    os << "    }\n";
+    // warp -> block -> block partials -> the last block folds them in block order
+    os << "    __shared__ ral_u64 red[RAL_THREADS / 32][" << S << "];\n";
+    os << "    __shared__ int s_last;\n";
+    for (int k = 0; k < S; k++) {
+        const auto& a = slots[k];
+        const std::string acc = "acc" + std::to_string(k);
+        os << "    for (int off = 16; off > 0; off >>= 1) { const " << acc_t(a) << " o = __shfl_down_sync(0xffffffffu, "
+           << acc << ", off); " << acc << " = " << slot_fold(a, acc, "o") << "; }\n";
+        os << "    if (lane == 0) red[threadIdx.x >> 5][" << k << "] = " << to_u64(a, acc) << ";\n";
+    }
+    os << "    __syncthreads();\n";
+    os << "    ral_u64* scratch = (ral_u64*)P.s[" << scratch_slot << "];\n";
+    os << "    ral_u64* partials = scratch + 1 + " << S << ";\n";
+    os << "    if (threadIdx.x == 0) {\n";
+    for (int k = 0; k < S; k++) {
+        const auto& a = slots[k];
+        os << "        {\n";
+        os << "            " << acc_t(a) << " v = " << from_u64(a, "red[0][" + std::to_string(k) + "]") << ";\n";
+        os << "            for (int w = 1; w < RAL_THREADS / 32; ++w) { const " << acc_t(a) << " o = "
+           << from_u64(a, "red[w][" + std::to_string(k) + "]") << "; v = " << slot_fold(a, "v", "o") << "; }\n";
+        os << "            partials[(ral_i64)blockIdx.x * " << S << " + " << k << "] = " << to_u64(a, "v") << ";\n";
+        os << "        }\n";
+    }
+    os << "        __threadfence();\n";
+    os << "        const unsigned done = atomicAdd((unsigned*)scratch, 1u);\n";
+    os << "        s_last = done == gridDim.x - 1;\n";
+    os << "    }\n";
+    os << "    __syncthreads();\n";
+    os << "    if (s_last && threadIdx.x < " << S << ") {\n";
+    os << "        __threadfence();\n";
+    os << "        const int k = threadIdx.x;\n";
+    for (int k = 0; k < S; k++) {
+        const auto& a = slots[k];
+        os << "        if (k == " << k << ") {\n";
+        os << "            " << acc_t(a) << " v = " << from_u64(a, "__ldcg(partials + " + std::to_string(k) + ")") << ";\n";
+        os << "            for (unsigned b = 1; b < gridDim.x; ++b) { const " << acc_t(a) << " o = "
+           << from_u64(a, "__ldcg(partials + (ral_i64)b * " + std::to_string(S) + " + " + std::to_string(k) + ")")
+           << "; v = " << slot_fold(a, "v", "o") << "; }\n";
+        os << "            scratch[1 + " << k << "] = " << to_u64(a, "v") << ";\n";
+        os << "        }\n";
+    }
+    os << "    }\n";
+    os << "}\n";
+    gk.source = os.str();
+    return gk;
+}
+
 int filter_max_width(const FilterSpec& f) {
     int w = 1;
     if (f.clone_stencil) w = std::max(w, gdf_dtype_size(f.frame_dtypes[f.clone_column]));

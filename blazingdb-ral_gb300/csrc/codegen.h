@@ -117,6 +117,32 @@ GeneratedKernel generate_eval_kernel(const Program& p, const Shape& s);
 
 // One output column of the fused filter kernel: either a gathered frame column
 // or an output of the projection program, written compacted.
+// ---- aggregate-input expressions fused with the reduction ----------------------------------
+// One reduction per slot, over either a program output (an evaluated aggregate input, its
+// narrowed value on every row: the reference reduces the evaluated column with null_count 0, so
+// its validity is not consulted) or a column of its own (a bare "$k" input; rows whose bit is
+// clear are skipped when the column has nulls).
+struct AggregateSlot {
+    int op = 0;             // GDF_SUM, GDF_MIN or GDF_MAX (AVG reduces as SUM; COUNT needs no kernel)
+    bool evaluated = false;
+    int index = -1;         // program output, or bare column (index into the bare-column list)
+    gdf_dtype dtype = GDF_invalid;  // dtype of the reduced column
+    bool skip_nulls = false;
+};
+
+// Scratch of an aggregate kernel (zeroed before the launch), 64-bit words: [0] finished-block
+// counter, [1 .. S] the results, then grid x S block partials.
+inline int64_t aggregate_scratch_words(int slots, int grid) { return 1 + slots + (int64_t)grid * slots; }
+
+// The kernel reads every referenced input once, runs the program per row, folds each slot into a
+// per-thread accumulator (integer SUM: int64, wrapping; float SUM: double; MIN / MAX: in the
+// column's type with cudf's identities, numeric_limits max / lowest), reduces warps and blocks in
+// a fixed order, and the last block folds the block partials in block order: deterministic for a
+// given grid.  Param slots: the eval layout, then [counts + 1] = scratch, then the data and the
+// validity pointers of the bare columns.
+GeneratedKernel generate_aggregate_kernel(const Program& p, const std::vector<AggregateSlot>& slots,
+                                          const std::vector<ColumnDesc>& bare, const Shape& s);
+
 struct FilterOutput {
     bool from_project = false;
     int index = -1;          // frame column (gathered) or projection output number

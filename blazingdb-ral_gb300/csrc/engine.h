@@ -86,6 +86,13 @@ int launch_blocks(const CompiledKernel& k, int threads, int64_t work_items_per_b
 // Parameter block filled in ParamLayout order.
 void fill_scalars(const Program& p, const ParamLayout& L, std::vector<uint64_t>& slots);
 
+// process_aggregate without GROUP BY, expressions fused with the reduction (aggregate.cpp).
+int process_aggregate(gdf_column* const* frame, int n_cols, const char* query, gdf_scalar* results, int capacity,
+                      int* num_results, cudaStream_t st);
+// Generated source (and optionally an NVRTC compile) of a plan's aggregate kernel.
+int aggregate_source(const gdf_dtype* dtypes, const int32_t* nullable, const int64_t* null_counts, int n_cols,
+                     const char* query, bool compile, std::string& source, std::string& log);
+
 // Count of kernels this library has launched (all entry points).
 void note_launch(int count = 1);
 long long launch_count();

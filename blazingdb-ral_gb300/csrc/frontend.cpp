@@ -490,4 +490,61 @@ ProjectPlan plan_project(const std::string& q, const std::vector<gdf_dtype>& fra
     return pp;
 }
 
+AggregatePlan plan_aggregate(const std::string& q, const std::vector<gdf_dtype>& frame) {
+    AggregatePlan ap;
+    const int n_frame = (int)frame.size();
+    if (q.find("LogicalAggregate") == std::string::npos) throw ParseError("not a LogicalAggregate: " + q);
+    auto exprs = project_expressions(q);
+    std::vector<std::unique_ptr<Expr>> trees;
+    std::vector<bool> used(n_frame, false);
+    for (auto& [name, text] : exprs) {
+        if (name == "group") {
+            // group=[{0, 1}]: the GROUP BY columns (get_group_columns)
+            for (size_t i = 0; i < text.size(); i++)
+                if (std::isdigit((unsigned char)text[i])) {
+                    size_t j = i;
+                    while (j < text.size() && std::isdigit((unsigned char)text[j])) j++;
+                    ap.group_columns.push_back(std::atoi(text.substr(i, j - i).c_str()));
+                    i = j;
+                }
+            continue;
+        }
+        AggregatePlan::Aggregation a;
+        a.name = name;
+        const std::string op = text.substr(0, text.find('('));
+        if (op == "SUM") a.op = GDF_SUM;
+        else if (op == "MIN") a.op = GDF_MIN;
+        else if (op == "MAX") a.op = GDF_MAX;
+        else if (op == "AVG") a.op = GDF_AVG;
+        else if (op == "COUNT") a.op = GDF_COUNT;
+        else if (op == "COUNT_DISTINCT") throw ParseError("COUNT_DISTINCT is not supported without a group by");
+        else throw ParseError("aggregation type not supported: " + op);
+        const size_t open = text.find('('), close = text.rfind(')');
+        const std::string input = (open == std::string::npos || close == std::string::npos || close < open)
+                                      ? std::string()
+                                      : text.substr(open + 1, close - open - 1);
+        if (contains_evaluation(input)) {
+            trees.push_back(parse_expression(input));
+            ap.eval_dtypes.push_back(expression_output_type(*trees.back(), frame));
+            collect_columns(*trees.back(), used);
+            a.evaluated = true;
+            a.index = (int)trees.size() - 1;
+        } else {
+            bool blank = true;
+            for (char c : input) blank = blank && c == ' ';
+            a.index = blank ? 0 : column_reference_index(input);
+            if (a.index < 0 || a.index >= n_frame) throw ParseError("column reference out of range");
+        }
+        ap.aggregations.push_back(a);
+    }
+    std::vector<int> remap(n_frame, -1);
+    for (int c = 0; c < n_frame; c++)
+        if (used[c]) { remap[c] = (int)ap.input_columns.size(); ap.input_columns.push_back(c); }
+    const int n_in = (int)ap.input_columns.size();
+    const int n_eval = (int)trees.size();
+    for (int k = 0; k < n_eval; k++) ap.pv.final_pos.push_back((int16_t)(n_in + k));
+    for (int k = 0; k < n_eval; k++) emit_expression(*trees[k], k, n_eval, n_in, remap, ap.pv);
+    return ap;
+}
+
 }  // namespace ral

@@ -84,4 +84,26 @@ struct ProjectPlan {
 };
 ProjectPlan plan_project(const std::string& query_part, const std::vector<gdf_dtype>& frame_dtypes);
 
+// Plan for a LogicalAggregate (process_aggregate, src/operators/GroupBy.cpp:531-590): the GROUP BY
+// columns, and per aggregation its operator (get_aggregation_operation,
+// CalciteExpressionParsing.cpp:483-507) and input, the text between the outer parentheses
+// (get_string_between_outer_parentheses, :756-767).  An input that contains an evaluation is an
+// output of ONE program over every evaluated input (the reference evaluates each into a column of
+// its own; data does not depend on op positions); any other input is a frame column (get_index,
+// an empty text -- COUNT() -- meaning column 0).
+struct AggregatePlan {
+    std::vector<int> group_columns;
+    std::vector<int> input_columns;         // program inputs: frame columns in register order
+    ProgramVectors pv;
+    std::vector<gdf_dtype> eval_dtypes;     // per evaluated input: get_output_type_expression
+    struct Aggregation {
+        std::string name;
+        int op = 0;                         // gdf_agg_op
+        bool evaluated = false;
+        int index = -1;                     // evaluated input number, or frame column
+    };
+    std::vector<Aggregation> aggregations;
+};
+AggregatePlan plan_aggregate(const std::string& query_part, const std::vector<gdf_dtype>& frame_dtypes);
+
 }  // namespace ral

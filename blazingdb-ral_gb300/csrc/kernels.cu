@@ -90,6 +90,91 @@ cudaError_t gather_by_index(const void* in, const uint32_t* in_valid, int64_t n_
 }
 
 
+// ---- every column of a frame gathered by one index column -----------------------------------
+// A warp takes 128 consecutive output rows per step; lane t handles rows base + t + 32 k (k < 4),
+// so each k is one coalesced index load, one coalesced store per column and one ballot-built
+// validity word per nullable column, and every lane has four independent gathers in flight per
+// column.  The index is read once for all columns (materialize_column, called once per column,
+// reads it twice per column: its bit gather and its data gather).
+constexpr int kGatherRowsPerLane = 4;
+
+template <typename I>
+__device__ __forceinline__ ral_i64 ral_load_index(const void* idx, ral_i64 i) {
+    return (ral_i64)__ldcs(reinterpret_cast<const I*>(idx) + i);
+}
+
+template <typename E>
+__device__ __forceinline__ void ral_gather_k(const GatherColumn& c, const ral_i64 (&j)[kGatherRowsPerLane],
+                                             const bool (&ok)[kGatherRowsPerLane], ral_i64 row0) {
+    const E* __restrict__ in = reinterpret_cast<const E*>(c.in);
+    E* __restrict__ out = reinterpret_cast<E*>(c.out);
+    E v[kGatherRowsPerLane];
+#pragma unroll
+    for (int k = 0; k < kGatherRowsPerLane; ++k)
+        if (ok[k]) v[k] = in[j[k]];
+#pragma unroll
+    for (int k = 0; k < kGatherRowsPerLane; ++k)
+        if (ok[k]) __stcs(out + row0 + 32 * k, v[k]);
+}
+
+__global__ void __launch_bounds__(256) gather_columns_kernel(const __grid_constant__ GatherColumnsParams P) {
+    __shared__ unsigned long long s_cnt[kMaxGatherColumns];
+    for (int c = threadIdx.x; c < P.num_columns; c += blockDim.x) s_cnt[c] = 0;
+    __syncthreads();
+    const int lane = threadIdx.x & 31;
+    const ral_i64 step_rows = 32 * kGatherRowsPerLane;
+    const ral_i64 nsteps = (P.n_out + step_rows - 1) / step_rows;
+    const ral_i64 gwarp = ((ral_i64)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const ral_i64 nwarp = ((ral_i64)gridDim.x * blockDim.x) >> 5;
+    for (ral_i64 s = gwarp; s < nsteps; s += nwarp) {
+        const ral_i64 base = s * step_rows;
+        ral_i64 j[kGatherRowsPerLane];
+        bool ok[kGatherRowsPerLane];
+#pragma unroll
+        for (int k = 0; k < kGatherRowsPerLane; ++k) {
+            const ral_i64 i = base + lane + 32 * k;
+            j[k] = -1;
+            if (i < P.n_out) {
+                switch (P.idx_width) {
+                case 1: j[k] = ral_load_index<int8_t>(P.idx, i); break;
+                case 2: j[k] = ral_load_index<int16_t>(P.idx, i); break;
+                case 4: j[k] = ral_load_index<int32_t>(P.idx, i); break;
+                default: j[k] = ral_load_index<long long>(P.idx, i); break;
+                }
+            }
+            ok[k] = j[k] >= 0 && j[k] < P.n_in;
+        }
+        const ral_i64 row0 = base + lane;
+        for (int c = 0; c < P.num_columns; ++c) {
+            const GatherColumn& col = P.col[c];
+            switch (col.width) {
+            case 1: ral_gather_k<int8_t>(col, j, ok, row0); break;
+            case 2: ral_gather_k<short>(col, j, ok, row0); break;
+            case 4: ral_gather_k<int>(col, j, ok, row0); break;
+            default: ral_gather_k<long long>(col, j, ok, row0); break;
+            }
+            if (col.out_valid) {
+                unsigned cnt = 0;
+#pragma unroll
+                for (int k = 0; k < kGatherRowsPerLane; ++k) {
+                    bool bit = ok[k];
+                    if (bit && col.in_valid) bit = (__ldg(col.in_valid + (j[k] >> 5)) >> (j[k] & 31)) & 1u;
+                    const ral_u32 word = __ballot_sync(0xffffffffu, bit);
+                    // word k covers rows base + 32 k .. +31; lane k writes it (masks are padded
+                    // to 64 bytes, so a partial last word stays inside the allocation)
+                    if (lane == k && base + 32 * k < P.n_out) col.out_valid[(base >> 5) + k] = word;
+                    cnt += __popc(word);
+                }
+                if (lane == 0 && cnt) atomicAdd(&s_cnt[c], (unsigned long long)cnt);
+            }
+        }
+    }
+    __syncthreads();
+    if (P.valid_counts)
+        for (int c = threadIdx.x; c < P.num_columns; c += blockDim.x)
+            if (s_cnt[c]) atomicAdd(P.valid_counts + c, s_cnt[c]);
+}
+
 // ---- single-pass stream compaction (decoupled look-back) ---------------------------------
 // Tile = 256 threads x 16 rows; the look-back is ral_lookback (device_rt.cuh).
 
@@ -193,6 +278,20 @@ cudaError_t launch_gather(int width, const void* in, const uint32_t* in_valid, i
     case 8: return gather_by_index<int64_t>(in, in_valid, n_in, idx, idx_width, n_out, out, out_valid, valid_count, st);
     default: return cudaErrorInvalidValue;
     }
+}
+
+cudaError_t launch_gather_columns(const GatherColumnsParams& p, cudaStream_t st) {
+    if (p.n_out <= 0 || p.num_columns <= 0) return cudaSuccess;
+    int dev = 0, sms = 1, per_sm = 1;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, gather_columns_kernel, 256, 0);
+    if (per_sm < 1) per_sm = 1;
+    const int64_t steps = (p.n_out + 32 * kGatherRowsPerLane - 1) / (32 * kGatherRowsPerLane);
+    const int64_t grid = std::max<int64_t>(1, std::min<int64_t>((steps + 7) / 8, (int64_t)sms * per_sm));
+    gather_columns_kernel<<<(int)grid, 256, 0, st>>>(p);
+    note_launch();
+    return cudaGetLastError();
 }
 
 }  // namespace ral

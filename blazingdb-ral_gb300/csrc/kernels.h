@@ -19,6 +19,34 @@ cudaError_t launch_gather(int width, const void* in, const uint32_t* in_valid, i
                           int idx_width, int64_t n_out, void* out, uint32_t* out_valid, unsigned long long* valid_count,
                           cudaStream_t st);
 
+// ---- many columns gathered by one index column (joins, order-by) ----------------------------
+
+constexpr int kMaxGatherColumns = 64;
+
+struct GatherColumn {
+    const void* in;            // n_in elements of `width` bytes
+    const uint32_t* in_valid;  // optional
+    void* out;                 // n_out elements
+    uint32_t* out_valid;       // optional: bit i = in bit idx[i] (0 outside [0, n_in); 1 if in_valid is null)
+    int32_t width;             // 1, 2, 4 or 8
+    int32_t pad;
+};
+
+struct GatherColumnsParams {
+    GatherColumn col[kMaxGatherColumns];
+    const void* idx;
+    int64_t n_in;
+    int64_t n_out;
+    unsigned long long* valid_counts;  // one counter per column with out_valid (zeroed), or null
+    int32_t num_columns;
+    int32_t idx_width;  // 1, 2, 4 or 8
+};
+
+// out_c[i] = in_c[idx[i]] for every column c, reading each index once; other indices leave
+// out_c[i] untouched.  Output validity words are built by ballot, 32 rows at a time, and their
+// set bits counted into valid_counts[c].
+cudaError_t launch_gather_columns(const GatherColumnsParams& p, cudaStream_t st);
+
 }  // namespace ral
 
 namespace ral {

@@ -9,17 +9,19 @@ library is missing the import of the first entry point raises.
 """
 from .capi import (RalError, lib, perform_operation, perform_operation_async, perform_operation_host, evaluate_expression,
                    process_filter, execute_project_plan, filter_project, project_output_types,
-                   materialize_column, apply_boolean_mask, add_expression_to_plan, get_output_type_expression,
+                   materialize_column, materialize_columns, apply_boolean_mask, add_expression_to_plan,
+                   get_output_type_expression,
                    debug_program_source, debug_filter_source, jit_stats, kernel_launches, version,
                    parse_project_plan, Batch, autotune_program, batch_tune_key, Server, softfp_selftest,
-                   debug_lookback_timeout)
+                   debug_lookback_timeout, process_aggregate, debug_aggregate_source)
 from .column import Column, Scalar, valid_alloc_size
 from . import dtypes
 
 __all__ = [
     "RalError", "lib", "perform_operation", "perform_operation_async", "perform_operation_host", "evaluate_expression",
     "process_filter", "execute_project_plan", "filter_project", "project_output_types",
-    "materialize_column", "apply_boolean_mask", "add_expression_to_plan", "get_output_type_expression",
+    "materialize_column", "materialize_columns", "apply_boolean_mask", "add_expression_to_plan", "get_output_type_expression",
     "debug_program_source", "debug_filter_source", "jit_stats", "kernel_launches", "version", "Column", "Scalar",
     "valid_alloc_size", "dtypes", "parse_project_plan", "Batch", "autotune_program", "batch_tune_key", "Server", "softfp_selftest", "debug_lookback_timeout",
+    "process_aggregate", "debug_aggregate_source",
 ]

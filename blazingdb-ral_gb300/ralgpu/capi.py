@@ -39,6 +39,7 @@ _SIGS = {
                                      C.POINTER(C.c_int32)]),
     "ral_apply_boolean_mask": (C.c_int, [C.POINTER(GdfColumn), C.POINTER(GdfColumn), C.POINTER(C.c_int32)]),
     "ral_materialize_column": (C.c_int, [C.POINTER(GdfColumn), C.POINTER(GdfColumn), C.POINTER(GdfColumn)]),
+    "ral_materialize_columns": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int32, C.POINTER(GdfColumn)]),
     "ral_add_expression_to_plan": (C.c_int, [C.c_char_p, C.c_int16, C.c_int16, C.c_int16, I16P, C.c_int32,
                                              I16P, I16P, I16P, I32P, I32P, SCP, SCP, I32P, C.c_int32]),
     "ral_get_output_type_expression": (C.c_int, [I32P, C.c_int32, C.c_char_p, I32P]),
@@ -48,6 +49,10 @@ _SIGS = {
     "ral_kernel_launches": (C.c_int64, []),
     "ral_debug_filter_source": (C.c_int, [I32P, I32P, C.c_int32, C.c_char_p, C.c_char_p, C.c_int32, C.c_char_p,
                                           C.c_int64, C.c_char_p, C.c_int64]),
+    "ral_debug_aggregate_source": (C.c_int, [I32P, I32P, C.c_void_p, C.c_int32, C.c_char_p, C.c_int32, C.c_char_p,
+                                             C.c_int64, C.c_char_p, C.c_int64]),
+    "ral_process_aggregate": (C.c_int, [C.c_void_p, C.c_int32, C.c_char_p, C.POINTER(GdfScalar), C.c_int32,
+                                        C.POINTER(C.c_int32)]),
     "ral_jit_stats": (C.c_int, [C.POINTER(C.c_int64), C.POINTER(C.c_int64), C.POINTER(C.c_int64),
                                 C.POINTER(C.c_double)]),
     "ral_parse_project_plan": (C.c_int, [I32P, C.c_int32, C.c_char_p, C.c_int32, C.c_int32, I32P, I32P, I32P, I32P,
@@ -325,6 +330,22 @@ def materialize_column(input_column: Column, row_indices: Column, with_valid: Op
     return out
 
 
+def materialize_columns(input_columns: List[Column], row_indices: Column,
+                        with_valid: Optional[Sequence[bool]] = None) -> List[Column]:
+    """Every column gathered by one index column in one kernel (the per-column materialize_column
+    loops of JoinOperator.cpp:130,135 and OrderBy.cpp:66)."""
+    n = row_indices.size
+    wv = [c.valid is not None for c in input_columns] if with_valid is None else list(with_valid)
+    outs = [Column.empty(c.dtype, n, with_valid=w) for c, w in zip(input_columns, wv)]
+    ia, _is = _colarray(input_columns)
+    oa, os_ = _colarray(outs)
+    rc = row_indices.to_c()
+    _check(lib().ral_materialize_columns(C.cast(ia, C.c_void_p), C.cast(oa, C.c_void_p), len(outs), C.byref(rc)))
+    for o, st in zip(outs, os_):
+        o.sync_from_c(st)
+    return outs
+
+
 def apply_boolean_mask(stencil: Column) -> Column:
     """Indices (INT32 column) of the rows whose stencil is valid and nonzero, in row order."""
     out = Column.empty(D.GDF_INT32, stencil.size, with_valid=False)
@@ -386,6 +407,31 @@ def debug_filter_source(frame_dtypes, frame_nullable, filter_query_part: str, pr
     _check(lib().ral_debug_filter_source(_p32(fd), _p32(fn), len(fd), filter_query_part.encode(),
                                          project_query_part.encode() if project_query_part else None,
                                          1 if compile else 0, src, len(src), log, len(log)))
+    return src.value.decode(), log.value.decode()
+
+
+def process_aggregate(frame: List[Column], query_part: str) -> List[Scalar]:
+    """process_aggregate without GROUP BY (src/operators/GroupBy.cpp:531-590): one Scalar per
+    aggregation, its expression inputs evaluated and reduced in one kernel."""
+    arr, _structs = _colarray(frame)
+    cap = 256
+    res = (GdfScalar * cap)()
+    n = C.c_int32(0)
+    _check(lib().ral_process_aggregate(C.cast(arr, C.c_void_p), len(frame), query_part.encode(), res, cap,
+                                       C.byref(n)))
+    return [Scalar.from_c(res[i]) for i in range(n.value)]
+
+
+def debug_aggregate_source(frame_dtypes, frame_nullable, frame_null_counts, query_part: str,
+                           compile: bool = False):
+    """Generated CUDA source (and NVRTC log when compile=True) of a LogicalAggregate's fused kernel;
+    needs no GPU."""
+    fd, fn = _i32(frame_dtypes), _i32(frame_nullable)
+    nc = np.ascontiguousarray(np.asarray(frame_null_counts, dtype=np.int64))
+    src = C.create_string_buffer(1 << 20)
+    log = C.create_string_buffer(1 << 16)
+    _check(lib().ral_debug_aggregate_source(_p32(fd), _p32(fn), nc.ctypes.data, len(fd), query_part.encode(),
+                                            1 if compile else 0, src, len(src), log, len(log)))
     return src.value.decode(), log.value.decode()
 
 

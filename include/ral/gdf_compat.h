@@ -155,6 +155,19 @@ typedef enum {
     BLZ_INVALID_UNARY
 } gdf_unary_operator;
 
+/* Aggregation operators (cudf's gdf_agg_op, the names src/operators/GroupBy.cpp and
+ * src/CalciteExpressionParsing.cpp:92-116,483-507 use; cudf is not vendored by the reference, so
+ * the values follow cudf's published order of that era). */
+typedef enum {
+    GDF_SUM = 0,
+    GDF_MIN,
+    GDF_MAX,
+    GDF_AVG,
+    GDF_COUNT,
+    GDF_COUNT_DISTINCT,
+    N_GDF_AGG_OPS
+} gdf_agg_op;
+
 /* Register index type and the two negative operand codes of the program. */
 typedef short column_index_type;
 #define SCALAR_INDEX ((column_index_type)-2)

@@ -11,6 +11,7 @@
 //                                 output columns passed explicitly)
 //   ral::execute_project_plan  <- src/CalciteInterpreter.h:61
 //   ral::materialize_column    <- src/ColumnManipulation.cuh:16-18
+//   ral::materialize_columns   <- the per-column materialize_column loops of joins and order-by
 //   ral::add_expression_to_plan<- src/LogicalFilter.h:26-42
 #ifndef RAL_HPP_
 #define RAL_HPP_
@@ -66,6 +67,14 @@ inline void execute_project_plan(const std::vector<gdf_column*>& frame, const st
 
 inline void materialize_column(gdf_column* input, gdf_column* output, gdf_column* row_indices) {
     check(ral_materialize_column(input, output, row_indices));
+}
+
+// Every column of a table gathered by one index column (the per-column loops of
+// JoinOperator.cpp:130,135 and OrderBy.cpp:66 in one call).
+inline void materialize_columns(const std::vector<gdf_column*>& inputs, const std::vector<gdf_column*>& outputs,
+                                gdf_column* row_indices) {
+    if (inputs.size() != outputs.size()) throw std::runtime_error("materialize_columns: inputs and outputs differ in count");
+    check(ral_materialize_columns(inputs.data(), outputs.data(), (int32_t)inputs.size(), row_indices));
 }
 
 inline void add_expression_to_plan(const std::string& expression, column_index_type expression_position,

@@ -165,6 +165,18 @@ int ral_filter_project(gdf_column *const *frame_columns, int32_t num_columns, co
 int ral_materialize_column(const gdf_column *input, gdf_column *output, const gdf_column *row_indices);
 
 /*
+ * materialize_column over many columns at once — the callers that gather every column of a table
+ * by the same index column: joins (src/operators/JoinOperator.cpp:130,135), order-by
+ * (src/operators/OrderBy.cpp:66) and the distribution primitives (src/distribution/primitives.cpp:
+ * 239,426,667) call materialize_column once per column.  Same per-column result as
+ * ral_materialize_column (including the recounted null_count and size of every output); the
+ * index column is read once for all columns, in one kernel.  All inputs must have the same size;
+ * 0 <= num_columns <= 64.
+ */
+int ral_materialize_columns(const gdf_column *const *inputs, gdf_column *const *outputs, int32_t num_columns,
+                            const gdf_column *row_indices);
+
+/*
  * apply_boolean_mask over the row-index column — src/CalciteInterpreter.cpp:531-543
  * (gdf_sequence iota + cudf::apply_boolean_mask).  Writes, in row order, the
  * indices of the rows whose stencil byte is nonzero and whose stencil validity
@@ -192,6 +204,24 @@ int ral_apply_boolean_mask(const gdf_column *stencil, gdf_column *out_indices, g
  */
 #define RAL_NOALLOC_MAX_ROWS ((int64_t)(256 * 1024 / 8 - 3) * 4096)
 int ral_apply_boolean_mask_noalloc(const gdf_column *stencil, gdf_column *out_indices, gdf_size_type *num_rows_out);
+
+/*
+ * process_aggregate without GROUP BY — src/operators/GroupBy.cpp:531-590 with compute_aggregations
+ * (:298-345) and aggregations_without_groupby (:231-296).  query_part is the LogicalAggregate
+ * ("LogicalAggregate(group=[{}], EXPR$0=[SUM(*($0, $1))], EXPR$1=[COUNT()], ...)"); each
+ * aggregation is SUM, MIN, MAX, AVG or COUNT of an expression over the frame or of a bare "$k".
+ * The reference evaluates every expression input into a full column and then reduces it; here all
+ * expression inputs run as one register program whose results are reduced in the same kernel, so
+ * no intermediate column is written.  results[i] receives aggregation i as the reference's one-row
+ * output column holds it (dtype by get_aggregation_output_type, CalciteExpressionParsing.cpp:92-116;
+ * is_valid false where the reference returns a null); *num_results the aggregation count.
+ * Results match the reference's flow: an evaluated input's nulls are not skipped (evaluate_expression
+ * leaves its null_count at 0), a bare input's are; COUNT() counts column 0's non-null rows.
+ * Float sums are deterministic on a given GPU but their rounding follows a tree order, not a
+ * sequential one.  A GROUP BY plan returns RAL_ERROR_UNSUPPORTED.  Synchronous.
+ */
+int ral_process_aggregate(gdf_column *const *frame_columns, int32_t num_columns, const char *query_part,
+                          gdf_scalar *results, int32_t capacity, int32_t *num_results);
 
 /*
  * add_expression_to_plan — src/LogicalFilter.h:26-42 (src/LogicalFilter.cpp:44-268).

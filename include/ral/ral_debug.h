@@ -40,6 +40,14 @@ int ral_debug_filter_source(const gdf_dtype *frame_dtypes, const int32_t *frame_
                             const char *filter_query_part, const char *project_query_part, int32_t compile,
                             char *source_out, int64_t source_capacity, char *log_out, int64_t log_capacity);
 
+/* Generated source of the fused aggregate kernel of a LogicalAggregate over a frame described by
+ * dtypes, mask presence and null counts (optionally NVRTC-compiled, no GPU needed); an empty
+ * source when the plan needs no kernel (COUNT only). */
+int ral_debug_aggregate_source(const gdf_dtype *frame_dtypes, const int32_t *frame_nullable,
+                               const int64_t *frame_null_counts, int32_t num_columns, const char *query_part,
+                               int32_t compile, char *source_out, int64_t source_capacity, char *log_out,
+                               int64_t log_capacity);
+
 /* Compiles every query's chunk function and links the dispatcher without loading it (no GPU
  * needed); the ptxas / link log goes to log_out. */
 int ral_server_debug_compile(ral_server *server, char *log_out, int64_t log_capacity);

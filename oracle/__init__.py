@@ -267,3 +267,68 @@ def execute_project_plan(frame: List[OColumn], query_part: str, **kw) -> List[OC
     for c in result:
         update_null_count(c)
     return result
+
+
+# ---- aggregations without GROUP BY (src/operators/GroupBy.cpp) -----------------------------------
+
+@dataclass
+class AggResult:
+    dtype: int
+    is_valid: bool
+    value: object = None        # int or float (the exactly rounded sum for a float SUM / AVG)
+    float_sum_bound: float = 0.0  # float SUM / AVG: sum of |x|, for the error bound of any order
+
+
+def process_aggregate(frame: List[OColumn], query_part: str, **kw) -> List[AggResult]:
+    """process_aggregate without GROUP BY, as the reference runs it (GroupBy.cpp:531-590,
+    compute_aggregations :298-345, aggregations_without_groupby :231-296): an input that contains
+    an evaluation is evaluated into a column of its own (evaluate_expression, which leaves the
+    column's null_count at 0, LogicalFilter.cpp:368); any other input is a frame column (get_index;
+    COUNT() reads column 0).  The reduction (cudf::reduce, not vendored) consults the mask only
+    when null_count > 0; SUM widens to INT64 / FLOAT64, MIN / MAX keep the input type with the
+    numeric_limits max / lowest identities, AVG divides the sum by size - null_count, COUNT is
+    size - null_count; an empty or all-null input gives a null (invalid) scalar.  A float SUM has
+    no defined order in the reference: its value here is the exactly rounded sum (math.fsum)."""
+    import math
+    groups, aggs = fe.parse_aggregate(query_part)
+    if groups:
+        raise OracleError("GROUP BY aggregations are not restated")
+    n = frame[0].size
+    dtypes = [c.dtype for c in frame]
+    out = []
+    for name, op, expr in aggs:
+        if fe.contains_evaluation(expr):
+            t = fe.get_output_type_expression(dtypes, expr)
+            col = evaluate_expression(frame, expr, alloc_column(t, n), **kw)
+            col.null_count = 0
+        else:
+            col = frame[fe.get_index(expr)]
+        out_t = fe.get_aggregation_output_type(col.dtype, op)
+        count = col.size - col.null_count
+        if op == fe.GDF_COUNT:
+            out.append(AggResult(out_t, True, int(count)))
+            continue
+        if col.size == 0 or col.size <= col.null_count:
+            out.append(AggResult(out_t, False))
+            continue
+        vals = col.data[col.valid_bools()] if (col.valid is not None and col.null_count > 0) else col.data
+        flt = fe.is_type_float(col.dtype)
+        if op in (fe.GDF_SUM, fe.GDF_AVG):
+            if flt:
+                v64 = vals.astype(np.float64)
+                s = math.fsum(v64.tolist())
+                bound = float(np.abs(v64).sum())
+            else:
+                s = int(vals.astype(np.int64).astype(np.uint64).sum(dtype=np.uint64).astype(np.int64))
+                bound = 0.0
+            if op == fe.GDF_SUM:
+                out.append(AggResult(out_t, True, s, bound))
+            else:
+                out.append(AggResult(fe.GDF_FLOAT64, True, float(s) / float(count), bound / float(count)))
+            continue
+        info = np.finfo(vals.dtype) if flt else np.iinfo(vals.dtype)
+        ident = info.max if op == fe.GDF_MIN else (info.min if not flt else -info.max)
+        m = vals.min() if op == fe.GDF_MIN else vals.max()
+        m = min(m, ident) if op == fe.GDF_MIN else max(m, ident)
+        out.append(AggResult(out_t, True, float(m) if flt else int(m)))
+    return out

@@ -559,6 +559,59 @@ def parse_project_plan(frame_dtypes: Sequence[int], query_part: str) -> ProjectP
     return ProjectPlan(plan, cols, out_types, columns, names)
 
 
+GDF_SUM, GDF_MIN, GDF_MAX, GDF_AVG, GDF_COUNT, GDF_COUNT_DISTINCT = range(6)
+AGG_OPS = {"SUM": GDF_SUM, "MIN": GDF_MIN, "MAX": GDF_MAX, "AVG": GDF_AVG, "COUNT": GDF_COUNT,
+           "COUNT_DISTINCT": GDF_COUNT_DISTINCT}
+
+
+def get_string_between_outer_parentheses(s: str) -> str:
+    """src/CalciteExpressionParsing.cpp:756-767."""
+    a, b = s.find("("), s.rfind(")")
+    if a < 0 or b < 0 or b < a:
+        return ""
+    return s[a + 1:b]
+
+
+def get_aggregation_operation(expression: str) -> int:
+    """src/CalciteExpressionParsing.cpp:483-507: the text between "=[" and the first "]", up to "("."""
+    start = expression.find("=[") + 2
+    end = expression.find("]")
+    op = expression[start:] if end < 0 else expression[start:end]
+    op = op[:op.find("(")] if "(" in op else op
+    if op not in AGG_OPS:
+        raise ValueError("aggregation type not supported: " + op)
+    return AGG_OPS[op]
+
+
+def parse_aggregate(query_part: str):
+    """process_aggregate's parse, src/operators/GroupBy.cpp:531-569: the GROUP BY columns and, per
+    aggregation, (name, gdf_agg_op, input expression text).  The combined expression drops the
+    character before the last ')' (the closing ']'), as the reference's substr does."""
+    a = query_part.find("(")
+    combined = query_part[a + 1:a + 1 + (query_part.rfind(")") - a - 1) - 1]
+    groups: List[int] = []
+    aggs = []
+    for e in get_expressions_from_expression_list(combined):
+        e = re.sub(r"^ +| +$|( ) +", r"\1", e)
+        if "group=" in e:
+            body = e[e.find("{") + 1:e.find("}")]
+            groups = [int(x) for x in body.replace(" ", "").split(",") if x != ""]
+            continue
+        aggs.append((e[:e.find("=[")], get_aggregation_operation(e), get_string_between_outer_parentheses(e)))
+    return groups, aggs
+
+
+def get_aggregation_output_type(t: int, op: int) -> int:
+    """src/CalciteExpressionParsing.cpp:92-116, without a GROUP BY."""
+    if op in (GDF_COUNT, GDF_COUNT_DISTINCT):
+        return GDF_INT64
+    if op == GDF_SUM:
+        return GDF_FLOAT64 if is_type_float(t) else GDF_INT64
+    if op in (GDF_MIN, GDF_MAX):
+        return t
+    return GDF_FLOAT64
+
+
 def get_named_expression(query_part: str, name: str) -> str:
     if query_part.find(name + "=[") < 0:
         return ""

@@ -179,3 +179,21 @@ PROJECT_KATS = [
     ("LogicalProject(EXPR$0=[CASE(IS NOT NULL($0), $0, -1)])",     # interops_coalesce_test.cu:36
      [([-1, 2, 3, 4, -1, -1, -1, -1, 9, 1], [1] * 10)]),
 ]
+
+# tests/integration/aggregation-without-group-by/test-aggregation-without-group-by.cpp: main.part
+# with p_partkey = 1..200 (INT32, no nulls).  TEST_01 (:66-118) aggregates the table; TEST_03
+# (:121-177) aggregates it behind LogicalFilter(<($0, 0)), i.e. over zero rows: COUNT is a valid 0,
+# the others are null (valid_result {1, 0, 0, 0, 0}).  Values are compared, as the test's
+# CHECK_RESULT compares printed values (MIN / MAX keep the INT32 input type,
+# CalciteExpressionParsing.cpp:103-106).
+PARTKEY = [(INT32, list(range(1, 201)), None)]
+AGG_QUERY = ("LogicalAggregate(group=[{}], EXPR$0=[COUNT()], EXPR$1=[SUM($0)], EXPR$2=[AVG($0)], "
+             "EXPR$3=[MAX($0)], EXPR$4=[MIN($0)])")
+AGG_KATS = [
+    {"name": "TEST_01", "filter": None,
+     "expected": [(INT64, True, 200), (INT64, True, 20100), (FLOAT64, True, 100.5), (INT32, True, 200),
+                  (INT32, True, 1)]},
+    {"name": "TEST_03", "filter": "LogicalFilter(condition=[<($0, 0)])",
+     "expected": [(INT64, True, 0), (INT64, False, None), (FLOAT64, False, None), (INT32, False, None),
+                  (INT32, False, None)]},
+]

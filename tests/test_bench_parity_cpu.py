@@ -108,3 +108,19 @@ def test_reference_arm_prints_the_same_config():
     b = bench.workload_config("filter_gather", 500_000_000, 0.5, 1)
     assert a == b and a["parallelism"] == "replicas x1"
     assert bench.workload_config("fused_project", 200_000_000, 0.5)["rows"] == 200_000_000
+
+
+def test_chunked_gather_parity(small_chunks):
+    rng = np.random.default_rng(2)
+    n = 3 * 4096 + 5
+    frame = [O.make_column(v, t, m) for t, v, m in W.filter_gather_host(n, seed=3, null_rate=0.1)]
+    idx = rng.permutation(n).astype(np.int32)
+    outs = [O.materialize_column(c, idx) for c in frame]
+    dev_outs = [_dev(c) for c in outs]
+    ctx = {"cols": [_dev(c) for c in frame], "outs": dev_outs, "out_structs": _structs(dev_outs),
+           "idx": R.Column(torch.from_numpy(idx), None, 3, size=n)}
+    res = bench.gather_parity(ctx)
+    assert res["mismatches"] == 0, res
+    ctx["outs"][3].data[n - 2] += 1.0
+    exp = int(outs[3].valid_bools()[n - 2]) if outs[3].valid is not None else 1
+    assert bench.gather_parity(ctx)["detail"]["data"] == exp

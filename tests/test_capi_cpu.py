@@ -77,3 +77,34 @@ def test_host_buffer_evaluation_checks_arguments_before_any_cuda_call():
         c.null_count = 5
     ralgpu.perform_operation_host(eouts, empty, *args)
     assert all(c.null_count == 0 for c in eouts)
+
+
+def test_materialize_columns_checks_arguments_before_any_cuda_call():
+    """ral_materialize_columns rejects more than 64 columns, a floating-point index column, width
+    mismatches and inputs of different sizes on the host; no columns is a no-op."""
+    import numpy as np
+    from ralgpu import dtypes as D
+    from ralgpu.column import GdfColumn
+    L = ralgpu.lib()
+    keep = []
+
+    def mk(t, n):
+        c = ralgpu.Column.from_numpy(np.zeros(n, dtype=D.NP[t]), t, None, device="cpu")
+        keep.append(c)
+        return c.to_c()
+
+    def call(ins, outs, idx):
+        ia = (ctypes.POINTER(GdfColumn) * max(1, len(ins)))(*[ctypes.pointer(x) for x in ins])
+        oa = (ctypes.POINTER(GdfColumn) * max(1, len(outs)))(*[ctypes.pointer(x) for x in outs])
+        keep.extend([ia, oa])
+        return L.ral_materialize_columns(ctypes.cast(ia, ctypes.c_void_p), ctypes.cast(oa, ctypes.c_void_p),
+                                         len(ins), ctypes.byref(idx))
+
+    idx = mk(D.GDF_INT32, 4)
+    cols = [mk(D.GDF_INT32, 8) for _ in range(65)]
+    assert call(cols, cols, idx) == 1 and b"columns" in L.ral_last_error()
+    assert call(cols[:1], cols[:1], mk(D.GDF_FLOAT32, 4)) == 1 and b"row_indices" in L.ral_last_error()
+    assert call([mk(D.GDF_INT32, 8), mk(D.GDF_INT64, 9)], [mk(D.GDF_INT32, 4), mk(D.GDF_INT64, 4)], idx) == 1
+    assert b"differ in size" in L.ral_last_error()
+    assert call([mk(D.GDF_INT32, 8)], [mk(D.GDF_INT64, 8)], idx) == 1 and b"width mismatch" in L.ral_last_error()
+    assert call([], [], idx) == 0

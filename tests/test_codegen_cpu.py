@@ -156,3 +156,38 @@ def test_default_shapes_keep_their_occupancy():
                                           W.FILTER_PROJECT_PROJECT, compile=True)
     assert "__launch_bounds__(RAL_THREADS, 5)" in src
     assert spills(log) == 0 and _registers(log) <= 51, log
+
+
+AGG_DTYPES = [4, 4, 6, 6, 3, 5, 1, 2]   # int64, int64, float64, float64, int32, float32, int8, int16
+
+
+@pytest.mark.parametrize("q", range(3))
+def test_aggregate_kernels_compile_for_sm103a(q):
+    """The fused aggregate kernels of the GPU test plans compile with NVRTC (no GPU needed)."""
+    from test_gpu_aggregate import QUERIES
+    src, log = ralgpu.debug_aggregate_source(AGG_DTYPES, [1, 1, 1, 1, 1, 0, 1, 0], [5, 5, 5, 5, 5, 0, 9, 0],
+                                             QUERIES[q], compile=True)
+    assert "ral_agg_" in src
+    assert "error" not in log.lower()
+
+
+def test_aggregate_count_only_needs_no_kernel_and_group_by_is_rejected():
+    src, _ = ralgpu.debug_aggregate_source([3], [1], [2], "LogicalAggregate(group=[{}], EXPR$0=[COUNT()])")
+    assert src == ""
+    with pytest.raises(ralgpu.RalError, match="GROUP BY"):
+        ralgpu.debug_aggregate_source([3, 4], [0, 0], [0, 0],
+                                      "LogicalAggregate(group=[{0}], EXPR$0=[SUM($1)])")
+    with pytest.raises(ralgpu.RalError):
+        ralgpu.debug_aggregate_source([3], [0], [0], "LogicalAggregate(group=[{}], EXPR$0=[STDDEV($0)])")
+
+
+def test_aggregate_plan_matches_the_oracle_parse():
+    """Library and oracle split a LogicalAggregate the same way (names, operators, inputs)."""
+    from oracle import frontend as fe
+    q = ("LogicalAggregate(group=[{}], EXPR$0=[COUNT()], s=[SUM(*($0, -(1, $1)))], EXPR$2=[AVG($1)], "
+         "m=[MIN(CAST($0):DOUBLE)], x=[MAX(+($0, 1))])")
+    groups, aggs = fe.parse_aggregate(q)
+    assert groups == [] and [a[1] for a in aggs] == [fe.GDF_COUNT, fe.GDF_SUM, fe.GDF_AVG, fe.GDF_MIN, fe.GDF_MAX]
+    src, _ = ralgpu.debug_aggregate_source([4, 6], [0, 0], [0, 0], q, compile=False)
+    # SUM, AVG, MIN and MAX each fold one slot; COUNT() needs none
+    assert src.count("acc3 =") >= 1 and "acc4" not in src

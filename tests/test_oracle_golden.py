@@ -95,3 +95,17 @@ def test_project_kats(query, expected):
         np.testing.assert_array_equal(vb, np.asarray(valids, dtype=bool))
         np.testing.assert_array_equal(col.data[vb], np.asarray(vals, dtype=col.data.dtype)[vb])
         assert col.null_count == int((~vb).sum())
+
+
+@pytest.mark.parametrize("kat", K.AGG_KATS, ids=lambda k: k["name"])
+def test_oracle_aggregation_without_group_by(kat):
+    """The oracle's process_aggregate against the reference's aggregation known-answer tests."""
+    frame = [O.make_column(v, t, m) for t, v, m in K.PARTKEY]
+    if kat["filter"]:
+        frame = O.process_filter(frame, kat["filter"])
+    got = O.process_aggregate(frame, K.AGG_QUERY)
+    assert len(got) == len(kat["expected"])
+    for g, (t, valid, value) in zip(got, kat["expected"]):
+        assert g.dtype == t and g.is_valid == valid
+        if valid:
+            assert g.value == value

@@ -75,7 +75,7 @@ def test_noalloc_makes_no_device_allocation():
     rt = _cudart()
     pool = ctypes.c_void_p()
     assert rt.cudaDeviceGetDefaultMemPool(ctypes.byref(pool), torch.cuda.current_device()) == 0
-    USED_HIGH = 8                           # cudaMemPoolAttrUsedMemHigh
+    USED_CURRENT, USED_HIGH = 7, 8          # cudaMemPoolAttrUsedMemCurrent / UsedMemHigh
     rng = np.random.default_rng(5)
     n = 2_000_003
     col = R.Column.from_numpy((rng.random(n) < 0.5).astype(np.int8), D.GDF_INT8, rng.random(n) >= 0.1)
@@ -85,8 +85,11 @@ def test_noalloc_makes_no_device_allocation():
     out0 = R.Column.empty(D.GDF_INT32, 0, with_valid=False)
     _noalloc(col, out)                      # warm: module loaded, kernel resolved
     torch.cuda.synchronize()
+    # resetting the high-water mark sets it to the pool memory in use now (other callers' blocks)
     zero = ctypes.c_uint64(0)
     assert rt.cudaMemPoolSetAttribute(pool, USED_HIGH, ctypes.byref(zero)) == 0
+    used0 = ctypes.c_uint64(0)
+    assert rt.cudaMemPoolGetAttribute(pool, USED_CURRENT, ctypes.byref(used0)) == 0
     free0, _ = torch.cuda.mem_get_info()
     got = _noalloc(col, out)
     assert _noalloc(empty, out0).size == 0
@@ -94,7 +97,7 @@ def test_noalloc_makes_no_device_allocation():
     free1, _ = torch.cuda.mem_get_info()
     high = ctypes.c_uint64(1)
     assert rt.cudaMemPoolGetAttribute(pool, USED_HIGH, ctypes.byref(high)) == 0
-    assert high.value == 0, "the call allocated from the default memory pool"
+    assert high.value <= used0.value, "the call allocated from the default memory pool"
     assert free1 == free0, "device free memory changed across the call"
     assert got.size == R.apply_boolean_mask(col).size
 
