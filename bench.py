@@ -842,6 +842,15 @@ def measure_workload(args, workload, n, selectivity, device, world, sampler, e2e
     }
     if "nout" in ctx:
         out["rows_out"] = ctx["nout"].value
+    if workload == "plain_vm":
+        # where a small synchronous call's time goes: the same calls again with the library's
+        # per-call timing on (host preparation, enqueue, wait, kernel device time)
+        R.call_timing(enable=True, reset=True)
+        for _ in range(max(20, args.steps)):
+            ctx["step"](stream)
+        torch.cuda.synchronize()
+        out["per_call_breakdown_us"] = R.call_timing(enable=False, reset=True)
+        out["per_call_breakdown_us"]["call_us"] = ms_per_step * 1e3
     if workload == "gather":
         # the same gather as one ral_materialize_column call per column (the reference's loop shape)
         for _ in range(2):

@@ -401,6 +401,10 @@ int ral_debug_aggregate_source(const gdf_dtype* frame_dtypes, const int32_t* fra
     });
 }
 
+int ral_debug_call_timing(int32_t enable, int32_t reset, int64_t* calls, double* us4) {
+    return call_timing_query(enable != 0, reset != 0, calls, us4);
+}
+
 int ral_apply_boolean_mask(const gdf_column* stencil, gdf_column* out_indices, gdf_size_type* num_rows_out) {
     return guarded([&] {
         if (!stencil || !out_indices || !num_rows_out) return set_error(kInvalidArgument, "null argument");

@@ -9,6 +9,7 @@
 
 #include <algorithm>
 #include <atomic>
+#include <chrono>
 #include <cstdlib>
 #include <cstring>
 #include <map>
@@ -156,6 +157,62 @@ const GeneratedKernel& generated_eval(const Program& p, const Shape& s) {
 }
 
 }  // namespace
+
+namespace {
+std::atomic<int> g_timing{-1};  // -1: not read from the environment yet
+std::atomic<int64_t> g_t_calls{0}, g_t_prep{0}, g_t_enq{0}, g_t_wait{0}, g_t_dev{0};  // nanoseconds
+thread_local std::chrono::steady_clock::time_point t_start, t_prepared;
+}  // namespace
+
+bool call_timing_enabled() {
+    int v = g_timing.load(std::memory_order_relaxed);
+    if (v < 0) {
+        const char* e = std::getenv("RAL_CALL_TIMING");
+        v = (e && e[0] == '1') ? 1 : 0;
+        int expect = -1;
+        g_timing.compare_exchange_strong(expect, v);
+        v = g_timing.load();
+    }
+    return v == 1;
+}
+
+void call_timing_start() {
+    if (call_timing_enabled()) t_start = t_prepared = std::chrono::steady_clock::now();
+}
+
+void call_timing_mark_prepared() {
+    if (call_timing_enabled()) t_prepared = std::chrono::steady_clock::now();
+}
+
+void call_timing_add(double enqueue_us, double wait_us, double device_us) {
+    if (!call_timing_enabled()) return;
+    const double prep = std::chrono::duration<double, std::micro>(t_prepared - t_start).count();
+    g_t_calls.fetch_add(1);
+    g_t_prep.fetch_add((int64_t)(prep * 1e3));
+    g_t_enq.fetch_add((int64_t)(enqueue_us * 1e3));
+    g_t_wait.fetch_add((int64_t)(wait_us * 1e3));
+    g_t_dev.fetch_add((int64_t)(device_us * 1e3));
+}
+
+int call_timing_query(bool enable, bool reset, int64_t* calls, double* us4) {
+    g_timing.store(enable ? 1 : 0);
+    if (calls) *calls = g_t_calls.load();
+    if (us4) {
+        const double c = std::max<int64_t>(1, g_t_calls.load());
+        us4[0] = g_t_prep.load() / 1e3 / c;
+        us4[1] = g_t_enq.load() / 1e3 / c;
+        us4[2] = g_t_wait.load() / 1e3 / c;
+        us4[3] = g_t_dev.load() / 1e3 / c;
+    }
+    if (reset) {
+        g_t_calls = 0;
+        g_t_prep = 0;
+        g_t_enq = 0;
+        g_t_wait = 0;
+        g_t_dev = 0;
+    }
+    return kSuccess;
+}
 
 int launch_blocks(const CompiledKernel& k, int threads, int64_t rows_per_block, int64_t rows) {
     const int sms = device_sms();

@@ -86,6 +86,17 @@ int launch_blocks(const CompiledKernel& k, int threads, int64_t work_items_per_b
 // Parameter block filled in ParamLayout order.
 void fill_scalars(const Program& p, const ParamLayout& L, std::vector<uint64_t>& slots);
 
+// ---- per-call timing of the synchronous filter entry points ----------------------------------
+// Off unless enabled (RAL_CALL_TIMING=1 or ral_debug_call_timing): each call adds its host
+// preparation (entry to the first enqueue), its enqueue (memsets, launch, copy back), its wait
+// for completion and the device time of its kernel (CUDA events around the launch), in
+// microseconds.
+bool call_timing_enabled();
+void call_timing_start();                       // at the entry point
+void call_timing_mark_prepared();               // before the first enqueue
+void call_timing_add(double enqueue_us, double wait_us, double device_us);  // after the sync
+int call_timing_query(bool enable, bool reset, int64_t* calls, double* us4);
+
 // process_aggregate without GROUP BY, expressions fused with the reduction (aggregate.cpp).
 int process_aggregate(gdf_column* const* frame, int n_cols, const char* query, gdf_scalar* results, int capacity,
                       int* num_results, cudaStream_t st);

@@ -7,6 +7,7 @@
 #include "filter.h"
 
 #include <algorithm>
+#include <chrono>
 #include <cstdlib>
 #include <mutex>
 #include <sstream>
@@ -372,6 +373,9 @@ int run_prepared(const PreparedFilter& pf, gdf_column* const* frame, gdf_column*
     const int64_t header = filter_scratch_header(NO);
     void* scratch = nullptr;
     if (int e = scratch_get((size_t)(header + ntiles) * 8, st, &scratch)) return e;
+    const bool timing = call_timing_enabled();
+    call_timing_mark_prepared();
+    const auto t_enq0 = std::chrono::steady_clock::now();
     cudaMemsetAsync(scratch, 0, (size_t)(header + ntiles) * 8, st);
     // output masks are assembled with OR at the edges of each warp's range: start from zero
     for (int q = 0; q < NO; q++)
@@ -397,16 +401,31 @@ int run_prepared(const PreparedFilter& pf, gdf_column* const* frame, gdf_column*
     }
     const int grid = launch_blocks(*pf.k, pf.gk.shape.threads, tile_rows * (pf.gk.shape.threads / 32), n);
     void* args[] = {slots.data()};
+    thread_local cudaEvent_t ev[2] = {nullptr, nullptr};
+    if (timing && !ev[0]) {
+        cudaEventCreate(&ev[0]);
+        cudaEventCreate(&ev[1]);
+    }
+    if (timing) cudaEventRecord(ev[0], st);
     if (int e = check_cuda(cudaLaunchKernel((const void*)pf.k->kernel, dim3(grid), dim3(pf.gk.shape.threads), args, 0, st),
                            "launch of the filter kernel"))
         return e;
+    if (timing) cudaEventRecord(ev[1], st);
     note_launch();
     unsigned long long h[64];
     std::vector<unsigned long long> hv;
     unsigned long long* hp = h;
     if (header > 64) { hv.resize(header); hp = hv.data(); }
     cudaMemcpyAsync(hp, scratch, (size_t)header * 8, cudaMemcpyDeviceToHost, st);
+    const auto t_wait0 = std::chrono::steady_clock::now();
     if (int e = check_cuda(cudaStreamSynchronize(st), "filter kernel")) return e;
+    if (timing) {
+        const auto t_end = std::chrono::steady_clock::now();
+        float dev_ms = 0.f;
+        cudaEventElapsedTime(&dev_ms, ev[0], ev[1]);
+        call_timing_add(std::chrono::duration<double, std::micro>(t_wait0 - t_enq0).count(),
+                        std::chrono::duration<double, std::micro>(t_end - t_wait0).count(), dev_ms * 1e3);
+    }
     if (hp[1]) return set_error(kTimeout, "filter look-back wait gave up");
     const int64_t n_out = (int64_t)hp[2];
     for (int q = 0; q < NO; q++) {
@@ -548,6 +567,7 @@ int debug_filter_source(gdf_column* const* frame, int ncols, const char* filter_
 
 int process_filter(gdf_column* const* frame, int ncols, const char* query_part, gdf_column* const* outs,
                    gdf_size_type* n_out, const FilterOptions& opt) {
+    call_timing_start();
     if (!frame || ncols <= 0 || !query_part || !outs || !n_out) return set_error(kInvalidArgument, "null argument");
     if (int e = check_outputs(frame, ncols, outs)) return e;
     const std::string cond = named_expression(query_part, "condition");
@@ -645,6 +665,7 @@ void filter_fill_slots(const FilterPlan& plan, const GeneratedKernel& gk, gdf_co
 
 int filter_project(gdf_column* const* frame, int ncols, const char* filter_q, const char* project_q,
                    gdf_column* const* outs, int n_outs, gdf_size_type* n_out, const FilterOptions& opt) {
+    call_timing_start();
     if (!frame || ncols <= 0 || !filter_q || !project_q || !outs || !n_out)
         return set_error(kInvalidArgument, "null argument");
     for (int c = 0; c < ncols; c++) {

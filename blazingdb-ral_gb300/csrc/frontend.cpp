@@ -20,6 +20,9 @@
 #include <cstring>
 #include <map>
 #include <regex>
+#include <sstream>
+#include <iomanip>
+#include <ctime>
 
 namespace ral {
 
@@ -119,6 +122,22 @@ bool is_date_literal(const std::string& s) {
     static const std::regex re{R"([12]\d{3}-(0[1-9]|1[0-2])-(0[1-9]|[12]\d|3[01]))"};
     return std::regex_match(s, re);
 }
+bool is_time_of_day(const std::string& s) {
+    static const std::regex re{R"(([01]\d|2[0-3]):[0-5]\d:[0-5]\d)"};
+    return std::regex_match(s, re);
+}
+
+// get_date_64_from_string (CalciteExpressionParsing.cpp:293-305): "%Y-%m-%d %H:%M:%S" read into a
+// zeroed std::tm (so tm_isdst = 0) and converted by mktime, i.e. in the process's local time zone,
+// then to milliseconds.  A date without a time of day is taken at 00:00:00 (the reference's
+// format would reject it).
+int64_t date64_from_string(const std::string& t) {
+    std::tm tm = {};
+    std::istringstream ss(t.size() == 10 ? t + " 00:00:00" : t);
+    if (!(ss >> std::get_time(&tm, "%Y-%m-%d %H:%M:%S"))) throw ParseError("Invalid datetime format: " + t);
+    const int64_t secs = (int64_t)std::mktime(&tm);
+    return secs * 1000;
+}
 
 struct Parser {
     const std::string& s;
@@ -166,6 +185,12 @@ struct Parser {
             return e;
         }
         if (word.empty()) throw ParseError("empty operand");
+        // a TIMESTAMP literal "YYYY-MM-DD HH:MM:SS": the time part after the space is part of it
+        if (is_date_literal(word) && i + 9 <= s.size() && s[i] == ' ' && is_time_of_day(s.substr(i + 1, 8)) &&
+            (i + 9 == s.size() || delim(s[i + 9]))) {
+            word += s.substr(i, 9);
+            i += 9;
+        }
         e->kind = Expr::Literal;
         e->text = word;
         return e;
@@ -209,9 +234,12 @@ gdf_scalar literal_scalar(const std::string& t) {
     gdf_scalar s;
     std::memset(&s, 0, sizeof s);
     s.is_valid = true;
-    if (is_date_literal(t))
-        throw ParseError("date literal " + t + ": the reference parses dates as '%Y-%m-%d %H:%M:%S', "
-                         "which tokenisation never delivers");
+    if (is_date_literal(t.substr(0, 10)) && (t.size() == 10 || (t.size() == 19 && is_time_of_day(t.substr(11))))) {
+        // get_type_from_string: neither an integer nor a float -> GDF_DATE64
+        s.dtype = GDF_DATE64;
+        s.data.dt64 = date64_from_string(t);
+        return s;
+    }
     if (!is_number_literal(t)) throw ParseError("unsupported token: " + t);
     if (is_int_literal(t)) {
         errno = 0;

@@ -53,6 +53,7 @@ _SIGS = {
                                              C.c_int64, C.c_char_p, C.c_int64]),
     "ral_process_aggregate": (C.c_int, [C.c_void_p, C.c_int32, C.c_char_p, C.POINTER(GdfScalar), C.c_int32,
                                         C.POINTER(C.c_int32)]),
+    "ral_debug_call_timing": (C.c_int, [C.c_int32, C.c_int32, C.POINTER(C.c_int64), C.POINTER(C.c_double)]),
     "ral_jit_stats": (C.c_int, [C.POINTER(C.c_int64), C.POINTER(C.c_int64), C.POINTER(C.c_int64),
                                 C.POINTER(C.c_double)]),
     "ral_parse_project_plan": (C.c_int, [I32P, C.c_int32, C.c_char_p, C.c_int32, C.c_int32, I32P, I32P, I32P, I32P,
@@ -433,6 +434,16 @@ def debug_aggregate_source(frame_dtypes, frame_nullable, frame_null_counts, quer
     _check(lib().ral_debug_aggregate_source(_p32(fd), _p32(fn), nc.ctypes.data, len(fd), query_part.encode(),
                                             1 if compile else 0, src, len(src), log, len(log)))
     return src.value.decode(), log.value.decode()
+
+
+def call_timing(enable: bool = True, reset: bool = False) -> dict:
+    """Mean per-call breakdown (microseconds) of the synchronous filter entry points since the last
+    reset: host preparation, enqueue, wait for completion and kernel device time."""
+    calls = C.c_int64(0)
+    us = (C.c_double * 4)()
+    _check(lib().ral_debug_call_timing(1 if enable else 0, 1 if reset else 0, C.byref(calls), us))
+    return {"calls": calls.value, "host_prepare_us": us[0], "enqueue_us": us[1], "wait_us": us[2],
+            "kernel_device_us": us[3]}
 
 
 def kernel_launches() -> int:

@@ -48,6 +48,12 @@ int ral_debug_aggregate_source(const gdf_dtype *frame_dtypes, const int32_t *fra
                                int32_t compile, char *source_out, int64_t source_capacity, char *log_out,
                                int64_t log_capacity);
 
+/* Per-call timing of the synchronous filter entry points (ral_process_filter, ral_filter_project):
+ * enable != 0 turns it on (also RAL_CALL_TIMING=1), reset != 0 clears it after reading.  *calls
+ * receives the calls timed and us4 their mean host preparation (entry to the first enqueue),
+ * enqueue, wait for completion and kernel device time, in microseconds. */
+int ral_debug_call_timing(int32_t enable, int32_t reset, int64_t *calls, double *us4);
+
 /* Compiles every query's chunk function and links the dispatcher without loading it (no GPU
  * needed); the ptxas / link log goes to log_out. */
 int ral_server_debug_compile(ral_server *server, char *log_out, int64_t log_capacity);

@@ -23,8 +23,10 @@ Reference files (paths relative to the reference project root):
 
 Where the reference silently emits a misaligned program (unary operator on a
 literal, literal-op-literal, unknown or `null` tokens, string literals) or
-throws (date literals, whose time part never survives tokenisation), this
-front end raises FrontendError; the library rejects the same inputs.
+throws, this front end raises FrontendError; the library rejects the same inputs.
+Date and timestamp literals, which the reference cannot run (its "%Y-%m-%d %H:%M:%S" parse rejects
+a bare date and its space split cuts a timestamp in two), are read as the DATE64 milliseconds that
+get_scalar_from_string intends, in both front ends.
 StringUtil::splitNotInQuotes (blazingdb-io, not in the reference tree) is
 taken to drop empty tokens, since is_operator_token would read past an empty
 string otherwise.
@@ -78,6 +80,8 @@ _COUNT_DISTINCT_RE = re.compile(r"COUNT\(DISTINCT (\W\(.+?\)|.+)\)", re.I)
 _INT_RE = re.compile(r"^[-+]?[0-9]+$")
 _FLOAT_RE = re.compile(r"^[-+]?[0-9]*\.?[0-9]+([eE][-+]?[0-9]+)?$")
 _DATE_RE = re.compile(r"[12]\d{3}-(0[1-9]|1[0-2])-(0[1-9]|[12]\d|3[01])")
+_TIME_RE = re.compile(r"([01]\d|2[0-3]):[0-5]\d:[0-5]\d")
+_DATETIME_RE = re.compile(r"([12]\d{3}-(?:0[1-9]|1[0-2])-(?:0[1-9]|[12]\d|3[01])) (([01]\d|2[0-3]):[0-5]\d:[0-5]\d)")
 
 
 def _quoted_vector(s: str) -> List[bool]:
@@ -224,7 +228,9 @@ def clean_calcite_expression(expression: str) -> str:
             out.append(" ")
         elif ch != "," and ch != ")":
             out.append(ch)
-    return "".join(out)
+    # a TIMESTAMP literal keeps its time part in the same token (the reference's space split would
+    # separate it; this restatement joins it with a "T", which get_scalar_from_string reads back)
+    return _DATETIME_RE.sub(r"\1T\2", "".join(out))
 
 
 def clean_project_expression(expression: str) -> str:
@@ -267,7 +273,12 @@ def is_number(s: str) -> bool:
 
 
 def is_date(s: str) -> bool:
-    return _DATE_RE.fullmatch(s) is not None
+    """is_date (CalciteExpressionParsing.cpp:272-276), also taking the joined "DATE" + "T" + "TIME"
+    token of a TIMESTAMP literal."""
+    if _DATE_RE.fullmatch(s) is not None:
+        return True
+    return len(s) == 19 and s[10] == "T" and _DATE_RE.fullmatch(s[:10]) is not None and \
+        _TIME_RE.fullmatch(s[11:]) is not None
 
 
 def is_operator_token(op: str) -> bool:
@@ -309,6 +320,14 @@ def get_scalar_from_string(s: str, dtype: int) -> Scalar:
         return Scalar(GDF_INT64, v)
     if dtype == GDF_FLOAT64:
         return Scalar(GDF_FLOAT64, float(s))
+    if dtype == GDF_DATE64 and is_date(s):
+        # get_date_64_from_string (:293-305): "%Y-%m-%d %H:%M:%S" into a zeroed std::tm (tm_isdst 0),
+        # mktime in the local time zone, milliseconds; a bare date is taken at 00:00:00
+        import time
+        d, t = (s[:10], s[11:]) if len(s) == 19 else (s, "00:00:00")
+        y, mo, da = (int(x) for x in d.split("-"))
+        h, mi, se = (int(x) for x in t.split(":"))
+        return Scalar(GDF_DATE64, int(time.mktime((y, mo, da, h, mi, se, 0, 0, 0))) * 1000)
     raise FrontendError("Invalid datetime format")
 
 

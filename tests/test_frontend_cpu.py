@@ -94,8 +94,30 @@ def test_multi_output_positions():
         same(expr, pos=k, nout=3, nin=3, remap=[0, 1, 2])
 
 
+@pytest.mark.parametrize("expr", [
+    ">($3, 1995-03-15)",
+    "<($3, 2019-01-01 00:00:00)",
+    "AND(>=($3, 1994-01-01), <($3, 1995-01-01 12:30:00))",
+    "+($3, 2000-02-29)",
+])
+def test_date_literals(expr):
+    """Date and timestamp literals become DATE64 scalars (milliseconds from mktime) in both front
+    ends, the time part staying with its date."""
+    same(expr)
+    g = ralgpu.add_expression_to_plan(expr, 0, 1, 4, [0, 1, 2, 3])
+    dates = [s for s in g["right_scalars"] if s.dtype == fe.GDF_DATE64]
+    assert dates and all(s.value % 1000 == 0 for s in dates)
+
+
+def test_date_literal_value():
+    import time
+    g = ralgpu.add_expression_to_plan("<($3, 2019-01-01 06:30:15)", 0, 1, 4, [0, 1, 2, 3])
+    want = int(time.mktime((2019, 1, 1, 6, 30, 15, 0, 0, 0))) * 1000
+    assert g["right_scalars"][0].value == want
+
+
 @pytest.mark.parametrize("expr", ["+(1, 2)", "SIN(2)", "LIKE($0, 'a%')", "=($0, 'abc')", "+($0, null)",
-                                  ">($3, 1995-03-15)", "+($0)", "*($0, $1, $2)"])
+                                  "+($0)", "*($0, $1, $2)", ">($3, 1995-13-40)"])
 def test_rejected(expr):
     with pytest.raises((RalError, fe.FrontendError)):
         fe_plan = oracle_plan(expr, 0, 1, 4, [0, 1, 2, 3])  # noqa: F841  (the oracle rejects too)
