@@ -191,6 +191,7 @@ int process_aggregate(gdf_column* const* frame, int n_cols, const char* query, g
     const int64_t n = frame[0]->size;
     for (int c = 1; c < n_cols; c++)
         if (frame[c]->size != n) return set_error(kInvalidArgument, "frame columns differ in size");
+    CategoryScope categories(frame, n_cols);
     AggregateBuild b;
     if (int rc = build_aggregate(b, dtypes, has_valid, nulls, query)) return rc;
     const int n_agg = (int)b.plan.aggregations.size();

@@ -121,6 +121,7 @@ int ral_evaluate_expression(gdf_column* const* frame, int32_t num_columns, const
     return guarded([&] {
         if (!frame || num_columns <= 0 || !expression || !output)
             return set_error(kInvalidArgument, "evaluate_expression: null argument");
+        CategoryScope categories(frame, num_columns);
         ExpressionPlan ep = plan_expression(expression, num_columns);
         cudaStream_t st = cudaStreamPerThread;
         if (ep.clone) {
@@ -194,6 +195,7 @@ int ral_project_output_types(const gdf_dtype* frame_dtypes, int32_t num_columns,
                              int32_t capacity) {
     return guarded([&] {
         std::vector<gdf_dtype> f(frame_dtypes, frame_dtypes + num_columns);
+        TypesOnlyScope types_only;
         ProjectPlan pp = plan_project(query_part, f);
         *num_projected = (int32_t)pp.columns.size();
         if ((int)pp.columns.size() > capacity) return set_error(kInvalidArgument, "capacity too small");
@@ -247,6 +249,7 @@ int ral_execute_project_plan(gdf_column* const* frame, int32_t num_columns, cons
     return guarded([&] {
         std::vector<gdf_dtype> f(num_columns);
         for (int c = 0; c < num_columns; c++) f[c] = frame[c]->dtype;
+        CategoryScope categories(frame, num_columns);
         ProjectPlan pp = plan_project(query_part, f);
         if ((int)pp.columns.size() != num_out_columns)
             return set_error(kInvalidArgument, "out_columns count differs from the projection's");

@@ -139,6 +139,7 @@ int gather_all(gdf_column* const* frame, int ncols, const int32_t* idx, int64_t 
     for (int c = 0; c < ncols; c++) {
         outs[c]->size = (gdf_size_type)n_out;
         outs[c]->null_count = outs[c]->valid ? (gdf_size_type)(n_out - (int64_t)h[c]) : 0;
+        if (frame[c]->dtype == GDF_STRING_CATEGORY) outs[c]->dtype_info.category = frame[c]->dtype_info.category;
     }
     return kSuccess;
 }
@@ -300,6 +301,8 @@ std::string frame_signature(gdf_column* const* frame, int ncols, gdf_column* con
         k += (char)('A' + (int)outs[q]->dtype);
         k += outs[q]->valid ? 'v' : '-';
     }
+    // string literals resolve to codes of the category columns' dictionaries
+    k += category_key(frame, ncols);
     return k;
 }
 
@@ -431,6 +434,9 @@ int run_prepared(const PreparedFilter& pf, gdf_column* const* frame, gdf_column*
     for (int q = 0; q < NO; q++) {
         outs[q]->size = (gdf_size_type)n_out;
         outs[q]->null_count = spec.outputs[q].has_valid ? (gdf_size_type)(n_out - (int64_t)hp[3 + q]) : 0;
+        // a gathered string-category column keeps its source's dictionary (codes unchanged)
+        if (!spec.outputs[q].from_project && frame[spec.outputs[q].index]->dtype == GDF_STRING_CATEGORY)
+            outs[q]->dtype_info.category = frame[spec.outputs[q].index]->dtype_info.category;
     }
     *n_out_p = (gdf_size_type)n_out;
     return kSuccess;
@@ -461,9 +467,10 @@ int prepared(const std::string& key0, bool aligned16, int64_t n, Build&& build, 
 std::mutex g_pp_mu;
 std::unordered_map<std::string, std::unique_ptr<ProjectPlan>> g_project_plans;
 
-const ProjectPlan& cached_project_plan(const char* project_q, const std::vector<gdf_dtype>& fd) {
+const ProjectPlan& cached_project_plan(const char* project_q, const std::vector<gdf_dtype>& fd,
+                                       const std::string& categories) {
     std::string key(project_q);
-    key += '|';
+    key += '|' + categories + '|';
     for (gdf_dtype t : fd) key += (char)('A' + (int)t);
     {
         std::lock_guard<std::mutex> lock(g_pp_mu);
@@ -572,6 +579,10 @@ int process_filter(gdf_column* const* frame, int ncols, const char* query_part, 
     if (int e = check_outputs(frame, ncols, outs)) return e;
     const std::string cond = named_expression(query_part, "condition");
     if (cond.empty()) return set_error(kParseError, "no condition=[...] in the LogicalFilter");
+    CategoryScope categories(frame, ncols);
+    // string literals first: a missing one rewrites its column's codes and dictionary, which the
+    // plan caches key on
+    if (has_string_literal(cond.c_str()) || frame_has_category(frame, ncols)) plan_expression(cond, ncols);
     if (frame[0]->size == 0) {
         // the reference leaves an empty frame untouched
         for (int c = 0; c < ncols; c++) { outs[c]->size = 0; outs[c]->null_count = 0; }
@@ -594,7 +605,10 @@ int plan_filter_project(gdf_column* const* frame, int ncols, const char* filter_
     if (cond.empty()) return set_error(kParseError, "no condition=[...] in the LogicalFilter");
     std::vector<gdf_dtype> fd(ncols);
     for (int c = 0; c < ncols; c++) fd[c] = frame[c]->dtype;
-    const ProjectPlan& pp = cached_project_plan(project_q, fd);
+    CategoryScope categories(frame, ncols);
+    if (has_string_literal(cond.c_str()) || frame_has_category(frame, ncols)) plan_expression(cond, ncols);
+    if (has_string_literal(project_q) || frame_has_category(frame, ncols)) plan_project(project_q, fd);
+    const ProjectPlan& pp = cached_project_plan(project_q, fd, category_key(frame, ncols));
     auto p = std::make_unique<FilterPlan>();
     frame_spec(frame, ncols, p->spec);
     if (int e = predicate_spec(frame, ncols, cond, p->spec, p->pred, p->have_pred)) return e;
@@ -677,7 +691,11 @@ int filter_project(gdf_column* const* frame, int ncols, const char* filter_q, co
     if (cond.empty()) return set_error(kParseError, "no condition=[...] in the LogicalFilter");
     std::vector<gdf_dtype> fd(ncols);
     for (int c = 0; c < ncols; c++) fd[c] = frame[c]->dtype;
-    const ProjectPlan& pp = cached_project_plan(project_q, fd);
+    CategoryScope categories(frame, ncols);
+    const bool cat = frame_has_category(frame, ncols);
+    if (has_string_literal(cond.c_str()) || cat) plan_expression(cond, ncols);
+    if (has_string_literal(project_q) || cat) plan_project(project_q, fd);
+    const ProjectPlan& pp = cached_project_plan(project_q, fd, category_key(frame, ncols));
     if ((int)pp.columns.size() != n_outs) return set_error(kInvalidArgument, "out_columns count differs from the projection's");
     for (int i = 0; i < n_outs; i++) {
         if (!outs[i]) return set_error(kInvalidArgument, "null out column");

@@ -151,7 +151,20 @@ struct Parser {
         if (i >= s.size()) throw ParseError("unexpected end of expression");
         auto e = std::make_unique<Expr>();
         if (s[i] == '\'') {
-            throw ParseError("string literals are not supported");
+            // a string literal, '' standing for one quote inside it
+            size_t j = i + 1;
+            for (;;) {
+                if (j >= s.size()) throw ParseError("unterminated string literal");
+                if (s[j] == '\'') {
+                    if (j + 1 < s.size() && s[j + 1] == '\'') { j += 2; continue; }
+                    break;
+                }
+                j++;
+            }
+            e->kind = Expr::Literal;
+            e->text = s.substr(i, j + 1 - i);
+            i = j + 1;
+            return e;
         }
         if (s[i] == '$') {
             size_t j = i + 1;
@@ -228,6 +241,23 @@ void normalise(std::unique_ptr<Expr>& e) {
 }
 
 bool is_literal_node(const Expr& e) { return e.kind == Expr::Literal; }
+bool is_string_node(const Expr& e) { return e.kind == Expr::Literal && !e.text.empty() && e.text[0] == '\''; }
+
+// The literal between its outer quotes, as the reference takes it (substr(1, size - 2)).
+std::string unquote(const std::string& t) { return t.size() >= 2 ? t.substr(1, t.size() - 2) : std::string(); }
+
+// A string literal compared with a string-category column: its INT32 code in the column's
+// dictionary (src/LogicalFilter.cpp:150-194).
+gdf_scalar category_scalar(const Expr& column, const Expr& literal) {
+    if (column.kind != Expr::Column)
+        throw ParseError("a string literal must be compared with a string-category column: " + literal.text);
+    gdf_scalar sc;
+    std::memset(&sc, 0, sizeof sc);
+    sc.dtype = GDF_INT32;
+    sc.is_valid = true;
+    sc.data.si32 = resolve_category_literal(column.column, unquote(literal.text));
+    return sc;
+}
 
 gdf_scalar literal_scalar(const std::string& t) {
     // get_type_from_string + get_scalar_from_string, CalciteExpressionParsing.cpp:323-417
@@ -297,6 +327,12 @@ struct Emitter {
             const Expr& L = *e.args[0];
             const Expr& R = *e.args[1];
             if (is_literal_node(L) && is_literal_node(R)) throw ParseError("operator on two literals is not supported");
+            if (is_string_node(L))
+                throw ParseError("a string literal on the left of an operator is not supported (as in the reference)");
+            // resolved before any op is emitted: a missing string rewrites the column's codes
+            gdf_scalar rstring{};
+            if (is_string_node(R)) rstring = category_scalar(L, R);
+            if (L.kind == Expr::Column && R.kind == Expr::Column) sync_category_columns(L.column, R.column);
             const int rreg = emit(R, -1);
             const int lreg = emit(L, -1);
             release(lreg);
@@ -309,7 +345,7 @@ struct Emitter {
                 pv.left.push_back(SCALAR_INDEX);
                 pv.right.push_back((int16_t)rreg);
             } else if (is_literal_node(R)) {
-                pv.rscalars.push_back(literal_scalar(R.text));
+                pv.rscalars.push_back(is_string_node(R) ? rstring : literal_scalar(R.text));
                 pv.lscalars.push_back(junk_scalar());
                 pv.right.push_back(SCALAR_INDEX);
                 pv.left.push_back((int16_t)lreg);

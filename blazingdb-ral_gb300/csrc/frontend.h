@@ -84,6 +84,32 @@ struct ProjectPlan {
 };
 ProjectPlan plan_project(const std::string& query_part, const std::vector<gdf_dtype>& frame_dtypes);
 
+// ---- string literals against string-category columns (category.cpp) -------------------------
+// A string literal on the right of a binary operator whose left operand is a frame column of dtype
+// GDF_STRING_CATEGORY becomes an INT32 scalar: the literal's code in the column's dictionary, the
+// string inserted (and the column's codes rewritten) when it is missing, as
+// src/LogicalFilter.cpp:150-194 does.  The frame is the one the calling entry point holds: a
+// CategoryScope makes it visible to the front end on this thread for the duration of a call.
+struct CategoryScope {
+    CategoryScope(gdf_column* const* frame, int ncols);
+    ~CategoryScope();
+    gdf_column* const* prev_frame;
+    int prev_n;
+};
+// Planning that only asks for output types (no frame): string literals resolve to a placeholder.
+struct TypesOnlyScope {
+    TypesOnlyScope();
+    ~TypesOnlyScope();
+    bool prev;
+};
+int32_t resolve_category_literal(int frame_column, const std::string& str);
+// Two category columns compared with each other: both moved to one merged dictionary.
+void sync_category_columns(int frame_column_a, int frame_column_b);
+bool frame_has_category(gdf_column* const* frame, int ncols);
+bool has_string_literal(const char* text);
+// The dictionaries of a frame's category columns, for plan-cache keys.
+std::string category_key(gdf_column* const* frame, int ncols);
+
 // Plan for a LogicalAggregate (process_aggregate, src/operators/GroupBy.cpp:531-590): the GROUP BY
 // columns, and per aggregation its operator (get_aggregation_operation,
 // CalciteExpressionParsing.cpp:483-507) and input, the text between the outer parentheses

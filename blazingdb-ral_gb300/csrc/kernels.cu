@@ -280,6 +280,40 @@ cudaError_t launch_gather(int width, const void* in, const uint32_t* in_valid, i
     }
 }
 
+namespace {
+__global__ void category_insert_kernel(int32_t* __restrict__ codes, ral_i64 n, int32_t pos) {
+    const ral_i64 stride = (ral_i64)gridDim.x * blockDim.x;
+    for (ral_i64 i = (ral_i64)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride)
+        if (codes[i] >= pos) codes[i] += 1;
+}
+__global__ void category_remap_kernel(int32_t* __restrict__ codes, ral_i64 n, const int32_t* __restrict__ table,
+                                      int32_t table_n) {
+    const ral_i64 stride = (ral_i64)gridDim.x * blockDim.x;
+    for (ral_i64 i = (ral_i64)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+        const int32_t c = codes[i];
+        if (c >= 0 && c < table_n) codes[i] = __ldg(table + c);
+    }
+}
+}  // namespace
+
+cudaError_t launch_category_remap(int32_t* codes, int64_t n, const int32_t* table, int32_t table_n, cudaStream_t st) {
+    if (n <= 0) return cudaSuccess;
+    const int threads = 256;
+    const int64_t blocks = std::max<int64_t>(1, std::min<int64_t>((n + threads - 1) / threads, 152 * 8));
+    category_remap_kernel<<<(int)blocks, threads, 0, st>>>(codes, n, table, table_n);
+    note_launch();
+    return cudaGetLastError();
+}
+
+cudaError_t launch_category_insert(int32_t* codes, int64_t n, int32_t pos, cudaStream_t st) {
+    if (n <= 0) return cudaSuccess;
+    const int threads = 256;
+    const int64_t blocks = std::max<int64_t>(1, std::min<int64_t>((n + threads - 1) / threads, 152 * 8));
+    category_insert_kernel<<<(int)blocks, threads, 0, st>>>(codes, n, pos);
+    note_launch();
+    return cudaGetLastError();
+}
+
 cudaError_t launch_gather_columns(const GatherColumnsParams& p, cudaStream_t st) {
     if (p.n_out <= 0 || p.num_columns <= 0) return cudaSuccess;
     int dev = 0, sms = 1, per_sm = 1;

@@ -47,6 +47,11 @@ struct GatherColumnsParams {
 // set bits counted into valid_counts[c].
 cudaError_t launch_gather_columns(const GatherColumnsParams& p, cudaStream_t st);
 
+// codes[i] += 1 where codes[i] >= pos: a string inserted at rank pos of a category dictionary.
+cudaError_t launch_category_insert(int32_t* codes, int64_t n, int32_t pos, cudaStream_t st);
+// codes[i] = table[codes[i]] for codes in [0, table_n): codes moved to a merged dictionary.
+cudaError_t launch_category_remap(int32_t* codes, int64_t n, const int32_t* table, int32_t table_n, cudaStream_t st);
+
 }  // namespace ral
 
 namespace ral {

@@ -54,6 +54,11 @@ _SIGS = {
     "ral_process_aggregate": (C.c_int, [C.c_void_p, C.c_int32, C.c_char_p, C.POINTER(GdfScalar), C.c_int32,
                                         C.POINTER(C.c_int32)]),
     "ral_debug_call_timing": (C.c_int, [C.c_int32, C.c_int32, C.POINTER(C.c_int64), C.POINTER(C.c_double)]),
+    "ral_category_create": (C.c_int, [C.c_void_p, C.c_int64, C.POINTER(C.c_void_p), I32P]),
+    "ral_category_size": (C.c_int, [C.c_void_p, C.POINTER(C.c_int64)]),
+    "ral_category_get_value": (C.c_int, [C.c_void_p, C.c_char_p, C.POINTER(C.c_int32)]),
+    "ral_category_key": (C.c_int, [C.c_void_p, C.c_int32, C.c_char_p, C.c_int64, C.POINTER(C.c_int64)]),
+    "ral_category_destroy": (C.c_int, [C.c_void_p]),
     "ral_jit_stats": (C.c_int, [C.POINTER(C.c_int64), C.POINTER(C.c_int64), C.POINTER(C.c_int64),
                                 C.POINTER(C.c_double)]),
     "ral_parse_project_plan": (C.c_int, [I32P, C.c_int32, C.c_char_p, C.c_int32, C.c_int32, I32P, I32P, I32P, I32P,
@@ -145,6 +150,14 @@ def _colarray(cols: Sequence[Column]):
     return arr, structs
 
 
+def _sync_categories(frame: Sequence[Column], structs) -> None:
+    """A call that resolved a string literal missing from a category column's dictionary points
+    the column at a new dictionary (and rewrote its codes): carry the new address over."""
+    for c, st in zip(frame, structs):
+        if c.dtype == D.GDF_STRING_CATEGORY and st.dtype_info.category:
+            c.category = int(st.dtype_info.category)
+
+
 def _scalars(ss: Sequence[Scalar]):
     arr = (GdfScalar * max(1, len(ss)))()
     for i, s in enumerate(ss):
@@ -226,6 +239,7 @@ def evaluate_expression(frame: List[Column], expression: str, output: Column) ->
     fa, _fs = _colarray(frame)
     oc = output.to_c()
     _check(lib().ral_evaluate_expression(fa, len(frame), expression.encode(), C.byref(oc)))
+    _sync_categories(frame, _fs)
     output.sync_from_c(oc)
     return output
 
@@ -238,6 +252,7 @@ def process_filter(frame: List[Column], query_part: str) -> List[Column]:
     oa, ostructs = _colarray(outs)
     n_out = C.c_int32(0)
     _check(lib().ral_process_filter(fa, len(frame), query_part.encode(), oa, C.byref(n_out)))
+    _sync_categories(frame, _fs)
     for col, s in zip(outs, ostructs):
         col.sync_from_c(s)
     return outs
@@ -266,6 +281,7 @@ def execute_project_plan(frame: List[Column], query_part: str) -> List[Column]:
         structs.append(s)
         arr[i] = C.pointer(s)
     _check(lib().ral_execute_project_plan(fa, len(frame), query_part.encode(), arr, len(outs)))
+    _sync_categories(frame, _fs)
     result = []
     for i, (c, s, e) in enumerate(zip(outs, structs, evald)):
         if e:
@@ -293,6 +309,7 @@ def filter_project(frame: List[Column], filter_query_part: str, project_query_pa
     n_out = C.c_int32(0)
     _check(lib().ral_filter_project(fa, len(frame), filter_query_part.encode(), project_query_part.encode(), oa,
                                     len(outs), C.byref(n_out)))
+    _sync_categories(frame, _fs)
     for col, s in zip(outs, ostructs):
         col.sync_from_c(s)
     return outs
@@ -420,6 +437,7 @@ def process_aggregate(frame: List[Column], query_part: str) -> List[Scalar]:
     n = C.c_int32(0)
     _check(lib().ral_process_aggregate(C.cast(arr, C.c_void_p), len(frame), query_part.encode(), res, cap,
                                        C.byref(n)))
+    _sync_categories(frame, _structs)
     return [Scalar.from_c(res[i]) for i in range(n.value)]
 
 
@@ -444,6 +462,69 @@ def call_timing(enable: bool = True, reset: bool = False) -> dict:
     _check(lib().ral_debug_call_timing(1 if enable else 0, 1 if reset else 0, C.byref(calls), us))
     return {"calls": calls.value, "host_prepare_us": us[0], "enqueue_us": us[1], "wait_us": us[2],
             "kernel_device_us": us[3]}
+
+
+class Category:
+    """A string-category dictionary (ral_category): its distinct strings in byte order; a column's
+    codes are their ranks.  Owned by the caller; dictionaries the library creates when a literal is
+    missing are adopted with Category.adopt."""
+
+    def __init__(self, handle: int):
+        self.handle = int(handle)
+
+    @staticmethod
+    def create(strings: Sequence[str]) -> Tuple["Category", np.ndarray]:
+        n = len(strings)
+        enc = [s.encode() for s in strings]
+        arr = (C.c_char_p * max(1, n))(*enc)
+        codes = np.zeros(max(1, n), dtype=np.int32)
+        h = C.c_void_p()
+        _check(lib().ral_category_create(arr, n, C.byref(h), codes.ctypes.data_as(I32P)))
+        return Category(h.value), codes[:n]
+
+    @staticmethod
+    def adopt(handle: int) -> "Category":
+        return Category(handle)
+
+    def size(self) -> int:
+        n = C.c_int64(0)
+        _check(lib().ral_category_size(C.c_void_p(self.handle), C.byref(n)))
+        return n.value
+
+    def get_value(self, s: str) -> int:
+        code = C.c_int32(0)
+        _check(lib().ral_category_get_value(C.c_void_p(self.handle), s.encode(), C.byref(code)))
+        return code.value
+
+    def keys(self) -> List[str]:
+        out = []
+        buf = C.create_string_buffer(1 << 12)
+        ln = C.c_int64(0)
+        for k in range(self.size()):
+            _check(lib().ral_category_key(C.c_void_p(self.handle), k, buf, len(buf), C.byref(ln)))
+            out.append(buf.raw[:ln.value].decode())
+        return out
+
+    def destroy(self) -> None:
+        if self.handle:
+            lib().ral_category_destroy(C.c_void_p(self.handle))
+            self.handle = 0
+
+
+def category_column(strings: Sequence[str], valids=None, device="cuda") -> Tuple[Column, Category]:
+    """A GDF_STRING_CATEGORY column of the given strings (codes on the device, dictionary attached)."""
+    cat, codes = Category.create(strings)
+    col = Column.from_numpy(codes, D.GDF_STRING_CATEGORY, valids, device=device)
+    col.category = cat.handle
+    return col, cat
+
+
+def decode_category(col: Column) -> List[Optional[str]]:
+    """The strings of a category column's rows (None where null)."""
+    keys = Category(col.category).keys()
+    codes = col.to_numpy()
+    vb = col.valid_bools()
+    return [keys[c] if v else None for c, v in zip(codes, vb)]
 
 
 def kernel_launches() -> int:

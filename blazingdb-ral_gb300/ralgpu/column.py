@@ -80,12 +80,14 @@ class Column:
     """A device column: data tensor (size elements), optional padded validity
     tensor (uint8, valid_alloc_size(capacity) bytes), dtype, null_count."""
 
-    def __init__(self, data, valid, dtype: int, size: Optional[int] = None, null_count: int = 0):
+    def __init__(self, data, valid, dtype: int, size: Optional[int] = None, null_count: int = 0,
+                 category: Optional[int] = None):
         self.data = data
         self.valid = valid
         self.dtype = dtype
         self.size = int(data.shape[0]) if size is None else int(size)
         self.null_count = int(null_count)
+        self.category = category   # GDF_STRING_CATEGORY: address of the ral_category dictionary
         self._c: Optional[GdfColumn] = None
 
     # -- construction -------------------------------------------------------------------------
@@ -145,12 +147,16 @@ class Column:
         c.size = self.size
         c.dtype = self.dtype
         c.null_count = self.null_count
+        if self.category:
+            c.dtype_info.category = self.category
         self._c = c
         return c
 
     def sync_from_c(self, c: GdfColumn) -> None:
         self.size = int(c.size)
         self.null_count = int(c.null_count)
+        if c.dtype_info.category:
+            self.category = int(c.dtype_info.category)
 
     def __repr__(self):
         return f"Column({D.NAMES.get(self.dtype, self.dtype)}, size={self.size}, nulls={self.null_count})"

@@ -224,6 +224,28 @@ int ral_process_aggregate(gdf_column *const *frame_columns, int32_t num_columns,
                           gdf_scalar *results, int32_t capacity, int32_t *num_results);
 
 /*
+ * String-category dictionaries — the NVCategory a GDF_STRING_CATEGORY column points at through
+ * dtype_info.category in the reference, where a string literal compared with such a column is looked
+ * up (src/LogicalFilter.cpp:150-194).  A ral_category keeps its distinct strings sorted by byte
+ * value; a column's int32 codes are the ranks of its strings, so comparing codes compares strings.
+ * ral_category_create builds one from n strings (duplicates allowed) and writes each string's code
+ * to codes_out (host array of n entries; may be NULL).  A filter or projection whose text compares
+ * such a column with a string literal ("=($k, 'abc')", literal on the right as the reference
+ * requires) uses the literal's code; when the dictionary lacks the string, the call makes a new
+ * dictionary with it, rewrites the column's codes to the new ranks on the device and points the
+ * column's dtype_info.category at the new dictionary, as the reference does.  The caller owns every
+ * dictionary, including ones the library made, and frees them with ral_category_destroy.
+ */
+typedef struct ral_category_s ral_category;
+int ral_category_create(const char *const *strings, int64_t n, ral_category **category, int32_t *codes_out);
+int ral_category_size(const ral_category *category, int64_t *num_keys);
+/* *code = the string's code, or -1 when the dictionary lacks it (NVCategory::get_value). */
+int ral_category_get_value(const ral_category *category, const char *str, int32_t *code);
+/* The string of a code, NUL-terminated and truncated to capacity; *length its full byte length. */
+int ral_category_key(const ral_category *category, int32_t code, char *buf, int64_t capacity, int64_t *length);
+int ral_category_destroy(ral_category *category);
+
+/*
  * add_expression_to_plan — src/LogicalFilter.h:26-42 (src/LogicalFilter.cpp:44-268).
  * The register-program emitter: appends the ops of `expression` to the arrays.
  * *num_operations is in/out (ops already present / after); arrays have room

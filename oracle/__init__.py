@@ -103,6 +103,7 @@ class OColumn:
     valid: Optional[np.ndarray]
     dtype: int
     null_count: int = 0
+    category: Optional[list] = None   # GDF_STRING_CATEGORY: the dictionary, strings as bytes, sorted
 
     @property
     def size(self) -> int:
@@ -192,9 +193,71 @@ def perform_plan(outputs: List[OColumn], inputs: List[OColumn], plan: fe.Plan, *
                       plan.operators, plan.unary_operators, plan.left_scalars, plan.right_scalars, **kw)
 
 
+def make_category_column(strings, valids=None) -> OColumn:
+    """A GDF_STRING_CATEGORY column: int32 codes = ranks of the strings in the sorted distinct set
+    (NVCategory::create_from_array)."""
+    keys = sorted(set(s.encode() for s in strings))
+    rank = {k: i for i, k in enumerate(keys)}
+    col = make_column([rank[s.encode()] for s in strings], fe.GDF_STRING_CATEGORY, valids)
+    col.category = keys
+    return col
+
+
+class _Categories:
+    """While planning over `frame`: a string literal compared with a category column is its code;
+    a missing string is inserted in sorted position, and the column's codes at or above it move up
+    by one (NVCategory::add_strings followed by the copy of the new values,
+    src/LogicalFilter.cpp:161-193)."""
+
+    def __init__(self, frame):
+        self.frame = frame
+
+    def resolve(self, col: int, s: str) -> int:
+        import bisect
+        c = self.frame[col]
+        if c.dtype != fe.GDF_STRING_CATEGORY or c.category is None:
+            raise OracleError("string literal compared with a column that is not a string category")
+        key = s.encode()
+        i = bisect.bisect_left(c.category, key)
+        if i < len(c.category) and c.category[i] == key:
+            return i
+        c.category = c.category[:i] + [key] + c.category[i:]
+        c.data[c.data >= i] += 1
+        return i
+
+    def sync(self, a: int, b: int) -> None:
+        ca, cb = self.frame[a], self.frame[b]
+        if a == b or ca.dtype != fe.GDF_STRING_CATEGORY or cb.dtype != fe.GDF_STRING_CATEGORY:
+            return
+        if ca.category == cb.category:
+            return
+        merged = sorted(set(ca.category) | set(cb.category))
+        rank = {k: i for i, k in enumerate(merged)}
+        for c in (ca, cb):
+            table = np.array([rank[k] for k in c.category], dtype=np.int32)
+            ok = (c.data >= 0) & (c.data < len(table))
+            c.data[ok] = table[c.data[ok]]
+            c.category = list(merged)
+
+    def __enter__(self):
+        self.prev = (fe.CATEGORY_RESOLVER, fe.CATEGORY_SYNC)
+        fe.CATEGORY_RESOLVER = self.resolve
+        fe.CATEGORY_SYNC = self.sync
+        return self
+
+    def __exit__(self, *a):
+        fe.CATEGORY_RESOLVER, fe.CATEGORY_SYNC = self.prev
+
+
+def decode_category(col: OColumn) -> list:
+    vb = col.valid_bools()
+    return [col.category[c].decode() if v else None for c, v in zip(col.data, vb)]
+
+
 def evaluate_expression(frame: List[OColumn], expression: str, output: OColumn, **kw) -> OColumn:
     """Returns the output column (a clone of a frame column for the "$n" shortcut)."""
-    res = fe.plan_evaluate_expression(len(frame), expression)
+    with _Categories(frame):
+        res = fe.plan_evaluate_expression(len(frame), expression)
     if res[0] == "clone":
         src = frame[res[1]]
         return OColumn(src.data.copy(), None if src.valid is None else src.valid.copy(), src.dtype,
@@ -232,7 +295,7 @@ def materialize_column(col: OColumn, idx: np.ndarray) -> OColumn:
                                     col.data.dtype.itemsize, idx.ctypes.data if n_out else None, n_out,
                                     data.ctypes.data, valid.ctypes.data if valid is not None else None,
                                     ctypes.byref(nc))
-    return OColumn(data[:n_out], valid, col.dtype, int(nc.value))
+    return OColumn(data[:n_out], valid, col.dtype, int(nc.value), col.category)
 
 
 def process_filter(frame: List[OColumn], query_part: str, **kw) -> List[OColumn]:
@@ -256,7 +319,8 @@ def filter_indices(frame: List[OColumn], query_part: str, **kw) -> np.ndarray:
 
 def execute_project_plan(frame: List[OColumn], query_part: str, **kw) -> List[OColumn]:
     """LogicalProject: every evaluated expression in one program, pass-through columns shared."""
-    pp = fe.parse_project_plan([c.dtype for c in frame], query_part)
+    with _Categories(frame):
+        pp = fe.parse_project_plan([c.dtype for c in frame], query_part)
     n = frame[0].size
     outs = [alloc_column(t, n) for t in pp.output_types]
     if outs:

@@ -345,6 +345,12 @@ class Plan:
     new_input_indices: List[int] = field(default_factory=list)
 
 
+# Set by the oracle's entry points while they plan over a frame: (frame column, string) -> code,
+# and (frame column, frame column) -> None for two category columns compared with each other.
+CATEGORY_RESOLVER = None
+CATEGORY_SYNC = None
+
+
 def add_expression_to_plan(expression: str, expression_position: int, num_outputs: int,
                            num_inputs: int, plan: Plan, new_input_indices: Sequence[int]) -> None:
     start = num_inputs + num_outputs
@@ -378,8 +384,8 @@ def add_expression_to_plan(expression: str, expression_position: int, num_output
                 op = BINARY_MAP[tok]
                 if is_literal(lt) and is_literal(rt):
                     raise FrontendError("operator on two literals is not supported")
-                if is_string(lt) or is_string(rt):
-                    raise FrontendError("string literals are not supported")
+                if is_string(lt):
+                    raise FrontendError("a string literal on the left of an operator is not supported")
                 plan.operators.append(op)
                 plan.unary_operators.append(BLZ_INVALID_UNARY)
                 if is_literal(lt):
@@ -388,6 +394,17 @@ def add_expression_to_plan(expression: str, expression_position: int, num_output
                     plan.right_scalars.append(JUNK)
                     plan.left.append(SCALAR_INDEX if sc.is_valid else SCALAR_NULL_INDEX)
                     plan.right.append(get_index(rt))
+                elif is_string(rt):
+                    # LogicalFilter.cpp:150-194: the string's code in the left column's dictionary,
+                    # the string added (and the column's codes rewritten) when it is missing
+                    dense = get_index(lt)
+                    if CATEGORY_RESOLVER is None or not lt.startswith("$") or dense not in new_input_indices:
+                        raise FrontendError("a string literal must be compared with a string-category column")
+                    sc = Scalar(GDF_INT32, CATEGORY_RESOLVER(list(new_input_indices).index(dense), rt[1:-1]))
+                    plan.right_scalars.append(sc)
+                    plan.left_scalars.append(JUNK)
+                    plan.right.append(SCALAR_INDEX)
+                    plan.left.append(dense)
                 elif is_literal(rt):
                     sc = get_scalar_from_string(rt, get_type_from_string(rt))
                     plan.right_scalars.append(sc)
@@ -395,8 +412,15 @@ def add_expression_to_plan(expression: str, expression_position: int, num_output
                     plan.right.append(SCALAR_INDEX if sc.is_valid else SCALAR_NULL_INDEX)
                     plan.left.append(get_index(lt))
                 else:
-                    plan.left.append(get_index(lt))
-                    plan.right.append(get_index(rt))
+                    li, ri = get_index(lt), get_index(rt)
+                    # two input columns: string-category columns move to one merged dictionary
+                    # (sync_column_categories, LogicalFilter.cpp:196-211)
+                    if CATEGORY_SYNC is not None and li < num_inputs and ri < num_inputs:
+                        idx = list(new_input_indices)
+                        if li in idx and ri in idx:
+                            CATEGORY_SYNC(idx.index(li), idx.index(ri))
+                    plan.left.append(li)
+                    plan.right.append(ri)
                     plan.left_scalars.append(JUNK)
                     plan.right_scalars.append(JUNK)
             elif tok in UNARY_MAP:

@@ -197,3 +197,11 @@ AGG_KATS = [
      "expected": [(INT64, True, 0), (INT64, False, None), (FLOAT64, False, None), (INT32, False, None),
                   (INT32, False, None)]},
 ]
+
+# tests/nvcategory/nvcategory-test.cu: string-category filters.  x INT32, y STRING_CATEGORY over the
+# strings below; LogicalFilter(<($1, 'e')) with 'e' in the dictionary (:363-402) and <($1, 'f') with
+# 'f' missing (:404-443, the dictionary grows); expected: the x of the rows whose y sorts below the
+# literal.  The test draws x at random; any x values give the same kept rows.
+CATEGORY_STRINGS = ["a", "b", "c", "d", "e", "g", "h", "i", "j", "k"]
+CATEGORY_KATS = [("LogicalFilter(condition=[<($1, 'e')])", "e"),
+                 ("LogicalFilter(condition=[<($1, 'f')])", "f")]

@@ -108,3 +108,15 @@ def test_materialize_columns_checks_arguments_before_any_cuda_call():
     assert b"differ in size" in L.ral_last_error()
     assert call([mk(D.GDF_INT32, 8)], [mk(D.GDF_INT64, 8)], idx) == 1 and b"width mismatch" in L.ral_last_error()
     assert call([], [], idx) == 0
+
+
+def test_category_dictionary_api_needs_no_gpu():
+    """ral_category: distinct strings sorted by byte value, codes are ranks, -1 for a missing string."""
+    strings = ["pear", "apple", "Zebra", "apple", "é", "banana", ""]
+    cat, codes = ralgpu.Category.create(strings)
+    keys = cat.keys()
+    assert keys == sorted(set(strings), key=lambda s: s.encode())
+    assert [keys[c] for c in codes] == strings
+    assert cat.get_value("banana") == keys.index("banana") and cat.get_value("kiwi") == -1
+    assert cat.size() == len(set(strings))
+    cat.destroy()

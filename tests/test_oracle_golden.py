@@ -109,3 +109,15 @@ def test_oracle_aggregation_without_group_by(kat):
         assert g.dtype == t and g.is_valid == valid
         if valid:
             assert g.value == value
+
+
+@pytest.mark.parametrize("query,literal", K.CATEGORY_KATS, ids=["exists", "missing"])
+def test_oracle_string_category_filter(query, literal):
+    """The reference's NVCategory filter tests: rows whose string sorts below the literal; a missing
+    literal is added to the dictionary and the codes follow."""
+    x = list(range(100, 100 + len(K.CATEGORY_STRINGS)))
+    frame = [O.make_column(x, fe.GDF_INT32), O.make_category_column(K.CATEGORY_STRINGS)]
+    out = O.process_filter(frame, query)
+    assert out[0].data.tolist() == [v for v, s in zip(x, K.CATEGORY_STRINGS) if s < literal]
+    assert O.decode_category(out[1]) == [s for s in K.CATEGORY_STRINGS if s < literal]
+    assert (literal.encode() in frame[1].category)
