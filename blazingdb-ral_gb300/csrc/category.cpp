@@ -36,23 +36,38 @@ int32_t find_key(const ral_category* c, const std::string& s) {
     return (int32_t)(it - c->keys.begin());
 }
 
-thread_local gdf_column* const* t_frame = nullptr;
-thread_local int t_ncols = 0;
+thread_local CategoryScope* t_scope = nullptr;
 thread_local bool t_types_only = false;
 
 }  // namespace
 
+int32_t resolve_and_grow(CategoryScope* sc, int col, const std::string& str);
+
 // The resolver the front end calls for a string literal compared with frame column `col`.
 int32_t resolve_category_literal(int col, const std::string& str) {
-    if (!t_frame) {
+    CategoryScope* sc = t_scope;
+    if (!sc) {
         // planning for output types only: the code does not matter
         if (t_types_only) return 0;
         throw ParseError("string literal '" + str + "': string-category columns are resolved by the entry points "
                          "that take the frame");
     }
-    if (col < 0 || col >= t_ncols || !t_frame[col])
+    if (sc->replaying) {
+        auto it = sc->codes.find(sc->current);
+        size_t& k = sc->next[sc->current];
+        if (it == sc->codes.end() || k >= it->second.size())
+            throw ParseError("string literal '" + str + "' was not resolved before planning");
+        return it->second[k++];
+    }
+    const int32_t code = resolve_and_grow(sc, col, str);
+    sc->codes[sc->current].push_back(code);
+    return code;
+}
+
+int32_t resolve_and_grow(CategoryScope* sc, int col, const std::string& str) {
+    if (col < 0 || col >= sc->ncols || !sc->frame[col])
         throw ParseError("string literal '" + str + "': column reference out of range");
-    gdf_column* c = t_frame[col];
+    gdf_column* c = sc->frame[col];
     if (c->dtype != GDF_STRING_CATEGORY || !c->dtype_info.category)
         throw ParseError("string literal '" + str + "' compared with a column that is not a string category");
     const ral_category* cat = static_cast<const ral_category*>(c->dtype_info.category);
@@ -105,9 +120,10 @@ void remap_to(gdf_column* c, const ral_category* merged) {
 // (sync_column_categories, called from src/LogicalFilter.cpp:203-211): the union of their strings,
 // each column's codes remapped to it.  Each column gets its own copy of the merged dictionary.
 void sync_category_columns(int a, int b) {
-    if (!t_frame || a < 0 || b < 0 || a >= t_ncols || b >= t_ncols || a == b) return;
-    gdf_column* ca = t_frame[a];
-    gdf_column* cb = t_frame[b];
+    CategoryScope* sc = t_scope;
+    if (!sc || sc->replaying || a < 0 || b < 0 || a >= sc->ncols || b >= sc->ncols || a == b) return;
+    gdf_column* ca = sc->frame[a];
+    gdf_column* cb = sc->frame[b];
     if (!ca || !cb || ca->dtype != GDF_STRING_CATEGORY || cb->dtype != GDF_STRING_CATEGORY) return;
     const ral_category* ka = static_cast<const ral_category*>(ca->dtype_info.category);
     const ral_category* kb = static_cast<const ral_category*>(cb->dtype_info.category);
@@ -138,13 +154,25 @@ bool frame_has_category(gdf_column* const* frame, int ncols) {
 TypesOnlyScope::TypesOnlyScope() : prev(t_types_only) { t_types_only = true; }
 TypesOnlyScope::~TypesOnlyScope() { t_types_only = prev; }
 
-CategoryScope::CategoryScope(gdf_column* const* frame, int ncols) : prev_frame(t_frame), prev_n(t_ncols) {
-    t_frame = frame;
-    t_ncols = ncols;
+CategoryScope::CategoryScope(gdf_column* const* f, int n) : frame(f), ncols(n), prev(t_scope) { t_scope = this; }
+CategoryScope::~CategoryScope() { t_scope = prev; }
+void CategoryScope::planning(const std::string& text) { current = text; }
+void category_planning(const std::string& text) {
+    if (t_scope) t_scope->planning(text);
 }
-CategoryScope::~CategoryScope() {
-    t_frame = prev_frame;
-    t_ncols = prev_n;
+void CategoryScope::replay() {
+    replaying = true;
+    next.clear();
+}
+std::string CategoryScope::recorded_key() const {
+    std::string k;
+    for (const auto& [text, v] : codes) {
+        if (v.empty()) continue;
+        k += "{";
+        for (int32_t c : v) k += std::to_string(c) + ",";
+        k += "}";
+    }
+    return k;
 }
 
 bool has_string_literal(const char* text) { return text && std::strchr(text, '\'') != nullptr; }

@@ -64,6 +64,7 @@ void apply_shape_tune(Shape& sh, const std::string& t) {
             else if (k == "P" && v >= 0 && v <= 64) sh.prefetch = v;
             else if (k == "D" && v >= -1 && v <= 1) sh.dense = v;
             else if (k == "K" && v >= 1 && v <= 2) sh.dense_unroll = v;
+            else if (k == "M" && v >= 0 && v <= 8 && v != 1) sh.tma_stages = v;
         }
         i = e + 1;
     }
@@ -379,10 +380,58 @@ std::vector<Kind> final_kinds(const Program& p, const ParamLayout& L) {
 
 }  // namespace
 
+namespace {
+
+// Layout of one stage of a staged eval kernel: every referenced input's tile, then the masks the
+// kernel reads (validity pass or raw bits), each region a multiple of 16 bytes.
+struct StageLayout {
+    std::vector<int> data_off, mask_off;  // -1: not staged
+    int bytes = 0;
+    bool masks_staged = false;
+};
+
+StageLayout stage_layout(const Program& p, const Shape& s) {
+    StageLayout st;
+    const int64_t tile = (int64_t)32 * s.G * s.J;
+    const auto ref = p.inputs_referenced();
+    const auto raw = p.inputs_raw_valid();
+    ValidEmitter ve(p);
+    st.data_off.assign(p.n_in, -1);
+    st.mask_off.assign(p.n_in, -1);
+    int off = 0;
+    for (int c = 0; c < p.n_in; c++) {
+        if (!ref[c]) continue;
+        const int64_t b = tile * gdf_dtype_size(p.inputs[c].dtype);
+        if (b % 16) return StageLayout{};
+        st.data_off[c] = off;
+        off += (int)b;
+    }
+    // masks: 4 bytes per 32 rows; a multiple of 16 bytes when the tile is a multiple of 128 rows
+    st.masks_staged = tile % 128 == 0;
+    if (st.masks_staged)
+        for (int c = 0; c < p.n_in; c++)
+            if (p.inputs[c].has_valid && ((ref[c] && ve.loads(c)) || raw[c])) {
+                st.mask_off[c] = off;
+                off += (int)(tile / 8);
+            }
+    st.bytes = off;
+    return st;
+}
+
+}  // namespace
+
+int eval_stage_bytes_per_warp(const Program& p, const Shape& s) {
+    if (s.tma_stages < 2) return 0;
+    const StageLayout st = stage_layout(p, s);
+    if (st.bytes == 0) return 0;
+    return 128 + s.tma_stages * st.bytes;  // barriers padded to 128 bytes, then the stages
+}
+
 GeneratedKernel generate_eval_kernel(const Program& p, const Shape& s) {
     GeneratedKernel gk;
     gk.shape = s;
-    gk.layout = make_layout(p, 0);
+    const int warp_smem = eval_stage_bytes_per_warp(p, s);
+    gk.layout = make_layout(p, warp_smem > 0 ? 1 : 0);  // staged kernels: an error word
     const ParamLayout& L = gk.layout;
     const auto ref = p.inputs_referenced();
     const auto raw = p.inputs_raw_valid();
@@ -392,8 +441,11 @@ GeneratedKernel generate_eval_kernel(const Program& p, const Shape& s) {
         if (p.out_has_valid[o]) vouts.push_back(o);
     const int NOV = (int)vouts.size();
 
+    const bool staged = warp_smem > 0;
+    const StageLayout SL = staged ? stage_layout(p, s) : StageLayout{};
     std::ostringstream key;
     key << "eval|" << p.structure_key() << "|G" << s.G << "J" << s.J << "T" << s.threads << "B" << s.min_blocks;
+    if (staged) key << "M" << s.tma_stages;
     char hex[32];
     snprintf(hex, sizeof hex, "%016llx", (unsigned long long)fnv1a(key.str()));
     gk.name = std::string("ral_eval_") + hex;
@@ -439,6 +491,62 @@ GeneratedKernel generate_eval_kernel(const Program& p, const Shape& s) {
     if (NOV > 0) os << "    ral_u64 vcnt[" << NOV << "];\n    for (int i = 0; i < " << NOV << "; ++i) vcnt[i] = 0;\n";
 
     // full tiles
+    if (staged) {
+        // per warp: S barriers (128 bytes), then S stages; lane 0 fills a stage with one bulk copy per
+        // staged column / mask of the tile and the warp waits on the stage's barrier
+        const int S = s.tma_stages;
+        os << "    extern __shared__ __align__(128) unsigned char ral_smem[];\n";
+        os << "    const int RAL_S = " << S << ", STAGE = " << SL.bytes << ", WARP_SMEM = " << warp_smem << ";\n";
+        os << "    unsigned char* wsm = ral_smem + (threadIdx.x >> 5) * WARP_SMEM;\n";
+        os << "    ral_u64* bars = (ral_u64*)wsm;\n";
+        os << "    unsigned char* stages = wsm + 128;\n";
+        os << "    ral_u64* err = (ral_u64*)P.s[" << L.counts << " + 1];\n";
+        os << "    if (lane == 0) { for (int q = 0; q < RAL_S; ++q) ral_mbar_init(bars + q, 1); ral_mbar_init_fence(); }\n";
+        os << "    __syncwarp();\n";
+        os << "    auto fill = [&](int q, ral_i64 t) {\n";
+        os << "        unsigned char* st = stages + q * STAGE;\n";
+        os << "        ral_mbar_expect_tx(bars + q, STAGE);\n";
+        for (int c = 0; c < p.n_in; c++) {
+            if (SL.data_off[c] >= 0) {
+                const int w = gdf_dtype_size(p.inputs[c].dtype);
+                os << "        ral_bulk_g2s(st + " << SL.data_off[c] << ", pin" << c << " + t * TILE, (unsigned)(TILE * " << w
+                   << "), bars + q);\n";
+            }
+            if (SL.mask_off[c] >= 0)
+                os << "        ral_bulk_g2s(st + " << SL.mask_off[c] << ", ((const ral_u32*)P.s[" << L.in_valid + c
+                   << "]) + t * (TILE / 32), (unsigned)(TILE / 8), bars + q);\n";
+        }
+        os << "    };\n";
+        os << "    if (lane == 0)\n";
+        os << "        for (int q = 0; q < RAL_S; ++q)\n";
+        os << "            if (gwarp + (ral_i64)q * nwarp < ntiles) fill(q, gwarp + (ral_i64)q * nwarp);\n";
+        os << "    bool ok = true;\n";
+        os << "    long k = 0;\n";
+        os << "    for (ral_i64 t = gwarp; t < ntiles; t += nwarp, ++k) {\n";
+        os << "        const int q = (int)(k % RAL_S);\n";
+        os << "        if (!ral_mbar_wait(bars + q, (unsigned)((k / RAL_S) & 1))) { ok = false; break; }\n";
+        os << "        const unsigned char* st = stages + q * STAGE;\n";
+        os << "        const ral_i64 base = t * TILE;\n";
+        os << "#pragma unroll\n";
+        os << "        for (int j = 0; j < RAL_J; ++j) {\n";
+        os << "            const int lr = j * 32 * RAL_G + lane * RAL_G;\n";
+        os << "            const ral_i64 r = base + lr;\n";
+        for (int c = 0; c < p.n_in; c++) {
+            if (!ref[c]) continue;
+            const char* et = element_ctype(p.inputs[c].dtype);
+            os << "            " << et << " a" << c << "[RAL_G]; ral_lds<" << et << ", RAL_G>((const " << et << "*)(st + "
+               << SL.data_off[c] << "), lr, a" << c << ");\n";
+        }
+        for (int c = 0; c < p.n_in; c++) {
+            if (!raw[c]) continue;
+            if (p.inputs[c].has_valid && SL.mask_off[c] >= 0)
+                os << "            const ral_u32 rw" << c << " = ((const ral_u32*)(st + " << SL.mask_off[c] << "))[lr >> 5];\n";
+            else if (p.inputs[c].has_valid)
+                os << "            const ral_u32 rw" << c << " = __ldg(pvr" << c << " + (r >> 5));\n";
+            else
+                os << "            const ral_u32 rw" << c << " = 0xffffffffu;\n";
+        }
+    } else {
     os << "    for (ral_i64 t = gwarp; t < ntiles; t += nwarp) {\n";
     os << "        const ral_i64 base = t * TILE;\n";
     os << "#pragma unroll\n";
@@ -453,6 +561,7 @@ GeneratedKernel generate_eval_kernel(const Program& p, const Shape& s) {
         if (!raw[c]) continue;
         if (p.inputs[c].has_valid) os << "            const ral_u32 rw" << c << " = __ldg(pvr" << c << " + (r >> 5));\n";
         else os << "            const ral_u32 rw" << c << " = 0xffffffffu;\n";
+    }
     }
     for (int o = 0; o < p.n_out; o++)
         os << "            " << element_ctype(p.out_dtypes[o]) << " b" << o << "[RAL_G];\n";
@@ -475,11 +584,43 @@ GeneratedKernel generate_eval_kernel(const Program& p, const Shape& s) {
     if (NOV > 0) {
         os << "        for (int wl = lane; wl < RAL_G * RAL_J; wl += 32) {\n";
         os << "            const ral_i64 w = (base >> 5) + wl;\n";
-        os << "            ral_u32 vo[" << NOV << "]; ral_vword(P, w, vo);\n";
+        if (staged && SL.masks_staged) {
+            // the validity pass over the staged mask words of the tile
+            os << "            ral_u32 vo[" << NOV << "];\n";
+            os << "            {\n";
+            ValidEmitter ve(p);
+            std::ostringstream vb;
+            ve.emit(vb, "                ", [&](int c) {
+                if (SL.mask_off[c] >= 0) return "((const ral_u32*)(st + " + std::to_string(SL.mask_off[c]) + "))[wl]";
+                return "__ldg(((const ral_u32*)P.s[" + std::to_string(L.in_valid + c) + "]) + w)";
+            });
+            os << vb.str();
+            for (int i = 0; i < NOV; i++) os << "                vo[" << i << "] = " << ve.name[p.final_pos[vouts[i]]] << ";\n";
+            os << "            }\n";
+        } else {
+            os << "            ral_u32 vo[" << NOV << "]; ral_vword(P, w, vo);\n";
+        }
         for (int i = 0; i < NOV; i++) os << "            pvo" << i << "[w] = vo[" << i << "]; vcnt[" << i << "] += __popc(vo[" << i << "]);\n";
         os << "        }\n";
     }
+    if (staged) {
+        // every lane is done with the stage: lane 0 refills it with the warp's tile S steps ahead
+        os << "        __syncwarp();\n";
+        os << "        if (lane == 0 && t + (ral_i64)RAL_S * nwarp < ntiles) {\n";
+        os << "            asm volatile(\"fence.proxy.async.shared::cta;\" ::: \"memory\");\n";
+        os << "            fill(q, t + (ral_i64)RAL_S * nwarp);\n";
+        os << "        }\n";
+    }
     os << "    }\n";
+    if (staged) {
+        // a wait that gave up: record it; before the warp exits, wait (bounded) for the copies it
+        // issued so that none lands in shared memory after the block has finished
+        os << "    if (!ok) {\n";
+        os << "        if (lane == 0) atomicExch((unsigned long long*)err, 1ull);\n";
+        os << "        for (ral_i64 t = gwarp + k * nwarp; t < ntiles && t < gwarp + (k + RAL_S) * nwarp; t += nwarp, ++k)\n";
+        os << "            ral_mbar_wait(bars + (int)(k % RAL_S), (unsigned)((k / RAL_S) & 1));\n";
+        os << "    }\n";
+    }
 
     // tail rows and words, one warp
     os << "    const ral_i64 tail0 = ntiles * TILE;\n";
@@ -535,6 +676,7 @@ GeneratedKernel generate_eval_kernel(const Program& p, const Shape& s) {
     }
     os << "}\n";
     gk.source = os.str();
+    if (staged) gk.dyn_smem = warp_smem * (s.threads / 32);
     return gk;
 }
 

@@ -30,6 +30,10 @@ struct Shape {
     // With the dense pass 2 any value > 0 prefetches the chunk's columns during the look-back
     // (also slower: the 200M-row filter + project at s = 0.5 ran 2.53 ms against 2.09).
     int prefetch = 0;
+    // eval kernels: 0 loads every tile from global memory into registers; S >= 2 stages each warp's
+    // tiles in shared memory through a ring of S stages filled by bulk copies (TMA), the next
+    // tiles in flight while the warp computes the current one
+    int tma_stages = 0;
     // filter kernels: pass 2 walks a shared-memory list of the chunk's kept rows, 32 at a time,
     // so every lane evaluates or gathers a kept row and stores are contiguous (1, the default;
     // -1 is the same), or takes its own G rows of each slice, skipping dropped ones (0)
@@ -74,7 +78,13 @@ struct GeneratedKernel {
     bool soft_fp = true;
     // relocatable item functions: register cap (0: RAL_BATCH_MAXRREG's)
     int max_registers = 0;
+    // dynamic shared memory a block needs (staged eval kernels)
+    int dyn_smem = 0;
 };
+
+// Shared-memory bytes one warp of a staged eval kernel needs (its barriers and S stages), or 0
+// when the program cannot be staged (a tile of a column not a multiple of 16 bytes).
+int eval_stage_bytes_per_warp(const Program& p, const Shape& s);
 
 // Batched and served launches run many programs in one persistent kernel.  Each program's warp
 // tile is a relocatable device function of its own, compiled once per program structure and

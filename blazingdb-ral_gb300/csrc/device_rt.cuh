@@ -250,6 +250,51 @@ RAL_FI void ral_stg(E* __restrict__ p, ral_i64 row, const E (&v)[G]) {
     __stcs(reinterpret_cast<V*>(p + row), u.vec);
 }
 
+// ---- bulk copies into shared memory (TMA) completing on an mbarrier ---------------------------
+// A warp's stage of a staged kernel is filled by one lane: arrive.expect_tx announces the bytes,
+// then one cp.async.bulk per contiguous range (16-byte aligned addresses, size a multiple of 16)
+// completes them; the warp waits on the barrier's phase parity.  Waits are bounded: after
+// RAL_STAGE_SPIN_LIMIT polls the wait gives up and reports it.
+#define RAL_STAGE_SPIN_LIMIT (1l << 24)
+RAL_FI unsigned ral_smem_u32(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
+RAL_FI void ral_mbar_init(ral_u64* bar, unsigned count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(ral_smem_u32(bar)), "r"(count) : "memory");
+}
+RAL_FI void ral_mbar_init_fence() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
+RAL_FI void ral_mbar_expect_tx(ral_u64* bar, unsigned bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(ral_smem_u32(bar)), "r"(bytes)
+                 : "memory");
+}
+RAL_FI void ral_bulk_g2s(void* dst, const void* src, unsigned bytes, ral_u64* bar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+                 ::"r"(ral_smem_u32(dst)), "l"(src), "r"(bytes), "r"(ral_smem_u32(bar))
+                 : "memory");
+}
+RAL_FI bool ral_mbar_test(ral_u64* bar, unsigned parity) {
+    unsigned ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(ral_smem_u32(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+// true when the phase completed; false after the spin limit
+RAL_FI bool ral_mbar_wait(ral_u64* bar, unsigned parity) {
+    for (long spins = 0; spins < RAL_STAGE_SPIN_LIMIT; ++spins)
+        if (ral_mbar_test(bar, parity)) return true;
+    return false;
+}
+// Vector load of G consecutive elements from shared memory (the staged copy of a column).
+template <typename E, int G>
+RAL_FI void ral_lds(const E* p, int row, E (&v)[G]) {
+    typedef typename RalVecT<sizeof(E) * G>::T V;
+    union { V vec; E e[G]; } u;
+    u.vec = *reinterpret_cast<const V*>(p + row);
+#pragma unroll
+    for (int g = 0; g < G; ++g) v[g] = u.e[g];
+}
+
 // ---- status-word access for the single-pass scan --------------------------------------------
 // A tile's status word carries its own value, and nothing else is published through it, so
 // relaxed gpu-scope accesses suffice: a store needs no fence (which would wait for the

@@ -123,14 +123,16 @@ int device_sms() {
 int blocks_per_sm(const CompiledKernel& k, int threads) {
     int dev = 0;
     cudaGetDevice(&dev);
-    const std::string key = k.name + "@" + std::to_string(dev) + "/" + std::to_string(threads);
+    const std::string key = k.name + "@" + std::to_string(dev) + "/" + std::to_string(threads) + "/" +
+                            std::to_string(k.dyn_smem);
     {
         std::lock_guard<std::mutex> lock(g_dev_mu);
         auto it = g_occupancy.find(key);
         if (it != g_occupancy.end()) return it->second;
     }
     int b = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, (const void*)k.kernel, threads, 0) != cudaSuccess) {
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, (const void*)k.kernel, threads, (size_t)k.dyn_smem) !=
+        cudaSuccess) {
         cudaGetLastError();
         b = 1;
     }
@@ -214,6 +216,40 @@ int call_timing_query(bool enable, bool reset, int64_t* calls, double* us4) {
     return kSuccess;
 }
 
+namespace {
+std::mutex g_err_mu;
+std::unordered_map<int, unsigned long long*> g_err_words;
+}  // namespace
+
+// A word per device that staged kernels set when a bounded wait gave up (allocated once, zeroed).
+unsigned long long* device_error_word() {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    std::lock_guard<std::mutex> lock(g_err_mu);
+    auto it = g_err_words.find(dev);
+    if (it != g_err_words.end()) return it->second;
+    unsigned long long* w = nullptr;
+    if (cudaMalloc((void**)&w, sizeof(unsigned long long)) != cudaSuccess) return nullptr;
+    cudaMemset(w, 0, sizeof(unsigned long long));
+    cudaDeviceSynchronize();
+    g_err_words[dev] = w;
+    return w;
+}
+
+// Reads and clears the device's error word after a synchronisation: kTimeout when a staged
+// kernel's wait gave up since the last check.
+int take_device_error(cudaStream_t st) {
+    unsigned long long* w = device_error_word();
+    if (!w) return kSuccess;
+    unsigned long long h = 0;
+    if (int e = check_cuda(cudaMemcpyAsync(&h, w, sizeof h, cudaMemcpyDeviceToHost, st), "cudaMemcpyAsync")) return e;
+    if (int e = check_cuda(cudaStreamSynchronize(st), "cudaStreamSynchronize")) return e;
+    if (!h) return kSuccess;
+    cudaMemsetAsync(w, 0, sizeof h, st);
+    cudaStreamSynchronize(st);
+    return set_error(kTimeout, "a staged kernel's wait for its bulk copies gave up");
+}
+
 int launch_blocks(const CompiledKernel& k, int threads, int64_t rows_per_block, int64_t rows) {
     const int sms = device_sms();
     const int per_sm = blocks_per_sm(k, threads);
@@ -250,6 +286,14 @@ int perform_operation(gdf_column* const* outputs, int n_out, gdf_column* const* 
             return set_error(kInvalidArgument, "validity masks must be 4-byte aligned");
     }
     if (!ok_align) { s.G = 1; s.J = 4; }
+    // staged tiles: bulk copies need 16-byte aligned column and mask addresses
+    if (s.tma_stages >= 2) {
+        bool ok16 = ok_align && n > 0;
+        for (int c = 0; c < n_in && ok16; c++)
+            if ((ref[c] && !aligned(inputs[c]->data, 16)) || (inputs[c]->valid && !aligned(inputs[c]->valid, 16)))
+                ok16 = false;
+        if (!ok16 || eval_stage_bytes_per_warp(p, s) == 0) s.tma_stages = 0;
+    }
     if (n > 0) {
         for (int c = 0; c < n_in; c++)
             if (ref[c] && !inputs[c]->data) return set_error(kInvalidArgument, "input column without data");
@@ -283,13 +327,20 @@ int perform_operation(gdf_column* const* outputs, int n_out, gdf_column* const* 
         slots[L.out_valid + o] = (uint64_t)(uintptr_t)outputs[o]->valid;
     }
     slots[L.counts] = (uint64_t)(uintptr_t)(d_counts ? d_counts : opt.device_valid_counts);
+    const bool staged = k->dyn_smem > 0;
+    if (staged) {
+        unsigned long long* ew = device_error_word();
+        if (!ew) return set_error(kAllocError, "device error word");
+        slots[L.counts + 1] = (uint64_t)(uintptr_t)ew;
+    }
     fill_scalars(p, L, slots);
 
     if (n > 0) {
         const int64_t rows_per_block = (int64_t)32 * s.G * s.J * (s.threads / 32);
         const int grid = launch_blocks(*k, s.threads, rows_per_block, n);
         void* args[] = {slots.data()};
-        if (int e = check_cuda(cudaLaunchKernel((const void*)k->kernel, dim3(grid), dim3(s.threads), args, 0, st),
+        if (int e = check_cuda(cudaLaunchKernel((const void*)k->kernel, dim3(grid), dim3(s.threads), args,
+                                                (size_t)k->dyn_smem, st),
                                "launch of the expression kernel"))
             return e;
         note_launch();
@@ -307,6 +358,10 @@ int perform_operation(gdf_column* const* outputs, int n_out, gdf_column* const* 
         if (int e = check_cuda(cudaStreamSynchronize(st), "cudaStreamSynchronize")) return e;
     }
     if (int e = check_cuda(cudaGetLastError(), "expression kernel")) return e;
+    // a synchronous call with a staged kernel reports a wait that gave up (asynchronous calls leave
+    // it to the next synchronous one on the device)
+    if (staged && n > 0 && (want_counts || opt.sync))
+        if (int e = take_device_error(st)) return e;
     return kSuccess;
 }
 

@@ -178,6 +178,7 @@ int filter_project_unfused(gdf_column* const* frame, int ncols, const std::strin
     if (int e = process_filter_unfused(frame, ncols, cond, tp.data(), n_out, st)) return e;
     std::vector<gdf_dtype> f(ncols);
     for (int c = 0; c < ncols; c++) f[c] = frame[c]->dtype;
+    category_planning(project_q);
     ProjectPlan pp = plan_project(project_q, f);
     std::vector<gdf_column*> evald;
     for (size_t i = 0; i < pp.columns.size(); i++)
@@ -484,11 +485,11 @@ const ProjectPlan& cached_project_plan(const char* project_q, const std::vector<
 }
 
 int process_filter_fused(gdf_column* const* frame, int ncols, const std::string& cond, gdf_column* const* outs,
-                         gdf_size_type* n_out, cudaStream_t st) {
+                         gdf_size_type* n_out, cudaStream_t st, const std::string& codes) {
     const std::string sig = frame_signature(frame, ncols, outs, ncols);
     const bool al = sig.find("|a|") != std::string::npos;
     const PreparedFilter* pf = nullptr;
-    int rc = prepared("F|" + cond + "|" + sig, al, frame[0]->size, [&](PreparedFilter& p) {
+    int rc = prepared("F|" + cond + "|" + sig + "|" + codes, al, frame[0]->size, [&](PreparedFilter& p) {
         frame_spec(frame, ncols, p.spec);
         if (int e = predicate_spec(frame, ncols, cond, p.spec, p.pred, p.have_pred)) return e;
         if (p.have_pred) p.spec.predicate = &p.pred;
@@ -580,9 +581,11 @@ int process_filter(gdf_column* const* frame, int ncols, const char* query_part, 
     const std::string cond = named_expression(query_part, "condition");
     if (cond.empty()) return set_error(kParseError, "no condition=[...] in the LogicalFilter");
     CategoryScope categories(frame, ncols);
-    // string literals first: a missing one rewrites its column's codes and dictionary, which the
-    // plan caches key on
+    // string literals first, once, in the reference's order: a missing one rewrites its column's
+    // codes and dictionary; the plans below replay the codes, which the plan caches key on
+    categories.planning(cond);
     if (has_string_literal(cond.c_str()) || frame_has_category(frame, ncols)) plan_expression(cond, ncols);
+    categories.replay();
     if (frame[0]->size == 0) {
         // the reference leaves an empty frame untouched
         for (int c = 0; c < ncols; c++) { outs[c]->size = 0; outs[c]->null_count = 0; }
@@ -590,7 +593,7 @@ int process_filter(gdf_column* const* frame, int ncols, const char* query_part, 
         return kSuccess;
     }
     if (filter_mode(opt) == 1) return process_filter_unfused(frame, ncols, cond, outs, n_out, opt.stream);
-    return process_filter_fused(frame, ncols, cond, outs, n_out, opt.stream);
+    return process_filter_fused(frame, ncols, cond, outs, n_out, opt.stream, categories.recorded_key());
 }
 
 int plan_filter_project(gdf_column* const* frame, int ncols, const char* filter_q, const char* project_q,
@@ -606,9 +609,13 @@ int plan_filter_project(gdf_column* const* frame, int ncols, const char* filter_
     std::vector<gdf_dtype> fd(ncols);
     for (int c = 0; c < ncols; c++) fd[c] = frame[c]->dtype;
     CategoryScope categories(frame, ncols);
+    categories.planning(cond);
     if (has_string_literal(cond.c_str()) || frame_has_category(frame, ncols)) plan_expression(cond, ncols);
+    categories.planning(project_q);
     if (has_string_literal(project_q) || frame_has_category(frame, ncols)) plan_project(project_q, fd);
-    const ProjectPlan& pp = cached_project_plan(project_q, fd, category_key(frame, ncols));
+    categories.replay();
+    const ProjectPlan& pp = cached_project_plan(project_q, fd, category_key(frame, ncols) + categories.recorded_key());
+    categories.planning(cond);
     auto p = std::make_unique<FilterPlan>();
     frame_spec(frame, ncols, p->spec);
     if (int e = predicate_spec(frame, ncols, cond, p->spec, p->pred, p->have_pred)) return e;
@@ -693,9 +700,16 @@ int filter_project(gdf_column* const* frame, int ncols, const char* filter_q, co
     for (int c = 0; c < ncols; c++) fd[c] = frame[c]->dtype;
     CategoryScope categories(frame, ncols);
     const bool cat = frame_has_category(frame, ncols);
+    // the filter's literals resolve before the projection's, as process_filter runs before
+    // execute_project_plan in the reference
+    categories.planning(cond);
     if (has_string_literal(cond.c_str()) || cat) plan_expression(cond, ncols);
+    categories.planning(project_q);
     if (has_string_literal(project_q) || cat) plan_project(project_q, fd);
-    const ProjectPlan& pp = cached_project_plan(project_q, fd, category_key(frame, ncols));
+    categories.replay();
+    const std::string codes = categories.recorded_key();
+    const ProjectPlan& pp = cached_project_plan(project_q, fd, category_key(frame, ncols) + codes);
+    categories.planning(cond);
     if ((int)pp.columns.size() != n_outs) return set_error(kInvalidArgument, "out_columns count differs from the projection's");
     for (int i = 0; i < n_outs; i++) {
         if (!outs[i]) return set_error(kInvalidArgument, "null out column");
@@ -715,7 +729,7 @@ int filter_project(gdf_column* const* frame, int ncols, const char* filter_q, co
     const std::string sig = frame_signature(frame, ncols, outs, n_outs);
     const bool al = sig.find("|a|") != std::string::npos;
     const PreparedFilter* pf = nullptr;
-    int rc = prepared("FP|" + cond + "|" + std::string(project_q) + "|" + sig, al, frame[0]->size,
+    int rc = prepared("FP|" + cond + "|" + std::string(project_q) + "|" + sig + "|" + codes, al, frame[0]->size,
                       [&](PreparedFilter& p) {
         frame_spec(frame, ncols, p.spec);
         if (int e = predicate_spec(frame, ncols, cond, p.spec, p.pred, p.have_pred)) return e;

@@ -8,6 +8,7 @@
 #pragma once
 
 #include <cstdint>
+#include <map>
 #include <memory>
 #include <string>
 #include <vector>
@@ -90,11 +91,25 @@ ProjectPlan plan_project(const std::string& query_part, const std::vector<gdf_dt
 // string inserted (and the column's codes rewritten) when it is missing, as
 // src/LogicalFilter.cpp:150-194 does.  The frame is the one the calling entry point holds: a
 // CategoryScope makes it visible to the front end on this thread for the duration of a call.
+//
+// The reference resolves each literal once, in its emission order, against the dictionary as it is
+// at that moment (a later insertion leaves an earlier literal's code as it was).  An entry point
+// that plans a text more than once (a resolving pass ahead of its plan caches) records the codes
+// of the first pass per text and replays them in order afterwards; the recorded codes are part of
+// the cache keys.
 struct CategoryScope {
     CategoryScope(gdf_column* const* frame, int ncols);
     ~CategoryScope();
-    gdf_column* const* prev_frame;
-    int prev_n;
+    void planning(const std::string& text);  // the text whose literals resolve next
+    void replay();                           // later resolutions return the recorded codes
+    std::string recorded_key() const;
+    gdf_column* const* frame;
+    int ncols;
+    CategoryScope* prev;
+    std::map<std::string, std::vector<int32_t>> codes;
+    std::map<std::string, size_t> next;
+    std::string current;
+    bool replaying = false;
 };
 // Planning that only asks for output types (no frame): string literals resolve to a placeholder.
 struct TypesOnlyScope {
@@ -103,6 +118,8 @@ struct TypesOnlyScope {
     bool prev;
 };
 int32_t resolve_category_literal(int frame_column, const std::string& str);
+// CategoryScope::planning on this thread's active scope, if any.
+void category_planning(const std::string& text);
 // Two category columns compared with each other: both moved to one merged dictionary.
 void sync_category_columns(int frame_column_a, int frame_column_b);
 bool frame_has_category(gdf_column* const* frame, int ncols);

@@ -215,6 +215,14 @@ const CompiledKernel* jit_get(const GeneratedKernel& gk, std::string& err) {
     ck->name = gk.name;
     ck->layout = gk.layout;
     ck->shape = gk.shape;
+    ck->dyn_smem = gk.dyn_smem;
+    if (gk.dyn_smem > 48 * 1024) {
+        ce = cudaFuncSetAttribute((const void*)ck->kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, gk.dyn_smem);
+        if (ce != cudaSuccess) {
+            err = std::string("cudaFuncSetAttribute(") + gk.name + "): " + cudaGetErrorString(ce);
+            return nullptr;
+        }
+    }
     ck->cubin_bytes = cubin.size();
     ck->compile_ms = ms;
     ck->ptxas_log = log;

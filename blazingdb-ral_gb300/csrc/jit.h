@@ -17,6 +17,7 @@ struct CompiledKernel {
     std::string name;
     ParamLayout layout;
     Shape shape;
+    int dyn_smem = 0;             // dynamic shared memory per block (staged eval kernels)
     size_t cubin_bytes = 0;
     double compile_ms = 0.0;      // 0 when it came from the disk cache
     std::string ptxas_log;
