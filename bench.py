@@ -393,12 +393,16 @@ def fused_project_e2e(ctx, steps, device):
                                  spec.uops, spec.lscalars, spec.rscalars)
 
     one()
-    t0 = time.perf_counter()
-    for _ in range(steps):
+    one()
+    times = []
+    for _ in range(max(steps, 5)):
+        t0 = time.perf_counter()
         one()
-    ms = (time.perf_counter() - t0) * 1e3 / steps
+        times.append((time.perf_counter() - t0) * 1e3)
+    ms = statistics.median(times)
     return {"value": n / (ms / 1e3), "unit": "rows/s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
-            "ms_per_step": ms, "api": "ral_perform_operation_host (row chunks on three streams)"}
+            "ms_per_step": ms, "timing": f"median of {len(times)} calls after 2 warm-up calls",
+            "api": "ral_perform_operation_host (row chunks on three streams)"}
 
 
 def _colarray(cols):
@@ -558,44 +562,36 @@ def cpu_gather(rows: int, threads: int):
 
 
 def filter_e2e(ctx, steps):
-    """Host buffers: pinned H2D of the frame, the fused filter, D2H of the kept rows of every output."""
+    """C ABI with host buffers: ral_filter_project_host over page-locked host columns into
+    page-locked host outputs -- row chunks streamed through the GPU on three streams, each chunk's
+    kept rows copied back to their place as soon as its count is known."""
     import torch
-    host_in = [(c.data.cpu().pin_memory(), None if c.valid is None else c.valid.cpu().pin_memory())
-               for c in ctx["cols"]]
-    host_out = [(torch.empty_like(o.data, device="cpu").pin_memory(),
-                 None if o.valid is None else torch.empty_like(o.valid, device="cpu").pin_memory()) for o in ctx["outs"]]
+    import ralgpu as R
+    from ralgpu import dtypes as D
+    n = ctx["cols"][0].size
+    host_in = [R.Column(c.data.cpu().pin_memory(), None if c.valid is None else c.valid.cpu().pin_memory(),
+                        c.dtype, n, c.null_count) for c in ctx["cols"]]
+    host_out = [R.Column(torch.empty(max(n, 1), dtype=D.torch_dtype(o.dtype)).pin_memory(),
+                         None if o.valid is None else torch.empty(R.valid_alloc_size(n), dtype=torch.uint8).pin_memory(),
+                         o.dtype, n) for o in ctx["outs"]]
 
     def one():
-        for (hd, hv), c in zip(host_in, ctx["cols"]):
-            c.data.copy_(hd, non_blocking=True)
-            if hv is not None:
-                c.valid.copy_(hv, non_blocking=True)
-        ctx["step"](None)
-        k = ctx["nout"].value
-        b = 0
-        for (hd, hv), o in zip(host_out, ctx["outs"]):
-            hd[:k].copy_(o.data[:k], non_blocking=True)
-            b += k * o.data.element_size()
-            if hv is not None:
-                nb = (k + 7) // 8
-                hv[:nb].copy_(o.valid[:nb], non_blocking=True)
-                b += nb
-        return b
+        return R.filter_project_host(host_in, ctx["fq"], ctx["pq"], host_out)
 
     one()
-    torch.cuda.synchronize()
-    start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    start.record()
-    d2h = 0
-    for _ in range(steps):
-        d2h = one()
-    end.record()
-    torch.cuda.synchronize()
-    ms = start.elapsed_time(end) / steps
-    n = ctx["cols"][0].size
-    h2d = sum(a.numel() * a.element_size() + (0 if b is None else b.numel()) for a, b in host_in)
+    one()
+    times = []
+    k = 0
+    for _ in range(max(steps, 5)):
+        t0 = time.perf_counter()
+        k = one()
+        times.append((time.perf_counter() - t0) * 1e3)
+    ms = statistics.median(times)
+    h2d = sum(c.data.numel() * c.data.element_size() + (0 if c.valid is None else (n + 7) // 8) for c in host_in)
+    d2h = sum(k * o.data.element_size() + (0 if o.valid is None else (k + 7) // 8) for o in host_out)
     return {"value": n / (ms / 1e3), "unit": "rows/s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
-            "ms_per_step": ms}
+            "ms_per_step": ms, "timing": f"median of {len(times)} calls after 2 warm-up calls",
+            "api": "ral_filter_project_host (row chunks streamed on three streams)"}
 
 
 # ---- full-size parity: the oracle as the checker, outside every timed region ----------------
@@ -927,7 +923,7 @@ def run_ours(args):
         "gpu_launches_main": main["gpu_launches"],
         "clocks": main["clocks"],
     }
-    for k in ("rows_out", "parity", "e2e", "cpu_baseline"):
+    for k in ("rows_out", "parity", "e2e", "cpu_baseline", "per_call_breakdown_us", "per_column_calls"):
         if k in main:
             out[k] = main[k]
     if extra:

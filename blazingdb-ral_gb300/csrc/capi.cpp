@@ -404,6 +404,15 @@ int ral_debug_aggregate_source(const gdf_dtype* frame_dtypes, const int32_t* fra
     });
 }
 
+int ral_filter_project_host(gdf_column* const* frame_columns, int32_t num_columns, const char* filter_query_part,
+                            const char* project_query_part, gdf_column* const* out_columns, int32_t num_out_columns,
+                            gdf_size_type* num_rows_out, int64_t chunk_rows) {
+    return guarded([&] {
+        return filter_host(frame_columns, num_columns, filter_query_part, project_query_part, out_columns,
+                           num_out_columns, num_rows_out, chunk_rows);
+    });
+}
+
 int ral_debug_call_timing(int32_t enable, int32_t reset, int64_t* calls, double* us4) {
     return call_timing_query(enable != 0, reset != 0, calls, us4);
 }

@@ -73,6 +73,9 @@ int32_t resolve_and_grow(CategoryScope* sc, int col, const std::string& str) {
     const ral_category* cat = static_cast<const ral_category*>(c->dtype_info.category);
     int32_t code = find_key(cat, str);
     if (code >= 0) return code;
+    if (sc->read_only)
+        throw ParseError("string literal '" + str + "' is not in the column's dictionary: adding it rewrites the "
+                         "column's codes, which needs the column in device memory");
     // add the string: codes at or above its rank move up by one
     auto* grown = new ral_category_s{cat->keys};
     auto it = std::lower_bound(grown->keys.begin(), grown->keys.end(), str);
@@ -129,6 +132,9 @@ void sync_category_columns(int a, int b) {
     const ral_category* kb = static_cast<const ral_category*>(cb->dtype_info.category);
     if (!ka || !kb) throw ParseError("string category column without a dictionary");
     if (ka == kb || ka->keys == kb->keys) return;  // codes already comparable
+    if (sc->read_only)
+        throw ParseError("two string-category columns with different dictionaries: merging them rewrites their codes, "
+                         "which needs the columns in device memory");
     std::vector<std::string> u;
     std::set_union(ka->keys.begin(), ka->keys.end(), kb->keys.begin(), kb->keys.end(), std::back_inserter(u));
     auto* ma = new ral_category_s{u};

@@ -968,6 +968,7 @@ GeneratedKernel generate_filter_kernel(const FilterSpec& f, const Shape& s, bool
     L.rscalar_slot = PL.rscalar_slot;
     gk.layout_project_lscalar = QL.lscalar_slot;
     gk.layout_project_rscalar = QL.rscalar_slot;
+    if (!item) L.obase = slot++;
     L.total = slot;
 
     std::vector<int> vouts;  // outputs with a mask
@@ -1146,6 +1147,8 @@ GeneratedKernel generate_filter_kernel(const FilterSpec& f, const Shape& s, bool
     // per-warp staging of one slice's compacted values, so that stores are contiguous
     if (s.stage) os << "    __shared__ ral_u64 s_stage[RAL_WARPS][32 * RAL_G];\n";
     os << "    const ral_i64 n = (ral_i64)P.s[" << L.n_rows << "];\n";
+    if (L.obase >= 0) os << "    const ral_u64 RAL_OBASE = (ral_u64)P.s[" << L.obase << "];\n";
+    else os << "    const ral_u64 RAL_OBASE = 0ull;\n";
     os << "    ral_u64* const scratch = (ral_u64*)P.s[" << L.scratch << "];\n";
     os << "    ral_u64* const status = scratch + " << filter_scratch_header(NO) << ";\n";
     for (int c = 0; c < NF; c++) {
@@ -1366,8 +1369,9 @@ GeneratedKernel generate_filter_kernel(const FilterSpec& f, const Shape& s, bool
         os << "        const ral_i64 chunk = chunkA;\n";
         os << "        const ral_u32 total = totalA;\n";
         os << "        const ral_i64 base = chunk * WT;\n";
-        os << "        const ral_u64 excl = ral_lookback_published(status, chunk, total, scratch + 1);\n";
-        os << "        if (chunk == nchunks - 1 && lane == 0) scratch[2] = excl + total;\n";
+        os << "        const ral_u64 excl0 = ral_lookback_published(status, chunk, total, scratch + 1);\n";
+        os << "        if (chunk == nchunks - 1 && lane == 0) scratch[2] = excl0 + total;\n";
+        os << "        const ral_u64 excl = excl0 + RAL_OBASE;\n";
         os << "        if (total != 0u) {\n";
         // A's kept-row list from its mask words: lane w holds word w, ranks by a warp scan
         os << "        {\n";
@@ -1381,8 +1385,9 @@ GeneratedKernel generate_filter_kernel(const FilterSpec& f, const Shape& s, bool
         os << "            for (ral_u32 m = kw; m; m &= m - 1u) s_lst[q++] = (unsigned short)(lane * 32 + __ffs(m) - 1);\n";
         os << "        }\n";
     } else {
-        os << "        const ral_u64 excl = ral_lookback(status, chunk, total, scratch + 1);\n";
-        os << "        if (chunk == nchunks - 1 && lane == 0) scratch[2] = excl + total;\n";
+        os << "        const ral_u64 excl0 = ral_lookback(status, chunk, total, scratch + 1);\n";
+        os << "        if (chunk == nchunks - 1 && lane == 0) scratch[2] = excl0 + total;\n";
+        os << "        const ral_u64 excl = excl0 + RAL_OBASE;\n";
         os << "        if (total == 0u) continue;\n";
     }
 

@@ -50,6 +50,10 @@ struct ParamLayout {
     int out_data = 0, out_valid = 0;    // first slot of the output pointers
     int counts = -1;                    // eval kernels: per output, count of valid bits
     int scratch = -1;                   // filter kernels: scratch block
+    // filter kernels: output row offset, 0 .. 31 -- kept row j is written at row obase + j of the
+    // output pointers and bit obase + j of the output masks (a chunk appended into a mask word
+    // that earlier rows have started); -1 in item functions
+    int obase = -1;
     std::vector<int> lscalar_slot, rscalar_slot;  // per op of the (predicate) program, -1 if none
     int total = 0;
 };

@@ -255,7 +255,7 @@ RAL_FI void ral_stg(E* __restrict__ p, ral_i64 row, const E (&v)[G]) {
 // then one cp.async.bulk per contiguous range (16-byte aligned addresses, size a multiple of 16)
 // completes them; the warp waits on the barrier's phase parity.  Waits are bounded: after
 // RAL_STAGE_SPIN_LIMIT polls the wait gives up and reports it.
-#define RAL_STAGE_SPIN_LIMIT (1l << 24)
+#define RAL_STAGE_SPIN_LIMIT (1l << 20)
 RAL_FI unsigned ral_smem_u32(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
 RAL_FI void ral_mbar_init(ral_u64* bar, unsigned count) {
     asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(ral_smem_u32(bar)), "r"(count) : "memory");

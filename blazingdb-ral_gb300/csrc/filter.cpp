@@ -9,6 +9,7 @@
 #include <algorithm>
 #include <chrono>
 #include <cstdlib>
+#include <map>
 #include <mutex>
 #include <sstream>
 #include <string>
@@ -359,9 +360,19 @@ int prepare_kernel(PreparedFilter& pf, bool aligned16, int64_t n) {
     return kSuccess;
 }
 
-// Launches a prepared fused filter over the frame.
-int run_prepared(const PreparedFilter& pf, gdf_column* const* frame, gdf_column* const* outs, gdf_size_type* n_out_p,
-                 cudaStream_t st) {
+// Scratch words a prepared filter needs over n rows: the header and one status word per chunk.
+int64_t prepared_scratch_words(const PreparedFilter& pf, int64_t n) {
+    const int64_t tile_rows = filter_tile_rows(pf.gk.shape);
+    return filter_scratch_header((int)pf.spec.outputs.size()) + (n + tile_rows - 1) / tile_rows;
+}
+
+// Enqueues a prepared fused filter over the frame on st: zeroes `scratch` (prepared_scratch_words)
+// and the output masks, launches with kept row j written at row obase + j of the outputs (obase in
+// 0 .. 31: a chunk that continues a mask word earlier rows have started; the data pointers are
+// taken obase rows lower, so row j still lands at element j), and copies the header -- kept count,
+// error word, valid counts -- to host_header.  ev (optional) brackets the launch.
+int enqueue_prepared(const PreparedFilter& pf, gdf_column* const* frame, gdf_column* const* outs, void* scratch,
+                     int obase, unsigned long long* host_header, cudaStream_t st, cudaEvent_t* ev) {
     const int64_t n = frame[0]->size;
     const FilterSpec& spec = pf.spec;
     const int NO = (int)spec.outputs.size();
@@ -371,19 +382,14 @@ int run_prepared(const PreparedFilter& pf, gdf_column* const* frame, gdf_column*
     for (int q = 0; q < NO; q++)
         if (outs[q]->valid && !aligned_to(outs[q]->valid, 4))
             return set_error(kInvalidArgument, "validity masks must be 4-byte aligned");
+    if (obase < 0 || obase > 31) return set_error(kInvalidArgument, "output row offset out of range");
     const ParamLayout& L = pf.gk.layout;
     const int64_t tile_rows = filter_tile_rows(pf.gk.shape);
-    const int64_t ntiles = (n + tile_rows - 1) / tile_rows;
     const int64_t header = filter_scratch_header(NO);
-    void* scratch = nullptr;
-    if (int e = scratch_get((size_t)(header + ntiles) * 8, st, &scratch)) return e;
-    const bool timing = call_timing_enabled();
-    call_timing_mark_prepared();
-    const auto t_enq0 = std::chrono::steady_clock::now();
-    cudaMemsetAsync(scratch, 0, (size_t)(header + ntiles) * 8, st);
+    cudaMemsetAsync(scratch, 0, (size_t)prepared_scratch_words(pf, n) * 8, st);
     // output masks are assembled with OR at the edges of each warp's range: start from zero
     for (int q = 0; q < NO; q++)
-        if (spec.outputs[q].has_valid) cudaMemsetAsync(outs[q]->valid, 0, (size_t)((n + 31) / 32) * 4, st);
+        if (spec.outputs[q].has_valid) cudaMemsetAsync(outs[q]->valid, 0, (size_t)((n + obase + 31) / 32) * 4, st);
 
     std::vector<uint64_t> slots(L.total, 0);
     slots[L.n_rows] = (uint64_t)n;
@@ -392,10 +398,12 @@ int run_prepared(const PreparedFilter& pf, gdf_column* const* frame, gdf_column*
         slots[L.in_valid + c] = (uint64_t)(uintptr_t)frame[c]->valid;
     }
     for (int q = 0; q < NO; q++) {
-        slots[L.out_data + q] = (uint64_t)(uintptr_t)outs[q]->data;
+        const uintptr_t d = (uintptr_t)outs[q]->data - (uintptr_t)obase * gdf_dtype_size(outs[q]->dtype);
+        slots[L.out_data + q] = (uint64_t)d;
         slots[L.out_valid + q] = (uint64_t)(uintptr_t)outs[q]->valid;
     }
     slots[L.scratch] = (uint64_t)(uintptr_t)scratch;
+    if (L.obase >= 0) slots[L.obase] = (uint64_t)obase;
     if (pf.have_pred) fill_scalars(pf.pred, L, slots);
     if (pf.have_proj) {
         ParamLayout QL;
@@ -405,22 +413,49 @@ int run_prepared(const PreparedFilter& pf, gdf_column* const* frame, gdf_column*
     }
     const int grid = launch_blocks(*pf.k, pf.gk.shape.threads, tile_rows * (pf.gk.shape.threads / 32), n);
     void* args[] = {slots.data()};
+    if (ev) cudaEventRecord(ev[0], st);
+    if (int e = check_cuda(cudaLaunchKernel((const void*)pf.k->kernel, dim3(grid), dim3(pf.gk.shape.threads), args, 0, st),
+                           "launch of the filter kernel"))
+        return e;
+    if (ev) cudaEventRecord(ev[1], st);
+    note_launch();
+    return check_cuda(cudaMemcpyAsync(host_header, scratch, (size_t)header * 8, cudaMemcpyDeviceToHost, st),
+                      "cudaMemcpyAsync");
+}
+
+// Sizes, null counts and dictionaries of a prepared filter's outputs from its header.
+void finish_outputs(const PreparedFilter& pf, gdf_column* const* frame, gdf_column* const* outs,
+                    const unsigned long long* hp, int64_t n_out) {
+    const FilterSpec& spec = pf.spec;
+    for (size_t q = 0; q < spec.outputs.size(); q++) {
+        outs[q]->size = (gdf_size_type)n_out;
+        outs[q]->null_count = spec.outputs[q].has_valid ? (gdf_size_type)(n_out - (int64_t)hp[3 + q]) : 0;
+        // a gathered string-category column keeps its source's dictionary (codes unchanged)
+        if (!spec.outputs[q].from_project && frame[spec.outputs[q].index]->dtype == GDF_STRING_CATEGORY)
+            outs[q]->dtype_info.category = frame[spec.outputs[q].index]->dtype_info.category;
+    }
+}
+
+// Launches a prepared fused filter over the frame and waits for it.
+int run_prepared(const PreparedFilter& pf, gdf_column* const* frame, gdf_column* const* outs, gdf_size_type* n_out_p,
+                 cudaStream_t st) {
+    const int64_t n = frame[0]->size;
+    const int64_t header = filter_scratch_header((int)pf.spec.outputs.size());
+    void* scratch = nullptr;
+    if (int e = scratch_get((size_t)prepared_scratch_words(pf, n) * 8, st, &scratch)) return e;
+    const bool timing = call_timing_enabled();
+    call_timing_mark_prepared();
+    const auto t_enq0 = std::chrono::steady_clock::now();
     thread_local cudaEvent_t ev[2] = {nullptr, nullptr};
     if (timing && !ev[0]) {
         cudaEventCreate(&ev[0]);
         cudaEventCreate(&ev[1]);
     }
-    if (timing) cudaEventRecord(ev[0], st);
-    if (int e = check_cuda(cudaLaunchKernel((const void*)pf.k->kernel, dim3(grid), dim3(pf.gk.shape.threads), args, 0, st),
-                           "launch of the filter kernel"))
-        return e;
-    if (timing) cudaEventRecord(ev[1], st);
-    note_launch();
     unsigned long long h[64];
     std::vector<unsigned long long> hv;
     unsigned long long* hp = h;
     if (header > 64) { hv.resize(header); hp = hv.data(); }
-    cudaMemcpyAsync(hp, scratch, (size_t)header * 8, cudaMemcpyDeviceToHost, st);
+    if (int e = enqueue_prepared(pf, frame, outs, scratch, 0, hp, st, timing ? ev : nullptr)) return e;
     const auto t_wait0 = std::chrono::steady_clock::now();
     if (int e = check_cuda(cudaStreamSynchronize(st), "filter kernel")) return e;
     if (timing) {
@@ -432,13 +467,7 @@ int run_prepared(const PreparedFilter& pf, gdf_column* const* frame, gdf_column*
     }
     if (hp[1]) return set_error(kTimeout, "filter look-back wait gave up");
     const int64_t n_out = (int64_t)hp[2];
-    for (int q = 0; q < NO; q++) {
-        outs[q]->size = (gdf_size_type)n_out;
-        outs[q]->null_count = spec.outputs[q].has_valid ? (gdf_size_type)(n_out - (int64_t)hp[3 + q]) : 0;
-        // a gathered string-category column keeps its source's dictionary (codes unchanged)
-        if (!spec.outputs[q].from_project && frame[spec.outputs[q].index]->dtype == GDF_STRING_CATEGORY)
-            outs[q]->dtype_info.category = frame[spec.outputs[q].index]->dtype_info.category;
-    }
+    finish_outputs(pf, frame, outs, hp, n_out);
     *n_out_p = (gdf_size_type)n_out;
     return kSuccess;
 }
@@ -484,12 +513,12 @@ const ProjectPlan& cached_project_plan(const char* project_q, const std::vector<
     return *res.first->second;
 }
 
-int process_filter_fused(gdf_column* const* frame, int ncols, const std::string& cond, gdf_column* const* outs,
-                         gdf_size_type* n_out, cudaStream_t st, const std::string& codes) {
+// The prepared fused LogicalFilter over this frame (every column gathered into outs).
+int prepare_filter(gdf_column* const* frame, int ncols, const std::string& cond, gdf_column* const* outs,
+                   const std::string& codes, const PreparedFilter** out) {
     const std::string sig = frame_signature(frame, ncols, outs, ncols);
     const bool al = sig.find("|a|") != std::string::npos;
-    const PreparedFilter* pf = nullptr;
-    int rc = prepared("F|" + cond + "|" + sig + "|" + codes, al, frame[0]->size, [&](PreparedFilter& p) {
+    return prepared("F|" + cond + "|" + sig + "|" + codes, al, frame[0]->size, [&](PreparedFilter& p) {
         frame_spec(frame, ncols, p.spec);
         if (int e = predicate_spec(frame, ncols, cond, p.spec, p.pred, p.have_pred)) return e;
         if (p.have_pred) p.spec.predicate = &p.pred;
@@ -502,8 +531,13 @@ int process_filter_fused(gdf_column* const* frame, int ncols, const std::string&
             p.spec.outputs.push_back(o);
         }
         return (int)kSuccess;
-    }, &pf);
-    if (rc) return rc;
+    }, out);
+}
+
+int process_filter_fused(gdf_column* const* frame, int ncols, const std::string& cond, gdf_column* const* outs,
+                         gdf_size_type* n_out, cudaStream_t st, const std::string& codes) {
+    const PreparedFilter* pf = nullptr;
+    if (int rc = prepare_filter(frame, ncols, cond, outs, codes, &pf)) return rc;
     return run_prepared(*pf, frame, outs, n_out, st);
 }
 
@@ -684,6 +718,10 @@ void filter_fill_slots(const FilterPlan& plan, const GeneratedKernel& gk, gdf_co
     }
 }
 
+int prepare_filter_project(gdf_column* const* frame, int ncols, const std::string& cond, const char* project_q,
+                           const ProjectPlan& pp, gdf_column* const* outs, int n_outs, const std::string& codes,
+                           const PreparedFilter** out);
+
 int filter_project(gdf_column* const* frame, int ncols, const char* filter_q, const char* project_q,
                    gdf_column* const* outs, int n_outs, gdf_size_type* n_out, const FilterOptions& opt) {
     call_timing_start();
@@ -726,10 +764,18 @@ int filter_project(gdf_column* const* frame, int ncols, const char* filter_q, co
         return kSuccess;
     }
     if (filter_mode(opt) == 1) return filter_project_unfused(frame, ncols, cond, project_q, outs, n_outs, n_out, opt.stream);
+    const PreparedFilter* pf = nullptr;
+    if (int rc = prepare_filter_project(frame, ncols, cond, project_q, pp, outs, n_outs, codes, &pf)) return rc;
+    return run_prepared(*pf, frame, outs, n_out, opt.stream);
+}
+
+// The prepared fused LogicalFilter + LogicalProject over this frame and these outputs.
+int prepare_filter_project(gdf_column* const* frame, int ncols, const std::string& cond, const char* project_q,
+                           const ProjectPlan& pp, gdf_column* const* outs, int n_outs, const std::string& codes,
+                           const PreparedFilter** out) {
     const std::string sig = frame_signature(frame, ncols, outs, n_outs);
     const bool al = sig.find("|a|") != std::string::npos;
-    const PreparedFilter* pf = nullptr;
-    int rc = prepared("FP|" + cond + "|" + std::string(project_q) + "|" + sig + "|" + codes, al, frame[0]->size,
+    return prepared("FP|" + cond + "|" + std::string(project_q) + "|" + sig + "|" + codes, al, frame[0]->size,
                       [&](PreparedFilter& p) {
         frame_spec(frame, ncols, p.spec);
         if (int e = predicate_spec(frame, ncols, cond, p.spec, p.pred, p.have_pred)) return e;
@@ -760,9 +806,279 @@ int filter_project(gdf_column* const* frame, int ncols, const char* filter_q, co
             p.spec.outputs.push_back(o);
         }
         return (int)kSuccess;
-    }, &pf);
-    if (rc) return rc;
-    return run_prepared(*pf, frame, outs, n_out, opt.stream);
+    }, out);
+}
+
+
+// ---- LogicalFilter (and LogicalProject over it) over columns in host memory ----------------------
+//
+// The rows stream through the GPU in chunks on three streams, each with its own device area: a
+// chunk's copies in, the fused filter kernel over the chunk, then its kept rows copied back to the
+// output's running row offset.  That offset is known once the earlier chunks' kept counts are read
+// back, so the host reads each chunk's count after its kernel (the copies of the next chunks are
+// already under way) and launches the kernel of chunk i with its output rows starting at bit
+// (offset mod 32) of the chunk's mask buffer: whole mask words then copy back to their place, and
+// the one word a chunk shares with the rows before it is merged on the host at the end.
+
+namespace {
+
+struct HostFilterArea {
+    size_t bytes = 0;
+    void* dev = nullptr;
+    unsigned long long* pinned = nullptr;  // headers of the three slots, then first mask words
+    size_t pinned_words = 0;
+    cudaStream_t s[3] = {nullptr, nullptr, nullptr};
+    cudaEvent_t kernel_done[3] = {nullptr, nullptr, nullptr};
+    ~HostFilterArea() {
+        if (dev) cudaFree(dev);
+        if (pinned) cudaFreeHost(pinned);
+        for (int k = 0; k < 3; k++) {
+            if (s[k]) cudaStreamDestroy(s[k]);
+            if (kernel_done[k]) cudaEventDestroy(kernel_done[k]);
+        }
+    }
+};
+
+size_t round256(size_t b) { return (b + 255) & ~(size_t)255; }
+
+}  // namespace
+
+int filter_host(gdf_column* const* frame, int ncols, const char* filter_q, const char* project_q,
+                gdf_column* const* outs, int n_outs, gdf_size_type* n_out_p, int64_t chunk_rows) {
+    if (!frame || ncols <= 0 || !filter_q || !outs || !n_out_p) return set_error(kInvalidArgument, "null argument");
+    for (int c = 0; c < ncols; c++) {
+        if (!frame[c]) return set_error(kInvalidArgument, "null frame column");
+        if (frame[c]->size != frame[0]->size) return set_error(kInvalidArgument, "frame columns differ in size");
+        if (gdf_dtype_size(frame[c]->dtype) == 0) return set_error(kUnsupported, "column dtype has no fixed width");
+    }
+    const std::string cond = named_expression(filter_q, "condition");
+    if (cond.empty()) return set_error(kParseError, "no condition=[...] in the LogicalFilter");
+    const int64_t n = frame[0]->size;
+    std::vector<gdf_dtype> fd(ncols);
+    for (int c = 0; c < ncols; c++) fd[c] = frame[c]->dtype;
+    // string literals resolve against the host columns' dictionaries; a literal the dictionary lacks
+    // (or two category columns with different dictionaries) would rewrite codes, which needs the
+    // column on the device: rejected here
+    CategoryScope categories(frame, ncols);
+    categories.read_only = true;
+    categories.planning(cond);
+    plan_expression(cond, ncols);
+    if (project_q) {
+        categories.planning(project_q);
+        plan_project(project_q, fd);
+    }
+    categories.replay();
+    const std::string codes = categories.recorded_key();
+    // output dtypes and mask presence
+    std::vector<gdf_dtype> odt;
+    std::vector<bool> ovalid;
+    const ProjectPlan* pp = nullptr;
+    if (project_q) {
+        pp = &cached_project_plan(project_q, fd, category_key(frame, ncols) + codes);
+        for (const auto& col : pp->columns) {
+            odt.push_back(col.first ? pp->eval_dtypes[col.second] : fd[col.second]);
+            ovalid.push_back(col.first ? true : frame[col.second]->valid != nullptr);
+        }
+    } else {
+        for (int c = 0; c < ncols; c++) {
+            odt.push_back(fd[c]);
+            ovalid.push_back(frame[c]->valid != nullptr);
+        }
+    }
+    const int NO = (int)odt.size();
+    if (n_outs != NO) return set_error(kInvalidArgument, "out_columns count differs from the plan's");
+    for (int q = 0; q < NO; q++) {
+        if (!outs[q]) return set_error(kInvalidArgument, "null out column");
+        if (outs[q]->dtype != odt[q]) return set_error(kInvalidArgument, "out column " + std::to_string(q) + " has the wrong dtype");
+        if ((outs[q]->valid != nullptr) != ovalid[q])
+            return set_error(kInvalidArgument, "out column " + std::to_string(q) + ": a validity buffer is expected exactly "
+                                               "when the output has one");
+        if (n > 0 && !outs[q]->data) return set_error(kInvalidArgument, "out column without data");
+        if (outs[q]->valid && !aligned_to(outs[q]->valid, 4)) return set_error(kInvalidArgument, "masks must be 4-byte aligned");
+    }
+    for (int c = 0; c < ncols; c++)
+        if (n > 0 && !frame[c]->data) return set_error(kInvalidArgument, "frame column without data");
+    if (n == 0) {
+        for (int q = 0; q < NO; q++) { outs[q]->size = 0; outs[q]->null_count = 0; }
+        *n_out_p = 0;
+        return kSuccess;
+    }
+    int64_t C = chunk_rows > 0 ? chunk_rows : ((int64_t)4 << 20);
+    C = std::max<int64_t>(1024, (C + 1023) / 1024 * 1024);
+    if (C > n) C = (n + 1023) / 1024 * 1024;
+    const int64_t nch = (n + C - 1) / C;
+
+    // one device area per stream: the frame's chunk, the outputs' chunk (32 rows of room for the
+    // row offset), the filter's scratch
+    std::vector<size_t> in_data_off(ncols), in_mask_off(ncols), out_data_off(NO), out_mask_off(NO);
+    size_t per_slot = 0;
+    for (int c = 0; c < ncols; c++) {
+        in_data_off[c] = per_slot;
+        per_slot += round256((size_t)C * gdf_dtype_size(fd[c]));
+        in_mask_off[c] = per_slot;
+        if (frame[c]->valid) per_slot += round256((size_t)gdf_valid_allocation_size(C));
+    }
+    for (int q = 0; q < NO; q++) {
+        out_data_off[q] = per_slot;
+        per_slot += round256((size_t)(C + 32) * gdf_dtype_size(odt[q]));
+        out_mask_off[q] = per_slot;
+        if (ovalid[q]) per_slot += round256((size_t)gdf_valid_allocation_size(C + 64));
+    }
+    const size_t scratch_off = per_slot;
+    // scratch: header + chunk states of the largest plan (the chunk size class bounds the tiles)
+    per_slot += round256((size_t)(filter_scratch_header(NO) + C / 32 + 64) * 8);
+
+    int dev = 0;
+    if (int e = check_cuda(cudaGetDevice(&dev), "cudaGetDevice")) return e;
+    static thread_local std::map<int, HostFilterArea> areas;
+    HostFilterArea& A = areas[dev];
+    for (int k = 0; k < 3; k++) {
+        if (!A.s[k] && check_cuda(cudaStreamCreateWithFlags(&A.s[k], cudaStreamNonBlocking), "cudaStreamCreate"))
+            return kCudaError;
+        if (!A.kernel_done[k] &&
+            check_cuda(cudaEventCreateWithFlags(&A.kernel_done[k], cudaEventDisableTiming), "cudaEventCreate"))
+            return kCudaError;
+    }
+    if (A.bytes < 3 * per_slot) {
+        if (A.dev) cudaFree(A.dev);
+        A.dev = nullptr;
+        A.bytes = 0;
+        if (int e = check_cuda(cudaMalloc(&A.dev, 3 * per_slot), "cudaMalloc")) return e;
+        A.bytes = 3 * per_slot;
+    }
+    const int64_t header = filter_scratch_header(NO);
+    const size_t want_pinned = (size_t)(3 * header + nch * NO + 8);
+    if (A.pinned_words < want_pinned) {
+        if (A.pinned) cudaFreeHost(A.pinned);
+        A.pinned = nullptr;
+        A.pinned_words = 0;
+        if (int e = check_cuda(cudaMallocHost((void**)&A.pinned, want_pinned * 8), "cudaMallocHost")) return e;
+        A.pinned_words = want_pinned;
+    }
+    auto slot_base = [&](int k) { return (char*)A.dev + (size_t)k * per_slot; };
+    uint32_t* first_words = (uint32_t*)(A.pinned + 3 * header);  // nch x NO words
+
+    // per slot: the device descriptors of the chunk frame and outputs
+    std::vector<gdf_column> dframe(3 * ncols), douts(3 * NO);
+    std::vector<gdf_column*> pframe(3 * ncols), pouts(3 * NO);
+    for (int k = 0; k < 3; k++) {
+        for (int c = 0; c < ncols; c++) {
+            gdf_column& d = dframe[k * ncols + c];
+            d = *frame[c];  // dtype, null_count (read by the validity pass), dictionary
+            d.data = slot_base(k) + in_data_off[c];
+            d.valid = frame[c]->valid ? (gdf_valid_type*)(slot_base(k) + in_mask_off[c]) : nullptr;
+            pframe[k * ncols + c] = &d;
+        }
+        for (int q = 0; q < NO; q++) {
+            gdf_column& d = douts[k * NO + q];
+            d = *outs[q];
+            d.data = slot_base(k) + out_data_off[q];
+            d.valid = ovalid[q] ? (gdf_valid_type*)(slot_base(k) + out_mask_off[q]) : nullptr;
+            pouts[k * NO + q] = &d;
+        }
+    }
+    auto rows_of = [&](int64_t i) { return std::min<int64_t>(C, n - i * C); };
+    auto copy_in = [&](int64_t i) -> int {
+        const int k = (int)(i % 3);
+        const int64_t r0 = i * C, rows = rows_of(i);
+        for (int c = 0; c < ncols; c++) {
+            const int w = gdf_dtype_size(fd[c]);
+            if (int e = check_cuda(cudaMemcpyAsync(slot_base(k) + in_data_off[c], (const char*)frame[c]->data + r0 * w,
+                                                   (size_t)(rows * w), cudaMemcpyHostToDevice, A.s[k]),
+                                   "cudaMemcpyAsync"))
+                return e;
+            if (frame[c]->valid)
+                if (int e = check_cuda(cudaMemcpyAsync(slot_base(k) + in_mask_off[c], (const char*)frame[c]->valid + r0 / 8,
+                                                       (size_t)((rows + 7) / 8), cudaMemcpyHostToDevice, A.s[k]),
+                                       "cudaMemcpyAsync"))
+                    return e;
+        }
+        return kSuccess;
+    };
+    for (int64_t i = 0; i < std::min<int64_t>(3, nch); i++)
+        if (int e = copy_in(i)) return e;
+
+    struct ChunkOut {
+        int64_t offset, kept, words;
+    };
+    std::vector<ChunkOut> done;
+    done.reserve(nch);
+    std::vector<int64_t> valid_count(NO, 0);
+    int64_t offset = 0;
+    for (int64_t i = 0; i < nch; i++) {
+        const int k = (int)(i % 3);
+        const int64_t rows = rows_of(i);
+        for (int c = 0; c < ncols; c++) dframe[k * ncols + c].size = (gdf_size_type)rows;
+        const PreparedFilter* pf = nullptr;
+        int rc = project_q ? prepare_filter_project(&pframe[k * ncols], ncols, cond, project_q, *pp, &pouts[k * NO], NO,
+                                                    codes, &pf)
+                           : prepare_filter(&pframe[k * ncols], ncols, cond, &pouts[k * NO], codes, &pf);
+        if (rc) return rc;
+        if ((int64_t)prepared_scratch_words(*pf, rows) * 8 > (int64_t)(per_slot - scratch_off))
+            return set_error(kInvalidArgument, "filter scratch larger than its area");
+        const int obase = (int)(offset & 31);
+        unsigned long long* hdr = A.pinned + k * header;
+        if (int e = enqueue_prepared(*pf, &pframe[k * ncols], &pouts[k * NO], slot_base(k) + scratch_off, obase, hdr,
+                                     A.s[k], nullptr))
+            return e;
+        if (int e = check_cuda(cudaEventRecord(A.kernel_done[k], A.s[k]), "cudaEventRecord")) return e;
+        if (int e = check_cuda(cudaEventSynchronize(A.kernel_done[k]), "filter kernel")) return e;
+        if (hdr[1]) return set_error(kTimeout, "filter look-back wait gave up");
+        const int64_t kept = (int64_t)hdr[2];
+        const int64_t words = (obase + kept + 31) / 32;
+        for (int q = 0; q < NO; q++) {
+            valid_count[q] += ovalid[q] ? (int64_t)hdr[3 + q] : 0;
+            const int w = gdf_dtype_size(odt[q]);
+            if (kept > 0)
+                if (int e = check_cuda(cudaMemcpyAsync((char*)outs[q]->data + offset * w, slot_base(k) + out_data_off[q],
+                                                       (size_t)(kept * w), cudaMemcpyDeviceToHost, A.s[k]),
+                                       "cudaMemcpyAsync"))
+                    return e;
+            if (!ovalid[q]) continue;
+            // word 0 (shared with the rows before the chunk) to the pinned area, words 1.. to their place
+            const char* dm = slot_base(k) + out_mask_off[q];
+            if (int e = check_cuda(cudaMemcpyAsync(first_words + i * NO + q, dm, 4, cudaMemcpyDeviceToHost, A.s[k]),
+                                   "cudaMemcpyAsync"))
+                return e;
+            if (words > 1)
+                if (int e = check_cuda(cudaMemcpyAsync((uint32_t*)outs[q]->valid + offset / 32 + 1, dm + 4,
+                                                       (size_t)(words - 1) * 4, cudaMemcpyDeviceToHost, A.s[k]),
+                                       "cudaMemcpyAsync"))
+                    return e;
+        }
+        done.push_back({offset, kept, words});
+        offset += kept;
+        // the stream's next chunk goes in after this chunk's copies back (stream order)
+        if (i + 3 < nch)
+            if (int e = copy_in(i + 3)) return e;
+    }
+    for (int k = 0; k < 3; k++)
+        if (int e = check_cuda(cudaStreamSynchronize(A.s[k]), "cudaStreamSynchronize")) return e;
+    // merge each chunk's first mask word into the output: a word no copy has written yet starts at 0
+    for (int q = 0; q < NO; q++) {
+        if (!ovalid[q]) continue;
+        uint32_t* hv = (uint32_t*)outs[q]->valid;
+        int64_t last_written = -1, last_zeroed = -1;
+        for (int64_t i = 0; i < nch; i++) {
+            const int64_t W = done[i].offset / 32;
+            if (W > last_written && W != last_zeroed) {
+                hv[W] = 0;
+                last_zeroed = W;
+            }
+            hv[W] |= first_words[i * NO + q];
+            if (done[i].words > 1) last_written = W + done[i].words - 1;
+        }
+    }
+    for (int q = 0; q < NO; q++) {
+        outs[q]->size = (gdf_size_type)offset;
+        outs[q]->null_count = ovalid[q] ? (gdf_size_type)(offset - valid_count[q]) : 0;
+        if (!(project_q && pp->columns[q].first)) {
+            const int src = project_q ? pp->columns[q].second : q;
+            if (frame[src]->dtype == GDF_STRING_CATEGORY) outs[q]->dtype_info.category = frame[src]->dtype_info.category;
+        }
+    }
+    *n_out_p = (gdf_size_type)offset;
+    return kSuccess;
 }
 
 }  // namespace ral

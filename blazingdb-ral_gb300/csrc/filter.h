@@ -33,6 +33,11 @@ int filter_project(gdf_column* const* frame, int num_columns, const char* filter
                    const char* project_query_part, gdf_column* const* out_columns, int num_out_columns,
                    gdf_size_type* num_rows_out, const FilterOptions& opt);
 
+// process_filter (project_q null) or filter_project over columns in host memory, streamed through
+// the GPU in chunks of chunk_rows (0: 4Mi) on three streams; outputs in host memory.
+int filter_host(gdf_column* const* frame, int ncols, const char* filter_q, const char* project_q,
+                gdf_column* const* outs, int n_outs, gdf_size_type* n_out, int64_t chunk_rows);
+
 // A LogicalProject over a LogicalFilter, planned for a frame: the fused filter's spec and the
 // dtype / mask presence of every output (evaluated outputs carry a mask; a pass-through output
 // carries one exactly when its frame column does).  Holds the programs the spec points to.

@@ -110,6 +110,7 @@ struct CategoryScope {
     std::map<std::string, size_t> next;
     std::string current;
     bool replaying = false;
+    bool read_only = false;  // columns in host memory: a rewrite of codes is refused
 };
 // Planning that only asks for output types (no frame): string literals resolve to a placeholder.
 struct TypesOnlyScope {

@@ -54,6 +54,8 @@ _SIGS = {
     "ral_process_aggregate": (C.c_int, [C.c_void_p, C.c_int32, C.c_char_p, C.POINTER(GdfScalar), C.c_int32,
                                         C.POINTER(C.c_int32)]),
     "ral_debug_call_timing": (C.c_int, [C.c_int32, C.c_int32, C.POINTER(C.c_int64), C.POINTER(C.c_double)]),
+    "ral_filter_project_host": (C.c_int, [C.c_void_p, C.c_int32, C.c_char_p, C.c_char_p, C.c_void_p, C.c_int32,
+                                          C.POINTER(C.c_int32), C.c_int64]),
     "ral_category_create": (C.c_int, [C.c_void_p, C.c_int64, C.POINTER(C.c_void_p), I32P]),
     "ral_category_size": (C.c_int, [C.c_void_p, C.POINTER(C.c_int64)]),
     "ral_category_get_value": (C.c_int, [C.c_void_p, C.c_char_p, C.POINTER(C.c_int32)]),
@@ -452,6 +454,22 @@ def debug_aggregate_source(frame_dtypes, frame_nullable, frame_null_counts, quer
     _check(lib().ral_debug_aggregate_source(_p32(fd), _p32(fn), nc.ctypes.data, len(fd), query_part.encode(),
                                             1 if compile else 0, src, len(src), log, len(log)))
     return src.value.decode(), log.value.decode()
+
+
+def filter_project_host(frame: List[Column], filter_query_part: str, project_query_part: Optional[str],
+                        out_columns: List[Column], chunk_rows: int = 0) -> int:
+    """The fused filter (+ projection) over host-memory columns (torch CPU tensors, pinned for
+    overlap) into host-memory outputs, streamed through the GPU in row chunks; returns the kept row
+    count (out columns' size and null_count are set)."""
+    fa, fs = _colarray(frame)
+    oa, os_ = _colarray(out_columns)
+    n = C.c_int32(0)
+    _check(lib().ral_filter_project_host(C.cast(fa, C.c_void_p), len(frame), filter_query_part.encode(),
+                                         project_query_part.encode() if project_query_part else None,
+                                         C.cast(oa, C.c_void_p), len(out_columns), C.byref(n), int(chunk_rows)))
+    for c, st in zip(out_columns, os_):
+        c.sync_from_c(st)
+    return n.value
 
 
 def call_timing(enable: bool = True, reset: bool = False) -> dict:

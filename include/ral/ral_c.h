@@ -157,6 +157,23 @@ int ral_filter_project(gdf_column *const *frame_columns, int32_t num_columns, co
                        gdf_size_type *num_rows_out);
 
 /*
+ * process_filter / the fused LogicalFilter + LogicalProject over columns in HOST memory (no
+ * reference counterpart: the reference's process_filter, src/CalciteInterpreter.cpp:509-573, works
+ * on device columns).  frame_columns and out_columns hold host pointers (page-locked for overlap);
+ * project_query_part NULL filters the frame (every column gathered, out_columns as for
+ * ral_process_filter), otherwise out_columns are as for ral_filter_project.  The rows stream
+ * through the GPU in chunks of chunk_rows (rounded up to a multiple of 1024; 0 = 4Mi rows) on three
+ * streams: each chunk's copies in, the fused filter kernel, and its kept rows copied back to their
+ * place in the outputs, overlapping the other chunks' copies.  Same results as the device entry
+ * points; sizes and null counts are set.  A string literal missing from a category column's
+ * dictionary is refused (adding it would rewrite the column, which lives in host memory).
+ * Synchronous.
+ */
+int ral_filter_project_host(gdf_column *const *frame_columns, int32_t num_columns, const char *filter_query_part,
+                            const char *project_query_part, gdf_column *const *out_columns, int32_t num_out_columns,
+                            gdf_size_type *num_rows_out, int64_t chunk_rows);
+
+/*
  * materialize_column — src/ColumnManipulation.cuh:16-18 (ColumnManipulation.cu:137-150).
  * output[i] = input[row_indices[i]] for row_indices[i] >= 0; valid bit i =
  * valid bit row_indices[i] (0 for a negative index); output->null_count is
