@@ -161,9 +161,10 @@ RAL_SF unsigned int ral_sf_umulhi32(unsigned int a, unsigned int b) {
 //   * digit 1: q1 = umulhi(ma >> 22, v) estimates T1 = ma * 2^30 / mb within [-4, +3] units (the
 //     reciprocal's error, the truncated dividend and divisor, the floor); taken 4 low, its
 //     remainder R1 = ma * 2^30 - q1 * mb lies in [mb, 8 mb] < 2^56 and is exact in 64 bits;
-//   * digit 2: q2 = umulhi(R1 >> 25, v) >> 4 estimates R1 * 2^23 / mb (below 2^26) within one
-//     unit either way, so R = R1 * 2^23 - q2 * mb (exact modulo 2^64, its true value small) needs
-//     one test per direction.
+//   * digit 2: umulhi(R1 >> 25, v) / 16 estimates T2 = R1 * 2^23 / mb (below 2^26) within
+//     [-0.094, +0.063] units (the reciprocal is within 1.002 units of 2^63 / dh for every dh, the
+//     dividend and divisor are truncated); taken 2/16 low and floored, q2 is floor(T2) or one less,
+//     so R = R1 * 2^23 - q2 * mb (exact modulo 2^64) lies in [0, 2 mb) and needs one test.
 // Only 32 x 32-bit products and 64-bit adds and shifts: no 64 x 64-bit multiply.
 RAL_SF double ral_sf_div(double a, double b) {
     const unsigned long long A = ral_sf_bits(a), B = ral_sf_bits(b);
@@ -196,15 +197,13 @@ RAL_SF double ral_sf_div(double a, double b) {
     }
     const unsigned q1 = ral_sf_umulhi32((unsigned)(ma >> 22), v) - 4u;
     const unsigned long long r1 = (ma << 30) - (unsigned long long)q1 * mb;          // in [mb, 8 mb]
-    const unsigned q2 = ral_sf_umulhi32((unsigned)(r1 >> 25), v) >> 4;
+    // the digit estimate, 2/16 low: never above floor(R1 * 2^23 / mb), at most one below it
+    const unsigned q2 = (ral_sf_umulhi32((unsigned)(r1 >> 25), v) - 2u) >> 4;
     unsigned long long q = ((unsigned long long)q1 << 23) + q2;
-    long long r = (long long)((r1 << 23) - (unsigned long long)q2 * mb);
-    if (r < 0) {
-        q -= 1;
-        r += (long long)mb;
-    } else if (r >= (long long)mb) {
+    unsigned long long r = (r1 << 23) - (unsigned long long)q2 * mb;  // in [0, 2 mb)
+    if (r >= mb) {
         q += 1;
-        r -= (long long)mb;
+        r -= mb;
     }
     // q in [2^53, 2^54): 53 significand bits, one rounding bit, sticky = r != 0
     unsigned long long m = q >> 1;
