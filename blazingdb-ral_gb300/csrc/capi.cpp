@@ -861,6 +861,12 @@ int ral_server_stats(ral_server* server, int64_t* stats6) {
     return kSuccess;
 }
 
+int ral_server_debug_solo(ral_server* server, int64_t* solo_requests) {
+    if (!server || !solo_requests) return set_error(kInvalidArgument, "null argument");
+    *solo_requests = server->s.stats().solo;
+    return kSuccess;
+}
+
 int ral_server_destroy(ral_server* server) {
     delete server;
     return kSuccess;

@@ -722,6 +722,61 @@ int prepare_filter_project(gdf_column* const* frame, int ncols, const std::strin
                            const ProjectPlan& pp, gdf_column* const* outs, int n_outs, const std::string& codes,
                            const PreparedFilter** out);
 
+int prepare_filter_project(gdf_column* const* frame, int ncols, const std::string& cond, const char* project_q,
+                           const ProjectPlan& pp, gdf_column* const* outs, int n_outs, const std::string& codes,
+                           const PreparedFilter** out);
+
+// String literals of a filter + project, resolved once in the reference's order (the filter's
+// before the projection's, as process_filter runs before execute_project_plan), then replayed;
+// returns the projection's plan, keyed on the recorded codes.
+const ProjectPlan& resolve_filter_project(gdf_column* const* frame, int ncols, const std::string& cond,
+                                          const char* project_q, const std::vector<gdf_dtype>& fd,
+                                          CategoryScope& categories, std::string& codes) {
+    const bool cat = frame_has_category(frame, ncols);
+    categories.planning(cond);
+    if (has_string_literal(cond.c_str()) || cat) plan_expression(cond, ncols);
+    categories.planning(project_q);
+    if (has_string_literal(project_q) || cat) plan_project(project_q, fd);
+    categories.replay();
+    codes = categories.recorded_key();
+    const ProjectPlan& pp = cached_project_plan(project_q, fd, category_key(frame, ncols) + codes);
+    categories.planning(cond);
+    return pp;
+}
+
+int prepare_standalone_filter(gdf_column* const* frame, int ncols, const char* filter_q, const char* project_q,
+                              gdf_column* const* outs, int n_outs, const void** handle) {
+    if (!frame || ncols <= 0 || !filter_q || !project_q || !outs || !handle)
+        return set_error(kInvalidArgument, "null argument");
+    try {
+        const std::string cond = named_expression(filter_q, "condition");
+        if (cond.empty()) return set_error(kParseError, "no condition=[...] in the LogicalFilter");
+        std::vector<gdf_dtype> fd(ncols);
+        for (int c = 0; c < ncols; c++) fd[c] = frame[c]->dtype;
+        CategoryScope categories(frame, ncols);
+        std::string codes;
+        const ProjectPlan& pp = resolve_filter_project(frame, ncols, cond, project_q, fd, categories, codes);
+        if ((int)pp.columns.size() != n_outs)
+            return set_error(kInvalidArgument, "out_columns count differs from the projection's");
+        const PreparedFilter* pf = nullptr;
+        if (int rc = prepare_filter_project(frame, ncols, cond, project_q, pp, outs, n_outs, codes, &pf)) return rc;
+        *handle = pf;
+        return kSuccess;
+    } catch (const ParseError& e) {
+        return set_error(kParseError, e.what());
+    }
+}
+
+int64_t standalone_scratch_words(const void* handle, int64_t n) {
+    return prepared_scratch_words(*static_cast<const PreparedFilter*>(handle), n);
+}
+
+int enqueue_standalone_filter(const void* handle, gdf_column* const* frame, gdf_column* const* outs, void* scratch,
+                              unsigned long long* host_header, cudaStream_t st) {
+    return enqueue_prepared(*static_cast<const PreparedFilter*>(handle), frame, outs, scratch, 0, host_header, st,
+                            nullptr);
+}
+
 int filter_project(gdf_column* const* frame, int ncols, const char* filter_q, const char* project_q,
                    gdf_column* const* outs, int n_outs, gdf_size_type* n_out, const FilterOptions& opt) {
     call_timing_start();
@@ -737,17 +792,8 @@ int filter_project(gdf_column* const* frame, int ncols, const char* filter_q, co
     std::vector<gdf_dtype> fd(ncols);
     for (int c = 0; c < ncols; c++) fd[c] = frame[c]->dtype;
     CategoryScope categories(frame, ncols);
-    const bool cat = frame_has_category(frame, ncols);
-    // the filter's literals resolve before the projection's, as process_filter runs before
-    // execute_project_plan in the reference
-    categories.planning(cond);
-    if (has_string_literal(cond.c_str()) || cat) plan_expression(cond, ncols);
-    categories.planning(project_q);
-    if (has_string_literal(project_q) || cat) plan_project(project_q, fd);
-    categories.replay();
-    const std::string codes = categories.recorded_key();
-    const ProjectPlan& pp = cached_project_plan(project_q, fd, category_key(frame, ncols) + codes);
-    categories.planning(cond);
+    std::string codes;
+    const ProjectPlan& pp = resolve_filter_project(frame, ncols, cond, project_q, fd, categories, codes);
     if ((int)pp.columns.size() != n_outs) return set_error(kInvalidArgument, "out_columns count differs from the projection's");
     for (int i = 0; i < n_outs; i++) {
         if (!outs[i]) return set_error(kInvalidArgument, "null out column");

@@ -38,6 +38,16 @@ int filter_project(gdf_column* const* frame, int num_columns, const char* filter
 int filter_host(gdf_column* const* frame, int ncols, const char* filter_q, const char* project_q,
                 gdf_column* const* outs, int n_outs, gdf_size_type* n_out, int64_t chunk_rows);
 
+// The standalone fused filter + project kernel over a whole frame, for a caller that launches it
+// itself (the served loop runs large requests this way): prepared (compiled) for a frame and the
+// outputs' dtypes and mask presence; enqueue_standalone_filter zeroes the scratch and the output
+// masks, launches, and copies the header (error word, kept count, valid counts) to host_header.
+int prepare_standalone_filter(gdf_column* const* frame, int ncols, const char* filter_q, const char* project_q,
+                              gdf_column* const* outs, int n_outs, const void** handle);
+int64_t standalone_scratch_words(const void* handle, int64_t n);
+int enqueue_standalone_filter(const void* handle, gdf_column* const* frame, gdf_column* const* outs, void* scratch,
+                              unsigned long long* host_header, cudaStream_t st);
+
 // A LogicalProject over a LogicalFilter, planned for a frame: the fused filter's spec and the
 // dtype / mask presence of every output (evaluated outputs carry a mask; a pass-through output
 // carries one exactly when its frame column does).  Holds the programs the spec points to.

@@ -103,21 +103,44 @@ __device__ __forceinline__ ral_i64 ral_load_index(const void* idx, ral_i64 i) {
     return (ral_i64)__ldcs(reinterpret_cast<const I*>(idx) + i);
 }
 
+// One column's step: the four data loads and the four validity-word loads are all issued before
+// any is used, so each lane has eight independent random reads in flight and a column costs one
+// memory round trip (the loaded values are consumed only by the stores and ballots after them).
 template <typename E>
-__device__ __forceinline__ void ral_gather_k(const GatherColumn& c, const ral_i64 (&j)[kGatherRowsPerLane],
-                                             const bool (&ok)[kGatherRowsPerLane], ral_i64 row0) {
+__device__ __forceinline__ unsigned ral_gather_k(const GatherColumn& c, const ral_i64 (&j)[kGatherRowsPerLane],
+                                                 const bool (&ok)[kGatherRowsPerLane], ral_i64 base, int lane,
+                                                 ral_i64 n_out) {
     const E* __restrict__ in = reinterpret_cast<const E*>(c.in);
     E* __restrict__ out = reinterpret_cast<E*>(c.out);
+    const ral_u32* __restrict__ iv = c.in_valid;
     E v[kGatherRowsPerLane];
+    ral_u32 w[kGatherRowsPerLane];
+#pragma unroll
+    for (int k = 0; k < kGatherRowsPerLane; ++k) {
+        v[k] = ok[k] ? __ldg(in + j[k]) : E(0);
+        w[k] = ok[k] ? (iv ? __ldg(iv + (j[k] >> 5)) : 0xffffffffu) : 0u;
+    }
 #pragma unroll
     for (int k = 0; k < kGatherRowsPerLane; ++k)
-        if (ok[k]) v[k] = in[j[k]];
+        if (ok[k]) __stcs(out + base + lane + 32 * k, v[k]);
+    unsigned cnt = 0;
+    if (c.out_valid) {
 #pragma unroll
-    for (int k = 0; k < kGatherRowsPerLane; ++k)
-        if (ok[k]) __stcs(out + row0 + 32 * k, v[k]);
+        for (int k = 0; k < kGatherRowsPerLane; ++k) {
+            const bool bit = (w[k] >> (j[k] & 31)) & 1u;
+            const ral_u32 word = __ballot_sync(0xffffffffu, bit);
+            // word k covers rows base + 32 k .. +31; lane k writes it (masks are padded to 64
+            // bytes, so a partial last word stays inside the allocation)
+            if (lane == k && base + 32 * k < n_out) c.out_valid[(base >> 5) + k] = word;
+            cnt += __popc(word);
+        }
+    }
+    return cnt;
 }
 
-__global__ void __launch_bounds__(256) gather_columns_kernel(const __grid_constant__ GatherColumnsParams P) {
+// 40 registers (six blocks of 256 threads per SM): the gathers are latency-bound, so resident
+// warps -- loads in flight -- matter more than registers.
+__global__ void __launch_bounds__(256, 6) gather_columns_kernel(const __grid_constant__ GatherColumnsParams P) {
     __shared__ unsigned long long s_cnt[kMaxGatherColumns];
     for (int c = threadIdx.x; c < P.num_columns; c += blockDim.x) s_cnt[c] = 0;
     __syncthreads();
@@ -144,29 +167,16 @@ __global__ void __launch_bounds__(256) gather_columns_kernel(const __grid_consta
             }
             ok[k] = j[k] >= 0 && j[k] < P.n_in;
         }
-        const ral_i64 row0 = base + lane;
         for (int c = 0; c < P.num_columns; ++c) {
             const GatherColumn& col = P.col[c];
+            unsigned cnt;
             switch (col.width) {
-            case 1: ral_gather_k<int8_t>(col, j, ok, row0); break;
-            case 2: ral_gather_k<short>(col, j, ok, row0); break;
-            case 4: ral_gather_k<int>(col, j, ok, row0); break;
-            default: ral_gather_k<long long>(col, j, ok, row0); break;
+            case 1: cnt = ral_gather_k<int8_t>(col, j, ok, base, lane, P.n_out); break;
+            case 2: cnt = ral_gather_k<short>(col, j, ok, base, lane, P.n_out); break;
+            case 4: cnt = ral_gather_k<int>(col, j, ok, base, lane, P.n_out); break;
+            default: cnt = ral_gather_k<long long>(col, j, ok, base, lane, P.n_out); break;
             }
-            if (col.out_valid) {
-                unsigned cnt = 0;
-#pragma unroll
-                for (int k = 0; k < kGatherRowsPerLane; ++k) {
-                    bool bit = ok[k];
-                    if (bit && col.in_valid) bit = (__ldg(col.in_valid + (j[k] >> 5)) >> (j[k] & 31)) & 1u;
-                    const ral_u32 word = __ballot_sync(0xffffffffu, bit);
-                    // word k covers rows base + 32 k .. +31; lane k writes it (masks are padded
-                    // to 64 bytes, so a partial last word stays inside the allocation)
-                    if (lane == k && base + 32 * k < P.n_out) col.out_valid[(base >> 5) + k] = word;
-                    cnt += __popc(word);
-                }
-                if (lane == 0 && cnt) atomicAdd(&s_cnt[c], (unsigned long long)cnt);
-            }
+            if (lane == 0 && cnt) atomicAdd(&s_cnt[c], (unsigned long long)cnt);
         }
     }
     __syncthreads();

@@ -63,7 +63,7 @@ RequestLayout request_layout(const ServerQuery& q, int64_t rows) {
     RequestLayout L;
     const FilterPlan& p = *q.plan;
     const int NO = (int)p.out_dtypes.size();
-    L.scratch_bytes = (size_t)(filter_scratch_header(NO) + q.chunks) * 8;
+    L.scratch_bytes = (size_t)std::max<int64_t>(filter_scratch_header(NO) + q.chunks, q.scratch_words) * 8;
     size_t off = round_up(L.scratch_bytes, 256);
     for (int k = 0; k < NO; k++) {
         L.valid_off.push_back(p.out_valid[k] ? off : (size_t)-1);
@@ -88,6 +88,10 @@ Server::Server(size_t budget_bytes, int max_waves, int max_wave_requests, int64_
     // measured at 90% load: 4 gives p50 / p99 3.6 / 41.6 ms, 1 gives 6.3 / 31.3 ms)
     const char* sd = std::getenv("RAL_SERVER_SLICE_DIV");
     slice_div_ = sd && std::atoi(sd) >= 1 && std::atoi(sd) <= 64 ? std::atoi(sd) : 2;
+    // RAL_SERVER_SOLO_ROWS: requests over tables of at least this many rows run the standalone
+    // fused kernel alone on a wave (default half a wave; 0 turns it off)
+    const char* so = std::getenv("RAL_SERVER_SOLO_ROWS");
+    solo_rows_ = so ? std::atoll(so) : wave_rows_ / 2;
     t0_ = 0;
     t0_ = now();
 }
@@ -147,6 +151,23 @@ int Server::add_query(int table_id, const char* filter_q, const char* project_q,
     q->item.max_registers = server_max_registers();
     // at least one chunk, so that an empty table's request still runs (and finishes) once
     q->chunks = std::max<int64_t>(1, (t.rows + filter_tile_rows(sh) - 1) / filter_tile_rows(sh));
+    if (solo_rows_ > 0 && t.rows >= solo_rows_ && max_waves_ > 1) {
+        // stand-in outputs: only dtypes and mask presence matter to the plan
+        const int NO = (int)q->plan->out_dtypes.size();
+        std::vector<gdf_column> stand(NO);
+        std::vector<gdf_column*> souts(NO);
+        for (int o = 0; o < NO; o++) {
+            stand[o] = gdf_column{};
+            stand[o].dtype = q->plan->out_dtypes[o];
+            stand[o].valid = q->plan->out_valid[o] ? (gdf_valid_type*)(uintptr_t)256 : nullptr;
+            stand[o].size = (gdf_size_type)t.rows;
+            souts[o] = &stand[o];
+        }
+        if (int e = prepare_standalone_filter(frame.data(), (int)frame.size(), filter_q, project_q, souts.data(), NO,
+                                              &q->solo))
+            return e;
+        q->scratch_words = standalone_scratch_words(q->solo, t.rows);
+    }
     q->reserve = request_layout(*q, t.rows).total;
     if (q->plan->out_dtypes.size() > 64) return set_error(kUnsupported, "more than 64 projected columns");
     if (tables_bytes_ + q->reserve > budget_)
@@ -320,19 +341,7 @@ int Server::launch_wave(Wave& w, const std::vector<int64_t>& reqs, const std::ve
         ServerQuery& q = *queries_[r.query];
         ServerTable& tb = tables_[q.table];
         if (r.next_chunk == 0) {
-            // first slice: the request's outputs and scratch, zeroed where the kernel expects it
-            const RequestLayout L = request_layout(q, tb.rows);
-            void* mem = nullptr;
-            if (int e = check_cuda(cudaMallocAsync(&mem, L.total, w.stream), "cudaMallocAsync")) return e;
-            cudaMemsetAsync(mem, 0, L.zero_bytes, w.stream);
-            r.scratch = mem;
-            const int NO = (int)q.plan->out_dtypes.size();
-            r.out_data.assign(NO, nullptr);
-            r.out_valid.assign(NO, nullptr);
-            for (int o = 0; o < NO; o++) {
-                r.out_data[o] = (char*)mem + L.data_off[o];
-                if (L.valid_off[o] != (size_t)-1) r.out_valid[o] = (char*)mem + L.valid_off[o];
-            }
+            if (int e = start_request(r, w.stream)) return e;
             r.t_launch = t;
         }
         if (r.slots.empty()) {
@@ -394,6 +403,79 @@ int Server::launch_wave(Wave& w, const std::vector<int64_t>& reqs, const std::ve
     return kSuccess;
 }
 
+// A request's first launch: its outputs and scratch, zeroed where the kernels expect it.
+int Server::start_request(ServerRequest& r, cudaStream_t st) {
+    ServerQuery& q = *queries_[r.query];
+    ServerTable& tb = tables_[q.table];
+    const RequestLayout L = request_layout(q, tb.rows);
+    void* mem = nullptr;
+    if (int e = check_cuda(cudaMallocAsync(&mem, L.total, st), "cudaMallocAsync")) return e;
+    cudaMemsetAsync(mem, 0, L.zero_bytes, st);
+    r.scratch = mem;
+    const int NO = (int)q.plan->out_dtypes.size();
+    r.out_data.assign(NO, nullptr);
+    r.out_valid.assign(NO, nullptr);
+    for (int o = 0; o < NO; o++) {
+        r.out_data[o] = (char*)mem + L.data_off[o];
+        if (L.valid_off[o] != (size_t)-1) r.out_valid[o] = (char*)mem + L.valid_off[o];
+    }
+    return kSuccess;
+}
+
+// A large request alone on a wave: the standalone fused filter + project kernel over its table,
+// its header (error word, kept count, valid counts) copied to the wave's first header slot.
+int Server::launch_solo(Wave& w, int64_t id) {
+    ServerRequest& r = *requests_[id];
+    ServerQuery& q = *queries_[r.query];
+    ServerTable& tb = tables_[q.table];
+    const double t = now();
+    if (int e = start_request(r, w.stream)) return e;
+    r.t_launch = t;
+    const int NO = (int)q.plan->out_dtypes.size();
+    std::vector<gdf_column*> frame;
+    for (auto& c : tb.cols) frame.push_back(&c);
+    std::vector<gdf_column> outs(NO);
+    std::vector<gdf_column*> pouts(NO);
+    for (int o = 0; o < NO; o++) {
+        outs[o] = gdf_column{};
+        outs[o].dtype = q.plan->out_dtypes[o];
+        outs[o].data = r.out_data[o];
+        outs[o].valid = (gdf_valid_type*)r.out_valid[o];
+        outs[o].size = (gdf_size_type)tb.rows;
+        pouts[o] = &outs[o];
+    }
+    if (int e = enqueue_standalone_filter(q.solo, frame.data(), pouts.data(), r.scratch,
+                                          (unsigned long long*)w.h_head, w.stream))
+        return e;
+    if (int e = check_cuda(cudaEventRecord(w.done, w.stream), "cudaEventRecord")) return e;
+    r.next_chunk = q.chunks;
+    r.in_wave = true;
+    w.reqs = {id};
+    w.take = {q.chunks};
+    w.last.assign(1, 1);
+    w.busy = true;
+    w.solo = true;
+    w.t_launch = t;
+    if (inflight_ == 0) busy_since_ = t;
+    inflight_++;
+    solo_inflight_++;
+    stats_.waves++;
+    stats_.solo++;
+    stats_.max_wave_requests = std::max<int64_t>(stats_.max_wave_requests, 1);
+    return kSuccess;
+}
+
+// Bookkeeping of a wave that is no longer in flight.
+void Server::wave_ended(Wave& w) {
+    w.reqs.clear();
+    w.busy = false;
+    if (w.solo) {
+        w.solo = false;
+        solo_inflight_--;
+    }
+    inflight_--;
+}
+
 void Server::finish_wave(Wave& w) {
     const double t = now();
     const uint64_t* hh = (const uint64_t*)w.h_head;
@@ -425,9 +507,7 @@ void Server::finish_wave(Wave& w) {
         active_.erase(std::find(active_.begin(), active_.end(), r.id));
         stats_.completed++;
     }
-    w.reqs.clear();
-    w.busy = false;
-    inflight_--;
+    wave_ended(w);
     if (inflight_ == 0 && busy_since_ >= 0) {
         stats_.busy_s += t - busy_since_;
         busy_since_ = -1;
@@ -448,12 +528,11 @@ void Server::loop() {
                 fatal_ = kCudaError;
                 fatal_msg_ = std::string("served wave failed: ") + cudaGetErrorString(q);
                 cudaGetLastError();
-                w.busy = false;
-                inflight_--;
                 for (int64_t id : w.reqs) {
                     requests_[id]->status = kCudaError;
                     requests_[id]->done = true;
                 }
+                wave_ended(w);
                 done_cv_.notify_all();
             }
         }
@@ -475,6 +554,29 @@ void Server::loop() {
                 pending_.pop_front();
             }
             stats_.peak_reserved = std::max(stats_.peak_reserved, reserved_);
+            // a large request not yet started runs alone on the standalone kernel, on at most all
+            // but one of the waves (one stays for the batched small requests)
+            if (!rc && solo_inflight_ < max_waves_ - 1) {
+                int64_t solo_id = -1;
+                for (int64_t id : active_) {
+                    const ServerRequest& r = *requests_[id];
+                    if (!r.in_wave && r.next_chunk == 0 && queries_[r.query]->solo) {
+                        solo_id = id;
+                        break;
+                    }
+                }
+                if (solo_id >= 0) {
+                    rc = launch_solo(*free_w, solo_id);
+                    if (rc) {
+                        fatal_ = rc;
+                        fatal_msg_ = last_error();
+                        requests_[solo_id]->status = rc;
+                        requests_[solo_id]->done = true;
+                        done_cv_.notify_all();
+                    }
+                    continue;
+                }
+            }
             // the wave: requests not in flight, fewest rows left (less a waiting credit) first,
             // each with at most a quarter of the wave, up to wave_rows_ rows
             std::vector<int64_t> reqs, take;
@@ -484,6 +586,7 @@ void Server::loop() {
                 const ServerRequest& r = *requests_[id];
                 if (r.in_wave) continue;
                 const ServerQuery& q = *queries_[r.query];
+                if (q.solo && r.next_chunk == 0) continue;  // waits for a solo wave
                 const double left = (double)(q.chunks - r.next_chunk) * (double)filter_tile_rows(q.item.shape);
                 cand.push_back({left - (tnow - r.t_submit) * kAgeRowsPerSecond, id});
             }

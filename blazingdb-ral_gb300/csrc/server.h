@@ -47,6 +47,10 @@ struct ServerQuery {
     int fn = -1;               // index in the dispatcher's function list
     size_t reserve = 0;        // output + scratch bytes of one request (every row kept)
     int64_t chunks = 0;        // work items of one request
+    // a table of at least the solo threshold: its requests run the standalone fused filter kernel
+    // alone on a wave's stream (the kernel ral_filter_project launches)
+    const void* solo = nullptr;
+    int64_t scratch_words = 0; // scratch of one request: the larger of the chunked and solo needs
 };
 
 struct ServerRequest {
@@ -67,6 +71,7 @@ struct ServerRequest {
 
 struct ServerStats {
     int64_t submitted = 0, completed = 0, waves = 0, max_wave_requests = 0;
+    int64_t solo = 0;          // requests run alone on the standalone kernel
     size_t peak_reserved = 0;
     double busy_s = 0;         // wall time with at least one wave in flight
 };
@@ -110,12 +115,16 @@ private:
         std::vector<int64_t> reqs;
         std::vector<int64_t> take;     // chunks of each request in this wave
         std::vector<char> last;        // the wave runs the request's last chunk
+        bool solo = false;             // one request on the standalone kernel
         bool busy = false;
         double t_launch = 0;
     };
     int ensure_linked();
     void collect_items(std::vector<GeneratedKernel>& tus, std::vector<DispatchEntry>& entries, int& stride, int& smem);
     int launch_wave(Wave& w, const std::vector<int64_t>& reqs, const std::vector<int64_t>& take);
+    int launch_solo(Wave& w, int64_t request_id);
+    int start_request(ServerRequest& r, cudaStream_t st);
+    void wave_ended(Wave& w);
     void finish_wave(Wave& w);
     void loop();
 
@@ -148,6 +157,8 @@ private:
     double t0_ = 0;
     double busy_since_ = -1;
     int inflight_ = 0;
+    int solo_inflight_ = 0;
+    int64_t solo_rows_ = 0;            // tables of at least this many rows run their requests solo
 };
 
 }  // namespace ral

@@ -58,6 +58,10 @@ int ral_debug_call_timing(int32_t enable, int32_t reset, int64_t *calls, double 
  * needed); the ptxas / link log goes to log_out. */
 int ral_server_debug_compile(ral_server *server, char *log_out, int64_t log_capacity);
 
+/* Requests the server ran alone on the standalone fused kernel (tables of at least
+ * RAL_SERVER_SOLO_ROWS rows). */
+int ral_server_debug_solo(ral_server *server, int64_t *solo_requests);
+
 /*
  * Device self-test of the integer-pipe double operations against the GPU's FP64 instructions
  * (no reference counterpart): n random operand sets from seed; mismatches[16] receives the

@@ -180,3 +180,28 @@ def test_empty_and_one_row_tables():
     assert got[0].size == 1 and got[0].to_numpy()[0] == 5.0 and got[1].to_numpy()[0] == 7
     assert srv.wait(srv.submit(qc))[0] == 0
     srv.close()
+
+
+def test_large_requests_run_solo_with_the_same_bits(served, monkeypatch):
+    """Requests over tables of at least RAL_SERVER_SOLO_ROWS rows run alone on the standalone fused
+    kernel, the others batched beside them: every result equals the batched-only server's, and
+    the solo count is the number of large requests."""
+    tabs, qs, host, dev = served
+    monkeypatch.setenv("RAL_SERVER_SOLO_ROWS", "0")
+    srv0, qids0 = _server(tabs, qs, dev, waves=3)
+    alone = {i: _alone(srv0, qids0[i]) for i in range(len(qs))}
+    assert srv0.stats()["solo"] == 0
+    srv0.close()
+    cut = int(np.median([t.rows for t in tabs]))
+    monkeypatch.setenv("RAL_SERVER_SOLO_ROWS", str(cut))
+    srv, qids = _server(tabs, qs, dev, waves=3)
+    big = [tabs[q.table].rows >= cut for q in qs]
+    assert any(big) and not all(big)
+    rids = [(srv.submit(qids[i % len(qs)], keep=True), i % len(qs)) for i in range(4 * len(qs))]
+    for rid, i in rids:
+        got = srv.result(rid, qids[i])
+        for j, (g, a) in enumerate(zip(got, alone[i])):
+            _same_bits(g, a, f"query {i} output {j} solo={big[i]}")
+    st = srv.stats()
+    assert st["solo"] == sum(big[i] for _, i in rids)
+    srv.close()
