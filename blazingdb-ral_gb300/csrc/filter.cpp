@@ -271,8 +271,27 @@ std::unordered_map<std::string, std::unique_ptr<PreparedFilter>> g_prepared;
 struct ThreadScratch {
     void* p = nullptr;
     size_t bytes = 0;
+    unsigned long long* head = nullptr;  // page-locked: the header copy back is a plain DMA
+    size_t head_words = 0;
 };
 thread_local std::unordered_map<int, ThreadScratch> t_scratch;
+
+// The calling thread's page-locked header buffer on the current device (at least `words`).
+int header_get(size_t words, unsigned long long** out) {
+    int dev = 0;
+    if (int e = check_cuda(cudaGetDevice(&dev), "cudaGetDevice")) return e;
+    ThreadScratch& ts = t_scratch[dev];
+    if (ts.head_words < words) {
+        if (ts.head) cudaFreeHost(ts.head);
+        ts.head = nullptr;
+        ts.head_words = 0;
+        const size_t want = std::max<size_t>(words, 128);
+        if (int e = check_cuda(cudaMallocHost((void**)&ts.head, want * 8), "cudaMallocHost")) return e;
+        ts.head_words = want;
+    }
+    *out = ts.head;
+    return kSuccess;
+}
 
 int scratch_get(size_t bytes, cudaStream_t st, void** out) {
     int dev = 0;
@@ -451,10 +470,8 @@ int run_prepared(const PreparedFilter& pf, gdf_column* const* frame, gdf_column*
         cudaEventCreate(&ev[0]);
         cudaEventCreate(&ev[1]);
     }
-    unsigned long long h[64];
-    std::vector<unsigned long long> hv;
-    unsigned long long* hp = h;
-    if (header > 64) { hv.resize(header); hp = hv.data(); }
+    unsigned long long* hp = nullptr;
+    if (int e = header_get((size_t)header, &hp)) return e;
     if (int e = enqueue_prepared(pf, frame, outs, scratch, 0, hp, st, timing ? ev : nullptr)) return e;
     const auto t_wait0 = std::chrono::steady_clock::now();
     if (int e = check_cuda(cudaStreamSynchronize(st), "filter kernel")) return e;

@@ -171,3 +171,40 @@ def test_batch_with_empty_tables():
         R.perform_operation(p["outs_p"], p["dev_in"], *_args(p["pp"]))
         for k, (x, y) in enumerate(zip(p["outs_b"], p["outs_p"])):
             _assert_same_bits(x, y, f"program {q} output {k}")
+
+
+TRANS = ["SIN", "COS", "TAN", "ATAN", "ASIN", "ACOS", "LN", "LOG10"]
+
+
+def test_batched_transcendentals_match_the_oracle_within_2_ulp():
+    """Batched item functions with sin / cos / tan / atan / asin / acos / ln / log10 against the
+    oracle (libm), one transcendental per output so that the per-operation bound applies."""
+    import torch
+    rng = np.random.default_rng(71)
+    progs = []
+    for k, op in enumerate(TRANS):
+        n = int(rng.integers(1000, 60_000))
+        x = rng.uniform(0.01, 0.99, n) if op in ("LN", "LOG10", "ASIN", "ACOS") else rng.uniform(-3, 3, n)
+        spec = [(D.GDF_FLOAT64, x, rng.random(n) >= 0.05), (D.GDF_INT32, rng.integers(1, 9, n).astype(np.int32), None)]
+        pp = R.parse_project_plan([D.GDF_FLOAT64, D.GDF_INT32],
+                                  f"LogicalProject(a=[{op}($0)], b=[{op}($1)])")
+        ins = [spec[c] for c in pp["input_columns"]]
+        dev_in = H.to_device(ins)
+        outs = [R.Column.empty(dt, n, with_valid=True) for dt in pp["evaluated_dtypes"]]
+        progs.append(dict(op=op, pp=pp, ins=ins, dev_in=dev_in, outs=outs, n=n))
+    b = R.Batch()
+    for p in progs:
+        b.add(p["outs"], p["dev_in"], *_args(p["pp"]))
+    b.prepare()
+    b.run()
+    torch.cuda.synchronize()
+    for p in progs:
+        pp = p["pp"]
+        ora_out = [O.alloc_column(dt, p["n"]) for dt in pp["evaluated_dtypes"]]
+        O.perform_operation(ora_out, H.to_oracle(p["ins"]), pp["left"], pp["right"], pp["outputs"],
+                            pp["final_output_positions"], pp["operators"], pp["unary_operators"],
+                            [fe.Scalar(s.dtype, s.value, s.is_valid) for s in pp["left_scalars"]],
+                            [fe.Scalar(s.dtype, s.value, s.is_valid) for s in pp["right_scalars"]], nthreads=8)
+        for k, (g, e) in enumerate(zip(p["outs"], ora_out)):
+            H.assert_columns_equal(g, e, tol_ulp=H.ULP_TOL, what=f"batched {p['op']} output {k}",
+                                   check_null_count=False)

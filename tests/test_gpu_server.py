@@ -141,10 +141,11 @@ def test_many_large_requests_in_one_wave():
     srv.close()
 
 
-def test_requests_sliced_over_many_waves_give_the_same_bits(served):
+def test_requests_sliced_over_many_waves_give_the_same_bits(served, monkeypatch):
     """A wave budget far below one table: every request runs as many slices, each chunk's
-    look-back continuing from the status words a previous wave left."""
+    look-back continuing from the status words a previous wave left (no request runs solo)."""
     tabs, qs, host, dev = served
+    monkeypatch.setenv("RAL_SERVER_SOLO_ROWS", "0")
     srv0, qids0 = _server(tabs, qs, dev)
     alone = {i: _alone(srv0, qids0[i]) for i in range(len(qs))}
     srv0.close()
@@ -204,4 +205,29 @@ def test_large_requests_run_solo_with_the_same_bits(served, monkeypatch):
             _same_bits(g, a, f"query {i} output {j} solo={big[i]}")
     st = srv.stats()
     assert st["solo"] == sum(big[i] for _, i in rids)
+    srv.close()
+
+
+def test_served_transcendentals_match_the_oracle_within_2_ulp():
+    """Served item functions with sin / cos / atan / ln in the projection against the oracle's
+    process_filter + execute_project_plan, within 2 ulp."""
+    from ralgpu import dtypes as D
+    rng = np.random.default_rng(72)
+    n = 250_000
+    host = [(D.GDF_INT32, rng.integers(-100, 100, n).astype(np.int32), rng.random(n) >= 0.05),
+            (D.GDF_FLOAT64, rng.uniform(0.01, 3.0, n), rng.random(n) >= 0.05)]
+    dev = H.to_device(host)
+    fq = "LogicalFilter(condition=[>($0, -20)])"
+    projects = ["LogicalProject(s=[SIN($1)], c=[COS($1)], k=[$0])",
+                "LogicalProject(a=[ATAN($1)], l=[LN($1)])"]
+    srv = R.Server(budget_bytes=4 << 30, max_waves=2, max_wave_requests=64)
+    tid = srv.add_table(dev)
+    qids = [srv.add_query(tid, fq, pq) for pq in projects]
+    srv.start()
+    ef = O.process_filter(H.to_oracle(host), fq)
+    for qid, pq in zip(qids, projects):
+        got = _alone(srv, qid)
+        ep = O.execute_project_plan(ef, pq)
+        for k, (g, e) in enumerate(zip(got, ep)):
+            H.assert_columns_equal(g, e, tol_ulp=H.ULP_TOL, what=f"served {pq} output {k}")
     srv.close()
