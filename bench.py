@@ -431,6 +431,7 @@ def filter_setup(workload, n, selectivity, device, null_rate=None):
         outs = [R.Column.empty(t, n) for t in types]
         in_b = [R.dtypes.WIDTH[c.dtype] + 1 / 8 for c in frame]   # every column (+ mask) is read
         out_b = sum(R.dtypes.WIDTH[t] + 1 / 8 for t in types)
+        pred_cols = {4}                               # k < T
     elif workload == "plain_vm":
         spec = W.plain_vm_host(n)
         frame = [R.Column.from_numpy(v, t, m) for t, v, m in spec]
@@ -439,6 +440,7 @@ def filter_setup(workload, n, selectivity, device, null_rate=None):
         outs = [R.Column.empty(t, n) for t in types]
         in_b = [8 + 0, 8 + 1 / 8, 4, 4]          # c0, c1 (+mask), c2, c3 read by the predicate / projection
         out_b = 8 + 1 / 8
+        pred_cols = {0, 1, 2, 3}
     else:
         frame = []
         for t, data, valid, nulls in W.filter_gather_device(n, device=device, null_rate=null_rate):
@@ -447,6 +449,7 @@ def filter_setup(workload, n, selectivity, device, null_rate=None):
         outs = [R.Column.empty(c.dtype, n, with_valid=c.valid is not None) for c in frame]
         in_b = [R.dtypes.WIDTH[c.dtype] for c in frame]
         out_b = sum(in_b)
+        pred_cols = {0}                               # <($0, T)
     fa, fs = _colarray(frame)
     oa, os_ = _colarray(outs)
     nout = ctypes.c_int32(0)
@@ -463,7 +466,25 @@ def filter_setup(workload, n, selectivity, device, null_rate=None):
         k = nout.value
         return n * sum(in_b) + k * out_b + 8
 
-    return dict(step=step, alg_bytes_fn=alg_bytes, nout=nout, cols=frame, outs=outs, out_structs=os_, fq=fq, pq=pq)
+    def touched_bytes():
+        """The bytes the kernel reaches at this selectivity: the predicate's columns whole, every
+        other column's 32-byte sectors that hold a kept row (kept rows independent with
+        probability s: a sector of r rows is touched with probability 1 - (1 - s)^r), the masks'
+        sectors alike, and the kept rows written."""
+        k = nout.value
+        sel = k / max(n, 1)
+        total = k * out_b
+        for i, c in enumerate(frame):
+            w = R.dtypes.WIDTH[c.dtype]
+            if i in pred_cols:
+                total += n * w + (n / 8 if c.valid is not None else 0)
+                continue
+            total += n * w * (1 - (1 - sel) ** (32 / w))
+            if c.valid is not None:
+                total += n / 8 * (1 - (1 - sel) ** 256)
+        return total
+
+    return dict(step=step, alg_bytes_fn=alg_bytes, touched_bytes_fn=touched_bytes, nout=nout, cols=frame, outs=outs, out_structs=os_, fq=fq, pq=pq)
 
 
 def gather_setup(n, pattern, device, null_rate=0.05):
@@ -838,6 +859,13 @@ def measure_workload(args, workload, n, selectivity, device, world, sampler, e2e
     }
     if "nout" in ctx:
         out["rows_out"] = ctx["nout"].value
+    if "touched_bytes_fn" in ctx:
+        # below s = 50% the kernel reads the non-predicate columns only around kept rows: the
+        # fraction against the bytes it can reach stays below 1 where the full-read one would not
+        touched = ctx["touched_bytes_fn"]()
+        out["roofline"]["touched_model_bytes_per_launch"] = touched
+        out["roofline"]["touched_model_gbs"] = touched / (kernel_ms / 1e3) / 1e9
+        out["roofline"]["touched_model_frac"] = out["roofline"]["touched_model_gbs"] / peak
     if workload == "plain_vm":
         # where a small synchronous call's time goes: the same calls again with the library's
         # per-call timing on (host preparation, enqueue, wait, kernel device time)
@@ -1234,7 +1262,10 @@ def run_served(args):
     for frac in (0.2, 0.4, 0.6, 0.8, 0.95):
         rate = frac * capacity
         tq, ta = W.served_trace(n_rate, rate, len(qs), seed=args.seed + int(frac * 100))
+        st0 = srv.stats()
         lat, rows, mk = srv.run_trace(tq, ta)
+        st1 = srv.stats()
+        n_done = max(1, st1["completed"] - st0["completed"])
         scanned = float(q_rows[tq].sum())
         # serial plain execution of the same arrivals: one request at a time, in arrival order
         done = 0.0
@@ -1246,7 +1277,10 @@ def run_served(args):
         per_rate.append({
             "rate_rps": rate, "fraction_of_served_capacity": frac, "requests": int(len(tq)),
             "served": {"p50_ms": float(np.percentile(lat, 50) * 1e3), "p99_ms": float(np.percentile(lat, 99) * 1e3),
-                       "rows_per_s": scanned / mk, "requests_per_s": len(tq) / mk},
+                       "rows_per_s": scanned / mk, "requests_per_s": len(tq) / mk,
+                       "mean_queue_ms": (st1["queue_s"] - st0["queue_s"]) / n_done * 1e3,
+                       "mean_run_ms": (st1["run_s"] - st0["run_s"]) / n_done * 1e3,
+                       "solo_requests": st1["solo"] - st0["solo"]},
             "serial_plain": {"p50_ms": float(np.percentile(slat, 50) * 1e3),
                              "p99_ms": float(np.percentile(slat, 99) * 1e3),
                              "rows_per_s": scanned / s_mk, "requests_per_s": len(tq) / s_mk},

@@ -861,9 +861,12 @@ int ral_server_stats(ral_server* server, int64_t* stats6) {
     return kSuccess;
 }
 
-int ral_server_debug_solo(ral_server* server, int64_t* solo_requests) {
-    if (!server || !solo_requests) return set_error(kInvalidArgument, "null argument");
-    *solo_requests = server->s.stats().solo;
+int ral_server_debug_stats(ral_server* server, int64_t* solo_requests, double* queue_s, double* run_s) {
+    if (!server) return set_error(kInvalidArgument, "null argument");
+    const ServerStats st = server->s.stats();
+    if (solo_requests) *solo_requests = st.solo;
+    if (queue_s) *queue_s = st.queue_s;
+    if (run_s) *run_s = st.run_s;
     return kSuccess;
 }
 

@@ -487,6 +487,8 @@ void Server::finish_wave(Wave& w) {
         const uint64_t* head = hh + k * 67;
         const int NO = (int)q.plan->out_dtypes.size();
         r.t_done = t;
+        stats_.queue_s += r.t_launch - r.t_submit;
+        stats_.run_s += t - r.t_launch;
         if (head[1]) {
             r.status = kTimeout;
             r.rows_out = -1;

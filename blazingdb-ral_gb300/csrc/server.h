@@ -72,6 +72,8 @@ struct ServerRequest {
 struct ServerStats {
     int64_t submitted = 0, completed = 0, waves = 0, max_wave_requests = 0;
     int64_t solo = 0;          // requests run alone on the standalone kernel
+    double queue_s = 0;        // summed over completed requests: submission to first launch
+    double run_s = 0;          // and first launch to completion
     size_t peak_reserved = 0;
     double busy_s = 0;         // wall time with at least one wave in flight
 };

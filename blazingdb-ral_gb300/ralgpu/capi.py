@@ -88,7 +88,7 @@ _SIGS = {
     "ral_server_run_trace": (C.c_int, [P, C.c_int32, I32P, C.POINTER(C.c_double), C.POINTER(C.c_double),
                                        C.POINTER(C.c_int64), C.POINTER(C.c_double)]),
     "ral_server_stats": (C.c_int, [P, C.POINTER(C.c_int64)]),
-    "ral_server_debug_solo": (C.c_int, [P, C.POINTER(C.c_int64)]),
+    "ral_server_debug_stats": (C.c_int, [P, C.POINTER(C.c_int64), C.POINTER(C.c_double), C.POINTER(C.c_double)]),
     "ral_server_destroy": (C.c_int, [P]),
     "ral_softfp_selftest": (C.c_int, [C.c_int64, C.c_uint64, C.POINTER(C.c_int64), C.POINTER(C.c_uint64)]),
     "ral_debug_lookback_timeout": (C.c_int, [C.c_int64, I32P, C.POINTER(C.c_int64)]),
@@ -766,10 +766,10 @@ class Server:
     def stats(self) -> dict:
         st = (C.c_int64 * 6)()
         _check(lib().ral_server_stats(self._h, st))
-        solo = C.c_int64(0)
-        _check(lib().ral_server_debug_solo(self._h, C.byref(solo)))
+        solo, qs, rs = C.c_int64(0), C.c_double(0), C.c_double(0)
+        _check(lib().ral_server_debug_stats(self._h, C.byref(solo), C.byref(qs), C.byref(rs)))
         return dict(submitted=st[0], completed=st[1], waves=st[2], max_wave_requests=st[3], peak_reserved=st[4],
-                    busy_s=st[5] / 1e6, solo=solo.value)
+                    busy_s=st[5] / 1e6, solo=solo.value, queue_s=qs.value, run_s=rs.value)
 
     def close(self) -> None:
         if self._h:

@@ -58,9 +58,10 @@ int ral_debug_call_timing(int32_t enable, int32_t reset, int64_t *calls, double 
  * needed); the ptxas / link log goes to log_out. */
 int ral_server_debug_compile(ral_server *server, char *log_out, int64_t log_capacity);
 
-/* Requests the server ran alone on the standalone fused kernel (tables of at least
- * RAL_SERVER_SOLO_ROWS rows). */
-int ral_server_debug_solo(ral_server *server, int64_t *solo_requests);
+/* Served-loop counters beside ral_server_stats: requests run alone on the standalone fused kernel
+ * (tables of at least RAL_SERVER_SOLO_ROWS rows), and the seconds summed over completed requests
+ * from submission to first launch (queue_s) and from first launch to completion (run_s). */
+int ral_server_debug_stats(ral_server *server, int64_t *solo_requests, double *queue_s, double *run_s);
 
 /*
  * Device self-test of the integer-pipe double operations against the GPU's FP64 instructions
