@@ -417,6 +417,12 @@ int ral_debug_call_timing(int32_t enable, int32_t reset, int64_t* calls, double*
     return call_timing_query(enable != 0, reset != 0, calls, us4);
 }
 
+int ral_debug_filter_grid_launches(int64_t* launches) {
+    if (!launches) return set_error(kInvalidArgument, "null argument");
+    *launches = filter_grid_launches();
+    return kSuccess;
+}
+
 int ral_apply_boolean_mask(const gdf_column* stencil, gdf_column* out_indices, gdf_size_type* num_rows_out) {
     return guarded([&] {
         if (!stencil || !out_indices || !num_rows_out) return set_error(kInvalidArgument, "null argument");

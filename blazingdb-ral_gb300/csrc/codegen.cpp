@@ -65,6 +65,7 @@ void apply_shape_tune(Shape& sh, const std::string& t) {
             else if (k == "D" && v >= -1 && v <= 1) sh.dense = v;
             else if (k == "K" && v >= 1 && v <= 2) sh.dense_unroll = v;
             else if (k == "M" && v >= 0 && v <= 8 && v != 1) sh.tma_stages = v;
+            else if (k == "R" && v >= 0 && v <= 64) sh.grid_k = v;
         }
         i = e + 1;
     }
@@ -969,6 +970,7 @@ GeneratedKernel generate_filter_kernel(const FilterSpec& f, const Shape& s, bool
     gk.layout_project_lscalar = QL.lscalar_slot;
     gk.layout_project_rscalar = QL.rscalar_slot;
     if (!item) L.obase = slot++;
+    if (!item && s.grid_k > 0) L.epoch = slot++;
     L.total = slot;
 
     std::vector<int> vouts;  // outputs with a mask
@@ -1031,6 +1033,7 @@ GeneratedKernel generate_filter_kernel(const FilterSpec& f, const Shape& s, bool
     }
     key << "|G" << s.G << "J" << s.J << "T" << s.threads << "B" << s.min_blocks << "U" << s.unroll << "S" << s.stage
         << "P" << s.prefetch << "D" << (dense ? 1 : 0) << "K" << s.dense_unroll;
+    if (!item && s.grid_k > 0) key << "R" << s.grid_k;
     if (item) key << "|item" << (s.soft ? "s" : "");
     char hex[32];
     snprintf(hex, sizeof hex, "%016llx", (unsigned long long)fnv1a(key.str()));
@@ -1041,6 +1044,7 @@ GeneratedKernel generate_filter_kernel(const FilterSpec& f, const Shape& s, bool
     os << "// generated: " << key.str() << "\n";
     os << "#define RAL_G " << s.G << "\n#define RAL_J " << s.J << "\n#define RAL_THREADS " << s.threads << "\n";
     os << "#define RAL_WARPS (RAL_THREADS / 32)\n";
+    if (!item && s.grid_k > 0) os << "#define RAL_K " << s.grid_k << "\n";
     os << "struct RalParams { ral_u64 s[" << L.total << "]; };\n\n";
     auto fdata = [&](int c) { return "f" + std::to_string(c); };
     auto fvalid = [&](int c) { return "fv" + std::to_string(c); };
@@ -1116,7 +1120,12 @@ GeneratedKernel generate_filter_kernel(const FilterSpec& f, const Shape& s, bool
     // round before, so A's predecessors have long published and the look-back rarely waits.
     // Pass 1 then records the keep bits as the chunk's 32 mask words (two chunks per warp in
     // shared memory) and pass 2 turns A's words into its kept-row list.
-    const bool pipe = wide_p1 && !item;
+    // Grid mode (Shape::grid_k): static chunks, pass 1 of all of a warp's chunks, one grid barrier,
+    // then pass 2 with offsets summed from block, warp and chunk counts -- no look-back chain,
+    // which at a few thousand small chunks costs more than the rows themselves.
+    const bool grid = wide_p1 && !item && s.grid_k > 0;
+    const bool pipe = wide_p1 && !item && !grid;
+    gk.shape.grid_k = grid ? s.grid_k : 0;
     const int KBW = (s.G * s.J + 31) / 32;  // packed keep-bit words per lane
     if (item) {
         // one chunk of a batched request: the dispatcher hands over the chunk index and this
@@ -1143,6 +1152,12 @@ GeneratedKernel generate_filter_kernel(const FilterSpec& f, const Shape& s, bool
             os << "    __shared__ unsigned short s_ls[RAL_WARPS][32 * RAL_G * RAL_J];\n";
         }
         if (pipe) os << "    __shared__ ral_u32 s_kp[RAL_WARPS][2][32];\n";
+        if (grid) {
+            os << "    __shared__ ral_u32 s_kp[RAL_WARPS][RAL_K][32];\n";
+            os << "    __shared__ ral_u32 s_ct[RAL_WARPS][RAL_K];\n";
+            os << "    __shared__ ral_u32 s_wt[RAL_WARPS];\n";
+            os << "    __shared__ ral_u64 s_bpre;\n";
+        }
     }
     // per-warp staging of one slice's compacted values, so that stores are contiguous
     if (s.stage) os << "    __shared__ ral_u64 s_stage[RAL_WARPS][32 * RAL_G];\n";
@@ -1173,13 +1188,23 @@ GeneratedKernel generate_filter_kernel(const FilterSpec& f, const Shape& s, bool
             if (n_proj_vouts) os << "    ral_u32 (*const s_pvw)[RAL_G * RAL_J] = s_pv[warp];\n";
             os << "    unsigned short* const s_lst = s_ls[warp];\n";
         }
-        if (pipe) os << "    ral_u32 (*const s_kpw)[32] = s_kp[warp];\n";
+        if (pipe || grid) os << "    ral_u32 (*const s_kpw)[32] = s_kp[warp];\n";
+        if (grid) os << "    ral_u32* const s_ctw = s_ct[warp];\n";
     }
     os << "    const ral_i64 WT = 32 * RAL_G * RAL_J;\n";
     os << "    const ral_i64 nchunks = (n + WT - 1) / WT;\n";
     os << "    const ral_u32 GMASK = (RAL_G == 32) ? 0xffffffffu : ((1u << RAL_G) - 1u);\n";
     if (NVO) os << "    ral_u32 vcnt[" << NVO << "];\n    for (int i = 0; i < " << NVO << "; ++i) vcnt[i] = 0;\n";
-    if (pipe) {
+    if (grid) {
+        os << "    const ral_u64 RAL_EPOCH = (ral_u64)P.s[" << L.epoch << "];\n";
+        os << "    const ral_i64 gw = (ral_i64)blockIdx.x * RAL_WARPS + warp;\n";
+        os << "    for (int kc = 0; kc < RAL_K; ++kc) {\n";
+        os << "        const ral_i64 chunk = gw * RAL_K + kc;\n";
+        os << "        if (chunk >= nchunks) { if (lane == 0) s_ctw[kc] = 0u; continue; }\n";
+        os << "        ral_u32* const kp = s_kpw[kc];\n";
+        os << "        kp[lane] = 0u;\n";
+        os << "        __syncwarp();\n";
+    } else if (pipe) {
         os << "    int chunkA = -1;\n    ral_u32 totalA = 0;\n    int bufA = 0;\n";
         os << "    for (;;) {\n";
         os << "        ral_u32 ticket = 0;\n";
@@ -1260,7 +1285,7 @@ GeneratedKernel generate_filter_kernel(const FilterSpec& f, const Shape& s, bool
         os << "            const ral_u32 word = __shfl_sync(0xffffffffu, swc, (int)(lr >> 5));\n";
         os << "            bits &= (word >> (lr & 31u)) & " << (G1 == 32 ? "0xffffffffu" : std::to_string((1u << G1) - 1u) + "u") << ";\n";
         os << "            if (!full) {\n#pragma unroll\n                for (int g = 0; g < " << G1 << "; ++g) if (r + g >= n) bits &= ~(1u << g);\n            }\n";
-        if (pipe) {
+        if (pipe || grid) {
             os << "            if (bits) atomicOr(kp + (lr >> 5), bits << (lr & 31u));\n";
             os << "            total += __reduce_add_sync(0xffffffffu, __popc(bits));\n";
         } else {
@@ -1361,7 +1386,67 @@ GeneratedKernel generate_filter_kernel(const FilterSpec& f, const Shape& s, bool
             os << "        }\n";
         }
     }
-    if (pipe) {
+    if (grid) {
+        os << "        if (lane == 0) s_ctw[kc] = total;\n";
+        os << "    }\n";  // pass-1 chunk loop
+        // before the barrier: this block's share of the output mask words zeroed (pass 2 ORs the
+        // words it shares with neighbouring chunks), block 0 zeroes the valid counts, and the
+        // block's kept count goes to its status word
+        os << "    {\n";
+        os << "        const ral_i64 mw = (n + (ral_i64)RAL_OBASE + 31) >> 5;\n";
+        os << "        for (ral_i64 q = (ral_i64)blockIdx.x * RAL_THREADS + threadIdx.x; q < mw; q += (ral_i64)gridDim.x * RAL_THREADS) {\n";
+        for (int k : vouts) os << "            ov" << k << "[q] = 0u;\n";
+        os << "        }\n";
+        os << "        if (blockIdx.x == 0 && threadIdx.x < " << NO << ") scratch[3 + threadIdx.x] = 0ull;\n";
+        os << "    }\n";
+        os << "    __syncwarp();\n";
+        os << "    if (lane == 0) {\n";
+        os << "        ral_u32 t = 0;\n";
+        os << "        for (int kc = 0; kc < RAL_K; ++kc) t += s_ctw[kc];\n";
+        os << "        s_wt[warp] = t;\n";
+        os << "    }\n";
+        os << "    __syncthreads();\n";
+        os << "    if (threadIdx.x == 0) {\n";
+        os << "        ral_u64 bt = 0;\n";
+        os << "        for (int w = 0; w < RAL_WARPS; ++w) bt += s_wt[w];\n";
+        os << "        ral_st_status(status + blockIdx.x, bt);\n";
+        os << "        ral_grid_barrier(scratch, RAL_EPOCH + gridDim.x, scratch + 1);\n";
+        os << "    }\n";
+        os << "    __syncthreads();\n";
+        // the block's offset: the counts of the blocks before it
+        os << "    if (warp == 0) {\n";
+        os << "        ral_u64 acc = 0;\n";
+        os << "        for (ral_i64 b = lane; b < (ral_i64)blockIdx.x; b += 32) acc += ral_ld_status(status + b);\n";
+        os << "        for (int off = 16; off > 0; off >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, off);\n";
+        os << "        if (lane == 0) s_bpre = acc;\n";
+        os << "    }\n";
+        os << "    __syncthreads();\n";
+        os << "    ral_u64 wpre = s_bpre;\n";
+        os << "    for (int w = 0; w < warp; ++w) wpre += s_wt[w];\n";
+        os << "    if (blockIdx.x == gridDim.x - 1 && threadIdx.x == 0) {\n";
+        os << "        ral_u64 bt = 0;\n";
+        os << "        for (int w = 0; w < RAL_WARPS; ++w) bt += s_wt[w];\n";
+        os << "        scratch[2] = s_bpre + bt;\n";
+        os << "    }\n";
+        os << "    for (int kc = 0; kc < RAL_K; ++kc) {\n";
+        os << "        const ral_i64 chunk = gw * RAL_K + kc;\n";
+        os << "        if (chunk >= nchunks) break;\n";
+        os << "        const ral_u32 total = s_ctw[kc];\n";
+        os << "        const ral_i64 base = chunk * WT;\n";
+        os << "        const ral_u64 excl = wpre + RAL_OBASE;\n";
+        os << "        wpre += total;\n";
+        os << "        if (total != 0u) {\n";
+        os << "        {\n";
+        os << "            const ral_u32 kw = (lane < RAL_G * RAL_J) ? s_kpw[kc][lane] : 0u;\n";
+        os << "            const ral_u32 c = __popc(kw);\n";
+        os << "            ral_u32 inc = c;\n";
+        os << "            for (int off = 1; off < 32; off <<= 1) {\n";
+        os << "                const ral_u32 t = __shfl_up_sync(0xffffffffu, inc, off);\n";
+        os << "                if (lane >= off) inc += t;\n            }\n";
+        os << "            ral_u32 q = inc - c;\n";
+        os << "            for (ral_u32 m = kw; m; m &= m - 1u) s_lst[q++] = (unsigned short)(lane * 32 + __ffs(m) - 1);\n";
+        os << "        }\n";
+    } else if (pipe) {
         os << "        ral_lookback_publish(status, chunk, total);\n";
         os << "        totalB = total;\n";
         os << "        }\n";  // chunk B
@@ -1688,7 +1773,10 @@ GeneratedKernel generate_filter_kernel(const FilterSpec& f, const Shape& s, bool
     }
     // the next chunk's pass 1 rewrites the list the lanes have just read
     if (dense && !NVO) os << "        __syncwarp();\n";
-    if (pipe) {
+    if (grid) {
+        os << "        }\n";  // total != 0
+        os << "    }\n";      // pass-2 chunk loop
+    } else if (pipe) {
         os << "        }\n";  // total != 0
         os << "        }\n";  // chunk A
         os << "        if (!moreB) break;\n";

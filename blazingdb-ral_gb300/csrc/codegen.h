@@ -41,6 +41,11 @@ struct Shape {
     // dense pass 2: list steps whose loads are issued together (1 or 2; 2 measured no faster:
     // 2.15 ms against 2.09 at s = 0.5, at five blocks per SM for its registers)
     int dense_unroll = 1;
+    // filter kernels: 0 (default) takes chunks by ticket and finds each chunk's output offset by
+    // look-back; K > 0 gives each warp K consecutive chunks of a cooperative launch and one
+    // grid-wide barrier between pass 1 and pass 2 (the offsets are then sums of block, warp and
+    // chunk counts), for launches small enough that every block is resident
+    int grid_k = 0;
 };
 
 // Slot order of the kernel's parameter block (all 8-byte slots).
@@ -54,6 +59,8 @@ struct ParamLayout {
     // output pointers and bit obase + j of the output masks (a chunk appended into a mask word
     // that earlier rows have started); -1 in item functions
     int obase = -1;
+    // filter kernels with Shape::grid_k: the grid barrier counter's value before the launch
+    int epoch = -1;
     std::vector<int> lscalar_slot, rscalar_slot;  // per op of the (predicate) program, -1 if none
     int total = 0;
 };

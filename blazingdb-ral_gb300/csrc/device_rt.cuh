@@ -387,4 +387,32 @@ __device__ __forceinline__ ral_u64 ral_lookback(ral_u64* status, ral_i64 tile, r
     return ral_lookback_published(status, tile, aggregate, error_word);
 }
 
+// ---- grid-wide barrier of a cooperative launch ----------------------------------------------
+// Called by one thread per block after a block barrier.  The counter is never reset: the host
+// passes its value before the launch, and the barrier is reached when every block has added one
+// (target = that value + gridDim.x).  The release fence before the add makes the block's earlier
+// writes (ordered before this thread by the block barrier) visible to every block that sees the
+// counter reach its target; the acquire load orders the block's later reads after theirs.
+// Bounded: past RAL_GRID_SPIN_LIMIT polls the thread adds one to *error_word (a count the host
+// compares with its value before the launch) and returns.
+#define RAL_GRID_SPIN_LIMIT (1l << 22)
+RAL_FI void ral_grid_barrier(ral_u64* counter, ral_u64 target, ral_u64* error_word) {
+    __threadfence();
+    atomicAdd((unsigned long long*)counter, 1ull);
+    long spins = 0;
+    unsigned pause = 32;
+    for (;;) {
+        ral_u64 v;
+        asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(counter) : "memory");
+        if (v >= target) break;
+        if (++spins > RAL_GRID_SPIN_LIMIT) {
+            atomicAdd((unsigned long long*)error_word, 1ull);
+            break;
+        }
+        __nanosleep(pause);
+        if (pause < 256) pause <<= 1;
+    }
+    __threadfence();
+}
+
 #endif  // RAL_DEVICE_RT_CUH_

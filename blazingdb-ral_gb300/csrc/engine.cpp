@@ -107,6 +107,8 @@ std::mutex g_dev_mu;
 std::unordered_map<int, DeviceInfo> g_devs;
 std::unordered_map<std::string, int> g_occupancy;  // kernel name + device -> blocks/SM
 
+}  // namespace
+
 int device_sms() {
     int dev = 0;
     cudaGetDevice(&dev);
@@ -141,6 +143,8 @@ int blocks_per_sm(const CompiledKernel& k, int threads) {
     g_occupancy[key] = b;
     return b;
 }
+
+namespace {
 
 bool aligned(const void* p, size_t a) { return ((uintptr_t)p % a) == 0; }
 

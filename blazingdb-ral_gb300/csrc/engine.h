@@ -82,6 +82,9 @@ int build_program(Program& p, gdf_column* const* outputs, int n_out, gdf_column*
 
 // Number of SMs and resident blocks per SM for a compiled kernel on the current device.
 int launch_blocks(const CompiledKernel& k, int threads, int64_t work_items_per_block_unit, int64_t units);
+// SMs of the current device; resident blocks per SM of a compiled kernel (cached per device).
+int device_sms();
+int blocks_per_sm(const CompiledKernel& k, int threads);
 
 // Parameter block filled in ParamLayout order.
 void fill_scalars(const Program& p, const ParamLayout& L, std::vector<uint64_t>& slots);

@@ -7,6 +7,7 @@
 #include "filter.h"
 
 #include <algorithm>
+#include <atomic>
 #include <chrono>
 #include <cstdlib>
 #include <map>
@@ -261,6 +262,10 @@ struct PreparedFilter {
     bool have_pred = false, have_proj = false;
     GeneratedKernel gk;
     const CompiledKernel* k = nullptr;
+    // the same filter in grid mode (Shape::grid_k), for synchronous calls whose blocks all fit
+    // on the device at once; null where the size class is large or the shape does not allow it
+    GeneratedKernel gk_grid;
+    const CompiledKernel* k_grid = nullptr;
 };
 
 std::mutex g_prep_mu;
@@ -368,15 +373,73 @@ Shape default_filter_shape(const FilterSpec& spec, bool aligned16, int64_t n) {
     return sh;
 }
 
-// Finishes a PreparedFilter whose spec (frame, predicate, projection, outputs) is filled in.
-int prepare_kernel(PreparedFilter& pf, bool aligned16, int64_t n) {
-    Shape sh = default_filter_shape(pf.spec, aligned16, n);
+// Size classes up to this many rows also get the grid-mode kernel.  Its pass 1 reads the whole
+// table before any pass 2 starts, so the predicate columns should still be in L2 by then.
+constexpr int64_t kGridModeMaxRows = (int64_t)1 << 23;
+
+// Finishes a PreparedFilter whose spec (frame, predicate, projection, outputs) is filled in, for
+// calls of n_shape rows (the shape) up to n_max rows (the size class).
+int prepare_kernel(PreparedFilter& pf, bool aligned16, int64_t n_shape, int64_t n_max) {
+    Shape sh = default_filter_shape(pf.spec, aligned16, n_shape);
     apply_tune(sh, filter_tune());
+    const int tuned_k = sh.grid_k;
+    sh.grid_k = 0;
     pf.gk = generate_filter_kernel(pf.spec, sh);
     std::string err;
     pf.k = jit_get(pf.gk, err);
     if (!pf.k) return set_error(kJitError, err);
+    // grid mode: K chunks per warp so that the class's largest call needs at most the blocks that
+    // min_blocks per SM give (checked again against the real occupancy at launch); RAL_FILTER_TUNE
+    // R=0 turns it off, R=K forces K
+    if (n_max <= kGridModeMaxRows || tuned_k > 0) {
+        Shape gs = sh;
+        const int64_t wt = filter_tile_rows(sh);
+        const int64_t warps = (int64_t)device_sms() * std::max(1, sh.min_blocks) * (sh.threads / 32);
+        const int64_t chunks = (std::max<int64_t>(n_max, 1) + wt - 1) / wt;
+        gs.grid_k = tuned_k > 0 ? tuned_k : (int)std::max<int64_t>(1, (chunks + warps - 1) / warps);
+        if (filter_tune().find("R=0") != std::string::npos) gs.grid_k = 0;
+        if (gs.grid_k > 0 && gs.grid_k <= 16) {
+            GeneratedKernel gg = generate_filter_kernel(pf.spec, gs);
+            if (gg.shape.grid_k > 0) {
+                pf.gk_grid = std::move(gg);
+                pf.k_grid = jit_get(pf.gk_grid, err);
+                if (!pf.k_grid) return set_error(kJitError, err);
+            }
+        }
+    }
     return kSuccess;
+}
+
+// Per thread and device: the grid-mode scratch (barrier counter, error count, kept count, valid
+// counts, one status word per block).  The barrier counter only grows, so the area is zeroed
+// once and then only after a failed call; `epoch` is the counter's value before the next launch.
+struct GridArea {
+    void* p = nullptr;
+    size_t words = 0;
+    uint64_t epoch = 0;
+    uint64_t err_seen = 0;
+    bool dirty = true;
+};
+thread_local std::unordered_map<int, GridArea> t_grid;
+constexpr size_t kGridAreaWords = 3 + 64 + 8192;
+std::atomic<int64_t> g_grid_launches{0};
+
+// A synchronous caller's request for grid mode (no other launch may share the calling thread's
+// grid area meanwhile): whether it was used, and the area's error count before the launch.
+struct GridCall {
+    bool used = false;
+    uint64_t err_base = 0;
+};
+
+// The grid-mode launch of a prepared filter over n rows, if its blocks fit on the device at once.
+int grid_blocks(const PreparedFilter& pf, int64_t n) {
+    if (!pf.k_grid || n <= 0) return 0;
+    const Shape& gs = pf.gk_grid.shape;
+    const int64_t per_block = filter_tile_rows(gs) * (gs.threads / 32) * gs.grid_k;
+    const int64_t need = (n + per_block - 1) / per_block;
+    const int64_t cap = (int64_t)blocks_per_sm(*pf.k_grid, gs.threads) * device_sms();
+    if (need > cap || need + 3 + 64 > (int64_t)kGridAreaWords) return 0;
+    return (int)need;
 }
 
 // Scratch words a prepared filter needs over n rows: the header and one status word per chunk.
@@ -391,7 +454,8 @@ int64_t prepared_scratch_words(const PreparedFilter& pf, int64_t n) {
 // taken obase rows lower, so row j still lands at element j), and copies the header -- kept count,
 // error word, valid counts -- to host_header.  ev (optional) brackets the launch.
 int enqueue_prepared(const PreparedFilter& pf, gdf_column* const* frame, gdf_column* const* outs, void* scratch,
-                     int obase, unsigned long long* host_header, cudaStream_t st, cudaEvent_t* ev) {
+                     int obase, unsigned long long* host_header, cudaStream_t st, cudaEvent_t* ev,
+                     GridCall* grid_call = nullptr) {
     const int64_t n = frame[0]->size;
     const FilterSpec& spec = pf.spec;
     const int NO = (int)spec.outputs.size();
@@ -402,13 +466,39 @@ int enqueue_prepared(const PreparedFilter& pf, gdf_column* const* frame, gdf_col
         if (outs[q]->valid && !aligned_to(outs[q]->valid, 4))
             return set_error(kInvalidArgument, "validity masks must be 4-byte aligned");
     if (obase < 0 || obase > 31) return set_error(kInvalidArgument, "output row offset out of range");
-    const ParamLayout& L = pf.gk.layout;
-    const int64_t tile_rows = filter_tile_rows(pf.gk.shape);
+    const int gblocks = grid_call ? grid_blocks(pf, n) : 0;
+    const GeneratedKernel& gk = gblocks ? pf.gk_grid : pf.gk;
+    const ParamLayout& L = gk.layout;
+    const int64_t tile_rows = filter_tile_rows(gk.shape);
     const int64_t header = filter_scratch_header(NO);
-    cudaMemsetAsync(scratch, 0, (size_t)prepared_scratch_words(pf, n) * 8, st);
-    // output masks are assembled with OR at the edges of each warp's range: start from zero
-    for (int q = 0; q < NO; q++)
-        if (spec.outputs[q].has_valid) cudaMemsetAsync(outs[q]->valid, 0, (size_t)((n + obase + 31) / 32) * 4, st);
+    GridArea* area = nullptr;
+    if (gblocks) {
+        // grid mode: the kernel zeroes the output masks and valid counts itself; the area is
+        // zeroed only when new or after a failed call
+        int dev = 0;
+        if (int e = check_cuda(cudaGetDevice(&dev), "cudaGetDevice")) return e;
+        area = &t_grid[dev];
+        if (!area->p) {
+            if (int e = check_cuda(cudaMalloc(&area->p, kGridAreaWords * 8), "cudaMalloc")) return e;
+            area->words = kGridAreaWords;
+            area->dirty = true;
+        }
+        if (area->dirty) {
+            if (int e = check_cuda(cudaMemsetAsync(area->p, 0, area->words * 8, st), "cudaMemsetAsync")) return e;
+            area->epoch = 0;
+            area->err_seen = 0;
+            area->dirty = false;
+        }
+        scratch = area->p;
+        grid_call->used = true;
+        grid_call->err_base = area->err_seen;
+    } else {
+        if (grid_call) grid_call->used = false;
+        cudaMemsetAsync(scratch, 0, (size_t)prepared_scratch_words(pf, n) * 8, st);
+        // output masks are assembled with OR at the edges of each warp's range: start from zero
+        for (int q = 0; q < NO; q++)
+            if (spec.outputs[q].has_valid) cudaMemsetAsync(outs[q]->valid, 0, (size_t)((n + obase + 31) / 32) * 4, st);
+    }
 
     std::vector<uint64_t> slots(L.total, 0);
     slots[L.n_rows] = (uint64_t)n;
@@ -423,19 +513,32 @@ int enqueue_prepared(const PreparedFilter& pf, gdf_column* const* frame, gdf_col
     }
     slots[L.scratch] = (uint64_t)(uintptr_t)scratch;
     if (L.obase >= 0) slots[L.obase] = (uint64_t)obase;
+    if (gblocks) slots[L.epoch] = area->epoch;
     if (pf.have_pred) fill_scalars(pf.pred, L, slots);
     if (pf.have_proj) {
         ParamLayout QL;
-        QL.lscalar_slot = pf.gk.layout_project_lscalar;
-        QL.rscalar_slot = pf.gk.layout_project_rscalar;
+        QL.lscalar_slot = gk.layout_project_lscalar;
+        QL.rscalar_slot = gk.layout_project_rscalar;
         fill_scalars(pf.proj, QL, slots);
     }
-    const int grid = launch_blocks(*pf.k, pf.gk.shape.threads, tile_rows * (pf.gk.shape.threads / 32), n);
     void* args[] = {slots.data()};
     if (ev) cudaEventRecord(ev[0], st);
-    if (int e = check_cuda(cudaLaunchKernel((const void*)pf.k->kernel, dim3(grid), dim3(pf.gk.shape.threads), args, 0, st),
-                           "launch of the filter kernel"))
-        return e;
+    if (gblocks) {
+        // every block must be resident for the grid barrier: a cooperative launch guarantees it
+        if (int e = check_cuda(cudaLaunchCooperativeKernel((const void*)pf.k_grid->kernel, dim3(gblocks),
+                                                           dim3(gk.shape.threads), args, 0, st),
+                               "cooperative launch of the filter kernel")) {
+            area->dirty = true;
+            return e;
+        }
+        area->epoch += (uint64_t)gblocks;
+        g_grid_launches++;
+    } else {
+        const int grid = launch_blocks(*pf.k, gk.shape.threads, tile_rows * (gk.shape.threads / 32), n);
+        if (int e = check_cuda(cudaLaunchKernel((const void*)pf.k->kernel, dim3(grid), dim3(gk.shape.threads), args, 0, st),
+                               "launch of the filter kernel"))
+            return e;
+    }
     if (ev) cudaEventRecord(ev[1], st);
     note_launch();
     return check_cuda(cudaMemcpyAsync(host_header, scratch, (size_t)header * 8, cudaMemcpyDeviceToHost, st),
@@ -472,7 +575,8 @@ int run_prepared(const PreparedFilter& pf, gdf_column* const* frame, gdf_column*
     }
     unsigned long long* hp = nullptr;
     if (int e = header_get((size_t)header, &hp)) return e;
-    if (int e = enqueue_prepared(pf, frame, outs, scratch, 0, hp, st, timing ? ev : nullptr)) return e;
+    GridCall gc;
+    if (int e = enqueue_prepared(pf, frame, outs, scratch, 0, hp, st, timing ? ev : nullptr, &gc)) return e;
     const auto t_wait0 = std::chrono::steady_clock::now();
     if (int e = check_cuda(cudaStreamSynchronize(st), "filter kernel")) return e;
     if (timing) {
@@ -482,7 +586,18 @@ int run_prepared(const PreparedFilter& pf, gdf_column* const* frame, gdf_column*
         call_timing_add(std::chrono::duration<double, std::micro>(t_wait0 - t_enq0).count(),
                         std::chrono::duration<double, std::micro>(t_end - t_wait0).count(), dev_ms * 1e3);
     }
-    if (hp[1]) return set_error(kTimeout, "filter look-back wait gave up");
+    if (gc.used) {
+        // the error word of the grid area counts the blocks whose barrier wait gave up
+        if (hp[1] != gc.err_base) {
+            int dev = 0;
+            cudaGetDevice(&dev);
+            t_grid[dev].err_seen = hp[1];
+            t_grid[dev].dirty = true;
+            return set_error(kTimeout, "filter grid barrier wait gave up");
+        }
+    } else if (hp[1]) {
+        return set_error(kTimeout, "filter look-back wait gave up");
+    }
     const int64_t n_out = (int64_t)hp[2];
     finish_outputs(pf, frame, outs, hp, n_out);
     *n_out_p = (gdf_size_type)n_out;
@@ -503,7 +618,7 @@ int prepared(const std::string& key0, bool aligned16, int64_t n, Build&& build, 
     }
     auto pf = std::make_unique<PreparedFilter>();
     if (int e = build(*pf)) return e;
-    if (int e = prepare_kernel(*pf, aligned16, cls / 2 + 1)) return e;
+    if (int e = prepare_kernel(*pf, aligned16, cls / 2 + 1, cls)) return e;
     std::lock_guard<std::mutex> lock(g_prep_mu);
     auto res = g_prepared.emplace(key, std::move(pf));
     *out = res.first->second.get();
@@ -905,6 +1020,8 @@ struct HostFilterArea {
 size_t round256(size_t b) { return (b + 255) & ~(size_t)255; }
 
 }  // namespace
+
+int64_t filter_grid_launches() { return g_grid_launches.load(); }
 
 int filter_host(gdf_column* const* frame, int ncols, const char* filter_q, const char* project_q,
                 gdf_column* const* outs, int n_outs, gdf_size_type* n_out_p, int64_t chunk_rows) {

@@ -48,6 +48,10 @@ int64_t standalone_scratch_words(const void* handle, int64_t n);
 int enqueue_standalone_filter(const void* handle, gdf_column* const* frame, gdf_column* const* outs, void* scratch,
                               unsigned long long* host_header, cudaStream_t st);
 
+// Launches of fused filter kernels in grid mode (a cooperative launch with one grid barrier in
+// place of the look-back) since the library was loaded.
+int64_t filter_grid_launches();
+
 // A LogicalProject over a LogicalFilter, planned for a frame: the fused filter's spec and the
 // dtype / mask presence of every output (evaluated outputs carry a mask; a pass-through output
 // carries one exactly when its frame column does).  Holds the programs the spec points to.

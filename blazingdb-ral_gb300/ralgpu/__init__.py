@@ -13,7 +13,7 @@ from .capi import (RalError, lib, perform_operation, perform_operation_async, pe
                    get_output_type_expression,
                    debug_program_source, debug_filter_source, jit_stats, kernel_launches, version,
                    parse_project_plan, Batch, autotune_program, batch_tune_key, Server, softfp_selftest,
-                   debug_lookback_timeout, process_aggregate, debug_aggregate_source, call_timing,
+                   debug_lookback_timeout, process_aggregate, debug_aggregate_source, call_timing, filter_grid_launches,
                    Category, category_column, decode_category, filter_project_host)
 from .column import Column, Scalar, valid_alloc_size
 from . import dtypes
@@ -24,6 +24,6 @@ __all__ = [
     "materialize_column", "materialize_columns", "apply_boolean_mask", "add_expression_to_plan", "get_output_type_expression",
     "debug_program_source", "debug_filter_source", "jit_stats", "kernel_launches", "version", "Column", "Scalar",
     "valid_alloc_size", "dtypes", "parse_project_plan", "Batch", "autotune_program", "batch_tune_key", "Server", "softfp_selftest", "debug_lookback_timeout",
-    "process_aggregate", "debug_aggregate_source", "call_timing", "Category", "category_column",
+    "process_aggregate", "debug_aggregate_source", "call_timing", "filter_grid_launches", "Category", "category_column",
     "decode_category", "filter_project_host",
 ]

@@ -54,6 +54,7 @@ _SIGS = {
     "ral_process_aggregate": (C.c_int, [C.c_void_p, C.c_int32, C.c_char_p, C.POINTER(GdfScalar), C.c_int32,
                                         C.POINTER(C.c_int32)]),
     "ral_debug_call_timing": (C.c_int, [C.c_int32, C.c_int32, C.POINTER(C.c_int64), C.POINTER(C.c_double)]),
+    "ral_debug_filter_grid_launches": (C.c_int, [C.POINTER(C.c_int64)]),
     "ral_filter_project_host": (C.c_int, [C.c_void_p, C.c_int32, C.c_char_p, C.c_char_p, C.c_void_p, C.c_int32,
                                           C.POINTER(C.c_int32), C.c_int64]),
     "ral_category_create": (C.c_int, [C.c_void_p, C.c_int64, C.POINTER(C.c_void_p), I32P]),
@@ -481,6 +482,13 @@ def call_timing(enable: bool = True, reset: bool = False) -> dict:
     _check(lib().ral_debug_call_timing(1 if enable else 0, 1 if reset else 0, C.byref(calls), us))
     return {"calls": calls.value, "host_prepare_us": us[0], "enqueue_us": us[1], "wait_us": us[2],
             "kernel_device_us": us[3]}
+
+
+def filter_grid_launches() -> int:
+    """Fused filter launches that ran in grid mode (one grid barrier in place of the look-back)."""
+    v = C.c_int64(0)
+    _check(lib().ral_debug_filter_grid_launches(C.byref(v)))
+    return v.value
 
 
 class Category:

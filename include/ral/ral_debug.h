@@ -54,6 +54,10 @@ int ral_debug_aggregate_source(const gdf_dtype *frame_dtypes, const int32_t *fra
  * enqueue, wait for completion and kernel device time, in microseconds. */
 int ral_debug_call_timing(int32_t enable, int32_t reset, int64_t *calls, double *us4);
 
+/* Fused filter launches that ran in grid mode (synchronous calls of at most 8Mi rows whose blocks
+ * all fit on the device: one cooperative launch, a grid barrier in place of the look-back). */
+int ral_debug_filter_grid_launches(int64_t *launches);
+
 /* Compiles every query's chunk function and links the dispatcher without loading it (no GPU
  * needed); the ptxas / link log goes to log_out. */
 int ral_server_debug_compile(ral_server *server, char *log_out, int64_t log_capacity);

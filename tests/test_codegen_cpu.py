@@ -94,7 +94,8 @@ FILTER_CASES = [
 
 
 @pytest.mark.parametrize("tune", ["", "S=1", "J=8,U=2,T=128,B=4", "J=64,U=8,T=512,B=1,S=1", "P=8", "P=4,J=16",
-                                  "D=1", "D=0", "D=1,J=8,T=128", "K=2,B=5", "P=1,K=2,B=4"])
+                                  "D=1", "D=0", "D=1,J=8,T=128", "K=2,B=5", "P=1,K=2,B=4", "R=1", "R=3,J=4",
+                                  "R=2,J=2,T=128", "R=4,D=0"])
 @pytest.mark.parametrize("case", FILTER_CASES, ids=[c[0] for c in FILTER_CASES])
 def test_filter_kernels_compile(case, tune, monkeypatch):
     _, dtypes, nullable, fq, pq = case
@@ -191,3 +192,22 @@ def test_aggregate_plan_matches_the_oracle_parse():
     src, _ = ralgpu.debug_aggregate_source([4, 6], [0, 0], [0, 0], q, compile=False)
     # SUM, AVG, MIN and MAX each fold one slot; COUNT() needs none
     assert src.count("acc3 =") >= 1 and "acc4" not in src
+
+
+def test_grid_mode_replaces_the_look_back(monkeypatch):
+    """R=K: each warp owns K consecutive chunks, pass 1 of all of them, one grid barrier, then pass
+    2 at offsets summed from block, warp and chunk counts; the kernel zeroes the output masks and
+    valid counts itself.  Shapes without the mask-word pass 1 (D=0) keep the look-back."""
+    p = W.fused_project_program()
+    monkeypatch.setenv("RAL_FILTER_TUNE", "R=2")
+    src, log = ralgpu.debug_filter_source(p.input_dtypes, [1] * 5, W.filter_project_filter(0.5),
+                                          W.FILTER_PROJECT_PROJECT, compile=True)
+    body = src[src.index("extern \"C\" __global__"):]
+    assert "ral_grid_barrier(scratch, RAL_EPOCH + gridDim.x, scratch + 1)" in body
+    assert "ral_lookback" not in body and "atomicAdd((unsigned int*)scratch" not in body
+    assert "#define RAL_K 2" in src and spills(log) <= 64
+    monkeypatch.setenv("RAL_FILTER_TUNE", "R=2,D=0")
+    src, _ = ralgpu.debug_filter_source(p.input_dtypes, [1] * 5, W.filter_project_filter(0.5),
+                                        W.FILTER_PROJECT_PROJECT)
+    body = src[src.index("extern \"C\" __global__"):]
+    assert "ral_grid_barrier" not in body and "ral_lookback" in body
