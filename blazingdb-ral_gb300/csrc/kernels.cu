@@ -93,19 +93,39 @@ cudaError_t gather_by_index(const void* in, const uint32_t* in_valid, int64_t n_
 // ---- every column of a frame gathered by one index column -----------------------------------
 // A warp takes 128 consecutive output rows per step; lane t handles rows base + t + 32 k (k < 4),
 // so each k is one coalesced index load, one coalesced store per column and one ballot-built
-// validity word per nullable column, and every lane has four independent gathers in flight per
-// column.  The index is read once for all columns (materialize_column, called once per column,
-// reads it twice per column: its bit gather and its data gather).
+// validity word per nullable column, and every lane has eight independent loads in flight per
+// column (four elements, four mask words).
+//
+// Two orders, chosen per launch from a sample of the index (every block computes the same choice):
+// * clustered indices (a filter's kept rows, a sorted join side): row-major -- a step gathers every
+//   column, so the index is read once and each column's nearby rows share cache lines;
+// * scattered indices (an order-by permutation, a hash join): column-major -- the whole grid
+//   gathers one column before the next.  Each column's random reads then stay within its own
+//   span, and its validity mask (n/8 bytes) stays in L2 instead of competing with every other
+//   column's mask; measured on six columns of 200M rows by a permutation, row-major took 48.7 ms
+//   against 33.4 ms for six one-column passes.  The index is re-read per column (4 B per row).
+// Element loads are marked evict-first (`ld.global.cs`): a scattered element is read once, and the
+// masks are what L2 should keep.
 constexpr int kGatherRowsPerLane = 4;
+constexpr int kGatherSamples = 64;          // index samples of 32 consecutive rows
+constexpr long long kGatherClusterSpan = 1 << 16;  // a sample spanning fewer input rows is clustered
 
 template <typename I>
 __device__ __forceinline__ ral_i64 ral_load_index(const void* idx, ral_i64 i) {
     return (ral_i64)__ldcs(reinterpret_cast<const I*>(idx) + i);
 }
 
-// One column's step: the four data loads and the four validity-word loads are all issued before
-// any is used, so each lane has eight independent random reads in flight and a column costs one
-// memory round trip (the loaded values are consumed only by the stores and ballots after them).
+__device__ __forceinline__ ral_i64 ral_index_at(const GatherColumnsParams& P, ral_i64 i) {
+    switch (P.idx_width) {
+    case 1: return ral_load_index<int8_t>(P.idx, i);
+    case 2: return ral_load_index<int16_t>(P.idx, i);
+    case 4: return ral_load_index<int32_t>(P.idx, i);
+    default: return ral_load_index<long long>(P.idx, i);
+    }
+}
+
+// One column's step: the four element loads and the four validity-word loads are all issued before
+// any is used (their values feed only the stores and ballots after them).
 template <typename E>
 __device__ __forceinline__ unsigned ral_gather_k(const GatherColumn& c, const ral_i64 (&j)[kGatherRowsPerLane],
                                                  const bool (&ok)[kGatherRowsPerLane], ral_i64 base, int lane,
@@ -117,7 +137,7 @@ __device__ __forceinline__ unsigned ral_gather_k(const GatherColumn& c, const ra
     ral_u32 w[kGatherRowsPerLane];
 #pragma unroll
     for (int k = 0; k < kGatherRowsPerLane; ++k) {
-        v[k] = ok[k] ? __ldg(in + j[k]) : E(0);
+        v[k] = ok[k] ? __ldcs(in + j[k]) : E(0);
         w[k] = ok[k] ? (iv ? __ldg(iv + (j[k] >> 5)) : 0xffffffffu) : 0u;
     }
 #pragma unroll
@@ -138,45 +158,90 @@ __device__ __forceinline__ unsigned ral_gather_k(const GatherColumn& c, const ra
     return cnt;
 }
 
-// 40 registers (six blocks of 256 threads per SM): the gathers are latency-bound, so resident
-// warps -- loads in flight -- matter more than registers.
-__global__ void __launch_bounds__(256, 6) gather_columns_kernel(const __grid_constant__ GatherColumnsParams P) {
+__device__ __forceinline__ unsigned ral_gather_column_step(const GatherColumn& col, const ral_i64 (&j)[kGatherRowsPerLane],
+                                                           const bool (&ok)[kGatherRowsPerLane], ral_i64 base,
+                                                           int lane, ral_i64 n_out) {
+    switch (col.width) {
+    case 1: return ral_gather_k<int8_t>(col, j, ok, base, lane, n_out);
+    case 2: return ral_gather_k<short>(col, j, ok, base, lane, n_out);
+    case 4: return ral_gather_k<int>(col, j, ok, base, lane, n_out);
+    default: return ral_gather_k<long long>(col, j, ok, base, lane, n_out);
+    }
+}
+
+__device__ __forceinline__ void ral_step_indices(const GatherColumnsParams& P, ral_i64 base, int lane,
+                                                 ral_i64 (&j)[kGatherRowsPerLane], bool (&ok)[kGatherRowsPerLane]) {
+#pragma unroll
+    for (int k = 0; k < kGatherRowsPerLane; ++k) {
+        const ral_i64 i = base + lane + 32 * k;
+        j[k] = i < P.n_out ? ral_index_at(P, i) : -1;
+        ok[k] = j[k] >= 0 && j[k] < P.n_in;
+    }
+}
+
+// Clustered samples among the 32 that warp `warp` (0 or 1) tests; kept out of line so that its
+// registers do not add to the gather loops'.
+__device__ __noinline__ int ral_gather_votes(const GatherColumnsParams& P, int warp, int lane) {
+    int votes = 0;
+    for (int q = warp * 32; q < warp * 32 + 32; ++q) {
+        const ral_i64 at = (P.n_out - 32) / (kGatherSamples - 1) * q;
+        const ral_i64 j = ral_index_at(P, at + lane);
+        const bool in = j >= 0 && j < P.n_in;
+        long long lo = in ? j : LLONG_MAX, hi = in ? j : LLONG_MIN;
+        for (int off = 16; off > 0; off >>= 1) {
+            lo = min(lo, __shfl_xor_sync(0xffffffffu, lo, off));
+            hi = max(hi, __shfl_xor_sync(0xffffffffu, hi, off));
+        }
+        votes += (hi < lo || hi - lo < kGatherClusterSpan) ? 1 : 0;
+    }
+    return votes;
+}
+
+// 48 registers, five resident blocks of 256 threads per SM (a bound of six spills registers in the
+// gather loops).
+__global__ void __launch_bounds__(256, 5) gather_columns_kernel(const __grid_constant__ GatherColumnsParams P) {
     __shared__ unsigned long long s_cnt[kMaxGatherColumns];
+    __shared__ int s_clustered;
     for (int c = threadIdx.x; c < P.num_columns; c += blockDim.x) s_cnt[c] = 0;
-    __syncthreads();
     const int lane = threadIdx.x & 31;
+    const int warp = threadIdx.x >> 5;
+    // the order: warps 0 and 1 each test 32 samples of 32 consecutive indices (the same samples in
+    // every block); a sample is clustered when its in-range indices span fewer than
+    // kGatherClusterSpan input rows; a launch is clustered when at least half its samples are
+    if (threadIdx.x == 0) s_clustered = 0;
+    __syncthreads();
+    if (P.num_columns > 1 && P.n_out >= 32 * kGatherSamples && warp < 2) {
+        const int votes = ral_gather_votes(P, warp, lane);
+        if (lane == 0) atomicAdd(&s_clustered, votes);
+    }
+    __syncthreads();
+    const bool row_major = P.num_columns == 1 || P.n_out < 32 * kGatherSamples || 2 * s_clustered >= kGatherSamples;
     const ral_i64 step_rows = 32 * kGatherRowsPerLane;
     const ral_i64 nsteps = (P.n_out + step_rows - 1) / step_rows;
     const ral_i64 gwarp = ((ral_i64)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const ral_i64 nwarp = ((ral_i64)gridDim.x * blockDim.x) >> 5;
-    for (ral_i64 s = gwarp; s < nsteps; s += nwarp) {
-        const ral_i64 base = s * step_rows;
-        ral_i64 j[kGatherRowsPerLane];
-        bool ok[kGatherRowsPerLane];
-#pragma unroll
-        for (int k = 0; k < kGatherRowsPerLane; ++k) {
-            const ral_i64 i = base + lane + 32 * k;
-            j[k] = -1;
-            if (i < P.n_out) {
-                switch (P.idx_width) {
-                case 1: j[k] = ral_load_index<int8_t>(P.idx, i); break;
-                case 2: j[k] = ral_load_index<int16_t>(P.idx, i); break;
-                case 4: j[k] = ral_load_index<int32_t>(P.idx, i); break;
-                default: j[k] = ral_load_index<long long>(P.idx, i); break;
-                }
+    if (row_major) {
+        for (ral_i64 s = gwarp; s < nsteps; s += nwarp) {
+            const ral_i64 base = s * step_rows;
+            ral_i64 j[kGatherRowsPerLane];
+            bool ok[kGatherRowsPerLane];
+            ral_step_indices(P, base, lane, j, ok);
+            for (int c = 0; c < P.num_columns; ++c) {
+                const unsigned cnt = ral_gather_column_step(P.col[c], j, ok, base, lane, P.n_out);
+                if (lane == 0 && cnt) atomicAdd(&s_cnt[c], (unsigned long long)cnt);
             }
-            ok[k] = j[k] >= 0 && j[k] < P.n_in;
         }
+    } else {
         for (int c = 0; c < P.num_columns; ++c) {
-            const GatherColumn& col = P.col[c];
-            unsigned cnt;
-            switch (col.width) {
-            case 1: cnt = ral_gather_k<int8_t>(col, j, ok, base, lane, P.n_out); break;
-            case 2: cnt = ral_gather_k<short>(col, j, ok, base, lane, P.n_out); break;
-            case 4: cnt = ral_gather_k<int>(col, j, ok, base, lane, P.n_out); break;
-            default: cnt = ral_gather_k<long long>(col, j, ok, base, lane, P.n_out); break;
+            unsigned long long cc = 0;
+            for (ral_i64 s = gwarp; s < nsteps; s += nwarp) {
+                const ral_i64 base = s * step_rows;
+                ral_i64 j[kGatherRowsPerLane];
+                bool ok[kGatherRowsPerLane];
+                ral_step_indices(P, base, lane, j, ok);
+                cc += ral_gather_column_step(P.col[c], j, ok, base, lane, P.n_out);
             }
-            if (lane == 0 && cnt) atomicAdd(&s_cnt[c], (unsigned long long)cnt);
+            if (lane == 0 && cc) atomicAdd(&s_cnt[c], cc);
         }
     }
     __syncthreads();
