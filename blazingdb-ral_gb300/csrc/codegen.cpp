@@ -970,7 +970,10 @@ GeneratedKernel generate_filter_kernel(const FilterSpec& f, const Shape& s, bool
     gk.layout_project_lscalar = QL.lscalar_slot;
     gk.layout_project_rscalar = QL.rscalar_slot;
     if (!item) L.obase = slot++;
-    if (!item && s.grid_k > 0) L.epoch = slot++;
+    if (!item && s.grid_k > 0) {
+        L.epoch = slot++;
+        L.hostmap = slot++;
+    }
     L.total = slot;
 
     std::vector<int> vouts;  // outputs with a mask
@@ -1794,6 +1797,24 @@ GeneratedKernel generate_filter_kernel(const FilterSpec& f, const Shape& s, bool
         os << "    for (int i = 0; i < " << NVO << "; ++i) {\n";
         os << "        const ral_u32 v = __reduce_add_sync(0xffffffffu, vcnt[i]);\n";
         os << "        if (lane == 0 && v) atomicAdd((unsigned long long*)(scratch + 3 + vmap[i]), (unsigned long long)v);\n";
+        os << "    }\n";
+    }
+    if (grid) {
+        // the grid counter takes a second step per block at the end (the launch moves it by twice
+        // the grid); the block that completes it copies the header -- error count, kept count,
+        // valid counts -- to the caller's host-mapped header and then writes the counter's final
+        // value as the completion tag, so the host sees the result without a copy back
+        os << "    __syncthreads();\n";
+        os << "    if (threadIdx.x == 0) {\n";
+        os << "        __threadfence();\n";
+        os << "        const ral_u64 fin = RAL_EPOCH + 2ull * gridDim.x;\n";
+        os << "        if (atomicAdd((unsigned long long*)scratch, 1ull) + 1ull == fin) {\n";
+        os << "            __threadfence();\n";
+        os << "            volatile ral_u64* const hm = (volatile ral_u64*)P.s[" << L.hostmap << "];\n";
+        os << "            for (int i = 1; i < " << 3 + NO << "; ++i) hm[i] = ral_ld_status(scratch + i);\n";
+        os << "            __threadfence_system();\n";
+        os << "            hm[0] = fin;\n";
+        os << "        }\n";
         os << "    }\n";
     }
     os << "}\n";

@@ -59,8 +59,11 @@ struct ParamLayout {
     // output pointers and bit obase + j of the output masks (a chunk appended into a mask word
     // that earlier rows have started); -1 in item functions
     int obase = -1;
-    // filter kernels with Shape::grid_k: the grid barrier counter's value before the launch
+    // filter kernels with Shape::grid_k: the grid counter's value before the launch, and the
+    // device address of the caller's host-mapped header (the last block to finish writes the
+    // header there, then a completion tag)
     int epoch = -1;
+    int hostmap = -1;
     std::vector<int> lscalar_slot, rscalar_slot;  // per op of the (predicate) program, -1 if none
     int total = 0;
 };

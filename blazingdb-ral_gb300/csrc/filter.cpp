@@ -263,9 +263,12 @@ struct PreparedFilter {
     GeneratedKernel gk;
     const CompiledKernel* k = nullptr;
     // the same filter in grid mode (Shape::grid_k), for synchronous calls whose blocks all fit
-    // on the device at once; null where the size class is large or the shape does not allow it
-    GeneratedKernel gk_grid;
-    const CompiledKernel* k_grid = nullptr;
+    // on the device at once: its shape is chosen with the plan, the kernel compiled on the first
+    // call that can use it (null where the size class is large or the shape does not allow it)
+    Shape grid_shape;
+    mutable std::once_flag grid_once;
+    mutable GeneratedKernel gk_grid;
+    mutable const CompiledKernel* k_grid = nullptr;
 };
 
 std::mutex g_prep_mu;
@@ -391,23 +394,29 @@ int prepare_kernel(PreparedFilter& pf, bool aligned16, int64_t n_shape, int64_t 
     // grid mode: K chunks per warp so that the class's largest call needs at most the blocks that
     // min_blocks per SM give (checked again against the real occupancy at launch); RAL_FILTER_TUNE
     // R=0 turns it off, R=K forces K
+    pf.grid_shape = sh;
     if (n_max <= kGridModeMaxRows || tuned_k > 0) {
-        Shape gs = sh;
         const int64_t wt = filter_tile_rows(sh);
         const int64_t warps = (int64_t)device_sms() * std::max(1, sh.min_blocks) * (sh.threads / 32);
         const int64_t chunks = (std::max<int64_t>(n_max, 1) + wt - 1) / wt;
-        gs.grid_k = tuned_k > 0 ? tuned_k : (int)std::max<int64_t>(1, (chunks + warps - 1) / warps);
-        if (filter_tune().find("R=0") != std::string::npos) gs.grid_k = 0;
-        if (gs.grid_k > 0 && gs.grid_k <= 16) {
-            GeneratedKernel gg = generate_filter_kernel(pf.spec, gs);
-            if (gg.shape.grid_k > 0) {
-                pf.gk_grid = std::move(gg);
-                pf.k_grid = jit_get(pf.gk_grid, err);
-                if (!pf.k_grid) return set_error(kJitError, err);
-            }
-        }
+        pf.grid_shape.grid_k = tuned_k > 0 ? tuned_k : (int)std::max<int64_t>(1, (chunks + warps - 1) / warps);
+        if (filter_tune().find("R=0") != std::string::npos || pf.grid_shape.grid_k > 16) pf.grid_shape.grid_k = 0;
     }
     return kSuccess;
+}
+
+// The grid-mode kernel of a prepared filter, compiled once on first use; null when the shape has
+// no grid mode or it failed to compile (the call then takes the look-back kernel).
+const CompiledKernel* grid_kernel(const PreparedFilter& pf) {
+    std::call_once(pf.grid_once, [&] {
+        if (pf.grid_shape.grid_k <= 0) return;
+        GeneratedKernel gg = generate_filter_kernel(pf.spec, pf.grid_shape);
+        if (gg.shape.grid_k <= 0) return;
+        std::string err;
+        pf.gk_grid = std::move(gg);
+        pf.k_grid = jit_get(pf.gk_grid, err);
+    });
+    return pf.k_grid;
 }
 
 // Per thread and device: the grid-mode scratch (barrier counter, error count, kept count, valid
@@ -419,6 +428,9 @@ struct GridArea {
     uint64_t epoch = 0;
     uint64_t err_seen = 0;
     bool dirty = true;
+    // page-locked, mapped: the kernel's last block writes the header here, then the tag (word 0)
+    unsigned long long* hmap = nullptr;
+    unsigned long long* dmap = nullptr;
 };
 thread_local std::unordered_map<int, GridArea> t_grid;
 constexpr size_t kGridAreaWords = 3 + 64 + 8192;
@@ -429,11 +441,13 @@ std::atomic<int64_t> g_grid_launches{0};
 struct GridCall {
     bool used = false;
     uint64_t err_base = 0;
+    const unsigned long long* hmap = nullptr;  // the header, complete once hmap[0] == tag
+    uint64_t tag = 0;
 };
 
 // The grid-mode launch of a prepared filter over n rows, if its blocks fit on the device at once.
 int grid_blocks(const PreparedFilter& pf, int64_t n) {
-    if (!pf.k_grid || n <= 0) return 0;
+    if (pf.grid_shape.grid_k <= 0 || n <= 0 || !grid_kernel(pf)) return 0;
     const Shape& gs = pf.gk_grid.shape;
     const int64_t per_block = filter_tile_rows(gs) * (gs.threads / 32) * gs.grid_k;
     const int64_t need = (n + per_block - 1) / per_block;
@@ -483,6 +497,13 @@ int enqueue_prepared(const PreparedFilter& pf, gdf_column* const* frame, gdf_col
             area->words = kGridAreaWords;
             area->dirty = true;
         }
+        if (!area->hmap) {
+            if (int e = check_cuda(cudaHostAlloc((void**)&area->hmap, 128 * 8, cudaHostAllocMapped), "cudaHostAlloc"))
+                return e;
+            if (int e = check_cuda(cudaHostGetDevicePointer((void**)&area->dmap, area->hmap, 0),
+                                   "cudaHostGetDevicePointer"))
+                return e;
+        }
         if (area->dirty) {
             if (int e = check_cuda(cudaMemsetAsync(area->p, 0, area->words * 8, st), "cudaMemsetAsync")) return e;
             area->epoch = 0;
@@ -492,6 +513,9 @@ int enqueue_prepared(const PreparedFilter& pf, gdf_column* const* frame, gdf_col
         scratch = area->p;
         grid_call->used = true;
         grid_call->err_base = area->err_seen;
+        grid_call->hmap = area->hmap;
+        grid_call->tag = area->epoch + 2ull * (uint64_t)gblocks;
+        __atomic_store_n(&area->hmap[0], 0ull, __ATOMIC_RELEASE);  // no earlier call's tag can match
     } else {
         if (grid_call) grid_call->used = false;
         cudaMemsetAsync(scratch, 0, (size_t)prepared_scratch_words(pf, n) * 8, st);
@@ -513,7 +537,10 @@ int enqueue_prepared(const PreparedFilter& pf, gdf_column* const* frame, gdf_col
     }
     slots[L.scratch] = (uint64_t)(uintptr_t)scratch;
     if (L.obase >= 0) slots[L.obase] = (uint64_t)obase;
-    if (gblocks) slots[L.epoch] = area->epoch;
+    if (gblocks) {
+        slots[L.epoch] = area->epoch;
+        slots[L.hostmap] = (uint64_t)(uintptr_t)area->dmap;
+    }
     if (pf.have_pred) fill_scalars(pf.pred, L, slots);
     if (pf.have_proj) {
         ParamLayout QL;
@@ -531,7 +558,7 @@ int enqueue_prepared(const PreparedFilter& pf, gdf_column* const* frame, gdf_col
             area->dirty = true;
             return e;
         }
-        area->epoch += (uint64_t)gblocks;
+        area->epoch += 2ull * (uint64_t)gblocks;  // the barrier step and the completion step
         g_grid_launches++;
     } else {
         const int grid = launch_blocks(*pf.k, gk.shape.threads, tile_rows * (gk.shape.threads / 32), n);
@@ -541,6 +568,7 @@ int enqueue_prepared(const PreparedFilter& pf, gdf_column* const* frame, gdf_col
     }
     if (ev) cudaEventRecord(ev[1], st);
     note_launch();
+    if (gblocks) return kSuccess;  // the header arrives through the mapped buffer
     return check_cuda(cudaMemcpyAsync(host_header, scratch, (size_t)header * 8, cudaMemcpyDeviceToHost, st),
                       "cudaMemcpyAsync");
 }
@@ -578,7 +606,29 @@ int run_prepared(const PreparedFilter& pf, gdf_column* const* frame, gdf_column*
     GridCall gc;
     if (int e = enqueue_prepared(pf, frame, outs, scratch, 0, hp, st, timing ? ev : nullptr, &gc)) return e;
     const auto t_wait0 = std::chrono::steady_clock::now();
+    if (gc.used) {
+        // the completion tag in the mapped header: polled, with the stream's own status checked
+        // every few polls, so an error ends the wait and a finished stream ends it too
+        for (unsigned spins = 1;; ++spins) {
+            if (__atomic_load_n(&gc.hmap[0], __ATOMIC_ACQUIRE) == gc.tag) break;
+            if ((spins & 255u) == 0u) {
+                const cudaError_t q = cudaStreamQuery(st);
+                if (q == cudaSuccess) break;
+                if (q != cudaErrorNotReady) return check_cuda(q, "filter kernel");
+            }
+        }
+    }
     if (int e = check_cuda(cudaStreamSynchronize(st), "filter kernel")) return e;
+    if (gc.used) {
+        if (__atomic_load_n(&gc.hmap[0], __ATOMIC_ACQUIRE) != gc.tag) {
+            int dev = 0;
+            cudaGetDevice(&dev);
+            t_grid[dev].dirty = true;
+            return set_error(kCudaError, "filter kernel finished without its completion tag");
+        }
+        for (int64_t i = 1; i < header; i++) hp[i] = gc.hmap[i];
+        hp[0] = 0;
+    }
     if (timing) {
         const auto t_end = std::chrono::steady_clock::now();
         float dev_ms = 0.f;

@@ -104,8 +104,9 @@ cudaError_t gather_by_index(const void* in, const uint32_t* in_valid, int64_t n_
 //   span, and its validity mask (n/8 bytes) stays in L2 instead of competing with every other
 //   column's mask; measured on six columns of 200M rows by a permutation, row-major took 48.7 ms
 //   against 33.4 ms for six one-column passes.  The index is re-read per column (4 B per row).
-// Element loads are marked evict-first (`ld.global.cs`): a scattered element is read once, and the
-// masks are what L2 should keep.
+// In the column-major order element loads are marked evict-first (`ld.global.cs`): a scattered
+// element is read once, and the masks are what L2 should keep (clustered rows share lines, so the
+// row-major order loads them normally).
 constexpr int kGatherRowsPerLane = 4;
 constexpr int kGatherSamples = 64;          // index samples of 32 consecutive rows
 constexpr long long kGatherClusterSpan = 1 << 16;  // a sample spanning fewer input rows is clustered
@@ -126,7 +127,7 @@ __device__ __forceinline__ ral_i64 ral_index_at(const GatherColumnsParams& P, ra
 
 // One column's step: the four element loads and the four validity-word loads are all issued before
 // any is used (their values feed only the stores and ballots after them).
-template <typename E>
+template <typename E, bool kScattered>
 __device__ __forceinline__ unsigned ral_gather_k(const GatherColumn& c, const ral_i64 (&j)[kGatherRowsPerLane],
                                                  const bool (&ok)[kGatherRowsPerLane], ral_i64 base, int lane,
                                                  ral_i64 n_out) {
@@ -137,7 +138,7 @@ __device__ __forceinline__ unsigned ral_gather_k(const GatherColumn& c, const ra
     ral_u32 w[kGatherRowsPerLane];
 #pragma unroll
     for (int k = 0; k < kGatherRowsPerLane; ++k) {
-        v[k] = ok[k] ? __ldcs(in + j[k]) : E(0);
+        v[k] = ok[k] ? (kScattered ? __ldcs(in + j[k]) : __ldg(in + j[k])) : E(0);
         w[k] = ok[k] ? (iv ? __ldg(iv + (j[k] >> 5)) : 0xffffffffu) : 0u;
     }
 #pragma unroll
@@ -158,14 +159,15 @@ __device__ __forceinline__ unsigned ral_gather_k(const GatherColumn& c, const ra
     return cnt;
 }
 
+template <bool kScattered>
 __device__ __forceinline__ unsigned ral_gather_column_step(const GatherColumn& col, const ral_i64 (&j)[kGatherRowsPerLane],
                                                            const bool (&ok)[kGatherRowsPerLane], ral_i64 base,
                                                            int lane, ral_i64 n_out) {
     switch (col.width) {
-    case 1: return ral_gather_k<int8_t>(col, j, ok, base, lane, n_out);
-    case 2: return ral_gather_k<short>(col, j, ok, base, lane, n_out);
-    case 4: return ral_gather_k<int>(col, j, ok, base, lane, n_out);
-    default: return ral_gather_k<long long>(col, j, ok, base, lane, n_out);
+    case 1: return ral_gather_k<int8_t, kScattered>(col, j, ok, base, lane, n_out);
+    case 2: return ral_gather_k<short, kScattered>(col, j, ok, base, lane, n_out);
+    case 4: return ral_gather_k<int, kScattered>(col, j, ok, base, lane, n_out);
+    default: return ral_gather_k<long long, kScattered>(col, j, ok, base, lane, n_out);
     }
 }
 
@@ -227,7 +229,7 @@ __global__ void __launch_bounds__(256, 5) gather_columns_kernel(const __grid_con
             bool ok[kGatherRowsPerLane];
             ral_step_indices(P, base, lane, j, ok);
             for (int c = 0; c < P.num_columns; ++c) {
-                const unsigned cnt = ral_gather_column_step(P.col[c], j, ok, base, lane, P.n_out);
+                const unsigned cnt = ral_gather_column_step<false>(P.col[c], j, ok, base, lane, P.n_out);
                 if (lane == 0 && cnt) atomicAdd(&s_cnt[c], (unsigned long long)cnt);
             }
         }
@@ -239,7 +241,7 @@ __global__ void __launch_bounds__(256, 5) gather_columns_kernel(const __grid_con
                 ral_i64 j[kGatherRowsPerLane];
                 bool ok[kGatherRowsPerLane];
                 ral_step_indices(P, base, lane, j, ok);
-                cc += ral_gather_column_step(P.col[c], j, ok, base, lane, P.n_out);
+                cc += ral_gather_column_step<true>(P.col[c], j, ok, base, lane, P.n_out);
             }
             if (lane == 0 && cc) atomicAdd(&s_cnt[c], cc);
         }

@@ -151,22 +151,13 @@ int Server::add_query(int table_id, const char* filter_q, const char* project_q,
     q->item.max_registers = server_max_registers();
     // at least one chunk, so that an empty table's request still runs (and finishes) once
     q->chunks = std::max<int64_t>(1, (t.rows + filter_tile_rows(sh) - 1) / filter_tile_rows(sh));
-    if (solo_rows_ > 0 && t.rows >= solo_rows_ && max_waves_ > 1) {
-        // stand-in outputs: only dtypes and mask presence matter to the plan
-        const int NO = (int)q->plan->out_dtypes.size();
-        std::vector<gdf_column> stand(NO);
-        std::vector<gdf_column*> souts(NO);
-        for (int o = 0; o < NO; o++) {
-            stand[o] = gdf_column{};
-            stand[o].dtype = q->plan->out_dtypes[o];
-            stand[o].valid = q->plan->out_valid[o] ? (gdf_valid_type*)(uintptr_t)256 : nullptr;
-            stand[o].size = (gdf_size_type)t.rows;
-            souts[o] = &stand[o];
-        }
-        if (int e = prepare_standalone_filter(frame.data(), (int)frame.size(), filter_q, project_q, souts.data(), NO,
-                                              &q->solo))
-            return e;
-        q->scratch_words = standalone_scratch_words(q->solo, t.rows);
+    if (solo_rows_ > 0 && max_waves_ > 1) {
+        // the standalone kernel is compiled when the server starts (all queries at once, on
+        // threads); its scratch is bounded here by one status word per 32 rows (its smallest chunk)
+        q->large = t.rows >= solo_rows_;
+        q->filter_text = filter_q;
+        q->project_text = project_q;
+        q->scratch_words = filter_scratch_header((int)q->plan->out_dtypes.size()) + (t.rows + 31) / 32 + 1;
     }
     q->reserve = request_layout(*q, t.rows).total;
     if (q->plan->out_dtypes.size() > 64) return set_error(kUnsupported, "more than 64 projected columns");
@@ -209,9 +200,65 @@ void Server::collect_items(std::vector<GeneratedKernel>& tus, std::vector<Dispat
 
 // Compiles the item functions of all queries and links the dispatcher; (re)allocates the
 // wave buffers.  Called with mu_ held and no wave in flight.
+// The standalone kernels of the queries that have none yet, compiled on host threads.
+int Server::prepare_solo_kernels() {
+    std::vector<ServerQuery*> todo;
+    for (auto& q : queries_)
+        if (!q->solo && !q->filter_text.empty()) todo.push_back(q.get());
+    if (todo.empty()) return kSuccess;
+    std::atomic<size_t> next{0};
+    std::atomic<int> failed{0};
+    std::mutex err_mu;
+    std::string first_err;
+    auto work = [&] {
+        cudaSetDevice(device_);
+        for (size_t i; (i = next++) < todo.size();) {
+            ServerQuery& q = *todo[i];
+            ServerTable& t = tables_[q.table];
+            std::vector<gdf_column*> frame;
+            for (auto& c : t.cols) frame.push_back(&c);
+            // stand-in outputs: only dtypes and mask presence matter to the plan
+            const int NO = (int)q.plan->out_dtypes.size();
+            std::vector<gdf_column> stand(NO);
+            std::vector<gdf_column*> souts(NO);
+            for (int o = 0; o < NO; o++) {
+                stand[o] = gdf_column{};
+                stand[o].dtype = q.plan->out_dtypes[o];
+                stand[o].valid = q.plan->out_valid[o] ? (gdf_valid_type*)(uintptr_t)256 : nullptr;
+                stand[o].size = (gdf_size_type)t.rows;
+                souts[o] = &stand[o];
+            }
+            const void* h = nullptr;
+            if (prepare_standalone_filter(frame.data(), (int)frame.size(), q.filter_text.c_str(), q.project_text.c_str(),
+                                          souts.data(), NO, &h) ||
+                standalone_scratch_words(h, t.rows) > q.scratch_words) {
+                std::lock_guard<std::mutex> lock(err_mu);
+                if (!failed++) first_err = last_error();
+                continue;
+            }
+            q.solo = h;
+        }
+    };
+    // a string literal missing from a category dictionary rewrites its column while planning:
+    // with category columns the kernels are prepared one at a time
+    bool categories = false;
+    for (const auto& t : tables_)
+        for (const auto& c : t.cols) categories |= c.dtype == GDF_STRING_CATEGORY;
+    const int nt = categories ? 1
+                              : (int)std::min<size_t>(todo.size(),
+                                                      std::max(1u, std::min(16u, std::thread::hardware_concurrency())));
+    std::vector<std::thread> pool;
+    for (int k = 1; k < nt; k++) pool.emplace_back(work);
+    work();
+    for (auto& th : pool) th.join();
+    if (failed) return set_error(kJitError, "standalone filter kernel of a served query: " + first_err);
+    return kSuccess;
+}
+
 int Server::ensure_linked() {
     if (linked_queries_ == (int)queries_.size() && kernel_) return kSuccess;
     if (queries_.empty()) return set_error(kInvalidArgument, "no queries");
+    if (int e = prepare_solo_kernels()) return e;
     std::vector<GeneratedKernel> tus;
     std::vector<DispatchEntry> entries;
     int stride = 1, smem = 0;
@@ -556,15 +603,24 @@ void Server::loop() {
                 pending_.pop_front();
             }
             stats_.peak_reserved = std::max(stats_.peak_reserved, reserved_);
-            // a large request not yet started runs alone on the standalone kernel, on at most all
-            // but one of the waves (one stays for the batched small requests)
-            if (!rc && solo_inflight_ < max_waves_ - 1) {
-                int64_t solo_id = -1;
+            // A request not yet started runs alone on the standalone kernel when its table is large
+            // (on at most all but one of the waves: one stays for the batched small requests), or
+            // when nothing else waits to be launched (a batch of one gains nothing from the
+            // dispatcher).
+            if (!rc) {
+                int64_t solo_id = -1, waiting = 0;
                 for (int64_t id : active_) {
                     const ServerRequest& r = *requests_[id];
-                    if (!r.in_wave && r.next_chunk == 0 && queries_[r.query]->solo) {
+                    if (r.in_wave) continue;
+                    waiting++;
+                    const ServerQuery& q = *queries_[r.query];
+                    if (solo_id < 0 && r.next_chunk == 0 && q.solo && q.large && solo_inflight_ < max_waves_ - 1)
                         solo_id = id;
-                        break;
+                }
+                if (solo_id < 0 && waiting == 1 && pending_.empty()) {
+                    for (int64_t id : active_) {
+                        const ServerRequest& r = *requests_[id];
+                        if (!r.in_wave && r.next_chunk == 0 && queries_[r.query]->solo) solo_id = id;
                     }
                 }
                 if (solo_id >= 0) {
@@ -588,7 +644,7 @@ void Server::loop() {
                 const ServerRequest& r = *requests_[id];
                 if (r.in_wave) continue;
                 const ServerQuery& q = *queries_[r.query];
-                if (q.solo && r.next_chunk == 0) continue;  // waits for a solo wave
+                if (q.solo && q.large && r.next_chunk == 0) continue;  // waits for a solo wave
                 const double left = (double)(q.chunks - r.next_chunk) * (double)filter_tile_rows(q.item.shape);
                 cand.push_back({left - (tnow - r.t_submit) * kAgeRowsPerSecond, id});
             }

@@ -47,9 +47,12 @@ struct ServerQuery {
     int fn = -1;               // index in the dispatcher's function list
     size_t reserve = 0;        // output + scratch bytes of one request (every row kept)
     int64_t chunks = 0;        // work items of one request
-    // a table of at least the solo threshold: its requests run the standalone fused filter kernel
-    // alone on a wave's stream (the kernel ral_filter_project launches)
+    // the standalone fused filter kernel over the query's table (the kernel ral_filter_project
+    // launches), for requests that run alone on a wave: every request over a table of at least
+    // the solo threshold (`large`), and any request that finds nothing else waiting
     const void* solo = nullptr;
+    bool large = false;
+    std::string filter_text, project_text;  // the query's texts, for the standalone kernel
     int64_t scratch_words = 0; // scratch of one request: the larger of the chunked and solo needs
 };
 
@@ -126,6 +129,7 @@ private:
     int launch_wave(Wave& w, const std::vector<int64_t>& reqs, const std::vector<int64_t>& take);
     int launch_solo(Wave& w, int64_t request_id);
     int start_request(ServerRequest& r, cudaStream_t st);
+    int prepare_solo_kernels();
     void wave_ended(Wave& w);
     void finish_wave(Wave& w);
     void loop();

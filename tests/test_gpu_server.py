@@ -185,8 +185,8 @@ def test_empty_and_one_row_tables():
 
 def test_large_requests_run_solo_with_the_same_bits(served, monkeypatch):
     """Requests over tables of at least RAL_SERVER_SOLO_ROWS rows run alone on the standalone fused
-    kernel, the others batched beside them: every result equals the batched-only server's, and
-    the solo count is the number of large requests."""
+    kernel, the others batched beside them (or alone when nothing else waits): every result equals
+    the batched-only server's, and every large request ran solo."""
     tabs, qs, host, dev = served
     monkeypatch.setenv("RAL_SERVER_SOLO_ROWS", "0")
     srv0, qids0 = _server(tabs, qs, dev, waves=3)
@@ -204,7 +204,22 @@ def test_large_requests_run_solo_with_the_same_bits(served, monkeypatch):
         for j, (g, a) in enumerate(zip(got, alone[i])):
             _same_bits(g, a, f"query {i} output {j} solo={big[i]}")
     st = srv.stats()
-    assert st["solo"] == sum(big[i] for _, i in rids)
+    assert st["solo"] >= sum(big[i] for _, i in rids)
+    srv.close()
+
+
+def test_a_request_alone_runs_solo(served):
+    """With nothing else waiting a request of any size runs on the standalone kernel, with the
+    same bits as ral_filter_project."""
+    tabs, qs, host, dev = served
+    srv, qids = _server(tabs, qs, dev, waves=2)
+    small = min(range(len(qs)), key=lambda i: tabs[qs[i].table].rows)
+    s0 = srv.stats()["solo"]
+    got = _alone(srv, qids[small])
+    assert srv.stats()["solo"] == s0 + 1
+    plain = R.filter_project(dev[qs[small].table], qs[small].filter, qs[small].project)
+    for k, (g, p) in enumerate(zip(got, plain)):
+        _same_bits(g, p, f"output {k}")
     srv.close()
 
 
