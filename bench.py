@@ -60,6 +60,69 @@ def load_traffic(key):
     return None
 
 
+# GB300's FP64 pipe: two thread instructions per clock per SM (from the counters: C2's 100M FP64
+# instructions ran at 63% pipe activity in 261 us at 2070 MHz = 1.93 per clock per SM)
+FP64_PER_CLOCK_PER_SM = 2.0
+SMS = 152
+
+
+def batch_mix_meta(n_programs, seed):
+    """Per program of the batched mix, without a GPU: rows and algorithmic bytes per row."""
+    import ralgpu as R
+    from ralgpu import dtypes as D
+    from ralgpu import workloads as W
+    out = []
+    for t in W.batched_mix(n_programs, seed=seed):
+        pp = R.parse_project_plan(t.dtypes, t.project)
+        bpr = 0.0
+        for c in pp["input_columns"]:
+            bpr += D.WIDTH[t.dtypes[c]] + (1 / 8 if t.null_rates[c] > 0 else 0)
+        bpr += sum(D.WIDTH[dt] + 1 / 8 for dt in pp["evaluated_dtypes"])
+        out.append({"rows": int(t.rows), "bytes_per_row": bpr})
+    return out
+
+
+def floor_table_from_ncu(csv_path, n_programs, seed, cap):
+    """profiles/batch_mix_fp64.json from an ncu CSV of the mix's plain calls over tables capped at
+    `cap` rows (one ral_eval launch per program, in program order): FP64 and all thread
+    instructions per row of every program."""
+    import csv
+    rows = [r for r in csv.reader(open(csv_path)) if len(r) > 14 and r[0].isdigit()]
+    by = {}
+    for r in rows:
+        by.setdefault(int(r[0]), {})[r[12]] = float(r[14].replace(",", ""))
+    ids = sorted(by)
+    meta = batch_mix_meta(n_programs, seed)
+    if len(ids) != len(meta):
+        raise SystemExit(f"{len(ids)} launches in {csv_path} for {len(meta)} programs")
+    progs = []
+    for i, m in zip(ids, meta):
+        rc = min(m["rows"], cap)
+        progs.append({"rows": m["rows"], "bytes_per_row": round(m["bytes_per_row"], 4),
+                      "fp64_per_row": by[i]["sm__thread_inst_executed_pipe_fp64_pred_on.sum"] / rc,
+                      "inst_per_row": by[i]["smsp__thread_inst_executed.sum"] / rc})
+    return {"what": "per program of the 256-program batched mix (seed %d), from plain calls over the first %d rows "
+                    "of each table" % (seed, cap),
+            "command": "ncu --metrics sm__thread_inst_executed_pipe_fp64_pred_on.sum,smsp__thread_inst_executed.sum,"
+                       "gpu__time_duration.sum --clock-control none -k regex:ral_eval -s 512 -c 256 --csv --log-file "
+                       "batch_fp64.csv python bench.py --workload batched --max-rows %d --steps 1 --warmup 1 "
+                       "--plain-steps 1 --capped-rows 0 --no-autotune" % cap,
+            "programs": progs}
+
+
+def batch_floor(table, sm_mhz, peak_gbs):
+    """The mix's floor: the FP64-pipe time of its instructions and the HBM time of its bytes, for
+    the whole mix overlapped (a batch) and program by program (plain calls, one after another)."""
+    rate = FP64_PER_CLOCK_PER_SM * SMS * sm_mhz * 1e6
+    fp = [p["rows"] * p["fp64_per_row"] / rate for p in table["programs"]]
+    hb = [p["rows"] * p["bytes_per_row"] / (peak_gbs * 1e9) for p in table["programs"]]
+    return {"fp64_ms": sum(fp) * 1e3, "hbm_ms": sum(hb) * 1e3,
+            "floor_ms": max(sum(fp), sum(hb)) * 1e3,
+            "per_program_floor_ms": sum(max(a, b) for a, b in zip(fp, hb)) * 1e3,
+            "fp64_rate": f"{FP64_PER_CLOCK_PER_SM} per clock per SM x {SMS} SMs x {sm_mhz:.0f} MHz",
+            "source": "profiles/batch_mix_fp64.json"}
+
+
 class ClockSampler:
     """nvidia-smi clocks and throttle reasons, sampled every 20 ms; only samples that arrive
     inside the timed window [mark_start, mark_end] are kept."""
@@ -1081,6 +1144,23 @@ def batched_capped(R, progs, cap, stream, plain_steps):
             "speedup_vs_plain": pms / bms}
 
 
+def batched_floor_block(args, clocks, ms_per_step, plain):
+    """The floor of the default mix from the committed per-program counters, at the clock measured
+    during the timed region; None for another mix."""
+    p = os.path.join(ROOT, "profiles", "batch_mix_fp64.json")
+    if not os.path.exists(p) or args.max_rows or args.programs != 256 or args.seed != 20261203:
+        return None
+    table = json.load(open(p))
+    mhz = (clocks or {}).get("sm_mhz") or 2070.0
+    peak, _ = load_peaks()
+    f = batch_floor(table, float(mhz), peak)
+    f["batched_frac_of_floor"] = f["floor_ms"] / ms_per_step
+    if plain:
+        f["plain_frac_of_floor"] = f["per_program_floor_ms"] / plain["ms_per_step"]
+        f["max_speedup_over_plain"] = plain["ms_per_step"] / f["floor_ms"]
+    return f
+
+
 def run_batched(args):
     import concurrent.futures as cf
     import torch
@@ -1180,6 +1260,7 @@ def run_batched(args):
                     "generate_s": round(gen_s, 2)},
         "plain_per_call": plain,
         "speedup_vs_plain": value / plain["value"] if plain else None,
+        "floor": batched_floor_block(args, clocks, ms_per_step, plain),
         "capped_tables": capped,
         "hbm_gbs": achieved,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
@@ -1411,6 +1492,9 @@ def main():
     ap.add_argument("--plain-steps", type=int, default=3)
     ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--max-rows", type=int, default=0, help="batched: cap every table (profiling captures)")
+    ap.add_argument("--floor-from-ncu", default=None,
+                    help="batched: write profiles/batch_mix_fp64.json from an ncu CSV of the capped plain calls "
+                         "(no GPU needed) and exit")
     ap.add_argument("--capped-rows", type=int, default=1_000_000,
                     help="batched: also compare batch and plain calls over the first N rows of every table")
     ap.add_argument("--selectivity", type=float, default=0.5)
@@ -1425,6 +1509,12 @@ def main():
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":
         args.warmup = 3
+    if args.floor_from_ncu:
+        table = floor_table_from_ncu(args.floor_from_ncu, args.programs, args.seed, args.max_rows or 200_000)
+        with open(os.path.join(ROOT, "profiles", "batch_mix_fp64.json"), "w") as f:
+            json.dump(table, f, indent=0)
+        print(json.dumps(batch_floor(table, 2070.0, load_peaks()[0])))
+        return
     if args.impl == "reference":
         run_reference(args)
     elif args.workload == "batched":

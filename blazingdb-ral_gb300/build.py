@@ -21,9 +21,10 @@ CUDA = os.environ.get("CUDA_HOME", "/usr/local/cuda")
 NVCC = os.path.join(CUDA, "bin", "nvcc")
 
 CPP = ["program.cpp", "frontend.cpp", "codegen.cpp", "jit.cpp", "engine.cpp", "filter.cpp", "batch.cpp", "server.cpp",
-       "selftest.cpp", "aggregate.cpp", "category.cpp", "capi.cpp"]
+       "selftest.cpp", "aggregate.cpp", "category.cpp", "textscan.cpp", "capi.cpp"]
 CU = ["kernels.cu", "noalloc.cu"]
-HEADERS = ["program.h", "frontend.h", "codegen.h", "jit.h", "engine.h", "filter.h", "batch.h", "server.h", "kernels.h", "device_rt.cuh", "softfp.cuh"]
+HEADERS = ["program.h", "frontend.h", "codegen.h", "jit.h", "engine.h", "filter.h", "batch.h", "server.h", "kernels.h", "device_rt.cuh", "softfp.cuh",
+           "textscan.cuh", "textscan.h"]
 INCLUDES = [f"-I{os.path.join(ROOT, 'include')}", f"-I{CSRC}", f"-I{os.path.join(CUDA, 'include')}"]
 GENCODE = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
@@ -42,9 +43,13 @@ def _embed_prelude() -> str:
     # softfp.cuh first: device_rt.cuh then skips its #include of it (NVRTC has no include path)
     src = open(os.path.join(CSRC, "softfp.cuh")).read() + "\n" + open(os.path.join(CSRC, "device_rt.cuh")).read()
     out = os.path.join(OUT, "prelude_embed.cpp")
-    text = ('// generated from csrc/softfp.cuh and csrc/device_rt.cuh by build.py\n'
+    scan = open(os.path.join(CSRC, "textscan.cuh")).read()
+    text = ('// generated from csrc/softfp.cuh, csrc/device_rt.cuh and csrc/textscan.cuh by build.py\n'
             'extern "C" const char* const ral_prelude_source;\n'
-            'extern "C" const char* const ral_prelude_source = R"RALPRELUDE(' + src + ')RALPRELUDE";\n')
+            'extern "C" const char* const ral_prelude_source = R"RALPRELUDE(' + src + ')RALPRELUDE";\n'
+            '// the field parsers of the text scan kernels (prepended to their generated source)\n'
+            'extern "C" const char* const ral_textscan_source;\n'
+            'extern "C" const char* const ral_textscan_source = R"RALPRELUDE(' + scan + ')RALPRELUDE";\n')
     if not os.path.exists(out) or open(out).read() != text:
         with open(out, "w") as f:
             f.write(text)

@@ -14,6 +14,7 @@
 #include "kernels.h"
 #include "server.h"
 #include "ral/ral_c.h"
+#include "textscan.h"
 #include "ral/ral_debug.h"
 
 using namespace ral;
@@ -321,6 +322,20 @@ int ral_materialize_column(const gdf_column* input, gdf_column* output, const gd
     });
 }
 
+int ral_text_scan_rows(const char* data, int64_t n_bytes, char line_terminator, int32_t skip_rows, int64_t* rows) {
+    return guarded([&] { return text_scan_rows(data, n_bytes, line_terminator, skip_rows, rows); });
+}
+
+int ral_text_scan_filter(const char* data, int64_t n_bytes, char delimiter, char line_terminator, int32_t skip_rows,
+                         const int32_t* file_dtypes, int32_t n_file_columns, const int32_t* projections,
+                         int32_t n_projections, const char* filter_query_part, gdf_column* const* out_columns,
+                         gdf_size_type* num_rows_out) {
+    return guarded([&] {
+        return text_scan_filter(data, n_bytes, delimiter, line_terminator, skip_rows, file_dtypes, n_file_columns,
+                                projections, n_projections, filter_query_part, out_columns, num_rows_out);
+    });
+}
+
 int ral_materialize_columns(const gdf_column* const* inputs, gdf_column* const* outputs, int32_t num_columns,
                             const gdf_column* row_indices) {
     return guarded([&] {
@@ -415,6 +430,19 @@ int ral_filter_project_host(gdf_column* const* frame_columns, int32_t num_column
 
 int ral_debug_call_timing(int32_t enable, int32_t reset, int64_t* calls, double* us4) {
     return call_timing_query(enable != 0, reset != 0, calls, us4);
+}
+
+int ral_debug_text_scan_source(const int32_t* file_dtypes, int32_t n_file_columns, const int32_t* projections,
+                               int32_t n_projections, const char* filter_query_part, int32_t compile, char* source_out,
+                               int64_t source_capacity, char* log_out, int64_t log_capacity) {
+    return guarded([&] {
+        std::string src, log;
+        const int rc = text_scan_source(file_dtypes, n_file_columns, projections, n_projections, filter_query_part,
+                                        compile != 0, src, log);
+        copy_out(src, source_out, source_capacity);
+        copy_out(log, log_out, log_capacity);
+        return rc;
+    });
 }
 
 int ral_debug_filter_grid_launches(int64_t* launches) {

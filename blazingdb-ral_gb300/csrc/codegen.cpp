@@ -1822,6 +1822,261 @@ GeneratedKernel generate_filter_kernel(const FilterSpec& f, const Shape& s, bool
     return gk;
 }
 
+// ---- delimited-text scan fused with its filter ---------------------------------------------
+// One warp per chunk of 32 J lines (ticket order).  Pass 1: lane t of slice j takes line
+// base + 32 j + t, finds its fields, parses the predicate's and evaluates the predicate (a blank
+// or skipped line keeps nothing); the slice's keep bits are one ballot word.  The warp looks back
+// for the chunk's output offset, turns the words into the kept-line list and, 32 kept lines per
+// step, parses every projected field of line list[k] in lane k and stores it at offset + k; each
+// output's validity bits of the step are one ballot, OR-ed in at the step's bit offset.
+extern "C" const char* const ral_textscan_source;
+
+GeneratedKernel generate_text_scan_kernel(const TextScanSpec& t, const Shape& s) {
+    if (s.J < 1 || s.J > 32) throw std::runtime_error("text scan kernel shape: J out of range");
+    GeneratedKernel gk;
+    gk.shape = s;
+    ParamLayout& L = gk.layout;
+    const int NP = (int)t.dtypes.size();
+    int slot = kTextScanFixedSlots;
+    L.n_rows = 0;
+    L.out_data = slot; slot += NP;
+    L.out_valid = slot; slot += NP;
+    L.scratch = slot++;
+    const Program* pred = t.predicate;
+    if (pred) {
+        L.lscalar_slot.assign(pred->ops.size(), -1);
+        L.rscalar_slot.assign(pred->ops.size(), -1);
+        for (size_t k = 0; k < pred->ops.size(); k++) {
+            if (pred->ops[k].left == SCALAR_INDEX) L.lscalar_slot[k] = slot++;
+            if (!pred->ops[k].unary && pred->ops[k].right == SCALAR_INDEX) L.rscalar_slot[k] = slot++;
+        }
+    }
+    L.total = slot;
+
+    // the file fields each pass needs: pass 1 the predicate's, pass 2 every projection's
+    std::vector<bool> pred_ref = pred ? pred->inputs_referenced() : std::vector<bool>();
+    std::vector<bool> pred_raw = pred ? pred->inputs_raw_valid() : std::vector<bool>();
+    std::vector<int> f1, f2;  // sorted distinct file columns
+    if (pred)
+        for (size_t c = 0; c < t.predicate_cols.size(); c++)
+            if (pred_ref[c] || pred_raw[c]) f1.push_back(t.file_cols[t.predicate_cols[c]]);
+    for (int q = 0; q < NP; q++) f2.push_back(t.file_cols[q]);
+    auto uniq = [](std::vector<int>& v) {
+        std::sort(v.begin(), v.end());
+        v.erase(std::unique(v.begin(), v.end()), v.end());
+    };
+    uniq(f1);
+    uniq(f2);
+    auto slot_of = [](const std::vector<int>& v, int fc) {
+        return (int)(std::lower_bound(v.begin(), v.end(), fc) - v.begin());
+    };
+
+    std::ostringstream key;
+    key << "textscan|";
+    for (int q = 0; q < NP; q++) key << (int)t.dtypes[q] << "@" << t.file_cols[q] << ",";
+    if (pred) {
+        key << "|P" << pred->structure_key() << "@";
+        for (int c : t.predicate_cols) key << c << ",";
+    }
+    key << "|J" << s.J << "T" << s.threads << "B" << s.min_blocks;
+    char hex[32];
+    snprintf(hex, sizeof hex, "%016llx", (unsigned long long)fnv1a(key.str()));
+    gk.name = std::string("ral_textscan_") + hex;
+    gk.soft_fp = true;
+
+    std::ostringstream os;
+    os << ral_textscan_source << "\n";
+    os << "// generated: " << key.str() << "\n";
+    os << "#define RAL_J " << s.J << "\n#define RAL_THREADS " << s.threads << "\n";
+    os << "#define RAL_WARPS (RAL_THREADS / 32)\n";
+    os << "struct RalParams { ral_u64 s[" << L.total << "]; };\n\n";
+    std::vector<Kind> pred_kind;
+    if (pred) {
+        emit_row_function(os, *pred, L, "ral_pred_row");
+        pred_kind = final_kinds(*pred, L);
+        os << "RAL_FI ral_u32 ral_pred_vrow(const ral_u32* fv) {\n";
+        ValidEmitter ve(*pred);
+        ve.emit(os, "    ", [&](int c) { return "fv[" + std::to_string(c) + "]"; });
+        os << "    return " << ve.name[pred->final_pos[0]] << ";\n}\n";
+    }
+    os << "RAL_FI void ral_text_line(const char* d, const ral_i64* ends, ral_i64 nterm, ral_i64 nb, ral_i64 i,\n"
+          "                          ral_i64& s, ral_i64& e) {\n"
+          "    s = i == 0 ? 0 : ends[i - 1] + 1;\n"
+          "    e = i < nterm ? ends[i] : nb;\n"
+          "    if (e > s && d[e - 1] == '\\r') --e;\n"
+          "}\n";
+    // field finders: the bounds of each needed field of a line (-1 where the line is shorter)
+    auto finder = [&](const char* name, const std::vector<int>& fields) {
+        os << "RAL_FI void " << name << "(const char* d, ral_i64 s, ral_i64 e, char delim, ral_i64* fs, ral_i64* fe) {\n";
+        os << "#pragma unroll\n    for (int k = 0; k < " << fields.size() << "; ++k) { fs[k] = -1; fe[k] = -1; }\n";
+        os << "    int f = 0;\n    ral_i64 p0 = s;\n";
+        os << "    for (ral_i64 p = s;; ++p) {\n";
+        os << "        const bool end = p >= e;\n";
+        os << "        if (end || d[p] == delim) {\n";
+        os << "            switch (f) {\n";
+        for (size_t k = 0; k < fields.size(); k++)
+            os << "            case " << fields[k] << ": fs[" << k << "] = p0; fe[" << k << "] = p; break;\n";
+        os << "            default: break;\n            }\n";
+        os << "            if (end || f >= " << fields.back() << ") break;\n";
+        os << "            ++f;\n            p0 = p + 1;\n";
+        os << "        }\n    }\n}\n";
+    };
+    if (!f1.empty()) finder("ral_fields_pred", f1);
+    finder("ral_fields_all", f2);
+    // parse of one field into a register value (column value widened) and a validity word
+    // (a refusal is counted where `counts` holds: idle lanes of pass 2 parse a kept line twice)
+    auto parse = [&](const std::string& ind, gdf_dtype dt, const std::string& k, const std::string& v,
+                     const std::string& vw, const std::string& counts) {
+        const bool isf = dt == GDF_FLOAT32 || dt == GDF_FLOAT64;
+        os << ind << (isf ? "double " : "ral_i64 ") << v << " = 0;\n";
+        os << ind << "ral_u32 " << vw << " = 0u;\n";
+        os << ind << "if (fs[" << k << "] >= 0) {\n";
+        if (isf) os << ind << "    double t = 0.0;\n" << ind << "    const int st = ral_tx_parse_double(d, fs[" << k << "], fe[" << k << "], &t);\n";
+        else if (dt == GDF_DATE32 || dt == GDF_DATE64)
+            os << ind << "    long long t = 0;\n" << ind << "    const int st = ral_tx_parse_date(d, fs[" << k << "], fe[" << k
+               << "], " << (dt == GDF_DATE64 ? "true" : "false") << ", &t);\n";
+        else os << ind << "    long long t = 0;\n" << ind << "    const int st = ral_tx_parse_int(d, fs[" << k << "], fe[" << k << "], &t);\n";
+        os << ind << "    if (st == RAL_TX_REFUSED && " << counts << ") ++refused;\n";
+        os << ind << "    if (st == RAL_TX_OK) {\n";
+        os << ind << "        " << vw << " = 0xffffffffu;\n";
+        switch (dt) {
+        case GDF_INT8: os << ind << "        " << v << " = (ral_i64)(signed char)t;\n"; break;
+        case GDF_INT16: os << ind << "        " << v << " = (ral_i64)(short)t;\n"; break;
+        case GDF_INT32: case GDF_DATE32: os << ind << "        " << v << " = (ral_i64)(int)t;\n"; break;
+        case GDF_FLOAT32: os << ind << "        " << v << " = (double)(float)t;\n"; break;
+        default: os << ind << "        " << v << " = t;\n"; break;
+        }
+        os << ind << "    }\n" << ind << "}\n";
+    };
+
+    os << "\nextern \"C\" __global__ void __launch_bounds__(RAL_THREADS, " << std::max(1, s.min_blocks) << ") " << gk.name
+       << "(const __grid_constant__ RalParams P) {\n";
+    os << "    __shared__ ral_u32 s_kp[RAL_WARPS][32];\n";
+    os << "    __shared__ unsigned short s_ls[RAL_WARPS][32 * RAL_J];\n";
+    os << "    const ral_i64 T = (ral_i64)P.s[0];\n";
+    os << "    const char* const d = (const char*)P.s[1];\n";
+    os << "    const ral_i64 nb = (ral_i64)P.s[2];\n";
+    os << "    const ral_i64* const ends = (const ral_i64*)P.s[3];\n";
+    os << "    const ral_i64 nterm = (ral_i64)P.s[4];\n";
+    os << "    const ral_i64 skip = (ral_i64)P.s[5];\n";
+    os << "    const char delim = (char)P.s[6];\n";
+    os << "    const ral_u64 cap = (ral_u64)P.s[7];\n";
+    os << "    ral_u64* const scratch = (ral_u64*)P.s[" << L.scratch << "];\n";
+    os << "    ral_u64* const status = scratch + " << text_scan_header(NP) << ";\n";
+    for (int q = 0; q < NP; q++) {
+        os << "    " << element_ctype(t.dtypes[q]) << "* __restrict__ o" << q << " = (" << element_ctype(t.dtypes[q])
+           << "*)P.s[" << L.out_data + q << "];\n";
+        os << "    ral_u32* __restrict__ ov" << q << " = (ral_u32*)P.s[" << L.out_valid + q << "];\n";
+    }
+    os << "    const int lane = threadIdx.x & 31;\n    const int warp = threadIdx.x >> 5;\n";
+    os << "    ral_u32* const s_kpw = s_kp[warp];\n    unsigned short* const s_lst = s_ls[warp];\n";
+    os << "    const ral_i64 CL = 32 * RAL_J;\n    const ral_i64 nchunks = (T + CL - 1) / CL;\n";
+    os << "    ral_u32 vcnt[" << NP << "];\n    for (int q = 0; q < " << NP << "; ++q) vcnt[q] = 0u;\n";
+    os << "    ral_u32 refused = 0, over = 0;\n";
+    os << "    for (;;) {\n";
+    os << "        ral_u32 ticket = 0;\n";
+    os << "        if (lane == 0) ticket = atomicAdd((unsigned int*)scratch, 1u);\n";
+    os << "        const ral_i64 chunk = __shfl_sync(0xffffffffu, ticket, 0);\n";
+    os << "        if (chunk >= nchunks) break;\n";
+    os << "        const ral_i64 base = chunk * CL;\n";
+    os << "        ral_u32 total = 0;\n";
+    os << "        for (int j = 0; j < RAL_J; ++j) {\n";
+    os << "            const ral_i64 i = base + (ral_i64)j * 32 + lane;\n";
+    os << "            bool keep = false;\n";
+    os << "            if (i < T && i >= skip) {\n";
+    os << "                ral_i64 s, e;\n";
+    os << "                ral_text_line(d, ends, nterm, nb, i, s, e);\n";
+    os << "                keep = e > s;\n";
+    if (pred) {
+        os << "                if (keep) {\n";
+        if (!f1.empty()) {
+            os << "                    ral_i64 fs[" << f1.size() << "], fe[" << f1.size() << "];\n";
+            os << "                    ral_fields_pred(d, s, e, delim, fs, fe);\n";
+        }
+        os << "                    ral_u32 fv[" << std::max<size_t>(1, t.predicate_cols.size()) << "];\n";
+        for (size_t c = 0; c < t.predicate_cols.size(); c++) {
+            const int q = t.predicate_cols[c];
+            if (!(pred_ref[c] || pred_raw[c])) {
+                os << "                    fv[" << c << "] = 0xffffffffu;\n";
+                continue;
+            }
+            parse("                    ", t.dtypes[q], std::to_string(slot_of(f1, t.file_cols[q])), "x" + std::to_string(c),
+                  "w" + std::to_string(c), "true");
+            os << "                    fv[" << c << "] = w" << c << ";\n";
+        }
+        os << "                    " << kind_ctype(pred_kind[0]) << " y0;\n";
+        os << "                    ral_pred_row(P";
+        for (size_t c = 0; c < t.predicate_cols.size(); c++)
+            if (pred_ref[c]) os << ", x" << c;
+        for (size_t c = 0; c < t.predicate_cols.size(); c++)
+            if (pred_raw[c]) os << ", w" << c << " & 1u";
+        os << ", y0);\n";
+        os << "                    keep = (ral_pred_vrow(fv) & 1u) != 0u && " << narrow("y0", pred_kind[0], GDF_INT8)
+           << " != 0;\n";
+        os << "                }\n";
+    }
+    os << "            }\n";
+    os << "            const ral_u32 w = __ballot_sync(0xffffffffu, keep);\n";
+    os << "            if (lane == j) s_kpw[j] = w;\n";
+    os << "            total += __popc(w);\n";
+    os << "        }\n";
+    os << "        __syncwarp();\n";
+    os << "        const ral_u64 excl = ral_lookback(status, chunk, total, scratch + 1);\n";
+    os << "        if (chunk == nchunks - 1 && lane == 0) scratch[2] = excl + total;\n";
+    os << "        if (total == 0u) continue;\n";
+    os << "        {\n";
+    os << "            const ral_u32 kw = lane < RAL_J ? s_kpw[lane] : 0u;\n";
+    os << "            const ral_u32 c = __popc(kw);\n";
+    os << "            ral_u32 inc = c;\n";
+    os << "            for (int off = 1; off < 32; off <<= 1) {\n";
+    os << "                const ral_u32 u = __shfl_up_sync(0xffffffffu, inc, off);\n";
+    os << "                if (lane >= off) inc += u;\n            }\n";
+    os << "            ral_u32 q = inc - c;\n";
+    os << "            for (ral_u32 m = kw; m; m &= m - 1u) s_lst[q++] = (unsigned short)(lane * 32 + __ffs(m) - 1);\n";
+    os << "        }\n";
+    os << "        __syncwarp();\n";
+    os << "        for (ral_u32 k0 = 0; k0 < total; k0 += 32) {\n";
+    os << "            const ral_u32 kA = k0 + lane;\n";
+    os << "            const bool act = kA < total;\n";
+    os << "            const ral_i64 i = base + s_lst[act ? kA : k0];\n";
+    os << "            ral_i64 s, e;\n";
+    os << "            ral_text_line(d, ends, nterm, nb, i, s, e);\n";
+    os << "            ral_i64 fs[" << f2.size() << "], fe[" << f2.size() << "];\n";
+    os << "            ral_fields_all(d, s, e, delim, fs, fe);\n";
+    os << "            const ral_u64 pos = excl + kA;\n";
+    os << "            const bool put = act && pos < cap;\n";
+    os << "            if (act && !put) ++over;\n";
+    os << "            const ral_u64 b = excl + k0;\n";
+    for (int q = 0; q < NP; q++) {
+        os << "            {\n";
+        parse("                ", t.dtypes[q], std::to_string(slot_of(f2, t.file_cols[q])), "v", "vw", "act");
+        os << "                if (put) o" << q << "[pos] = (" << element_ctype(t.dtypes[q]) << ")v;\n";
+        os << "                const ral_u32 bal = __ballot_sync(0xffffffffu, put && vw != 0u);\n";
+        os << "                if (lane == 0 && bal) {\n";
+        os << "                    vcnt[" << q << "] += __popc(bal);\n";
+        os << "                    const ral_u64 X = (ral_u64)bal << (b & 31u);\n";
+        os << "                    atomicOr(ov" << q << " + (b >> 5), (ral_u32)X);\n";
+        os << "                    if ((ral_u32)(X >> 32)) atomicOr(ov" << q << " + (b >> 5) + 1, (ral_u32)(X >> 32));\n";
+        os << "                }\n";
+        os << "            }\n";
+    }
+    os << "        }\n";
+    os << "        __syncwarp();\n";
+    os << "    }\n";
+    // counts: one atomic per warp and counter
+    os << "    for (int q = 0; q < " << NP << "; ++q) {\n";
+    os << "        const ral_u32 v = __reduce_add_sync(0xffffffffu, vcnt[q]);\n";
+    os << "        if (lane == 0 && v) atomicAdd((unsigned long long*)(scratch + 3 + q), (unsigned long long)v);\n";
+    os << "    }\n";
+    os << "    const ral_u32 rf = __reduce_add_sync(0xffffffffu, refused);\n";
+    os << "    const ral_u32 ov = __reduce_add_sync(0xffffffffu, over);\n";
+    os << "    if (lane == 0 && rf) atomicAdd((unsigned long long*)(scratch + " << 3 + NP << "), (unsigned long long)rf);\n";
+    os << "    if (lane == 0 && ov) atomicAdd((unsigned long long*)(scratch + " << 4 + NP << "), (unsigned long long)ov);\n";
+    os << "}\n";
+    gk.source = os.str();
+    return gk;
+}
+
 GeneratedKernel generate_batch_item(const Program& p, const Shape& sh) {
     GeneratedKernel gk;
     gk.shape = sh;

@@ -205,4 +205,24 @@ GeneratedKernel generate_filter_kernel(const FilterSpec& f, const Shape& s, bool
 // C type name of a column element.
 const char* element_ctype(gdf_dtype t);
 
+// ---- delimited-text scan fused with its filter ---------------------------------------------
+// The scanned frame is the projected file columns (BindableTableScan projects=[...]); the
+// predicate (optional) reads scanned-frame columns predicate_cols.  Every output carries a mask.
+struct TextScanSpec {
+    std::vector<gdf_dtype> dtypes;       // per projected column
+    std::vector<int> file_cols;          // file column of each projected column
+    const Program* predicate = nullptr;  // the LogicalFilter's program, or none (the scan alone)
+    std::vector<int> predicate_cols;     // scanned-frame column of each predicate input
+};
+// Scratch of a text scan launch: ticket, look-back error, kept rows, one valid count per output,
+// refused fields, rows past the outputs' capacity; then one status word per chunk.
+inline int64_t text_scan_header(int n_outputs) { return 5 + n_outputs; }
+// Parameter slots before the outputs: lines, text, bytes, terminator positions, terminators,
+// rows skipped, delimiter, output capacity.
+constexpr int kTextScanFixedSlots = 8;
+// Lines per look-back chunk of a text scan kernel: J mask words of 32 lines.
+inline int64_t text_scan_chunk_lines(const Shape& s) { return (int64_t)32 * s.J; }
+
+GeneratedKernel generate_text_scan_kernel(const TextScanSpec& t, const Shape& s);
+
 }  // namespace ral

@@ -100,12 +100,13 @@ std::string disk_key(const GeneratedKernel& gk) {
     return buf;
 }
 
-// Register cap of relocatable item functions (RAL_BATCH_MAXRREG).  Default 96: on the
-// 256-program mix 96 ran 129 ms (64: 131 ms) and, over tables capped at 1M rows, 19.8 ms (64: 24.0).
+// Register cap of relocatable item functions (RAL_BATCH_MAXRREG).  Default 80 (three blocks of
+// 256 threads per SM): on the 256-program mix 80 / 96 / 64 ran 116.2 / 118.2 / 116.9 ms and, over
+// tables capped at 1M rows, 80 / 96 ran 14.12 / 14.30 ms.
 int relocatable_max_registers() {
     const char* e = std::getenv("RAL_BATCH_MAXRREG");
-    const int v = e && *e ? std::atoi(e) : 96;
-    return v >= 32 && v <= 255 ? v : 96;
+    const int v = e && *e ? std::atoi(e) : 80;
+    return v >= 32 && v <= 255 ? v : 80;
 }
 
 bool compile(const GeneratedKernel& gk, std::vector<char>& cubin, std::string& log, std::string& err,

@@ -373,6 +373,150 @@ __global__ void category_remap_kernel(int32_t* __restrict__ codes, ral_i64 n, co
 }
 }  // namespace
 
+// ---- line index of a delimited text buffer ---------------------------------------------------
+// Tile t of 4096 bytes: thread k of its block reads bytes [16 k, 16 k + 16) of the tile (one
+// 16-byte load where the buffer allows it), so a block's terminators come out in order from a
+// block-wide scan of the threads' counts.
+
+__device__ __forceinline__ ral_u32 ral_text_term_bits(const char* data, int64_t n, int64_t at, char term) {
+    ral_u32 bits = 0;
+    if (at + 16 <= n && ((uintptr_t)(data + at) & 15) == 0) {
+        const uint4 v = __ldcs(reinterpret_cast<const uint4*>(data + at));
+        const ral_u32 w[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+        for (int k = 0; k < 16; ++k)
+            bits |= ((ral_u32)(((w[k >> 2] >> (8 * (k & 3))) & 0xffu) == (ral_u32)(unsigned char)term)) << k;
+    } else {
+        for (int k = 0; k < 16; ++k)
+            if (at + k < n && data[at + k] == term) bits |= 1u << k;
+    }
+    return bits;
+}
+
+__global__ void __launch_bounds__(256) text_term_count_kernel(const char* __restrict__ data, int64_t n, char term,
+                                                              ral_u32* __restrict__ counts) {
+    const int64_t tile = blockIdx.x;
+    const ral_u32 c = __popc(ral_text_term_bits(data, n, tile * kTextTileBytes + 16 * (int64_t)threadIdx.x, term));
+    __shared__ ral_u32 s_w[8];
+    const ral_u32 wsum = __reduce_add_sync(0xffffffffu, c);
+    if ((threadIdx.x & 31) == 0) s_w[threadIdx.x >> 5] = wsum;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        ral_u32 t = 0;
+        for (int w = 0; w < 8; ++w) t += s_w[w];
+        counts[tile] = t;
+    }
+}
+
+__global__ void __launch_bounds__(1024) exclusive_scan_u32_kernel(const ral_u32* __restrict__ counts, int64_t m,
+                                                                  unsigned long long* __restrict__ offsets) {
+    __shared__ unsigned long long s_w[32];
+    __shared__ unsigned long long s_carry;
+    if (threadIdx.x == 0) s_carry = 0;
+    __syncthreads();
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int64_t base = 0; base < m; base += 1024) {
+        const int64_t i = base + threadIdx.x;
+        const unsigned long long v = i < m ? counts[i] : 0ull;
+        unsigned long long inc = v;
+        for (int off = 1; off < 32; off <<= 1) {
+            const unsigned long long t = __shfl_up_sync(0xffffffffu, inc, off);
+            if (lane >= off) inc += t;
+        }
+        if (lane == 31) s_w[warp] = inc;
+        __syncthreads();
+        if (warp == 0) {
+            unsigned long long w = s_w[lane];
+            for (int off = 1; off < 32; off <<= 1) {
+                const unsigned long long t = __shfl_up_sync(0xffffffffu, w, off);
+                if (lane >= off) w += t;
+            }
+            s_w[lane] = w;  // inclusive over warps
+        }
+        __syncthreads();
+        const unsigned long long carry = s_carry;
+        const unsigned long long before = (warp ? s_w[warp - 1] : 0ull) + inc - v;
+        if (i < m) offsets[i] = carry + before;
+        __syncthreads();
+        if (threadIdx.x == 0) s_carry = carry + s_w[31];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) offsets[m] = s_carry;
+}
+
+__global__ void __launch_bounds__(256) text_term_positions_kernel(const char* __restrict__ data, int64_t n, char term,
+                                                                  const unsigned long long* __restrict__ offsets,
+                                                                  long long* __restrict__ ends) {
+    const int64_t tile = blockIdx.x;
+    const int64_t at = tile * kTextTileBytes + 16 * (int64_t)threadIdx.x;
+    ral_u32 bits = ral_text_term_bits(data, n, at, term);
+    const ral_u32 c = __popc(bits);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    ral_u32 inc = c;
+    for (int off = 1; off < 32; off <<= 1) {
+        const ral_u32 t = __shfl_up_sync(0xffffffffu, inc, off);
+        if (lane >= off) inc += t;
+    }
+    __shared__ ral_u32 s_w[8];
+    if (lane == 31) s_w[warp] = inc;
+    __syncthreads();
+    ral_u32 before = inc - c;
+    for (int w = 0; w < warp; ++w) before += s_w[w];
+    unsigned long long k = offsets[tile] + before;
+    for (; bits; bits &= bits - 1u) ends[k++] = at + __ffs(bits) - 1;
+}
+
+__global__ void __launch_bounds__(256) text_present_count_kernel(const char* __restrict__ data, int64_t n,
+                                                                 const long long* __restrict__ ends, int64_t nterm,
+                                                                 int64_t lines, int64_t skip,
+                                                                 unsigned long long* count) {
+    ral_u32 c = 0;
+    for (int64_t i = skip + (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < lines;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        const long long s = i == 0 ? 0 : ends[i - 1] + 1;
+        long long e = i < nterm ? ends[i] : n;
+        if (e > s && data[e - 1] == '\r') --e;
+        c += e > s ? 1u : 0u;
+    }
+    c = __reduce_add_sync(0xffffffffu, c);
+    if ((threadIdx.x & 31) == 0 && c) atomicAdd(count, (unsigned long long)c);
+}
+
+cudaError_t launch_text_present_count(const char* data, int64_t n, const long long* ends, int64_t nterm, int64_t lines,
+                                      int64_t skip, unsigned long long* count, cudaStream_t st) {
+    if (lines <= skip) return cudaSuccess;
+    const int64_t blocks = std::max<int64_t>(1, std::min<int64_t>((lines - skip + 255) / 256, 152 * 8));
+    text_present_count_kernel<<<(int)blocks, 256, 0, st>>>(data, n, ends, nterm, lines, skip, count);
+    note_launch();
+    return cudaGetLastError();
+}
+
+cudaError_t launch_text_term_counts(const char* data, int64_t n, char term, uint32_t* counts, cudaStream_t st) {
+    const int64_t tiles = text_tiles(n);
+    if (tiles <= 0) return cudaSuccess;
+    if (tiles > 0x7fffffffll) return cudaErrorInvalidValue;
+    text_term_count_kernel<<<(unsigned)tiles, 256, 0, st>>>(data, n, term, counts);
+    note_launch();
+    return cudaGetLastError();
+}
+
+cudaError_t launch_exclusive_scan_u32(const uint32_t* counts, int64_t tiles, unsigned long long* offsets,
+                                      cudaStream_t st) {
+    exclusive_scan_u32_kernel<<<1, 1024, 0, st>>>(counts, tiles, offsets);
+    note_launch();
+    return cudaGetLastError();
+}
+
+cudaError_t launch_text_term_positions(const char* data, int64_t n, char term, const unsigned long long* offsets,
+                                       long long* ends, cudaStream_t st) {
+    const int64_t tiles = text_tiles(n);
+    if (tiles <= 0) return cudaSuccess;
+    if (tiles > 0x7fffffffll) return cudaErrorInvalidValue;
+    text_term_positions_kernel<<<(unsigned)tiles, 256, 0, st>>>(data, n, term, offsets, ends);
+    note_launch();
+    return cudaGetLastError();
+}
+
 cudaError_t launch_category_remap(int32_t* codes, int64_t n, const int32_t* table, int32_t table_n, cudaStream_t st) {
     if (n <= 0) return cudaSuccess;
     const int threads = 256;

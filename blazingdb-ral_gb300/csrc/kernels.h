@@ -47,6 +47,26 @@ struct GatherColumnsParams {
 // set bits counted into valid_counts[c].
 cudaError_t launch_gather_columns(const GatherColumnsParams& p, cudaStream_t st);
 
+// ---- line index of a delimited text buffer (the text scan) ---------------------------------
+
+// Each block handles kTextTileBytes bytes of the buffer: 256 threads x 16 bytes.
+constexpr int64_t kTextTileBytes = 4096;
+inline int64_t text_tiles(int64_t n_bytes) { return (n_bytes + kTextTileBytes - 1) / kTextTileBytes; }
+
+// counts[t] = line terminators in tile t of data[0, n).
+cudaError_t launch_text_term_counts(const char* data, int64_t n, char term, uint32_t* counts, cudaStream_t st);
+// offsets[t] = counts[0] + .. + counts[t-1] for t <= tiles (offsets[tiles] = the total), one block.
+cudaError_t launch_exclusive_scan_u32(const uint32_t* counts, int64_t tiles, unsigned long long* offsets,
+                                      cudaStream_t st);
+// ends[k] = position of the k-th line terminator of data[0, n), in order.
+cudaError_t launch_text_term_positions(const char* data, int64_t n, char term, const unsigned long long* offsets,
+                                       long long* ends, cudaStream_t st);
+
+// *count += lines i in [skip, lines) that are not blank (a '\r' before the terminator dropped);
+// line i spans (ends[i - 1], ends[i]), the last one (i == nterm) ending at n.
+cudaError_t launch_text_present_count(const char* data, int64_t n, const long long* ends, int64_t nterm, int64_t lines,
+                                      int64_t skip, unsigned long long* count, cudaStream_t st);
+
 // codes[i] += 1 where codes[i] >= pos: a string inserted at rank pos of a category dictionary.
 cudaError_t launch_category_insert(int32_t* codes, int64_t n, int32_t pos, cudaStream_t st);
 // codes[i] = table[codes[i]] for codes in [0, table_n): codes moved to a merged dictionary.

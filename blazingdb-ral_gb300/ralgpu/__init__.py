@@ -14,7 +14,8 @@ from .capi import (RalError, lib, perform_operation, perform_operation_async, pe
                    debug_program_source, debug_filter_source, jit_stats, kernel_launches, version,
                    parse_project_plan, Batch, autotune_program, batch_tune_key, Server, softfp_selftest,
                    debug_lookback_timeout, process_aggregate, debug_aggregate_source, call_timing, filter_grid_launches,
-                   Category, category_column, decode_category, filter_project_host)
+                   Category, category_column, decode_category, filter_project_host,
+                   text_scan_rows, text_scan_filter, debug_text_scan_source)
 from .column import Column, Scalar, valid_alloc_size
 from . import dtypes
 
@@ -25,5 +26,5 @@ __all__ = [
     "debug_program_source", "debug_filter_source", "jit_stats", "kernel_launches", "version", "Column", "Scalar",
     "valid_alloc_size", "dtypes", "parse_project_plan", "Batch", "autotune_program", "batch_tune_key", "Server", "softfp_selftest", "debug_lookback_timeout",
     "process_aggregate", "debug_aggregate_source", "call_timing", "filter_grid_launches", "Category", "category_column",
-    "decode_category", "filter_project_host",
+    "decode_category", "filter_project_host", "text_scan_rows", "text_scan_filter", "debug_text_scan_source",
 ]

@@ -55,6 +55,11 @@ _SIGS = {
                                         C.POINTER(C.c_int32)]),
     "ral_debug_call_timing": (C.c_int, [C.c_int32, C.c_int32, C.POINTER(C.c_int64), C.POINTER(C.c_double)]),
     "ral_debug_filter_grid_launches": (C.c_int, [C.POINTER(C.c_int64)]),
+    "ral_text_scan_rows": (C.c_int, [C.c_void_p, C.c_int64, C.c_char, C.c_int32, C.POINTER(C.c_int64)]),
+    "ral_text_scan_filter": (C.c_int, [C.c_void_p, C.c_int64, C.c_char, C.c_char, C.c_int32, I32P, C.c_int32, I32P,
+                                       C.c_int32, C.c_char_p, C.c_void_p, C.POINTER(C.c_int32)]),
+    "ral_debug_text_scan_source": (C.c_int, [I32P, C.c_int32, I32P, C.c_int32, C.c_char_p, C.c_int32, C.c_char_p,
+                                             C.c_int64, C.c_char_p, C.c_int64]),
     "ral_filter_project_host": (C.c_int, [C.c_void_p, C.c_int32, C.c_char_p, C.c_char_p, C.c_void_p, C.c_int32,
                                           C.POINTER(C.c_int32), C.c_int64]),
     "ral_category_create": (C.c_int, [C.c_void_p, C.c_int64, C.POINTER(C.c_void_p), I32P]),
@@ -366,6 +371,56 @@ def materialize_columns(input_columns: List[Column], row_indices: Column,
     for o, st in zip(outs, os_):
         o.sync_from_c(st)
     return outs
+
+
+def _text_device(data):
+    """A uint8 device tensor of the text (bytes are copied to the GPU)."""
+    import torch
+    if isinstance(data, (bytes, bytearray, memoryview)):
+        b = bytes(data)
+        t = torch.frombuffer(bytearray(b), dtype=torch.uint8) if b else torch.zeros(0, dtype=torch.uint8)
+        return t.to("cuda")
+    return data
+
+
+def text_scan_rows(data, line_terminator: bytes = b"\n", skip_rows: int = 0) -> int:
+    """Rows of a delimited text buffer: lines after the first skip_rows that are not blank."""
+    t = _text_device(data)
+    rows = C.c_int64(0)
+    _check(lib().ral_text_scan_rows(C.c_void_p(t.data_ptr() if t.numel() else 0), t.numel(), line_terminator,
+                                    skip_rows, C.byref(rows)))
+    return rows.value
+
+
+def text_scan_filter(data, file_dtypes, projections, filter_query_part: Optional[str] = None, delimiter: bytes = b"|",
+                     line_terminator: bytes = b"\n", skip_rows: int = 0, capacity: Optional[int] = None) -> List[Column]:
+    """BindableTableScan over delimited text (projects = projections) fused with its LogicalFilter
+    (None: the scan alone): the kept rows of the projected columns, every column with a mask."""
+    t = _text_device(data)
+    if capacity is None:
+        capacity = text_scan_rows(t, line_terminator, skip_rows)
+    outs = [Column.empty(file_dtypes[c], capacity, with_valid=True) for c in projections]
+    oa, os_ = _colarray(outs)
+    n = C.c_int32(0)
+    fd, pr = _i32(file_dtypes), _i32(projections)
+    _check(lib().ral_text_scan_filter(C.c_void_p(t.data_ptr() if t.numel() else 0), t.numel(), delimiter,
+                                      line_terminator, skip_rows, _p32(fd), len(fd), _p32(pr), len(pr),
+                                      filter_query_part.encode() if filter_query_part else None,
+                                      C.cast(oa, C.c_void_p), C.byref(n)))
+    for o, st in zip(outs, os_):
+        o.sync_from_c(st)
+    return outs
+
+
+def debug_text_scan_source(file_dtypes, projections, filter_query_part: Optional[str] = None, compile: bool = False):
+    """Generated CUDA source (and NVRTC log when compile=True) of the text scan kernel; needs no GPU."""
+    fd, pr = _i32(file_dtypes), _i32(projections)
+    src = C.create_string_buffer(1 << 20)
+    log = C.create_string_buffer(1 << 16)
+    _check(lib().ral_debug_text_scan_source(_p32(fd), len(fd), _p32(pr), len(pr),
+                                            filter_query_part.encode() if filter_query_part else None,
+                                            1 if compile else 0, src, len(src), log, len(log)))
+    return src.value.decode(), log.value.decode()
 
 
 def apply_boolean_mask(stencil: Column) -> Column:

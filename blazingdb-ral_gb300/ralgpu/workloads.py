@@ -443,3 +443,95 @@ def served_table_device(t: ServedTable, device="cuda"):
         valid, nulls = random_valid_mask(n, SERVED_NULL_RATE, g, device)
         cols.append((dt, v, valid, nulls))
     return cols
+
+
+# ---- delimited text (scan -> filter) ----------------------------------------------------------
+# A lineitem-like '|'-delimited table in fixed-width fields, so that a large one is built with
+# vectorised digit arithmetic: orderkey INT64 (10 digits), partkey INT32 (7), quantity INT32 (2),
+# extendedprice FLOAT64 (8.2), discount FLOAT64 (0.dd), tax FLOAT32 (0.dd), shipdate DATE64
+# (YYYY-MM-DD between 1992 and 1998), commitdate DATE32.
+TEXT_DTYPES = [D.GDF_INT64, D.GDF_INT32, D.GDF_INT32, D.GDF_FLOAT64, D.GDF_FLOAT64, D.GDF_FLOAT32, D.GDF_DATE64,
+               D.GDF_DATE32]
+# TPC-H Q6's conditions over the scan of quantity, extendedprice, discount and shipdate
+TEXT_PROJECTIONS = [2, 3, 4, 6]
+TEXT_FILTER = ("LogicalFilter(condition=[AND(>=($3, 1994-01-01), <($3, 1995-01-01), >=($2, 0.05), <=($2, 0.07), "
+               "<($0, 24))])")
+
+
+def _digits(v: np.ndarray, width: int) -> np.ndarray:
+    """(n, width) ASCII digits of non-negative integers, zero-padded."""
+    out = np.empty((v.shape[0], width), dtype=np.uint8)
+    x = v.astype(np.int64).copy()
+    for k in range(width - 1, -1, -1):
+        out[:, k] = (x % 10).astype(np.uint8) + 48
+        x //= 10
+    return out
+
+
+def _date_chars(days: np.ndarray) -> np.ndarray:
+    """(n, 10) YYYY-MM-DD of days since 1970-01-01."""
+    d = np.datetime64("1970-01-01") + days.astype("timedelta64[D]")
+    y = d.astype("datetime64[Y]").astype(np.int64) + 1970
+    m = (d.astype("datetime64[M]").astype(np.int64) % 12) + 1
+    dd = (d - d.astype("datetime64[M]")).astype(np.int64) + 1
+    dash = np.full((days.shape[0], 1), ord("-"), dtype=np.uint8)
+    return np.concatenate([_digits(y, 4), dash, _digits(m, 2), dash, _digits(dd, 2)], axis=1)
+
+
+TEXT_ROW_BYTES = 66
+
+
+def text_table(n: int, seed: int = SEED, values: bool = False):
+    """n rows of the lineitem-like table, each ended by '\\n' (fixed width: 66 bytes a row); with
+    values=True also the column values the text spells (for a check that needs no parse)."""
+    rng = np.random.default_rng(seed)
+    bar = np.full((n, 1), ord("|"), dtype=np.uint8)
+    point = np.full((n, 1), ord("."), dtype=np.uint8)
+    zero = np.full((n, 1), ord("0"), dtype=np.uint8)
+    price = rng.integers(90000, 10500000, n)              # cents
+    disc = rng.integers(0, 11, n)                         # hundredths
+    tax = rng.integers(0, 9, n)
+    ship = rng.integers(8036, 10591, n)                   # 1992-01-02 .. 1998-12-31
+    okey, pkey, qty = rng.integers(1, 6_000_000_000, n), rng.integers(1, 2_000_000, n), rng.integers(1, 51, n)
+    commit = ship + rng.integers(-60, 60, n)
+    parts = [_digits(okey, 10), bar, _digits(pkey, 7), bar,
+             _digits(qty, 2), bar, _digits(price // 100, 8), point, _digits(price % 100, 2), bar,
+             zero, point, _digits(disc, 2), bar, zero, point, _digits(tax, 2), bar, _date_chars(ship), bar,
+             _date_chars(commit), np.full((n, 1), 10, dtype=np.uint8)]
+    text = np.concatenate(parts, axis=1).tobytes()
+    if not values:
+        return text
+    # the nearest double of d.dd is price / 100 rounded once (the division of two exact values)
+    cols = [okey.astype(np.int64), pkey.astype(np.int32), qty.astype(np.int32), price / 100.0, disc / 100.0,
+            (tax / 100.0).astype(np.float32), ship.astype(np.int64) * 86_400_000, commit.astype(np.int32)]
+    return text, cols
+
+
+def text_table_varied(n: int, seed: int = SEED) -> bytes:
+    """A small table of the same schema that exercises the field rules: signs, spaces, empty and
+    unreadable fields, exponents, short rows, blank lines and '\\r\\n' line ends; a header line."""
+    import random
+    rng = random.Random(seed)
+    out = ["orderkey|partkey|quantity|extendedprice|discount|tax|shipdate|commitdate"]
+    for r in range(n):
+        if rng.random() < 0.03:
+            out.append("")
+            continue
+        def pick(f, bad):
+            x = rng.random()
+            return "" if x < 0.04 else (bad if x < 0.06 else f)
+        y, m, d = rng.randint(1992, 1998), rng.randint(1, 12), rng.randint(1, 28)
+        fields = [pick(str(rng.randint(-(1 << 40), 1 << 40)), "12x"),
+                  pick(f" {rng.randint(-99999, 99999)} ", "+"),
+                  pick(str(rng.randint(1, 50)), "1.5"),
+                  pick(rng.choice([f"{rng.randint(0, 10**7)}.{rng.randint(0, 99):02d}", f"{rng.randint(1, 999)}e{rng.randint(-5, 5)}",
+                                   f"-{rng.random():.6f}", f"{rng.randint(0, 10**12)}"]), "1.2.3"),
+                  pick(f"0.{rng.randint(0, 10):02d}", "x"),
+                  pick(f"{rng.randint(0, 8) / 100:.2f}", "."),
+                  pick(f"{y:04d}-{m:02d}-{d:02d}" + (f" {rng.randint(0, 23):02d}:{rng.randint(0, 59):02d}:00"
+                                                     if rng.random() < 0.2 else ""), "1995-02-30"),
+                  pick(f"{y:04d}-{m:02d}-{d:02d}", "19950101")]
+        if rng.random() < 0.05:
+            fields = fields[:rng.randint(1, 7)]
+        out.append("|".join(fields) + ("\r" if rng.random() < 0.1 else ""))
+    return ("\n".join(out) + ("\n" if rng.random() < 0.5 else "")).encode()

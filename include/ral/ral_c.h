@@ -241,6 +241,32 @@ int ral_process_aggregate(gdf_column *const *frame_columns, int32_t num_columns,
                           gdf_scalar *results, int32_t capacity, int32_t *num_results);
 
 /*
+ * Scan -> filter fusion over delimited text — a BindableTableScan of a CSV table
+ * (src/CalciteInterpreter.cpp:745-767: `projects=[...]` picks the file columns, loaded through
+ * csv_parser::parse, src/io/data_parser/CSVParser.cpp:176-233, with '|' as the default delimiter,
+ * no header, blank lines skipped) followed by its LogicalFilter (src/CalciteInterpreter.cpp:509),
+ * evaluated while the text is parsed: only the fields the condition reads are parsed for every
+ * row, and the projected fields only for the rows kept.
+ *
+ * `data` holds n_bytes of text in device memory.  Lines end at line_terminator (the last may lack
+ * it; a '\r' before it is dropped); the first skip_rows lines are skipped and blank lines are not
+ * rows.  file_dtypes gives the file's n_file_columns column types (INT8/16/32/64, FLOAT32/64,
+ * DATE32, DATE64); projections lists the file column of each scanned column, in the scan's order.
+ * filter_query_part is the LogicalFilter text over the scanned columns ($k = k-th projection), or
+ * NULL for the scan alone.  out_columns: one per projection, of the file column's dtype, with a
+ * validity mask (4-byte aligned) and size = capacity in rows (ral_text_scan_rows gives the number
+ * of rows); on return size = rows kept and null_count set.  Field rules (empty or unreadable
+ * fields are null; decimals rounded to nearest, refused with RAL_ERROR_UNSUPPORTED where the
+ * exact method does not reach; dates YYYY-MM-DD[ HH:MM:SS]) are those of csrc/textscan.cuh.
+ * Synchronous.
+ */
+int ral_text_scan_rows(const char *data, int64_t n_bytes, char line_terminator, int32_t skip_rows, int64_t *rows);
+int ral_text_scan_filter(const char *data, int64_t n_bytes, char delimiter, char line_terminator, int32_t skip_rows,
+                         const int32_t *file_dtypes, int32_t n_file_columns, const int32_t *projections,
+                         int32_t n_projections, const char *filter_query_part, gdf_column *const *out_columns,
+                         gdf_size_type *num_rows_out);
+
+/*
  * String-category dictionaries — the NVCategory a GDF_STRING_CATEGORY column points at through
  * dtype_info.category in the reference, where a string literal compared with such a column is looked
  * up (src/LogicalFilter.cpp:150-194).  A ral_category keeps its distinct strings sorted by byte

@@ -58,6 +58,12 @@ int ral_debug_call_timing(int32_t enable, int32_t reset, int64_t *calls, double 
  * all fit on the device: one cooperative launch, a grid barrier in place of the look-back). */
 int ral_debug_filter_grid_launches(int64_t *launches);
 
+/* Generated source of the text scan kernel for a file schema, projections and filter (NULL: none),
+ * with an NVRTC-only compile when compile != 0 (log_out gets the ptxas log); needs no GPU. */
+int ral_debug_text_scan_source(const int32_t *file_dtypes, int32_t n_file_columns, const int32_t *projections,
+                               int32_t n_projections, const char *filter_query_part, int32_t compile, char *source_out,
+                               int64_t source_capacity, char *log_out, int64_t log_capacity);
+
 /* Compiles every query's chunk function and links the dispatcher without loading it (no GPU
  * needed); the ptxas / link log goes to log_out. */
 int ral_server_debug_compile(ral_server *server, char *log_out, int64_t log_capacity);

@@ -211,3 +211,12 @@ def test_grid_mode_replaces_the_look_back(monkeypatch):
                                         W.FILTER_PROJECT_PROJECT)
     body = src[src.index("extern \"C\" __global__"):]
     assert "ral_grid_barrier" not in body and "ral_lookback" in body
+
+
+@pytest.mark.parametrize("fq", [None, "LogicalFilter(condition=[>($2, 25)])",
+                                "LogicalFilter(condition=[OR(IS NULL($3), <($4, 0.03))])",
+                                "LogicalFilter(condition=[AND(>=($6, 1995-01-01), <($6, 1996-01-01 00:00:00))])"])
+def test_text_scan_kernels_compile(fq):
+    src, log = ralgpu.debug_text_scan_source(W.TEXT_DTYPES, list(range(8)), fq, compile=True)
+    assert "ral_textscan_" in src and "ral_tx_parse_double" in src
+    assert spills(log) == 0, log
