@@ -14,6 +14,8 @@ ral_perform_operation_async on HBM-resident columns.  Other workloads:
                                rows) and 96 prepared filter + project queries of 4-32 ops, at 5
                                rates, ~50k requests: p50 / p99 latency and rows/s of the served
                                (continuously batched) loop against serial plain execution
+  --workload scan_filter       20M-row lineitem-like '|'-delimited text (1.3 GB) scanned and
+                               filtered by TPC-H Q6's conditions in one fused kernel
 
 value     rows/s over the timed steps (inputs resident in HBM; every input > L2, so no flush)
 e2e       same metric through the C ABI with host buffers: pinned H2D of the inputs and D2H of
@@ -285,7 +287,46 @@ def cpu_filter_project(rows: int, threads: int, selectivity: float):
     return time.perf_counter() - t0
 
 
+def _scan_chunk(args):
+    """A process-pool task: the oracle's scan of text rows [r0, r1) of the fixed-width table."""
+    text, proj = args
+    from oracle import textscan as T
+    from ralgpu import workloads as W
+    return [(c.data[:c.size].copy(), c.valid_bools().copy()) for c in T.scan(text, W.TEXT_DTYPES, proj)]
+
+
+_SCAN_POOL = None
+
+
+def cpu_scan_filter(rows, threads):
+    """The oracle's text scan (one process per thread, each a slice of the rows) and its filter;
+    returns seconds.  The pool starts from a clean interpreter (spawn) and is kept between calls."""
+    import multiprocessing as mp
+    import numpy as np
+    import oracle as O
+    from ralgpu import workloads as W
+    global _SCAN_POOL
+    text = W.text_table(rows, seed=W.SEED + 5)
+    w = W.TEXT_ROW_BYTES
+    per = (rows + threads - 1) // threads
+    tasks = [(text[k * per * w:min(rows, (k + 1) * per) * w], W.TEXT_PROJECTIONS) for k in range(threads) if k * per < rows]
+    if threads > 1 and _SCAN_POOL is None:
+        _SCAN_POOL = mp.get_context("spawn").Pool(threads)
+        _SCAN_POOL.map(_scan_chunk, [(b"1|2|3|4|5|6|1995-01-01|1995-01-01\n", W.TEXT_PROJECTIONS)] * threads)
+    t0 = time.perf_counter()
+    parts = _SCAN_POOL.map(_scan_chunk, tasks) if threads > 1 else [_scan_chunk(t) for t in tasks]
+    frame = []
+    for k, c in enumerate(W.TEXT_PROJECTIONS):
+        v = np.concatenate([p[k][0] for p in parts])
+        m = np.concatenate([p[k][1] for p in parts])
+        frame.append(O.make_column(v, W.TEXT_DTYPES[c], m))
+    O.process_filter(frame, W.TEXT_FILTER, nthreads=threads)
+    return time.perf_counter() - t0
+
+
 def cpu_time(workload, rows, threads, selectivity):
+    if workload == "scan_filter":
+        return cpu_scan_filter(rows, threads)
     if workload == "gather":
         return cpu_gather(rows, threads)
     if workload == "fused_project":
@@ -314,7 +355,8 @@ def cpu_baseline(workload, full_rows, selectivity, budget_s=12.0, single_budget_
     """rows/s of the oracle on all cores over a bounded sample sized for about budget_s of work, and
     on one thread over a sample sized for about single_budget_s."""
     threads = os.cpu_count() or 1
-    probe = min(full_rows, 2_000_000)
+    # the text scan's oracle parses in Python: a smaller first probe
+    probe = min(full_rows, 200_000 if workload == "scan_filter" else 2_000_000)
     dt = cpu_time(workload, probe, threads, selectivity)
     rate = probe / max(dt, 1e-9)
     rows = int(min(full_rows, max(probe, rate * budget_s / 3)))
@@ -324,7 +366,7 @@ def cpu_baseline(workload, full_rows, selectivity, budget_s=12.0, single_budget_
            "sample": f"{rows} of {full_rows} rows, median of 3 runs, {threads} threads",
            "cpu_model": cpu_model()}
     if single_budget_s > 0:
-        p1 = min(full_rows, 200_000)
+        p1 = min(full_rows, 20_000 if workload == "scan_filter" else 200_000)
         d1 = cpu_time(workload, p1, 1, selectivity)
         r1 = int(min(full_rows, max(p1, (p1 / max(d1, 1e-9)) * single_budget_s / 3)))
         t1 = statistics.median([cpu_time(workload, r1, 1, selectivity) for _ in range(3)])
@@ -384,7 +426,7 @@ def cpu_served(threads: int, n_queries: int, rows_cap: int, seed: int = 20261203
 # ---- GPU workloads --------------------------------------------------------------------------------
 
 DEFAULT_ROWS = {"fused_project": 200_000_000, "plain_vm": 1_000_000, "filter_gather": 500_000_000,
-                "filter_project": 200_000_000, "gather": 200_000_000}
+                "filter_project": 200_000_000, "gather": 200_000_000, "scan_filter": 20_000_000}
 
 
 def workload_config(workload, n, selectivity, world=1):
@@ -403,6 +445,14 @@ def workload_config(workload, n, selectivity, world=1):
                "columns": "int32, int64, float32, float64, date32, bool8; 5% nulls", "index": "int32",
                "api": "ral_materialize_columns (all columns in one kernel)",
                "l2": "columns (5.8 GB at 200M rows) exceed L2; no flush"}
+    elif workload == "scan_filter":
+        from ralgpu import workloads as W
+        cfg = {"workload": "scan_filter", "rows": n, "text_bytes": n * W.TEXT_ROW_BYTES,
+               "table": "lineitem-like '|'-delimited text: orderkey int64, partkey int32, quantity int32, "
+                        "extendedprice float64, discount float64, tax float32, shipdate date64, commitdate date32",
+               "scan": f"BindableTableScan projects={W.TEXT_PROJECTIONS}", "filter": "TPC-H Q6's conditions",
+               "fused": "parse + filter + compaction in one kernel (after a line index)",
+               "l2": "text (1.3 GB at 20M rows) exceeds L2; no flush"}
     elif workload == "plain_vm":
         cfg = {"workload": "plain_vm", "rows": n, "filter": "((c2>=24 AND c1<0.05) OR c0%7=3) AND c3<1200",
                "project": "c1*(1-c1)+c2", "fused": "filter+project in one kernel",
@@ -414,6 +464,103 @@ def workload_config(workload, n, selectivity, world=1):
                "l2": "inputs exceed L2; no flush"}
     cfg["parallelism"] = f"replicas x{world}"
     return cfg
+
+
+def scan_filter_setup(n, device):
+    """The lineitem-like text table in device memory, its ground-truth column values, and one step:
+    ral_text_scan_filter of TPC-H Q6's conditions over the scan of quantity, extendedprice, discount
+    and shipdate, into outputs sized for every row."""
+    import ctypes
+    import torch
+    import ralgpu as R
+    from ralgpu import dtypes as D
+    from ralgpu import workloads as W
+    L = R.lib()
+    text, values = W.text_table(n, seed=W.SEED, values=True)
+    host = torch.frombuffer(bytearray(text), dtype=torch.uint8).pin_memory()
+    dev = host.to(device)
+    proj = W.TEXT_PROJECTIONS
+    outs = [R.Column.empty(W.TEXT_DTYPES[c], n, with_valid=True, device=device) for c in proj]
+    oa, os_ = _colarray(outs)
+    fd = (ctypes.c_int32 * len(W.TEXT_DTYPES))(*W.TEXT_DTYPES)
+    pr = (ctypes.c_int32 * len(proj))(*proj)
+    nout = ctypes.c_int32(0)
+    fq = W.TEXT_FILTER.encode()
+
+    def scan(ptr):
+        rc = L.ral_text_scan_filter(ctypes.c_void_p(ptr), len(text), b"|", b"\n", 0, fd, len(fd), pr, len(pr), fq,
+                                    ctypes.cast(oa, ctypes.c_void_p), ctypes.byref(nout))
+        if rc:
+            raise RuntimeError(L.ral_last_error().decode())
+
+    def step(stream):
+        scan(dev.data_ptr())
+
+    def alg_bytes():
+        k = nout.value
+        return len(text) + k * sum(D.WIDTH[W.TEXT_DTYPES[c]] + 1 / 8 for c in proj)
+
+    return dict(step=step, scan=scan, alg_bytes_fn=alg_bytes, nout=nout, outs=outs, out_structs=os_, values=values,
+                host_text=host, dev_text=dev, text_bytes=len(text), cols=[R.Column(dev, None, D.GDF_INT8, len(text))])
+
+
+def scan_filter_parity(ctx):
+    """The kept rows against the oracle's filter over the values the text spells (the oracle's own
+    parse of the same fixed-width fields is checked against those values by the tests)."""
+    import numpy as np
+    import oracle as O
+    from ralgpu import workloads as W
+    t0 = time.perf_counter()
+    n = len(ctx["values"][0])
+    frame = [O.make_column(np.asarray(ctx["values"][c]), W.TEXT_DTYPES[c], np.ones(n, dtype=bool))
+             for c in W.TEXT_PROJECTIONS]
+    exp = O.process_filter(frame, W.TEXT_FILTER, nthreads=os.cpu_count() or 1)
+    stats = {"valid": 0, "data": 0, "rows_out": abs(ctx["nout"].value - exp[0].size), "null_count": 0}
+    for g, e in zip(ctx["outs"], exp):
+        O.update_null_count(e)
+        k = min(g.size, e.size)
+        if k:
+            _compare(g, 0, k, e, stats)
+        stats["null_count"] += abs(g.null_count - e.null_count)
+    return {"rows": n, "rows_out": ctx["nout"].value, "mismatches": sum(stats.values()), "detail": stats,
+            "checked": "every kept row, bit for bit: data, validity bits, null counts, kept row count and order",
+            "seconds": round(time.perf_counter() - t0, 2)}
+
+
+def scan_filter_e2e(ctx, steps):
+    """The text from page-locked host memory: each step copies it in, runs the fused scan and copies
+    the kept rows' columns and masks back."""
+    import torch
+    import ralgpu as R
+    host, dev = ctx["host_text"], ctx["dev_text"]
+    outs = ctx["outs"]
+    back = [(torch.empty_like(o.data, device="cpu").pin_memory(), torch.empty_like(o.valid, device="cpu").pin_memory())
+            for o in outs]
+    stream = torch.cuda.current_stream()
+
+    def one():
+        dev.copy_(host, non_blocking=True)
+        ctx["scan"](dev.data_ptr())
+        k = ctx["nout"].value
+        for (bd, bv), o in zip(back, outs):
+            bd[:k].copy_(o.data[:k], non_blocking=True)
+            bv[:(k + 7) // 8].copy_(o.valid[:(k + 7) // 8], non_blocking=True)
+        stream.synchronize()
+        return k
+
+    one()
+    times = []
+    k = 0
+    for _ in range(max(steps, 5)):
+        t0 = time.perf_counter()
+        k = one()
+        times.append((time.perf_counter() - t0) * 1e3)
+    ms = statistics.median(times)
+    d2h = sum(k * o.data.element_size() + (k + 7) // 8 for o in outs)
+    n = len(ctx["values"][0])
+    return {"value": n / (ms / 1e3), "unit": "rows/s", "h2d_bytes_per_step": int(ctx["text_bytes"]),
+            "d2h_bytes_per_step": int(d2h), "ms_per_step": ms, "timing": f"median of {len(times)} steps after one",
+            "api": "ral_text_scan_filter on the text copied in from page-locked memory, kept columns copied back"}
 
 
 def fused_project_setup(n, device):
@@ -877,6 +1024,8 @@ def measure_workload(args, workload, n, selectivity, device, world, sampler, e2e
     rank = int(os.environ.get("RANK", "0"))
     if workload == "fused_project":
         ctx = fused_project_setup(n, device)
+    elif workload == "scan_filter":
+        ctx = scan_filter_setup(n, device)
     elif workload == "gather":
         ctx = gather_setup(n, selectivity, device)
     else:
@@ -986,15 +1135,21 @@ def measure_workload(args, workload, n, selectivity, device, world, sampler, e2e
             out["roofline"]["sector_model_gbs"] = touched / (kernel_ms / 1e3) / 1e9
     if rank == 0:
         if e2e and not args.skip_e2e and workload != "gather":
-            out["e2e"] = (fused_project_e2e(ctx, max(2, min(args.steps, 3)), device) if workload == "fused_project"
-                          else filter_e2e(ctx, max(2, min(args.steps, 3))))
+            if workload == "fused_project":
+                out["e2e"] = fused_project_e2e(ctx, max(2, min(args.steps, 3)), device)
+            elif workload == "scan_filter":
+                out["e2e"] = scan_filter_e2e(ctx, max(2, min(args.steps, 3)))
+            else:
+                out["e2e"] = filter_e2e(ctx, max(2, min(args.steps, 3)))
             link = host_link_peak()
             moved = out["e2e"]["h2d_bytes_per_step"] + out["e2e"]["d2h_bytes_per_step"]
             out["e2e"]["host_link"] = dict(link, e2e_gbs=moved / (out["e2e"]["ms_per_step"] / 1e3) / 1e9)
             out["e2e"]["host_link"]["frac_of_link"] = out["e2e"]["host_link"]["e2e_gbs"] / link["both_gbs"]
         # the device outputs (the e2e leg rewrote them with the same bits) against the oracle
         if parity and not args.skip_parity:
-            out["parity"] = gather_parity(ctx) if workload == "gather" else parity_check(workload, ctx, selectivity)
+            out["parity"] = (gather_parity(ctx) if workload == "gather" else
+                             scan_filter_parity(ctx) if workload == "scan_filter" else
+                             parity_check(workload, ctx, selectivity))
         if cpu and not args.skip_cpu:
             out["cpu_baseline"] = cpu_baseline(workload, n, selectivity, budget_s=cpu_budget_s,
                                                single_budget_s=cpu_budget_s / 3)
@@ -1005,7 +1160,7 @@ def measure_workload(args, workload, n, selectivity, device, world, sampler, e2e
 
 # Workloads measured beside the default one in the same run: the 200M-row fused filter + project at
 # s = 0.5 (the target kernel) and the 500M-row filter + gather of six columns at s = 0.5.
-EXTRA_WORKLOADS = [("filter_project", 0.5), ("filter_gather", 0.5), ("gather", "permutation")]
+EXTRA_WORKLOADS = [("filter_project", 0.5), ("filter_gather", 0.5), ("gather", "permutation"), ("scan_filter", None)]
 
 
 def run_ours(args):
@@ -1030,7 +1185,8 @@ def run_ours(args):
         "vs_baseline": None,
         "dtype": {"fused_project": "f64+int64", "filter_project": "f64+int64", "plain_vm": "f64+int64",
                   "filter_gather": "int32/int64/f32/f64/date32/bool8 gather",
-                  "gather": "int32/int64/f32/f64/date32/bool8 gather"}[args.workload],
+                  "gather": "int32/int64/f32/f64/date32/bool8 gather",
+                  "scan_filter": "u8 text -> int32/f64/date64"}[args.workload],
         "data": "synthetic (seeded, generated on the GPU)",
         "config": main["config"],
         "hbm_gbs": main["roofline"]["achieved"],
@@ -1450,7 +1606,7 @@ def run_reference(args):
     threads = os.cpu_count() or 1
     # bounded sample per step, sized from a probe so the whole run stays within a few minutes
     sel = args.pattern if args.workload == "gather" else args.selectivity
-    probe = min(n, 1_000_000)
+    probe = min(n, 100_000 if args.workload == "scan_filter" else 1_000_000)
     dt = cpu_time(args.workload, probe, threads, sel)
     rows = int(min(n, max(probe, (probe / max(dt, 1e-9)) * 4.0)))
     for _ in range(args.warmup):
@@ -1463,7 +1619,8 @@ def run_reference(args):
            "vs_baseline": None,
            "dtype": {"fused_project": "f64+int64", "filter_project": "f64+int64", "plain_vm": "f64+int64",
                      "filter_gather": "int32/int64/f32/f64/date32/bool8 gather",
-                  "gather": "int32/int64/f32/f64/date32/bool8 gather"}[args.workload],
+                  "gather": "int32/int64/f32/f64/date32/bool8 gather",
+                  "scan_filter": "u8 text -> int32/f64/date64"}[args.workload],
            "data": "synthetic (seeded)", "impl": "reference",
            "config": workload_config(args.workload, n, sel, world),
            "cpu_baseline": {"value": v, "unit": "rows/s", "cores": threads, "kind": "port",
