@@ -1905,6 +1905,30 @@ GeneratedKernel generate_text_scan_kernel(const TextScanSpec& t, const Shape& s)
           "    e = i < nterm ? ends[i] : nb;\n"
           "    if (e > s && d[e - 1] == '\\r') --e;\n"
           "}\n";
+    // The text [S, E) of up to 32 lines copied into the warp's stage by all lanes (16-byte loads
+    // where the text allows, never past its end), so that the lanes' byte-by-byte parsing reads
+    // shared memory instead of 32 lines' worth of global addresses per instruction.  Returns the
+    // pointer through which text position p reads its staged copy, or the text itself when the
+    // span does not fit.
+    os << "#define RAL_STAGE 4096\n";
+    os << "RAL_FI const char* ral_text_stage(const char* d, ral_i64 nb, ral_i64 S, ral_i64 E, char* stage, int lane) {\n"
+          "    const ral_i64 a = S & ~15ll;\n"
+          "    if (E <= S || E - a > RAL_STAGE) return d;\n"
+          "    __syncwarp();\n"
+          "    if ((((unsigned long long)d) & 15ull) == 0ull) {\n"
+          "        for (ral_i64 o = a + 16 * lane; o < E; o += 512) {\n"
+          "            if (o + 16 <= nb) {\n"
+          "                *reinterpret_cast<uint4*>(stage + (o - a)) = __ldcs(reinterpret_cast<const uint4*>(d + o));\n"
+          "            } else {\n"
+          "                for (ral_i64 k = o; k < nb; ++k) stage[k - a] = d[k];\n"
+          "            }\n"
+          "        }\n"
+          "    } else {\n"
+          "        for (ral_i64 o = a + lane; o < E; o += 32) stage[o - a] = d[o];\n"
+          "    }\n"
+          "    __syncwarp();\n"
+          "    return stage - a;\n"
+          "}\n";
     // field finders: the bounds of each needed field of a line (-1 where the line is shorter)
     auto finder = [&](const char* name, const std::vector<int>& fields) {
         os << "RAL_FI void " << name << "(const char* d, ral_i64 s, ral_i64 e, char delim, ral_i64* fs, ral_i64* fe) {\n";
@@ -1931,11 +1955,11 @@ GeneratedKernel generate_text_scan_kernel(const TextScanSpec& t, const Shape& s)
         os << ind << (isf ? "double " : "ral_i64 ") << v << " = 0;\n";
         os << ind << "ral_u32 " << vw << " = 0u;\n";
         os << ind << "if (fs[" << k << "] >= 0) {\n";
-        if (isf) os << ind << "    double t = 0.0;\n" << ind << "    const int st = ral_tx_parse_double(d, fs[" << k << "], fe[" << k << "], &t);\n";
+        if (isf) os << ind << "    double t = 0.0;\n" << ind << "    const int st = ral_tx_parse_double(ds, fs[" << k << "], fe[" << k << "], &t);\n";
         else if (dt == GDF_DATE32 || dt == GDF_DATE64)
-            os << ind << "    long long t = 0;\n" << ind << "    const int st = ral_tx_parse_date(d, fs[" << k << "], fe[" << k
+            os << ind << "    long long t = 0;\n" << ind << "    const int st = ral_tx_parse_date(ds, fs[" << k << "], fe[" << k
                << "], " << (dt == GDF_DATE64 ? "true" : "false") << ", &t);\n";
-        else os << ind << "    long long t = 0;\n" << ind << "    const int st = ral_tx_parse_int(d, fs[" << k << "], fe[" << k << "], &t);\n";
+        else os << ind << "    long long t = 0;\n" << ind << "    const int st = ral_tx_parse_int(ds, fs[" << k << "], fe[" << k << "], &t);\n";
         os << ind << "    if (st == RAL_TX_REFUSED && " << counts << ") ++refused;\n";
         os << ind << "    if (st == RAL_TX_OK) {\n";
         os << ind << "        " << vw << " = 0xffffffffu;\n";
@@ -1953,6 +1977,7 @@ GeneratedKernel generate_text_scan_kernel(const TextScanSpec& t, const Shape& s)
        << "(const __grid_constant__ RalParams P) {\n";
     os << "    __shared__ ral_u32 s_kp[RAL_WARPS][32];\n";
     os << "    __shared__ unsigned short s_ls[RAL_WARPS][32 * RAL_J];\n";
+    os << "    __shared__ __align__(16) char s_tx[RAL_WARPS][RAL_STAGE];\n";
     os << "    const ral_i64 T = (ral_i64)P.s[0];\n";
     os << "    const char* const d = (const char*)P.s[1];\n";
     os << "    const ral_i64 nb = (ral_i64)P.s[2];\n";
@@ -1970,6 +1995,7 @@ GeneratedKernel generate_text_scan_kernel(const TextScanSpec& t, const Shape& s)
     }
     os << "    const int lane = threadIdx.x & 31;\n    const int warp = threadIdx.x >> 5;\n";
     os << "    ral_u32* const s_kpw = s_kp[warp];\n    unsigned short* const s_lst = s_ls[warp];\n";
+    os << "    char* const s_txw = s_tx[warp];\n";
     os << "    const ral_i64 CL = 32 * RAL_J;\n    const ral_i64 nchunks = (T + CL - 1) / CL;\n";
     os << "    ral_u32 vcnt[" << NP << "];\n    for (int q = 0; q < " << NP << "; ++q) vcnt[q] = 0u;\n";
     os << "    ral_u32 refused = 0, over = 0;\n";
@@ -1981,17 +2007,32 @@ GeneratedKernel generate_text_scan_kernel(const TextScanSpec& t, const Shape& s)
     os << "        const ral_i64 base = chunk * CL;\n";
     os << "        ral_u32 total = 0;\n";
     os << "        for (int j = 0; j < RAL_J; ++j) {\n";
-    os << "            const ral_i64 i = base + (ral_i64)j * 32 + lane;\n";
+    os << "            const ral_i64 i0 = base + (ral_i64)j * 32;\n";
+    os << "            if (i0 >= T) {\n";
+    os << "                if (lane == j) s_kpw[j] = 0u;\n";
+    os << "                continue;\n";
+    os << "            }\n";
+    os << "            const ral_i64 i = i0 + lane;\n";
+    os << "            const char* ds = d;\n";
+    if (pred) {
+        // the slice's lines staged only when the condition has fields to parse
+        os << "            {\n";
+        os << "                const ral_i64 i1 = i0 + 31 < T ? i0 + 31 : T - 1;\n";
+        os << "                const ral_i64 S = i0 == 0 ? 0 : ends[i0 - 1] + 1;\n";
+        os << "                const ral_i64 E = i1 < nterm ? ends[i1] : nb;\n";
+        os << "                ds = ral_text_stage(d, nb, S, E, s_txw, lane);\n";
+        os << "            }\n";
+    }
     os << "            bool keep = false;\n";
     os << "            if (i < T && i >= skip) {\n";
     os << "                ral_i64 s, e;\n";
-    os << "                ral_text_line(d, ends, nterm, nb, i, s, e);\n";
+    os << "                ral_text_line(ds, ends, nterm, nb, i, s, e);\n";
     os << "                keep = e > s;\n";
     if (pred) {
         os << "                if (keep) {\n";
         if (!f1.empty()) {
             os << "                    ral_i64 fs[" << f1.size() << "], fe[" << f1.size() << "];\n";
-            os << "                    ral_fields_pred(d, s, e, delim, fs, fe);\n";
+            os << "                    ral_fields_pred(ds, s, e, delim, fs, fe);\n";
         }
         os << "                    ral_u32 fv[" << std::max<size_t>(1, t.predicate_cols.size()) << "];\n";
         for (size_t c = 0; c < t.predicate_cols.size(); c++) {
@@ -2039,10 +2080,18 @@ GeneratedKernel generate_text_scan_kernel(const TextScanSpec& t, const Shape& s)
     os << "            const ral_u32 kA = k0 + lane;\n";
     os << "            const bool act = kA < total;\n";
     os << "            const ral_i64 i = base + s_lst[act ? kA : k0];\n";
+    os << "            const char* ds = d;\n";
+    os << "            {\n";
+    os << "                const ral_i64 i0 = base + s_lst[k0];\n";
+    os << "                const ral_i64 i1 = base + s_lst[k0 + 31u < total ? k0 + 31u : total - 1u];\n";
+    os << "                const ral_i64 S = i0 == 0 ? 0 : ends[i0 - 1] + 1;\n";
+    os << "                const ral_i64 E = i1 < nterm ? ends[i1] : nb;\n";
+    os << "                ds = ral_text_stage(d, nb, S, E, s_txw, lane);\n";
+    os << "            }\n";
     os << "            ral_i64 s, e;\n";
-    os << "            ral_text_line(d, ends, nterm, nb, i, s, e);\n";
+    os << "            ral_text_line(ds, ends, nterm, nb, i, s, e);\n";
     os << "            ral_i64 fs[" << f2.size() << "], fe[" << f2.size() << "];\n";
-    os << "            ral_fields_all(d, s, e, delim, fs, fe);\n";
+    os << "            ral_fields_all(ds, s, e, delim, fs, fe);\n";
     os << "            const ral_u64 pos = excl + kA;\n";
     os << "            const bool put = act && pos < cap;\n";
     os << "            if (act && !put) ++over;\n";
