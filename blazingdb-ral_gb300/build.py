@@ -21,10 +21,10 @@ CUDA = os.environ.get("CUDA_HOME", "/usr/local/cuda")
 NVCC = os.path.join(CUDA, "bin", "nvcc")
 
 CPP = ["program.cpp", "frontend.cpp", "codegen.cpp", "jit.cpp", "engine.cpp", "filter.cpp", "batch.cpp", "server.cpp",
-       "selftest.cpp", "aggregate.cpp", "category.cpp", "textscan.cpp", "capi.cpp"]
+       "selftest.cpp", "aggregate.cpp", "category.cpp", "textscan.cpp", "parquet_meta.cpp", "parquet_scan.cpp", "capi.cpp"]
 CU = ["kernels.cu", "noalloc.cu"]
 HEADERS = ["program.h", "frontend.h", "codegen.h", "jit.h", "engine.h", "filter.h", "batch.h", "server.h", "kernels.h", "device_rt.cuh", "softfp.cuh",
-           "textscan.cuh", "textscan.h"]
+           "textscan.cuh", "textscan.h", "parquet_meta.h"]
 INCLUDES = [f"-I{os.path.join(ROOT, 'include')}", f"-I{CSRC}", f"-I{os.path.join(CUDA, 'include')}"]
 GENCODE = ["-gencode", "arch=compute_103a,code=sm_103a"]
 

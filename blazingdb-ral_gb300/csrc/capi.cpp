@@ -336,6 +336,18 @@ int ral_text_scan_filter(const char* data, int64_t n_bytes, char delimiter, char
     });
 }
 
+int ral_parquet_schema(const uint8_t* file, int64_t n_bytes, int64_t* rows, int32_t* n_columns, int32_t* dtypes,
+                       int32_t capacity) {
+    return guarded([&] { return parquet_schema(file, n_bytes, rows, n_columns, dtypes, capacity); });
+}
+
+int ral_parquet_scan_filter(const uint8_t* file, int64_t n_bytes, const int32_t* projections, int32_t n_projections,
+                            const char* filter_query_part, gdf_column* const* out_columns, gdf_size_type* num_rows_out) {
+    return guarded([&] {
+        return parquet_scan_filter(file, n_bytes, projections, n_projections, filter_query_part, out_columns, num_rows_out);
+    });
+}
+
 int ral_materialize_columns(const gdf_column* const* inputs, gdf_column* const* outputs, int32_t num_columns,
                             const gdf_column* row_indices) {
     return guarded([&] {

@@ -374,9 +374,10 @@ __global__ void category_remap_kernel(int32_t* __restrict__ codes, ral_i64 n, co
 }  // namespace
 
 // ---- line index of a delimited text buffer ---------------------------------------------------
-// Tile t of 4096 bytes: thread k of its block reads bytes [16 k, 16 k + 16) of the tile (one
-// 16-byte load where the buffer allows it), so a block's terminators come out in order from a
-// block-wide scan of the threads' counts.
+// Tile t of 64 KiB in 16 steps of 4 KiB: in step k, thread j reads bytes [16 j, 16 j + 16) of the
+// step (one 16-byte load where the buffer allows it; a warp's loads are one contiguous 512 bytes),
+// so a step's terminators come out in order from a block-wide scan of the threads' counts, and the
+// steps in turn.
 
 __device__ __forceinline__ ral_u32 ral_text_term_bits(const char* data, int64_t n, int64_t at, char term) {
     ral_u32 bits = 0;
@@ -396,7 +397,10 @@ __device__ __forceinline__ ral_u32 ral_text_term_bits(const char* data, int64_t 
 __global__ void __launch_bounds__(256) text_term_count_kernel(const char* __restrict__ data, int64_t n, char term,
                                                               ral_u32* __restrict__ counts) {
     const int64_t tile = blockIdx.x;
-    const ral_u32 c = __popc(ral_text_term_bits(data, n, tile * kTextTileBytes + 16 * (int64_t)threadIdx.x, term));
+    ral_u32 c = 0;
+#pragma unroll 4
+    for (int k = 0; k < (int)(kTextTileBytes / kTextStepBytes); ++k)
+        c += __popc(ral_text_term_bits(data, n, tile * kTextTileBytes + k * kTextStepBytes + 16 * (int64_t)threadIdx.x, term));
     __shared__ ral_u32 s_w[8];
     const ral_u32 wsum = __reduce_add_sync(0xffffffffu, c);
     if ((threadIdx.x & 31) == 0) s_w[threadIdx.x >> 5] = wsum;
@@ -448,22 +452,31 @@ __global__ void __launch_bounds__(256) text_term_positions_kernel(const char* __
                                                                   const unsigned long long* __restrict__ offsets,
                                                                   long long* __restrict__ ends) {
     const int64_t tile = blockIdx.x;
-    const int64_t at = tile * kTextTileBytes + 16 * (int64_t)threadIdx.x;
-    ral_u32 bits = ral_text_term_bits(data, n, at, term);
-    const ral_u32 c = __popc(bits);
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    ral_u32 inc = c;
-    for (int off = 1; off < 32; off <<= 1) {
-        const ral_u32 t = __shfl_up_sync(0xffffffffu, inc, off);
-        if (lane >= off) inc += t;
+    __shared__ ral_u32 s_w[2][8];
+    unsigned long long base = offsets[tile];
+    for (int k = 0; k < (int)(kTextTileBytes / kTextStepBytes); ++k) {
+        const int64_t at = tile * kTextTileBytes + k * kTextStepBytes + 16 * (int64_t)threadIdx.x;
+        if (tile * kTextTileBytes + k * kTextStepBytes >= n) break;  // block-uniform
+        ral_u32 bits = ral_text_term_bits(data, n, at, term);
+        const ral_u32 c = __popc(bits);
+        ral_u32 inc = c;
+        for (int off = 1; off < 32; off <<= 1) {
+            const ral_u32 t = __shfl_up_sync(0xffffffffu, inc, off);
+            if (lane >= off) inc += t;
+        }
+        if (lane == 31) s_w[k & 1][warp] = inc;  // double-buffered: no barrier between a step's reads and the next step's writes
+        __syncthreads();
+        ral_u32 before = inc - c, step_total = 0;
+        for (int w = 0; w < 8; ++w) {
+            const ral_u32 x = s_w[k & 1][w];
+            if (w < warp) before += x;
+            step_total += x;
+        }
+        unsigned long long q = base + before;
+        for (; bits; bits &= bits - 1u) ends[q++] = at + __ffs(bits) - 1;
+        base += step_total;
     }
-    __shared__ ral_u32 s_w[8];
-    if (lane == 31) s_w[warp] = inc;
-    __syncthreads();
-    ral_u32 before = inc - c;
-    for (int w = 0; w < warp; ++w) before += s_w[w];
-    unsigned long long k = offsets[tile] + before;
-    for (; bits; bits &= bits - 1u) ends[k++] = at + __ffs(bits) - 1;
 }
 
 __global__ void __launch_bounds__(256) text_present_count_kernel(const char* __restrict__ data, int64_t n,
@@ -513,6 +526,189 @@ cudaError_t launch_text_term_positions(const char* data, int64_t n, char term, c
     if (tiles <= 0) return cudaSuccess;
     if (tiles > 0x7fffffffll) return cudaErrorInvalidValue;
     text_term_positions_kernel<<<(unsigned)tiles, 256, 0, st>>>(data, n, term, offsets, ends);
+    note_launch();
+    return cudaGetLastError();
+}
+
+// ---- Parquet data pages ----------------------------------------------------------------------
+// One block per page.  A required column's page is its values back to back; an optional
+// column's page starts with the 4-byte length of its definition levels (bit width 1) in the RLE /
+// bit-packed hybrid (a run header varint h: h odd -> h >> 1 groups of 8 bit-packed levels, h even
+// -> h >> 1 repeats of the next byte's level), then the values of the present rows only.  Thread 0
+// turns the run headers into a table in shared memory (a batch of up to kPqRuns runs at a time);
+// the block then takes 256 rows per step: each thread finds its row's level (binary search in
+// the table), a block scan of the levels gives each present row its value's index, and each
+// warp's 32 levels are one ballot OR-ed in at the rows' bit offset.
+
+constexpr int kPqRuns = 1024;
+
+__device__ __forceinline__ unsigned long long ral_load_le(const uint8_t* p, int w) {
+    unsigned long long v = 0;
+    for (int k = 0; k < w; ++k) v |= (unsigned long long)p[k] << (8 * k);
+    return v;
+}
+
+__device__ __forceinline__ void ral_store_w(void* base, int64_t i, int w, unsigned long long v) {
+    if (w == 8) reinterpret_cast<unsigned long long*>(base)[i] = v;
+    else reinterpret_cast<unsigned int*>(base)[i] = (unsigned int)v;
+}
+
+__global__ void __launch_bounds__(256) parquet_decode_kernel(const __grid_constant__ ParquetDecodeParams P) {
+    __shared__ int s_row[kPqRuns + 1];
+    __shared__ int s_info[kPqRuns];
+    __shared__ unsigned char s_kind[kPqRuns];
+    __shared__ int s_nruns, s_end_row, s_bad;
+    __shared__ long long s_pos;
+    __shared__ ral_u32 s_w[8];
+    const ParquetPage pg = P.pages[blockIdx.x];
+    const ParquetColumnOut col = P.out[pg.column];
+    const uint8_t* const d = P.file + pg.data;
+    const int w = col.width;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    int64_t lo = 0;                  // offset of the values in the page data
+    int64_t nvals = 0;               // values present in the page data
+    int32_t lev_bytes = 0;
+    if (pg.optional) {
+        if (pg.data_bytes < 4) {
+            if (threadIdx.x == 0) atomicAdd(P.status, 1ull);
+            return;
+        }
+        lev_bytes = (int32_t)ral_load_le(d, 4);
+        lo = 4 + (int64_t)lev_bytes;
+        if (lev_bytes < 0 || lo > pg.data_bytes) {
+            if (threadIdx.x == 0) atomicAdd(P.status, 1ull);
+            return;
+        }
+    }
+    nvals = (pg.data_bytes - lo) / w;
+    const uint8_t* const lev = d + 4;
+    const uint8_t* const vals = d + lo;
+    if (threadIdx.x == 0) {
+        s_pos = 0;
+        s_end_row = 0;
+        s_bad = 0;
+    }
+    __syncthreads();
+    long long vbase = 0;             // values taken by the rows before this step
+    unsigned long long present = 0;  // this thread's share of the page's present rows
+    while (true) {
+        // the next batch of runs (all rows of a required column form one run of present levels)
+        if (threadIdx.x == 0) {
+            int k = 0;
+            int row = s_end_row;
+            if (!pg.optional) {
+                if (row < pg.rows) {
+                    s_row[0] = row;
+                    s_kind[0] = 0;
+                    s_info[0] = 1;
+                    row = pg.rows;
+                    k = 1;
+                }
+            } else {
+                long long pos = s_pos;
+                while (k < kPqRuns && row < pg.rows) {
+                    unsigned long long h = 0;
+                    int shift = 0;
+                    while (true) {
+                        if (pos >= lev_bytes || shift > 35) {
+                            s_bad = 1;
+                            break;
+                        }
+                        const uint8_t b = lev[pos++];
+                        h |= (unsigned long long)(b & 0x7f) << shift;
+                        shift += 7;
+                        if (!(b & 0x80)) break;
+                    }
+                    if (s_bad) break;
+                    s_row[k] = row;
+                    if (h & 1) {
+                        const long long groups = (long long)(h >> 1);
+                        s_kind[k] = 1;
+                        s_info[k] = (int)pos;
+                        pos += groups;
+                        row += (int)min((long long)pg.rows - row, groups * 8);
+                    } else {
+                        if (pos >= lev_bytes) {
+                            s_bad = 1;
+                            break;
+                        }
+                        s_kind[k] = 0;
+                        s_info[k] = lev[pos++] & 1;
+                        row += (int)min((long long)pg.rows - row, (long long)(h >> 1));
+                    }
+                    if (pos > lev_bytes) {
+                        s_bad = 1;
+                        break;
+                    }
+                    ++k;
+                }
+                s_pos = pos;
+            }
+            s_row[k] = row;
+            s_nruns = k;
+        }
+        __syncthreads();
+        const int nruns = s_nruns;
+        const int r_lo = s_end_row, r_hi = s_row[nruns];
+        if (s_bad) {
+            if (threadIdx.x == 0) atomicAdd(P.status, 1ull);
+            return;
+        }
+        if (nruns == 0) break;
+        for (int r0 = r_lo; r0 < r_hi; r0 += 256) {
+            const int r = r0 + (int)threadIdx.x;
+            bool v = false;
+            if (r < r_hi) {
+                int a = 0, b = nruns - 1;  // the last run starting at or before r
+                while (a < b) {
+                    const int m = (a + b + 1) >> 1;
+                    if (s_row[m] <= r) a = m;
+                    else b = m - 1;
+                }
+                v = s_kind[a] ? ((lev[s_info[a] + ((r - s_row[a]) >> 3)] >> ((r - s_row[a]) & 7)) & 1) != 0 : s_info[a] != 0;
+            }
+            const ral_u32 bal = __ballot_sync(0xffffffffu, v);
+            const ral_u32 before_lane = __popc(bal & ((1u << lane) - 1u));
+            if (lane == 0) s_w[warp] = __popc(bal);
+            __syncthreads();
+            ral_u32 before = before_lane, step_total = 0;
+            for (int k = 0; k < 8; ++k) {
+                const ral_u32 x = s_w[k];
+                if (k < warp) before += x;
+                step_total += x;
+            }
+            const long long vi = vbase + before;
+            const int64_t g = pg.row_start + r;
+            if (r < r_hi) {
+                unsigned long long x = 0;
+                if (v) {
+                    if (vi < nvals) x = ral_load_le(vals + vi * w, w);
+                    else atomicAdd((unsigned int*)&s_bad, 1u);
+                }
+                ral_store_w(col.data, g, w, x);
+            }
+            if (lane == 0 && bal) {
+                const int64_t g0 = pg.row_start + r0 + 32 * warp;
+                const unsigned long long X = (unsigned long long)bal << (g0 & 31);
+                atomicOr(col.valid + (g0 >> 5), (ral_u32)X);
+                if ((ral_u32)(X >> 32)) atomicOr(col.valid + (g0 >> 5) + 1, (ral_u32)(X >> 32));
+            }
+            present += v ? 1 : 0;
+            vbase += step_total;
+            __syncthreads();
+        }
+        if (threadIdx.x == 0) s_end_row = r_hi;
+        __syncthreads();
+        if (r_hi >= pg.rows) break;
+    }
+    if (s_bad && threadIdx.x == 0) atomicAdd(P.status, 1ull);
+    const unsigned long long wp = __reduce_add_sync(0xffffffffu, (ral_u32)present);
+    if (lane == 0 && wp) atomicAdd(P.status + 1 + pg.column, wp);
+}
+
+cudaError_t launch_parquet_decode(const ParquetDecodeParams& p, cudaStream_t st) {
+    if (p.num_pages <= 0) return cudaSuccess;
+    parquet_decode_kernel<<<p.num_pages, 256, 0, st>>>(p);
     note_launch();
     return cudaGetLastError();
 }

@@ -49,8 +49,9 @@ cudaError_t launch_gather_columns(const GatherColumnsParams& p, cudaStream_t st)
 
 // ---- line index of a delimited text buffer (the text scan) ---------------------------------
 
-// Each block handles kTextTileBytes bytes of the buffer: 256 threads x 16 bytes.
-constexpr int64_t kTextTileBytes = 4096;
+// Each block handles kTextTileBytes bytes of the buffer: 16 steps of 256 threads x 16 bytes.
+constexpr int64_t kTextStepBytes = 4096;
+constexpr int64_t kTextTileBytes = 16 * kTextStepBytes;
 inline int64_t text_tiles(int64_t n_bytes) { return (n_bytes + kTextTileBytes - 1) / kTextTileBytes; }
 
 // counts[t] = line terminators in tile t of data[0, n).
@@ -66,6 +67,35 @@ cudaError_t launch_text_term_positions(const char* data, int64_t n, char term, c
 // line i spans (ends[i - 1], ends[i]), the last one (i == nterm) ending at n.
 cudaError_t launch_text_present_count(const char* data, int64_t n, const long long* ends, int64_t nterm, int64_t lines,
                                       int64_t skip, unsigned long long* count, cudaStream_t st);
+
+// ---- Parquet data pages ------------------------------------------------------------------
+
+// One uncompressed data page (v1, PLAIN values) of a projected column, in device memory.
+struct ParquetPage {
+    int64_t row_start;      // the page's first row in the table
+    int64_t data;           // offset of the page's data (after its header) in the file buffer
+    int32_t rows;           // values in the page, nulls included
+    int32_t data_bytes;     // the data's length
+    int32_t column;         // output column
+    int32_t optional;       // definition levels (bit width 1, RLE / bit-packed hybrid) precede the values
+};
+struct ParquetColumnOut {
+    void* data;             // rows x width
+    uint32_t* valid;        // zeroed; bit r = value present
+    int32_t width;
+    int32_t pad;
+};
+constexpr int kParquetMaxColumns = 64;
+struct ParquetDecodeParams {
+    const uint8_t* file;
+    const ParquetPage* pages;
+    ParquetColumnOut out[kParquetMaxColumns];
+    unsigned long long* status;  // [0] pages whose levels or values run past their data, [1..] valid counts
+    int32_t num_pages;
+    int32_t num_columns;
+};
+// Every page decoded into its column: values of present rows in row order, validity bits set.
+cudaError_t launch_parquet_decode(const ParquetDecodeParams& p, cudaStream_t st);
 
 // codes[i] += 1 where codes[i] >= pos: a string inserted at rank pos of a category dictionary.
 cudaError_t launch_category_insert(int32_t* codes, int64_t n, int32_t pos, cudaStream_t st);

@@ -22,4 +22,10 @@ int text_scan_filter(const char* data, int64_t n, char delim, char term, int32_t
 int text_scan_source(const int32_t* file_dtypes, int32_t n_file, const int32_t* projections, int32_t n_proj,
                      const char* filter_q, bool compile, std::string& source, std::string& log);
 
+// Parquet (parquet_scan.cpp): the file's rows, leaf count and the dtype each leaf scans as
+// (GDF_invalid where unsupported); the scan of the projected leaves filtered by filter_q.
+int parquet_schema(const uint8_t* file, int64_t n, int64_t* rows, int32_t* n_columns, int32_t* dtypes, int32_t capacity);
+int parquet_scan_filter(const uint8_t* file, int64_t n, const int32_t* projections, int32_t n_proj, const char* filter_q,
+                        gdf_column* const* outs, gdf_size_type* n_out);
+
 }  // namespace ral

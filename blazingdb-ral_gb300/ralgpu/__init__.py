@@ -15,7 +15,8 @@ from .capi import (RalError, lib, perform_operation, perform_operation_async, pe
                    parse_project_plan, Batch, autotune_program, batch_tune_key, Server, softfp_selftest,
                    debug_lookback_timeout, process_aggregate, debug_aggregate_source, call_timing, filter_grid_launches,
                    Category, category_column, decode_category, filter_project_host,
-                   text_scan_rows, text_scan_filter, debug_text_scan_source)
+                   text_scan_rows, text_scan_filter, debug_text_scan_source, parquet_schema,
+                   parquet_scan_filter)
 from .column import Column, Scalar, valid_alloc_size
 from . import dtypes
 
@@ -27,4 +28,5 @@ __all__ = [
     "valid_alloc_size", "dtypes", "parse_project_plan", "Batch", "autotune_program", "batch_tune_key", "Server", "softfp_selftest", "debug_lookback_timeout",
     "process_aggregate", "debug_aggregate_source", "call_timing", "filter_grid_launches", "Category", "category_column",
     "decode_category", "filter_project_host", "text_scan_rows", "text_scan_filter", "debug_text_scan_source",
+    "parquet_schema", "parquet_scan_filter",
 ]

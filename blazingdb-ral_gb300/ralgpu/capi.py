@@ -60,6 +60,10 @@ _SIGS = {
                                        C.c_int32, C.c_char_p, C.c_void_p, C.POINTER(C.c_int32)]),
     "ral_debug_text_scan_source": (C.c_int, [I32P, C.c_int32, I32P, C.c_int32, C.c_char_p, C.c_int32, C.c_char_p,
                                              C.c_int64, C.c_char_p, C.c_int64]),
+    "ral_parquet_schema": (C.c_int, [C.c_void_p, C.c_int64, C.POINTER(C.c_int64), C.POINTER(C.c_int32), I32P,
+                                     C.c_int32]),
+    "ral_parquet_scan_filter": (C.c_int, [C.c_void_p, C.c_int64, I32P, C.c_int32, C.c_char_p, C.c_void_p,
+                                          C.POINTER(C.c_int32)]),
     "ral_filter_project_host": (C.c_int, [C.c_void_p, C.c_int32, C.c_char_p, C.c_char_p, C.c_void_p, C.c_int32,
                                           C.POINTER(C.c_int32), C.c_int64]),
     "ral_category_create": (C.c_int, [C.c_void_p, C.c_int64, C.POINTER(C.c_void_p), I32P]),
@@ -421,6 +425,32 @@ def debug_text_scan_source(file_dtypes, projections, filter_query_part: Optional
                                             filter_query_part.encode() if filter_query_part else None,
                                             1 if compile else 0, src, len(src), log, len(log)))
     return src.value.decode(), log.value.decode()
+
+
+def parquet_schema(file: bytes):
+    """(rows, [gdf dtype each leaf scans as, GDF_invalid where unsupported]) of a Parquet file."""
+    buf = C.create_string_buffer(bytes(file), len(file))
+    rows, ncols = C.c_int64(0), C.c_int32(0)
+    dts = np.zeros(256, dtype=np.int32)
+    _check(lib().ral_parquet_schema(buf, len(file), C.byref(rows), C.byref(ncols), _p32(dts), len(dts)))
+    return rows.value, [int(x) for x in dts[:ncols.value]]
+
+
+def parquet_scan_filter(file: bytes, projections, filter_query_part: Optional[str] = None) -> List[Column]:
+    """BindableTableScan over a Parquet file (host bytes; projections = leaf indices) followed by
+    its LogicalFilter (None: the scan alone)."""
+    rows, dts = parquet_schema(file)
+    outs = [Column.empty(dts[c], rows, with_valid=True) for c in projections]
+    oa, os_ = _colarray(outs)
+    pr = _i32(projections)
+    n = C.c_int32(0)
+    buf = C.create_string_buffer(bytes(file), len(file))
+    _check(lib().ral_parquet_scan_filter(buf, len(file), _p32(pr), len(pr),
+                                         filter_query_part.encode() if filter_query_part else None,
+                                         C.cast(oa, C.c_void_p), C.byref(n)))
+    for o, st in zip(outs, os_):
+        o.sync_from_c(st)
+    return outs
 
 
 def apply_boolean_mask(stencil: Column) -> Column:

@@ -535,3 +535,197 @@ def text_table_varied(n: int, seed: int = SEED) -> bytes:
             fields = fields[:rng.randint(1, 7)]
         out.append("|".join(fields) + ("\r" if rng.random() < 0.1 else ""))
     return ("\n".join(out) + ("\n" if rng.random() < 0.5 else "")).encode()
+
+
+# ---- Parquet files (scan -> filter over Parquet pages) ---------------------------------------
+# A minimal writer of the Apache Parquet format (flat schema, uncompressed data pages v1, PLAIN
+# values, definition levels of optional columns in the RLE / bit-packed hybrid), for the tests
+# and the benchmark: the GPU image has no Parquet library.  Metadata is Thrift's compact protocol.
+
+_PQ_TYPE = {D.GDF_INT32: 1, D.GDF_DATE32: 1, D.GDF_INT64: 2, D.GDF_DATE64: 2, D.GDF_FLOAT32: 4, D.GDF_FLOAT64: 5}
+_PQ_CONVERTED = {D.GDF_DATE32: 6, D.GDF_DATE64: 9}   # DATE, TIMESTAMP_MILLIS
+
+
+class _Compact:
+    def __init__(self):
+        self.b = bytearray()
+        self.last = [0]
+
+    def varint(self, v: int):
+        while True:
+            x = v & 0x7F
+            v >>= 7
+            if v:
+                self.b.append(x | 0x80)
+            else:
+                self.b.append(x)
+                return
+
+    @staticmethod
+    def zigzag(v: int) -> int:
+        return (v << 1) ^ (v >> 63) if v < 0 else v << 1
+
+    def field(self, fid: int, ftype: int):
+        delta = fid - self.last[-1]
+        if 0 < delta <= 15:
+            self.b.append((delta << 4) | ftype)
+        else:
+            self.b.append(ftype)
+            self.varint(self.zigzag(fid))
+        self.last[-1] = fid
+
+    def i32(self, fid, v):
+        self.field(fid, 5)
+        self.varint(self.zigzag(v))
+
+    def i64(self, fid, v):
+        self.field(fid, 6)
+        self.varint(self.zigzag(v))
+
+    def binary(self, fid, bs: bytes):
+        self.field(fid, 8)
+        self.varint(len(bs))
+        self.b += bs
+
+    def begin(self, fid):
+        self.field(fid, 12)
+        self.last.append(0)
+
+    def end(self):
+        self.b.append(0)
+        self.last.pop()
+
+    def list_header(self, fid, etype, n):
+        self.field(fid, 9)
+        if n < 15:
+            self.b.append((n << 4) | etype)
+        else:
+            self.b.append(0xF0 | etype)
+            self.varint(n)
+
+    def elem_begin(self):
+        self.last.append(0)
+
+    def elem_end(self):
+        self.b.append(0)
+        self.last.pop()
+
+
+def _def_levels(valid: np.ndarray) -> bytes:
+    """Definition levels (bit width 1) in the RLE / bit-packed hybrid: runs of 16 or more equal
+    levels as RLE runs, the rest bit-packed in groups of 8."""
+    out = bytearray()
+    n = valid.shape[0]
+    i = 0
+    enc = _Compact()
+    while i < n:
+        j = i
+        while j < n and valid[j] == valid[i]:
+            j += 1
+        if j - i >= 16:
+            enc.b = bytearray()
+            enc.varint((j - i) << 1)
+            out += enc.b + bytes([1 if valid[i] else 0])
+            i = j
+            continue
+        # bit-packed: up to the next long run (whole groups of 8; the last group padded)
+        k = i
+        while k < n:
+            r = k
+            while r < n and valid[r] == valid[k]:
+                r += 1
+            if r - k >= 16 and (k - i) % 8 == 0 and k > i:
+                break
+            k = r if r - k < 16 else k + 8
+            if k > n:
+                k = n
+        k = min(k, n)
+        groups = (k - i + 7) // 8
+        bits = np.zeros(groups * 8, dtype=np.uint8)
+        bits[:k - i] = valid[i:k]
+        enc.b = bytearray()
+        enc.varint((groups << 1) | 1)
+        out += enc.b + np.packbits(bits, bitorder="little").tobytes()
+        i = k
+    return len(out).to_bytes(4, "little") + bytes(out)
+
+
+def parquet_bytes(columns, row_group_rows: int = 1 << 20, page_rows: int = 1 << 17) -> bytes:
+    """columns: [(name, gdf dtype, values, valid bools or None for a required column)]."""
+    n = len(columns[0][2])
+    out = bytearray(b"PAR1")
+    row_groups = []
+    for r0 in range(0, max(n, 1), row_group_rows):
+        r1 = min(n, r0 + row_group_rows)
+        chunks = []
+        for name, dt, vals, valid in columns:
+            start = len(out)
+            nbytes = 0
+            for p0 in range(r0, max(r1, r0 + 1), page_rows):
+                p1 = min(r1, p0 + page_rows)
+                v = np.asarray(vals[p0:p1])
+                body = bytearray()
+                if valid is not None:
+                    m = np.asarray(valid[p0:p1], dtype=bool)
+                    body += _def_levels(m)
+                    v = v[m]
+                body += np.ascontiguousarray(v.astype(D.NP[dt])).tobytes()
+                h = _Compact()
+                h.i32(1, 0)                       # DATA_PAGE
+                h.i32(2, len(body))
+                h.i32(3, len(body))
+                h.begin(5)                        # DataPageHeader
+                h.i32(1, p1 - p0)
+                h.i32(2, 0)                       # PLAIN
+                h.i32(3, 3)                       # RLE
+                h.i32(4, 3)
+                h.end()
+                h.b.append(0)
+                out += h.b + body
+                nbytes += len(h.b) + len(body)
+                if r1 == r0:
+                    break
+            chunks.append((name, dt, start, nbytes, r1 - r0))
+        row_groups.append((r1 - r0, chunks))
+        if n == 0:
+            break
+    m = _Compact()
+    m.i32(1, 1)
+    m.list_header(2, 12, len(columns) + 1)
+    m.elem_begin(); m.binary(4, b"schema"); m.i32(5, len(columns)); m.elem_end()
+    for name, dt, vals, valid in columns:
+        m.elem_begin()
+        m.i32(1, _PQ_TYPE[dt])
+        m.i32(3, 0 if valid is None else 1)
+        m.binary(4, name.encode())
+        if dt in _PQ_CONVERTED:
+            m.i32(6, _PQ_CONVERTED[dt])
+        m.elem_end()
+    m.i64(3, n)
+    m.list_header(4, 12, len(row_groups))
+    for rows, chunks in row_groups:
+        m.elem_begin()
+        m.list_header(1, 12, len(chunks))
+        total = 0
+        for name, dt, start, nbytes, crow in chunks:
+            total += nbytes
+            m.elem_begin()
+            m.i64(2, start)
+            m.begin(3)
+            m.i32(1, _PQ_TYPE[dt])
+            m.list_header(2, 5, 2); m.varint(m.zigzag(0)); m.varint(m.zigzag(3))
+            m.list_header(3, 8, 1); m.varint(len(name)); m.b += name.encode()
+            m.i32(4, 0)
+            m.i64(5, crow)
+            m.i64(6, nbytes)
+            m.i64(7, nbytes)
+            m.i64(9, start)
+            m.end()
+            m.elem_end()
+        m.i64(2, total)
+        m.i64(3, rows)
+        m.elem_end()
+    m.binary(6, b"ralgpu parquet writer")
+    m.b.append(0)
+    out += m.b + len(m.b).to_bytes(4, "little") + b"PAR1"
+    return bytes(out)

@@ -267,6 +267,24 @@ int ral_text_scan_filter(const char *data, int64_t n_bytes, char delimiter, char
                          gdf_size_type *num_rows_out);
 
 /*
+ * The same fusion over a Parquet file — a BindableTableScan of a Parquet table (parquet_parser::parse,
+ * src/io/data_parser/ParquetParser.cpp:36-90, cudf's Parquet reader) followed by its LogicalFilter.
+ * `file` holds the whole file (n_bytes) in host memory; it is copied to the device once, every data
+ * page of the projected leaves is decoded by one kernel, and the fused filter kernel filters the
+ * decoded columns.  ral_parquet_schema gives the row count, the leaf count and the gdf dtype each
+ * leaf scans as (GDF_invalid where unsupported; dtypes: host array of `capacity` entries).
+ * Supported: flat schemas; INT32 (DATE as DATE32), INT64 (TIMESTAMP_MILLIS as DATE64), FLOAT,
+ * DOUBLE; required and optional leaves; uncompressed v1 data pages of PLAIN values with RLE /
+ * bit-packed definition levels — anything else returns RAL_ERROR_UNSUPPORTED.  out_columns: one per
+ * projection, of its dtype, with a 4-byte aligned mask and room for every row of the file; on return
+ * size = rows kept.  Synchronous.
+ */
+int ral_parquet_schema(const uint8_t *file, int64_t n_bytes, int64_t *rows, int32_t *n_columns, int32_t *dtypes,
+                       int32_t capacity);
+int ral_parquet_scan_filter(const uint8_t *file, int64_t n_bytes, const int32_t *projections, int32_t n_projections,
+                            const char *filter_query_part, gdf_column *const *out_columns, gdf_size_type *num_rows_out);
+
+/*
  * String-category dictionaries — the NVCategory a GDF_STRING_CATEGORY column points at through
  * dtype_info.category in the reference, where a string literal compared with such a column is looked
  * up (src/LogicalFilter.cpp:150-194).  A ral_category keeps its distinct strings sorted by byte

@@ -1,0 +1,71 @@
+"""Scan -> filter over Parquet on the GPU: ral_parquet_scan_filter against the values each file
+holds (pyarrow's fixture with its .npz, and files of ralgpu.workloads.parquet_bytes) and the oracle's
+process_filter over them, bit for bit; required and optional leaves, many pages and row groups, RLE
+and bit-packed definition levels."""
+import os
+
+import numpy as np
+import pytest
+
+import helpers as H
+import oracle as O
+import ralgpu as R
+from conftest import ROOT
+from ralgpu import dtypes as D
+from ralgpu import workloads as W
+from test_parquet_cpu import _writer_table
+
+pytestmark = pytest.mark.gpu
+GOLDEN = os.path.join(ROOT, "tests", "golden")
+
+FILTERS = [None,
+           "LogicalFilter(condition=[>($0, 0)])",
+           "LogicalFilter(condition=[OR(IS NULL($2), <($3, 0))])",
+           "LogicalFilter(condition=[AND(>=($4, 1995-01-01), <($1, 0))])",
+           "LogicalFilter(condition=[<(*($3, 2), $2)])"]
+
+
+def _check(file_bytes, frame, proj, fq):
+    exp_frame = [frame[c] for c in proj]
+    exp = exp_frame if fq is None else O.process_filter(exp_frame, fq)
+    got = R.parquet_scan_filter(file_bytes, proj, fq)
+    assert len(got) == len(exp)
+    for k, (g, e) in enumerate(zip(got, exp)):
+        O.update_null_count(e)
+        H.assert_columns_equal(g, e, what=f"column {k} ({fq})")
+
+
+@pytest.mark.parametrize("fq", FILTERS)
+def test_pyarrow_fixture(fq):
+    b = open(os.path.join(GOLDEN, "parquet_plain.parquet"), "rb").read()
+    v = np.load(os.path.join(GOLDEN, "parquet_plain.npz"))
+    n = len(v["b"])
+    ones = np.ones(n, bool)
+    frame = [O.make_column(v["a"], D.GDF_INT32, v["a_valid"]), O.make_column(v["b"], D.GDF_INT64, ones),
+             O.make_column(v["c"], D.GDF_FLOAT32, v["c_valid"]), O.make_column(v["d"], D.GDF_FLOAT64, ones),
+             O.make_column(v["e"], D.GDF_DATE32, v["e_valid"]), O.make_column(v["f"], D.GDF_DATE64, ones)]
+    _check(b, frame, [0, 1, 2, 3, 4, 5], fq)
+
+
+def _frame_of(cols):
+    return [O.make_column(v, dt, np.ones(len(v), bool) if m is None else m) for _, dt, v, m in cols]
+
+
+@pytest.mark.parametrize("rows,rg,page", [(1, 1, 1), (33, 10, 7), (5000, 2000, 700), (1_000_003, 300_000, 65_536)])
+def test_writer_files(rows, rg, page):
+    cols = _writer_table(rows, rows)
+    b = W.parquet_bytes(cols, row_group_rows=rg, page_rows=page)
+    frame = _frame_of(cols)
+    _check(b, frame, [0, 1, 2, 3, 4, 5], None)
+    # projections reorder the scanned frame: $0 = a, $1 = f, $2 = c, $3 = b, $4 = d
+    _check(b, frame, [0, 5, 2, 1, 3], "LogicalFilter(condition=[OR(IS NULL($2), <($3, 0))])")
+
+
+@pytest.mark.parametrize("name", ["parquet_snappy", "parquet_dictionary"])
+def test_unsupported_files_fail_cleanly(name):
+    b = open(os.path.join(GOLDEN, name + ".parquet"), "rb").read()
+    with pytest.raises(R.RalError):
+        R.parquet_scan_filter(b, [0, 1])
+    # the context stays usable
+    good = W.parquet_bytes(_writer_table(100, 5))
+    assert R.parquet_scan_filter(good, [0])[0].size == 100

@@ -1,0 +1,82 @@
+"""Parquet metadata on the host: the minimal writer of ralgpu.workloads reads back in pyarrow (where
+it is installed), the footer reader gives the fixtures' schemas, and unsupported files are refused
+before any device work."""
+import ctypes
+import io
+import os
+
+import numpy as np
+import pytest
+
+import ralgpu as R
+from conftest import ROOT
+from ralgpu import dtypes as D
+from ralgpu import workloads as W
+
+GOLDEN = os.path.join(ROOT, "tests", "golden")
+
+
+def _writer_table(n, seed):
+    rng = np.random.default_rng(seed)
+    va = rng.random(n) >= 0.1
+    va[100:400] = True          # a long run of present levels (an RLE run)
+    va[500:700] = False         # a long run of nulls
+    cols = [("a", D.GDF_INT32, rng.integers(-99, 99, n).astype(np.int32), va),
+            ("b", D.GDF_FLOAT64, rng.standard_normal(n), None),
+            ("c", D.GDF_DATE32, rng.integers(0, 20000, n).astype(np.int32), rng.random(n) >= 0.5),
+            ("d", D.GDF_DATE64, rng.integers(0, 10**12, n).astype(np.int64), None),
+            ("e", D.GDF_FLOAT32, rng.standard_normal(n).astype(np.float32), rng.random(n) >= 0.02),
+            ("f", D.GDF_INT64, rng.integers(-(1 << 60), 1 << 60, n).astype(np.int64), None)]
+    return cols
+
+
+def test_writer_output_reads_back_in_pyarrow():
+    pq = pytest.importorskip("pyarrow.parquet")
+    cols = _writer_table(20_000, 1)
+    t = pq.read_table(io.BytesIO(W.parquet_bytes(cols, row_group_rows=7000, page_rows=3000)))
+    for name, dt, v, m in cols:
+        c = t.column(name)
+        got_valid = np.asarray(c.is_valid())
+        assert np.array_equal(got_valid, np.ones(len(v), bool) if m is None else m), name
+        import pyarrow as pa
+        raw = c.cast(pa.int64() if dt in (D.GDF_DATE64,) else (pa.int32() if dt == D.GDF_DATE32 else c.type)).fill_null(0)
+        arr = raw.to_numpy()
+        keep = got_valid
+        assert np.array_equal(arr[keep].astype(v.dtype).view(np.uint8), v[keep].view(np.uint8)), name
+
+
+def test_schema_of_the_fixtures():
+    b = open(os.path.join(GOLDEN, "parquet_plain.parquet"), "rb").read()
+    rows, dts = R.parquet_schema(b)
+    assert rows == 3000
+    assert dts == [D.GDF_INT32, D.GDF_INT64, D.GDF_FLOAT32, D.GDF_FLOAT64, D.GDF_DATE32, D.GDF_DATE64]
+    b = W.parquet_bytes(_writer_table(5000, 2), row_group_rows=2000, page_rows=700)
+    rows, dts = R.parquet_schema(b)
+    assert rows == 5000 and dts == [D.GDF_INT32, D.GDF_FLOAT64, D.GDF_DATE32, D.GDF_DATE64, D.GDF_FLOAT32, D.GDF_INT64]
+
+
+@pytest.mark.parametrize("name,reason", [("parquet_snappy", "compressed"), ("parquet_dictionary", "dictionary")])
+def test_unsupported_files_are_refused_before_device_work(name, reason):
+    b = open(os.path.join(GOLDEN, name + ".parquet"), "rb").read()
+    rows, dts = R.parquet_schema(b)
+    L = R.lib()
+    # out columns with placeholder pointers: the refusal comes before anything is dereferenced
+    outs = (R.capi.GdfColumn * 1)()
+    outs[0].data = ctypes.c_void_p(256)
+    outs[0].valid = ctypes.c_void_p(256)
+    outs[0].size = rows
+    outs[0].dtype = dts[0]
+    ptrs = (ctypes.c_void_p * 1)(ctypes.addressof(outs[0]))
+    pr = (ctypes.c_int32 * 1)(0)
+    n = ctypes.c_int32(0)
+    buf = ctypes.create_string_buffer(b, len(b))
+    rc = L.ral_parquet_scan_filter(buf, len(b), pr, 1, None, ctypes.cast(ptrs, ctypes.c_void_p), ctypes.byref(n))
+    assert rc != 0 and reason in L.ral_last_error().decode()
+
+
+def test_not_parquet_and_truncated():
+    with pytest.raises(R.RalError):
+        R.parquet_schema(b"PAR1 not a parquet file")
+    b = open(os.path.join(GOLDEN, "parquet_plain.parquet"), "rb").read()
+    with pytest.raises(R.RalError):
+        R.parquet_schema(b[:-20] + b[-8:])
