@@ -426,7 +426,8 @@ def cpu_served(threads: int, n_queries: int, rows_cap: int, seed: int = 20261203
 # ---- GPU workloads --------------------------------------------------------------------------------
 
 DEFAULT_ROWS = {"fused_project": 200_000_000, "plain_vm": 1_000_000, "filter_gather": 500_000_000,
-                "filter_project": 200_000_000, "gather": 200_000_000, "scan_filter": 20_000_000}
+                "filter_project": 200_000_000, "gather": 200_000_000, "scan_filter": 20_000_000,
+                "parquet_filter": 20_000_000}
 
 
 def workload_config(workload, n, selectivity, world=1):
@@ -445,6 +446,14 @@ def workload_config(workload, n, selectivity, world=1):
                "columns": "int32, int64, float32, float64, date32, bool8; 5% nulls", "index": "int32",
                "api": "ral_materialize_columns (all columns in one kernel)",
                "l2": "columns (5.8 GB at 200M rows) exceed L2; no flush"}
+    elif workload == "parquet_filter":
+        from ralgpu import workloads as W
+        cfg = {"workload": "parquet_filter", "rows": n,
+               "table": "the lineitem-like table as Parquet: 8 required columns, uncompressed PLAIN v1 pages, "
+                        "1Mi-row row groups, in page-locked host memory",
+               "scan": f"BindableTableScan projects={W.TEXT_PROJECTIONS}", "filter": "TPC-H Q6's conditions",
+               "fused": "projected column chunks copied in, one page-decode kernel, the fused filter kernel",
+               "l2": "decoded columns (560 MB at 20M rows) exceed L2; no flush"}
     elif workload == "scan_filter":
         from ralgpu import workloads as W
         cfg = {"workload": "scan_filter", "rows": n, "text_bytes": n * W.TEXT_ROW_BYTES,
@@ -502,6 +511,42 @@ def scan_filter_setup(n, device):
 
     return dict(step=step, scan=scan, alg_bytes_fn=alg_bytes, nout=nout, outs=outs, out_structs=os_, values=values,
                 host_text=host, dev_text=dev, text_bytes=len(text), cols=[R.Column(dev, None, D.GDF_INT8, len(text))])
+
+
+def parquet_filter_setup(n, device):
+    """The lineitem-like table as a Parquet file in page-locked host memory, and one step:
+    ral_parquet_scan_filter of TPC-H Q6's conditions over the scan of quantity, extendedprice,
+    discount and shipdate (the projected column chunks copied in, decoded, filtered)."""
+    import ctypes
+    import torch
+    import ralgpu as R
+    from ralgpu import dtypes as D
+    from ralgpu import workloads as W
+    L = R.lib()
+    values = W.lineitem_values(n, W.SEED)
+    blob = W.parquet_bytes([(nm, dt, v, None) for nm, dt, v in zip(W.LINEITEM_NAMES, W.TEXT_DTYPES, values)])
+    host = torch.frombuffer(bytearray(blob), dtype=torch.uint8).pin_memory()
+    proj = W.TEXT_PROJECTIONS
+    outs = [R.Column.empty(W.TEXT_DTYPES[c], n, with_valid=True, device=device) for c in proj]
+    oa, os_ = _colarray(outs)
+    pr = (ctypes.c_int32 * len(proj))(*proj)
+    nout = ctypes.c_int32(0)
+    fq = W.TEXT_FILTER.encode()
+
+    def step(stream):
+        rc = L.ral_parquet_scan_filter(ctypes.c_void_p(host.data_ptr()), len(blob), pr, len(pr), fq,
+                                       ctypes.cast(oa, ctypes.c_void_p), ctypes.byref(nout))
+        if rc:
+            raise RuntimeError(L.ral_last_error().decode())
+
+    chunk_bytes = n * sum(D.WIDTH[W.TEXT_DTYPES[c]] for c in proj)
+
+    def alg_bytes():
+        k = nout.value
+        return chunk_bytes + k * sum(D.WIDTH[W.TEXT_DTYPES[c]] + 1 / 8 for c in proj)
+
+    return dict(step=step, alg_bytes_fn=alg_bytes, nout=nout, outs=outs, out_structs=os_, values=values,
+                file_bytes=len(blob), chunk_bytes=chunk_bytes, cols=[R.Column(host, None, D.GDF_INT8, len(blob))])
 
 
 def scan_filter_parity(ctx):
@@ -1026,6 +1071,8 @@ def measure_workload(args, workload, n, selectivity, device, world, sampler, e2e
         ctx = fused_project_setup(n, device)
     elif workload == "scan_filter":
         ctx = scan_filter_setup(n, device)
+    elif workload == "parquet_filter":
+        ctx = parquet_filter_setup(n, device)
     elif workload == "gather":
         ctx = gather_setup(n, selectivity, device)
     else:
@@ -1139,6 +1186,12 @@ def measure_workload(args, workload, n, selectivity, device, world, sampler, e2e
                 out["e2e"] = fused_project_e2e(ctx, max(2, min(args.steps, 3)), device)
             elif workload == "scan_filter":
                 out["e2e"] = scan_filter_e2e(ctx, max(2, min(args.steps, 3)))
+            elif workload == "parquet_filter":
+                # the call itself starts from host memory: its step time is the end-to-end time
+                out["e2e"] = {"value": out["value"], "unit": "rows/s", "h2d_bytes_per_step": int(ctx["chunk_bytes"]),
+                              "d2h_bytes_per_step": 0, "ms_per_step": out["ms_per_step"],
+                              "api": "ral_parquet_scan_filter on the file in page-locked host memory (kept rows stay "
+                                     "on the device)"}
             else:
                 out["e2e"] = filter_e2e(ctx, max(2, min(args.steps, 3)))
             link = host_link_peak()
@@ -1148,11 +1201,13 @@ def measure_workload(args, workload, n, selectivity, device, world, sampler, e2e
         # the device outputs (the e2e leg rewrote them with the same bits) against the oracle
         if parity and not args.skip_parity:
             out["parity"] = (gather_parity(ctx) if workload == "gather" else
-                             scan_filter_parity(ctx) if workload == "scan_filter" else
+                             scan_filter_parity(ctx) if workload in ("scan_filter", "parquet_filter") else
                              parity_check(workload, ctx, selectivity))
-        if cpu and not args.skip_cpu:
+        if cpu and not args.skip_cpu and workload != "parquet_filter":
             out["cpu_baseline"] = cpu_baseline(workload, n, selectivity, budget_s=cpu_budget_s,
                                                single_budget_s=cpu_budget_s / 3)
+        if workload == "parquet_filter":
+            out["cpu_baseline_note"] = "no CPU Parquet reader exists on the GPU image (the oracle reads the text form)"
     del ctx
     torch.cuda.empty_cache()
     return out
@@ -1160,7 +1215,8 @@ def measure_workload(args, workload, n, selectivity, device, world, sampler, e2e
 
 # Workloads measured beside the default one in the same run: the 200M-row fused filter + project at
 # s = 0.5 (the target kernel) and the 500M-row filter + gather of six columns at s = 0.5.
-EXTRA_WORKLOADS = [("filter_project", 0.5), ("filter_gather", 0.5), ("gather", "permutation"), ("scan_filter", None)]
+EXTRA_WORKLOADS = [("filter_project", 0.5), ("filter_gather", 0.5), ("gather", "permutation"), ("scan_filter", None),
+                   ("parquet_filter", None)]
 
 
 def run_ours(args):
@@ -1176,7 +1232,7 @@ def run_ours(args):
     extra = {}
     if args.workload == "fused_project" and not args.rows and not args.no_extra:
         for wl, sel in EXTRA_WORKLOADS:
-            key = f"{wl}_{sel}" if isinstance(sel, str) else f"{wl}_s{sel}"
+            key = wl if sel is None else f"{wl}_{sel}" if isinstance(sel, str) else f"{wl}_s{sel}"
             extra[key] = measure_workload(args, wl, DEFAULT_ROWS[wl], sel, device, world, sampler, cpu_budget_s=6.0)
     sampler.stop()
     out = {
@@ -1186,7 +1242,8 @@ def run_ours(args):
         "dtype": {"fused_project": "f64+int64", "filter_project": "f64+int64", "plain_vm": "f64+int64",
                   "filter_gather": "int32/int64/f32/f64/date32/bool8 gather",
                   "gather": "int32/int64/f32/f64/date32/bool8 gather",
-                  "scan_filter": "u8 text -> int32/f64/date64"}[args.workload],
+                  "scan_filter": "u8 text -> int32/f64/date64",
+                  "parquet_filter": "Parquet pages -> int32/f64/date64"}[args.workload],
         "data": "synthetic (seeded, generated on the GPU)",
         "config": main["config"],
         "hbm_gbs": main["roofline"]["achieved"],
@@ -1620,7 +1677,8 @@ def run_reference(args):
            "dtype": {"fused_project": "f64+int64", "filter_project": "f64+int64", "plain_vm": "f64+int64",
                      "filter_gather": "int32/int64/f32/f64/date32/bool8 gather",
                   "gather": "int32/int64/f32/f64/date32/bool8 gather",
-                  "scan_filter": "u8 text -> int32/f64/date64"}[args.workload],
+                  "scan_filter": "u8 text -> int32/f64/date64",
+                  "parquet_filter": "Parquet pages -> int32/f64/date64"}[args.workload],
            "data": "synthetic (seeded)", "impl": "reference",
            "config": workload_config(args.workload, n, sel, world),
            "cpu_baseline": {"value": v, "unit": "rows/s", "cores": threads, "kind": "port",
@@ -1637,7 +1695,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="fused_project",
                     choices=["fused_project", "plain_vm", "filter_gather", "filter_project", "gather", "batched",
-                             "served"])
+                             "served", "scan_filter", "parquet_filter"])
     ap.add_argument("--tables", type=int, default=24)
     ap.add_argument("--queries", type=int, default=96)
     ap.add_argument("--requests", type=int, default=50_000)

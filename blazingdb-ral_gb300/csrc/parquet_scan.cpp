@@ -4,8 +4,8 @@
 // `projects=[...]` picks the columns) through parquet_parser::parse
 // (src/io/data_parser/ParquetParser.cpp:36-90, cudf's Parquet reader), and a LogicalFilter above
 // it evaluates its condition over the scanned frame and compacts it (CalciteInterpreter.cpp:509).
-// Here the footer and page headers are read on the host (parquet_meta.cpp), the file is copied to
-// the device once, one kernel decodes every data page of the projected columns into columns, and
+// Here the footer and page headers are read on the host (parquet_meta.cpp), the projected columns'
+// chunks are copied to the device (one copy each), one kernel decodes every data page into columns, and
 // the fused filter kernel (filter.cpp) filters them -- or, without a filter, the decoded columns are
 // the result.  Supported: flat schemas; INT32 (DATE), INT64 (TIMESTAMP_MILLIS), FLOAT, DOUBLE;
 // required and optional columns; uncompressed v1 data pages with PLAIN values.  Anything else
@@ -95,8 +95,14 @@ int parquet_scan_filter(const uint8_t* file, int64_t n, const int32_t* projectio
         if (outs[q]->size < rows)
             return set_error(kInvalidArgument, "out columns must hold every row of the file (" + std::to_string(rows) + ")");
     }
-    // the data pages of the projected columns
+    // the data pages of the projected columns; only their column chunks travel to the device, packed
+    // one after another (a page's `data` is its offset in that packed copy)
     std::vector<ParquetPage> pages;
+    struct Range {
+        int64_t file_off, bytes, dev_off;
+    };
+    std::vector<Range> ranges;
+    int64_t packed = 0;
     int64_t row0 = 0;
     for (const pq::RowGroupMeta& g : meta.row_groups) {
         for (int q = 0; q < n_proj; q++) {
@@ -106,6 +112,7 @@ int parquet_scan_filter(const uint8_t* file, int64_t n, const int32_t* projectio
             if (cc.dictionary_page_offset >= 0)
                 return set_error(kUnsupported, "column '" + l.name + "': dictionary-encoded pages are not supported");
             int64_t at = cc.data_page_offset, seen = 0;
+            const size_t first_page = pages.size();
             while (seen < cc.num_values) {
                 pq::PageHeader ph;
                 const std::string err = pq::read_page_header(file, n, at, ph);
@@ -129,6 +136,10 @@ int parquet_scan_filter(const uint8_t* file, int64_t n, const int32_t* projectio
                 at = data + ph.compressed_size;
             }
             if (seen != g.num_rows) return set_error(kUnsupported, "column '" + l.name + "': page values differ from the row group's rows");
+            const Range r{cc.data_page_offset, at - cc.data_page_offset, packed};
+            for (size_t k = first_page; k < pages.size(); k++) pages[k].data = r.dev_off + (pages[k].data - r.file_off);
+            ranges.push_back(r);
+            packed += (r.bytes + 15) & ~15ll;
         }
         row0 += g.num_rows;
     }
@@ -160,8 +171,12 @@ int parquet_scan_filter(const uint8_t* file, int64_t n, const int32_t* projectio
         pframe[q] = &frame[q];
         cudaMemsetAsync(frame[q].valid, 0, gdf_valid_allocation_size(std::max<int64_t>(rows, 1)), st);
     }
-    if (int e = dfile.alloc((size_t)n)) return e;
-    if (int e = check_cuda(cudaMemcpyAsync(dfile.p, file, (size_t)n, cudaMemcpyHostToDevice, st), "cudaMemcpyAsync")) return e;
+    if (int e = dfile.alloc((size_t)packed)) return e;
+    for (const Range& r : ranges)
+        if (r.bytes > 0 && check_cuda(cudaMemcpyAsync((char*)dfile.p + r.dev_off, file + r.file_off, (size_t)r.bytes,
+                                                      cudaMemcpyHostToDevice, st),
+                                      "cudaMemcpyAsync"))
+            return kCudaError;
     if (int e = dpages.alloc(pages.size() * sizeof(ParquetPage))) return e;
     if (!pages.empty() &&
         check_cuda(cudaMemcpyAsync(dpages.p, pages.data(), pages.size() * sizeof(ParquetPage), cudaMemcpyHostToDevice, st),

@@ -481,19 +481,41 @@ def _date_chars(days: np.ndarray) -> np.ndarray:
 TEXT_ROW_BYTES = 66
 
 
-def text_table(n: int, seed: int = SEED, values: bool = False):
-    """n rows of the lineitem-like table, each ended by '\\n' (fixed width: 66 bytes a row); with
-    values=True also the column values the text spells (for a check that needs no parse)."""
+def _lineitem_draws(n: int, seed: int):
     rng = np.random.default_rng(seed)
-    bar = np.full((n, 1), ord("|"), dtype=np.uint8)
-    point = np.full((n, 1), ord("."), dtype=np.uint8)
-    zero = np.full((n, 1), ord("0"), dtype=np.uint8)
     price = rng.integers(90000, 10500000, n)              # cents
     disc = rng.integers(0, 11, n)                         # hundredths
     tax = rng.integers(0, 9, n)
     ship = rng.integers(8036, 10591, n)                   # 1992-01-02 .. 1998-12-31
     okey, pkey, qty = rng.integers(1, 6_000_000_000, n), rng.integers(1, 2_000_000, n), rng.integers(1, 51, n)
     commit = ship + rng.integers(-60, 60, n)
+    return okey, pkey, qty, price, disc, tax, ship, commit
+
+
+def lineitem_values(n: int, seed: int = SEED):
+    """The column values of the lineitem-like table (TEXT_DTYPES), as text_table spells them."""
+    okey, pkey, qty, price, disc, tax, ship, commit = _lineitem_draws(n, seed)
+    # the nearest double of d.dd is price / 100 rounded once (the division of two exact values)
+    return [okey.astype(np.int64), pkey.astype(np.int32), qty.astype(np.int32), price / 100.0, disc / 100.0,
+            (tax / 100.0).astype(np.float32), ship.astype(np.int64) * 86_400_000, commit.astype(np.int32)]
+
+
+LINEITEM_NAMES = ["orderkey", "partkey", "quantity", "extendedprice", "discount", "tax", "shipdate", "commitdate"]
+
+
+def lineitem_parquet(n: int, seed: int = SEED) -> bytes:
+    """The lineitem-like table as a Parquet file (required columns, 1Mi-row row groups)."""
+    vals = lineitem_values(n, seed)
+    return parquet_bytes([(nm, dt, v, None) for nm, dt, v in zip(LINEITEM_NAMES, TEXT_DTYPES, vals)])
+
+
+def text_table(n: int, seed: int = SEED, values: bool = False):
+    """n rows of the lineitem-like table, each ended by '\\n' (fixed width: 66 bytes a row); with
+    values=True also the column values the text spells (for a check that needs no parse)."""
+    bar = np.full((n, 1), ord("|"), dtype=np.uint8)
+    point = np.full((n, 1), ord("."), dtype=np.uint8)
+    zero = np.full((n, 1), ord("0"), dtype=np.uint8)
+    okey, pkey, qty, price, disc, tax, ship, commit = _lineitem_draws(n, seed)
     parts = [_digits(okey, 10), bar, _digits(pkey, 7), bar,
              _digits(qty, 2), bar, _digits(price // 100, 8), point, _digits(price % 100, 2), bar,
              zero, point, _digits(disc, 2), bar, zero, point, _digits(tax, 2), bar, _date_chars(ship), bar,
@@ -501,10 +523,7 @@ def text_table(n: int, seed: int = SEED, values: bool = False):
     text = np.concatenate(parts, axis=1).tobytes()
     if not values:
         return text
-    # the nearest double of d.dd is price / 100 rounded once (the division of two exact values)
-    cols = [okey.astype(np.int64), pkey.astype(np.int32), qty.astype(np.int32), price / 100.0, disc / 100.0,
-            (tax / 100.0).astype(np.float32), ship.astype(np.int64) * 86_400_000, commit.astype(np.int32)]
-    return text, cols
+    return text, lineitem_values(n, seed)
 
 
 def text_table_varied(n: int, seed: int = SEED) -> bytes:

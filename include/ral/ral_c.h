@@ -269,9 +269,9 @@ int ral_text_scan_filter(const char *data, int64_t n_bytes, char delimiter, char
 /*
  * The same fusion over a Parquet file — a BindableTableScan of a Parquet table (parquet_parser::parse,
  * src/io/data_parser/ParquetParser.cpp:36-90, cudf's Parquet reader) followed by its LogicalFilter.
- * `file` holds the whole file (n_bytes) in host memory; it is copied to the device once, every data
- * page of the projected leaves is decoded by one kernel, and the fused filter kernel filters the
- * decoded columns.  ral_parquet_schema gives the row count, the leaf count and the gdf dtype each
+ * `file` holds the whole file (n_bytes) in host memory; the projected leaves' column chunks are copied
+ * to the device (page-locked memory makes the copies faster), every data page is decoded by one
+ * kernel, and the fused filter kernel filters the decoded columns.  ral_parquet_schema gives the row count, the leaf count and the gdf dtype each
  * leaf scans as (GDF_invalid where unsupported; dtypes: host array of `capacity` entries).
  * Supported: flat schemas; INT32 (DATE as DATE32), INT64 (TIMESTAMP_MILLIS as DATE64), FLOAT,
  * DOUBLE; required and optional leaves; uncompressed v1 data pages of PLAIN values with RLE /
