@@ -1207,7 +1207,7 @@ def measure_workload(args, workload, n, selectivity, device, world, sampler, e2e
             out["cpu_baseline"] = cpu_baseline(workload, n, selectivity, budget_s=cpu_budget_s,
                                                single_budget_s=cpu_budget_s / 3)
         if workload == "parquet_filter":
-            out["cpu_baseline_note"] = "no CPU Parquet reader exists on the GPU image (the oracle reads the text form)"
+            out["cpu_baseline_note"] = "no CPU Parquet reader is installed where the benchmark runs (the oracle reads the text form)"
     del ctx
     torch.cuda.empty_cache()
     return out
