@@ -497,6 +497,8 @@ def scan_filter_setup(n, device):
     fq = W.TEXT_FILTER.encode()
 
     def scan(ptr):
+        for st in os_:  # the outputs' capacity (a call leaves size = rows kept)
+            st.size = n
         rc = L.ral_text_scan_filter(ctypes.c_void_p(ptr), len(text), b"|", b"\n", 0, fd, len(fd), pr, len(pr), fq,
                                     ctypes.cast(oa, ctypes.c_void_p), ctypes.byref(nout))
         if rc:
@@ -534,6 +536,8 @@ def parquet_filter_setup(n, device):
     fq = W.TEXT_FILTER.encode()
 
     def step(stream):
+        for st in os_:  # the outputs' capacity (a call leaves size = rows kept)
+            st.size = n
         rc = L.ral_parquet_scan_filter(ctypes.c_void_p(host.data_ptr()), len(blob), pr, len(pr), fq,
                                        ctypes.cast(oa, ctypes.c_void_p), ctypes.byref(nout))
         if rc:
