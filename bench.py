@@ -452,7 +452,8 @@ def workload_config(workload, n, selectivity, world=1):
                "table": "the lineitem-like table as Parquet: 8 required columns, uncompressed PLAIN v1 pages, "
                         "1Mi-row row groups, in page-locked host memory",
                "scan": f"BindableTableScan projects={W.TEXT_PROJECTIONS}", "filter": "TPC-H Q6's conditions",
-               "fused": "projected column chunks copied in, one page-decode kernel, the fused filter kernel",
+               "fused": "the projected pages read in place from page-locked host memory by the page-value kernel "
+                        "(a block per 8192-row item of a page), then the fused filter kernel",
                "l2": "decoded columns (560 MB at 20M rows) exceed L2; no flush"}
     elif workload == "scan_filter":
         from ralgpu import workloads as W
@@ -518,7 +519,7 @@ def scan_filter_setup(n, device):
 def parquet_filter_setup(n, device):
     """The lineitem-like table as a Parquet file in page-locked host memory, and one step:
     ral_parquet_scan_filter of TPC-H Q6's conditions over the scan of quantity, extendedprice,
-    discount and shipdate (the projected column chunks copied in, decoded, filtered)."""
+    discount and shipdate (the projected pages read in place over the host link, decoded, filtered)."""
     import ctypes
     import torch
     import ralgpu as R

@@ -101,7 +101,8 @@ void fill_scalars(const Program& p, const ParamLayout& L, std::vector<uint64_t>&
 namespace {
 
 struct DeviceInfo {
-    int sms = 0;
+    int sms = 0;             // 0: not read yet
+    bool pool_kept = false;  // keep_pool_memory ran
 };
 std::mutex g_dev_mu;
 std::unordered_map<int, DeviceInfo> g_devs;
@@ -113,13 +114,25 @@ int device_sms() {
     int dev = 0;
     cudaGetDevice(&dev);
     std::lock_guard<std::mutex> lock(g_dev_mu);
-    auto it = g_devs.find(dev);
-    if (it != g_devs.end()) return it->second.sms;
-    DeviceInfo d;
+    DeviceInfo& d = g_devs[dev];
+    if (d.sms > 0) return d.sms;
     cudaDeviceGetAttribute(&d.sms, cudaDevAttrMultiProcessorCount, dev);
     if (d.sms <= 0) d.sms = 1;
-    g_devs[dev] = d;
     return d.sms;
+}
+
+void keep_pool_memory() {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return;
+    std::lock_guard<std::mutex> lock(g_dev_mu);
+    DeviceInfo& d = g_devs[dev];
+    if (d.pool_kept) return;
+    cudaMemPool_t pool;
+    if (cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) {
+        uint64_t thr = UINT64_MAX;
+        cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr);
+    }
+    d.pool_kept = true;
 }
 
 int blocks_per_sm(const CompiledKernel& k, int threads) {

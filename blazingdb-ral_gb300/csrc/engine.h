@@ -85,6 +85,10 @@ int launch_blocks(const CompiledKernel& k, int threads, int64_t work_items_per_b
 // SMs of the current device; resident blocks per SM of a compiled kernel (cached per device).
 int device_sms();
 int blocks_per_sm(const CompiledKernel& k, int threads);
+// Freed stream-ordered allocations of the current device stay in its default pool instead of going
+// back to the driver at each synchronisation, so the large per-call buffers of the scans and the
+// server are reused rather than mapped again (set once per device for the process).
+void keep_pool_memory();
 
 // Parameter block filled in ParamLayout order.
 void fill_scalars(const Program& p, const ParamLayout& L, std::vector<uint64_t>& slots);

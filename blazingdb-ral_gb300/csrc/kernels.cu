@@ -531,184 +531,317 @@ cudaError_t launch_text_term_positions(const char* data, int64_t n, char term, c
 }
 
 // ---- Parquet data pages ----------------------------------------------------------------------
-// One block per page.  A required column's page is its values back to back; an optional
-// column's page starts with the 4-byte length of its definition levels (bit width 1) in the RLE /
-// bit-packed hybrid (a run header varint h: h odd -> h >> 1 groups of 8 bit-packed levels, h even
-// -> h >> 1 repeats of the next byte's level), then the values of the present rows only.  Thread 0
-// turns the run headers into a table in shared memory (a batch of up to kPqRuns runs at a time);
-// the block then takes 256 rows per step: each thread finds its row's level (binary search in
-// the table), a block scan of the levels gives each present row its value's index, and each
-// warp's 32 levels are one ballot OR-ed in at the rows' bit offset.
+// A required column's page is its values back to back; an optional column's page starts with the
+// 4-byte length of its definition levels (bit width 1) in the RLE / bit-packed hybrid (a run
+// header varint h: h odd -> h >> 1 groups of 8 bit-packed levels, h even -> h >> 1 repeats of the
+// next byte's level), then the values of the present rows only.  Two kernels:
+//  * levels, one block per optional page: the level bytes are staged in shared memory, thread 0
+//    turns the run headers into a table (a batch of up to kPqRuns runs at a time), and the block
+//    writes the validity words from it, 32 rows per thread, counting the present rows of each
+//    8192-row item; the counts become each item's first value index;
+//  * values, one block per 8192-row item of a page: a required page copies its rows' values; an
+//    optional page ranks each row among its item's present rows (a block scan of the validity
+//    words' popcounts) and fetches its value.
 
 constexpr int kPqRuns = 1024;
+constexpr int kPqStage = 32768;  // level bytes of a page staged in shared memory
 
-__device__ __forceinline__ unsigned long long ral_load_le(const uint8_t* p, int w) {
-    unsigned long long v = 0;
-    for (int k = 0; k < w; ++k) v |= (unsigned long long)p[k] << (8 * k);
-    return v;
+// An 8- or 4-byte little-endian value at base + i * w, where base has any alignment: two aligned
+// loads and a funnel shift (the second load stays inside the 8-byte word holding the value's last
+// byte, so it never leaves the buffer).
+__device__ __forceinline__ unsigned long long ral_pq_value(const uint8_t* base, int64_t i, int w) {
+    const uintptr_t a = (uintptr_t)(base + i * w);
+    if (w == 8) {
+        const int s = (int)(a & 7);
+        const unsigned long long* q = reinterpret_cast<const unsigned long long*>(a - s);
+        const unsigned long long lo = q[0];
+        return s ? (lo >> (8 * s)) | (q[1] << (64 - 8 * s)) : lo;
+    }
+    const int s = (int)(a & 3);
+    const ral_u32* q = reinterpret_cast<const ral_u32*>(a - s);
+    const ral_u32 lo = q[0];
+    return s ? (ral_u32)((lo >> (8 * s)) | (q[1] << (32 - 8 * s))) : lo;
 }
 
-__device__ __forceinline__ void ral_store_w(void* base, int64_t i, int w, unsigned long long v) {
+__device__ __forceinline__ void ral_pq_store(void* base, int64_t i, int w, unsigned long long v) {
     if (w == 8) reinterpret_cast<unsigned long long*>(base)[i] = v;
     else reinterpret_cast<unsigned int*>(base)[i] = (unsigned int)v;
 }
 
-__global__ void __launch_bounds__(256) parquet_decode_kernel(const __grid_constant__ ParquetDecodeParams P) {
+__global__ void __launch_bounds__(256) parquet_levels_kernel(const __grid_constant__ ParquetDecodeParams P) {
+    __shared__ ral_u32 s_lw[kPqStage / 4 + 2];
     __shared__ int s_row[kPqRuns + 1];
-    __shared__ int s_info[kPqRuns];
+    __shared__ int s_info[kPqRuns];  // bit-packed: byte offset of the run's levels; RLE: the level
     __shared__ unsigned char s_kind[kPqRuns];
-    __shared__ int s_nruns, s_end_row, s_bad;
+    __shared__ int s_n, s_bad, s_emit, s_emit_end, s_done;
     __shared__ long long s_pos;
-    __shared__ ral_u32 s_w[8];
-    const ParquetPage pg = P.pages[blockIdx.x];
+    const ParquetPage pg = P.pages[P.page_lo + blockIdx.x];
+    if (!pg.optional || pg.rows <= 0) return;
     const ParquetColumnOut col = P.out[pg.column];
-    const uint8_t* const d = P.file + pg.data;
-    const int w = col.width;
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    int64_t lo = 0;                  // offset of the values in the page data
-    int64_t nvals = 0;               // values present in the page data
-    int32_t lev_bytes = 0;
-    if (pg.optional) {
-        if (pg.data_bytes < 4) {
-            if (threadIdx.x == 0) atomicAdd(P.status, 1ull);
-            return;
-        }
-        lev_bytes = (int32_t)ral_load_le(d, 4);
-        lo = 4 + (int64_t)lev_bytes;
-        if (lev_bytes < 0 || lo > pg.data_bytes) {
-            if (threadIdx.x == 0) atomicAdd(P.status, 1ull);
-            return;
-        }
+    const uint8_t* const lev = P.file + pg.data + 4;
+    const int lev_bytes = pg.levels;
+    const int off = (int)((uintptr_t)lev & 3);
+    const int staged = min(lev_bytes, kPqStage);
+    {
+        // aligned words covering [lev, lev + staged): they stay inside the page's data or the
+        // buffer's 16-byte padding
+        const ral_u32* gw = reinterpret_cast<const ral_u32*>(lev - off);
+        const int nw = (off + staged + 3) >> 2;
+        for (int i = threadIdx.x; i < nw; i += blockDim.x) s_lw[i] = gw[i];
     }
-    nvals = (pg.data_bytes - lo) / w;
-    const uint8_t* const lev = d + 4;
-    const uint8_t* const vals = d + lo;
+    const uint8_t* const sb = reinterpret_cast<const uint8_t*>(s_lw) + off;
+    auto lb = [&](long long p) -> unsigned long long {
+        return p < staged ? sb[p] : (p < lev_bytes ? lev[p] : 0u);
+    };
     if (threadIdx.x == 0) {
         s_pos = 0;
-        s_end_row = 0;
+        s_n = 0;
+        s_row[0] = 0;
         s_bad = 0;
+        s_emit = 0;
+        s_done = 0;
     }
     __syncthreads();
-    long long vbase = 0;             // values taken by the rows before this step
-    unsigned long long present = 0;  // this thread's share of the page's present rows
+    const int words = (pg.rows + 31) >> 5;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     while (true) {
-        // the next batch of runs (all rows of a required column form one run of present levels)
         if (threadIdx.x == 0) {
-            int k = 0;
-            int row = s_end_row;
-            if (!pg.optional) {
-                if (row < pg.rows) {
-                    s_row[0] = row;
-                    s_kind[0] = 0;
-                    s_info[0] = 1;
-                    row = pg.rows;
-                    k = 1;
+            // append runs after the carried ones; runs of no rows are skipped
+            int k = s_n;
+            int row = s_row[k];
+            long long pos = s_pos;
+            while (k < kPqRuns && row < pg.rows) {
+                unsigned long long h = 0;
+                int shift = 0;
+                bool ok = true;
+                while (true) {
+                    if (pos >= lev_bytes || shift > 35) {
+                        ok = false;
+                        break;
+                    }
+                    const unsigned long long b = lb(pos++);
+                    h |= (b & 0x7f) << shift;
+                    shift += 7;
+                    if (!(b & 0x80)) break;
                 }
-            } else {
-                long long pos = s_pos;
-                while (k < kPqRuns && row < pg.rows) {
-                    unsigned long long h = 0;
-                    int shift = 0;
-                    while (true) {
-                        if (pos >= lev_bytes || shift > 35) {
-                            s_bad = 1;
-                            break;
-                        }
-                        const uint8_t b = lev[pos++];
-                        h |= (unsigned long long)(b & 0x7f) << shift;
-                        shift += 7;
-                        if (!(b & 0x80)) break;
-                    }
-                    if (s_bad) break;
-                    s_row[k] = row;
-                    if (h & 1) {
-                        const long long groups = (long long)(h >> 1);
-                        s_kind[k] = 1;
-                        s_info[k] = (int)pos;
-                        pos += groups;
-                        row += (int)min((long long)pg.rows - row, groups * 8);
-                    } else {
-                        if (pos >= lev_bytes) {
-                            s_bad = 1;
-                            break;
-                        }
-                        s_kind[k] = 0;
-                        s_info[k] = lev[pos++] & 1;
-                        row += (int)min((long long)pg.rows - row, (long long)(h >> 1));
-                    }
-                    if (pos > lev_bytes) {
+                if (!ok) {
+                    s_bad = 1;
+                    break;
+                }
+                int len;
+                if (h & 1) {
+                    const long long groups = (long long)(h >> 1);
+                    if (pos + groups > lev_bytes) {
                         s_bad = 1;
                         break;
                     }
-                    ++k;
+                    s_kind[k] = 1;
+                    s_info[k] = (int)pos;
+                    pos += groups;
+                    len = (int)min((long long)pg.rows - row, groups * 8);
+                } else {
+                    if (pos >= lev_bytes) {
+                        s_bad = 1;
+                        break;
+                    }
+                    s_kind[k] = 0;
+                    s_info[k] = (int)(lb(pos++) & 1);
+                    len = (int)min((long long)pg.rows - row, (long long)(h >> 1));
                 }
-                s_pos = pos;
+                if (len <= 0) continue;
+                s_row[k] = row;
+                row += len;
+                ++k;
+                s_row[k] = row;
             }
-            s_row[k] = row;
-            s_nruns = k;
+            s_pos = pos;
+            s_n = k;
+            // whole words covered by the table (all of them once the page's rows are)
+            s_emit_end = row >= pg.rows ? words : (row >> 5);
         }
         __syncthreads();
-        const int nruns = s_nruns;
-        const int r_lo = s_end_row, r_hi = s_row[nruns];
-        if (s_bad) {
-            if (threadIdx.x == 0) atomicAdd(P.status, 1ull);
-            return;
-        }
-        if (nruns == 0) break;
-        for (int r0 = r_lo; r0 < r_hi; r0 += 256) {
-            const int r = r0 + (int)threadIdx.x;
-            bool v = false;
-            if (r < r_hi) {
-                int a = 0, b = nruns - 1;  // the last run starting at or before r
+        if (s_bad) break;
+        const int n = s_n, e0 = s_emit, e1 = s_emit_end;
+        for (int k0 = e0; k0 < e1; k0 += 256) {
+            const int k = k0 + (int)threadIdx.x;
+            ral_u32 X = 0;
+            if (k < e1) {
+                const int r0 = 32 * k, r1 = min(r0 + 32, pg.rows);
+                int a = 0, b = n - 1;  // the last run starting at or before r0
                 while (a < b) {
                     const int m = (a + b + 1) >> 1;
-                    if (s_row[m] <= r) a = m;
+                    if (s_row[m] <= r0) a = m;
                     else b = m - 1;
                 }
-                v = s_kind[a] ? ((lev[s_info[a] + ((r - s_row[a]) >> 3)] >> ((r - s_row[a]) & 7)) & 1) != 0 : s_info[a] != 0;
-            }
-            const ral_u32 bal = __ballot_sync(0xffffffffu, v);
-            const ral_u32 before_lane = __popc(bal & ((1u << lane) - 1u));
-            if (lane == 0) s_w[warp] = __popc(bal);
-            __syncthreads();
-            ral_u32 before = before_lane, step_total = 0;
-            for (int k = 0; k < 8; ++k) {
-                const ral_u32 x = s_w[k];
-                if (k < warp) before += x;
-                step_total += x;
-            }
-            const long long vi = vbase + before;
-            const int64_t g = pg.row_start + r;
-            if (r < r_hi) {
-                unsigned long long x = 0;
-                if (v) {
-                    if (vi < nvals) x = ral_load_le(vals + vi * w, w);
-                    else atomicAdd((unsigned int*)&s_bad, 1u);
+                for (int r = r0; r < r1; ++a) {
+                    const int re = min(s_row[a + 1], r1);
+                    const int len = re - r;
+                    const ral_u32 m = len == 32 ? 0xffffffffu : ((1u << len) - 1u);
+                    ral_u32 bits;
+                    if (s_kind[a]) {
+                        const int bo = r - s_row[a];
+                        const long long p = s_info[a] + (bo >> 3);
+                        const unsigned long long v = lb(p) | lb(p + 1) << 8 | lb(p + 2) << 16 | lb(p + 3) << 24 | lb(p + 4) << 32;
+                        bits = (ral_u32)(v >> (bo & 7)) & m;
+                    } else {
+                        bits = s_info[a] ? m : 0u;
+                    }
+                    X |= bits << (r - r0);
+                    r = re;
                 }
-                ral_store_w(col.data, g, w, x);
             }
-            if (lane == 0 && bal) {
-                const int64_t g0 = pg.row_start + r0 + 32 * warp;
-                const unsigned long long X = (unsigned long long)bal << (g0 & 31);
-                atomicOr(col.valid + (g0 >> 5), (ral_u32)X);
-                if ((ral_u32)(X >> 32)) atomicOr(col.valid + (g0 >> 5) + 1, (ral_u32)(X >> 32));
+            // present rows per item (a warp's 32 words lie in at most two items)
+            const int first = (k0 + 32 * warp) >> 8;
+            const ral_u32 c = __popc(X);
+            const ral_u32 ca = (k >> 8) == first ? c : 0u;
+            const ral_u32 sa = __reduce_add_sync(0xffffffffu, ca);
+            const ral_u32 sb2 = __reduce_add_sync(0xffffffffu, c - ca);
+            if (lane == 0) {
+                if (sa) atomicAdd(P.item_base + pg.item0 + first, sa);
+                if (sb2) atomicAdd(P.item_base + pg.item0 + first + 1, sb2);
             }
-            present += v ? 1 : 0;
-            vbase += step_total;
-            __syncthreads();
+            if (X) {
+                const int64_t g = pg.row_start + 32 * (int64_t)k;
+                const int sh = (int)(g & 31);
+                ral_u32* const vw = col.valid + (g >> 5);
+                if (sh == 0 && 32 * k + 32 <= pg.rows) {
+                    *vw = X;  // the word holds rows of this page only
+                } else {
+                    atomicOr(vw, X << sh);
+                    const ral_u32 hi = sh ? X >> (32 - sh) : 0u;
+                    if (hi) atomicOr(vw + 1, hi);
+                }
+            }
         }
-        if (threadIdx.x == 0) s_end_row = r_hi;
         __syncthreads();
-        if (r_hi >= pg.rows) break;
+        if (threadIdx.x == 0) {
+            s_emit = e1;
+            if (e1 >= words) {
+                s_done = 1;
+            } else {
+                // carry the runs that reach into the first word not written yet
+                const int from = 32 * e1;
+                int a = 0;
+                while (a < n && s_row[a + 1] <= from) ++a;
+                for (int j = a; j <= n; ++j) {
+                    s_row[j - a] = s_row[j];
+                    if (j < n) {
+                        s_kind[j - a] = s_kind[j];
+                        s_info[j - a] = s_info[j];
+                    }
+                }
+                s_n = n - a;
+            }
+        }
+        __syncthreads();
+        if (s_done) break;
     }
-    if (s_bad && threadIdx.x == 0) atomicAdd(P.status, 1ull);
-    const unsigned long long wp = __reduce_add_sync(0xffffffffu, (ral_u32)present);
-    if (lane == 0 && wp) atomicAdd(P.status + 1 + pg.column, wp);
+    if (threadIdx.x == 0) {
+        if (s_bad) {
+            atomicAdd(P.status, 1ull);
+            return;
+        }
+        // item counts -> each item's first value index; the page's values must cover them
+        const int items = (pg.rows + kParquetItemRows - 1) / kParquetItemRows;
+        ral_u32 run = 0;
+        for (int i = 0; i < items; ++i) {
+            const ral_u32 c = __ldcg(P.item_base + pg.item0 + i);
+            P.item_base[pg.item0 + i] = run;
+            run += c;
+        }
+        const int64_t nvals = (pg.data_bytes - 4 - (int64_t)lev_bytes) / col.width;
+        if ((int64_t)run > nvals) atomicAdd(P.status, 1ull);
+        if (run) atomicAdd(P.status + 1 + pg.column, (unsigned long long)run);
+    }
 }
 
-cudaError_t launch_parquet_decode(const ParquetDecodeParams& p, cudaStream_t st) {
-    if (p.num_pages <= 0) return cudaSuccess;
-    parquet_decode_kernel<<<p.num_pages, 256, 0, st>>>(p);
+__global__ void __launch_bounds__(256) parquet_values_kernel(const __grid_constant__ ParquetDecodeParams P) {
+    __shared__ ral_u32 s_word[256];
+    __shared__ ral_u32 s_base[256];
+    __shared__ ral_u32 s_wsum[8];
+    const int item = P.item_lo + (int)blockIdx.x;
+    int a = P.page_lo, b = P.page_hi - 1;  // the last page whose first item is at or before this one
+    while (a < b) {
+        const int m = (a + b + 1) >> 1;
+        if (P.pages[m].item0 <= item) a = m;
+        else b = m - 1;
+    }
+    const ParquetPage pg = P.pages[a];
+    const ParquetColumnOut col = P.out[pg.column];
+    const int w = col.width;
+    const int rel0 = (item - pg.item0) * kParquetItemRows;
+    const int rel1 = min(rel0 + kParquetItemRows, pg.rows);
+    const int64_t lo = pg.optional ? 4 + (int64_t)pg.levels : 0;
+    const uint8_t* const vals = P.file + pg.data + lo;
+    if (!pg.optional) {
+        // every row has its value (the page's length is checked on the host)
+        int r = rel0 + (int)threadIdx.x;
+        for (; r + 768 < rel1; r += 1024) {
+            const unsigned long long x0 = ral_pq_value(vals, r, w), x1 = ral_pq_value(vals, r + 256, w);
+            const unsigned long long x2 = ral_pq_value(vals, r + 512, w), x3 = ral_pq_value(vals, r + 768, w);
+            ral_pq_store(col.data, pg.row_start + r, w, x0);
+            ral_pq_store(col.data, pg.row_start + r + 256, w, x1);
+            ral_pq_store(col.data, pg.row_start + r + 512, w, x2);
+            ral_pq_store(col.data, pg.row_start + r + 768, w, x3);
+        }
+        for (; r < rel1; r += 256) ral_pq_store(col.data, pg.row_start + r, w, ral_pq_value(vals, r, w));
+        return;
+    }
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int64_t nvals = (pg.data_bytes - lo) / w;
+    // this item's validity words, page-relative (rows of the next page masked off)
+    ral_u32 X = 0;
+    {
+        const int r0 = rel0 + 32 * (int)threadIdx.x;
+        if (r0 < rel1) {
+            const int64_t g = pg.row_start + r0;
+            const int sh = (int)(g & 31);
+            const int nb = min(32, rel1 - r0);
+            const ral_u32* vw = col.valid + (g >> 5);
+            X = vw[0] >> sh;
+            if (sh && nb > 32 - sh) X |= vw[1] << (32 - sh);
+            if (nb < 32) X &= (1u << nb) - 1u;
+        }
+    }
+    // exclusive scan of the words' popcounts
+    const ral_u32 c = __popc(X);
+    ral_u32 incl = c;
+    for (int d = 1; d < 32; d <<= 1) {
+        const ral_u32 y = __shfl_up_sync(0xffffffffu, incl, d);
+        if (lane >= d) incl += y;
+    }
+    if (lane == 31) s_wsum[warp] = incl;
+    s_word[threadIdx.x] = X;
+    __syncthreads();
+    ral_u32 before = 0;
+    for (int k = 0; k < warp; ++k) before += s_wsum[k];
+    s_base[threadIdx.x] = before + incl - c;
+    __syncthreads();
+    const int64_t base = (int64_t)P.item_base[item];
+    // each warp takes one word (32 rows) per step
+    for (int t = warp; t * 32 < rel1 - rel0; t += 8) {
+        const int r = rel0 + 32 * t + lane;
+        if (r >= rel1) break;
+        const ral_u32 Xw = s_word[t];
+        unsigned long long x = 0;
+        if ((Xw >> lane) & 1u) {
+            const int64_t vi = base + s_base[t] + __popc(Xw & ((1u << lane) - 1u));
+            if (vi < nvals) x = ral_pq_value(vals, vi, w);
+        }
+        ral_pq_store(col.data, pg.row_start + r, w, x);
+    }
+}
+
+cudaError_t launch_parquet_levels(const ParquetDecodeParams& p, cudaStream_t st) {
+    if (p.page_hi <= p.page_lo) return cudaSuccess;
+    parquet_levels_kernel<<<p.page_hi - p.page_lo, 256, 0, st>>>(p);
+    note_launch();
+    return cudaGetLastError();
+}
+
+cudaError_t launch_parquet_values(const ParquetDecodeParams& p, cudaStream_t st) {
+    if (p.item_hi <= p.item_lo) return cudaSuccess;
+    parquet_values_kernel<<<p.item_hi - p.item_lo, 256, 0, st>>>(p);
     note_launch();
     return cudaGetLastError();
 }

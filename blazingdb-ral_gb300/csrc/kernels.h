@@ -78,6 +78,8 @@ struct ParquetPage {
     int32_t data_bytes;     // the data's length
     int32_t column;         // output column
     int32_t optional;       // definition levels (bit width 1, RLE / bit-packed hybrid) precede the values
+    int32_t levels;         // optional pages: bytes of the level runs (after their 4-byte length)
+    int32_t item0;          // the page's first item (kParquetItemRows rows of a page per item)
 };
 struct ParquetColumnOut {
     void* data;             // rows x width
@@ -86,16 +88,22 @@ struct ParquetColumnOut {
     int32_t pad;
 };
 constexpr int kParquetMaxColumns = 64;
+constexpr int kParquetItemRows = 8192;
 struct ParquetDecodeParams {
     const uint8_t* file;
     const ParquetPage* pages;
     ParquetColumnOut out[kParquetMaxColumns];
     unsigned long long* status;  // [0] pages whose levels or values run past their data, [1..] valid counts
-    int32_t num_pages;
-    int32_t num_columns;
+    uint32_t* item_base;         // per item of an optional page: its page's present rows before it (zeroed)
+    int32_t page_lo, page_hi;    // the pages of this launch
+    int32_t item_lo, item_hi;    // their items
 };
-// Every page decoded into its column: values of present rows in row order, validity bits set.
-cudaError_t launch_parquet_decode(const ParquetDecodeParams& p, cudaStream_t st);
+// Optional pages of [page_lo, page_hi): validity bits from the definition levels, each item's
+// first value index in item_base, the present rows in status[1 + column].
+cudaError_t launch_parquet_levels(const ParquetDecodeParams& p, cudaStream_t st);
+// Items [item_lo, item_hi): values of the present rows in row order (null rows 0).  Optional
+// pages' levels must have been decoded by an earlier launch_parquet_levels.
+cudaError_t launch_parquet_values(const ParquetDecodeParams& p, cudaStream_t st);
 
 // codes[i] += 1 where codes[i] >= pos: a string inserted at rank pos of a category dictionary.
 cudaError_t launch_category_insert(int32_t* codes, int64_t n, int32_t pos, cudaStream_t st);

@@ -337,11 +337,7 @@ int Server::start() {
     if (started_) return kSuccess;
     cudaGetDevice(&device_);
     // keep freed request memory in the pool instead of returning it to the driver each time
-    cudaMemPool_t pool;
-    if (cudaDeviceGetDefaultMemPool(&pool, device_) == cudaSuccess) {
-        uint64_t thr = UINT64_MAX;
-        cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr);
-    }
+    keep_pool_memory();
     if (int e = ensure_linked()) return e;
     started_ = true;
     stop_ = false;

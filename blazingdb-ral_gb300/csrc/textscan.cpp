@@ -259,6 +259,7 @@ int text_scan_filter(const char* data, int64_t n, char delim, char term, int32_t
     if (int e = prepare_scan(dtypes, file_cols, filter_q, &ps)) return e;
     const int NP = n_proj;
     cudaStream_t st = cudaStreamPerThread;
+    keep_pool_memory();
     LineIndex li(st);
     if (int e = build_line_index(data, n, term, st, li)) return e;
     const GeneratedKernel& gk = ps->gk;

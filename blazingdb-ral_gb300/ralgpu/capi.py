@@ -436,15 +436,22 @@ def parquet_schema(file: bytes):
     return rows.value, [int(x) for x in dts[:ncols.value]]
 
 
-def parquet_scan_filter(file: bytes, projections, filter_query_part: Optional[str] = None) -> List[Column]:
+def parquet_scan_filter(file: bytes, projections, filter_query_part: Optional[str] = None,
+                        page_locked: bool = False) -> List[Column]:
     """BindableTableScan over a Parquet file (host bytes; projections = leaf indices) followed by
-    its LogicalFilter (None: the scan alone)."""
+    its LogicalFilter (None: the scan alone).  page_locked=True hands the library the file in
+    page-locked memory, which its kernels read in place instead of copying the pages in."""
     rows, dts = parquet_schema(file)
     outs = [Column.empty(dts[c], rows, with_valid=True) for c in projections]
     oa, os_ = _colarray(outs)
     pr = _i32(projections)
     n = C.c_int32(0)
-    buf = C.create_string_buffer(bytes(file), len(file))
+    if page_locked:
+        import torch
+        host = torch.frombuffer(bytearray(file), dtype=torch.uint8).pin_memory() if len(file) else None
+        buf = C.c_void_p(host.data_ptr() if host is not None else 0)
+    else:
+        buf = C.create_string_buffer(bytes(file), len(file))
     _check(lib().ral_parquet_scan_filter(buf, len(file), _p32(pr), len(pr),
                                          filter_query_part.encode() if filter_query_part else None,
                                          C.cast(oa, C.c_void_p), C.byref(n)))

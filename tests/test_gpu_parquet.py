@@ -26,13 +26,15 @@ FILTERS = [None,
 
 
 def _check(file_bytes, frame, proj, fq):
+    """Both ways in: pages copied from pageable memory, and read in place from page-locked memory."""
     exp_frame = [frame[c] for c in proj]
     exp = exp_frame if fq is None else O.process_filter(exp_frame, fq)
-    got = R.parquet_scan_filter(file_bytes, proj, fq)
-    assert len(got) == len(exp)
-    for k, (g, e) in enumerate(zip(got, exp)):
-        O.update_null_count(e)
-        H.assert_columns_equal(g, e, what=f"column {k} ({fq})")
+    for page_locked in (False, True):
+        got = R.parquet_scan_filter(file_bytes, proj, fq, page_locked=page_locked)
+        assert len(got) == len(exp)
+        for k, (g, e) in enumerate(zip(got, exp)):
+            O.update_null_count(e)
+            H.assert_columns_equal(g, e, what=f"column {k} ({fq}, page-locked {page_locked})")
 
 
 @pytest.mark.parametrize("fq", FILTERS)
@@ -51,8 +53,11 @@ def _frame_of(cols):
     return [O.make_column(v, dt, np.ones(len(v), bool) if m is None else m) for _, dt, v, m in cols]
 
 
-@pytest.mark.parametrize("rows,rg,page", [(1, 1, 1), (33, 10, 7), (5000, 2000, 700), (1_000_003, 300_000, 65_536)])
+@pytest.mark.parametrize("rows,rg,page", [(1, 1, 1), (33, 10, 7), (5000, 2000, 700), (1_000_003, 300_000, 65_536),
+                                          (600_000, 600_000, 300_000)])
 def test_writer_files(rows, rg, page):
+    # the last case: pages whose levels exceed the 32 KiB staged in shared memory and hold more
+    # than the 1024 runs of one table batch
     cols = _writer_table(rows, rows)
     b = W.parquet_bytes(cols, row_group_rows=rg, page_rows=page)
     frame = _frame_of(cols)
@@ -64,8 +69,21 @@ def test_writer_files(rows, rg, page):
 @pytest.mark.parametrize("name", ["parquet_snappy", "parquet_dictionary"])
 def test_unsupported_files_fail_cleanly(name):
     b = open(os.path.join(GOLDEN, name + ".parquet"), "rb").read()
-    with pytest.raises(R.RalError):
-        R.parquet_scan_filter(b, [0, 1])
+    for page_locked in (False, True):
+        with pytest.raises(R.RalError):
+            R.parquet_scan_filter(b, [0, 1], page_locked=page_locked)
     # the context stays usable
     good = W.parquet_bytes(_writer_table(100, 5))
     assert R.parquet_scan_filter(good, [0])[0].size == 100
+
+
+@pytest.mark.parametrize("batch_bytes", ["1", "4096", "100000"])
+def test_copy_batches(monkeypatch, batch_bytes):
+    """Pages copied and decoded in many small batches (one page per batch at 1 byte); the
+    page-locked leg reads the pages in place in one launch."""
+    monkeypatch.setenv("RAL_PARQUET_BATCH_BYTES", batch_bytes)
+    cols = _writer_table(20_011, 3)
+    b = W.parquet_bytes(cols, row_group_rows=7000, page_rows=999)
+    frame = _frame_of(cols)
+    _check(b, frame, [0, 1, 2, 3, 4, 5], None)
+    _check(b, frame, [2, 4, 0], "LogicalFilter(condition=[OR(IS NULL($1), <($0, 1995-01-01))])")
