@@ -177,6 +177,11 @@ struct OpEmitter {
                 auto t01 = [&](const std::string& v, Kind k) {
                     return k == Kind::I64 ? "((" + v + ") != 0)" : "(!ral_dzero(" + v + "))";
                 };
+                // the precomputed multiplier and shift of a literal integer divisor
+                auto divider = [&](size_t j) {
+                    const std::string m = std::to_string(L.rdiv_slot[j]);
+                    return "(ral_i64)P.s[" + m + "], (ral_i64)P.s[" + m + " + 1]";
+                };
                 const std::string ld = l01 ? d01(l, lk) : to_d(l, lk);
                 const std::string rd = r01 ? d01(r, rk) : to_d(r, rk);
                 auto arith = [&](const char* dop, const char* iop) {
@@ -199,8 +204,18 @@ struct OpEmitter {
                     else e = arith("__dmul_rn", "ral_muli");
                     res01 = l01 && r01;
                     break;
-                case GDF_DIV: case GDF_FLOOR_DIV: e = arith("ral_ddiv", "ral_divi"); break;
-                case GDF_MOD: e = conv("ral_modi(" + to_i(l, lk) + ", " + to_i(r, rk) + ")", Kind::I64, ok); break;
+                case GDF_DIV: case GDF_FLOOR_DIV:
+                    if (L.rdiv_slot.size() > k && L.rdiv_slot[k] >= 0)
+                        e = conv("ral_sf_divc(" + l + ", " + r + ", " + divider(k) + ")", Kind::I64, ok);
+                    else
+                        e = arith("ral_ddiv", "ral_divi");
+                    break;
+                case GDF_MOD:
+                    if (L.rdiv_slot.size() > k && L.rdiv_slot[k] >= 0)
+                        e = conv("ral_sf_modc(" + to_i(l, lk) + ", " + r + ", " + divider(k) + ")", Kind::I64, ok);
+                    else
+                        e = conv("ral_modi(" + to_i(l, lk) + ", " + to_i(r, rk) + ")", Kind::I64, ok);
+                    break;
                 case GDF_POW:
                     if (dtype_is_float(op.ltype) || dtype_is_float(op.rtype))
                         e = conv("pow(" + to_d(l, lk) + ", " + to_d(r, rk) + ")", Kind::F64, ok);
@@ -341,15 +356,11 @@ ParamLayout make_layout(const Program& p, int extra_slots_before_scalars) {
     L.out_valid = s; s += p.n_out;
     L.counts = s++;
     s += extra_slots_before_scalars;
-    L.lscalar_slot.assign(p.ops.size(), -1);
-    L.rscalar_slot.assign(p.ops.size(), -1);
-    for (size_t k = 0; k < p.ops.size(); k++) {
-        if (p.ops[k].left == SCALAR_INDEX) L.lscalar_slot[k] = s++;
-        if (!p.ops[k].unary && p.ops[k].right == SCALAR_INDEX) L.rscalar_slot[k] = s++;
-    }
+    assign_scalar_slots(p, L, s);
     L.total = s;
     return L;
 }
+
 
 // The row function: one row through the program, typed registers in, final
 // register values out.
@@ -380,6 +391,26 @@ std::vector<Kind> final_kinds(const Program& p, const ParamLayout& L) {
 }
 
 }  // namespace
+
+bool divides_by_int_literal(const Op& op) {
+    if (op.unary || op.right != SCALAR_INDEX || op.rk != Kind::I64) return false;
+    if (op.bop == GDF_MOD) return true;  // both operands are taken as int64
+    return (op.bop == GDF_DIV || op.bop == GDF_FLOOR_DIV) && op.lk == Kind::I64;
+}
+
+void assign_scalar_slots(const Program& p, ParamLayout& L, int& slot) {
+    L.lscalar_slot.assign(p.ops.size(), -1);
+    L.rscalar_slot.assign(p.ops.size(), -1);
+    L.rdiv_slot.assign(p.ops.size(), -1);
+    for (size_t k = 0; k < p.ops.size(); k++) {
+        if (p.ops[k].left == SCALAR_INDEX) L.lscalar_slot[k] = slot++;
+        if (!p.ops[k].unary && p.ops[k].right == SCALAR_INDEX) L.rscalar_slot[k] = slot++;
+        if (divides_by_int_literal(p.ops[k])) {
+            L.rdiv_slot[k] = slot;
+            slot += 2;
+        }
+    }
+}
 
 namespace {
 
@@ -950,25 +981,17 @@ GeneratedKernel generate_filter_kernel(const FilterSpec& f, const Shape& s, bool
     L.scratch = slot++;
     ParamLayout PL, QL;  // scalar slots of the predicate and projection programs
     if (f.predicate) {
-        PL.lscalar_slot.assign(f.predicate->ops.size(), -1);
-        PL.rscalar_slot.assign(f.predicate->ops.size(), -1);
-        for (size_t k = 0; k < f.predicate->ops.size(); k++) {
-            if (f.predicate->ops[k].left == SCALAR_INDEX) PL.lscalar_slot[k] = slot++;
-            if (!f.predicate->ops[k].unary && f.predicate->ops[k].right == SCALAR_INDEX) PL.rscalar_slot[k] = slot++;
-        }
+        assign_scalar_slots(*f.predicate, PL, slot);
     }
     if (f.project) {
-        QL.lscalar_slot.assign(f.project->ops.size(), -1);
-        QL.rscalar_slot.assign(f.project->ops.size(), -1);
-        for (size_t k = 0; k < f.project->ops.size(); k++) {
-            if (f.project->ops[k].left == SCALAR_INDEX) QL.lscalar_slot[k] = slot++;
-            if (!f.project->ops[k].unary && f.project->ops[k].right == SCALAR_INDEX) QL.rscalar_slot[k] = slot++;
-        }
+        assign_scalar_slots(*f.project, QL, slot);
     }
     L.lscalar_slot = PL.lscalar_slot;
     L.rscalar_slot = PL.rscalar_slot;
+    L.rdiv_slot = PL.rdiv_slot;
     gk.layout_project_lscalar = QL.lscalar_slot;
     gk.layout_project_rscalar = QL.rscalar_slot;
+    gk.layout_project_rdiv = QL.rdiv_slot;
     if (!item) L.obase = slot++;
     if (!item && s.grid_k > 0) {
         L.epoch = slot++;
@@ -1844,12 +1867,7 @@ GeneratedKernel generate_text_scan_kernel(const TextScanSpec& t, const Shape& s)
     L.scratch = slot++;
     const Program* pred = t.predicate;
     if (pred) {
-        L.lscalar_slot.assign(pred->ops.size(), -1);
-        L.rscalar_slot.assign(pred->ops.size(), -1);
-        for (size_t k = 0; k < pred->ops.size(); k++) {
-            if (pred->ops[k].left == SCALAR_INDEX) L.lscalar_slot[k] = slot++;
-            if (!pred->ops[k].unary && pred->ops[k].right == SCALAR_INDEX) L.rscalar_slot[k] = slot++;
-        }
+        assign_scalar_slots(*pred, L, slot);
     }
     L.total = slot;
 

@@ -65,8 +65,18 @@ struct ParamLayout {
     int epoch = -1;
     int hostmap = -1;
     std::vector<int> lscalar_slot, rscalar_slot;  // per op of the (predicate) program, -1 if none
+    // per op: for an integer division or remainder by a literal, the first of two slots holding
+    // the literal's precomputed multiplier and shift (ral_sf_make_divider), -1 if none
+    std::vector<int> rdiv_slot;
     int total = 0;
 };
+
+// True for an integer division or remainder whose divisor is a literal (computed with a
+// multiplier precomputed on the host instead of a division per row).
+bool divides_by_int_literal(const Op& op);
+// Gives each literal operand of p's ops its slot (and an integer divisor its two divider slots),
+// from `slot` on.
+void assign_scalar_slots(const Program& p, ParamLayout& L, int& slot);
 
 // Largest element width (bytes) over the columns a kernel reads or writes.
 int max_width(const Program& p);
@@ -83,6 +93,7 @@ struct GeneratedKernel {
     Shape shape;
     // filter kernels: scalar slots of the projection program
     std::vector<int> layout_project_lscalar, layout_project_rscalar;
+    std::vector<int> layout_project_rdiv;
     // filter item functions: shared-memory words the function needs in its warp's area
     int item_smem_words = 0;
     // integer-pipe double operations (softfp.cuh) unless RAL_SOFT_FP=0.  Batched item functions

@@ -16,6 +16,8 @@
 #include <mutex>
 #include <unordered_map>
 
+#include "softfp.cuh"
+
 namespace ral {
 
 namespace {
@@ -95,6 +97,11 @@ void fill_scalars(const Program& p, const ParamLayout& L, std::vector<uint64_t>&
     for (size_t k = 0; k < p.ops.size(); k++) {
         if (L.lscalar_slot[k] >= 0) slots[L.lscalar_slot[k]] = p.ops[k].lscalar;
         if (L.rscalar_slot[k] >= 0) slots[L.rscalar_slot[k]] = p.ops[k].rscalar;
+        if (k < L.rdiv_slot.size() && L.rdiv_slot[k] >= 0) {
+            const RalDivider v = ral_sf_make_divider((long long)p.ops[k].rscalar);
+            slots[L.rdiv_slot[k]] = (uint64_t)v.mult;
+            slots[L.rdiv_slot[k] + 1] = (uint64_t)v.shift_mode;
+        }
     }
 }
 

@@ -546,6 +546,7 @@ int enqueue_prepared(const PreparedFilter& pf, gdf_column* const* frame, gdf_col
         ParamLayout QL;
         QL.lscalar_slot = gk.layout_project_lscalar;
         QL.rscalar_slot = gk.layout_project_rscalar;
+        QL.rdiv_slot = gk.layout_project_rdiv;
         fill_scalars(pf.proj, QL, slots);
     }
     void* args[] = {slots.data()};
@@ -896,6 +897,7 @@ void filter_fill_slots(const FilterPlan& plan, const GeneratedKernel& gk, gdf_co
         ParamLayout QL;
         QL.lscalar_slot = gk.layout_project_lscalar;
         QL.rscalar_slot = gk.layout_project_rscalar;
+        QL.rdiv_slot = gk.layout_project_rdiv;
         fill_scalars(plan.proj, QL, slots);
     }
 }

@@ -583,6 +583,86 @@ RAL_SF long long ral_sf_mod64(long long a, long long b) {
     return a < 0 ? (long long)(0ull - r) : (long long)r;
 }
 
+// ---- 64-bit integer division by an invariant divisor -------------------------------------------
+//
+// n / d and n % d (C semantics: truncation, the remainder takes the dividend's sign) for a divisor
+// known before the kernel runs, a literal of the program.  The host finds a multiplier M and a shift
+// s once; then trunc(n / d) = (high word of M * n, plus n when d > 0 > M, minus n when d < 0 < M)
+// shifted right arithmetically by s, plus one when that is negative (Granlund and Montgomery,
+// "Division by invariant integers using multiplication", PLDI 1994; the signed multiplier search
+// of Warren, "Hacker's Delight", 2nd ed., section 10-4, carried to 64 bits).  Divisors without a
+// multiplier (0, 1, -1, INT64_MIN) are marked by a mode in the shift word and handled directly, with
+// this library's values for the undefined cases: x / 0 = x % 0 = 0, INT64_MIN / -1 = INT64_MIN.
+struct RalDivider {
+    long long mult;
+    long long shift_mode;  // bits 0-7: s; bits 8+: 0 multiplier, 1 d = 0, 2 d = 1, 3 d = -1, 4 d = INT64_MIN
+};
+
+RAL_SF RalDivider ral_sf_make_divider(long long d) {
+    RalDivider v{0, 0};
+    if (d == 0 || d == 1 || d == -1 || d == (long long)RAL_SF_SIGN) {
+        v.shift_mode = (long long)(d == 0 ? 1 : d == 1 ? 2 : d == -1 ? 3 : 4) << 8;
+        return v;
+    }
+    const unsigned long long two63 = RAL_SF_SIGN;
+    const unsigned long long ad = d < 0 ? 0ull - (unsigned long long)d : (unsigned long long)d;
+    const unsigned long long t = two63 + ((unsigned long long)d >> 63);
+    const unsigned long long anc = t - 1 - t % ad;  // |nc|: the largest dividend with nc % ad == ad - 1
+    int p = 63;
+    unsigned long long q1 = two63 / anc, r1 = two63 - q1 * anc;  // 2^p / |nc|
+    unsigned long long q2 = two63 / ad, r2 = two63 - q2 * ad;    // 2^p / |d|
+    unsigned long long delta;
+    do {
+        p += 1;
+        q1 <<= 1;
+        r1 <<= 1;
+        if (r1 >= anc) {
+            q1 += 1;
+            r1 -= anc;
+        }
+        q2 <<= 1;
+        r2 <<= 1;
+        if (r2 >= ad) {
+            q2 += 1;
+            r2 -= ad;
+        }
+        delta = ad - r2;
+    } while (q1 < delta || (q1 == delta && r1 == 0));
+    const unsigned long long m = q2 + 1;
+    v.mult = (long long)(d < 0 ? 0ull - m : m);
+    v.shift_mode = p - 64;
+    return v;
+}
+
+RAL_SF long long ral_sf_mulhs(long long a, long long b) {
+#if defined(__CUDA_ARCH__)
+    return __mul64hi(a, b);
+#else
+    return (long long)(((__int128)a * b) >> 64);
+#endif
+}
+
+RAL_SF long long ral_sf_divc(long long n, long long d, long long mult, long long shift_mode) {
+    const int mode = (int)(shift_mode >> 8);
+    if (mode != 0) {
+        if (mode == 1) return 0;
+        if (mode == 2) return n;
+        if (mode == 3) return (long long)(0ull - (unsigned long long)n);
+        return n == (long long)RAL_SF_SIGN ? 1 : 0;
+    }
+    unsigned long long q = (unsigned long long)ral_sf_mulhs(mult, n);
+    if (d > 0 && mult < 0) q += (unsigned long long)n;
+    else if (d < 0 && mult > 0) q -= (unsigned long long)n;
+    long long qs = (long long)q >> (int)(shift_mode & 0xff);
+    return qs + (long long)((unsigned long long)qs >> 63);
+}
+
+RAL_SF long long ral_sf_modc(long long n, long long d, long long mult, long long shift_mode) {
+    if ((shift_mode >> 8) == 1) return 0;  // d == 0
+    const long long q = ral_sf_divc(n, d, mult, shift_mode);
+    return (long long)((unsigned long long)n - (unsigned long long)q * (unsigned long long)d);
+}
+
 // ---- sine and cosine ---------------------------------------------------------------------------
 
 // 64-bit value V (a leading one anywhere) times 2^E, rounded to nearest even as a double (normal

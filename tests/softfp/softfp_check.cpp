@@ -88,6 +88,18 @@ int main(int argc, char** argv) {
             std::snprintf(cd16.first, sizeof cd16.first, "%lld / %lld: want %lld %lld got %lld %lld", a, b, a / b,
                           a % b, ral_sf_div64_16(a, b), ral_sf_mod64_16(a, b));
     };
+    Counter cdc{"divc"};
+    auto check_divc = [&](long long a, long long b) {  // by a precomputed divider (every b)
+        const RalDivider v = ral_sf_make_divider(b);
+        long long wq, wr;
+        if (b == 0) wq = wr = 0;
+        else if (b == -1) wq = (long long)(0ull - (unsigned long long)a), wr = 0;
+        else wq = a / b, wr = a % b;
+        cdc.n++;
+        const long long gq = ral_sf_divc(a, b, v.mult, v.shift_mode), gr = ral_sf_modc(a, b, v.mult, v.shift_mode);
+        if ((gq != wq || gr != wr) && cdc.bad++ == 0)
+            std::snprintf(cdc.first, sizeof cdc.first, "%lld / %lld: want %lld %lld got %lld %lld", a, b, wq, wr, gq, gr);
+    };
     Counter cd32{"div64_32"};
     auto check_d32 = [&](unsigned long long n, unsigned int d) {
         if (d == 0) return;
@@ -189,6 +201,22 @@ int main(int argc, char** argv) {
         check_d32(rng(), 0xffffffffu - (unsigned)(rng() % 3));
         check_d32(rng(), (1u << (rng() % 32)) + (unsigned)(rng() % 3) - 1u);
         check_div64(INT64_MAX, xb);
+        // division by a precomputed divider: divisors of every size and sign, powers of two and
+        // their neighbours, the extremes; dividends likewise
+        {
+            const long long pb = (long long)(1ull << (rng() % 63)) + (long long)(rng() % 3) - 1;
+            const long long dvs[] = {xb, (long long)(0ull - (unsigned long long)xb), (long long)(1 + rng() % 1000), -(long long)(1 + rng() % 1000), pb, -pb,
+                                     0, 1, -1, 2, -2, 3, 7, -7, INT64_MAX, INT64_MIN, INT64_MIN + 1,
+                                     (long long)(rng() >> 1), (long long)(1ull << 62), -(long long)(1ull << 62)};
+            for (long long dd : dvs) {
+                check_divc(xa, dd);
+                check_divc(INT64_MIN, dd);
+                check_divc(INT64_MAX, dd);
+                check_divc((long long)rng(), dd);
+                check_divc(dd, dd);
+                check_divc((long long)((unsigned long long)dd - 1ull), dd);
+            }
+        }
         // divisors below 2^16: every size, powers of two and their neighbours, the extremes
         const long long d16 = (long long)(1 + (rng() >> (48 + rng() % 16)) % 65535) * ((rng() & 1) ? -1 : 1);
         const long long p16 = (long long)(1ull << (rng() % 16)) + (long long)(rng() % 3) - 1;
@@ -251,6 +279,6 @@ int main(int argc, char** argv) {
     for (double v : {0.7853981633974483, 0.7853981633974482, 0.7853981633974484, 0x1p-26, 0x1p-27, 0x1p20,
                      0x1.fffffffffffffp19, 3.141592653589793, 1.5707963267948966, 1e6, -1e6})
         check_trig(v);
-    for (Counter* c : {&csin, &cd16, &cd32, &cdiv64, &cdiv, &cfloor, &cceil, &cabs, &ccmp, &ci2d, &cd2i, &cf2d, &cd2f, &czero}) c->report();
+    for (Counter* c : {&csin, &cdc, &cd16, &cd32, &cdiv64, &cdiv, &cfloor, &cceil, &cabs, &ccmp, &ci2d, &cd2i, &cf2d, &cd2f, &czero}) c->report();
     return 0;
 }

@@ -79,6 +79,9 @@ def test_plain_vm_filter_program_compiles(nullable):
         [ralgpu.Scalar(s.dtype, s.value, s.is_valid) for s in plan.left_scalars],
         [ralgpu.Scalar(s.dtype, s.value, s.is_valid) for s in plan.right_scalars], compile=True)
     assert spills(log) == 0, log
+    # MOD($0, 7): the remainder by a literal uses the host's precomputed divider
+    import re
+    assert re.search(r"ral_sf_modc\((?!long long)", src) and not re.search(r"ral_modi\((?!ral_i64 a)", src)
 
 
 FILTER_CASES = [

@@ -506,6 +506,30 @@ def test_integer_division_by_zero_and_overflow_are_defined():
         H.assert_columns_equal(g, e, what=f"output {k}", check_null_count=False)
 
 
+@pytest.mark.parametrize("d", [0, 1, -1, 2, -2, 3, 7, -7, 10, 1000, -1000, 65537, 1 << 31, -(1 << 31), (1 << 32) + 1,
+                               1 << 62, -(1 << 62), (1 << 63) - 1, -(1 << 63)])
+def test_integer_division_by_literal(d):
+    """Division and remainder by a literal run with a multiplier precomputed on the host (no
+    division per row); every divisor class (0, +-1, powers of two, INT64_MIN, the largest) against
+    the oracle, on int64, int32 and float64 dividends including the extremes."""
+    n = 4096
+    rng = np.random.default_rng(abs(d) % 1000 + 5)
+    a = rng.integers(np.iinfo(np.int64).min, np.iinfo(np.int64).max, n, dtype=np.int64)
+    a[:8] = [np.iinfo(np.int64).min, np.iinfo(np.int64).max, 0, 1, -1, d if d > np.iinfo(np.int64).min else 0, -7, 7]
+    a[8:1000] >>= rng.integers(0, 63, 992)
+    b = rng.integers(-(1 << 31), 1 << 31, n).astype(np.int32)
+    x = rng.standard_normal(n) * 1e6
+    spec = [(D.GDF_INT64, a, rng.random(n) > 0.1), (D.GDF_INT32, b, None), (D.GDF_FLOAT64, x, None)]
+    J = (D.GDF_INT32, 0)
+    L = (D.GDF_INT64, d)
+    prog = dict(left=[0, 0, 0, 1, 1, 2], right=[-2] * 6, outputs=[3, 4, 5, 6, 7, 8], final=[3, 4, 5, 6, 7, 8],
+                ops=[D.GDF_DIV, D.GDF_MOD, D.GDF_FLOOR_DIV, D.GDF_DIV, D.GDF_MOD, D.GDF_MOD],
+                uops=[D.BLZ_INVALID_UNARY] * 6, lscalars=[J] * 6, rscalars=[L] * 6)
+    dev, ora = H.run_program_both(spec, [D.GDF_INT64] * 6, prog)
+    for k, (g, e) in enumerate(zip(dev, ora)):
+        H.assert_columns_equal(g, e, what=f"output {k}, divisor {d}", check_null_count=False)
+
+
 def test_nan_to_integer_is_int64_min_as_on_the_gpu():
     """MOD converts its operands with cvt.rzi.s64.f64, which turns a NaN into INT64_MIN; the
     oracle does the same (INT64_MIN % k, then stored through the float register)."""

@@ -26,7 +26,7 @@ def test_every_operation_matches_ieee(checker):
     for line in res.strip().splitlines():
         name, n, bad, *first = line.split(" ", 3)
         rows[name] = (int(n), int(bad), first[0] if first else "")
-    for name in ("sincos", "div64_16", "div64_32", "div64", "div", "div_rcp", "floor", "ceil", "fabs", "compare", "i2d", "d2i", "f2d", "d2f", "is_zero"):
+    for name in ("sincos", "divc", "div64_16", "div64_32", "div64", "div", "div_rcp", "floor", "ceil", "fabs", "compare", "i2d", "d2i", "f2d", "d2f", "is_zero"):
         n, bad, first = rows[name]
         assert n >= 1_000_000 and bad == 0, f"{name}: {bad} of {n} differ, first {first}"
 
