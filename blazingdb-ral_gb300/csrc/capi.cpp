@@ -336,6 +336,16 @@ int ral_text_scan_filter(const char* data, int64_t n_bytes, char delimiter, char
     });
 }
 
+int ral_text_scan_filter_host(const char* text, int64_t n_bytes, char delimiter, char line_terminator,
+                              int32_t skip_rows, const int32_t* file_dtypes, int32_t n_file_columns,
+                              const int32_t* projections, int32_t n_projections, const char* filter_query_part,
+                              gdf_column* const* out_columns, gdf_size_type* num_rows_out) {
+    return guarded([&] {
+        return text_scan_filter_host(text, n_bytes, delimiter, line_terminator, skip_rows, file_dtypes, n_file_columns,
+                                     projections, n_projections, filter_query_part, out_columns, num_rows_out);
+    });
+}
+
 int ral_parquet_schema(const uint8_t* file, int64_t n_bytes, int64_t* rows, int32_t* n_columns, int32_t* dtypes,
                        int32_t capacity) {
     return guarded([&] { return parquet_schema(file, n_bytes, rows, n_columns, dtypes, capacity); });

@@ -2004,6 +2004,7 @@ GeneratedKernel generate_text_scan_kernel(const TextScanSpec& t, const Shape& s)
     os << "    const ral_i64 skip = (ral_i64)P.s[5];\n";
     os << "    const char delim = (char)P.s[6];\n";
     os << "    const ral_u64 cap = (ral_u64)P.s[7];\n";
+    os << "    const ral_u64 obase = (ral_u64)P.s[8];\n";
     os << "    ral_u64* const scratch = (ral_u64*)P.s[" << L.scratch << "];\n";
     os << "    ral_u64* const status = scratch + " << text_scan_header(NP) << ";\n";
     for (int q = 0; q < NP; q++) {
@@ -2110,10 +2111,11 @@ GeneratedKernel generate_text_scan_kernel(const TextScanSpec& t, const Shape& s)
     os << "            ral_text_line(ds, ends, nterm, nb, i, s, e);\n";
     os << "            ral_i64 fs[" << f2.size() << "], fe[" << f2.size() << "];\n";
     os << "            ral_fields_all(ds, s, e, delim, fs, fe);\n";
-    os << "            const ral_u64 pos = excl + kA;\n";
-    os << "            const bool put = act && pos < cap;\n";
+    os << "            const ral_u64 pos0 = excl + kA;\n";
+    os << "            const bool put = act && pos0 < cap;\n";
     os << "            if (act && !put) ++over;\n";
-    os << "            const ral_u64 b = excl + k0;\n";
+    os << "            const ral_u64 pos = pos0 + obase;\n";
+    os << "            const ral_u64 b = excl + k0 + obase;\n";
     for (int q = 0; q < NP; q++) {
         os << "            {\n";
         parse("                ", t.dtypes[q], std::to_string(slot_of(f2, t.file_cols[q])), "v", "vw", "act");

@@ -229,8 +229,10 @@ struct TextScanSpec {
 // refused fields, rows past the outputs' capacity; then one status word per chunk.
 inline int64_t text_scan_header(int n_outputs) { return 5 + n_outputs; }
 // Parameter slots before the outputs: lines, text, bytes, terminator positions, terminators,
-// rows skipped, delimiter, output capacity.
-constexpr int kTextScanFixedSlots = 8;
+// rows skipped, delimiter, output capacity, output row base (0 .. 31: kept row j is written at
+// row base + j of the output pointers and masks, which a piece of a longer scan appends into a
+// mask word the rows before it have started).
+constexpr int kTextScanFixedSlots = 9;
 // Lines per look-back chunk of a text scan kernel: J mask words of 32 lines.
 inline int64_t text_scan_chunk_lines(const Shape& s) { return (int64_t)32 * s.J; }
 

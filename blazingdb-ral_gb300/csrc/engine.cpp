@@ -142,6 +142,28 @@ void keep_pool_memory() {
     d.pool_kept = true;
 }
 
+int copy_lane(CopyLane*& out) {
+    int dev = 0;
+    if (int e = check_cuda(cudaGetDevice(&dev), "cudaGetDevice")) return e;
+    static thread_local std::map<int, CopyLane> lanes;
+    CopyLane& l = lanes[dev];
+    if (!l.s && check_cuda(cudaStreamCreateWithFlags(&l.s, cudaStreamNonBlocking), "cudaStreamCreate")) return kCudaError;
+    if (!l.ready && check_cuda(cudaEventCreateWithFlags(&l.ready, cudaEventDisableTiming), "cudaEventCreate"))
+        return kCudaError;
+    out = &l;
+    return kSuccess;
+}
+
+int lane_event(CopyLane& lane, size_t k, cudaEvent_t* ev) {
+    while (lane.events.size() <= k) {
+        cudaEvent_t e = nullptr;
+        if (check_cuda(cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "cudaEventCreate")) return kCudaError;
+        lane.events.push_back(e);
+    }
+    *ev = lane.events[k];
+    return kSuccess;
+}
+
 int blocks_per_sm(const CompiledKernel& k, int threads) {
     int dev = 0;
     cudaGetDevice(&dev);

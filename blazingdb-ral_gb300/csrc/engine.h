@@ -90,6 +90,27 @@ int blocks_per_sm(const CompiledKernel& k, int threads);
 // server are reused rather than mapped again (set once per device for the process).
 void keep_pool_memory();
 
+// The copy stream of the calling thread on the current device, with its events (made once, kept
+// for the thread's life): host-to-device copies issued on it overlap kernels on the caller's stream.
+struct CopyLane {
+    cudaStream_t s = nullptr;
+    cudaEvent_t ready = nullptr;
+    std::vector<cudaEvent_t> events;  // grown on demand by lane_event
+};
+int copy_lane(CopyLane*& out);
+// The lane's k-th event (created on first use).
+int lane_event(CopyLane& lane, size_t k, cudaEvent_t* ev);
+// On every exit of its scope: the calling stream waits for the copies issued on the lane so far,
+// so buffers freed on the calling stream afterwards are no longer being written.
+struct LaneJoin {
+    CopyLane* lane;
+    cudaStream_t st;
+    ~LaneJoin() {
+        cudaEventRecord(lane->ready, lane->s);
+        cudaStreamWaitEvent(st, lane->ready, 0);
+    }
+};
+
 // Parameter block filled in ParamLayout order.
 void fill_scalars(const Program& p, const ParamLayout& L, std::vector<uint64_t>& slots);
 

@@ -51,35 +51,6 @@ int64_t batch_bytes() {
     return v > 0 ? (int64_t)v : ((int64_t)24 << 20);
 }
 
-// The copy stream of a calling thread on one device, with its events (made once, kept for the
-// thread's life).
-struct CopyLane {
-    cudaStream_t s = nullptr;
-    cudaEvent_t ready = nullptr;
-    std::vector<cudaEvent_t> copied;
-};
-
-int copy_lane(int dev, CopyLane*& out) {
-    static thread_local std::map<int, CopyLane> lanes;
-    CopyLane& l = lanes[dev];
-    if (!l.s && check_cuda(cudaStreamCreateWithFlags(&l.s, cudaStreamNonBlocking), "cudaStreamCreate")) return kCudaError;
-    if (!l.ready && check_cuda(cudaEventCreateWithFlags(&l.ready, cudaEventDisableTiming), "cudaEventCreate"))
-        return kCudaError;
-    out = &l;
-    return kSuccess;
-}
-
-// On every exit: the calling stream waits for the copies issued so far, so buffers freed on it
-// afterwards are no longer being written.
-struct LaneJoin {
-    CopyLane* lane;
-    cudaStream_t st;
-    ~LaneJoin() {
-        cudaEventRecord(lane->ready, lane->s);
-        cudaStreamWaitEvent(st, lane->ready, 0);
-    }
-};
-
 // The address kernels read file[0, n) at when it is page-locked (or mapped) host memory of this
 // process, else null.  Both ends are checked: a registered range covers the whole buffer.
 const uint8_t* device_view(const uint8_t* file, int64_t n) {
@@ -228,10 +199,8 @@ int parquet_scan_filter(const uint8_t* file, int64_t n, const int32_t* projectio
 
     cudaStream_t st = cudaStreamPerThread;
     keep_pool_memory();
-    int dev = 0;
-    if (check_cuda(cudaGetDevice(&dev), "cudaGetDevice")) return kCudaError;
     CopyLane* lane = nullptr;
-    if (int e = copy_lane(dev, lane)) return e;
+    if (int e = copy_lane(lane)) return e;
     DevBuf dfile(st), dpages(st), dstatus(st), ditems(st);
     // decoded columns: the outputs themselves without a filter, a frame of temporaries with one
     std::vector<std::unique_ptr<DevBuf>> owned;
@@ -325,13 +294,10 @@ int parquet_scan_filter(const uint8_t* file, int64_t n, const int32_t* projectio
                 return kCudaError;
             a = b + 1;
         }
-        if (batch >= lane->copied.size()) {
-            cudaEvent_t ev = nullptr;
-            if (int e = check_cuda(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming), "cudaEventCreate")) return e;
-            lane->copied.push_back(ev);
-        }
-        if (int e = check_cuda(cudaEventRecord(lane->copied[batch], lane->s), "cudaEventRecord")) return e;
-        if (int e = check_cuda(cudaStreamWaitEvent(st, lane->copied[batch], 0), "cudaStreamWaitEvent")) return e;
+        cudaEvent_t copied = nullptr;
+        if (int e = lane_event(*lane, batch, &copied)) return e;
+        if (int e = check_cuda(cudaEventRecord(copied, lane->s), "cudaEventRecord")) return e;
+        if (int e = check_cuda(cudaStreamWaitEvent(st, copied, 0), "cudaStreamWaitEvent")) return e;
         dp.page_lo = (int32_t)p0;
         dp.page_hi = (int32_t)p1;
         dp.item_lo = pages[p0].item0;

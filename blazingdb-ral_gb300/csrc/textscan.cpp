@@ -12,6 +12,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cstdlib>
 #include <cstring>
 #include <map>
 #include <memory>
@@ -238,39 +239,40 @@ int text_scan_source(const int32_t* file_dtypes, int32_t n_file, const int32_t* 
     return kSuccess;
 }
 
-int text_scan_filter(const char* data, int64_t n, char delim, char term, int32_t skip_rows, const int32_t* file_dtypes,
-                     int32_t n_file, const int32_t* projections, int32_t n_proj, const char* filter_q,
-                     gdf_column* const* outs, gdf_size_type* n_out) {
-    if (n < 0 || skip_rows < 0 || (n > 0 && !data) || !outs || !n_out) return set_error(kInvalidArgument, "bad argument");
-    if (delim == term) return set_error(kInvalidArgument, "the delimiter and the line terminator are the same byte");
-    std::vector<gdf_dtype> dtypes;
-    std::vector<int> file_cols;
-    if (int e = scan_columns(file_dtypes, n_file, projections, n_proj, dtypes, file_cols)) return e;
-    int64_t cap = INT64_MAX;
-    for (int q = 0; q < n_proj; q++) {
+namespace {
+
+// Checks the out columns against the scanned dtypes; their smallest size is the capacity.
+int check_outs(const std::vector<gdf_dtype>& dtypes, gdf_column* const* outs, int64_t* cap) {
+    *cap = INT64_MAX;
+    for (size_t q = 0; q < dtypes.size(); q++) {
         gdf_column* o = outs[q];
         if (!o) return set_error(kInvalidArgument, "null out column");
         if (o->dtype != dtypes[q]) return set_error(kInvalidArgument, "out column " + std::to_string(q) + " has the wrong dtype");
         if (!o->valid || ((uintptr_t)o->valid & 3)) return set_error(kInvalidArgument, "out columns need a 4-byte aligned mask");
         if (o->size > 0 && !o->data) return set_error(kInvalidArgument, "out column without data");
-        cap = std::min<int64_t>(cap, o->size);
+        *cap = std::min<int64_t>(*cap, o->size);
     }
-    const PreparedScan* ps = nullptr;
-    if (int e = prepare_scan(dtypes, file_cols, filter_q, &ps)) return e;
-    const int NP = n_proj;
-    cudaStream_t st = cudaStreamPerThread;
-    keep_pool_memory();
+    return kSuccess;
+}
+
+// One scan launch over data[0, n) (device memory): its kept rows go to rows row0 .. of the
+// outputs (whose masks are zeroed), at most cap of them; adds the rows kept and each output's
+// valid rows to kept / valid.  Synchronous on st.
+int scan_piece(const PreparedScan& ps, const char* data, int64_t n, char delim, char term, int32_t skip_rows,
+               gdf_column* const* outs, int NP, int64_t row0, int64_t cap, cudaStream_t st, int64_t& kept,
+               std::vector<int64_t>& valid) {
     LineIndex li(st);
     if (int e = build_line_index(data, n, term, st, li)) return e;
-    const GeneratedKernel& gk = ps->gk;
+    const GeneratedKernel& gk = ps.gk;
     const ParamLayout& L = gk.layout;
     const int64_t chunks = (li.lines + text_scan_chunk_lines(gk.shape) - 1) / text_scan_chunk_lines(gk.shape);
+    if (chunks == 0) return kSuccess;
     const int64_t header = text_scan_header(NP);
     StreamBuffer scratch(st);
     if (int e = scratch.alloc((size_t)(header + chunks) * 8)) return e;
     cudaMemsetAsync(scratch.p, 0, (size_t)(header + chunks) * 8, st);
-    for (int q = 0; q < NP; q++)
-        if (cap > 0) cudaMemsetAsync(outs[q]->valid, 0, (size_t)((cap + 31) / 32) * 4, st);
+    // the outputs seen from the word holding row0: row (row0 & 31) + j is kept row j
+    const int64_t obase = row0 & 31;
     std::vector<uint64_t> slots(L.total, 0);
     slots[0] = (uint64_t)li.lines;
     slots[1] = (uint64_t)(uintptr_t)data;
@@ -280,22 +282,25 @@ int text_scan_filter(const char* data, int64_t n, char delim, char term, int32_t
     slots[5] = (uint64_t)skip_rows;
     slots[6] = (uint64_t)(unsigned char)delim;
     slots[7] = (uint64_t)std::max<int64_t>(cap, 0);
+    slots[8] = (uint64_t)obase;
     for (int q = 0; q < NP; q++) {
-        slots[L.out_data + q] = (uint64_t)(uintptr_t)outs[q]->data;
-        slots[L.out_valid + q] = (uint64_t)(uintptr_t)outs[q]->valid;
+        const int64_t w = gdf_dtype_size(outs[q]->dtype);
+        slots[L.out_data + q] = (uint64_t)(uintptr_t)((char*)outs[q]->data + (row0 - obase) * w);
+        slots[L.out_valid + q] = (uint64_t)(uintptr_t)((uint32_t*)outs[q]->valid + (row0 >> 5));
     }
     slots[L.scratch] = (uint64_t)(uintptr_t)scratch.p;
-    if (ps->have_pred) fill_scalars(ps->pred, L, slots);
-    unsigned long long h[70];
-    if (chunks > 0) {
-        const int grid = launch_blocks(*ps->k, gk.shape.threads, text_scan_chunk_lines(gk.shape) * (gk.shape.threads / 32),
-                                       li.lines);
-        void* args[] = {slots.data()};
-        if (int e = check_cuda(cudaLaunchKernel((const void*)ps->k->kernel, dim3(grid), dim3(gk.shape.threads), args, 0, st),
-                               "launch of the text scan kernel"))
-            return e;
-        note_launch();
-    }
+    if (ps.have_pred) fill_scalars(ps.pred, L, slots);
+    // the header comes back into page-locked memory: a copy into pageable memory would wait
+    // behind the host-to-device copies of a streamed scan
+    thread_local unsigned long long* h = nullptr;
+    if (!h && check_cuda(cudaMallocHost((void**)&h, 8 * 72), "cudaMallocHost")) return kCudaError;
+    const int grid = launch_blocks(*ps.k, gk.shape.threads, text_scan_chunk_lines(gk.shape) * (gk.shape.threads / 32),
+                                   li.lines);
+    void* args[] = {slots.data()};
+    if (int e = check_cuda(cudaLaunchKernel((const void*)ps.k->kernel, dim3(grid), dim3(gk.shape.threads), args, 0, st),
+                           "launch of the text scan kernel"))
+        return e;
+    note_launch();
     if (int e = check_cuda(cudaMemcpyAsync(h, scratch.p, (size_t)header * 8, cudaMemcpyDeviceToHost, st), "cudaMemcpyAsync"))
         return e;
     if (int e = check_cuda(cudaStreamSynchronize(st), "text scan kernel")) return e;
@@ -304,12 +309,140 @@ int text_scan_filter(const char* data, int64_t n, char delim, char term, int32_t
         return set_error(kUnsupported, std::to_string(h[3 + NP]) + " decimal fields outside the exactly rounded range "
                                        "(more than 19 significant digits, above 2^53 or a power of ten beyond 1e22)");
     if (h[4 + NP]) return set_error(kInvalidArgument, "the out columns hold fewer rows than the scan keeps");
-    const int64_t kept = chunks > 0 ? (int64_t)h[2] : 0;
+    kept += (int64_t)h[2];
+    for (int q = 0; q < NP; q++) valid[q] += (int64_t)h[3 + q];
+    return kSuccess;
+}
+
+void set_outputs(gdf_column* const* outs, int NP, int64_t kept, const std::vector<int64_t>& valid, gdf_size_type* n_out) {
     for (int q = 0; q < NP; q++) {
         outs[q]->size = (gdf_size_type)kept;
-        outs[q]->null_count = (gdf_size_type)(kept - (int64_t)h[3 + q]);
+        outs[q]->null_count = (gdf_size_type)(kept - valid[q]);
     }
     *n_out = (gdf_size_type)kept;
+}
+
+// Text handed over in host memory goes to the device in pieces of about this many bytes (whole
+// lines; RAL_SCAN_PIECE_BYTES overrides), each scanned while the next ones are copied.
+int64_t piece_bytes() {
+    const char* e = std::getenv("RAL_SCAN_PIECE_BYTES");
+    const long long v = e ? std::atoll(e) : 0;
+    return v > 0 ? (int64_t)v : ((int64_t)64 << 20);
+}
+
+}  // namespace
+
+int text_scan_filter(const char* data, int64_t n, char delim, char term, int32_t skip_rows, const int32_t* file_dtypes,
+                     int32_t n_file, const int32_t* projections, int32_t n_proj, const char* filter_q,
+                     gdf_column* const* outs, gdf_size_type* n_out) {
+    if (n < 0 || skip_rows < 0 || (n > 0 && !data) || !outs || !n_out) return set_error(kInvalidArgument, "bad argument");
+    if (delim == term) return set_error(kInvalidArgument, "the delimiter and the line terminator are the same byte");
+    std::vector<gdf_dtype> dtypes;
+    std::vector<int> file_cols;
+    if (int e = scan_columns(file_dtypes, n_file, projections, n_proj, dtypes, file_cols)) return e;
+    int64_t cap = 0;
+    if (int e = check_outs(dtypes, outs, &cap)) return e;
+    const PreparedScan* ps = nullptr;
+    if (int e = prepare_scan(dtypes, file_cols, filter_q, &ps)) return e;
+    const int NP = n_proj;
+    cudaStream_t st = cudaStreamPerThread;
+    keep_pool_memory();
+    for (int q = 0; q < NP; q++)
+        if (cap > 0) cudaMemsetAsync(outs[q]->valid, 0, (size_t)((cap + 31) / 32) * 4, st);
+    int64_t kept = 0;
+    std::vector<int64_t> valid(NP, 0);
+    if (int e = scan_piece(*ps, data, n, delim, term, skip_rows, outs, NP, 0, cap, st, kept, valid)) return e;
+    set_outputs(outs, NP, kept, valid, n_out);
+    return kSuccess;
+}
+
+int text_scan_filter_host(const char* text, int64_t n, char delim, char term, int32_t skip_rows,
+                          const int32_t* file_dtypes, int32_t n_file, const int32_t* projections, int32_t n_proj,
+                          const char* filter_q, gdf_column* const* outs, gdf_size_type* n_out) {
+    if (n < 0 || skip_rows < 0 || (n > 0 && !text) || !outs || !n_out) return set_error(kInvalidArgument, "bad argument");
+    if (delim == term) return set_error(kInvalidArgument, "the delimiter and the line terminator are the same byte");
+    std::vector<gdf_dtype> dtypes;
+    std::vector<int> file_cols;
+    if (int e = scan_columns(file_dtypes, n_file, projections, n_proj, dtypes, file_cols)) return e;
+    int64_t cap = 0;
+    if (int e = check_outs(dtypes, outs, &cap)) return e;
+    const PreparedScan* ps = nullptr;
+    if (int e = prepare_scan(dtypes, file_cols, filter_q, &ps)) return e;
+    const int NP = n_proj;
+    // the skipped lines are passed over here: every piece starts at a line
+    int64_t off = 0;
+    for (int32_t k = 0; k < skip_rows && off < n; k++) {
+        const void* t = std::memchr(text + off, term, (size_t)(n - off));
+        off = t ? (int64_t)((const char*)t - text) + 1 : n;
+    }
+    // pieces of whole lines: each ends just after a terminator (the last at the end of the text).
+    // A piece is copied from the 256-byte boundary at or before its first line (copies from
+    // unaligned host addresses run slower, and the kernels read aligned text 16 bytes at a time);
+    // the lines before its first one there all end inside it and are skipped by the scan.
+    const int64_t P = piece_bytes();
+    struct Piece {
+        int64_t from, to, skip;
+    };
+    std::vector<Piece> pieces;
+    int64_t biggest = 0;
+    for (int64_t s0 = off; s0 < n;) {
+        int64_t e0 = std::min(n, s0 + P);
+        if (e0 < n) {
+            const void* t = std::memchr(text + e0 - 1, term, (size_t)(n - (e0 - 1)));
+            e0 = t ? (int64_t)((const char*)t - text) + 1 : n;
+        }
+        const int64_t a = s0 & ~(int64_t)255;
+        int64_t skip = 0;
+        for (int64_t p = a; p < s0; p++) skip += text[p] == term;
+        pieces.push_back({a, e0, skip});
+        biggest = std::max(biggest, e0 - a);
+        s0 = e0;
+    }
+    cudaStream_t st = cudaStreamPerThread;
+    keep_pool_memory();
+    for (int q = 0; q < NP; q++)
+        if (cap > 0) cudaMemsetAsync(outs[q]->valid, 0, (size_t)((cap + 31) / 32) * 4, st);
+    int64_t kept = 0;
+    std::vector<int64_t> valid(NP, 0);
+    if (pieces.empty()) {
+        set_outputs(outs, NP, kept, valid, n_out);
+        return kSuccess;
+    }
+    // three piece buffers: two copies run ahead of the scan
+    const int NB = (int)std::min<size_t>(3, pieces.size());
+    std::vector<std::unique_ptr<StreamBuffer>> bufs;
+    for (int b = 0; b < NB; b++) {
+        bufs.emplace_back(new StreamBuffer(st));
+        if (int e = bufs.back()->alloc((size_t)biggest)) return e;
+    }
+    CopyLane* lane = nullptr;
+    if (int e = copy_lane(lane)) return e;
+    if (int e = check_cuda(cudaEventRecord(lane->ready, st), "cudaEventRecord")) return e;
+    if (int e = check_cuda(cudaStreamWaitEvent(lane->s, lane->ready, 0), "cudaStreamWaitEvent")) return e;
+    LaneJoin join{lane, st};  // before the buffers are freed, this stream waits for every copy
+    auto copy = [&](size_t k) -> int {
+        const int64_t s0 = pieces[k].from, bytes = pieces[k].to - pieces[k].from;
+        if (int e = check_cuda(cudaMemcpyAsync(bufs[k % NB]->p, text + s0, (size_t)bytes, cudaMemcpyHostToDevice, lane->s),
+                               "cudaMemcpyAsync"))
+            return e;
+        cudaEvent_t ev = nullptr;
+        if (int e = lane_event(*lane, k, &ev)) return e;
+        return check_cuda(cudaEventRecord(ev, lane->s), "cudaEventRecord");
+    };
+    for (size_t k = 0; k + 1 < (size_t)NB; k++)
+        if (int e = copy(k)) return e;
+    for (size_t k = 0; k < pieces.size(); k++) {
+        // the buffer of piece k + NB - 1 held piece k - 1, whose scan has finished
+        if (k + NB - 1 < pieces.size())
+            if (int e = copy(k + NB - 1)) return e;
+        cudaEvent_t ev = nullptr;
+        if (int e = lane_event(*lane, k, &ev)) return e;
+        if (int e = check_cuda(cudaStreamWaitEvent(st, ev, 0), "cudaStreamWaitEvent")) return e;
+        if (int e = scan_piece(*ps, (const char*)bufs[k % NB]->p, pieces[k].to - pieces[k].from, delim, term,
+                               (int32_t)pieces[k].skip, outs, NP, kept, cap - kept, st, kept, valid))
+            return e;
+    }
+    set_outputs(outs, NP, kept, valid, n_out);
     return kSuccess;
 }
 

@@ -17,6 +17,11 @@ int text_scan_rows(const char* data, int64_t n, char term, int32_t skip_rows, in
 int text_scan_filter(const char* data, int64_t n, char delim, char term, int32_t skip_rows, const int32_t* file_dtypes,
                      int32_t n_file, const int32_t* projections, int32_t n_proj, const char* filter_q,
                      gdf_column* const* outs, gdf_size_type* n_out);
+// The same over text in host memory, copied in pieces of whole lines that are scanned while the
+// next pieces are copied; see ral_text_scan_filter_host in ral_c.h.
+int text_scan_filter_host(const char* text, int64_t n, char delim, char term, int32_t skip_rows,
+                          const int32_t* file_dtypes, int32_t n_file, const int32_t* projections, int32_t n_proj,
+                          const char* filter_q, gdf_column* const* outs, gdf_size_type* n_out);
 
 // Generated source (and optionally an NVRTC-only compile) of the scan kernel; needs no GPU.
 int text_scan_source(const int32_t* file_dtypes, int32_t n_file, const int32_t* projections, int32_t n_proj,

@@ -58,6 +58,8 @@ _SIGS = {
     "ral_text_scan_rows": (C.c_int, [C.c_void_p, C.c_int64, C.c_char, C.c_int32, C.POINTER(C.c_int64)]),
     "ral_text_scan_filter": (C.c_int, [C.c_void_p, C.c_int64, C.c_char, C.c_char, C.c_int32, I32P, C.c_int32, I32P,
                                        C.c_int32, C.c_char_p, C.c_void_p, C.POINTER(C.c_int32)]),
+    "ral_text_scan_filter_host": (C.c_int, [C.c_void_p, C.c_int64, C.c_char, C.c_char, C.c_int32, I32P, C.c_int32,
+                                            I32P, C.c_int32, C.c_char_p, C.c_void_p, C.POINTER(C.c_int32)]),
     "ral_debug_text_scan_source": (C.c_int, [I32P, C.c_int32, I32P, C.c_int32, C.c_char_p, C.c_int32, C.c_char_p,
                                              C.c_int64, C.c_char_p, C.c_int64]),
     "ral_parquet_schema": (C.c_int, [C.c_void_p, C.c_int64, C.POINTER(C.c_int64), C.POINTER(C.c_int32), I32P,
@@ -397,20 +399,34 @@ def text_scan_rows(data, line_terminator: bytes = b"\n", skip_rows: int = 0) -> 
 
 
 def text_scan_filter(data, file_dtypes, projections, filter_query_part: Optional[str] = None, delimiter: bytes = b"|",
-                     line_terminator: bytes = b"\n", skip_rows: int = 0, capacity: Optional[int] = None) -> List[Column]:
+                     line_terminator: bytes = b"\n", skip_rows: int = 0, capacity: Optional[int] = None,
+                     from_host: bool = False) -> List[Column]:
     """BindableTableScan over delimited text (projects = projections) fused with its LogicalFilter
-    (None: the scan alone): the kept rows of the projected columns, every column with a mask."""
-    t = _text_device(data)
-    if capacity is None:
-        capacity = text_scan_rows(t, line_terminator, skip_rows)
+    (None: the scan alone): the kept rows of the projected columns, every column with a mask.
+    from_host=True passes the text in host memory (ral_text_scan_filter_host: copied in pieces,
+    each scanned while the next is copied); otherwise it is copied to the device first."""
+    if from_host:
+        import torch
+        if isinstance(data, torch.Tensor):
+            h = data
+        else:
+            b = bytes(data)
+            h = torch.frombuffer(bytearray(b), dtype=torch.uint8) if b else torch.zeros(0, dtype=torch.uint8)
+        if capacity is None:
+            capacity = text_scan_rows(h.to("cuda"), line_terminator, skip_rows)
+        t, fn = h, lib().ral_text_scan_filter_host
+    else:
+        t = _text_device(data)
+        if capacity is None:
+            capacity = text_scan_rows(t, line_terminator, skip_rows)
+        fn = lib().ral_text_scan_filter
     outs = [Column.empty(file_dtypes[c], capacity, with_valid=True) for c in projections]
     oa, os_ = _colarray(outs)
     n = C.c_int32(0)
     fd, pr = _i32(file_dtypes), _i32(projections)
-    _check(lib().ral_text_scan_filter(C.c_void_p(t.data_ptr() if t.numel() else 0), t.numel(), delimiter,
-                                      line_terminator, skip_rows, _p32(fd), len(fd), _p32(pr), len(pr),
-                                      filter_query_part.encode() if filter_query_part else None,
-                                      C.cast(oa, C.c_void_p), C.byref(n)))
+    _check(fn(C.c_void_p(t.data_ptr() if t.numel() else 0), t.numel(), delimiter, line_terminator, skip_rows, _p32(fd),
+              len(fd), _p32(pr), len(pr), filter_query_part.encode() if filter_query_part else None,
+              C.cast(oa, C.c_void_p), C.byref(n)))
     for o, st in zip(outs, os_):
         o.sync_from_c(st)
     return outs

@@ -265,13 +265,22 @@ int ral_text_scan_filter(const char *data, int64_t n_bytes, char delimiter, char
                          const int32_t *file_dtypes, int32_t n_file_columns, const int32_t *projections,
                          int32_t n_projections, const char *filter_query_part, gdf_column *const *out_columns,
                          gdf_size_type *num_rows_out);
+/* The same with `text` in host memory (page-locked for full speed): the text goes to the device in
+ * pieces of whole lines (64 MiB by default), each scanned while the next ones are copied, the kept
+ * rows appended to out_columns in order.  Same arguments, results and errors. */
+int ral_text_scan_filter_host(const char *text, int64_t n_bytes, char delimiter, char line_terminator,
+                              int32_t skip_rows, const int32_t *file_dtypes, int32_t n_file_columns,
+                              const int32_t *projections, int32_t n_projections, const char *filter_query_part,
+                              gdf_column *const *out_columns, gdf_size_type *num_rows_out);
 
 /*
  * The same fusion over a Parquet file — a BindableTableScan of a Parquet table (parquet_parser::parse,
  * src/io/data_parser/ParquetParser.cpp:36-90, cudf's Parquet reader) followed by its LogicalFilter.
- * `file` holds the whole file (n_bytes) in host memory; the projected leaves' column chunks are copied
- * to the device (page-locked memory makes the copies faster), every data page is decoded by one
- * kernel, and the fused filter kernel filters the decoded columns.  ral_parquet_schema gives the row count, the leaf count and the gdf dtype each
+ * `file` holds the whole file (n_bytes) in host memory.  In page-locked memory the decode kernels read
+ * the projected pages in place over the host link; otherwise the projected leaves' column chunks
+ * are copied in, in batches decoded while the next batch is copied.  A levels kernel decodes the
+ * definition levels of optional leaves, a values kernel every page's values in 8192-row items, and
+ * the fused filter kernel filters the decoded columns.  ral_parquet_schema gives the row count, the leaf count and the gdf dtype each
  * leaf scans as (GDF_invalid where unsupported; dtypes: host array of `capacity` entries).
  * Supported: flat schemas; INT32 (DATE as DATE32), INT64 (TIMESTAMP_MILLIS as DATE64), FLOAT,
  * DOUBLE; required and optional leaves; uncompressed v1 data pages of PLAIN values with RLE /

@@ -15,12 +15,15 @@ pytestmark = pytest.mark.gpu
 
 
 def _check(text, dtypes, proj, fq, **kw):
+    """Both ways in: text already on the device, and text in host memory streamed in pieces."""
     exp = T.scan_filter(text, dtypes, proj, fq, **kw)
-    got = R.text_scan_filter(text, dtypes, proj, fq, **kw)
-    assert len(got) == len(exp)
-    for k, (g, e) in enumerate(zip(got, exp)):
+    for k, e in enumerate(exp):
         O.update_null_count(e)
-        H.assert_columns_equal(g, e, what=f"column {k} ({fq})")
+    for from_host in (False, True):
+        got = R.text_scan_filter(text, dtypes, proj, fq, from_host=from_host, **kw)
+        assert len(got) == len(exp)
+        for k, (g, e) in enumerate(zip(got, exp)):
+            H.assert_columns_equal(g, e, what=f"column {k} ({fq}, from host {from_host})")
     return got
 
 
@@ -36,6 +39,16 @@ FILTERS = [None,
 def test_varied_table_every_column(fq):
     text = W.text_table_varied(3000, seed=21)
     _check(text, W.TEXT_DTYPES, list(range(8)), fq, skip_rows=1)
+
+
+@pytest.mark.parametrize("piece", ["1", "100", "4097", "65536"])
+def test_host_text_in_small_pieces(monkeypatch, piece):
+    """Host text cut into pieces of one line up to many: each piece's kept rows are appended at a
+    row that is not a multiple of 32 (the mask word shared with the piece before)."""
+    monkeypatch.setenv("RAL_SCAN_PIECE_BYTES", piece)
+    text = W.text_table_varied(3000, seed=33)
+    _check(text, W.TEXT_DTYPES, list(range(8)), FILTERS[4], skip_rows=1)
+    _check(text, W.TEXT_DTYPES, [6, 0, 3], None, skip_rows=5)
 
 
 def test_projection_order_and_repeats():
@@ -75,14 +88,16 @@ def test_refused_decimal_fails_the_call():
     text = b"1|2.5\n2|0.12345678901234567891\n3|4\n"
     with pytest.raises(T.ScanRefused):
         T.scan_filter(text, [D.GDF_INT32, D.GDF_FLOAT64], [0, 1], None)
-    with pytest.raises(R.RalError):
-        R.text_scan_filter(text, [D.GDF_INT32, D.GDF_FLOAT64], [0, 1])
+    for from_host in (False, True):
+        with pytest.raises(R.RalError):
+            R.text_scan_filter(text, [D.GDF_INT32, D.GDF_FLOAT64], [0, 1], from_host=from_host)
     # a refused field in a row the filter drops, in a column the condition does not read: no error
     _check(text, [D.GDF_INT32, D.GDF_FLOAT64], [0, 1], "LogicalFilter(condition=[<>($0, 2)])")
 
 
 def test_capacity_below_the_kept_rows_fails():
     text = b"1\n2\n3\n4\n"
-    with pytest.raises(R.RalError):
-        R.text_scan_filter(text, [D.GDF_INT32], [0], capacity=2)
+    for from_host in (False, True):
+        with pytest.raises(R.RalError):
+            R.text_scan_filter(text, [D.GDF_INT32], [0], capacity=2, from_host=from_host)
     assert R.text_scan_rows(text) == 4 and R.text_scan_rows(text, skip_rows=3) == 1
