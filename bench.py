@@ -1202,9 +1202,13 @@ def measure_workload(args, workload, n, selectivity, device, world, sampler, e2e
             else:
                 out["e2e"] = filter_e2e(ctx, max(2, min(args.steps, 3)))
             link = host_link_peak()
-            moved = out["e2e"]["h2d_bytes_per_step"] + out["e2e"]["d2h_bytes_per_step"]
-            out["e2e"]["host_link"] = dict(link, e2e_gbs=moved / (out["e2e"]["ms_per_step"] / 1e3) / 1e9)
-            out["e2e"]["host_link"]["frac_of_link"] = out["e2e"]["host_link"]["e2e_gbs"] / link["both_gbs"]
+            bi, bo = out["e2e"]["h2d_bytes_per_step"], out["e2e"]["d2h_bytes_per_step"]
+            out["e2e"]["host_link"] = dict(link, e2e_gbs=(bi + bo) / (out["e2e"]["ms_per_step"] / 1e3) / 1e9)
+            # the copies alone at the measured rates: each direction at its own rate, both at once
+            # no faster than the two-stream figure
+            floor_ms = max(bi / (link["h2d_gbs"] * 1e9), bo / (link["d2h_gbs"] * 1e9), (bi + bo) / (link["both_gbs"] * 1e9)) * 1e3
+            out["e2e"]["host_link"]["copy_floor_ms"] = floor_ms
+            out["e2e"]["host_link"]["frac_of_link"] = floor_ms / out["e2e"]["ms_per_step"]
         # the device outputs (the e2e leg rewrote them with the same bits) against the oracle
         if parity and not args.skip_parity:
             out["parity"] = (gather_parity(ctx) if workload == "gather" else

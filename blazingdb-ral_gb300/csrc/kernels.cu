@@ -773,21 +773,42 @@ __global__ void __launch_bounds__(256) parquet_values_kernel(const __grid_consta
     const int rel1 = min(rel0 + kParquetItemRows, pg.rows);
     const int64_t lo = pg.optional ? 4 + (int64_t)pg.levels : 0;
     const uint8_t* const vals = P.file + pg.data + lo;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     if (!pg.optional) {
-        // every row has its value (the page's length is checked on the host)
-        int r = rel0 + (int)threadIdx.x;
-        for (; r + 768 < rel1; r += 1024) {
-            const unsigned long long x0 = ral_pq_value(vals, r, w), x1 = ral_pq_value(vals, r + 256, w);
-            const unsigned long long x2 = ral_pq_value(vals, r + 512, w), x3 = ral_pq_value(vals, r + 768, w);
-            ral_pq_store(col.data, pg.row_start + r, w, x0);
-            ral_pq_store(col.data, pg.row_start + r + 256, w, x1);
-            ral_pq_store(col.data, pg.row_start + r + 512, w, x2);
-            ral_pq_store(col.data, pg.row_start + r + 768, w, x3);
+        // Every row has its value (the page's length is checked on the host).  The lanes of a
+        // warp take consecutive rows: each loads the aligned word where its value starts and
+        // takes the next word from the lane after it (the last lane of the run loads it), so a
+        // warp reads one contiguous aligned span whatever the values' alignment.
+        const uintptr_t va = (uintptr_t)vals;
+        if (w == 8) {
+            const int sh = (int)(va & 7) * 8;
+            const unsigned long long* q = reinterpret_cast<const unsigned long long*>(va - (va & 7));
+            unsigned long long* out = reinterpret_cast<unsigned long long*>(col.data) + pg.row_start;
+#pragma unroll 4
+            for (int r0 = rel0 + 32 * warp; r0 < rel1; r0 += 256) {
+                const int r = r0 + lane;
+                const bool in = r < rel1;
+                const unsigned long long lo = in ? q[r] : 0ull;
+                unsigned long long nx = __shfl_down_sync(0xffffffffu, lo, 1);
+                if (sh && in && (lane == 31 || r + 1 >= rel1)) nx = q[r + 1];
+                if (in) out[r] = sh ? (lo >> sh) | (nx << (64 - sh)) : lo;
+            }
+        } else {
+            const int sh = (int)(va & 3) * 8;
+            const ral_u32* q = reinterpret_cast<const ral_u32*>(va - (va & 3));
+            ral_u32* out = reinterpret_cast<ral_u32*>(col.data) + pg.row_start;
+#pragma unroll 4
+            for (int r0 = rel0 + 32 * warp; r0 < rel1; r0 += 256) {
+                const int r = r0 + lane;
+                const bool in = r < rel1;
+                const ral_u32 lo = in ? q[r] : 0u;
+                ral_u32 nx = __shfl_down_sync(0xffffffffu, lo, 1);
+                if (sh && in && (lane == 31 || r + 1 >= rel1)) nx = q[r + 1];
+                if (in) out[r] = sh ? (lo >> sh) | (nx << (32 - sh)) : lo;
+            }
         }
-        for (; r < rel1; r += 256) ral_pq_store(col.data, pg.row_start + r, w, ral_pq_value(vals, r, w));
         return;
     }
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int64_t nvals = (pg.data_bytes - lo) / w;
     // this item's validity words, page-relative (rows of the next page masked off)
     ral_u32 X = 0;
