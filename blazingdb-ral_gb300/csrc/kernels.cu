@@ -578,7 +578,7 @@ __global__ void __launch_bounds__(256) parquet_levels_kernel(const __grid_consta
     const ParquetPage pg = P.pages[P.page_lo + blockIdx.x];
     if (!pg.optional || pg.rows <= 0) return;
     const ParquetColumnOut col = P.out[pg.column];
-    const uint8_t* const lev = P.file + pg.data + 4;
+    const uint8_t* const lev = (const uint8_t*)pg.data + pg.lev_off;
     const int lev_bytes = pg.levels;
     const int off = (int)((uintptr_t)lev & 3);
     const int staged = min(lev_bytes, kPqStage);
@@ -739,6 +739,7 @@ __global__ void __launch_bounds__(256) parquet_levels_kernel(const __grid_consta
     if (threadIdx.x == 0) {
         if (s_bad) {
             atomicAdd(P.status, 1ull);
+            P.page_present[P.page_lo + blockIdx.x] = 0u;  // no indices are read for this page
             return;
         }
         // item counts -> each item's first value index; the page's values must cover them
@@ -749,8 +750,11 @@ __global__ void __launch_bounds__(256) parquet_levels_kernel(const __grid_consta
             P.item_base[pg.item0 + i] = run;
             run += c;
         }
-        const int64_t nvals = (pg.data_bytes - 4 - (int64_t)lev_bytes) / col.width;
-        if ((int64_t)run > nvals) atomicAdd(P.status, 1ull);
+        // PLAIN values must cover the present rows (a dictionary page's indices are checked by
+        // their own kernel)
+        const int64_t nvals = (pg.data_bytes - (int64_t)pg.values_off) / col.width;
+        if (pg.dict_count == 0 && (int64_t)run > nvals) atomicAdd(P.status, 1ull);
+        P.page_present[P.page_lo + blockIdx.x] = run;
         if (run) atomicAdd(P.status + 1 + pg.column, (unsigned long long)run);
     }
 }
@@ -771,9 +775,19 @@ __global__ void __launch_bounds__(256) parquet_values_kernel(const __grid_consta
     const int w = col.width;
     const int rel0 = (item - pg.item0) * kParquetItemRows;
     const int rel1 = min(rel0 + kParquetItemRows, pg.rows);
-    const int64_t lo = pg.optional ? 4 + (int64_t)pg.levels : 0;
-    const uint8_t* const vals = P.file + pg.data + lo;
+    const int64_t lo = pg.values_off;
+    const uint8_t* const vals = (const uint8_t*)pg.data + lo;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (pg.dict_count > 0 && !pg.optional) {
+        // a dictionary-encoded required page: row r's entry is idx[idx0 + r] (checked in range)
+        const uint8_t* const dict = (const uint8_t*)pg.dict;
+        const uint32_t* const ix = P.idx + pg.idx0;
+        for (int r = rel0 + (int)threadIdx.x; r < rel1; r += 256) {
+            const uint32_t k = ix[r];  // in range unless the page was malformed (then reported)
+            ral_pq_store(col.data, pg.row_start + r, w, k < (uint32_t)pg.dict_count ? ral_pq_value(dict, k, w) : 0ull);
+        }
+        return;
+    }
     if (!pg.optional) {
         // Every row has its value (the page's length is checked on the host).  The lanes of a
         // warp take consecutive rows: each loads the aligned word where its value starts and
@@ -809,7 +823,10 @@ __global__ void __launch_bounds__(256) parquet_values_kernel(const __grid_consta
         }
         return;
     }
-    const int64_t nvals = (pg.data_bytes - lo) / w;
+    // PLAIN values, or a dictionary's entries through the present rows' indices
+    const int64_t nvals = pg.dict_count > 0 ? (int64_t)0x7fffffffffffffffll : (pg.data_bytes - lo) / w;
+    const uint8_t* const dict = (const uint8_t*)pg.dict;
+    const uint32_t* const ix = P.idx + pg.idx0;
     // this item's validity words, page-relative (rows of the next page masked off)
     ral_u32 X = 0;
     {
@@ -847,10 +864,294 @@ __global__ void __launch_bounds__(256) parquet_values_kernel(const __grid_consta
         unsigned long long x = 0;
         if ((Xw >> lane) & 1u) {
             const int64_t vi = base + s_base[t] + __popc(Xw & ((1u << lane) - 1u));
-            if (vi < nvals) x = ral_pq_value(vals, vi, w);
+            if (pg.dict_count > 0) {
+                const uint32_t k = ix[vi];
+                if (k < (uint32_t)pg.dict_count) x = ral_pq_value(dict, k, w);
+            }
+            else if (vi < nvals) x = ral_pq_value(vals, vi, w);
         }
         ral_pq_store(col.data, pg.row_start + r, w, x);
     }
+}
+
+// One block per dictionary-encoded page: after the bit width byte, the present rows' indices in
+// the RLE / bit-packed hybrid (a run header varint h: h odd -> (h >> 1) groups of 8 values of the
+// bit width, packed from the low bits; h even -> h >> 1 repeats of the next ceil(width / 8) bytes).
+// Thread 0 walks the run headers into a table (a batch of up to kPqRuns runs at a time), then the
+// block writes the batch's indices, checking each against the dictionary's size.
+__global__ void __launch_bounds__(256) parquet_dict_index_kernel(const __grid_constant__ ParquetDecodeParams P) {
+    __shared__ int s_row[kPqRuns + 1];
+    __shared__ long long s_info[kPqRuns];  // bit-packed: byte offset of the run's values; RLE: the value
+    __shared__ unsigned char s_kind[kPqRuns];
+    __shared__ int s_n, s_bad, s_done;
+    __shared__ long long s_pos;
+    const int p = P.page_lo + (int)blockIdx.x;
+    const ParquetPage pg = P.pages[p];
+    if (pg.dict_count <= 0 || pg.rows <= 0) return;
+    const int n_idx = pg.optional ? (int)min((unsigned)pg.rows, P.page_present[p]) : pg.rows;
+    const uint8_t* const sv = (const uint8_t*)pg.data + pg.values_off;
+    const long long sbytes = (long long)pg.data_bytes - pg.values_off;
+    uint32_t* const ix = P.idx + pg.idx0;
+    if (n_idx <= 0) return;
+    if (sbytes < 1 || sv[0] > 32) {
+        if (threadIdx.x == 0) atomicAdd(P.status, 1ull);
+        return;
+    }
+    const int bw = sv[0];
+    const int vbytes = (bw + 7) >> 3;
+    const uint8_t* const st = sv + 1;
+    const long long nb = sbytes - 1;
+    auto byte = [&](long long q) -> unsigned long long { return q < nb ? st[q] : 0u; };
+    const unsigned long long mask = bw == 32 ? 0xffffffffull : ((1ull << bw) - 1ull);
+    if (threadIdx.x == 0) {
+        s_pos = 0;
+        s_row[0] = 0;
+        s_bad = 0;
+        s_done = 0;
+    }
+    __syncthreads();
+    while (true) {
+        if (threadIdx.x == 0) {
+            int k = 0;
+            int row = s_row[0];
+            long long pos = s_pos;
+            while (k < kPqRuns && row < n_idx) {
+                unsigned long long h = 0;
+                int shift = 0;
+                bool ok = true;
+                while (true) {
+                    if (pos >= nb || shift > 35) {
+                        ok = false;
+                        break;
+                    }
+                    const unsigned long long b = st[pos++];
+                    h |= (b & 0x7f) << shift;
+                    shift += 7;
+                    if (!(b & 0x80)) break;
+                }
+                if (!ok) {
+                    s_bad = 1;
+                    break;
+                }
+                long long len;
+                if (h & 1) {
+                    const long long groups = (long long)(h >> 1);
+                    if (pos + groups * bw > nb) {
+                        s_bad = 1;
+                        break;
+                    }
+                    s_kind[k] = 1;
+                    s_info[k] = pos;
+                    pos += groups * bw;
+                    len = groups * 8;
+                } else {
+                    if (pos + vbytes > nb) {
+                        s_bad = 1;
+                        break;
+                    }
+                    unsigned long long v = 0;
+                    for (int j = 0; j < vbytes; ++j) v |= (unsigned long long)st[pos + j] << (8 * j);
+                    pos += vbytes;
+                    s_kind[k] = 0;
+                    s_info[k] = (long long)(v & mask);
+                    len = (long long)(h >> 1);
+                }
+                len = min(len, (long long)(n_idx - row));
+                if (len <= 0) continue;
+                s_row[k] = row;
+                row += (int)len;
+                ++k;
+                s_row[k] = row;
+            }
+            s_pos = pos;
+            s_n = k;
+            if (row >= n_idx) s_done = 1;
+            else if (k == 0) s_bad = 1;
+        }
+        __syncthreads();
+        if (s_bad) break;
+        const int n = s_n, r_lo = s_row[0], r_hi = s_row[n];
+        for (int i = r_lo + (int)threadIdx.x; i < r_hi; i += 256) {
+            int a = 0, b = n - 1;  // the last run starting at or before i
+            while (a < b) {
+                const int m = (a + b + 1) >> 1;
+                if (s_row[m] <= i) a = m;
+                else b = m - 1;
+            }
+            unsigned long long v;
+            if (s_kind[a]) {
+                const long long bo = (long long)(i - s_row[a]) * bw;
+                const long long q = s_info[a] + (bo >> 3);
+                const unsigned long long x = byte(q) | byte(q + 1) << 8 | byte(q + 2) << 16 | byte(q + 3) << 24 | byte(q + 4) << 32;
+                v = (x >> (bo & 7)) & mask;
+            } else {
+                v = (unsigned long long)s_info[a];
+            }
+            if (v >= (unsigned long long)pg.dict_count) {
+                s_bad = 1;  // benign race: any writer sets it
+                v = 0;
+            }
+            ix[i] = (uint32_t)v;
+        }
+        __syncthreads();
+        if (s_bad || s_done) break;
+        if (threadIdx.x == 0) s_row[0] = r_hi;
+        __syncthreads();
+    }
+    if (threadIdx.x == 0 && s_bad) atomicAdd(P.status, 1ull);
+}
+
+cudaError_t launch_parquet_dict_indices(const ParquetDecodeParams& p, cudaStream_t st) {
+    if (p.page_hi <= p.page_lo) return cudaSuccess;
+    parquet_dict_index_kernel<<<p.page_hi - p.page_lo, 256, 0, st>>>(p);
+    note_launch();
+    return cudaGetLastError();
+}
+
+// ---- Snappy --------------------------------------------------------------------------------
+// The raw Snappy format (google/snappy format_description.txt): a varint of the uncompressed
+// length, then elements, each a tag byte whose low two bits give its kind: 0 a literal (length - 1
+// in the tag's upper six bits, or for 60 .. 63 in the next 1 .. 4 bytes, little-endian), followed by
+// its bytes; 1 a copy of 4 + ((tag >> 2) & 7) bytes from offset ((tag >> 5) << 8 | next byte);
+// 2 and 3 a copy of 1 + (tag >> 2) bytes from a 2- or 4-byte little-endian offset.  A copy reads
+// the output `offset` bytes back and may overlap itself (byte i reads byte i - offset).
+// One warp per page: every lane decodes the same tags from a window of the input staged in shared
+// memory (so control flow stays uniform), and the lanes move an element's bytes together: byte i of
+// a copy is output[op - offset + i % offset], which precedes op, so one pass suffices.
+
+constexpr int kSnapWin = 2048;
+
+__global__ void __launch_bounds__(256) snappy_decompress_kernel(const SnappyJob* __restrict__ jobs, int32_t n_jobs,
+                                                                unsigned long long* status) {
+    __shared__ uint8_t s_win[8][kSnapWin];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int j = (int)blockIdx.x * 8 + warp;
+    if (j >= n_jobs) return;
+    const SnappyJob job = jobs[j];
+    uint8_t* const win = s_win[warp];
+    for (int i = lane; i < job.prefix; i += 32) job.dst[i] = job.src[i - job.prefix];
+    uint8_t* const out = job.dst + job.prefix;
+    const uint8_t* const in = job.src;
+    const int nin = job.src_bytes, nout = job.dst_bytes;
+    int wbase = 0;
+    auto load = [&](int at) {
+        __syncwarp();
+        for (int i = lane; i < kSnapWin; i += 32) win[i] = at + i < nin ? in[at + i] : 0;
+        __syncwarp();
+        wbase = at;
+    };
+    auto inb = [&](int q) -> unsigned {
+        return (q >= wbase && q < wbase + kSnapWin) ? (unsigned)win[q - wbase] : (q < nin ? (unsigned)in[q] : 0u);
+    };
+    load(0);
+    bool bad = false;
+    int ip = 0, op = 0;
+    {
+        unsigned long long ulen = 0;
+        int shift = 0;
+        while (true) {
+            if (ip >= nin || shift > 35) {
+                bad = true;
+                break;
+            }
+            const unsigned b = inb(ip++);
+            ulen |= (unsigned long long)(b & 0x7f) << shift;
+            shift += 7;
+            if (!(b & 0x80)) break;
+        }
+        if (ulen != (unsigned long long)nout) bad = true;
+    }
+    while (!bad && ip < nin) {
+        if (ip + 5 > wbase + kSnapWin) load(ip);  // the tag and its extra bytes in the window
+        const unsigned tag = inb(ip);
+        int len = 0, off = 0;
+        const unsigned kind = tag & 3u;
+        if (kind == 0u) {
+            const unsigned l = tag >> 2;
+            if (l < 60u) {
+                len = (int)l + 1;
+                ip += 1;
+            } else {
+                const int nb = (int)l - 59;
+                unsigned long long v = 0;
+                for (int k = 0; k < nb; ++k) v |= (unsigned long long)inb(ip + 1 + k) << (8 * k);
+                if (ip + 1 + nb > nin || v >= 0x7fffffffull) {
+                    bad = true;
+                    break;
+                }
+                len = (int)v + 1;
+                ip += 1 + nb;
+            }
+            if (len > nin - ip || len > nout - op) {
+                bad = true;
+                break;
+            }
+            for (int i = lane; i < len; i += 32) out[op + i] = (uint8_t)inb(ip + i);
+            ip += len;
+        } else {
+            if (kind == 1u) {
+                len = 4 + (int)((tag >> 2) & 7u);
+                off = (int)(((tag >> 5) << 8) | inb(ip + 1));
+                ip += 2;
+            } else if (kind == 2u) {
+                len = 1 + (int)(tag >> 2);
+                off = (int)(inb(ip + 1) | inb(ip + 2) << 8);
+                ip += 3;
+            } else {
+                len = 1 + (int)(tag >> 2);
+                const unsigned long long o = (unsigned long long)inb(ip + 1) | (unsigned long long)inb(ip + 2) << 8 |
+                                             (unsigned long long)inb(ip + 3) << 16 | (unsigned long long)inb(ip + 4) << 24;
+                if (o > 0x7fffffffull) {
+                    bad = true;
+                    break;
+                }
+                off = (int)o;
+                ip += 5;
+            }
+            if (ip > nin || off == 0 || off > op || len > nout - op) {
+                bad = true;
+                break;
+            }
+            __syncwarp();  // the bytes it reads, written by any lane, are visible
+            for (int i = lane; i < len; i += 32) out[op + i] = out[op - off + i % off];
+        }
+        op += len;
+        __syncwarp();
+    }
+    if (op != nout) bad = true;
+    if (bad && lane == 0) atomicAdd(status, 1ull);
+}
+
+cudaError_t launch_snappy_decompress(const SnappyJob* jobs, int32_t n_jobs, unsigned long long* status, cudaStream_t st) {
+    if (n_jobs <= 0) return cudaSuccess;
+    snappy_decompress_kernel<<<(n_jobs + 7) / 8, 256, 0, st>>>(jobs, n_jobs, status);
+    note_launch();
+    return cudaGetLastError();
+}
+
+__global__ void parquet_level_lengths_kernel(const __grid_constant__ ParquetDecodeParams P) {
+    const int p = P.page_lo + (int)(blockIdx.x * blockDim.x + threadIdx.x);
+    if (p >= P.page_hi) return;
+    ParquetPage& pg = P.pages[p];
+    if (pg.levels >= 0) return;
+    const uint8_t* const d = (const uint8_t*)pg.data;
+    long long lev = -1;
+    if (pg.data_bytes >= 4) lev = (long long)((unsigned)d[0] | (unsigned)d[1] << 8 | (unsigned)d[2] << 16 | (unsigned)d[3] << 24);
+    if (lev < 0 || 4 + lev > pg.data_bytes) {
+        atomicAdd(P.status, 1ull);
+        pg.levels = 0;  // the later kernels then find nothing to read
+        pg.values_off = pg.data_bytes;
+    } else {
+        pg.levels = (int32_t)lev;
+        pg.values_off = 4 + (int32_t)lev;
+    }
+}
+
+cudaError_t launch_parquet_level_lengths(const ParquetDecodeParams& p, cudaStream_t st) {
+    if (p.page_hi <= p.page_lo) return cudaSuccess;
+    parquet_level_lengths_kernel<<<(p.page_hi - p.page_lo + 255) / 256, 256, 0, st>>>(p);
+    note_launch();
+    return cudaGetLastError();
 }
 
 cudaError_t launch_parquet_levels(const ParquetDecodeParams& p, cudaStream_t st) {

@@ -70,16 +70,21 @@ cudaError_t launch_text_present_count(const char* data, int64_t n, const long lo
 
 // ---- Parquet data pages ------------------------------------------------------------------
 
-// One uncompressed data page (v1, PLAIN values) of a projected column, in device memory.
+// One uncompressed data page (v1 or v2) of a projected column, in memory the kernels read.
 struct ParquetPage {
     int64_t row_start;      // the page's first row in the table
-    int64_t data;           // offset of the page's data (after its header) in the file buffer
+    int64_t data;           // device-visible address of the page's (uncompressed) data
+    int64_t dict;           // dictionary-encoded pages: address of the chunk's dictionary (PLAIN values)
     int32_t rows;           // values in the page, nulls included
     int32_t data_bytes;     // the data's length
     int32_t column;         // output column
-    int32_t optional;       // definition levels (bit width 1, RLE / bit-packed hybrid) precede the values
-    int32_t levels;         // optional pages: bytes of the level runs (after their 4-byte length)
+    int32_t optional;       // definition levels (bit width 1, RLE / bit-packed hybrid) come first
+    int32_t lev_off;        // optional pages: offset of the level runs in the data (v1 4, v2 0)
+    int32_t levels;         // optional pages: bytes of the level runs (-1: read from the data's first 4 bytes)
+    int32_t values_off;     // offset of the values: PLAIN values, or the bit width and the indices
     int32_t item0;          // the page's first item (kParquetItemRows rows of a page per item)
+    int32_t dict_count;     // entries of the dictionary; 0: PLAIN values
+    int32_t idx0;           // dictionary-encoded pages: first slot of their indices in idx
 };
 struct ParquetColumnOut {
     void* data;             // rows x width
@@ -90,19 +95,41 @@ struct ParquetColumnOut {
 constexpr int kParquetMaxColumns = 64;
 constexpr int kParquetItemRows = 8192;
 struct ParquetDecodeParams {
-    const uint8_t* file;
-    const ParquetPage* pages;
+    ParquetPage* pages;
     ParquetColumnOut out[kParquetMaxColumns];
-    unsigned long long* status;  // [0] pages whose levels or values run past their data, [1..] valid counts
+    unsigned long long* status;  // [0] malformed pages (levels, indices or values past their data), [1..] valid counts
     uint32_t* item_base;         // per item of an optional page: its page's present rows before it (zeroed)
+    uint32_t* page_present;      // per page: present rows (written for optional pages by the levels kernel)
+    uint32_t* idx;               // dictionary indices of the present rows of dictionary-encoded pages
     int32_t page_lo, page_hi;    // the pages of this launch
     int32_t item_lo, item_hi;    // their items
 };
+// One Snappy-compressed page body (a Parquet page of a SNAPPY column chunk): `prefix` raw bytes
+// (a v2 page's levels, stored uncompressed before the values) are copied from src - prefix, then
+// the raw Snappy stream src[0, src_bytes) is decompressed after them; its length must be dst_bytes.
+struct SnappyJob {
+    const uint8_t* src;
+    uint8_t* dst;
+    int32_t src_bytes;
+    int32_t dst_bytes;
+    int32_t prefix;
+    int32_t pad;
+};
+// One warp per job; a malformed stream or a length mismatch adds one to *status.
+cudaError_t launch_snappy_decompress(const SnappyJob* jobs, int32_t n_jobs, unsigned long long* status, cudaStream_t st);
+
+// Pages of [page_lo, page_hi) whose level length is -1 (Snappy v1 pages): the length from the
+// first 4 bytes of their decompressed data, and their values' offset after it.
+cudaError_t launch_parquet_level_lengths(const ParquetDecodeParams& p, cudaStream_t st);
 // Optional pages of [page_lo, page_hi): validity bits from the definition levels, each item's
 // first value index in item_base, the present rows in status[1 + column].
 cudaError_t launch_parquet_levels(const ParquetDecodeParams& p, cudaStream_t st);
+// Dictionary-encoded pages of [page_lo, page_hi): the index of every present row (RLE / bit-packed
+// hybrid of the page's bit width) into idx, checked against the dictionary's size.  After
+// launch_parquet_levels for optional pages.
+cudaError_t launch_parquet_dict_indices(const ParquetDecodeParams& p, cudaStream_t st);
 // Items [item_lo, item_hi): values of the present rows in row order (null rows 0).  Optional
-// pages' levels must have been decoded by an earlier launch_parquet_levels.
+// pages' levels and dictionary pages' indices must have been decoded by the launches above.
 cudaError_t launch_parquet_values(const ParquetDecodeParams& p, cudaStream_t st);
 
 // codes[i] += 1 where codes[i] >= pos: a string inserted at rank pos of a category dictionary.

@@ -228,7 +228,7 @@ std::string read_page_header(const uint8_t* file, int64_t n, int64_t at, PageHea
             if (id == 1 && t == 5) ph.type = (int32_t)r.zigzag();
             else if (id == 2 && t == 5) ph.uncompressed_size = (int32_t)r.zigzag();
             else if (id == 3 && t == 5) ph.compressed_size = (int32_t)r.zigzag();
-            else if (id == 5 && t == 12) {
+            else if (id == 5 && t == 12) {  // DataPageHeader
                 r.begin();
                 int16_t did;
                 int dt;
@@ -236,6 +236,30 @@ std::string read_page_header(const uint8_t* file, int64_t n, int64_t at, PageHea
                     if (did == 1 && dt == 5) ph.num_values = (int32_t)r.zigzag();
                     else if (did == 2 && dt == 5) ph.encoding = (int32_t)r.zigzag();
                     else if (did == 3 && dt == 5) ph.def_encoding = (int32_t)r.zigzag();
+                    else r.skip(dt);
+                }
+                r.end();
+            } else if (id == 7 && t == 12) {  // DictionaryPageHeader
+                r.begin();
+                int16_t did;
+                int dt;
+                while (r.field(did, dt)) {
+                    if (did == 1 && dt == 5) ph.num_values = (int32_t)r.zigzag();
+                    else if (did == 2 && dt == 5) ph.encoding = (int32_t)r.zigzag();
+                    else r.skip(dt);
+                }
+                r.end();
+            } else if (id == 8 && t == 12) {  // DataPageHeaderV2
+                r.begin();
+                int16_t did;
+                int dt;
+                while (r.field(did, dt)) {
+                    if (did == 1 && dt == 5) ph.num_values = (int32_t)r.zigzag();
+                    else if (did == 2 && dt == 5) ph.num_nulls = (int32_t)r.zigzag();
+                    else if (did == 4 && dt == 5) ph.encoding = (int32_t)r.zigzag();
+                    else if (did == 5 && dt == 5) ph.def_bytes = (int32_t)r.zigzag();
+                    else if (did == 6 && dt == 5) ph.rep_bytes = (int32_t)r.zigzag();
+                    else if (did == 7 && (dt == 1 || dt == 2)) ph.v2_compressed = dt == 1;
                     else r.skip(dt);
                 }
                 r.end();

@@ -40,9 +40,15 @@ struct PageHeader {
     int32_t type = -1;             // 0 DATA_PAGE, 2 DICTIONARY_PAGE, 3 DATA_PAGE_V2
     int32_t uncompressed_size = 0;
     int32_t compressed_size = 0;
-    int32_t num_values = 0;
-    int32_t encoding = -1;         // of the values: 0 PLAIN
-    int32_t def_encoding = -1;     // 3 RLE
+    int32_t num_values = 0;        // data pages: values (nulls included); dictionary pages: entries
+    int32_t encoding = -1;         // of the values: 0 PLAIN, 2 PLAIN_DICTIONARY, 8 RLE_DICTIONARY
+    int32_t def_encoding = -1;     // v1: 3 RLE
+    // DATA_PAGE_V2: the levels' lengths (never compressed, no length prefix), and whether the
+    // values section is compressed
+    int32_t num_nulls = 0;
+    int32_t def_bytes = 0;
+    int32_t rep_bytes = 0;
+    bool v2_compressed = true;
     int64_t header_bytes = 0;      // length of the header itself
 };
 

@@ -458,7 +458,11 @@ def parquet_scan_filter(file: bytes, projections, filter_query_part: Optional[st
     its LogicalFilter (None: the scan alone).  page_locked=True hands the library the file in
     page-locked memory, which its kernels read in place instead of copying the pages in."""
     rows, dts = parquet_schema(file)
-    outs = [Column.empty(dts[c], rows, with_valid=True) for c in projections]
+    for c in projections:
+        if 0 <= c < len(dts) and dts[c] == D.GDF_invalid:
+            # the library refuses the leaf too; no out column of its type can be made here
+            raise RalError(2, f"leaf {c}: only INT32 (DATE), INT64 (TIMESTAMP_MILLIS), FLOAT and DOUBLE columns are scanned")
+    outs = [Column.empty(dts[c] if 0 <= c < len(dts) else D.GDF_INT32, rows, with_valid=True) for c in projections]
     oa, os_ = _colarray(outs)
     pr = _i32(projections)
     n = C.c_int32(0)

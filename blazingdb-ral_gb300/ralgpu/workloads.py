@@ -670,8 +670,28 @@ def _def_levels(valid: np.ndarray) -> bytes:
     return len(out).to_bytes(4, "little") + bytes(out)
 
 
-def parquet_bytes(columns, row_group_rows: int = 1 << 20, page_rows: int = 1 << 17) -> bytes:
-    """columns: [(name, gdf dtype, values, valid bools or None for a required column)]."""
+def _snappy_literals(raw: bytes, length=None) -> bytes:
+    """A raw Snappy stream holding `raw` as literal elements only (valid Snappy, no back-references);
+    `length` overrides the stream's stated uncompressed length (a malformed stream for tests)."""
+    enc = _Compact()
+    enc.varint(len(raw) if length is None else length)
+    out = bytearray(enc.b)
+    for i in range(0, len(raw), 1 << 16):
+        n = len(raw[i:i + (1 << 16)]) - 1
+        if n < 60:
+            out.append(n << 2)
+        else:
+            out.append(61 << 2)                   # the length - 1 in the next two bytes
+            out += n.to_bytes(2, "little")
+        out += raw[i:i + (1 << 16)]
+    return bytes(out)
+
+
+def parquet_bytes(columns, row_group_rows: int = 1 << 20, page_rows: int = 1 << 17, snappy: bool = False,
+                  snappy_length_delta: int = 0) -> bytes:
+    """columns: [(name, gdf dtype, values, valid bools or None for a required column)].  snappy=True
+    writes SNAPPY chunks whose page bodies are literal-only Snappy streams (snappy_length_delta != 0
+    states a wrong uncompressed length in every stream: a malformed file for tests)."""
     n = len(columns[0][2])
     out = bytearray(b"PAR1")
     row_groups = []
@@ -690,9 +710,12 @@ def parquet_bytes(columns, row_group_rows: int = 1 << 20, page_rows: int = 1 << 
                     body += _def_levels(m)
                     v = v[m]
                 body += np.ascontiguousarray(v.astype(D.NP[dt])).tobytes()
+                raw_len = len(body)
+                if snappy:
+                    body = bytearray(_snappy_literals(bytes(body), raw_len + snappy_length_delta))
                 h = _Compact()
                 h.i32(1, 0)                       # DATA_PAGE
-                h.i32(2, len(body))
+                h.i32(2, raw_len)
                 h.i32(3, len(body))
                 h.begin(5)                        # DataPageHeader
                 h.i32(1, p1 - p0)
@@ -735,7 +758,7 @@ def parquet_bytes(columns, row_group_rows: int = 1 << 20, page_rows: int = 1 << 
             m.i32(1, _PQ_TYPE[dt])
             m.list_header(2, 5, 2); m.varint(m.zigzag(0)); m.varint(m.zigzag(3))
             m.list_header(3, 8, 1); m.varint(len(name)); m.b += name.encode()
-            m.i32(4, 0)
+            m.i32(4, 1 if snappy else 0)          # codec
             m.i64(5, crow)
             m.i64(6, nbytes)
             m.i64(7, nbytes)

@@ -278,13 +278,17 @@ int ral_text_scan_filter_host(const char *text, int64_t n_bytes, char delimiter,
  * src/io/data_parser/ParquetParser.cpp:36-90, cudf's Parquet reader) followed by its LogicalFilter.
  * `file` holds the whole file (n_bytes) in host memory.  In page-locked memory the decode kernels read
  * the projected pages in place over the host link; otherwise the projected leaves' column chunks
- * are copied in, in batches decoded while the next batch is copied.  A levels kernel decodes the
- * definition levels of optional leaves, a values kernel every page's values in 8192-row items, and
- * the fused filter kernel filters the decoded columns.  ral_parquet_schema gives the row count, the leaf count and the gdf dtype each
- * leaf scans as (GDF_invalid where unsupported; dtypes: host array of `capacity` entries).
+ * are copied in, in batches decoded while the next batch is copied.  Snappy pages are decompressed
+ * on the device (one warp per page), a levels kernel decodes the definition levels of optional
+ * leaves, a dictionary kernel the indices of dictionary-encoded pages, a values kernel every page's
+ * values in 8192-row items, and the fused filter kernel filters the decoded columns.
+ * ral_parquet_schema gives the row count, the leaf count and the gdf dtype each leaf scans as
+ * (GDF_invalid where unsupported; dtypes: host array of `capacity` entries).
  * Supported: flat schemas; INT32 (DATE as DATE32), INT64 (TIMESTAMP_MILLIS as DATE64), FLOAT,
- * DOUBLE; required and optional leaves; uncompressed v1 data pages of PLAIN values with RLE /
- * bit-packed definition levels — anything else returns RAL_ERROR_UNSUPPORTED.  out_columns: one per
+ * DOUBLE; required and optional leaves; v1 and v2 data pages of PLAIN values or dictionary indices
+ * (PLAIN_DICTIONARY / RLE_DICTIONARY, with the chunk's PLAIN dictionary page), RLE / bit-packed
+ * definition levels; uncompressed or SNAPPY column chunks — anything else returns
+ * RAL_ERROR_UNSUPPORTED, as does a page that does not decode within its bytes.  out_columns: one per
  * projection, of its dtype, with a 4-byte aligned mask and room for every row of the file; on return
  * size = rows kept.  Synchronous.
  */

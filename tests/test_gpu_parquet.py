@@ -1,7 +1,8 @@
 """Scan -> filter over Parquet on the GPU: ral_parquet_scan_filter against the values each file
-holds (pyarrow's fixture with its .npz, and files of ralgpu.workloads.parquet_bytes) and the oracle's
-process_filter over them, bit for bit; required and optional leaves, many pages and row groups, RLE
-and bit-packed definition levels."""
+holds (pyarrow's fixtures with their .npz, and files of ralgpu.workloads.parquet_bytes) and the
+oracle's process_filter over them, bit for bit; required and optional leaves, many pages and row
+groups, RLE and bit-packed definition levels, v1 and v2 pages, PLAIN values and dictionary indices
+(with pyarrow's fallback to PLAIN pages), uncompressed and Snappy chunks, pyarrow's defaults."""
 import os
 
 import numpy as np
@@ -37,10 +38,15 @@ def _check(file_bytes, frame, proj, fq):
             H.assert_columns_equal(g, e, what=f"column {k} ({fq}, page-locked {page_locked})")
 
 
+PYARROW_FILES = ["parquet_plain", "parquet_snappy", "parquet_dictionary", "parquet_dict_fallback", "parquet_v2",
+                 "parquet_v2_snappy_dict", "parquet_defaults"]
+
+
+@pytest.mark.parametrize("name", PYARROW_FILES)
 @pytest.mark.parametrize("fq", FILTERS)
-def test_pyarrow_fixture(fq):
-    b = open(os.path.join(GOLDEN, "parquet_plain.parquet"), "rb").read()
-    v = np.load(os.path.join(GOLDEN, "parquet_plain.npz"))
+def test_pyarrow_fixture(name, fq):
+    b = open(os.path.join(GOLDEN, name + ".parquet"), "rb").read()
+    v = np.load(os.path.join(GOLDEN, name + ".npz"))
     n = len(v["b"])
     ones = np.ones(n, bool)
     frame = [O.make_column(v["a"], D.GDF_INT32, v["a_valid"]), O.make_column(v["b"], D.GDF_INT64, ones),
@@ -66,24 +72,36 @@ def test_writer_files(rows, rg, page):
     _check(b, frame, [0, 5, 2, 1, 3], "LogicalFilter(condition=[OR(IS NULL($2), <($3, 0))])")
 
 
-@pytest.mark.parametrize("name", ["parquet_snappy", "parquet_dictionary"])
-def test_unsupported_files_fail_cleanly(name):
-    b = open(os.path.join(GOLDEN, name + ".parquet"), "rb").read()
+def test_unsupported_files_fail_cleanly():
     for page_locked in (False, True):
-        with pytest.raises(R.RalError):
-            R.parquet_scan_filter(b, [0, 1], page_locked=page_locked)
+        with pytest.raises(R.RalError):  # a GZIP-compressed file
+            R.parquet_scan_filter(open(os.path.join(GOLDEN, "parquet_gzip.parquet"), "rb").read(), [0, 1],
+                                  page_locked=page_locked)
+        with pytest.raises(R.RalError):  # a string leaf
+            R.parquet_scan_filter(open(os.path.join(GOLDEN, "parquet_plain.parquet"), "rb").read(), [6],
+                                  page_locked=page_locked)
     # the context stays usable
     good = W.parquet_bytes(_writer_table(100, 5))
     assert R.parquet_scan_filter(good, [0])[0].size == 100
 
 
-@pytest.mark.parametrize("batch_bytes", ["1", "4096", "100000"])
-def test_copy_batches(monkeypatch, batch_bytes):
-    """Pages copied and decoded in many small batches (one page per batch at 1 byte); the
-    page-locked leg reads the pages in place in one launch."""
-    monkeypatch.setenv("RAL_PARQUET_BATCH_BYTES", batch_bytes)
-    cols = _writer_table(20_011, 3)
-    b = W.parquet_bytes(cols, row_group_rows=7000, page_rows=999)
+@pytest.mark.parametrize("rows,rg,page", [(33, 10, 7), (5000, 2000, 700), (300_001, 100_000, 65_536)])
+def test_writer_files_snappy(rows, rg, page):
+    """The project writer's Snappy chunks (literal-only streams, long literals with 2-byte lengths)."""
+    cols = _writer_table(rows, rows + 1)
+    b = W.parquet_bytes(cols, row_group_rows=rg, page_rows=page, snappy=True)
     frame = _frame_of(cols)
     _check(b, frame, [0, 1, 2, 3, 4, 5], None)
-    _check(b, frame, [2, 4, 0], "LogicalFilter(condition=[OR(IS NULL($1), <($0, 1995-01-01))])")
+    _check(b, frame, [0, 5, 2, 1, 3], "LogicalFilter(condition=[OR(IS NULL($2), <($3, 0))])")
+
+
+@pytest.mark.parametrize("delta", [-1, 1])
+def test_corrupt_snappy_page_is_an_error(delta):
+    """Snappy streams whose stated length differs from their page's: the call fails, nothing faults."""
+    b = W.parquet_bytes(_writer_table(5000, 2), row_group_rows=2000, page_rows=700, snappy=True,
+                        snappy_length_delta=delta)
+    for page_locked in (False, True):
+        with pytest.raises(R.RalError):
+            R.parquet_scan_filter(b, [0, 1], page_locked=page_locked)
+    good = W.parquet_bytes(_writer_table(100, 5))
+    assert R.parquet_scan_filter(good, [0])[0].size == 100

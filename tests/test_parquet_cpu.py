@@ -30,10 +30,11 @@ def _writer_table(n, seed):
     return cols
 
 
-def test_writer_output_reads_back_in_pyarrow():
+@pytest.mark.parametrize("snappy", [False, True])
+def test_writer_output_reads_back_in_pyarrow(snappy):
     pq = pytest.importorskip("pyarrow.parquet")
     cols = _writer_table(20_000, 1)
-    t = pq.read_table(io.BytesIO(W.parquet_bytes(cols, row_group_rows=7000, page_rows=3000)))
+    t = pq.read_table(io.BytesIO(W.parquet_bytes(cols, row_group_rows=7000, page_rows=3000, snappy=snappy)))
     for name, dt, v, m in cols:
         c = t.column(name)
         got_valid = np.asarray(c.is_valid())
@@ -49,14 +50,16 @@ def test_schema_of_the_fixtures():
     b = open(os.path.join(GOLDEN, "parquet_plain.parquet"), "rb").read()
     rows, dts = R.parquet_schema(b)
     assert rows == 3000
-    assert dts == [D.GDF_INT32, D.GDF_INT64, D.GDF_FLOAT32, D.GDF_FLOAT64, D.GDF_DATE32, D.GDF_DATE64]
+    # g is a string leaf: no scanned dtype
+    assert dts == [D.GDF_INT32, D.GDF_INT64, D.GDF_FLOAT32, D.GDF_FLOAT64, D.GDF_DATE32, D.GDF_DATE64, D.GDF_invalid]
     b = W.parquet_bytes(_writer_table(5000, 2), row_group_rows=2000, page_rows=700)
     rows, dts = R.parquet_schema(b)
     assert rows == 5000 and dts == [D.GDF_INT32, D.GDF_FLOAT64, D.GDF_DATE32, D.GDF_DATE64, D.GDF_FLOAT32, D.GDF_INT64]
 
 
-@pytest.mark.parametrize("name,reason", [("parquet_snappy", "compressed"), ("parquet_dictionary", "dictionary")])
-def test_unsupported_files_are_refused_before_device_work(name, reason):
+@pytest.mark.parametrize("name,leaf,reason", [("parquet_gzip", 0, "Snappy-compressed"),
+                                              ("parquet_plain", 6, "columns are scanned")])
+def test_unsupported_files_are_refused_before_device_work(name, leaf, reason):
     b = open(os.path.join(GOLDEN, name + ".parquet"), "rb").read()
     rows, dts = R.parquet_schema(b)
     L = R.lib()
@@ -65,9 +68,9 @@ def test_unsupported_files_are_refused_before_device_work(name, reason):
     outs[0].data = ctypes.c_void_p(256)
     outs[0].valid = ctypes.c_void_p(256)
     outs[0].size = rows
-    outs[0].dtype = dts[0]
+    outs[0].dtype = dts[leaf]
     ptrs = (ctypes.c_void_p * 1)(ctypes.addressof(outs[0]))
-    pr = (ctypes.c_int32 * 1)(0)
+    pr = (ctypes.c_int32 * 1)(leaf)
     n = ctypes.c_int32(0)
     buf = ctypes.create_string_buffer(b, len(b))
     rc = L.ral_parquet_scan_filter(buf, len(b), pr, 1, None, ctypes.cast(ptrs, ctypes.c_void_p), ctypes.byref(n))
