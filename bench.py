@@ -427,7 +427,7 @@ def cpu_served(threads: int, n_queries: int, rows_cap: int, seed: int = 20261203
 
 DEFAULT_ROWS = {"fused_project": 200_000_000, "plain_vm": 1_000_000, "filter_gather": 500_000_000,
                 "filter_project": 200_000_000, "gather": 200_000_000, "scan_filter": 20_000_000,
-                "parquet_filter": 20_000_000}
+                "parquet_filter": 20_000_000, "parquet_dict_filter": 20_000_000}
 
 
 def workload_config(workload, n, selectivity, world=1):
@@ -446,14 +446,18 @@ def workload_config(workload, n, selectivity, world=1):
                "columns": "int32, int64, float32, float64, date32, bool8; 5% nulls", "index": "int32",
                "api": "ral_materialize_columns (all columns in one kernel)",
                "l2": "columns (5.8 GB at 200M rows) exceed L2; no flush"}
-    elif workload == "parquet_filter":
+    elif workload in PARQUET_WORKLOADS:
         from ralgpu import workloads as W
-        cfg = {"workload": "parquet_filter", "rows": n,
-               "table": "the lineitem-like table as Parquet: 8 required columns, uncompressed PLAIN v1 pages, "
-                        "1Mi-row row groups, in page-locked host memory",
+        dictionary = workload == "parquet_dict_filter"
+        cfg = {"workload": workload, "rows": n,
+               "table": "the lineitem-like table as Parquet: 8 required columns, uncompressed "
+                        + ("dictionary-encoded v1 pages (a chunk of at most 65,536 distinct values as a PLAIN "
+                           "dictionary and RLE_DICTIONARY pages, others PLAIN)" if dictionary else "PLAIN v1 pages")
+                        + ", 1Mi-row row groups, in page-locked host memory",
                "scan": f"BindableTableScan projects={W.TEXT_PROJECTIONS}", "filter": "TPC-H Q6's conditions",
-               "fused": "the projected pages read in place from page-locked host memory by the page-value kernel "
-                        "(a block per 8192-row item of a page), then the fused filter kernel",
+               "fused": "the projected pages read in place from page-locked host memory"
+                        + (", dictionary indices decoded by one block per page" if dictionary else "")
+                        + ", the page-value kernel (a block per 8192-row item of a page), then the fused filter kernel",
                "l2": "decoded columns (560 MB at 20M rows) exceed L2; no flush"}
     elif workload == "scan_filter":
         from ralgpu import workloads as W
@@ -517,7 +521,10 @@ def scan_filter_setup(n, device):
                 host_text=host, dev_text=dev, text_bytes=len(text), cols=[R.Column(dev, None, D.GDF_INT8, len(text))])
 
 
-def parquet_filter_setup(n, device):
+PARQUET_WORKLOADS = ("parquet_filter", "parquet_dict_filter")
+
+
+def parquet_filter_setup(n, device, dictionary=False):
     """The lineitem-like table as a Parquet file in page-locked host memory, and one step:
     ral_parquet_scan_filter of TPC-H Q6's conditions over the scan of quantity, extendedprice,
     discount and shipdate (the projected pages read in place over the host link, decoded, filtered)."""
@@ -528,7 +535,9 @@ def parquet_filter_setup(n, device):
     from ralgpu import workloads as W
     L = R.lib()
     values = W.lineitem_values(n, W.SEED)
-    blob = W.parquet_bytes([(nm, dt, v, None) for nm, dt, v in zip(W.LINEITEM_NAMES, W.TEXT_DTYPES, values)])
+    sizes = []
+    blob = W.parquet_bytes([(nm, dt, v, None) for nm, dt, v in zip(W.LINEITEM_NAMES, W.TEXT_DTYPES, values)],
+                           dictionary=dictionary, chunk_bytes=sizes)
     host = torch.frombuffer(bytearray(blob), dtype=torch.uint8).pin_memory()
     proj = W.TEXT_PROJECTIONS
     outs = [R.Column.empty(W.TEXT_DTYPES[c], n, with_valid=True, device=device) for c in proj]
@@ -545,7 +554,8 @@ def parquet_filter_setup(n, device):
         if rc:
             raise RuntimeError(L.ral_last_error().decode())
 
-    chunk_bytes = n * sum(D.WIDTH[W.TEXT_DTYPES[c]] for c in proj)
+    # the bytes that cross the link: the projected leaves' column chunks
+    chunk_bytes = sum(b for c, b in sizes if c in proj)
 
     def alg_bytes():
         k = nout.value
@@ -1078,8 +1088,8 @@ def measure_workload(args, workload, n, selectivity, device, world, sampler, e2e
         ctx = fused_project_setup(n, device)
     elif workload == "scan_filter":
         ctx = scan_filter_setup(n, device)
-    elif workload == "parquet_filter":
-        ctx = parquet_filter_setup(n, device)
+    elif workload in PARQUET_WORKLOADS:
+        ctx = parquet_filter_setup(n, device, dictionary=workload == "parquet_dict_filter")
     elif workload == "gather":
         ctx = gather_setup(n, selectivity, device)
     else:
@@ -1193,7 +1203,7 @@ def measure_workload(args, workload, n, selectivity, device, world, sampler, e2e
                 out["e2e"] = fused_project_e2e(ctx, max(2, min(args.steps, 3)), device)
             elif workload == "scan_filter":
                 out["e2e"] = scan_filter_e2e(ctx, max(2, min(args.steps, 3)))
-            elif workload == "parquet_filter":
+            elif workload in PARQUET_WORKLOADS:
                 # the call itself starts from host memory: its step time is the end-to-end time
                 out["e2e"] = {"value": out["value"], "unit": "rows/s", "h2d_bytes_per_step": int(ctx["chunk_bytes"]),
                               "d2h_bytes_per_step": 0, "ms_per_step": out["ms_per_step"],
@@ -1212,12 +1222,12 @@ def measure_workload(args, workload, n, selectivity, device, world, sampler, e2e
         # the device outputs (the e2e leg rewrote them with the same bits) against the oracle
         if parity and not args.skip_parity:
             out["parity"] = (gather_parity(ctx) if workload == "gather" else
-                             scan_filter_parity(ctx) if workload in ("scan_filter", "parquet_filter") else
+                             scan_filter_parity(ctx) if workload in ("scan_filter",) + PARQUET_WORKLOADS else
                              parity_check(workload, ctx, selectivity))
-        if cpu and not args.skip_cpu and workload != "parquet_filter":
+        if cpu and not args.skip_cpu and workload not in PARQUET_WORKLOADS:
             out["cpu_baseline"] = cpu_baseline(workload, n, selectivity, budget_s=cpu_budget_s,
                                                single_budget_s=cpu_budget_s / 3)
-        if workload == "parquet_filter":
+        if workload in PARQUET_WORKLOADS:
             out["cpu_baseline_note"] = "no CPU Parquet reader is installed where the benchmark runs (the oracle reads the text form)"
     del ctx
     torch.cuda.empty_cache()
@@ -1227,7 +1237,7 @@ def measure_workload(args, workload, n, selectivity, device, world, sampler, e2e
 # Workloads measured beside the default one in the same run: the 200M-row fused filter + project at
 # s = 0.5 (the target kernel) and the 500M-row filter + gather of six columns at s = 0.5.
 EXTRA_WORKLOADS = [("filter_project", 0.5), ("filter_gather", 0.5), ("gather", "permutation"), ("scan_filter", None),
-                   ("parquet_filter", None)]
+                   ("parquet_filter", None), ("parquet_dict_filter", None)]
 
 
 def run_ours(args):
@@ -1254,7 +1264,8 @@ def run_ours(args):
                   "filter_gather": "int32/int64/f32/f64/date32/bool8 gather",
                   "gather": "int32/int64/f32/f64/date32/bool8 gather",
                   "scan_filter": "u8 text -> int32/f64/date64",
-                  "parquet_filter": "Parquet pages -> int32/f64/date64"}[args.workload],
+                  "parquet_filter": "Parquet pages -> int32/f64/date64",
+                  "parquet_dict_filter": "Parquet pages -> int32/f64/date64"}[args.workload],
         "data": "synthetic (seeded, generated on the GPU)",
         "config": main["config"],
         "hbm_gbs": main["roofline"]["achieved"],
@@ -1689,7 +1700,8 @@ def run_reference(args):
                      "filter_gather": "int32/int64/f32/f64/date32/bool8 gather",
                   "gather": "int32/int64/f32/f64/date32/bool8 gather",
                   "scan_filter": "u8 text -> int32/f64/date64",
-                  "parquet_filter": "Parquet pages -> int32/f64/date64"}[args.workload],
+                  "parquet_filter": "Parquet pages -> int32/f64/date64",
+                  "parquet_dict_filter": "Parquet pages -> int32/f64/date64"}[args.workload],
            "data": "synthetic (seeded)", "impl": "reference",
            "config": workload_config(args.workload, n, sel, world),
            "cpu_baseline": {"value": v, "unit": "rows/s", "cores": threads, "kind": "port",
@@ -1706,7 +1718,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="fused_project",
                     choices=["fused_project", "plain_vm", "filter_gather", "filter_project", "gather", "batched",
-                             "served", "scan_filter", "parquet_filter"])
+                             "served", "scan_filter", "parquet_filter", "parquet_dict_filter"])
     ap.add_argument("--tables", type=int, default=24)
     ap.add_argument("--queries", type=int, default=96)
     ap.add_argument("--requests", type=int, default=50_000)

@@ -784,7 +784,9 @@ __global__ void __launch_bounds__(256) parquet_values_kernel(const __grid_consta
         const uint32_t* const ix = P.idx + pg.idx0;
         for (int r = rel0 + (int)threadIdx.x; r < rel1; r += 256) {
             const uint32_t k = ix[r];  // in range unless the page was malformed (then reported)
-            ral_pq_store(col.data, pg.row_start + r, w, k < (uint32_t)pg.dict_count ? ral_pq_value(dict, k, w) : 0ull);
+            unsigned long long x = 0;
+            if (k < (uint32_t)pg.dict_count) x = ral_pq_value(dict, k, w);
+            ral_pq_store(col.data, pg.row_start + r, w, x);
         }
         return;
     }
@@ -877,14 +879,21 @@ __global__ void __launch_bounds__(256) parquet_values_kernel(const __grid_consta
 // One block per dictionary-encoded page: after the bit width byte, the present rows' indices in
 // the RLE / bit-packed hybrid (a run header varint h: h odd -> (h >> 1) groups of 8 values of the
 // bit width, packed from the low bits; h even -> h >> 1 repeats of the next ceil(width / 8) bytes).
-// Thread 0 walks the run headers into a table (a batch of up to kPqRuns runs at a time), then the
-// block writes the batch's indices, checking each against the dictionary's size.
-__global__ void __launch_bounds__(256) parquet_dict_index_kernel(const __grid_constant__ ParquetDecodeParams P) {
+// Thread 0 walks the run headers into a batch of segments (an RLE run, or up to kDictStage bytes of
+// a bit-packed run: a long run is cut at group boundaries), the block copies the batch's span of
+// packed bytes into shared memory with 16-byte loads, then writes the batch's indices from there,
+// each checked against the dictionary's size.
+
+constexpr int kDictStage = 32768;  // packed index bytes staged per batch
+constexpr int kDictThreads = 1024;
+
+__global__ void __launch_bounds__(kDictThreads) parquet_dict_index_kernel(const __grid_constant__ ParquetDecodeParams P) {
+    __shared__ __align__(16) uint8_t s_buf[kDictStage + 64];
     __shared__ int s_row[kPqRuns + 1];
-    __shared__ long long s_info[kPqRuns];  // bit-packed: byte offset of the run's values; RLE: the value
+    __shared__ long long s_info[kPqRuns];  // bit-packed: stream offset of the segment's first value; RLE: the value
     __shared__ unsigned char s_kind[kPqRuns];
     __shared__ int s_n, s_bad, s_done;
-    __shared__ long long s_pos;
+    __shared__ long long s_pos, s_rem_groups, s_rem_pos, s_span0, s_span1;
     const int p = P.page_lo + (int)blockIdx.x;
     const ParquetPage pg = P.pages[p];
     if (pg.dict_count <= 0 || pg.rows <= 0) return;
@@ -901,21 +910,44 @@ __global__ void __launch_bounds__(256) parquet_dict_index_kernel(const __grid_co
     const int vbytes = (bw + 7) >> 3;
     const uint8_t* const st = sv + 1;
     const long long nb = sbytes - 1;
-    auto byte = [&](long long q) -> unsigned long long { return q < nb ? st[q] : 0u; };
     const unsigned long long mask = bw == 32 ? 0xffffffffull : ((1ull << bw) - 1ull);
+    // groups of one bit-packed segment: a batch's span stays within the stage
+    const long long seg_groups = bw > 0 ? (long long)(kDictStage - 32) / bw : (1ll << 40);
     if (threadIdx.x == 0) {
         s_pos = 0;
         s_row[0] = 0;
         s_bad = 0;
         s_done = 0;
+        s_rem_groups = 0;
+        s_rem_pos = 0;
     }
     __syncthreads();
     while (true) {
         if (threadIdx.x == 0) {
             int k = 0;
             int row = s_row[0];
-            long long pos = s_pos;
+            long long pos = s_pos, rem = s_rem_groups, rpos = s_rem_pos;
+            long long span0 = -1, span1 = -1;
             while (k < kPqRuns && row < n_idx) {
+                if (rem > 0) {
+                    // the next segment of the bit-packed run in progress
+                    if (span0 < 0) span0 = rpos;
+                    const long long room = (long long)(kDictStage - 32) - (rpos - span0);
+                    long long g = bw > 0 ? min(rem, room / bw) : rem;
+                    g = min(g, seg_groups);
+                    if (g <= 0) break;  // the stage is full: the next batch goes on from here
+                    const long long len = min(g * 8, (long long)(n_idx - row));
+                    s_kind[k] = 1;
+                    s_info[k] = rpos;
+                    s_row[k] = row;
+                    row += (int)len;
+                    ++k;
+                    s_row[k] = row;
+                    rpos += g * bw;
+                    span1 = rpos;
+                    rem -= g;
+                    continue;
+                }
                 unsigned long long h = 0;
                 int shift = 0;
                 bool ok = true;
@@ -933,17 +965,15 @@ __global__ void __launch_bounds__(256) parquet_dict_index_kernel(const __grid_co
                     s_bad = 1;
                     break;
                 }
-                long long len;
                 if (h & 1) {
                     const long long groups = (long long)(h >> 1);
                     if (pos + groups * bw > nb) {
                         s_bad = 1;
                         break;
                     }
-                    s_kind[k] = 1;
-                    s_info[k] = pos;
+                    rem = groups;
+                    rpos = pos;
                     pos += groups * bw;
-                    len = groups * 8;
                 } else {
                     if (pos + vbytes > nb) {
                         s_bad = 1;
@@ -952,27 +982,43 @@ __global__ void __launch_bounds__(256) parquet_dict_index_kernel(const __grid_co
                     unsigned long long v = 0;
                     for (int j = 0; j < vbytes; ++j) v |= (unsigned long long)st[pos + j] << (8 * j);
                     pos += vbytes;
+                    const long long len = min((long long)(h >> 1), (long long)(n_idx - row));
+                    if (len <= 0) continue;
                     s_kind[k] = 0;
                     s_info[k] = (long long)(v & mask);
-                    len = (long long)(h >> 1);
+                    s_row[k] = row;
+                    row += (int)len;
+                    ++k;
+                    s_row[k] = row;
                 }
-                len = min(len, (long long)(n_idx - row));
-                if (len <= 0) continue;
-                s_row[k] = row;
-                row += (int)len;
-                ++k;
-                s_row[k] = row;
             }
             s_pos = pos;
+            s_rem_groups = row >= n_idx ? 0 : rem;
+            s_rem_pos = rpos;
             s_n = k;
+            s_span0 = span0;
+            s_span1 = span1;
             if (row >= n_idx) s_done = 1;
-            else if (k == 0) s_bad = 1;
+            else if (k == 0 && !s_bad) s_bad = 1;
         }
         __syncthreads();
         if (s_bad) break;
         const int n = s_n, r_lo = s_row[0], r_hi = s_row[n];
-        for (int i = r_lo + (int)threadIdx.x; i < r_hi; i += 256) {
-            int a = 0, b = n - 1;  // the last run starting at or before i
+        // the batch's packed bytes [span0, span1) into the stage: 16-byte loads from the aligned
+        // address at or before them (inside the page's buffer, which is 16-byte padded)
+        const long long span0 = s_span0, span1 = s_span1;
+        long long sbase = 0;
+        if (span0 >= 0) {
+            const uintptr_t a0 = (uintptr_t)(st + span0) & ~(uintptr_t)15;
+            const uintptr_t a1 = ((uintptr_t)(st + span1) + 15) & ~(uintptr_t)15;
+            const int nv = (int)((a1 - a0) >> 4);
+            for (int i = threadIdx.x; i < nv; i += blockDim.x)
+                reinterpret_cast<uint4*>(s_buf)[i] = reinterpret_cast<const uint4*>(a0)[i];
+            sbase = (long long)(a0 - (uintptr_t)st);  // stream offset of s_buf[0] (may be negative)
+        }
+        __syncthreads();
+        for (int i = r_lo + (int)threadIdx.x; i < r_hi; i += kDictThreads) {
+            int a = 0, b = n - 1;  // the last segment starting at or before i
             while (a < b) {
                 const int m = (a + b + 1) >> 1;
                 if (s_row[m] <= i) a = m;
@@ -981,8 +1027,10 @@ __global__ void __launch_bounds__(256) parquet_dict_index_kernel(const __grid_co
             unsigned long long v;
             if (s_kind[a]) {
                 const long long bo = (long long)(i - s_row[a]) * bw;
-                const long long q = s_info[a] + (bo >> 3);
-                const unsigned long long x = byte(q) | byte(q + 1) << 8 | byte(q + 2) << 16 | byte(q + 3) << 24 | byte(q + 4) << 32;
+                const long long q = s_info[a] + (bo >> 3) - sbase;  // in the stage
+                unsigned long long x = 0;
+#pragma unroll
+                for (int j = 0; j < 5; ++j) x |= (unsigned long long)s_buf[q + j] << (8 * j);
                 v = (x >> (bo & 7)) & mask;
             } else {
                 v = (unsigned long long)s_info[a];
@@ -1003,7 +1051,7 @@ __global__ void __launch_bounds__(256) parquet_dict_index_kernel(const __grid_co
 
 cudaError_t launch_parquet_dict_indices(const ParquetDecodeParams& p, cudaStream_t st) {
     if (p.page_hi <= p.page_lo) return cudaSuccess;
-    parquet_dict_index_kernel<<<p.page_hi - p.page_lo, 256, 0, st>>>(p);
+    parquet_dict_index_kernel<<<p.page_hi - p.page_lo, kDictThreads, 0, st>>>(p);
     note_launch();
     return cudaGetLastError();
 }
@@ -1150,6 +1198,32 @@ __global__ void parquet_level_lengths_kernel(const __grid_constant__ ParquetDeco
 cudaError_t launch_parquet_level_lengths(const ParquetDecodeParams& p, cudaStream_t st) {
     if (p.page_hi <= p.page_lo) return cudaSuccess;
     parquet_level_lengths_kernel<<<(p.page_hi - p.page_lo + 255) / 256, 256, 0, st>>>(p);
+    note_launch();
+    return cudaGetLastError();
+}
+
+// One block per job: bytes [src, src + bytes) to dst (16-byte loads and stores where both sides
+// share an alignment, single bytes otherwise).
+__global__ void __launch_bounds__(256) copy_jobs_kernel(const CopyJob* __restrict__ jobs, int32_t n_jobs) {
+    const CopyJob j = jobs[blockIdx.x];
+    const uintptr_t s = (uintptr_t)j.src, d = (uintptr_t)j.dst;
+    if (((s ^ d) & 15) == 0) {
+        const int64_t lead = (int64_t)((16 - (s & 15)) & 15);
+        const int64_t head = j.bytes < lead ? j.bytes : lead;
+        for (int64_t i = threadIdx.x; i < head; i += blockDim.x) j.dst[i] = j.src[i];
+        const int64_t nv = (j.bytes - head) >> 4;
+        const uint4* sv = reinterpret_cast<const uint4*>(j.src + head);
+        uint4* dv = reinterpret_cast<uint4*>(j.dst + head);
+        for (int64_t i = threadIdx.x; i < nv; i += blockDim.x) dv[i] = sv[i];
+        for (int64_t i = head + nv * 16 + threadIdx.x; i < j.bytes; i += blockDim.x) j.dst[i] = j.src[i];
+    } else {
+        for (int64_t i = threadIdx.x; i < j.bytes; i += blockDim.x) j.dst[i] = j.src[i];
+    }
+}
+
+cudaError_t launch_copy_jobs(const CopyJob* jobs, int32_t n_jobs, cudaStream_t st) {
+    if (n_jobs <= 0) return cudaSuccess;
+    copy_jobs_kernel<<<n_jobs, 256, 0, st>>>(jobs, n_jobs);
     note_launch();
     return cudaGetLastError();
 }

@@ -118,6 +118,15 @@ struct SnappyJob {
 // One warp per job; a malformed stream or a length mismatch adds one to *status.
 cudaError_t launch_snappy_decompress(const SnappyJob* jobs, int32_t n_jobs, unsigned long long* status, cudaStream_t st);
 
+// Byte copies gathered into one launch (one block per job): small pieces of a page-locked file
+// (dictionaries) brought into device memory.
+struct CopyJob {
+    const uint8_t* src;
+    uint8_t* dst;
+    int64_t bytes;
+};
+cudaError_t launch_copy_jobs(const CopyJob* jobs, int32_t n_jobs, cudaStream_t st);
+
 // Pages of [page_lo, page_hi) whose level length is -1 (Snappy v1 pages): the length from the
 // first 4 bytes of their decompressed data, and their values' offset after it.
 cudaError_t launch_parquet_level_lengths(const ParquetDecodeParams& p, cudaStream_t st);

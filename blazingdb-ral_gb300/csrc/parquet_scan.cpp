@@ -337,9 +337,45 @@ int parquet_scan_filter(const uint8_t* file, int64_t n, const int32_t* projectio
     auto where_at = [&](const PageWhere& w) -> const uint8_t* {
         return w.unpack >= 0 ? (const uint8_t*)dunpack.p + w.unpack : file_at(w.file_off, w.chunk);
     };
+    // read in place, a dictionary would be looked up at random over the host link: the
+    // dictionaries come into device memory first (one small copy job each, one launch)
+    DevBuf ddict(st), dcopies(st);
+    std::map<int64_t, int64_t> dict_copy;  // a dictionary's file offset -> its offset in ddict
+    std::vector<CopyJob> cjobs;
+    if (direct) {
+        int64_t dbytes = 0;
+        for (size_t k = 0; k < pages.size(); k++) {
+            const PageWhere& dw = plan.dict_where[k];
+            if (pages[k].dict_count <= 0 || dw.unpack >= 0 || dict_copy.count(dw.file_off)) continue;
+            dict_copy[dw.file_off] = dbytes;
+            const int64_t b = (int64_t)pages[k].dict_count * gdf_dtype_size(dtypes[pages[k].column]);
+            cjobs.push_back({direct + dw.file_off, nullptr, b});
+            dbytes += std::max<int64_t>(16, (b + 15) & ~15ll);
+        }
+        if (!cjobs.empty()) {
+            if (int e = ddict.alloc((size_t)dbytes)) return e;
+            for (size_t k = 0; k < pages.size(); k++) {
+                const PageWhere& dw = plan.dict_where[k];
+                if (pages[k].dict_count <= 0 || dw.unpack >= 0) continue;
+                pages[k].dict = (int64_t)(uintptr_t)((char*)ddict.p + dict_copy[dw.file_off]);
+            }
+            for (CopyJob& cj : cjobs) {
+                const int64_t off = (int64_t)(cj.src - direct);
+                cj.dst = (uint8_t*)ddict.p + dict_copy[off];
+            }
+            if (int e = dcopies.alloc(cjobs.size() * sizeof(CopyJob))) return e;
+            if (int e = check_cuda(cudaMemcpyAsync(dcopies.p, cjobs.data(), cjobs.size() * sizeof(CopyJob),
+                                                   cudaMemcpyHostToDevice, st),
+                                   "cudaMemcpyAsync"))
+                return e;
+            if (int e = check_cuda(launch_copy_jobs((const CopyJob*)dcopies.p, (int32_t)cjobs.size(), st), "dictionary copies"))
+                return e;
+        }
+    }
     for (size_t k = 0; k < pages.size(); k++) {
         pages[k].data = (int64_t)(uintptr_t)where_at(plan.where[k]);
-        if (pages[k].dict_count > 0) pages[k].dict = (int64_t)(uintptr_t)where_at(plan.dict_where[k]);
+        if (pages[k].dict_count > 0 && !(direct && plan.dict_where[k].unpack < 0))
+            pages[k].dict = (int64_t)(uintptr_t)where_at(plan.dict_where[k]);
     }
     std::vector<SnappyJob> jobs(plan.unpacks.size());
     for (size_t k = 0; k < jobs.size(); k++) {
@@ -404,15 +440,17 @@ int parquet_scan_filter(const uint8_t* file, int64_t n, const int32_t* projectio
         if (dict && check_cuda(launch_parquet_dict_indices(dp, st), "Parquet dictionary indices")) return kCudaError;
         return check_cuda(launch_parquet_values(dp, st), "Parquet page values");
     };
+    // the copy lane starts after this stream's work so far; on every exit this stream waits for
+    // the lane before any buffer is freed
+    if (int e = check_cuda(cudaEventRecord(lane->ready, st), "cudaEventRecord")) return e;
+    if (int e = check_cuda(cudaStreamWaitEvent(lane->s, lane->ready, 0), "cudaStreamWaitEvent")) return e;
+    LaneJoin join{lane, st};
     if (direct) {
         if (!plan.chunks.empty())
             if (int e = decode(0, plan.chunks.size())) return e;
     }
     // Otherwise the chunks go in batches of about kBatchBytes: a batch's chunks are copied on the
     // copy lane's stream while the batch before it is decoded on this one.
-    if (int e = check_cuda(cudaEventRecord(lane->ready, st), "cudaEventRecord")) return e;
-    if (int e = check_cuda(cudaStreamWaitEvent(lane->s, lane->ready, 0), "cudaStreamWaitEvent")) return e;
-    LaneJoin join{lane, st};  // before the buffers are freed, this stream waits for every copy
     const int64_t kBatchBytes = batch_bytes();
     size_t batch = 0;
     for (size_t c0 = direct ? plan.chunks.size() : 0; c0 < plan.chunks.size(); batch++) {

@@ -687,48 +687,110 @@ def _snappy_literals(raw: bytes, length=None) -> bytes:
     return bytes(out)
 
 
+def _bit_packed(idx: np.ndarray, bw: int) -> bytes:
+    """idx (non-negative, below 2^bw) as one bit-packed run of the RLE / bit-packed hybrid."""
+    k = idx.shape[0]
+    groups = (k + 7) // 8
+    enc = _Compact()
+    enc.varint((groups << 1) | 1)
+    if bw == 0 or k == 0:
+        return bytes(enc.b)
+    padded = np.zeros(groups * 8, dtype=np.uint64)
+    padded[:k] = idx
+    bits = ((padded[:, None] >> np.arange(bw, dtype=np.uint64)) & np.uint64(1)).astype(np.uint8)
+    return bytes(enc.b) + np.packbits(bits.reshape(-1), bitorder="little").tobytes()
+
+
+def _page_header(kind: int, raw_len: int, stored_len: int, rows: int, encoding: int) -> bytes:
+    h = _Compact()
+    h.i32(1, kind)                        # 0 DATA_PAGE, 2 DICTIONARY_PAGE
+    h.i32(2, raw_len)
+    h.i32(3, stored_len)
+    if kind == 2:
+        h.begin(7)                        # DictionaryPageHeader
+        h.i32(1, rows)
+        h.i32(2, encoding)
+    else:
+        h.begin(5)                        # DataPageHeader
+        h.i32(1, rows)
+        h.i32(2, encoding)
+        h.i32(3, 3)                       # RLE definition levels
+        h.i32(4, 3)
+    h.end()
+    h.b.append(0)
+    return bytes(h.b)
+
+
 def parquet_bytes(columns, row_group_rows: int = 1 << 20, page_rows: int = 1 << 17, snappy: bool = False,
-                  snappy_length_delta: int = 0) -> bytes:
+                  snappy_length_delta: int = 0, dictionary: bool = False, dictionary_max: int = 65536,
+                  chunk_bytes: Optional[list] = None) -> bytes:
     """columns: [(name, gdf dtype, values, valid bools or None for a required column)].  snappy=True
     writes SNAPPY chunks whose page bodies are literal-only Snappy streams (snappy_length_delta != 0
-    states a wrong uncompressed length in every stream: a malformed file for tests)."""
+    states a wrong uncompressed length in every stream: a malformed file for tests).
+    dictionary=True writes a column chunk with at most dictionary_max distinct values (by bit pattern)
+    as a PLAIN dictionary page and RLE_DICTIONARY data pages (the indices as one bit-packed run).
+    chunk_bytes, when given, receives (column index, bytes) of every column chunk written."""
     n = len(columns[0][2])
     out = bytearray(b"PAR1")
     row_groups = []
+
+    def put(body: bytearray, kind: int, rows: int, encoding: int) -> int:
+        raw_len = len(body)
+        if snappy:
+            body = bytearray(_snappy_literals(bytes(body), raw_len + snappy_length_delta))
+        hb = _page_header(kind, raw_len, len(body), rows, encoding)
+        out.extend(hb)
+        out.extend(body)
+        return len(hb) + len(body)
+
     for r0 in range(0, max(n, 1), row_group_rows):
         r1 = min(n, r0 + row_group_rows)
         chunks = []
         for name, dt, vals, valid in columns:
             start = len(out)
             nbytes = 0
+            bits_of = np.dtype(D.NP[dt]).itemsize * 8
+            cv = np.ascontiguousarray(np.asarray(vals[r0:r1]).astype(D.NP[dt]))
+            cm = None if valid is None else np.asarray(valid[r0:r1], dtype=bool)
+            dict_vals = None
+            if dictionary and r1 > r0:
+                key = cv.view(np.uint32 if bits_of == 32 else np.uint64)
+                present = key if cm is None else key[cm]
+                uniq, inv = np.unique(present, return_inverse=True)
+                if 0 < len(uniq) <= dictionary_max:
+                    dict_vals = uniq.view(cv.dtype)
+                    bw = int(len(uniq) - 1).bit_length()
+                    nbytes += put(bytearray(np.ascontiguousarray(dict_vals).tobytes()), 2, len(uniq), 0)
+                    inv_all = np.zeros(r1 - r0, dtype=np.int64)
+                    if cm is None:
+                        inv_all[:] = inv
+                    else:
+                        inv_all[cm] = inv
+            data_start = len(out)
             for p0 in range(r0, max(r1, r0 + 1), page_rows):
                 p1 = min(r1, p0 + page_rows)
-                v = np.asarray(vals[p0:p1])
+                v = cv[p0 - r0:p1 - r0]
                 body = bytearray()
-                if valid is not None:
-                    m = np.asarray(valid[p0:p1], dtype=bool)
-                    body += _def_levels(m)
-                    v = v[m]
-                body += np.ascontiguousarray(v.astype(D.NP[dt])).tobytes()
-                raw_len = len(body)
-                if snappy:
-                    body = bytearray(_snappy_literals(bytes(body), raw_len + snappy_length_delta))
-                h = _Compact()
-                h.i32(1, 0)                       # DATA_PAGE
-                h.i32(2, raw_len)
-                h.i32(3, len(body))
-                h.begin(5)                        # DataPageHeader
-                h.i32(1, p1 - p0)
-                h.i32(2, 0)                       # PLAIN
-                h.i32(3, 3)                       # RLE
-                h.i32(4, 3)
-                h.end()
-                h.b.append(0)
-                out += h.b + body
-                nbytes += len(h.b) + len(body)
+                keep = None
+                if cm is not None:
+                    keep = cm[p0 - r0:p1 - r0]
+                    body += _def_levels(keep)
+                if dict_vals is not None:
+                    ix = inv_all[p0 - r0:p1 - r0]
+                    if keep is not None:
+                        ix = ix[keep]
+                    body += bytes([bw]) + _bit_packed(ix.astype(np.uint64), bw)
+                    nbytes += put(body, 0, p1 - p0, 8)
+                else:
+                    if keep is not None:
+                        v = v[keep]
+                    body += v.tobytes()
+                    nbytes += put(body, 0, p1 - p0, 0)
                 if r1 == r0:
                     break
-            chunks.append((name, dt, start, nbytes, r1 - r0))
+            chunks.append((name, dt, start, nbytes, r1 - r0, data_start if dict_vals is not None else -1))
+            if chunk_bytes is not None:
+                chunk_bytes.append((len(chunks) - 1, nbytes))
         row_groups.append((r1 - r0, chunks))
         if n == 0:
             break
@@ -750,19 +812,24 @@ def parquet_bytes(columns, row_group_rows: int = 1 << 20, page_rows: int = 1 << 
         m.elem_begin()
         m.list_header(1, 12, len(chunks))
         total = 0
-        for name, dt, start, nbytes, crow in chunks:
+        for name, dt, start, nbytes, crow, data_start in chunks:
             total += nbytes
             m.elem_begin()
             m.i64(2, start)
             m.begin(3)
             m.i32(1, _PQ_TYPE[dt])
-            m.list_header(2, 5, 2); m.varint(m.zigzag(0)); m.varint(m.zigzag(3))
+            if data_start >= 0:
+                m.list_header(2, 5, 3); m.varint(m.zigzag(0)); m.varint(m.zigzag(3)); m.varint(m.zigzag(8))
+            else:
+                m.list_header(2, 5, 2); m.varint(m.zigzag(0)); m.varint(m.zigzag(3))
             m.list_header(3, 8, 1); m.varint(len(name)); m.b += name.encode()
             m.i32(4, 1 if snappy else 0)          # codec
             m.i64(5, crow)
             m.i64(6, nbytes)
             m.i64(7, nbytes)
-            m.i64(9, start)
+            m.i64(9, data_start if data_start >= 0 else start)
+            if data_start >= 0:
+                m.i64(11, start)                  # dictionary_page_offset
             m.end()
             m.elem_end()
         m.i64(2, total)

@@ -95,6 +95,23 @@ def test_writer_files_snappy(rows, rg, page):
     _check(b, frame, [0, 5, 2, 1, 3], "LogicalFilter(condition=[OR(IS NULL($2), <($3, 0))])")
 
 
+@pytest.mark.parametrize("rows,rg,page,snappy", [(33, 10, 7, False), (5000, 2000, 700, True),
+                                                (300_001, 100_000, 65_536, False)])
+def test_writer_files_dictionary(rows, rg, page, snappy):
+    """The project writer's dictionary-encoded chunks: index bit widths 0 (one entry), 1, 10 and 16,
+    optional and required leaves, chunks past the dictionary cap written as PLAIN pages."""
+    cols = _writer_table(rows, rows + 2)
+    cols[0] = (cols[0][0], cols[0][1], np.full(rows, 7, np.int32), cols[0][3])                 # one entry
+    cols[2] = (cols[2][0], cols[2][1], (cols[2][2] % 2).astype(np.int32), cols[2][3])          # two
+    cols[3] = (cols[3][0], cols[3][1], (cols[3][2] % 1000).astype(np.int64), cols[3][3])       # 1000
+    cols[4] = (cols[4][0], cols[4][1], np.round(cols[4][2] * 8000).astype(np.float32), cols[4][3])
+    b = W.parquet_bytes(cols, row_group_rows=rg, page_rows=page, snappy=snappy, dictionary=True,
+                        dictionary_max=40_000)
+    frame = _frame_of(cols)
+    _check(b, frame, [0, 1, 2, 3, 4, 5], None)
+    _check(b, frame, [0, 5, 2, 1, 3, 4], "LogicalFilter(condition=[OR(IS NULL($2), <($4, 500))])")
+
+
 @pytest.mark.parametrize("delta", [-1, 1])
 def test_corrupt_snappy_page_is_an_error(delta):
     """Snappy streams whose stated length differs from their page's: the call fails, nothing faults."""

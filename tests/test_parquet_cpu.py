@@ -30,11 +30,19 @@ def _writer_table(n, seed):
     return cols
 
 
-@pytest.mark.parametrize("snappy", [False, True])
-def test_writer_output_reads_back_in_pyarrow(snappy):
+@pytest.mark.parametrize("snappy,dictionary", [(False, False), (True, False), (False, True), (True, True)])
+def test_writer_output_reads_back_in_pyarrow(snappy, dictionary):
     pq = pytest.importorskip("pyarrow.parquet")
     cols = _writer_table(20_000, 1)
-    t = pq.read_table(io.BytesIO(W.parquet_bytes(cols, row_group_rows=7000, page_rows=3000, snappy=snappy)))
+    if dictionary:  # few distinct values in some columns, too many (PLAIN pages) in others
+        cols[0] = (cols[0][0], cols[0][1], (cols[0][2] % 7).astype(np.int32), cols[0][3])
+        cols[3] = (cols[3][0], cols[3][1], (cols[3][2] % 1000).astype(np.int64), cols[3][3])
+    b = W.parquet_bytes(cols, row_group_rows=7000, page_rows=3000, snappy=snappy, dictionary=dictionary,
+                        dictionary_max=1000)
+    if dictionary:
+        md = pq.ParquetFile(io.BytesIO(b)).metadata.row_group(0)
+        assert [md.column(k).has_dictionary_page for k in range(6)] == [True, False, False, True, False, False]
+    t = pq.read_table(io.BytesIO(b))
     for name, dt, v, m in cols:
         c = t.column(name)
         got_valid = np.asarray(c.is_valid())
