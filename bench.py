@@ -562,7 +562,28 @@ def parquet_filter_setup(n, device, dictionary=False):
         return chunk_bytes + k * sum(D.WIDTH[W.TEXT_DTYPES[c]] + 1 / 8 for c in proj)
 
     return dict(step=step, alg_bytes_fn=alg_bytes, nout=nout, outs=outs, out_structs=os_, values=values,
-                file_bytes=len(blob), chunk_bytes=chunk_bytes, cols=[R.Column(host, None, D.GDF_INT8, len(blob))])
+                file_bytes=len(blob), chunk_bytes=chunk_bytes, cols=[R.Column(host, None, D.GDF_INT8, len(blob))],
+                blob=blob, rows=n, row_group_rows=1 << 20, row_groups=(n + (1 << 20) - 1) >> 20)
+
+
+def cpu_parquet(ctx, budget_s=10.0):
+    """The oracle's Parquet reader (numpy page decode, oracle/parquet.py) and process_filter on all
+    host threads, over the first row groups of the same file: as many as fit the budget."""
+    import oracle.parquet as OP
+    from ralgpu import workloads as W
+    blob = ctx["blob"]
+    threads = os.cpu_count() or 1
+    t0 = time.perf_counter()
+    OP.scan_filter(blob, W.TEXT_PROJECTIONS, W.TEXT_FILTER, max_row_groups=1, nthreads=threads)
+    one = max(time.perf_counter() - t0, 1e-3)
+    groups = int(max(1, min(ctx["row_groups"], budget_s / one)))
+    t0 = time.perf_counter()
+    OP.scan_filter(blob, W.TEXT_PROJECTIONS, W.TEXT_FILTER, max_row_groups=groups, nthreads=threads)
+    dt = time.perf_counter() - t0
+    rows = min(ctx["rows"], groups * ctx["row_group_rows"])
+    return {"value": rows / dt, "unit": "rows/s", "cores": threads, "kind": "port",
+            "sample": f"first {groups} row groups ({rows} rows): page decode on one thread (numpy), "
+                      f"the filter on {threads}", "cpu_model": cpu_model()}
 
 
 def scan_filter_parity(ctx):
@@ -1227,8 +1248,8 @@ def measure_workload(args, workload, n, selectivity, device, world, sampler, e2e
         if cpu and not args.skip_cpu and workload not in PARQUET_WORKLOADS:
             out["cpu_baseline"] = cpu_baseline(workload, n, selectivity, budget_s=cpu_budget_s,
                                                single_budget_s=cpu_budget_s / 3)
-        if workload in PARQUET_WORKLOADS:
-            out["cpu_baseline_note"] = "no CPU Parquet reader is installed where the benchmark runs (the oracle reads the text form)"
+        if cpu and not args.skip_cpu and workload in PARQUET_WORKLOADS:
+            out["cpu_baseline"] = cpu_parquet(ctx, budget_s=min(cpu_budget_s, 6.0))
     del ctx
     torch.cuda.empty_cache()
     return out

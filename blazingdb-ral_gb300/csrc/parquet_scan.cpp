@@ -128,7 +128,8 @@ int plan_chunks(const uint8_t* file, int64_t n, const pq::FileMeta& meta, const 
             if (cc.codec != 0 && cc.codec != 1)
                 return set_error(kUnsupported, col + "only uncompressed and Snappy-compressed column chunks are supported");
             const bool snappy = cc.codec == 1;
-            const int64_t start = cc.dictionary_page_offset >= 0 ? std::min(cc.dictionary_page_offset, cc.data_page_offset)
+            // a dictionary page offset below 4 (inside the leading magic) means "none": some writers store 0
+            const int64_t start = cc.dictionary_page_offset >= 4 ? std::min(cc.dictionary_page_offset, cc.data_page_offset)
                                                                  : cc.data_page_offset;
             Chunk ch;
             ch.file_off = start;

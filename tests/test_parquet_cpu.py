@@ -91,3 +91,46 @@ def test_not_parquet_and_truncated():
     b = open(os.path.join(GOLDEN, "parquet_plain.parquet"), "rb").read()
     with pytest.raises(R.RalError):
         R.parquet_schema(b[:-20] + b[-8:])
+
+
+FIXTURES = ["parquet_plain", "parquet_snappy", "parquet_dictionary", "parquet_dict_fallback", "parquet_v2",
+            "parquet_v2_snappy_dict", "parquet_defaults"]
+FIXTURE_DTYPES = [D.GDF_INT32, D.GDF_INT64, D.GDF_FLOAT32, D.GDF_FLOAT64, D.GDF_DATE32, D.GDF_DATE64]
+
+
+def _same_column(got, values, valid, what):
+    n = len(values)
+    assert got.size == n, what
+    gv = got.valid_bools()
+    assert np.array_equal(gv, valid), what
+    a = got.data[valid].view(np.uint8)
+    b = np.ascontiguousarray(np.asarray(values)[valid]).astype(got.data.dtype).view(np.uint8)
+    assert np.array_equal(a, b), what
+
+
+@pytest.mark.parametrize("name", FIXTURES)
+def test_oracle_reads_the_pyarrow_fixtures(name):
+    """The oracle's Parquet reader against the values pyarrow wrote (pins the oracle)."""
+    from oracle import parquet as OP
+    b = open(os.path.join(GOLDEN, name + ".parquet"), "rb").read()
+    v = np.load(os.path.join(GOLDEN, name + ".npz"))
+    n = len(v["b"])
+    ones = np.ones(n, bool)
+    cols = OP.scan(b, list(range(6)))
+    for k, (key, m) in enumerate([("a", v["a_valid"]), ("b", ones), ("c", v["c_valid"]), ("d", ones),
+                                  ("e", v["e_valid"]), ("f", ones)]):
+        assert cols[k].dtype == FIXTURE_DTYPES[k]
+        _same_column(cols[k], v[key], m, f"{name} {key}")
+    with pytest.raises(OP.Unsupported):
+        OP.scan(b, [6])  # the string leaf
+
+
+@pytest.mark.parametrize("snappy,dictionary", [(False, False), (True, False), (False, True), (True, True)])
+def test_oracle_reads_the_writer_files(snappy, dictionary):
+    from oracle import parquet as OP
+    cols = _writer_table(5000, 11)
+    b = W.parquet_bytes(cols, row_group_rows=2000, page_rows=700, snappy=snappy, dictionary=dictionary,
+                        dictionary_max=3000)
+    got = OP.scan(b, list(range(6)))
+    for k, (name, dt, v, m) in enumerate(cols):
+        _same_column(got[k], v, np.ones(len(v), bool) if m is None else m, f"{name}")
