@@ -348,10 +348,12 @@ int parquet_scan_filter(const uint8_t* file, int64_t n, const int32_t* projectio
         for (size_t k = 0; k < pages.size(); k++) {
             const PageWhere& dw = plan.dict_where[k];
             if (pages[k].dict_count <= 0 || dw.unpack >= 0 || dict_copy.count(dw.file_off)) continue;
-            dict_copy[dw.file_off] = dbytes;
+            // the copy keeps the source's offset within 16 bytes, so that it moves whole 16-byte words
+            const int64_t mis = (int64_t)((uintptr_t)(direct + dw.file_off) & 15);
+            dict_copy[dw.file_off] = dbytes + mis;
             const int64_t b = (int64_t)pages[k].dict_count * gdf_dtype_size(dtypes[pages[k].column]);
             cjobs.push_back({direct + dw.file_off, nullptr, b});
-            dbytes += std::max<int64_t>(16, (b + 15) & ~15ll);
+            dbytes += ((mis + b + 15) & ~15ll) + 16;
         }
         if (!cjobs.empty()) {
             if (int e = ddict.alloc((size_t)dbytes)) return e;

@@ -27,9 +27,17 @@ FILTERS = [None,
 
 
 def _check(file_bytes, frame, proj, fq):
-    """Both ways in: pages copied from pageable memory, and read in place from page-locked memory."""
+    """Both ways in: pages copied from pageable memory, and read in place from page-locked memory;
+    against the values the file was written from and against the oracle's own read of the file."""
+    from oracle import parquet as OP
     exp_frame = [frame[c] for c in proj]
     exp = exp_frame if fq is None else O.process_filter(exp_frame, fq)
+    ora = OP.scan_filter(file_bytes, proj, fq)
+    assert len(ora) == len(exp)
+    for k, (a, e) in enumerate(zip(ora, exp)):
+        av, ev = a.valid_bools(), e.valid_bools()
+        assert np.array_equal(av, ev), f"oracle column {k} ({fq}): validity"
+        assert np.array_equal(a.data[av].view(np.uint8), e.data[ev].view(np.uint8)), f"oracle column {k} ({fq}): data"
     for page_locked in (False, True):
         got = R.parquet_scan_filter(file_bytes, proj, fq, page_locked=page_locked)
         assert len(got) == len(exp)
