@@ -99,6 +99,10 @@ struct OpEmitter {
     // emitted once where first needed.
     std::vector<std::string> absrc;
 
+    // integer division / remainder by a column take the divisors' reciprocals from the kernel's
+    // shared table (ral_rcp_of; eval kernels of such programs declare and fill it)
+    bool rcp = false;
+
     OpEmitter(const Program& prog, const ParamLayout& layout) : p(prog), L(layout) {
         int maxreg = p.n_in;
         for (const Op& op : p.ops) maxreg = std::max<int>(maxreg, op.out);
@@ -207,12 +211,16 @@ struct OpEmitter {
                 case GDF_DIV: case GDF_FLOOR_DIV:
                     if (L.rdiv_slot.size() > k && L.rdiv_slot[k] >= 0)
                         e = conv("ral_sf_divc(" + l + ", " + r + ", " + divider(k) + ")", Kind::I64, ok);
+                    else if (rcp && !f && op.right >= 0)
+                        e = conv("ral_divi_m(" + l + ", " + r + ", ral_rcp_of(" + r + "))", Kind::I64, ok);
                     else
                         e = arith("ral_ddiv", "ral_divi");
                     break;
                 case GDF_MOD:
                     if (L.rdiv_slot.size() > k && L.rdiv_slot[k] >= 0)
                         e = conv("ral_sf_modc(" + to_i(l, lk) + ", " + r + ", " + divider(k) + ")", Kind::I64, ok);
+                    else if (rcp && op.right >= 0)
+                        e = conv("ral_modi_m(" + to_i(l, lk) + ", " + to_i(r, rk) + ", ral_rcp_of(" + to_i(r, rk) + "))", Kind::I64, ok);
                     else
                         e = conv("ral_modi(" + to_i(l, lk) + ", " + to_i(r, rk) + ")", Kind::I64, ok);
                     break;
@@ -364,7 +372,8 @@ ParamLayout make_layout(const Program& p, int extra_slots_before_scalars) {
 
 // The row function: one row through the program, typed registers in, final
 // register values out.
-void emit_row_function(std::ostream& os, const Program& p, const ParamLayout& L, const char* fname) {
+void emit_row_function(std::ostream& os, const Program& p, const ParamLayout& L, const char* fname,
+                       bool rcp = false) {
     auto ref = p.inputs_referenced();
     auto raw = p.inputs_raw_valid();
     os << "RAL_FI void " << fname << "(const RalParams& P";
@@ -373,12 +382,23 @@ void emit_row_function(std::ostream& os, const Program& p, const ParamLayout& L,
     for (int c = 0; c < p.n_in; c++)
         if (raw[c]) os << ", const ral_u32 rb" << c;
     OpEmitter em(p, L);
+    em.rcp = rcp;
     std::ostringstream body;
     em.emit(body, "    ");
     for (int o = 0; o < p.n_out; o++) os << ", " << kind_ctype(em.kind[p.final_pos[o]]) << "& y" << o;
     os << ") {\n" << body.str();
     for (int o = 0; o < p.n_out; o++) os << "    y" << o << " = " << em.name[p.final_pos[o]] << ";\n";
     os << "}\n";
+}
+
+// Whether a program divides integers by a column (its eval kernel then keeps a reciprocal table).
+bool divides_by_column(const Program& p) {
+    for (const Op& op : p.ops) {
+        if (op.unary || op.right < 0) continue;
+        if (op.bop == GDF_MOD) return true;
+        if ((op.bop == GDF_DIV || op.bop == GDF_FLOOR_DIV) && op.lk == Kind::I64 && op.rk == Kind::I64) return true;
+    }
+    return false;
 }
 
 std::vector<Kind> final_kinds(const Program& p, const ParamLayout& L) {
@@ -486,7 +506,14 @@ GeneratedKernel generate_eval_kernel(const Program& p, const Shape& s) {
     os << "// generated: " << key.str() << "\n";
     os << "#define RAL_G " << s.G << "\n#define RAL_J " << s.J << "\n#define RAL_THREADS " << s.threads << "\n";
     os << "struct RalParams { ral_u64 s[" << L.total << "]; };\n\n";
-    emit_row_function(os, p, L, "ral_row");
+    const bool rcp = divides_by_column(p);
+    if (rcp) {
+        os << "__shared__ unsigned ral_rcp_tab[RAL_RCP_TAB];\n";
+        os << "RAL_FI unsigned ral_rcp_of(ral_i64 b) {\n"
+              "    const ral_u64 ub = b < 0 ? 0ull - (ral_u64)b : (ral_u64)b;\n"
+              "    return ub < RAL_RCP_TAB ? ral_rcp_tab[ub] : 0u;\n}\n";
+    }
+    emit_row_function(os, p, L, "ral_row", rcp);
 
     // validity word function
     if (NOV > 0) {
@@ -502,6 +529,10 @@ GeneratedKernel generate_eval_kernel(const Program& p, const Shape& s) {
     os << "\nextern \"C\" __global__ void __launch_bounds__(RAL_THREADS, " << s.min_blocks << ") " << gk.name
        << "(const __grid_constant__ RalParams P) {\n";
     os << "    const ral_i64 n = (ral_i64)P.s[" << L.n_rows << "];\n";
+    if (rcp) {
+        os << "    for (int i = threadIdx.x; i < RAL_RCP_TAB; i += RAL_THREADS) ral_rcp_tab[i] = i ? 0xffffffffu / (unsigned)i : 0u;\n";
+        os << "    __syncthreads();\n";
+    }
     for (int c = 0; c < p.n_in; c++) {
         if (ref[c])
             os << "    const " << element_ctype(p.inputs[c].dtype) << "* __restrict__ pin" << c << " = (const "

@@ -146,6 +146,33 @@ RAL_FI ral_i64 ral_modi(ral_i64 a, ral_i64 b) {
     return a % b;
 #endif
 }
+// ral_divi / ral_modi for kernels that keep the reciprocals m(d) = floor((2^32 - 1) / d) of the
+// divisors below RAL_RCP_TAB in a shared-memory table (the eval kernel of a program that divides
+// by a column): m is the table's entry for |b|, or 0 when |b| is not below RAL_RCP_TAB (then the
+// compiler's division).  Same results as ral_divi / ral_modi.
+#define RAL_RCP_TAB 4096
+// the rare divisors outside the table, out of line: they do not add to the caller's registers
+static __device__ __noinline__ ral_i64 ral_div_wide(ral_i64 a, ral_i64 b) { return a / b; }
+static __device__ __noinline__ ral_i64 ral_mod_wide(ral_i64 a, ral_i64 b) { return a % b; }
+RAL_FI ral_i64 ral_divi_m(ral_i64 a, ral_i64 b, unsigned m) {
+    if (b == 0) return 0;
+    if (b == -1) return (ral_i64)(0ull - (ral_u64)a);
+    if (m == 0u) return ral_div_wide(a, b);
+    const ral_u64 ua = a < 0 ? 0ull - (ral_u64)a : (ral_u64)a;
+    const unsigned ub = (unsigned)(b < 0 ? 0ll - b : b);
+    unsigned long long q, r;
+    ral_sf_udivmod64_16m(ua, ub, m, &q, &r);
+    return ((a < 0) != (b < 0)) ? (ral_i64)(0ull - q) : (ral_i64)q;
+}
+RAL_FI ral_i64 ral_modi_m(ral_i64 a, ral_i64 b, unsigned m) {
+    if (b == 0 || b == -1) return 0;
+    if (m == 0u) return ral_mod_wide(a, b);
+    const ral_u64 ua = a < 0 ? 0ull - (ral_u64)a : (ral_u64)a;
+    const unsigned ub = (unsigned)(b < 0 ? 0ll - b : b);
+    unsigned long long q, r;
+    ral_sf_udivmod64_16m(ua, ub, m, &q, &r);
+    return a < 0 ? (ral_i64)(0ull - r) : (ral_i64)r;
+}
 // Integer POWER: the reference multiplies `base` into 1, `e` times (e <= 0 -> 1);
 // square-and-multiply gives the same value modulo 2^64.
 RAL_FI ral_i64 ral_powi(ral_i64 base, ral_i64 e) {

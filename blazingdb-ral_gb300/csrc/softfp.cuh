@@ -183,9 +183,11 @@ RAL_SF double ral_sf_div(double a, double b) {
     {
         // r ~ 2^31 / dh from the float 1.f of mb's top 24 bits; v0 = r * 2^32 from r's fields
         const float r = ral_sf_rcp_estimate(ral_sf_float(0x3f800000u | ((unsigned)(mb >> 29) & 0x7fffffu)));
+        // r is within a few ulps of 1 / [1, 2): biased exponent 125 or 126 below 1 (the 24-bit
+        // significand shifted left by 7 or 8 stays below 2^32), 127 at or above 1 (saturated)
         const unsigned rb = ral_sf_fbits(r);
-        const unsigned long long big = (unsigned long long)((rb & 0x7fffffu) | 0x800000u) << (((rb >> 23) & 0xffu) - 118u);
-        const unsigned v0 = big > 0xffffffffull ? 0xffffffffu : (unsigned)big;
+        const unsigned re = (rb >> 23) & 0xffu;
+        const unsigned v0 = re >= 127u ? 0xffffffffu : (((rb & 0x7fffffu) | 0x800000u) << (re - 118u));
         // Newton: v1 = v0 + v0 * (2^63 - dh * v0) / 2^63, the error term (|err| < 2^43) scaled down
         // to 22 bits so that its product with v0 is one 32 x 32-bit multiply
         const long long err = (long long)((1ull << 63) - (unsigned long long)dh * v0);
@@ -472,9 +474,9 @@ RAL_SF unsigned int ral_sf_divstep16(unsigned int x, unsigned int d, unsigned in
     return q;
 }
 
-RAL_SF void ral_sf_udivmod64_16(unsigned long long n, unsigned int d, unsigned long long* q_out,
-                                unsigned long long* r_out) {
-    const unsigned int m = 0xffffffffu / d;
+// The same with m = floor((2^32 - 1) / d) given (a table of them spares the division).
+RAL_SF void ral_sf_udivmod64_16m(unsigned long long n, unsigned int d, unsigned int m, unsigned long long* q_out,
+                                 unsigned long long* r_out) {
     unsigned int r;
     if ((n >> 48) == 0) {  // a dividend below 2^48 (the common case) as 32 + 16 bits: two steps
         const unsigned int q1 = ral_sf_divstep16((unsigned int)(n >> 16), d, m, &r);
@@ -489,6 +491,11 @@ RAL_SF void ral_sf_udivmod64_16(unsigned long long n, unsigned int d, unsigned l
     const unsigned int q0 = ral_sf_divstep16((r << 16) | (lo & 0xffffu), d, m, &r);
     *q_out = ((unsigned long long)q2 << 32) | ((unsigned long long)q1 << 16) | q0;
     *r_out = r;
+}
+
+RAL_SF void ral_sf_udivmod64_16(unsigned long long n, unsigned int d, unsigned long long* q_out,
+                                unsigned long long* r_out) {
+    ral_sf_udivmod64_16m(n, d, 0xffffffffu / d, q_out, r_out);
 }
 
 // Signed quotient and remainder (C semantics) for 1 <= |b| < 2^16; b == -1 is left to the caller.
