@@ -15,7 +15,7 @@ or SNAPPY chunks.  It is pinned by pyarrow's files with the values each holds
 """
 from __future__ import annotations
 
-from typing import List, Optional, Sequence
+from typing import Optional, Sequence
 
 import numpy as np
 
