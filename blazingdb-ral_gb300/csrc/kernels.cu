@@ -797,17 +797,35 @@ __global__ void __launch_bounds__(256) parquet_values_kernel(const __grid_consta
         // warp reads one contiguous aligned span whatever the values' alignment.
         const uintptr_t va = (uintptr_t)vals;
         if (w == 8) {
-            const int sh = (int)(va & 7) * 8;
-            const unsigned long long* q = reinterpret_cast<const unsigned long long*>(va - (va & 7));
+            // 16-byte words: lane l takes rows 2m, 2m + 1 (m = the warp's pair + l), bytes
+            // [s + 16m, s + 16m + 16) past the aligned base: word m and, when s > 0, word m + 1
+            // from the next lane (the last lane of the run loads it, when its values reach it)
+            const int s16 = (int)(va & 15);
+            const int k = s16 >> 2, f = (s16 & 3) * 8;
+            const uint4* q = reinterpret_cast<const uint4*>(va - s16);
             unsigned long long* out = reinterpret_cast<unsigned long long*>(col.data) + pg.row_start;
-#pragma unroll 4
-            for (int r0 = rel0 + 32 * warp; r0 < rel1; r0 += 256) {
-                const int r = r0 + lane;
+#pragma unroll 2
+            for (int m0 = (rel0 >> 1) + 32 * warp; 2 * m0 < rel1; m0 += 256) {
+                const int m = m0 + lane;
+                const int r = 2 * m;
                 const bool in = r < rel1;
-                const unsigned long long lo = in ? q[r] : 0ull;
-                unsigned long long nx = __shfl_down_sync(0xffffffffu, lo, 1);
-                if (sh && in && (lane == 31 || r + 1 >= rel1)) nx = q[r + 1];
-                if (in) out[r] = sh ? (lo >> sh) | (nx << (64 - sh)) : lo;
+                const uint4 a = in ? q[m] : make_uint4(0u, 0u, 0u, 0u);
+                uint4 b;
+                b.x = __shfl_down_sync(0xffffffffu, a.x, 1);
+                b.y = __shfl_down_sync(0xffffffffu, a.y, 1);
+                b.z = __shfl_down_sync(0xffffffffu, a.z, 1);
+                b.w = __shfl_down_sync(0xffffffffu, a.w, 1);
+                const bool two = r + 1 < rel1;
+                if (in && (lane == 31 || r + 2 >= rel1) && s16 + (two ? 16 : 8) > 16) b = q[m + 1];
+                ral_u32 o0, o1, o2, o3;
+                switch (k) {  // uniform over the page
+                case 0: o0 = a.x; o1 = a.y; o2 = a.z; o3 = a.w; if (f) { o0 = __funnelshift_r(a.x, a.y, f); o1 = __funnelshift_r(a.y, a.z, f); o2 = __funnelshift_r(a.z, a.w, f); o3 = __funnelshift_r(a.w, b.x, f); } break;
+                case 1: o0 = __funnelshift_r(a.y, a.z, f); o1 = __funnelshift_r(a.z, a.w, f); o2 = __funnelshift_r(a.w, b.x, f); o3 = __funnelshift_r(b.x, b.y, f); break;
+                case 2: o0 = __funnelshift_r(a.z, a.w, f); o1 = __funnelshift_r(a.w, b.x, f); o2 = __funnelshift_r(b.x, b.y, f); o3 = __funnelshift_r(b.y, b.z, f); break;
+                default: o0 = __funnelshift_r(a.w, b.x, f); o1 = __funnelshift_r(b.x, b.y, f); o2 = __funnelshift_r(b.y, b.z, f); o3 = __funnelshift_r(b.z, b.w, f); break;
+                }
+                if (in) out[r] = (unsigned long long)o1 << 32 | o0;
+                if (two) out[r + 1] = (unsigned long long)o3 << 32 | o2;
             }
         } else {
             const int sh = (int)(va & 3) * 8;
