@@ -33,8 +33,18 @@ typedef unsigned int ral_u32;
 RAL_FI ral_i64 ral_d2i(double d) { return ral_sf_d2i(d); }
 RAL_FI double ral_i2d(ral_i64 x) { return ral_sf_i2d(x); }
 RAL_FI double ral_ddiv(double a, double b) { return ral_sf_div(a, b); }
+// RAL_SOFT_ROUND 0: floor / ceil by the FP64 pipe's rounding instruction (one FP64 instruction
+// against ~28 integer ones; same bits), the other operations staying on the integer pipes
+#ifndef RAL_SOFT_ROUND
+#define RAL_SOFT_ROUND 1
+#endif
+#if RAL_SOFT_ROUND
 RAL_FI double ral_dfloor(double x) { return ral_sf_floor(x); }
 RAL_FI double ral_dceil(double x) { return ral_sf_ceil(x); }
+#else
+RAL_FI double ral_dfloor(double x) { return floor(x); }
+RAL_FI double ral_dceil(double x) { return ceil(x); }
+#endif
 RAL_FI bool ral_dlt(double a, double b) { return ral_sf_lt(a, b); }
 RAL_FI bool ral_dle(double a, double b) { return ral_sf_le(a, b); }
 RAL_FI bool ral_dgt(double a, double b) { return ral_sf_gt(a, b); }

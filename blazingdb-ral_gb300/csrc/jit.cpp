@@ -63,6 +63,9 @@ const std::string& soft_fp_define(bool soft) {
         const char* i = std::getenv("RAL_SOFT_INT_DIV");
         if (i && (std::string(i) == "0" || std::string(i) == "1" || std::string(i) == "2" || std::string(i) == "3"))
             out += std::string("#define RAL_SOFT_INT_DIV ") + i + "\n";
+        // RAL_SOFT_ROUND=0: floor / ceil on the FP64 pipe
+        const char* r = std::getenv("RAL_SOFT_ROUND");
+        if (r && std::string(r) == "0") out += "#define RAL_SOFT_ROUND 0\n";
         return out;
     }();
     return d;
