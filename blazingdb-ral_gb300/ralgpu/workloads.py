@@ -557,10 +557,10 @@ def text_table_varied(n: int, seed: int = SEED) -> bytes:
 
 
 # ---- Parquet files (scan -> filter over Parquet pages) ---------------------------------------
-# A minimal writer of the Apache Parquet format (flat schema, uncompressed data pages v1, PLAIN
-# values, definition levels of optional columns in the RLE / bit-packed hybrid), for the tests
-# and the benchmark, which run where no Parquet library is installed.  Metadata is Thrift's compact
-# protocol.
+# A minimal writer of the Apache Parquet format (flat schema, data pages v1 of PLAIN values or
+# dictionary indices, definition levels of optional columns in the RLE / bit-packed hybrid,
+# uncompressed or literal-only Snappy), for the tests and the benchmark, which run where no Parquet
+# library is installed.  Metadata is Thrift's compact protocol.
 
 _PQ_TYPE = {D.GDF_INT32: 1, D.GDF_DATE32: 1, D.GDF_INT64: 2, D.GDF_DATE64: 2, D.GDF_FLOAT32: 4, D.GDF_FLOAT64: 5}
 _PQ_CONVERTED = {D.GDF_DATE32: 6, D.GDF_DATE64: 9}   # DATE, TIMESTAMP_MILLIS
