@@ -209,14 +209,10 @@ RAL_SF double ral_sf_div(double a, double b) {
     }
     // q in [2^53, 2^54): 53 significand bits, one rounding bit, sticky = r != 0
     unsigned long long m = q >> 1;
-    const unsigned rnd = (unsigned)(q & 1u);
-    if (rnd && (r != 0 || (m & 1u))) m += 1;
-    if (m == (1ull << 53)) {
-        m >>= 1;
-        e += 1;
-    }
-    if (e <= 0 || e >= 2047) return ral_sf_hw_div(a, b);  // subnormal or overflowing quotient
-    return ral_sf_double(((A ^ B) & RAL_SF_SIGN) | ((unsigned long long)e << 52) | (m & RAL_SF_FRAC));
+    m += (q & 1ull) & ((r != 0ull ? 1ull : 0ull) | (m & 1ull));
+    // m in [2^52, 2^53]: added to (e - 1) << 52 it carries a rounded-up 2^53 into the exponent
+    if (e <= 0 || e + (int)(m >> 53) >= 2047) return ral_sf_hw_div(a, b);  // subnormal or overflowing quotient
+    return ral_sf_double(((A ^ B) & RAL_SF_SIGN) + ((unsigned long long)(e - 1) << 52) + m);
 }
 
 // An integer the compiler cannot see through.  A double chosen between two constants (0.0, 1.0,
