@@ -64,6 +64,8 @@ FILES = {
                                                    row_group_size=1500, data_page_size=2048)),
     "parquet_defaults": (3000, 9, True, dict()),
     "parquet_gzip": (300, 10, False, dict(compression="GZIP", use_dictionary=False)),
+    "parquet_delta": (300, 11, False, dict(compression="NONE", use_dictionary=False,
+                                           column_encoding={"b": "DELTA_BINARY_PACKED"})),
 }
 
 

@@ -66,7 +66,8 @@ def test_schema_of_the_fixtures():
 
 
 @pytest.mark.parametrize("name,leaf,reason", [("parquet_gzip", 0, "Snappy-compressed"),
-                                              ("parquet_plain", 6, "columns are scanned")])
+                                              ("parquet_plain", 6, "columns are scanned"),
+                                              ("parquet_delta", 1, "page encoding")])
 def test_unsupported_files_are_refused_before_device_work(name, leaf, reason):
     b = open(os.path.join(GOLDEN, name + ".parquet"), "rb").read()
     rows, dts = R.parquet_schema(b)
