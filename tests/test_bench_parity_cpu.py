@@ -124,3 +124,28 @@ def test_chunked_gather_parity(small_chunks):
     ctx["outs"][3].data[n - 2] += 1.0
     exp = int(outs[3].valid_bools()[n - 2]) if outs[3].valid is not None else 1
     assert bench.gather_parity(ctx)["detail"]["data"] == exp
+
+
+def test_parquet_cpu_baseline_reads_a_bounded_sample():
+    """The Parquet blocks' CPU baseline: the oracle's reader and filter over the first row groups."""
+    import bench as B
+    from ralgpu import workloads as W
+    n = 300_000
+    values = W.lineitem_values(n, W.SEED)
+    for dictionary in (False, True):
+        blob = W.parquet_bytes([(nm, dt, v, None) for nm, dt, v in zip(W.LINEITEM_NAMES, W.TEXT_DTYPES, values)],
+                               row_group_rows=100_000, dictionary=dictionary)
+        out = B.cpu_parquet(dict(blob=blob, rows=n, row_group_rows=100_000, row_groups=3), budget_s=0.5)
+        assert out["kind"] == "port" and out["value"] > 0 and out["cores"] >= 1
+        assert "row groups" in out["sample"]
+
+
+def test_batched_floor_from_the_committed_table():
+    """The mix's floor from profiles/batch_mix_fp64.json: FP64-bound, about 87 ms at 2070 MHz."""
+    import json
+    import os
+    import bench as B
+    table = json.load(open(os.path.join(B.ROOT, "profiles", "batch_mix_fp64.json")))
+    f = B.batch_floor(table, 2070.0, 6782.4)
+    assert 80.0 < f["fp64_ms"] < 95.0 and f["hbm_ms"] < f["fp64_ms"]
+    assert f["floor_ms"] == max(f["fp64_ms"], f["hbm_ms"])
