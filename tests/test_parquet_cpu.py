@@ -135,3 +135,29 @@ def test_oracle_reads_the_writer_files(snappy, dictionary):
     got = OP.scan(b, list(range(6)))
     for k, (name, dt, v, m) in enumerate(cols):
         _same_column(got[k], v, np.ones(len(v), bool) if m is None else m, f"{name}")
+
+
+def test_oracle_hybrid_runs():
+    """The RLE / bit-packed hybrid: RLE runs, bit-packed runs padded to whole groups, width 0."""
+    from oracle import parquet as OP
+    # RLE: 5 x value 3 (width 2: one byte), then bit-packed: 1 group of 8 values 0..7 at width 3
+    buf = bytes([5 << 1, 3]) + bytes([(1 << 1) | 1]) + bytes([0b10001000, 0b11000110, 0b11111010])
+    got = OP.hybrid(buf, 0, len(buf), 3, 13)
+    assert got.tolist() == [3] * 5 + list(range(8))
+    # only the first 6 of a padded group are asked for
+    assert OP.hybrid(buf, 2, len(buf), 3, 6).tolist() == list(range(6))
+    # width 0: every value 0
+    assert OP.hybrid(bytes([(2 << 1) | 1]), 0, 1, 0, 16).tolist() == [0] * 16
+    with pytest.raises(OP.Unsupported):
+        OP.hybrid(bytes([4 << 1, 1]), 0, 2, 1, 5)  # runs end before the values do
+
+
+def test_oracle_snappy_back_references():
+    """Raw Snappy: a literal, then an overlapping copy (offset 1 repeats one byte)."""
+    from oracle import parquet as OP
+    # length 7, literal "ab" (tag (2-1) << 2), copy of 5 bytes at offset 1 (1-byte offset form:
+    # len 4 + ((tag >> 2) & 7), offset (tag >> 5) << 8 | next byte)
+    stream = bytes([7, (2 - 1) << 2]) + b"ab" + bytes([((5 - 4) << 2) | 1, 1])
+    assert OP.snappy_decompress(stream) == b"abbbbbb"
+    with pytest.raises(OP.Unsupported):
+        OP.snappy_decompress(bytes([8, (2 - 1) << 2]) + b"ab" + bytes([((5 - 4) << 2) | 1, 1]))
