@@ -104,3 +104,30 @@ def test_exact_decimals_are_correctly_rounded(checker):
     for (k, f), (st, bits) in zip(cases, got):
         assert st == T.OK, f
         assert bits == struct.unpack("<q", struct.pack("<d", float(f)))[0], f
+
+
+@pytest.mark.parametrize("host", [False, True])
+def test_scan_arguments_are_checked_before_device_work(host):
+    """Both entry points refuse bad arguments on the host (no device is touched): the delimiter equal
+    to the line terminator, a projection outside the file, an unscannable column type."""
+    import ctypes
+    import ralgpu as R
+    L = R.lib()
+    fn = L.ral_text_scan_filter_host if host else L.ral_text_scan_filter
+    text = ctypes.create_string_buffer(b"1|2\n3|4\n")
+    fd = (ctypes.c_int32 * 2)(fe.GDF_INT32, fe.GDF_INT32)
+    outs = (R.capi.GdfColumn * 1)()
+    outs[0].data = ctypes.c_void_p(256)
+    outs[0].valid = ctypes.c_void_p(256)
+    outs[0].size = 2
+    outs[0].dtype = fe.GDF_INT32
+    ptrs = (ctypes.c_void_p * 1)(ctypes.addressof(outs[0]))
+    n = ctypes.c_int32(0)
+    for delim, term, proj, why in [(b"|", b"|", 0, "same byte"), (b"|", b"\n", 5, "out of range")]:
+        pr = (ctypes.c_int32 * 1)(proj)
+        rc = fn(text, 8, delim, term, 0, fd, 2, pr, 1, None, ctypes.cast(ptrs, ctypes.c_void_p), ctypes.byref(n))
+        assert rc != 0 and why in L.ral_last_error().decode()
+    fd_bad = (ctypes.c_int32 * 2)(fe.GDF_INT32, fe.GDF_STRING_CATEGORY)
+    pr = (ctypes.c_int32 * 1)(1)
+    rc = fn(text, 8, b"|", b"\n", 0, fd_bad, 2, pr, 1, None, ctypes.cast(ptrs, ctypes.c_void_p), ctypes.byref(n))
+    assert rc != 0 and "floating-point and date" in L.ral_last_error().decode()
